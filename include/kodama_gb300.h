@@ -1,0 +1,179 @@
+/*
+ * kodama_gb300 — C ABI of the GB300 (sm_103a) implementation of KODAMA.matrix's
+ * label-evolution hot path.
+ *
+ * This is the drop-in boundary behind the reference's `backend = "cuda"` seam.
+ * The reference exposes the path as C++ functions in
+ * inst/include/kodama/kodama.hpp whose CUDA variants are only declared in the
+ * reference tree (the kernels live outside it).  Each entry point below
+ * replaces one of those declarations; a C++ `*_CUDA` definition marshals its
+ * std::vector arguments into these plain pointers.
+ *
+ * Conventions
+ *   - All pointers are HOST pointers; arrays are row-major, C-contiguous.
+ *   - Every function returns KGB_OK (0) or a KGB_E* status; no C++ exception
+ *     crosses the boundary.  kgb_last_error() returns the message of the last
+ *     failure on the calling thread.
+ *   - There is no CPU fallback: without a usable CUDA device every compute
+ *     entry point returns KGB_ECUDA.
+ *   - Calls may come from several host threads; each call runs on its own
+ *     stream of the selected device and synchronises before returning.
+ */
+#ifndef KODAMA_GB300_H
+#define KODAMA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KGB_OK 0
+#define KGB_EINVAL 1    /* invalid argument (std::invalid_argument in the reference) */
+#define KGB_ENOMEM 2    /* device allocation failed */
+#define KGB_ECUDA 3     /* CUDA runtime error or no device */
+#define KGB_ETIMEOUT 4  /* a bounded device-side wait gave up */
+#define KGB_EINTERNAL 5 /* internal consistency check failed (std::runtime_error) */
+
+/* Evolution-policy switches (kodama.hpp:49-61 EvolutionPolicy). 1 = on. */
+typedef struct kgb_policy {
+  int32_t prediction_guidance;
+  int32_t adaptive_proposal_size;
+  int32_t transition_proposal;
+  int32_t stochastic_acceptance;
+  int32_t diversity_multiplier;
+  int32_t pls_transition_coarsening;
+  int32_t pls_fragmentation_penalty;
+  int32_t reject_single_class;
+} kgb_policy;
+
+/* KODAMA.matrix options (kodama.hpp KODAMAMatrixOptions, the subset the
+ * label-evolution path reads). */
+typedef struct kgb_matrix_options {
+  int32_t runs;              /* M */
+  int32_t cycles;            /* Tcycle */
+  int32_t landmarks;         /* default 10000 */
+  int32_t splitting;         /* 0 = 100 if n < 40000 else 300 */
+  int32_t graph_neighbors;   /* K, default 100 */
+  int32_t folds;             /* default 5 */
+  int32_t knn_k;             /* default 30 */
+  int32_t classifier;        /* 0 = kNN, 1 = PLS-LDA */
+  int32_t components;        /* PLS components, default 50 */
+  int32_t materialize_graph; /* return the (corrected) graph */
+  int32_t apply_dissimilarity;
+  int32_t metric;            /* 2 = Euclidean (the only metric of the path) */
+  int32_t device;            /* CUDA device ordinal */
+  int32_t host_threads;      /* host worker threads for per-run set-up, 0 = auto */
+  uint64_t seed;             /* default 1234 */
+  kgb_policy policy;
+} kgb_matrix_options;
+
+/* Caller-allocated outputs of a KODAMA.matrix call. NULL = not wanted
+ * (res, acc and v are required). */
+typedef struct kgb_matrix_result {
+  int32_t* res;              /* runs x n labels (KODAMAMatrixResult::res) */
+  double* acc;               /* runs (best CV accuracy per run) */
+  double* v;                 /* runs x cycles (accuracy trace) */
+  uint64_t* run_hashes;      /* runs x 3: landmark rows, initial labels, folds (FNV-1a) */
+  int32_t* run_counters;     /* runs x 8: run, cycles, transition att/acc, m2o att/acc, cv_evals, landmarks */
+  int32_t* cycle_diag;       /* runs x cycles x 5: proposal size, active classes, accepted, improving, temperature */
+  int32_t* knn_idx;          /* n x knn_cap one-based neighbour ids (materialize_graph) */
+  float* knn_dist;           /* n x knn_cap */
+  int32_t knn_cap;           /* capacity (columns) of knn_idx/knn_dist */
+  int32_t knn_k;             /* out: columns written */
+  int32_t effective_landmarks; /* out */
+  double timings[8];         /* out: total, graph, atlas, landmarks+init, evolution, projection, dissimilarity, h2d+d2h */
+} kgb_matrix_result;
+
+/* Replaces KODAMAMatrix_CUDA (kodama.hpp:1077-1083; dispatch
+ * kodama_matrix.cpp:4521-4531): raw data in, the exact kNN graph is built on
+ * the device (graph-input semantics of kodama_matrix.cpp:3528-3558). */
+int kgb_kodama_matrix(const float* x, int32_t n, int32_t d, const kgb_matrix_options* opt,
+                      kgb_matrix_result* out);
+
+/* Replaces KODAMAMatrixFromGraphData_CUDA (kodama.hpp:1215-1222,
+ * kodama_matrix.cpp:4676-4699): data plus a caller graph (n x gk, indices
+ * zero- or one-based: index_base 0, 1, or -1 = auto as GraphIndexBase::Auto). */
+int kgb_kodama_matrix_from_graph_data(const float* x, int32_t n, int32_t d, const int32_t* gidx,
+                                      const float* gdist, int32_t gk, int32_t index_base,
+                                      const kgb_matrix_options* opt, kgb_matrix_result* out);
+
+/* Core options (kodama.hpp:280-314 CoreOptions with its KNNOptions cv block). */
+typedef struct kgb_core_options {
+  int32_t cycles;
+  int32_t k;                 /* knn.k */
+  int32_t folds;             /* knn.cv.folds */
+  int32_t stratified;        /* knn.cv.stratified */
+  int32_t evolutionary_search;
+  int32_t guarded_diversity;
+  int32_t many_to_one_absorption;
+  int32_t adaptive_proposal_size;
+  int32_t device;
+  int32_t reserved;
+  uint64_t seed;
+  uint64_t cv_seed;
+  kgb_policy policy;
+} kgb_core_options;
+
+/* CoreResult (kodama.hpp:316-349) for one problem; caller-allocated. */
+typedef struct kgb_core_result {
+  int32_t* clbest;           /* samples */
+  int32_t* cvpredbest;       /* samples */
+  int32_t* fold_assignments; /* samples */
+  double* vect_acc;          /* cycles */
+  double* vect_score;        /* cycles */
+  int32_t* proposal_size;    /* cycles */
+  int32_t* active_classes;   /* cycles */
+  uint8_t* flags;            /* cycles x 3: accepted, improving, temperature */
+  double accbest;            /* out */
+  double scorebest;          /* out */
+  int32_t counters[16];      /* out: cycles_completed, proposals_evaluated, best_state_updates,
+                                current_state_accepts, stochastic_attempts, stochastic_accepts,
+                                current_state_rejections, coarsening_moves, absorption_moves,
+                                transition_attempted, transition_accepted, many_to_one_attempted,
+                                many_to_one_accepted, cv_evaluations, success, 0 */
+} kgb_core_result;
+
+/* Replaces CoreKNNGraph_CUDA (kodama.hpp:1043-1050, core.cpp:1684-1700):
+ * label evolution over a precomputed neighbour graph.  constrain / fixed may
+ * be NULL (empty vectors in the reference). */
+int kgb_core_knn_graph(const int32_t* gidx, const float* gdist, int32_t samples, int32_t gk,
+                       int32_t index_base, const int32_t* labels, const int32_t* constrain,
+                       const int32_t* fixed, const kgb_core_options* opt, kgb_core_result* out);
+
+/* Batched CoreKNNGraph: `problems` independent evolutions over ONE graph
+ * (labels is problems x samples; seeds[p] / cv_seeds[p] per problem; out is
+ * an array of `problems` results).  All problems run in one persistent launch.
+ * No single counterpart in the reference: it is the M-lane scheduler
+ * (kodama_matrix.cpp:3823-3850) applied to CoreKNNGraph_CUDA. */
+int kgb_core_knn_graph_batch(const int32_t* gidx, const float* gdist, int32_t samples, int32_t gk,
+                             int32_t index_base, int32_t problems, const int32_t* labels,
+                             const uint64_t* seeds, const uint64_t* cv_seeds,
+                             const kgb_core_options* opt, kgb_core_result* out);
+
+/* Exact kNN graph on the device: for each row its K nearest other rows by
+ * squared Euclidean distance (float32, coordinate order, no FMA), ties by
+ * index; idx zero-based, dist = sqrtf(d2).  Replaces
+ * native_cuda_exact_knn_search (native_cuda_backend.hpp:165) as used by
+ * self_knn_graph (kodama_matrix.cpp:391-533). */
+int kgb_knn_graph(const float* x, int32_t n, int32_t d, int32_t K, int32_t device, int32_t* idx,
+                  float* dist);
+
+/* Replaces the Backend::CUDA branch of KODAMADissimilarityInPlace
+ * (kodama.hpp:1181-1189, kodama_matrix.cpp:4383-4463): co-label proximity on a
+ * one-based graph, in place.  res is runs x samples. */
+int kgb_dissimilarity_inplace(int32_t* gidx, float* gdist, int32_t samples, int32_t gk,
+                              const int32_t* res, int32_t runs, int32_t device);
+
+/* Message of the last failure on this thread; returns its full length. */
+int kgb_last_error(char* buf, size_t len);
+
+/* Library version string. */
+const char* kgb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KODAMA_GB300_H */

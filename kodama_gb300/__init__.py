@@ -1,0 +1,286 @@
+"""kodama_gb300: GB300-native KODAMA.matrix label-evolution hot path.
+
+Python mirror of the reference's C++ entry points for the path
+(inst/include/kodama/kodama.hpp): same names, argument meaning and error
+behaviour (ValueError where the reference throws std::invalid_argument).
+Every call goes through the C ABI (include/kodama_gb300.h) into the CUDA
+library; there is no CPU fallback.
+
+    KODAMA_matrix(x, graph=None, ...)   KODAMAMatrix_CUDA / KODAMAMatrixFromGraphData_CUDA
+    CoreKNNGraph(graph_idx, graph_dist, labels, ...)   CoreKNNGraph_CUDA
+    CoreKNNGraph_batch(...)             M independent CoreKNNGraph problems, one launch
+    knn_graph(x, K)                     exact kNN graph (native_cuda_exact_knn_search)
+    KODAMADissimilarityInPlace(...)     KODAMADissimilarityInPlace(backend=CUDA)
+"""
+
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _native as N
+
+__all__ = ["KODAMA_matrix", "CoreKNNGraph", "CoreKNNGraph_batch", "knn_graph",
+           "KODAMADissimilarityInPlace", "MatrixResult", "CoreResult", "EvolutionPolicy",
+           "library_path", "version"]
+
+
+def library_path() -> str:
+    return N.LIB_PATH
+
+
+def version() -> str:
+    return N.load().kgb_version().decode()
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+@dataclass
+class EvolutionPolicy:
+    """EvolutionPolicy (kodama.hpp:49-61); from_name mirrors core.cpp:35-61."""
+    prediction_guidance: bool = True
+    adaptive_proposal_size: bool = True
+    transition_proposal: bool = True
+    stochastic_acceptance: bool = True
+    diversity_multiplier: bool = True
+    pls_transition_coarsening: bool = True
+    pls_fragmentation_penalty: bool = True
+    reject_single_class: bool = True
+
+    @staticmethod
+    def from_name(name: str) -> "EvolutionPolicy":
+        p = EvolutionPolicy()
+        flag = {"no_prediction_guidance": "prediction_guidance",
+                "fixed_proposal_budget": "adaptive_proposal_size",
+                "no_transition_proposal": "transition_proposal",
+                "greedy_acceptance": "stochastic_acceptance",
+                "raw_cv_score": "diversity_multiplier",
+                "no_pls_transition_coarsening": "pls_transition_coarsening",
+                "no_pls_fragmentation_penalty": "pls_fragmentation_penalty"}
+        if name == "full":
+            return p
+        if name not in flag:
+            raise ValueError(
+                f"Unknown evolution policy '{name}'. Expected full, no_prediction_guidance, "
+                "fixed_proposal_budget, no_transition_proposal, greedy_acceptance, raw_cv_score, "
+                "no_pls_transition_coarsening, or no_pls_fragmentation_penalty.")
+        setattr(p, flag[name], False)
+        return p
+
+    def _c(self) -> N.Policy:
+        return N.Policy(*[int(getattr(self, f)) for f, _ in N.Policy._fields_])
+
+
+@dataclass
+class MatrixResult:
+    """KODAMAMatrixResult (kodama.hpp:604-682): the fields of the path."""
+    res: np.ndarray
+    acc: np.ndarray
+    v: np.ndarray
+    run_hashes: np.ndarray
+    run_counters: np.ndarray
+    cycle_diag: np.ndarray
+    knn_idx: np.ndarray | None
+    knn_dist: np.ndarray | None
+    effective_landmarks: int
+    timings: dict = field(default_factory=dict)
+
+
+_TIMING_NAMES = ("total", "knn_graph", "shared_landmark_partition", "landmark_initialization",
+                 "core_evolution", "label_projection", "kodama_dissimilarity", "transfers")
+
+
+def _matrix_options(runs, cycles, landmarks, splitting, graph_neighbors, folds, knn_k, seed,
+                    materialize_graph, apply_dissimilarity, device, host_threads, policy):
+    pol = policy if isinstance(policy, EvolutionPolicy) else EvolutionPolicy.from_name(policy or "full")
+    return N.MatrixOptions(runs=runs, cycles=cycles, landmarks=landmarks, splitting=splitting,
+                           graph_neighbors=graph_neighbors, folds=folds, knn_k=knn_k, classifier=0,
+                           components=50, materialize_graph=int(materialize_graph),
+                           apply_dissimilarity=int(apply_dissimilarity), metric=2, device=device,
+                           host_threads=host_threads, seed=seed, policy=pol._c())
+
+
+def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitting=0,
+                  graph_neighbors=100, folds=5, knn_k=30, seed=1234, materialize_graph=False,
+                  apply_dissimilarity=True, index_base=-1, device=0, host_threads=0,
+                  policy="full") -> MatrixResult:
+    """KODAMA.matrix with the kNN classifier on the GPU.
+
+    ``graph`` = (indices, distances) of shape (n, K) runs the graph-input path
+    (KODAMAMatrixFromGraphData_CUDA); without it the exact kNN graph is built
+    on the device (KODAMAMatrix_CUDA with exact-graph semantics).
+    Defaults are those of KODAMAMatrixOptions (kodama.hpp:535-570).
+    """
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    if x.ndim != 2:
+        raise ValueError("x must be a 2-D matrix")
+    n, d = x.shape
+    opt = _matrix_options(runs, cycles, landmarks, splitting, graph_neighbors, folds, knn_k, seed,
+                          materialize_graph, apply_dissimilarity, device, host_threads, policy)
+    res = np.zeros((runs, n), np.int32)
+    acc = np.zeros(runs, np.float64)
+    v = np.zeros((runs, max(cycles, 0)), np.float64)
+    hashes = np.zeros((runs, 3), np.uint64)
+    counters = np.zeros((runs, 8), np.int32)
+    cdiag = np.zeros((runs, max(cycles, 0), 5), np.int32)
+    cap = max(1, graph_neighbors if graph is None else np.asarray(graph[0]).shape[1])
+    kidx = np.zeros((n, cap), np.int32) if materialize_graph else None
+    kdist = np.zeros((n, cap), np.float32) if materialize_graph else None
+    out = N.MatrixResult()
+    out.res = res.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+    out.acc = acc.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    out.v = v.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    out.run_hashes = hashes.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))
+    out.run_counters = counters.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+    out.cycle_diag = cdiag.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+    if materialize_graph:
+        out.knn_idx = kidx.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+        out.knn_dist = kdist.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    out.knn_cap = cap
+    lib = N.load()
+    if graph is None:
+        rc = lib.kgb_kodama_matrix(_ptr(x), n, d, ctypes.byref(opt), ctypes.byref(out))
+    else:
+        gi = np.ascontiguousarray(graph[0], dtype=np.int32)
+        gd = np.ascontiguousarray(graph[1], dtype=np.float32)
+        if gi.shape != gd.shape or gi.shape[0] != n:
+            raise ValueError("NeighborGraph indices/distances size must equal samples * neighbors.")
+        rc = lib.kgb_kodama_matrix_from_graph_data(_ptr(x), n, d, _ptr(gi), _ptr(gd), gi.shape[1],
+                                                   index_base, ctypes.byref(opt), ctypes.byref(out))
+    N.check(rc)
+    k = out.knn_k
+    return MatrixResult(
+        res=res, acc=acc, v=v, run_hashes=hashes, run_counters=counters, cycle_diag=cdiag,
+        knn_idx=kidx[:, :k].copy() if (materialize_graph and k) else None,
+        knn_dist=kdist[:, :k].copy() if (materialize_graph and k) else None,
+        effective_landmarks=out.effective_landmarks,
+        timings=dict(zip(_TIMING_NAMES, list(out.timings))))
+
+
+@dataclass
+class CoreResult:
+    """CoreResult (kodama.hpp:316-349)."""
+    clbest: np.ndarray
+    cvpredbest: np.ndarray
+    fold_assignments: np.ndarray
+    vect_acc: np.ndarray
+    vect_score: np.ndarray
+    proposal_size: np.ndarray
+    active_classes: np.ndarray
+    flags: np.ndarray
+    accbest: float
+    scorebest: float
+    counters: np.ndarray
+
+
+def _core_options(cycles, k, folds, stratified, evolutionary_search, guarded_diversity,
+                  many_to_one_absorption, adaptive_proposal_size, seed, cv_seed, device, policy):
+    pol = policy if isinstance(policy, EvolutionPolicy) else EvolutionPolicy.from_name(policy or "full")
+    return N.CoreOptions(cycles=cycles, k=k, folds=folds, stratified=int(stratified),
+                         evolutionary_search=int(evolutionary_search),
+                         guarded_diversity=int(guarded_diversity),
+                         many_to_one_absorption=int(many_to_one_absorption),
+                         adaptive_proposal_size=int(adaptive_proposal_size), device=device,
+                         reserved=0, seed=seed, cv_seed=cv_seed, policy=pol._c())
+
+
+def _alloc_core(samples, cycles):
+    bufs = dict(clbest=np.zeros(samples, np.int32), cvpredbest=np.zeros(samples, np.int32),
+                fold_assignments=np.zeros(samples, np.int32),
+                vect_acc=np.zeros(max(cycles, 1), np.float64),
+                vect_score=np.zeros(max(cycles, 1), np.float64),
+                proposal_size=np.zeros(max(cycles, 1), np.int32),
+                active_classes=np.zeros(max(cycles, 1), np.int32),
+                flags=np.zeros((max(cycles, 1), 3), np.uint8))
+    r = N.CoreResult()
+    for name, arr in bufs.items():
+        ctype = dict(N.CoreResult._fields_)[name]
+        setattr(r, name, arr.ctypes.data_as(ctype))
+    return r, bufs
+
+
+def _wrap_core(r, bufs, cycles):
+    return CoreResult(
+        clbest=bufs["clbest"], cvpredbest=bufs["cvpredbest"], fold_assignments=bufs["fold_assignments"],
+        vect_acc=bufs["vect_acc"][:cycles], vect_score=bufs["vect_score"][:cycles],
+        proposal_size=bufs["proposal_size"][:cycles], active_classes=bufs["active_classes"][:cycles],
+        flags=bufs["flags"][:cycles], accbest=r.accbest, scorebest=r.scorebest,
+        counters=np.array(list(r.counters), np.int32))
+
+
+def CoreKNNGraph_batch(graph_idx, graph_dist, labels, seeds, cv_seeds, *, cycles=100, k=30,
+                       folds=10, stratified=True, evolutionary_search=False,
+                       guarded_diversity=False, many_to_one_absorption=False,
+                       adaptive_proposal_size=True, index_base=-1, device=0,
+                       policy="full") -> list[CoreResult]:
+    """`len(seeds)` independent CoreKNNGraph evolutions over one graph in one launch."""
+    gi = np.ascontiguousarray(graph_idx, dtype=np.int32)
+    gd = np.ascontiguousarray(graph_dist, dtype=np.float32)
+    samples, gk = gi.shape
+    lab = np.ascontiguousarray(labels, dtype=np.int32).reshape(-1, samples)
+    problems = lab.shape[0]
+    s = np.ascontiguousarray(seeds, dtype=np.uint64)
+    cs = np.ascontiguousarray(cv_seeds, dtype=np.uint64)
+    if s.shape[0] != problems or cs.shape[0] != problems:
+        raise ValueError("one seed and one cv seed per problem")
+    opt = _core_options(cycles, k, folds, stratified, evolutionary_search, guarded_diversity,
+                        many_to_one_absorption, adaptive_proposal_size, 0, 0, device, policy)
+    arr = (N.CoreResult * problems)()
+    keep = []
+    for p in range(problems):
+        r, bufs = _alloc_core(samples, cycles)
+        arr[p] = r
+        keep.append(bufs)
+    rc = N.load().kgb_core_knn_graph_batch(_ptr(gi), _ptr(gd), samples, gk, index_base, problems,
+                                           _ptr(lab), _ptr(s), _ptr(cs), ctypes.byref(opt), arr)
+    N.check(rc)
+    return [_wrap_core(arr[p], keep[p], cycles) for p in range(problems)]
+
+
+def CoreKNNGraph(graph_idx, graph_dist, labels, *, constrain=None, fixed=None, cycles=100, k=30,
+                 folds=10, stratified=True, evolutionary_search=False, guarded_diversity=False,
+                 many_to_one_absorption=False, adaptive_proposal_size=True, seed=1, cv_seed=1,
+                 index_base=-1, device=0, policy="full") -> CoreResult:
+    """CoreKNNGraph_CUDA (kodama.hpp:1043): label evolution over a neighbour graph."""
+    gi = np.ascontiguousarray(graph_idx, dtype=np.int32)
+    gd = np.ascontiguousarray(graph_dist, dtype=np.float32)
+    samples, gk = gi.shape
+    lab = np.ascontiguousarray(labels, dtype=np.int32)
+    if lab.shape[0] != samples:
+        raise ValueError("initial labels size must match NeighborGraph samples.")
+    con = None if constrain is None else np.ascontiguousarray(constrain, dtype=np.int32)
+    fix = None if fixed is None else np.ascontiguousarray(fixed, dtype=np.int32)
+    opt = _core_options(cycles, k, folds, stratified, evolutionary_search, guarded_diversity,
+                        many_to_one_absorption, adaptive_proposal_size, seed, cv_seed, device, policy)
+    r, bufs = _alloc_core(samples, cycles)
+    rc = N.load().kgb_core_knn_graph(_ptr(gi), _ptr(gd), samples, gk, index_base, _ptr(lab),
+                                     _ptr(con), _ptr(fix), ctypes.byref(opt), ctypes.byref(r))
+    N.check(rc)
+    return _wrap_core(r, bufs, cycles)
+
+
+def knn_graph(x, K: int, *, device: int = 0):
+    """Exact kNN graph: zero-based (n, K) indices and sqrt distances."""
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    n, d = x.shape
+    idx = np.zeros((n, K), np.int32)
+    dist = np.zeros((n, K), np.float32)
+    N.check(N.load().kgb_knn_graph(_ptr(x), n, d, K, device, _ptr(idx), _ptr(dist)))
+    return idx, dist
+
+
+def KODAMADissimilarityInPlace(graph_idx: np.ndarray, graph_dist: np.ndarray, run_labels: np.ndarray,
+                               *, device: int = 0) -> None:
+    """Co-label proximity correction of a one-based graph, in place."""
+    if graph_idx.dtype != np.int32 or graph_dist.dtype != np.float32:
+        raise ValueError("graph arrays must be int32 / float32")
+    if not (graph_idx.flags.c_contiguous and graph_dist.flags.c_contiguous):
+        raise ValueError("graph arrays must be C-contiguous")
+    res = np.ascontiguousarray(run_labels, dtype=np.int32)
+    samples, gk = graph_idx.shape
+    N.check(N.load().kgb_dissimilarity_inplace(_ptr(graph_idx), _ptr(graph_dist), samples, gk, _ptr(res),
+                                               res.shape[0], device))

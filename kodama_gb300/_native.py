@@ -1,0 +1,131 @@
+"""ctypes declarations of the C ABI in include/kodama_gb300.h.
+
+Loads kodama_gb300/_lib/libkodama_gb300.so (built in-tree by
+kodama_gb300/build.py).  There is no fallback: if the library is missing or
+no CUDA device is usable, every call raises.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libkodama_gb300.so")
+
+KGB_OK, KGB_EINVAL, KGB_ENOMEM, KGB_ECUDA, KGB_ETIMEOUT, KGB_EINTERNAL = range(6)
+
+EXPORTED = (
+    "kgb_kodama_matrix",
+    "kgb_kodama_matrix_from_graph_data",
+    "kgb_core_knn_graph",
+    "kgb_core_knn_graph_batch",
+    "kgb_knn_graph",
+    "kgb_dissimilarity_inplace",
+    "kgb_last_error",
+    "kgb_version",
+)
+
+
+class Policy(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int32) for n in (
+        "prediction_guidance", "adaptive_proposal_size", "transition_proposal",
+        "stochastic_acceptance", "diversity_multiplier", "pls_transition_coarsening",
+        "pls_fragmentation_penalty", "reject_single_class")]
+
+
+class MatrixOptions(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int32) for n in (
+        "runs", "cycles", "landmarks", "splitting", "graph_neighbors", "folds", "knn_k",
+        "classifier", "components", "materialize_graph", "apply_dissimilarity", "metric",
+        "device", "host_threads")] + [("seed", ctypes.c_uint64), ("policy", Policy)]
+
+
+class MatrixResult(ctypes.Structure):
+    _fields_ = [
+        ("res", ctypes.POINTER(ctypes.c_int32)),
+        ("acc", ctypes.POINTER(ctypes.c_double)),
+        ("v", ctypes.POINTER(ctypes.c_double)),
+        ("run_hashes", ctypes.POINTER(ctypes.c_uint64)),
+        ("run_counters", ctypes.POINTER(ctypes.c_int32)),
+        ("cycle_diag", ctypes.POINTER(ctypes.c_int32)),
+        ("knn_idx", ctypes.POINTER(ctypes.c_int32)),
+        ("knn_dist", ctypes.POINTER(ctypes.c_float)),
+        ("knn_cap", ctypes.c_int32),
+        ("knn_k", ctypes.c_int32),
+        ("effective_landmarks", ctypes.c_int32),
+        ("timings", ctypes.c_double * 8),
+    ]
+
+
+class CoreOptions(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int32) for n in (
+        "cycles", "k", "folds", "stratified", "evolutionary_search", "guarded_diversity",
+        "many_to_one_absorption", "adaptive_proposal_size", "device", "reserved")] + [
+        ("seed", ctypes.c_uint64), ("cv_seed", ctypes.c_uint64), ("policy", Policy)]
+
+
+class CoreResult(ctypes.Structure):
+    _fields_ = [
+        ("clbest", ctypes.POINTER(ctypes.c_int32)),
+        ("cvpredbest", ctypes.POINTER(ctypes.c_int32)),
+        ("fold_assignments", ctypes.POINTER(ctypes.c_int32)),
+        ("vect_acc", ctypes.POINTER(ctypes.c_double)),
+        ("vect_score", ctypes.POINTER(ctypes.c_double)),
+        ("proposal_size", ctypes.POINTER(ctypes.c_int32)),
+        ("active_classes", ctypes.POINTER(ctypes.c_int32)),
+        ("flags", ctypes.POINTER(ctypes.c_uint8)),
+        ("accbest", ctypes.c_double),
+        ("scorebest", ctypes.c_double),
+        ("counters", ctypes.c_int32 * 16),
+    ]
+
+
+_lib = None
+
+
+def load():
+    """Load the CUDA library (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(
+            f"{LIB_PATH} is missing: build it with `python -m kodama_gb300.build` "
+            "(there is no CPU fallback)")
+    lib = ctypes.CDLL(LIB_PATH)
+    P = ctypes.c_void_p
+    i32 = ctypes.c_int32
+    lib.kgb_kodama_matrix.argtypes = [P, i32, i32, ctypes.POINTER(MatrixOptions), ctypes.POINTER(MatrixResult)]
+    lib.kgb_kodama_matrix_from_graph_data.argtypes = [
+        P, i32, i32, P, P, i32, i32, ctypes.POINTER(MatrixOptions), ctypes.POINTER(MatrixResult)]
+    lib.kgb_core_knn_graph.argtypes = [P, P, i32, i32, i32, P, P, P, ctypes.POINTER(CoreOptions),
+                                       ctypes.POINTER(CoreResult)]
+    lib.kgb_core_knn_graph_batch.argtypes = [P, P, i32, i32, i32, i32, P, P, P, ctypes.POINTER(CoreOptions),
+                                             ctypes.POINTER(CoreResult)]
+    lib.kgb_knn_graph.argtypes = [P, i32, i32, i32, i32, P, P]
+    lib.kgb_dissimilarity_inplace.argtypes = [P, P, i32, i32, P, i32, i32]
+    lib.kgb_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    lib.kgb_version.restype = ctypes.c_char_p
+    for name in EXPORTED:
+        if name not in ("kgb_version",):
+            getattr(lib, name).restype = ctypes.c_int
+    _lib = lib
+    return lib
+
+
+class KodamaError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"[kgb status {code}] {message}")
+        self.code = code
+
+
+def check(rc: int) -> None:
+    if rc == KGB_OK:
+        return
+    buf = ctypes.create_string_buffer(4096)
+    load().kgb_last_error(buf, 4096)
+    msg = buf.value.decode(errors="replace")
+    if rc == KGB_EINVAL:
+        raise ValueError(msg)
+    raise KodamaError(rc, msg)

@@ -1,0 +1,866 @@
+// C ABI of the GB300 label-evolution engine (include/kodama_gb300.h).
+//
+// Host orchestration in C++; every per-row / per-cycle computation runs in the
+// CUDA kernels of evolve.cu, kmeans.cu, graph_ops.cu and knn.cu.  There is no
+// CPU fallback: without a device every compute entry point fails with
+// KGB_ECUDA.
+#include "../../include/kodama_gb300.h"
+#include "evolve.cuh"
+#include "graph_ops.cuh"
+#include "host_plan.h"
+#include "kmeans.cuh"
+#include "knn.cuh"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <exception>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <thread>
+#include <vector>
+
+namespace {
+
+thread_local std::string g_error;
+
+struct KgbError : std::runtime_error {
+  int code;
+  KgbError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+[[noreturn]] void fail(int code, const std::string& msg) { throw KgbError(code, msg); }
+
+void ck(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return;
+  if (e == cudaErrorMemoryAllocation) fail(KGB_ENOMEM, std::string(what) + ": " + cudaGetErrorString(e));
+  fail(KGB_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+void ck_launch(int e, const char* what) { ck(static_cast<cudaError_t>(e), what); }
+
+template <class F>
+int guarded(F&& f) {
+  try {
+    f();
+    return KGB_OK;
+  } catch (const KgbError& e) {
+    g_error = e.what();
+    return e.code;
+  } catch (const std::invalid_argument& e) {
+    g_error = e.what();
+    return KGB_EINVAL;
+  } catch (const std::bad_alloc& e) {
+    g_error = "host allocation failed";
+    return KGB_ENOMEM;
+  } catch (const std::exception& e) {
+    g_error = e.what();
+    return KGB_EINTERNAL;
+  }
+}
+
+// Per-call device context: device selection, one stream, stream-ordered
+// allocations released when the call ends.
+class Ctx {
+ public:
+  explicit Ctx(int device) {
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) fail(KGB_ECUDA, "no CUDA device is available");
+    if (device < 0 || device >= count) fail(KGB_EINVAL, "CUDA device ordinal out of range");
+    ck(cudaSetDevice(device), "cudaSetDevice");
+    ck(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+    ck(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, device), "device attribute");
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+      uint64_t keep = ~0ull;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+  }
+  ~Ctx() {
+    for (void* p : bufs_) cudaFreeAsync(p, stream_);
+    cudaStreamSynchronize(stream_);
+    cudaStreamDestroy(stream_);
+  }
+  Ctx(const Ctx&) = delete;
+  Ctx& operator=(const Ctx&) = delete;
+
+  template <class T>
+  T* alloc(size_t count) {
+    void* p = nullptr;
+    const size_t bytes = std::max<size_t>(1, count * sizeof(T));
+    ck(cudaMallocAsync(&p, bytes, stream_), "cudaMallocAsync");
+    bufs_.push_back(p);
+    return static_cast<T*>(p);
+  }
+  template <class T>
+  T* upload(const T* host, size_t count) {
+    T* d = alloc<T>(count);
+    if (count) ck(cudaMemcpyAsync(d, host, count * sizeof(T), cudaMemcpyHostToDevice, stream_), "H2D");
+    return d;
+  }
+  template <class T>
+  void download(T* host, const T* dev, size_t count) {
+    if (count) ck(cudaMemcpyAsync(host, dev, count * sizeof(T), cudaMemcpyDeviceToHost, stream_), "D2H");
+  }
+  void sync() { ck(cudaStreamSynchronize(stream_), "stream synchronize"); }
+  cudaStream_t stream() const { return stream_; }
+  int sms() const { return sms_; }
+
+ private:
+  cudaStream_t stream_ = nullptr;
+  int sms_ = 1;
+  std::vector<void*> bufs_;
+};
+
+struct Clock {
+  std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+  double lap() {
+    const auto now = std::chrono::steady_clock::now();
+    const double s = std::chrono::duration<double>(now - t).count();
+    t = now;
+    return s;
+  }
+};
+
+kgb_policy default_policy() {
+  kgb_policy p;
+  p.prediction_guidance = 1;
+  p.adaptive_proposal_size = 1;
+  p.transition_proposal = 1;
+  p.stochastic_acceptance = 1;
+  p.diversity_multiplier = 1;
+  p.pls_transition_coarsening = 1;
+  p.pls_fragmentation_penalty = 1;
+  p.reject_single_class = 1;
+  return p;
+}
+
+bool policy_is_zero(const kgb_policy& p) {
+  return !p.prediction_guidance && !p.adaptive_proposal_size && !p.transition_proposal &&
+         !p.stochastic_acceptance && !p.diversity_multiplier && !p.pls_transition_coarsening &&
+         !p.pls_fragmentation_penalty && !p.reject_single_class;
+}
+
+// Label coding of one problem: codes = ranks among the sorted distinct labels.
+struct Coding {
+  std::vector<int> code2label;
+  std::vector<uint16_t> codes;
+  bool nocollide = true;
+};
+
+Coding code_labels(const int* labels, int n, uint64_t bucket_count) {
+  Coding c;
+  c.code2label.assign(labels, labels + n);
+  std::sort(c.code2label.begin(), c.code2label.end());
+  c.code2label.erase(std::unique(c.code2label.begin(), c.code2label.end()), c.code2label.end());
+  if (c.code2label.size() > 65535) fail(KGB_EINVAL, "more than 65535 distinct labels");
+  c.codes.resize(static_cast<size_t>(n));
+  for (int i = 0; i < n; ++i) {
+    c.codes[i] = static_cast<uint16_t>(std::lower_bound(c.code2label.begin(), c.code2label.end(), labels[i]) -
+                                       c.code2label.begin());
+  }
+  for (int l : c.code2label) {
+    if (l < 0 || static_cast<uint64_t>(l) >= bucket_count) c.nocollide = false;
+  }
+  return c;
+}
+
+int host_threads(int requested) {
+  if (requested > 0) return requested;
+  const unsigned hc = std::thread::hardware_concurrency();
+  return hc ? static_cast<int>(std::min(hc, 32u)) : 4;
+}
+
+template <class F>
+void parallel_for(int n, int threads, F&& f) {
+  threads = std::max(1, std::min(threads, n));
+  if (threads == 1) {
+    for (int i = 0; i < n; ++i) f(i);
+    return;
+  }
+  std::vector<std::thread> pool;
+  std::vector<std::exception_ptr> errs(static_cast<size_t>(threads));
+  for (int t = 0; t < threads; ++t) {
+    pool.emplace_back([&, t]() {
+      try {
+        for (int i = t; i < n; i += threads) f(i);
+      } catch (...) {
+        errs[t] = std::current_exception();
+      }
+    });
+  }
+  for (auto& th : pool) th.join();
+  for (auto& e : errs) if (e) std::rethrow_exception(e);
+}
+
+struct EvolveBuffers {
+  uint16_t* clbest;
+  uint16_t* cvpredbest;
+  double* vect_acc;
+  double* vect_score;
+  int* psize;
+  int* active;
+  uint8_t* flags;
+  int* counters;
+  double* best;
+  int* status;
+};
+
+// Common launcher of the persistent kernel for `problems` problems of L rows.
+EvolveBuffers run_evolution(Ctx& ctx, kgb::EvolveParams P, int C0max) {
+  const int problems = P.problems, L = P.L, T = P.T;
+  EvolveBuffers b;
+  b.clbest = ctx.alloc<uint16_t>(static_cast<size_t>(problems) * L);
+  b.cvpredbest = ctx.alloc<uint16_t>(static_cast<size_t>(problems) * L);
+  b.vect_acc = ctx.alloc<double>(static_cast<size_t>(problems) * std::max(T, 1));
+  b.vect_score = ctx.alloc<double>(static_cast<size_t>(problems) * std::max(T, 1));
+  b.psize = ctx.alloc<int>(static_cast<size_t>(problems) * std::max(T, 1));
+  b.active = ctx.alloc<int>(static_cast<size_t>(problems) * std::max(T, 1));
+  b.flags = ctx.alloc<uint8_t>(static_cast<size_t>(problems) * std::max(T, 1) * 3);
+  b.counters = ctx.alloc<int>(static_cast<size_t>(problems) * 16);
+  b.best = ctx.alloc<double>(static_cast<size_t>(problems) * 2);
+  b.status = ctx.alloc<int>(static_cast<size_t>(problems));
+  P.clbest = b.clbest;
+  P.cvpredbest = b.cvpredbest;
+  P.vect_acc = b.vect_acc;
+  P.vect_score = b.vect_score;
+  P.proposal_size = b.psize;
+  P.active = b.active;
+  P.flags = b.flags;
+  P.counters = b.counters;
+  P.best = b.best;
+  P.status = b.status;
+  P.C0max = C0max;
+  P.trans = (P.absorption && P.pol_transition)
+                ? ctx.alloc<int>(static_cast<size_t>(problems) * C0max * C0max)
+                : ctx.alloc<int>(1);
+  P.foldcnt = ctx.alloc<int>(static_cast<size_t>(problems) * P.F * C0max);
+  const int grid = std::min(problems, ctx.sms());
+  size_t smem = kgb::evolve_smem_bytes(L, C0max, true);
+  P.smem_rows = 1;
+  if (smem > 220 * 1024) {
+    P.smem_rows = 0;
+    smem = kgb::evolve_smem_bytes(L, C0max, false);
+    if (smem > 220 * 1024) fail(KGB_EINVAL, "too many distinct labels for the evolution kernel");
+    const size_t Lp = (static_cast<size_t>(L) + 7) / 8 * 8;
+    P.rows_scratch = ctx.alloc<uint16_t>(static_cast<size_t>(grid) * 5 * Lp);
+  } else {
+    P.rows_scratch = nullptr;
+  }
+  ck_launch(kgb::evolve_launch(P, grid, smem, ctx.stream()), "evolution kernel launch");
+  return b;
+}
+
+void validate_matrix_options(const kgb_matrix_options* o) {
+  if (o == nullptr) fail(KGB_EINVAL, "options pointer is null");
+  if (o->runs < 1) fail(KGB_EINVAL, "KODAMAMatrixOptions::runs must be positive.");
+  if (o->cycles < 0) fail(KGB_EINVAL, "KODAMAMatrixOptions::cycles must be non-negative.");
+  if (o->folds < 2) fail(KGB_EINVAL, "KODAMAMatrixOptions::folds must be at least two.");
+  if (o->folds > 255) fail(KGB_EINVAL, "at most 255 folds are supported");
+  if (o->classifier != 0) fail(KGB_EINVAL, "only the kNN classifier is implemented by this entry point");
+  if (o->metric != 2 && o->metric != 0) fail(KGB_EINVAL, "only the Euclidean metric is supported");
+}
+
+// The KODAMA.matrix path after the global graph (n x K zero-based, compacted,
+// distances finite >= 0) is resident on the device.
+void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_gidx, float* d_gdist, int K,
+                              const kgb_matrix_options* o, kgb_matrix_result* out, Clock& clk) {
+  const kgb_policy pol = policy_is_zero(o->policy) ? default_policy() : o->policy;
+  int landmarks = o->landmarks > 0 ? o->landmarks : 10000;
+  if (landmarks >= n) landmarks = static_cast<int>(std::ceil(static_cast<double>(n) * 0.75));
+  landmarks = std::max(2, std::min(landmarks, n - 1));
+  const int splitting = o->splitting > 0 ? o->splitting : (n < 40000 ? 100 : 300);
+  const int coarse_k = std::max(2, std::min(splitting, n));
+  const int M = o->runs, T = o->cycles, F = o->folds;
+  const uint64_t seed = o->seed;
+  const int knn_k = std::max(o->knn_k, 1);
+  const int w = std::max(1, std::min(knn_k, K));
+  if (w > 32) fail(KGB_EINVAL, "knn.k above 32 is not supported by the vote kernel");
+  if (knn_k > kgb::kMaxProjectK) fail(KGB_EINVAL, "knn.k too large for the projection kernel");
+  cudaStream_t st = ctx.stream();
+
+  // shared landmark atlas (kodama_matrix.cpp:3662-3734)
+  float* d_pnorm = ctx.alloc<float>(n);
+  ck_launch(kgb::kmeans_row_norms(d_x, n, d, d_pnorm, st), "row norms");
+  std::mt19937_64 shared_rng(seed + 1u);
+  const int ck_atlas = std::max(1, std::min(coarse_k, n));
+  const std::vector<int> atlas_init = kgb::permutation_head(n, kgb::kmeans_seed_from_draw(shared_rng()), ck_atlas);
+  const int kmax = std::max(ck_atlas, splitting);
+  const std::vector<float> split_u = kgb::split_uniforms(kmax);
+  float* d_split = ctx.upload(split_u.data(), split_u.size());
+  int* d_atlas_labels = ctx.alloc<int>(n);
+  {
+    kgb::KMeansBatch B{};
+    B.problems = 1;
+    B.n = n;
+    B.d = d;
+    B.k = ck_atlas;
+    B.max_iter = 10;
+    B.x = d_x;
+    B.rows = nullptr;
+    B.pnorm = d_pnorm;
+    B.init_rows = ctx.upload(atlas_init.data(), atlas_init.size());
+    B.split_uniform = d_split;
+    B.cent = ctx.alloc<float>(static_cast<size_t>(ck_atlas) * d);
+    B.cnorm = ctx.alloc<float>(ck_atlas);
+    B.assign = ctx.alloc<int>(n);
+    ck(cudaMemsetAsync(B.assign, 0xff, sizeof(int) * n, st), "memset");
+    B.members = ctx.alloc<int>(n);
+    B.active = ctx.alloc<int>(1);
+    B.changed = ctx.alloc<int>(1);
+    B.labels = d_atlas_labels;
+    ck_launch(kgb::kmeans_run(B, st), "atlas k-means");
+  }
+  std::vector<int> atlas(static_cast<size_t>(n));
+  ctx.download(atlas.data(), d_atlas_labels, n);
+  ctx.sync();
+  out->timings[2] = clk.lap();
+
+  // per-run landmarks, folds and k-means seeds (host, libstdc++ streams)
+  const kgb::Strata strata = kgb::index_strata(atlas, coarse_k);
+  const int init_k = std::max(2, std::min(splitting, landmarks));
+  const int kk = std::max(1, std::min(init_k, landmarks));
+  std::vector<kgb::RunPlan> plans(static_cast<size_t>(M));
+  parallel_for(M, host_threads(o->host_threads), [&](int r) {
+    plans[r] = kgb::plan_run(strata, landmarks, init_k, F, seed, r + 1);
+  });
+  const int L = static_cast<int>(plans[0].landmarks.size());
+  std::vector<int> land(static_cast<size_t>(M) * L), init_rows(static_cast<size_t>(M) * kk);
+  std::vector<uint8_t> folds(static_cast<size_t>(M) * L);
+  for (int r = 0; r < M; ++r) {
+    std::copy(plans[r].landmarks.begin(), plans[r].landmarks.end(), land.begin() + static_cast<size_t>(r) * L);
+    std::copy(plans[r].init_rows.begin(), plans[r].init_rows.end(), init_rows.begin() + static_cast<size_t>(r) * kk);
+    std::copy(plans[r].folds.begin(), plans[r].folds.end(), folds.begin() + static_cast<size_t>(r) * L);
+  }
+  int* d_land = ctx.upload(land.data(), land.size());
+  uint8_t* d_folds = ctx.upload(folds.data(), folds.size());
+  int* d_init_labels = ctx.alloc<int>(static_cast<size_t>(M) * L);
+  {
+    kgb::KMeansBatch B{};
+    B.problems = M;
+    B.n = L;
+    B.d = d;
+    B.k = kk;
+    B.max_iter = 10;
+    B.x = d_x;
+    B.rows = d_land;
+    B.pnorm = d_pnorm;
+    B.init_rows = ctx.upload(init_rows.data(), init_rows.size());
+    B.split_uniform = d_split;
+    B.cent = ctx.alloc<float>(static_cast<size_t>(M) * kk * d);
+    B.cnorm = ctx.alloc<float>(static_cast<size_t>(M) * kk);
+    B.assign = ctx.alloc<int>(static_cast<size_t>(M) * L);
+    ck(cudaMemsetAsync(B.assign, 0xff, sizeof(int) * static_cast<size_t>(M) * L, st), "memset");
+    B.members = ctx.alloc<int>(static_cast<size_t>(M) * L);
+    B.active = ctx.alloc<int>(M);
+    B.changed = ctx.alloc<int>(M);
+    B.labels = d_init_labels;
+    ck_launch(kgb::kmeans_run(B, st), "landmark k-means");
+  }
+  std::vector<int> init_labels(static_cast<size_t>(M) * L);
+  ctx.download(init_labels.data(), d_init_labels, init_labels.size());
+  ctx.sync();
+
+  // label coding per run (labels 1..init_k, all inside the bucket range)
+  const uint64_t bc = kgb::unordered_bucket_count(static_cast<size_t>(L));
+  std::vector<Coding> codings(static_cast<size_t>(M));
+  parallel_for(M, host_threads(o->host_threads), [&](int r) {
+    codings[r] = code_labels(init_labels.data() + static_cast<size_t>(r) * L, L, bc);
+  });
+  int C0max = F;
+  for (const auto& c : codings) C0max = std::max<int>(C0max, static_cast<int>(c.code2label.size()));
+  std::vector<uint16_t> codes(static_cast<size_t>(M) * L);
+  std::vector<int> c2l(static_cast<size_t>(M) * C0max, 0), ncodes(static_cast<size_t>(M));
+  std::vector<uint8_t> nocol(static_cast<size_t>(M));
+  for (int r = 0; r < M; ++r) {
+    std::copy(codings[r].codes.begin(), codings[r].codes.end(), codes.begin() + static_cast<size_t>(r) * L);
+    std::copy(codings[r].code2label.begin(), codings[r].code2label.end(), c2l.begin() + static_cast<size_t>(r) * C0max);
+    ncodes[r] = static_cast<int>(codings[r].code2label.size());
+    nocol[r] = codings[r].nocollide ? 1 : 0;
+  }
+  out->timings[3] = clk.lap();
+
+  // per-run fold-filtered vote tables over the landmark subgraph
+  int* d_g2l = ctx.alloc<int>(static_cast<size_t>(M) * n);
+  ck_launch(kgb::build_g2l(d_land, M, L, n, d_g2l, st), "landmark index");
+  uint16_t* d_nb = ctx.alloc<uint16_t>(static_cast<size_t>(M) * L * w);
+  float* d_sc = ctx.alloc<float>(static_cast<size_t>(M) * L * w);
+  {
+    kgb::VoteTableArgs a{};
+    a.problems = M;
+    a.L = L;
+    a.n = n;
+    a.K = K;
+    a.w = w;
+    a.gidx = d_gidx;
+    a.gdist = d_gdist;
+    a.land = d_land;
+    a.g2l = d_g2l;
+    a.folds = d_folds;
+    a.nb = d_nb;
+    a.sc = d_sc;
+    ck_launch(kgb::build_vote_tables(a, st), "vote tables");
+  }
+  std::vector<int> identity(static_cast<size_t>(L));
+  for (int i = 0; i < L; ++i) identity[i] = i;
+  std::vector<int> goff(static_cast<size_t>(L) + 1);
+  for (int i = 0; i <= L; ++i) goff[i] = i;
+  std::vector<uint64_t> seeds(static_cast<size_t>(M));
+  for (int r = 0; r < M; ++r) seeds[r] = seed + static_cast<uint64_t>(r + 1);
+
+  kgb::EvolveParams P{};
+  P.problems = M;
+  P.L = L;
+  P.w = w;
+  P.T = T;
+  P.F = F;
+  P.G = L;
+  P.singleton = 1;
+  P.evolutionary = 1;
+  P.guarded = 1;
+  P.absorption = 1;
+  P.adaptive = 1;
+  P.pol_guidance = pol.prediction_guidance != 0;
+  P.pol_adaptive = pol.adaptive_proposal_size != 0;
+  P.pol_transition = pol.transition_proposal != 0;
+  P.pol_stochastic = pol.stochastic_acceptance != 0;
+  P.pol_diversity = pol.diversity_multiplier != 0;
+  P.pol_reject1 = pol.reject_single_class != 0;
+  P.bucket_count = bc;
+  P.nb = d_nb;
+  P.sc = d_sc;
+  P.init = ctx.upload(codes.data(), codes.size());
+  P.code2label = ctx.upload(c2l.data(), c2l.size());
+  P.ncodes = ctx.upload(ncodes.data(), ncodes.size());
+  P.nocollide = ctx.upload(nocol.data(), nocol.size());
+  P.folds = d_folds;
+  P.fixed = nullptr;
+  P.goff = ctx.upload(goff.data(), goff.size());
+  P.gmem = ctx.upload(identity.data(), identity.size());
+  P.seeds = ctx.upload(seeds.data(), seeds.size());
+  const EvolveBuffers eb = run_evolution(ctx, P, C0max);
+
+  // projection of non-landmarks and result matrix
+  int* d_res = ctx.alloc<int>(static_cast<size_t>(M) * n);
+  {
+    kgb::ProjectArgs a{};
+    a.problems = M;
+    a.L = L;
+    a.n = n;
+    a.K = K;
+    a.pk = knn_k;
+    a.C0max = C0max;
+    a.gidx = d_gidx;
+    a.g2l = d_g2l;
+    a.clbest = eb.clbest;
+    a.code2label = P.code2label;
+    a.res = d_res;
+    ck_launch(kgb::project_labels(a, st), "projection");
+  }
+  ctx.sync();
+  out->timings[4] = clk.lap();
+
+  // outputs
+  ctx.download(out->res, d_res, static_cast<size_t>(M) * n);
+  std::vector<double> best(static_cast<size_t>(M) * 2);
+  ctx.download(best.data(), eb.best, best.size());
+  ctx.download(out->v, eb.vect_acc, static_cast<size_t>(M) * T);
+  std::vector<int> psize(static_cast<size_t>(M) * T), active(static_cast<size_t>(M) * T),
+      counters(static_cast<size_t>(M) * 16);
+  std::vector<uint8_t> flags(static_cast<size_t>(M) * T * 3);
+  ctx.download(psize.data(), eb.psize, psize.size());
+  ctx.download(active.data(), eb.active, active.size());
+  ctx.download(flags.data(), eb.flags, flags.size());
+  ctx.download(counters.data(), eb.counters, counters.size());
+  int* d_oidx = nullptr;
+  float* d_odist = nullptr;
+  const bool want_graph = o->materialize_graph && out->knn_idx != nullptr && out->knn_dist != nullptr;
+  if (want_graph) {
+    if (out->knn_cap < K) fail(KGB_EINVAL, "knn_cap is smaller than the graph width");
+    if (o->apply_dissimilarity) {
+      int* d_lbs = ctx.alloc<int>(static_cast<size_t>(M) * n);
+      ck_launch(kgb::transpose_runs(d_res, M, n, d_lbs, st), "transpose");
+      d_oidx = ctx.alloc<int>(static_cast<size_t>(n) * K);
+      d_odist = ctx.alloc<float>(static_cast<size_t>(n) * K);
+      kgb::DissimArgs a{};
+      a.n = n;
+      a.K = K;
+      a.runs = M;
+      a.in_one_based = 0;
+      a.out_one_based = 1;
+      a.idx = d_gidx;
+      a.dist = d_gdist;
+      a.lbs = d_lbs;
+      a.out_idx = d_oidx;
+      a.out_dist = d_odist;
+      ck_launch(kgb::dissimilarity(a, st), "dissimilarity");
+    }
+  }
+  ctx.sync();
+  const double t_dl = clk.lap();
+  if (want_graph) {
+    std::vector<int> gi(static_cast<size_t>(n) * K);
+    std::vector<float> gd(static_cast<size_t>(n) * K);
+    if (o->apply_dissimilarity) {
+      ctx.download(gi.data(), d_oidx, gi.size());
+      ctx.download(gd.data(), d_odist, gd.size());
+    } else {
+      ctx.download(gi.data(), d_gidx, gi.size());
+      ctx.download(gd.data(), d_gdist, gd.size());
+    }
+    ctx.sync();
+    for (int i = 0; i < n; ++i) {
+      for (int j = 0; j < K; ++j) {
+        int v = gi[static_cast<size_t>(i) * K + j];
+        if (!o->apply_dissimilarity && v >= 0) v += 1;
+        out->knn_idx[static_cast<size_t>(i) * out->knn_cap + j] = v;
+        out->knn_dist[static_cast<size_t>(i) * out->knn_cap + j] = gd[static_cast<size_t>(i) * K + j];
+      }
+    }
+    out->knn_k = K;
+  } else {
+    out->knn_k = 0;
+  }
+  out->timings[6] = clk.lap() + t_dl;
+  for (int r = 0; r < M; ++r) {
+    out->acc[r] = best[2 * r];
+    if (out->run_hashes) {
+      out->run_hashes[3 * r + 0] = plans[r].landmark_hash;
+      out->run_hashes[3 * r + 1] = kgb::fnv_hash(init_labels.data() + static_cast<size_t>(r) * L, L);
+      out->run_hashes[3 * r + 2] = plans[r].fold_hash;
+    }
+    if (out->run_counters) {
+      const int* c = counters.data() + static_cast<size_t>(r) * 16;
+      int* rc = out->run_counters + 8 * r;
+      rc[0] = r + 1;
+      rc[1] = c[0];
+      rc[2] = c[9];
+      rc[3] = c[10];
+      rc[4] = c[11];
+      rc[5] = c[12];
+      rc[6] = c[13];
+      rc[7] = L;
+    }
+    if (out->cycle_diag) {
+      for (int c = 0; c < T; ++c) {
+        int* cd = out->cycle_diag + (static_cast<size_t>(r) * T + c) * 5;
+        const size_t o1 = static_cast<size_t>(r) * T + c;
+        cd[0] = psize[o1];
+        cd[1] = active[o1];
+        cd[2] = flags[3 * o1 + 0];
+        cd[3] = flags[3 * o1 + 1];
+        cd[4] = flags[3 * o1 + 2];
+      }
+    }
+  }
+  out->effective_landmarks = L;
+}
+
+}  // namespace
+
+extern "C" {
+
+int kgb_last_error(char* buf, size_t len) {
+  if (buf != nullptr && len > 0) {
+    std::strncpy(buf, g_error.c_str(), len - 1);
+    buf[len - 1] = '\0';
+  }
+  return static_cast<int>(g_error.size());
+}
+
+const char* kgb_version(void) { return "kodama_gb300 0.1 (sm_103a)"; }
+
+int kgb_kodama_matrix_from_graph_data(const float* x, int32_t n, int32_t d, const int32_t* gidx,
+                                      const float* gdist, int32_t gk, int32_t index_base,
+                                      const kgb_matrix_options* opt, kgb_matrix_result* out) {
+  return guarded([&]() {
+    if (x == nullptr || gidx == nullptr || gdist == nullptr || out == nullptr) fail(KGB_EINVAL, "null pointer");
+    if (n < 3) fail(KGB_EINVAL, "KODAMAMatrix requires at least 3 rows.");
+    if (d < 1) fail(KGB_EINVAL, "Input matrix must have at least one column.");
+    if (gk <= 0) fail(KGB_EINVAL, "NeighborGraph.neighbors must be positive.");
+    validate_matrix_options(opt);
+    if (out->res == nullptr || out->acc == nullptr || out->v == nullptr) fail(KGB_EINVAL, "null result buffer");
+    Clock total, clk;
+    for (double& t : out->timings) t = 0.0;
+    Ctx ctx(opt->device);
+    int landmarks = opt->landmarks > 0 ? opt->landmarks : 10000;
+    if (landmarks >= n) landmarks = static_cast<int>(std::ceil(static_cast<double>(n) * 0.75));
+    landmarks = std::max(2, std::min(landmarks, n - 1));
+    const int requested = opt->graph_neighbors > 0 ? opt->graph_neighbors : 100;
+    const int neighbors = std::max(1, static_cast<int>(std::floor(std::min(
+        {static_cast<double>(landmarks), static_cast<double>(n) * 0.75 - 1.0, static_cast<double>(requested)}))));
+    const int K = std::max(1, std::min(gk, neighbors));
+    const float* d_x = ctx.upload(x, static_cast<size_t>(n) * d);
+    const int* d_in_idx = ctx.upload(gidx, static_cast<size_t>(n) * gk);
+    const float* d_in_dist = ctx.upload(gdist, static_cast<size_t>(n) * gk);
+    int* d_mm = ctx.alloc<int>(2);
+    ck_launch(kgb::graph_minmax(d_in_idx, static_cast<size_t>(n) * gk, d_mm, ctx.stream()), "graph min/max");
+    int* d_gidx = ctx.alloc<int>(static_cast<size_t>(n) * K);
+    float* d_gdist = ctx.alloc<float>(static_cast<size_t>(n) * K);
+    ck_launch(kgb::normalize_external(d_in_idx, d_in_dist, n, gk, K, index_base, d_mm, d_gidx, d_gdist,
+                                      ctx.stream()), "graph normalisation");
+    ctx.sync();
+    out->timings[1] = clk.lap();
+    matrix_from_device_graph(ctx, d_x, n, d, d_gidx, d_gdist, K, opt, out, clk);
+    out->timings[0] = total.lap();
+  });
+}
+
+int kgb_kodama_matrix(const float* x, int32_t n, int32_t d, const kgb_matrix_options* opt, kgb_matrix_result* out) {
+  return guarded([&]() {
+    if (x == nullptr || out == nullptr) fail(KGB_EINVAL, "null pointer");
+    if (n < 3) fail(KGB_EINVAL, "KODAMAMatrix requires at least 3 rows.");
+    if (d < 1) fail(KGB_EINVAL, "Input matrix must have at least one column.");
+    validate_matrix_options(opt);
+    if (out->res == nullptr || out->acc == nullptr || out->v == nullptr) fail(KGB_EINVAL, "null result buffer");
+    Clock total, clk;
+    for (double& t : out->timings) t = 0.0;
+    Ctx ctx(opt->device);
+    int landmarks = opt->landmarks > 0 ? opt->landmarks : 10000;
+    if (landmarks >= n) landmarks = static_cast<int>(std::ceil(static_cast<double>(n) * 0.75));
+    landmarks = std::max(2, std::min(landmarks, n - 1));
+    const int requested = opt->graph_neighbors > 0 ? opt->graph_neighbors : 100;
+    const int K = std::max(1, static_cast<int>(std::floor(std::min(
+        {static_cast<double>(landmarks), static_cast<double>(n) * 0.75 - 1.0, static_cast<double>(requested)}))));
+    const float* d_x = ctx.upload(x, static_cast<size_t>(n) * d);
+    int* d_gidx = ctx.alloc<int>(static_cast<size_t>(n) * K);
+    float* d_gdist = ctx.alloc<float>(static_cast<size_t>(n) * K);
+    const int segments = 4;
+    void* scratch = ctx.alloc<unsigned char>(kgb::knn_bruteforce_scratch(n, K, segments));
+    ck_launch(kgb::knn_bruteforce(d_x, n, d, K, segments, scratch, d_gidx, d_gdist, ctx.stream()), "kNN graph");
+    ctx.sync();
+    out->timings[1] = clk.lap();
+    matrix_from_device_graph(ctx, d_x, n, d, d_gidx, d_gdist, K, opt, out, clk);
+    out->timings[0] = total.lap();
+  });
+}
+
+int kgb_core_knn_graph_batch(const int32_t* gidx, const float* gdist, int32_t samples, int32_t gk,
+                             int32_t index_base, int32_t problems, const int32_t* labels,
+                             const uint64_t* seeds, const uint64_t* cv_seeds, const kgb_core_options* opt,
+                             kgb_core_result* out) {
+  return guarded([&]() {
+    if (gidx == nullptr || gdist == nullptr || labels == nullptr || seeds == nullptr || cv_seeds == nullptr ||
+        opt == nullptr || out == nullptr) {
+      fail(KGB_EINVAL, "null pointer");
+    }
+    if (samples < 2) fail(KGB_EINVAL, "CoreKNNGraph requires at least two samples.");
+    if (samples > 65535) fail(KGB_EINVAL, "at most 65535 samples per problem are supported");
+    if (gk <= 0) fail(KGB_EINVAL, "NeighborGraph.neighbors must be positive.");
+    if (problems < 1) fail(KGB_EINVAL, "problems must be positive");
+    if (opt->cycles < 0) fail(KGB_EINVAL, "Core cycles must be non-negative.");
+    if (opt->k < 1) fail(KGB_EINVAL, "KNNOptions::k must be positive.");
+    if (opt->folds < 2) fail(KGB_EINVAL, "Number of folds must be at least 2.");
+    if (opt->folds > 255) fail(KGB_EINVAL, "at most 255 folds are supported");
+    const int w = std::max(1, std::min(opt->k, gk));
+    if (w > 32) fail(KGB_EINVAL, "knn.k above 32 is not supported by the vote kernel");
+    const kgb_policy pol = policy_is_zero(opt->policy) ? default_policy() : opt->policy;
+    Ctx ctx(opt->device);
+    cudaStream_t st = ctx.stream();
+    const size_t total = static_cast<size_t>(samples) * gk;
+    const int* d_in_idx = ctx.upload(gidx, total);
+    const float* d_in_dist = ctx.upload(gdist, total);
+    int* d_mm = ctx.alloc<int>(2);
+    ck_launch(kgb::graph_minmax(d_in_idx, total, d_mm, st), "graph min/max");
+    int* d_gidx = ctx.alloc<int>(total);
+    float* d_gdist = ctx.alloc<float>(total);
+    ck_launch(kgb::normalize_indices(d_in_idx, d_in_dist, total, samples, index_base, d_mm, d_gidx, d_gdist, st),
+              "graph normalisation");
+    // singleton groups (no constraint)
+    std::vector<int> goff, gmem;
+    goff.reserve(static_cast<size_t>(samples) + 1);
+    for (int i = 0; i <= samples; ++i) goff.push_back(i);
+    for (int i = 0; i < samples; ++i) gmem.push_back(i);
+    const uint64_t bc = kgb::unordered_bucket_count(static_cast<size_t>(samples));
+    std::vector<Coding> codings(static_cast<size_t>(problems));
+    std::vector<std::vector<int>> folds(static_cast<size_t>(problems));
+    parallel_for(problems, host_threads(0), [&](int p) {
+      const int* lab = labels + static_cast<size_t>(p) * samples;
+      codings[p] = code_labels(lab, samples, bc);
+      folds[p] = kgb::make_folds(std::vector<int>(lab, lab + samples), {}, opt->folds, opt->stratified != 0,
+                                 cv_seeds[p]);
+    });
+    int C0max = opt->folds;
+    for (const auto& c : codings) C0max = std::max<int>(C0max, static_cast<int>(c.code2label.size()));
+    std::vector<uint16_t> codes(static_cast<size_t>(problems) * samples);
+    std::vector<int> c2l(static_cast<size_t>(problems) * C0max, 0), ncodes(static_cast<size_t>(problems));
+    std::vector<uint8_t> nocol(static_cast<size_t>(problems)), fo8(static_cast<size_t>(problems) * samples);
+    for (int p = 0; p < problems; ++p) {
+      std::copy(codings[p].codes.begin(), codings[p].codes.end(), codes.begin() + static_cast<size_t>(p) * samples);
+      std::copy(codings[p].code2label.begin(), codings[p].code2label.end(), c2l.begin() + static_cast<size_t>(p) * C0max);
+      ncodes[p] = static_cast<int>(codings[p].code2label.size());
+      nocol[p] = codings[p].nocollide ? 1 : 0;
+      for (int i = 0; i < samples; ++i) fo8[static_cast<size_t>(p) * samples + i] = static_cast<uint8_t>(folds[p][i]);
+    }
+    uint8_t* d_folds = ctx.upload(fo8.data(), fo8.size());
+    uint16_t* d_nb = ctx.alloc<uint16_t>(static_cast<size_t>(problems) * samples * w);
+    float* d_sc = ctx.alloc<float>(static_cast<size_t>(problems) * samples * w);
+    {
+      kgb::VoteTableArgs a{};
+      a.problems = problems;
+      a.L = samples;
+      a.n = samples;
+      a.K = gk;
+      a.w = w;
+      a.gidx = d_gidx;
+      a.gdist = d_gdist;
+      a.land = nullptr;
+      a.g2l = nullptr;
+      a.folds = d_folds;
+      a.nb = d_nb;
+      a.sc = d_sc;
+      ck_launch(kgb::build_vote_tables(a, st), "vote tables");
+    }
+    kgb::EvolveParams P{};
+    P.problems = problems;
+    P.L = samples;
+    P.w = w;
+    P.T = opt->cycles;
+    P.F = opt->folds;
+    P.G = samples;
+    P.singleton = 1;
+    P.evolutionary = opt->evolutionary_search != 0;
+    P.guarded = opt->guarded_diversity != 0;
+    P.absorption = opt->many_to_one_absorption != 0;
+    P.adaptive = opt->adaptive_proposal_size != 0;
+    P.pol_guidance = pol.prediction_guidance != 0;
+    P.pol_adaptive = pol.adaptive_proposal_size != 0;
+    P.pol_transition = pol.transition_proposal != 0;
+    P.pol_stochastic = pol.stochastic_acceptance != 0;
+    P.pol_diversity = pol.diversity_multiplier != 0;
+    P.pol_reject1 = pol.reject_single_class != 0;
+    P.bucket_count = bc;
+    P.nb = d_nb;
+    P.sc = d_sc;
+    P.init = ctx.upload(codes.data(), codes.size());
+    P.code2label = ctx.upload(c2l.data(), c2l.size());
+    P.ncodes = ctx.upload(ncodes.data(), ncodes.size());
+    P.nocollide = ctx.upload(nocol.data(), nocol.size());
+    P.folds = d_folds;
+    P.fixed = nullptr;
+    P.goff = ctx.upload(goff.data(), goff.size());
+    P.gmem = ctx.upload(gmem.data(), gmem.size());
+    P.seeds = ctx.upload(seeds, static_cast<size_t>(problems));
+    const EvolveBuffers eb = run_evolution(ctx, P, C0max);
+    const int T = opt->cycles;
+    std::vector<uint16_t> hb(static_cast<size_t>(problems) * samples), hp(hb.size());
+    std::vector<double> best(static_cast<size_t>(problems) * 2);
+    std::vector<int> counters(static_cast<size_t>(problems) * 16);
+    ctx.download(hb.data(), eb.clbest, hb.size());
+    ctx.download(hp.data(), eb.cvpredbest, hp.size());
+    ctx.download(best.data(), eb.best, best.size());
+    ctx.download(counters.data(), eb.counters, counters.size());
+    std::vector<double> va(static_cast<size_t>(problems) * T), vs(va.size());
+    std::vector<int> ps(va.size()), ac(va.size());
+    std::vector<uint8_t> fl(va.size() * 3);
+    ctx.download(va.data(), eb.vect_acc, va.size());
+    ctx.download(vs.data(), eb.vect_score, vs.size());
+    ctx.download(ps.data(), eb.psize, ps.size());
+    ctx.download(ac.data(), eb.active, ac.size());
+    ctx.download(fl.data(), eb.flags, fl.size());
+    ctx.sync();
+    for (int p = 0; p < problems; ++p) {
+      kgb_core_result& r = out[p];
+      const int* map = c2l.data() + static_cast<size_t>(p) * C0max;
+      for (int i = 0; i < samples; ++i) {
+        const size_t o1 = static_cast<size_t>(p) * samples + i;
+        if (r.clbest) r.clbest[i] = map[hb[o1]];
+        if (r.cvpredbest) r.cvpredbest[i] = map[hp[o1]];
+        if (r.fold_assignments) r.fold_assignments[i] = folds[p][i];
+      }
+      for (int c = 0; c < T; ++c) {
+        const size_t o1 = static_cast<size_t>(p) * T + c;
+        if (r.vect_acc) r.vect_acc[c] = va[o1];
+        if (r.vect_score) r.vect_score[c] = vs[o1];
+        if (r.proposal_size) r.proposal_size[c] = ps[o1];
+        if (r.active_classes) r.active_classes[c] = ac[o1];
+        if (r.flags) {
+          r.flags[3 * c] = fl[3 * o1];
+          r.flags[3 * c + 1] = fl[3 * o1 + 1];
+          r.flags[3 * c + 2] = fl[3 * o1 + 2];
+        }
+      }
+      r.accbest = best[2 * p];
+      r.scorebest = best[2 * p + 1];
+      std::memcpy(r.counters, counters.data() + static_cast<size_t>(p) * 16, sizeof(r.counters));
+    }
+  });
+}
+
+int kgb_knn_graph(const float* x, int32_t n, int32_t d, int32_t K, int32_t device, int32_t* idx, float* dist) {
+  return guarded([&]() {
+    if (x == nullptr || idx == nullptr || dist == nullptr) fail(KGB_EINVAL, "null pointer");
+    if (n < 1 || d < 1 || K < 1) fail(KGB_EINVAL, "invalid kNN graph dimensions");
+    Ctx ctx(device);
+    const float* d_x = ctx.upload(x, static_cast<size_t>(n) * d);
+    int* d_idx = ctx.alloc<int>(static_cast<size_t>(n) * K);
+    float* d_dist = ctx.alloc<float>(static_cast<size_t>(n) * K);
+    const int segments = 4;
+    void* scratch = ctx.alloc<unsigned char>(kgb::knn_bruteforce_scratch(n, K, segments));
+    ck_launch(kgb::knn_bruteforce(d_x, n, d, K, segments, scratch, d_idx, d_dist, ctx.stream()), "kNN graph");
+    ctx.download(idx, d_idx, static_cast<size_t>(n) * K);
+    ctx.download(dist, d_dist, static_cast<size_t>(n) * K);
+    ctx.sync();
+  });
+}
+
+int kgb_dissimilarity_inplace(int32_t* gidx, float* gdist, int32_t samples, int32_t gk, const int32_t* res,
+                              int32_t runs, int32_t device) {
+  return guarded([&]() {
+    if (gidx == nullptr || gdist == nullptr || res == nullptr) fail(KGB_EINVAL, "null pointer");
+    if (runs <= 0 || samples <= 0 || gk <= 0) {
+      fail(KGB_EINVAL, "KODAMADissimilarityInPlace requires a non-empty graph and label matrix.");
+    }
+    const size_t total = static_cast<size_t>(samples) * gk;
+    for (size_t i = 0; i < total; ++i) {
+      const int v = gidx[i];
+      if (v < 0) continue;
+      if (v < 1 || v > samples) fail(KGB_EINVAL, "KODAMADissimilarityInPlace expects public one-based graph indices.");
+    }
+    Ctx ctx(device);
+    cudaStream_t st = ctx.stream();
+    int* d_idx = ctx.upload(gidx, total);
+    float* d_dist = ctx.upload(gdist, total);
+    const int* d_res = ctx.upload(res, static_cast<size_t>(runs) * samples);
+    int* d_lbs = ctx.alloc<int>(static_cast<size_t>(runs) * samples);
+    ck_launch(kgb::transpose_runs(d_res, runs, samples, d_lbs, st), "transpose");
+    int* d_oidx = ctx.alloc<int>(total);
+    float* d_odist = ctx.alloc<float>(total);
+    kgb::DissimArgs a{};
+    a.n = samples;
+    a.K = gk;
+    a.runs = runs;
+    a.in_one_based = 1;
+    a.out_one_based = 1;
+    a.idx = d_idx;
+    a.dist = d_dist;
+    a.lbs = d_lbs;
+    a.out_idx = d_oidx;
+    a.out_dist = d_odist;
+    ck_launch(kgb::dissimilarity(a, st), "dissimilarity");
+    ctx.download(gidx, d_oidx, total);
+    ctx.download(gdist, d_odist, total);
+    ctx.sync();
+  });
+}
+
+int kgb_core_knn_graph(const int32_t* gidx, const float* gdist, int32_t samples, int32_t gk, int32_t index_base,
+                       const int32_t* labels, const int32_t* constrain, const int32_t* fixed,
+                       const kgb_core_options* opt, kgb_core_result* out) {
+  if (constrain != nullptr || fixed != nullptr) {
+    g_error = "constrain / fixed are not supported yet by the CUDA CoreKNNGraph entry point";
+    return KGB_EINVAL;
+  }
+  if (opt == nullptr) {
+    g_error = "null options";
+    return KGB_EINVAL;
+  }
+  const uint64_t s = opt->seed, cs = opt->cv_seed;
+  return kgb_core_knn_graph_batch(gidx, gdist, samples, gk, index_base, 1, labels, &s, &cs, opt, out);
+}
+
+}  // extern "C"

@@ -1,0 +1,57 @@
+// Parameters of the persistent label-evolution kernel (evolve.cu).
+#pragma once
+
+#include <stdint.h>
+
+namespace kgb {
+
+constexpr uint16_t kNoRow = 0xFFFFu;
+
+// Per-problem layout: problem p owns rows [p*L, (p+1)*L) of every per-row
+// array, p*C0max entries of per-code arrays, p*T of per-cycle arrays.
+struct EvolveParams {
+  int problems;
+  int L;            // rows (landmarks) per problem
+  int w;            // neighbour-table width k' (<= 32)
+  int T;            // cycles
+  int F;            // folds
+  int C0max;        // stride of per-code arrays
+  int G;            // groups (shared by all problems)
+  int singleton;    // every group has exactly one member
+  int evolutionary, guarded, absorption, adaptive;
+  int pol_guidance, pol_adaptive, pol_transition, pol_stochastic, pol_diversity, pol_reject1;
+  uint64_t bucket_count;   // libstdc++ bucket count after reserve(L)
+  int smem_rows;           // 1 = label arrays in shared memory
+  // inputs
+  const uint16_t* nb;      // problems x L x w local neighbour ids (kNoRow = none)
+  const float* sc;         // problems x L x w scores -(d*d)
+  const uint16_t* init;    // problems x L initial label codes
+  const int* code2label;   // problems x C0max sorted distinct initial labels
+  const int* ncodes;       // problems
+  const uint8_t* nocollide;// problems: 1 if all labels lie in [0, bucket_count)
+  const uint8_t* folds;    // problems x L
+  const int* fixed;        // L (shared) or nullptr; value 1 = fixed
+  const int* goff;         // G+1 group offsets
+  const int* gmem;         // L group members (rows), ascending within a group
+  const uint64_t* seeds;   // problems
+  // outputs
+  uint16_t* clbest;        // problems x L
+  uint16_t* cvpredbest;    // problems x L
+  double* vect_acc;        // problems x T
+  double* vect_score;      // problems x T
+  int* proposal_size;      // problems x T
+  int* active;             // problems x T
+  uint8_t* flags;          // problems x T x 3
+  int* counters;           // problems x 16
+  double* best;            // problems x 2 (accbest, scorebest)
+  int* status;             // problems
+  // scratch
+  int* trans;              // problems x C0max x C0max
+  int* foldcnt;            // problems x F x C0max
+  uint16_t* rows_scratch;  // problems x 5 x L (when label arrays do not fit in shared memory)
+};
+
+size_t evolve_smem_bytes(int L, int C0max, bool rows_in_smem);
+int evolve_launch(const EvolveParams& p, int grid, size_t smem, void* stream);
+
+}  // namespace kgb

@@ -1,0 +1,308 @@
+// Graph-side kernels of the KODAMA.matrix path.
+//
+//   graph_minmax / normalize_external: the caller graph as
+//     normalize_external_graph (kodama_matrix.cpp:1292-1330) leaves it:
+//     one-based detection, invalid / self / non-finite entries dropped,
+//     survivors compacted to the left, distances clamped at 0, width K.
+//   normalize_indices: normalize_graph_indices (core.cpp:586-622): positions
+//     kept, invalid ids -> -1, non-finite or negative distances -> +inf.
+//   build_vote_tables: per problem and landmark row, the first k' valid,
+//     non-self, out-of-fold neighbours among landmark rows with score -(d*d):
+//     subset_graph_to_rows (kodama_matrix.cpp:1332-1365) followed by
+//     precompute_knn_cv_graph (core.cpp:624-692).
+//   project_labels: non-landmark label = majority over the first knn.k
+//     landmark neighbours of its graph row, ties to the smaller label, none ->
+//     label of the first landmark (kodama_matrix.cpp:3221-3261, :169).
+//   dissimilarity: co-label proximity (kodama_matrix.cpp:2685-2776):
+//     d' = (1 + d) / (same/valid)^2 or +inf, row stably sorted by (d', id).
+#include "graph_ops.cuh"
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+namespace kgb {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+__global__ void minmax_kernel(const int* __restrict__ idx, size_t total, int* mm) {
+  int lo = 0x7fffffff, hi = (-0x7fffffff - 1);
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < total;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    const int v = idx[i];
+    if (v < 0) continue;
+    lo = min(lo, v);
+    hi = max(hi, v);
+  }
+  lo = __reduce_min_sync(kFull, lo);
+  hi = __reduce_max_sync(kFull, hi);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&mm[0], lo);
+    atomicMax(&mm[1], hi);
+  }
+}
+
+__device__ __forceinline__ bool one_based_of(int base, const int* mm, int samples) {
+  return base == 1 || (base < 0 && mm[0] >= 1 && mm[1] <= samples);
+}
+
+__global__ void normalize_external_kernel(const int* __restrict__ in_idx, const float* __restrict__ in_dist,
+                                          int n, int gk, int K, int base, const int* mm,
+                                          int* __restrict__ out_idx, float* __restrict__ out_dist) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const bool ob = one_based_of(base, mm, n);
+  int col = 0;
+  for (int j = 0; j < gk && col < K; ++j) {
+    const size_t src = static_cast<size_t>(i) * gk + j;
+    int id = in_idx[src];
+    if (ob && id > 0) --id;
+    if (id < 0 || id >= n || id == i) continue;
+    const float d = in_dist[src];
+    if (!isfinite(d)) continue;
+    out_idx[static_cast<size_t>(i) * K + col] = id;
+    out_dist[static_cast<size_t>(i) * K + col] = (0.0f < d) ? d : 0.0f;  // std::max(0.0f, d)
+    ++col;
+  }
+  for (; col < K; ++col) {
+    out_idx[static_cast<size_t>(i) * K + col] = -1;
+    out_dist[static_cast<size_t>(i) * K + col] = INFINITY;
+  }
+}
+
+__global__ void normalize_indices_kernel(const int* __restrict__ in_idx, const float* __restrict__ in_dist,
+                                         size_t total, int samples, int base, const int* mm,
+                                         int* __restrict__ out_idx, float* __restrict__ out_dist) {
+  const bool ob = one_based_of(base, mm, samples);
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < total;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    int id = in_idx[i];
+    if (ob && id > 0) --id;
+    if (id < 0 || id >= samples) {
+      out_idx[i] = -1;
+      out_dist[i] = INFINITY;
+      continue;
+    }
+    out_idx[i] = id;
+    const float d = in_dist[i];
+    out_dist[i] = (isfinite(d) && d >= 0.0f) ? d : INFINITY;
+  }
+}
+
+__global__ void scatter_g2l_kernel(const int* __restrict__ land, int problems, int L, int n, int* __restrict__ g2l) {
+  const size_t t = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x;
+  if (t >= static_cast<size_t>(problems) * L) return;
+  const int p = static_cast<int>(t / L), i = static_cast<int>(t % L);
+  g2l[static_cast<size_t>(p) * n + land[t]] = i;
+}
+
+// One thread per (problem, row).
+__global__ void vote_table_kernel(VoteTableArgs a) {
+  const size_t t = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x;
+  if (t >= static_cast<size_t>(a.problems) * a.L) return;
+  const int p = static_cast<int>(t / a.L), i = static_cast<int>(t % a.L);
+  const int grow = a.land ? a.land[t] : i;
+  const int* g2l = a.g2l ? a.g2l + static_cast<size_t>(p) * a.n : nullptr;
+  const uint8_t* fo = a.folds + static_cast<size_t>(p) * a.L;
+  const int myfold = fo[i];
+  uint16_t* nb = a.nb + t * a.w;
+  float* sc = a.sc + t * a.w;
+  int col = 0;
+  for (int j = 0; j < a.K && col < a.w; ++j) {
+    const size_t src = static_cast<size_t>(grow) * a.K + j;
+    const int gnb = a.gidx[src];
+    if (gnb < 0 || gnb >= a.n) continue;
+    const int loc = g2l ? g2l[gnb] : gnb;
+    if (loc < 0 || loc == i) continue;
+    if (fo[loc] == myfold) continue;
+    const float dist = a.gdist[src];
+    if (!isfinite(dist)) continue;
+    const float dc = (0.0f < dist) ? dist : 0.0f;
+    nb[col] = static_cast<uint16_t>(loc);
+    sc[col] = -__fmul_rn(dc, dc);
+    ++col;
+  }
+  for (; col < a.w; ++col) {
+    nb[col] = 0xFFFFu;
+    sc[col] = -INFINITY;
+  }
+}
+
+// One thread per (problem, global row).
+__global__ void project_kernel(ProjectArgs a) {
+  const size_t t = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x;
+  if (t >= static_cast<size_t>(a.problems) * a.n) return;
+  const int p = static_cast<int>(t / a.n), r = static_cast<int>(t % a.n);
+  const int* g2l = a.g2l + static_cast<size_t>(p) * a.n;
+  const uint16_t* best = a.clbest + static_cast<size_t>(p) * a.L;
+  const int* c2l = a.code2label + static_cast<size_t>(p) * a.C0max;
+  const int loc = g2l[r];
+  int code;
+  if (loc >= 0) {
+    code = best[loc];
+  } else {
+    int votes[kMaxProjectK];
+    int nv = 0;
+    for (int j = 0; j < a.K && nv < a.pk; ++j) {
+      const int gnb = a.gidx[static_cast<size_t>(r) * a.K + j];
+      if (gnb < 0 || gnb >= a.n) continue;
+      const int l = g2l[gnb];
+      if (l >= 0) votes[nv++] = best[l];
+    }
+    if (nv == 0) {
+      code = best[0];
+    } else {
+      int bl = 0x7fffffff, bc = 0;
+      for (int q = 0; q < nv; ++q) {
+        const int v = votes[q];
+        int c = 0;
+        for (int u = 0; u < nv; ++u) c += votes[u] == v;
+        if (c > bc || (c == bc && v < bl)) {
+          bl = v;
+          bc = c;
+        }
+      }
+      code = bl;
+    }
+  }
+  a.res[t] = c2l[code];
+}
+
+__global__ void transpose_kernel(const int* __restrict__ res, int runs, int n, int* __restrict__ out) {
+  __shared__ int tile[32][33];
+  const int r0 = blockIdx.y * 32, s0 = blockIdx.x * 32;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int r = r0 + k, s = s0 + threadIdx.x;
+    if (r < runs && s < n) tile[k][threadIdx.x] = res[static_cast<size_t>(r) * n + s];
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int s = s0 + k, r = r0 + threadIdx.x;
+    if (r < runs && s < n) out[static_cast<size_t>(s) * runs + r] = tile[threadIdx.x][k];
+  }
+}
+
+// One warp per row; lanes cooperate over runs for each neighbour, then a
+// rank sort of the row in shared memory.
+__global__ void dissimilarity_kernel(DissimArgs a) {
+  extern __shared__ unsigned char dsm[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int wpb = blockDim.x >> 5;
+  float* kd = reinterpret_cast<float*>(dsm) + static_cast<size_t>(warp) * a.K;
+  int* ki = reinterpret_cast<int*>(reinterpret_cast<float*>(dsm) + static_cast<size_t>(wpb) * a.K) +
+            static_cast<size_t>(warp) * a.K;
+  const int i = blockIdx.x * wpb + warp;
+  if (i >= a.n) return;
+  const int* li = a.lbs + static_cast<size_t>(i) * a.runs;
+  for (int j = 0; j < a.K; ++j) {
+    const size_t off = static_cast<size_t>(i) * a.K + j;
+    const int stored = a.idx[off];
+    const int nb = (stored >= 0 && a.in_one_based) ? stored - 1 : stored;
+    float d = a.dist[off];
+    if (nb < 0 || nb >= a.n || !isfinite(d)) {
+      if (lane == 0) {
+        kd[j] = INFINITY;
+        ki[j] = stored;
+      }
+      continue;
+    }
+    const int* lj = a.lbs + static_cast<size_t>(nb) * a.runs;
+    int same = 0, valid = 0;
+    for (int r = lane; r < a.runs; r += 32) {
+      const int x = li[r], y = lj[r];
+      const int pv = (x != 0) & (y != 0);
+      valid += pv;
+      same += pv & (x == y);
+    }
+    same = __reduce_add_sync(kFull, same);
+    valid = __reduce_add_sync(kFull, valid);
+    if (lane == 0) {
+      if (same == 0 || valid == 0) {
+        d = INFINITY;
+      } else {
+        const double agr = __ddiv_rn(static_cast<double>(same), static_cast<double>(valid));
+        d = static_cast<float>(__ddiv_rn(__dadd_rn(1.0, static_cast<double>(d)), __dmul_rn(agr, agr)));
+      }
+      kd[j] = d;
+      ki[j] = a.out_one_based ? nb + 1 : nb;
+    }
+  }
+  __syncwarp();
+  // stable rank sort by (distance, id)
+  for (int j = lane; j < a.K; j += 32) {
+    const float dj = kd[j];
+    const int ij = ki[j];
+    int rank = 0;
+    for (int q = 0; q < a.K; ++q) {
+      const float dq = kd[q];
+      const int iq = ki[q];
+      const bool less = dq < dj || (!(dj < dq) && iq < ij);
+      const bool equal_before = !(dq < dj) && !(dj < dq) && iq == ij && q < j;
+      rank += less || equal_before;
+    }
+    a.out_idx[static_cast<size_t>(i) * a.K + rank] = ij;
+    a.out_dist[static_cast<size_t>(i) * a.K + rank] = dj;
+  }
+}
+
+}  // namespace
+
+int graph_minmax(const int* idx, size_t total, int* mm, cudaStream_t st) {
+  const int init[2] = {0x7fffffff, (-0x7fffffff - 1)};
+  cudaMemcpyAsync(mm, init, sizeof(init), cudaMemcpyHostToDevice, st);
+  const int blocks = static_cast<int>((total + 255) / 256 < 2048 ? (total + 255) / 256 : 2048);
+  minmax_kernel<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(idx, total, mm);
+  return static_cast<int>(cudaGetLastError());
+}
+
+int normalize_external(const int* in_idx, const float* in_dist, int n, int gk, int K, int base, const int* mm,
+                       int* out_idx, float* out_dist, cudaStream_t st) {
+  normalize_external_kernel<<<(n + 255) / 256, 256, 0, st>>>(in_idx, in_dist, n, gk, K, base, mm, out_idx, out_dist);
+  return static_cast<int>(cudaGetLastError());
+}
+
+int normalize_indices(const int* in_idx, const float* in_dist, size_t total, int samples, int base, const int* mm,
+                      int* out_idx, float* out_dist, cudaStream_t st) {
+  const int blocks = static_cast<int>((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096);
+  normalize_indices_kernel<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(in_idx, in_dist, total, samples, base, mm,
+                                                                  out_idx, out_dist);
+  return static_cast<int>(cudaGetLastError());
+}
+
+int build_g2l(const int* land, int problems, int L, int n, int* g2l, cudaStream_t st) {
+  cudaMemsetAsync(g2l, 0xff, sizeof(int) * static_cast<size_t>(problems) * n, st);
+  const size_t total = static_cast<size_t>(problems) * L;
+  scatter_g2l_kernel<<<static_cast<unsigned>((total + 255) / 256), 256, 0, st>>>(land, problems, L, n, g2l);
+  return static_cast<int>(cudaGetLastError());
+}
+
+int build_vote_tables(const VoteTableArgs& a, cudaStream_t st) {
+  const size_t total = static_cast<size_t>(a.problems) * a.L;
+  vote_table_kernel<<<static_cast<unsigned>((total + 255) / 256), 256, 0, st>>>(a);
+  return static_cast<int>(cudaGetLastError());
+}
+
+int project_labels(const ProjectArgs& a, cudaStream_t st) {
+  const size_t total = static_cast<size_t>(a.problems) * a.n;
+  project_kernel<<<static_cast<unsigned>((total + 255) / 256), 256, 0, st>>>(a);
+  return static_cast<int>(cudaGetLastError());
+}
+
+int transpose_runs(const int* res, int runs, int n, int* out, cudaStream_t st) {
+  dim3 grid((n + 31) / 32, (runs + 31) / 32);
+  transpose_kernel<<<grid, dim3(32, 8), 0, st>>>(res, runs, n, out);
+  return static_cast<int>(cudaGetLastError());
+}
+
+int dissimilarity(const DissimArgs& a, cudaStream_t st) {
+  const int wpb = 8;
+  const size_t smem = static_cast<size_t>(wpb) * a.K * (sizeof(float) + sizeof(int));
+  if (smem > 48 * 1024) cudaFuncSetAttribute(dissimilarity_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            static_cast<int>(smem));
+  dissimilarity_kernel<<<(a.n + wpb - 1) / wpb, wpb * 32, smem, st>>>(a);
+  return static_cast<int>(cudaGetLastError());
+}
+
+}  // namespace kgb

@@ -1,0 +1,33 @@
+// Batched bit-exact k-means (kmeans.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+namespace kgb {
+
+struct KMeansBatch {
+  int problems;
+  int n;                    // rows per problem
+  int d;
+  int k;
+  int max_iter;
+  const float* x;           // device matrix (rows x d)
+  const int* rows;          // problems x n row ids into x, or nullptr = identity (problems == 1)
+  const float* pnorm;       // per row of x: dot(x_r, x_r)
+  const int* init_rows;     // problems x k: initial centroid rows (indices into the problem's rows)
+  const float* split_uniform; // mt19937(1234) uniforms for empty-cluster splitting (k entries)
+  float* cent;              // problems x k x d
+  float* cnorm;             // problems x k
+  int* assign;              // problems x n (must start at -1)
+  int* members;             // problems x n scratch
+  int* active;              // problems
+  int* changed;             // problems
+  int* labels;              // problems x n output, 1-based
+};
+
+size_t kmeans_update_smem(int k);
+int kmeans_row_norms(const float* x, int n, int d, float* out, cudaStream_t st);
+int kmeans_run(const KMeansBatch& b, cudaStream_t st);
+
+}  // namespace kgb

@@ -23,7 +23,7 @@
 //     long double: ext80.h.
 // Build with -ffp-contract=off so no multiply-add is fused.
 
-#include "ext80.h"
+#include "../kodama_gb300/csrc/ext80.h"
 
 #include <algorithm>
 #include <atomic>
