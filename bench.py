@@ -1,0 +1,306 @@
+#!/usr/bin/env python
+"""Benchmark: KODAMA.matrix label evolution on one GB300 (and its CPU baseline).
+
+Workload (one "step" = one full KODAMA.matrix call): N=20000 points, d=50,
+12-cluster Gaussian mixture (synthetic, seed 2), M=100 runs x Tcycle=100,
+exact kNN graph K=30, knn.k=30, 10 folds, splitting=50, landmarks=10000
+(L=10000 per run), kNN classifier, default evolution policy.
+
+value  : device seconds per step (CUDA events on the library's stream), input
+         matrix already resident in HBM, label matrix left in HBM;
+e2e    : seconds per step through the public host-buffer C-ABI call
+         (pinned host input copied in, label matrix + traces copied out);
+roofline: the persistent evolution kernel (the dominant kernel) against
+         the measured HBM copy bandwidth;
+cpu_baseline / --impl reference: the CPU restatement of the reference
+         algorithm (oracle/, all host threads) on a bounded sample of the same
+         workload, extrapolated to M=100 runs.
+
+Launch: python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+(N>1 under torchrun: every rank runs its own replica; weak scaling).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "KODAMA.matrix wall-s at N=20k,d=50,M=100: learned vs plain GPU at equal CV acc"
+WORKLOAD = dict(n=20000, d=50, runs=100, cycles=100, graph_neighbors=30, knn_k=30, folds=10,
+                splitting=50, landmarks=10000, seed=1234)
+CPU_SAMPLE_RUNS = 16
+# DRAM bytes (read + write) of one evolution-kernel launch, scaled from the
+# ncu capture summarised in profiles/evolve_kernel_cfg2.md (None until captured).
+EVOLVE_TRAFFIC_BYTES = None
+
+
+def _config(extra=None):
+    c = {"workload": "KODAMA.matrix kNN N=20000 d=50 (12-cluster Gaussian mixture), M=100 runs, "
+                     "Tcycle=100, exact graph K=30, knn.k=30, folds=10, splitting=50, landmarks=10000",
+         "global_batch": WORKLOAD["runs"], "seq_len": WORKLOAD["cycles"],
+         "parallelism": "replicas", "l2": "flushed between steps (512 MB write)",
+         "data": "synthetic gaussian_mixture(seed=2)"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+def _data():
+    from kodama_gb300 import datasets
+    x, _ = datasets.gaussian_mixture(n=WORKLOAD["n"], d=WORKLOAD["d"], seed=2)
+    return np.ascontiguousarray(x, np.float32)
+
+
+def _matrix_kw():
+    return dict(runs=WORKLOAD["runs"], cycles=WORKLOAD["cycles"], landmarks=WORKLOAD["landmarks"],
+                splitting=WORKLOAD["splitting"], graph_neighbors=WORKLOAD["graph_neighbors"],
+                folds=WORKLOAD["folds"], knn_k=WORKLOAD["knn_k"], seed=WORKLOAD["seed"])
+
+
+def _peaks():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def evolve_bytes_per_launch(L, w, runs, cycles):
+    """Algorithmic bytes of one evolution-kernel launch: per CV evaluation of a
+    run, the L x k' neighbour table (2-byte ids + 4-byte scores) is streamed
+    once and L 2-byte labels read and L 2-byte predictions written; M*(T+1)
+    evaluations."""
+    return runs * (cycles + 1) * (L * w * (2 + 4) + L * 2 * 2)
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    FIELDS = ("clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.active",
+              "clocks_event_reasons.hw_slowdown", "clocks_event_reasons.hw_thermal_slowdown",
+              "clocks_event_reasons.sw_thermal_slowdown", "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.proc = None
+        self.device_index = device_index
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device_index), "--query-gpu=" + ",".join(self.FIELDS),
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is None:
+            return
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        if not self.lines:
+            return None
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except (ValueError, IndexError):
+                continue
+            for name, val in zip(names, parts[4:8]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(x, threads=None):
+    """The CPU restatement on a bounded sample: exact graph + atlas + 16 runs,
+    extrapolated to M=100 runs (runs are independent)."""
+    from oracle import oracle
+    if not oracle.available():
+        oracle.build()
+    threads = threads or os.cpu_count() or 1
+    t0 = time.perf_counter()
+    gi, gd = oracle.exact_knn(x, WORKLOAD["graph_neighbors"], threads=threads)
+    t_graph = time.perf_counter() - t0
+    kw = _matrix_kw()
+    kw["runs"] = CPU_SAMPLE_RUNS
+    t1 = time.perf_counter()
+    r = oracle.kodama_matrix_graph_data(x, gi, gd, 0, seed=kw.pop("seed"), threads=threads, materialize=0, **kw)
+    t_matrix = time.perf_counter() - t1
+    t_atlas, t_runs = float(r.timings[4]), float(r.timings[2])
+    total = t_graph + t_atlas + t_runs * (WORKLOAD["runs"] / CPU_SAMPLE_RUNS) + max(0.0, t_matrix - t_atlas - t_runs)
+    return {"value": round(total, 4), "unit": "s", "cores": threads, "kind": "port",
+            "sample": f"exact graph (N=20000) + atlas + {CPU_SAMPLE_RUNS} of 100 runs timed "
+                      f"({t_graph + t_matrix:.2f} s), runs scaled x{WORKLOAD['runs'] / CPU_SAMPLE_RUNS:g}",
+            "stages_s": {"graph": round(t_graph, 3), "atlas": round(t_atlas, 3),
+                         "runs_sample": round(t_runs, 3)}}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    x = _data()
+    for _ in range(args.warmup):
+        cpu_baseline(x)
+    vals = []
+    last = None
+    for _ in range(args.steps):
+        last = cpu_baseline(x)
+        vals.append(last["value"])
+    v = float(np.mean(vals))
+    line = {"metric": METRIC, "value": round(v, 4), "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(v * 1000, 2), "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32/f64", "data": "synthetic",
+            "config": _config(), "impl": "reference",
+            "cpu_baseline": dict(last, value=round(v, 4)),
+            "e2e": {"value": round(v, 4), "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_gpu(args):
+    import torch
+
+    import kodama_gb300 as kg
+    from kodama_gb300 import build as kbuild
+
+    kbuild.build()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    x = _data()
+    kw = _matrix_kw()
+    n, runs, cycles = WORKLOAD["n"], WORKLOAD["runs"], WORKLOAD["cycles"]
+    x_dev = torch.from_numpy(x).to(f"cuda:{local}")
+    res_dev = torch.empty((runs, n), dtype=torch.int32, device=f"cuda:{local}")
+    x_pin = torch.from_numpy(x).pin_memory()
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        kg.KODAMA_matrix(x_dev, res_out=res_dev, device=local, **kw)
+    kg.KODAMA_matrix(x_pin.numpy(), device=local, **kw)
+
+    # device-resident timing
+    spans, evo, walls, accs = [], [], [], []
+    launches0 = kg.launch_count()
+    barrier()
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r = kg.KODAMA_matrix(x_dev, res_out=res_dev, device=local, **kw)
+            walls.append(time.perf_counter() - t0)
+            spans.append(r.kernel_ms["device_span"] / 1000.0)
+            evo.append(r.kernel_ms["evolution"] / 1000.0)
+            accs.append(float(r.acc.mean()))
+        barrier()
+    launches = (kg.launch_count() - launches0) // max(1, args.steps)
+    value = float(np.mean(spans))
+    stage_ms = {k: round(v, 3) for k, v in r.kernel_ms.items()}
+
+    # end-to-end through the host-buffer C-ABI call
+    e2e = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        re = kg.KODAMA_matrix(x_pin.numpy(), device=local, **kw)
+        e2e.append(time.perf_counter() - t0)
+    e2e_v = float(np.mean(e2e))
+    same = bool(np.array_equal(re.acc, r.acc))
+
+    if dist is not None:
+        t = torch.tensor([value, e2e_v], device=f"cuda:{local}", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        value, e2e_v = float(t[0]), float(t[1])
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    L = min(WORKLOAD["landmarks"], n - 1)
+    w = min(WORKLOAD["knn_k"], WORKLOAD["graph_neighbors"])
+    evo_s = float(np.mean(evo))
+    bytes_launch = evolve_bytes_per_launch(L, w, runs, cycles)
+    peak, peak_kind = _peaks()
+    achieved = bytes_launch / evo_s / 1e9
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                "kernel": "evolve_kernel (persistent, one CTA per run)",
+                "algorithmic_bytes_per_launch": bytes_launch,
+                "launch_ms": round(evo_s * 1000, 3),
+                "traffic": EVOLVE_TRAFFIC_BYTES}
+    h2d = x.nbytes
+    d2h = runs * n * 4 + runs * 8 + runs * cycles * 8 + runs * 3 * 8 + runs * 8 * 4 + runs * cycles * 5 * 4
+    line = {"metric": METRIC, "value": round(value, 5), "unit": "s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(value * 1000, 3), "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32/f64", "data": "synthetic",
+            "config": _config({"parallelism": f"replicas{world}"}),
+            "e2e": {"value": round(e2e_v, 5), "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "roofline": roofline,
+            "gpu_launches": int(launches),
+            "clocks": clocks.summary(),
+            "stage_ms": stage_ms,
+            "host_wall_s": round(float(np.mean(walls)), 5),
+            "mean_final_cv_acc": round(float(np.mean(accs)), 6),
+            "e2e_matches_resident": same}
+    if world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(x)
+    print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

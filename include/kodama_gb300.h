@@ -83,7 +83,13 @@ typedef struct kgb_matrix_result {
   int32_t knn_cap;           /* capacity (columns) of knn_idx/knn_dist */
   int32_t knn_k;             /* out: columns written */
   int32_t effective_landmarks; /* out */
-  double timings[8];         /* out: total, graph, atlas, landmarks+init, evolution, projection, dissimilarity, h2d+d2h */
+  double timings[8];         /* out: host seconds: total, graph, atlas, landmarks+init, evolution+projection,
+                                unused, dissimilarity+outputs, unused */
+  double kernel_ms[8];       /* out: CUDA-event milliseconds on the call's stream: graph build, atlas k-means,
+                                landmark planning + k-means, vote tables, evolution kernel, projection,
+                                dissimilarity, whole device span */
+  int32_t res_on_device;     /* in: 1 = `res` is a device pointer (the label matrix stays in HBM) */
+  int32_t reserved;
 } kgb_matrix_result;
 
 /* Replaces KODAMAMatrix_CUDA (kodama.hpp:1077-1083; dispatch
@@ -91,6 +97,12 @@ typedef struct kgb_matrix_result {
  * the device (graph-input semantics of kodama_matrix.cpp:3528-3558). */
 int kgb_kodama_matrix(const float* x, int32_t n, int32_t d, const kgb_matrix_options* opt,
                       kgb_matrix_result* out);
+
+/* Same as kgb_kodama_matrix with `x` already resident in device memory (a
+ * CUDA device pointer on opt->device).  Set out->res_on_device to keep the
+ * label matrix in HBM as well.  Used to time the path without host copies. */
+int kgb_kodama_matrix_resident(const float* x_device, int32_t n, int32_t d, const kgb_matrix_options* opt,
+                               kgb_matrix_result* out);
 
 /* Replaces KODAMAMatrixFromGraphData_CUDA (kodama.hpp:1215-1222,
  * kodama_matrix.cpp:4676-4699): data plus a caller graph (n x gk, indices
@@ -165,6 +177,9 @@ int kgb_knn_graph(const float* x, int32_t n, int32_t d, int32_t K, int32_t devic
  * one-based graph, in place.  res is runs x samples. */
 int kgb_dissimilarity_inplace(int32_t* gidx, float* gdist, int32_t samples, int32_t gk,
                               const int32_t* res, int32_t runs, int32_t device);
+
+/* Number of kernels this library has launched since it was loaded. */
+int64_t kgb_launch_count(void);
 
 /* Message of the last failure on this thread; returns its full length. */
 int kgb_last_error(char* buf, size_t len);

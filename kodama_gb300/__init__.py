@@ -24,7 +24,7 @@ from . import _native as N
 
 __all__ = ["KODAMA_matrix", "CoreKNNGraph", "CoreKNNGraph_batch", "knn_graph",
            "KODAMADissimilarityInPlace", "MatrixResult", "CoreResult", "EvolutionPolicy",
-           "library_path", "version"]
+           "library_path", "version", "launch_count"]
 
 
 def library_path() -> str:
@@ -88,10 +88,13 @@ class MatrixResult:
     knn_dist: np.ndarray | None
     effective_landmarks: int
     timings: dict = field(default_factory=dict)
+    kernel_ms: dict = field(default_factory=dict)
 
 
 _TIMING_NAMES = ("total", "knn_graph", "shared_landmark_partition", "landmark_initialization",
-                 "core_evolution", "label_projection", "kodama_dissimilarity", "transfers")
+                 "core_evolution", "unused", "kodama_dissimilarity", "unused2")
+_KERNEL_NAMES = ("knn_graph", "atlas_kmeans", "landmark_kmeans", "vote_tables", "evolution",
+                 "projection", "dissimilarity", "device_span")
 
 
 def _matrix_options(runs, cycles, landmarks, splitting, graph_neighbors, folds, knn_k, seed,
@@ -107,18 +110,29 @@ def _matrix_options(runs, cycles, landmarks, splitting, graph_neighbors, folds, 
 def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitting=0,
                   graph_neighbors=100, folds=5, knn_k=30, seed=1234, materialize_graph=False,
                   apply_dissimilarity=True, index_base=-1, device=0, host_threads=0,
-                  policy="full") -> MatrixResult:
+                  policy="full", res_out=None) -> MatrixResult:
     """KODAMA.matrix with the kNN classifier on the GPU.
 
     ``graph`` = (indices, distances) of shape (n, K) runs the graph-input path
     (KODAMAMatrixFromGraphData_CUDA); without it the exact kNN graph is built
     on the device (KODAMAMatrix_CUDA with exact-graph semantics).
+    ``x`` may also be a CUDA torch tensor (float32, contiguous): the data is
+    then read in place from HBM (kgb_kodama_matrix_resident); pass
+    ``res_out`` (a CUDA int32 tensor of shape (runs, n)) to keep the label
+    matrix on the device too.
     Defaults are those of KODAMAMatrixOptions (kodama.hpp:535-570).
     """
-    x = np.ascontiguousarray(x, dtype=np.float32)
-    if x.ndim != 2:
-        raise ValueError("x must be a 2-D matrix")
-    n, d = x.shape
+    x_dev = None
+    if hasattr(x, "is_cuda") and x.is_cuda:
+        if graph is not None:
+            raise ValueError("device-resident input is supported for raw data only")
+        x_dev = x
+        n, d = int(x.shape[0]), int(x.shape[1])
+    else:
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        if x.ndim != 2:
+            raise ValueError("x must be a 2-D matrix")
+        n, d = x.shape
     opt = _matrix_options(runs, cycles, landmarks, splitting, graph_neighbors, folds, knn_k, seed,
                           materialize_graph, apply_dissimilarity, device, host_threads, policy)
     res = np.zeros((runs, n), np.int32)
@@ -131,7 +145,13 @@ def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitt
     kidx = np.zeros((n, cap), np.int32) if materialize_graph else None
     kdist = np.zeros((n, cap), np.float32) if materialize_graph else None
     out = N.MatrixResult()
-    out.res = res.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+    if res_out is not None:
+        if tuple(res_out.shape) != (runs, n) or not res_out.is_cuda:
+            raise ValueError("res_out must be a CUDA int32 tensor of shape (runs, n)")
+        out.res = ctypes.cast(ctypes.c_void_p(res_out.data_ptr()), ctypes.POINTER(ctypes.c_int32))
+        out.res_on_device = 1
+    else:
+        out.res = res.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
     out.acc = acc.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
     out.v = v.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
     out.run_hashes = hashes.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))
@@ -142,7 +162,10 @@ def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitt
         out.knn_dist = kdist.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
     out.knn_cap = cap
     lib = N.load()
-    if graph is None:
+    if x_dev is not None:
+        rc = lib.kgb_kodama_matrix_resident(ctypes.c_void_p(x_dev.data_ptr()), n, d, ctypes.byref(opt),
+                                            ctypes.byref(out))
+    elif graph is None:
         rc = lib.kgb_kodama_matrix(_ptr(x), n, d, ctypes.byref(opt), ctypes.byref(out))
     else:
         gi = np.ascontiguousarray(graph[0], dtype=np.int32)
@@ -158,7 +181,13 @@ def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitt
         knn_idx=kidx[:, :k].copy() if (materialize_graph and k) else None,
         knn_dist=kdist[:, :k].copy() if (materialize_graph and k) else None,
         effective_landmarks=out.effective_landmarks,
-        timings=dict(zip(_TIMING_NAMES, list(out.timings))))
+        timings=dict(zip(_TIMING_NAMES, list(out.timings))),
+        kernel_ms=dict(zip(_KERNEL_NAMES, list(out.kernel_ms))))
+
+
+def launch_count() -> int:
+    """Kernels launched by the CUDA library since it was loaded."""
+    return int(N.load().kgb_launch_count())
 
 
 @dataclass

@@ -18,6 +18,8 @@ KGB_OK, KGB_EINVAL, KGB_ENOMEM, KGB_ECUDA, KGB_ETIMEOUT, KGB_EINTERNAL = range(6
 EXPORTED = (
     "kgb_kodama_matrix",
     "kgb_kodama_matrix_from_graph_data",
+    "kgb_kodama_matrix_resident",
+    "kgb_launch_count",
     "kgb_core_knn_graph",
     "kgb_core_knn_graph_batch",
     "kgb_knn_graph",
@@ -55,6 +57,9 @@ class MatrixResult(ctypes.Structure):
         ("knn_k", ctypes.c_int32),
         ("effective_landmarks", ctypes.c_int32),
         ("timings", ctypes.c_double * 8),
+        ("kernel_ms", ctypes.c_double * 8),
+        ("res_on_device", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
     ]
 
 
@@ -97,6 +102,10 @@ def load():
     P = ctypes.c_void_p
     i32 = ctypes.c_int32
     lib.kgb_kodama_matrix.argtypes = [P, i32, i32, ctypes.POINTER(MatrixOptions), ctypes.POINTER(MatrixResult)]
+    lib.kgb_kodama_matrix_resident.argtypes = [P, i32, i32, ctypes.POINTER(MatrixOptions),
+                                               ctypes.POINTER(MatrixResult)]
+    lib.kgb_launch_count.restype = ctypes.c_int64
+    lib.kgb_launch_count.argtypes = []
     lib.kgb_kodama_matrix_from_graph_data.argtypes = [
         P, i32, i32, P, P, i32, i32, ctypes.POINTER(MatrixOptions), ctypes.POINTER(MatrixResult)]
     lib.kgb_core_knn_graph.argtypes = [P, P, i32, i32, i32, P, P, P, ctypes.POINTER(CoreOptions),
@@ -108,7 +117,7 @@ def load():
     lib.kgb_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     lib.kgb_version.restype = ctypes.c_char_p
     for name in EXPORTED:
-        if name not in ("kgb_version",):
+        if name not in ("kgb_version", "kgb_launch_count"):
             getattr(lib, name).restype = ctypes.c_int
     _lib = lib
     return lib

@@ -10,10 +10,12 @@
 #include "host_plan.h"
 #include "kmeans.cuh"
 #include "knn.cuh"
+#include "launch_count.cuh"
 
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -23,6 +25,14 @@
 #include <string>
 #include <thread>
 #include <vector>
+
+namespace kgb {
+namespace {
+std::atomic<long long> g_launches{0};
+}
+void count_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long g_launches_value() { return g_launches.load(std::memory_order_relaxed); }
+}  // namespace kgb
 
 namespace {
 
@@ -83,7 +93,20 @@ class Ctx {
   ~Ctx() {
     for (void* p : bufs_) cudaFreeAsync(p, stream_);
     cudaStreamSynchronize(stream_);
+    for (int i = 0; i < nev_; ++i) cudaEventDestroy(ev_[i]);
     cudaStreamDestroy(stream_);
+  }
+  // CUDA events on the call's stream, for per-stage device timings.
+  int mark() {
+    if (nev_ >= kMaxEvents) return nev_ - 1;
+    ck(cudaEventCreate(&ev_[nev_]), "cudaEventCreate");
+    ck(cudaEventRecord(ev_[nev_], stream_), "cudaEventRecord");
+    return nev_++;
+  }
+  double ms(int a, int b) {
+    float v = 0.0f;
+    if (a < 0 || b < 0 || cudaEventElapsedTime(&v, ev_[a], ev_[b]) != cudaSuccess) return 0.0;
+    return static_cast<double>(v);
   }
   Ctx(const Ctx&) = delete;
   Ctx& operator=(const Ctx&) = delete;
@@ -111,9 +134,12 @@ class Ctx {
   int sms() const { return sms_; }
 
  private:
+  static constexpr int kMaxEvents = 32;
   cudaStream_t stream_ = nullptr;
   int sms_ = 1;
   std::vector<void*> bufs_;
+  cudaEvent_t ev_[kMaxEvents];
+  int nev_ = 0;
 };
 
 struct Clock {
@@ -268,7 +294,8 @@ void validate_matrix_options(const kgb_matrix_options* o) {
 // The KODAMA.matrix path after the global graph (n x K zero-based, compacted,
 // distances finite >= 0) is resident on the device.
 void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_gidx, float* d_gdist, int K,
-                              const kgb_matrix_options* o, kgb_matrix_result* out, Clock& clk) {
+                              const kgb_matrix_options* o, kgb_matrix_result* out, Clock& clk, int ev_start,
+                              int ev_graph) {
   const kgb_policy pol = policy_is_zero(o->policy) ? default_policy() : o->policy;
   int landmarks = o->landmarks > 0 ? o->landmarks : 10000;
   if (landmarks >= n) landmarks = static_cast<int>(std::ceil(static_cast<double>(n) * 0.75));
@@ -315,6 +342,7 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     B.labels = d_atlas_labels;
     ck_launch(kgb::kmeans_run(B, st), "atlas k-means");
   }
+  const int ev_atlas = ctx.mark();
   std::vector<int> atlas(static_cast<size_t>(n));
   ctx.download(atlas.data(), d_atlas_labels, n);
   ctx.sync();
@@ -384,6 +412,7 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   }
   out->timings[3] = clk.lap();
 
+  const int ev_init = ctx.mark();
   // per-run fold-filtered vote tables over the landmark subgraph
   int* d_g2l = ctx.alloc<int>(static_cast<size_t>(M) * n);
   ck_launch(kgb::build_g2l(d_land, M, L, n, d_g2l, st), "landmark index");
@@ -405,6 +434,7 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     a.sc = d_sc;
     ck_launch(kgb::build_vote_tables(a, st), "vote tables");
   }
+  const int ev_tables = ctx.mark();
   std::vector<int> identity(static_cast<size_t>(L));
   for (int i = 0; i < L; ++i) identity[i] = i;
   std::vector<int> goff(static_cast<size_t>(L) + 1);
@@ -442,7 +472,9 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   P.goff = ctx.upload(goff.data(), goff.size());
   P.gmem = ctx.upload(identity.data(), identity.size());
   P.seeds = ctx.upload(seeds.data(), seeds.size());
+  const int ev_evo0 = ctx.mark();
   const EvolveBuffers eb = run_evolution(ctx, P, C0max);
+  const int ev_evo1 = ctx.mark();
 
   // projection of non-landmarks and result matrix
   int* d_res = ctx.alloc<int>(static_cast<size_t>(M) * n);
@@ -461,11 +493,17 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     a.res = d_res;
     ck_launch(kgb::project_labels(a, st), "projection");
   }
+  const int ev_proj = ctx.mark();
   ctx.sync();
   out->timings[4] = clk.lap();
 
   // outputs
-  ctx.download(out->res, d_res, static_cast<size_t>(M) * n);
+  if (out->res_on_device) {
+    ck(cudaMemcpyAsync(out->res, d_res, sizeof(int) * static_cast<size_t>(M) * n, cudaMemcpyDeviceToDevice, st),
+       "D2D");
+  } else {
+    ctx.download(out->res, d_res, static_cast<size_t>(M) * n);
+  }
   std::vector<double> best(static_cast<size_t>(M) * 2);
   ctx.download(best.data(), eb.best, best.size());
   ctx.download(out->v, eb.vect_acc, static_cast<size_t>(M) * T);
@@ -500,8 +538,17 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
       ck_launch(kgb::dissimilarity(a, st), "dissimilarity");
     }
   }
+  const int ev_dis = ctx.mark();
   ctx.sync();
   const double t_dl = clk.lap();
+  out->kernel_ms[0] = ctx.ms(ev_start, ev_graph);
+  out->kernel_ms[1] = ctx.ms(ev_graph, ev_atlas);
+  out->kernel_ms[2] = ctx.ms(ev_atlas, ev_init);
+  out->kernel_ms[3] = ctx.ms(ev_init, ev_tables);
+  out->kernel_ms[4] = ctx.ms(ev_evo0, ev_evo1);
+  out->kernel_ms[5] = ctx.ms(ev_evo1, ev_proj);
+  out->kernel_ms[6] = ctx.ms(ev_proj, ev_dis);
+  out->kernel_ms[7] = ctx.ms(ev_start, ev_dis);
   if (want_graph) {
     std::vector<int> gi(static_cast<size_t>(n) * K);
     std::vector<float> gd(static_cast<size_t>(n) * K);
@@ -560,6 +607,56 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   out->effective_landmarks = L;
 }
 
+// Shared body of the KODAMA.matrix entry points: x on the host (copied in) or
+// already on the device; a caller graph (normalised like
+// normalize_external_graph) or the exact graph built on the device.
+void matrix_entry(const float* x, bool x_on_device, int n, int d, const int32_t* gidx, const float* gdist, int gk,
+                  int index_base, const kgb_matrix_options* opt, kgb_matrix_result* out) {
+  if (x == nullptr || out == nullptr) fail(KGB_EINVAL, "null pointer");
+  if (n < 3) fail(KGB_EINVAL, "KODAMAMatrix requires at least 3 rows.");
+  if (d < 1) fail(KGB_EINVAL, "Input matrix must have at least one column.");
+  validate_matrix_options(opt);
+  if (out->res == nullptr || out->acc == nullptr || out->v == nullptr) fail(KGB_EINVAL, "null result buffer");
+  Clock total, clk;
+  for (double& t : out->timings) t = 0.0;
+  for (double& t : out->kernel_ms) t = 0.0;
+  Ctx ctx(opt->device);
+  int landmarks = opt->landmarks > 0 ? opt->landmarks : 10000;
+  if (landmarks >= n) landmarks = static_cast<int>(std::ceil(static_cast<double>(n) * 0.75));
+  landmarks = std::max(2, std::min(landmarks, n - 1));
+  const int requested = opt->graph_neighbors > 0 ? opt->graph_neighbors : 100;
+  const int neighbors = std::max(1, static_cast<int>(std::floor(std::min(
+      {static_cast<double>(landmarks), static_cast<double>(n) * 0.75 - 1.0, static_cast<double>(requested)}))));
+  const int ev_start = ctx.mark();
+  const float* d_x = x_on_device ? x : ctx.upload(x, static_cast<size_t>(n) * d);
+  int K;
+  int* d_gidx;
+  float* d_gdist;
+  if (gidx != nullptr) {
+    K = std::max(1, std::min(gk, neighbors));
+    const int* d_in_idx = ctx.upload(gidx, static_cast<size_t>(n) * gk);
+    const float* d_in_dist = ctx.upload(gdist, static_cast<size_t>(n) * gk);
+    int* d_mm = ctx.alloc<int>(2);
+    ck_launch(kgb::graph_minmax(d_in_idx, static_cast<size_t>(n) * gk, d_mm, ctx.stream()), "graph min/max");
+    d_gidx = ctx.alloc<int>(static_cast<size_t>(n) * K);
+    d_gdist = ctx.alloc<float>(static_cast<size_t>(n) * K);
+    ck_launch(kgb::normalize_external(d_in_idx, d_in_dist, n, gk, K, index_base, d_mm, d_gidx, d_gdist,
+                                      ctx.stream()), "graph normalisation");
+  } else {
+    K = neighbors;
+    d_gidx = ctx.alloc<int>(static_cast<size_t>(n) * K);
+    d_gdist = ctx.alloc<float>(static_cast<size_t>(n) * K);
+    const int segments = 4;
+    void* scratch = ctx.alloc<unsigned char>(kgb::knn_bruteforce_scratch(n, K, segments));
+    ck_launch(kgb::knn_bruteforce(d_x, n, d, K, segments, scratch, d_gidx, d_gdist, ctx.stream()), "kNN graph");
+  }
+  const int ev_graph = ctx.mark();
+  ctx.sync();
+  out->timings[1] = clk.lap();
+  matrix_from_device_graph(ctx, d_x, n, d, d_gidx, d_gdist, K, opt, out, clk, ev_start, ev_graph);
+  out->timings[0] = total.lap();
+}
+
 }  // namespace
 
 extern "C" {
@@ -578,66 +675,22 @@ int kgb_kodama_matrix_from_graph_data(const float* x, int32_t n, int32_t d, cons
                                       const float* gdist, int32_t gk, int32_t index_base,
                                       const kgb_matrix_options* opt, kgb_matrix_result* out) {
   return guarded([&]() {
-    if (x == nullptr || gidx == nullptr || gdist == nullptr || out == nullptr) fail(KGB_EINVAL, "null pointer");
-    if (n < 3) fail(KGB_EINVAL, "KODAMAMatrix requires at least 3 rows.");
-    if (d < 1) fail(KGB_EINVAL, "Input matrix must have at least one column.");
+    if (gidx == nullptr || gdist == nullptr) fail(KGB_EINVAL, "null graph pointer");
     if (gk <= 0) fail(KGB_EINVAL, "NeighborGraph.neighbors must be positive.");
-    validate_matrix_options(opt);
-    if (out->res == nullptr || out->acc == nullptr || out->v == nullptr) fail(KGB_EINVAL, "null result buffer");
-    Clock total, clk;
-    for (double& t : out->timings) t = 0.0;
-    Ctx ctx(opt->device);
-    int landmarks = opt->landmarks > 0 ? opt->landmarks : 10000;
-    if (landmarks >= n) landmarks = static_cast<int>(std::ceil(static_cast<double>(n) * 0.75));
-    landmarks = std::max(2, std::min(landmarks, n - 1));
-    const int requested = opt->graph_neighbors > 0 ? opt->graph_neighbors : 100;
-    const int neighbors = std::max(1, static_cast<int>(std::floor(std::min(
-        {static_cast<double>(landmarks), static_cast<double>(n) * 0.75 - 1.0, static_cast<double>(requested)}))));
-    const int K = std::max(1, std::min(gk, neighbors));
-    const float* d_x = ctx.upload(x, static_cast<size_t>(n) * d);
-    const int* d_in_idx = ctx.upload(gidx, static_cast<size_t>(n) * gk);
-    const float* d_in_dist = ctx.upload(gdist, static_cast<size_t>(n) * gk);
-    int* d_mm = ctx.alloc<int>(2);
-    ck_launch(kgb::graph_minmax(d_in_idx, static_cast<size_t>(n) * gk, d_mm, ctx.stream()), "graph min/max");
-    int* d_gidx = ctx.alloc<int>(static_cast<size_t>(n) * K);
-    float* d_gdist = ctx.alloc<float>(static_cast<size_t>(n) * K);
-    ck_launch(kgb::normalize_external(d_in_idx, d_in_dist, n, gk, K, index_base, d_mm, d_gidx, d_gdist,
-                                      ctx.stream()), "graph normalisation");
-    ctx.sync();
-    out->timings[1] = clk.lap();
-    matrix_from_device_graph(ctx, d_x, n, d, d_gidx, d_gdist, K, opt, out, clk);
-    out->timings[0] = total.lap();
+    matrix_entry(x, false, n, d, gidx, gdist, gk, index_base, opt, out);
   });
 }
 
 int kgb_kodama_matrix(const float* x, int32_t n, int32_t d, const kgb_matrix_options* opt, kgb_matrix_result* out) {
-  return guarded([&]() {
-    if (x == nullptr || out == nullptr) fail(KGB_EINVAL, "null pointer");
-    if (n < 3) fail(KGB_EINVAL, "KODAMAMatrix requires at least 3 rows.");
-    if (d < 1) fail(KGB_EINVAL, "Input matrix must have at least one column.");
-    validate_matrix_options(opt);
-    if (out->res == nullptr || out->acc == nullptr || out->v == nullptr) fail(KGB_EINVAL, "null result buffer");
-    Clock total, clk;
-    for (double& t : out->timings) t = 0.0;
-    Ctx ctx(opt->device);
-    int landmarks = opt->landmarks > 0 ? opt->landmarks : 10000;
-    if (landmarks >= n) landmarks = static_cast<int>(std::ceil(static_cast<double>(n) * 0.75));
-    landmarks = std::max(2, std::min(landmarks, n - 1));
-    const int requested = opt->graph_neighbors > 0 ? opt->graph_neighbors : 100;
-    const int K = std::max(1, static_cast<int>(std::floor(std::min(
-        {static_cast<double>(landmarks), static_cast<double>(n) * 0.75 - 1.0, static_cast<double>(requested)}))));
-    const float* d_x = ctx.upload(x, static_cast<size_t>(n) * d);
-    int* d_gidx = ctx.alloc<int>(static_cast<size_t>(n) * K);
-    float* d_gdist = ctx.alloc<float>(static_cast<size_t>(n) * K);
-    const int segments = 4;
-    void* scratch = ctx.alloc<unsigned char>(kgb::knn_bruteforce_scratch(n, K, segments));
-    ck_launch(kgb::knn_bruteforce(d_x, n, d, K, segments, scratch, d_gidx, d_gdist, ctx.stream()), "kNN graph");
-    ctx.sync();
-    out->timings[1] = clk.lap();
-    matrix_from_device_graph(ctx, d_x, n, d, d_gidx, d_gdist, K, opt, out, clk);
-    out->timings[0] = total.lap();
-  });
+  return guarded([&]() { matrix_entry(x, false, n, d, nullptr, nullptr, 0, -1, opt, out); });
 }
+
+int kgb_kodama_matrix_resident(const float* x_device, int32_t n, int32_t d, const kgb_matrix_options* opt,
+                               kgb_matrix_result* out) {
+  return guarded([&]() { matrix_entry(x_device, true, n, d, nullptr, nullptr, 0, -1, opt, out); });
+}
+
+int64_t kgb_launch_count(void) { return kgb::g_launches_value(); }
 
 int kgb_core_knn_graph_batch(const int32_t* gidx, const float* gdist, int32_t samples, int32_t gk,
                              int32_t index_base, int32_t problems, const int32_t* labels,

@@ -21,6 +21,7 @@
 // iteration order that fixes the summation order of the diversity term is
 // reproduced (reverse first-insertion order, bucket runs on collisions).
 #include "evolve.cuh"
+#include "launch_count.cuh"
 #include "rng.cuh"
 
 #include <cuda_runtime.h>
@@ -749,6 +750,7 @@ int evolve_launch(const EvolveParams& p, int grid, size_t smem, void* stream) {
                                        static_cast<int>(smem));
   if (e != cudaSuccess) return static_cast<int>(e);
   evolve_kernel<<<grid, kThreads, smem, static_cast<cudaStream_t>(stream)>>>(p);
+  count_launch();
   return static_cast<int>(cudaGetLastError());
 }
 

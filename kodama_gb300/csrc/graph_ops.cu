@@ -16,6 +16,7 @@
 //   dissimilarity: co-label proximity (kodama_matrix.cpp:2685-2776):
 //     d' = (1 + d) / (same/valid)^2 or +inf, row stably sorted by (d', id).
 #include "graph_ops.cuh"
+#include "launch_count.cuh"
 
 #include <cuda_runtime.h>
 #include <math.h>
@@ -254,12 +255,14 @@ int graph_minmax(const int* idx, size_t total, int* mm, cudaStream_t st) {
   cudaMemcpyAsync(mm, init, sizeof(init), cudaMemcpyHostToDevice, st);
   const int blocks = static_cast<int>((total + 255) / 256 < 2048 ? (total + 255) / 256 : 2048);
   minmax_kernel<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(idx, total, mm);
+  count_launch();
   return static_cast<int>(cudaGetLastError());
 }
 
 int normalize_external(const int* in_idx, const float* in_dist, int n, int gk, int K, int base, const int* mm,
                        int* out_idx, float* out_dist, cudaStream_t st) {
   normalize_external_kernel<<<(n + 255) / 256, 256, 0, st>>>(in_idx, in_dist, n, gk, K, base, mm, out_idx, out_dist);
+  count_launch();
   return static_cast<int>(cudaGetLastError());
 }
 
@@ -268,6 +271,7 @@ int normalize_indices(const int* in_idx, const float* in_dist, size_t total, int
   const int blocks = static_cast<int>((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096);
   normalize_indices_kernel<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(in_idx, in_dist, total, samples, base, mm,
                                                                   out_idx, out_dist);
+  count_launch();
   return static_cast<int>(cudaGetLastError());
 }
 
@@ -281,18 +285,21 @@ int build_g2l(const int* land, int problems, int L, int n, int* g2l, cudaStream_
 int build_vote_tables(const VoteTableArgs& a, cudaStream_t st) {
   const size_t total = static_cast<size_t>(a.problems) * a.L;
   vote_table_kernel<<<static_cast<unsigned>((total + 255) / 256), 256, 0, st>>>(a);
+  count_launch();
   return static_cast<int>(cudaGetLastError());
 }
 
 int project_labels(const ProjectArgs& a, cudaStream_t st) {
   const size_t total = static_cast<size_t>(a.problems) * a.n;
   project_kernel<<<static_cast<unsigned>((total + 255) / 256), 256, 0, st>>>(a);
+  count_launch();
   return static_cast<int>(cudaGetLastError());
 }
 
 int transpose_runs(const int* res, int runs, int n, int* out, cudaStream_t st) {
   dim3 grid((n + 31) / 32, (runs + 31) / 32);
   transpose_kernel<<<grid, dim3(32, 8), 0, st>>>(res, runs, n, out);
+  count_launch();
   return static_cast<int>(cudaGetLastError());
 }
 
@@ -302,6 +309,7 @@ int dissimilarity(const DissimArgs& a, cudaStream_t st) {
   if (smem > 48 * 1024) cudaFuncSetAttribute(dissimilarity_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             static_cast<int>(smem));
   dissimilarity_kernel<<<(a.n + wpb - 1) / wpb, wpb * 32, smem, st>>>(a);
+  count_launch();
   return static_cast<int>(cudaGetLastError());
 }
 

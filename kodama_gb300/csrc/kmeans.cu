@@ -14,6 +14,7 @@
 //   max(0, size-1) with mt19937(1234) uniforms (:566-662).
 // Every product and sum uses explicit round-to-nearest intrinsics.
 #include "kmeans.cuh"
+#include "launch_count.cuh"
 
 #include <cuda_runtime.h>
 #include <math.h>
@@ -285,6 +286,7 @@ size_t kmeans_update_smem(int k) { return sizeof(int) * (32 * k + k + k + 1) + s
 
 int kmeans_row_norms(const float* x, int n, int d, float* out, cudaStream_t st) {
   row_norms_kernel<<<(n + 255) / 256, 256, 0, st>>>(x, n, d, out);
+  count_launch();
   return static_cast<int>(cudaGetLastError());
 }
 
@@ -314,6 +316,7 @@ int kmeans_run(const KMeansBatch& B, cudaStream_t st) {
   }
   centroid_norms_kernel<<<ngrid, 128, 0, st>>>(B, 1);
   launch_assign(1);
+  count_launch(1 + 3 * iters + 2);
   return static_cast<int>(cudaGetLastError());
 }
 

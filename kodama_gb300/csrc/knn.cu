@@ -12,6 +12,7 @@
 // tiles and split over `segments` CTAs along grid.y; each thread keeps a
 // sorted top-K list; segment lists are merged by a second kernel.
 #include "knn.cuh"
+#include "launch_count.cuh"
 
 #include <cuda_runtime.h>
 #include <math.h>
@@ -146,6 +147,7 @@ int knn_bruteforce(const float* x, int n, int d, int K, int segments, void* scra
   else if (d <= 64) knn_segment_kernel<4><<<grid, kQ, smem, st>>>(x, n, d, K, seg_len, pd, pi);
   else knn_segment_kernel<0><<<grid, kQ, smem, st>>>(x, n, d, K, seg_len, pd, pi);
   knn_merge_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, K, segments, pd, pi, idx, dist);
+  count_launch(2);
   return static_cast<int>(cudaGetLastError());
 }
 

@@ -27,6 +27,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -941,7 +942,11 @@ struct RunOut {
 void kodama_matrix(const float* x, int n, int d, const int* gidx_in, const float* gdist_in, int gk_in,
                    int index_base, const MatrixOpts& o, uint64_t seed,
                    int* res_out, double* acc_out, double* v_out, uint64_t* hashes_out, int* counters_out,
-                   int* cycle_out, int* knn_idx_out, float* knn_dist_out, int* knn_k_out) {
+                   int* cycle_out, int* knn_idx_out, float* knn_dist_out, int* knn_k_out, double* timings) {
+  const auto t0 = std::chrono::steady_clock::now();
+  auto since = [](std::chrono::steady_clock::time_point a) {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - a).count();
+  };
   if (n < 3) throw std::invalid_argument("KODAMAMatrix requires at least 3 rows.");
   if (o.runs < 1 || o.cycles < 0 || o.folds < 2) throw std::invalid_argument("invalid KODAMA.matrix options");
   if (o.classifier != 0) throw std::invalid_argument("oracle restates the kNN classifier only");
@@ -982,6 +987,8 @@ void kodama_matrix(const float* x, int n, int d, const int* gidx_in, const float
   std::mt19937_64 shared_rng(seed + 1u);
   const std::vector<int> shared = kmeans_labels(x, n, d, coarse_k, shared_rng, 10);
   const Strata strata = index_strata(shared, coarse_k);
+  const double t_atlas = since(t0);
+  const auto t1 = std::chrono::steady_clock::now();
 
   std::vector<RunOut> outs(static_cast<size_t>(o.runs));
   std::atomic<int> next{1};
@@ -1077,6 +1084,7 @@ void kodama_matrix(const float* x, int n, int d, const int* gidx_in, const float
   std::vector<std::thread> pool;
   for (int w = 0; w < workers; ++w) pool.emplace_back(worker);
   for (auto& th : pool) th.join();
+  const double t_runs = since(t1);
 
   for (int r = 0; r < o.runs; ++r) {
     const RunOut& ro = outs[r];
@@ -1094,6 +1102,12 @@ void kodama_matrix(const float* x, int n, int d, const int* gidx_in, const float
       knn_idx_out[i] = gidx[i] >= 0 ? gidx[i] + 1 : gidx[i];
       knn_dist_out[i] = gdist[i];
     }
+  }
+  if (timings) {
+    timings[0] = since(t0);
+    timings[2] = t_runs;
+    timings[4] = t_atlas;
+    timings[5] = timings[0];
   }
 }
 
@@ -1212,9 +1226,10 @@ int orc_kodama_matrix_graph_data(
 ) {
   try {
     orc::MatrixOpts mo{o[0], o[1], o[2], o[3], o[4], o[5], o[6], o[7], o[8], o[9], o[10], o[11]};
-    orc::kodama_matrix(x, n, d, gidx, gdist, gk, index_base, mo, seed, res, acc, v,
-                       reinterpret_cast<uint64_t*>(hashes), run_counters, cycle_diag, out_idx, out_dist, out_k);
     if (timings) for (int i = 0; i < 6; ++i) timings[i] = 0.0;
+    orc::kodama_matrix(x, n, d, gidx, gdist, gk, index_base, mo, seed, res, acc, v,
+                       reinterpret_cast<uint64_t*>(hashes), run_counters, cycle_diag, out_idx, out_dist, out_k,
+                       timings);
     return 0;
   } catch (const std::exception& e) {
     orc::g_error = e.what();
