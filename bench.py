@@ -41,7 +41,7 @@ WORKLOAD = dict(n=20000, d=50, runs=100, cycles=100, graph_neighbors=30, knn_k=3
 CPU_SAMPLE_RUNS = 16
 # DRAM bytes (read + write) of one evolution-kernel launch, scaled from the
 # ncu capture summarised in profiles/evolve_kernel_cfg2.md (None until captured).
-EVOLVE_TRAFFIC_BYTES = None
+EVOLVE_TRAFFIC_BYTES = 280837120
 
 
 def _config(extra=None):
