@@ -84,7 +84,8 @@ typedef struct kgb_matrix_result {
   int32_t knn_k;             /* out: columns written */
   int32_t effective_landmarks; /* out */
   double timings[8];         /* out: host seconds: total, graph, atlas, landmarks+init, evolution+projection,
-                                unused, dissimilarity+outputs, unused */
+                                landmark sampling (part of landmarks+init), dissimilarity+outputs,
+                                label coding (part of landmarks+init) */
   double kernel_ms[8];       /* out: CUDA-event milliseconds on the call's stream: graph build, atlas k-means,
                                 landmark planning + k-means, vote tables, evolution kernel, projection,
                                 dissimilarity, whole device span */

@@ -92,7 +92,7 @@ class MatrixResult:
 
 
 _TIMING_NAMES = ("total", "knn_graph", "shared_landmark_partition", "landmark_initialization",
-                 "core_evolution", "unused", "kodama_dissimilarity", "unused2")
+                 "core_evolution", "landmark_sampling", "kodama_dissimilarity", "label_coding")
 _KERNEL_NAMES = ("knn_graph", "atlas_kmeans", "landmark_kmeans", "vote_tables", "evolution",
                  "projection", "dissimilarity", "device_span")
 

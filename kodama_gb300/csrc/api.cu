@@ -20,6 +20,7 @@
 #include <cmath>
 #include <cstring>
 #include <exception>
+#include <future>
 #include <map>
 #include <stdexcept>
 #include <string>
@@ -261,21 +262,54 @@ EvolveBuffers run_evolution(Ctx& ctx, kgb::EvolveParams P, int C0max) {
   P.best = b.best;
   P.status = b.status;
   P.C0max = C0max;
-  P.trans = (P.absorption && P.pol_transition)
-                ? ctx.alloc<int>(static_cast<size_t>(problems) * C0max * C0max)
-                : ctx.alloc<int>(1);
+  P.trans = ctx.alloc<int>(static_cast<size_t>(problems) * C0max * C0max);
   P.foldcnt = ctx.alloc<int>(static_cast<size_t>(problems) * P.F * C0max);
   const int grid = std::min(problems, ctx.sms());
-  size_t smem = kgb::evolve_smem_bytes(L, C0max, true);
-  P.smem_rows = 1;
-  if (smem > 220 * 1024) {
-    P.smem_rows = 0;
-    smem = kgb::evolve_smem_bytes(L, C0max, false);
-    if (smem > 220 * 1024) fail(KGB_EINVAL, "too many distinct labels for the evolution kernel");
-    const size_t Lp = (static_cast<size_t>(L) + 7) / 8 * 8;
-    P.rows_scratch = ctx.alloc<uint16_t>(static_cast<size_t>(grid) * 5 * Lp);
-  } else {
-    P.rows_scratch = nullptr;
+  constexpr size_t kSmemBudget = 224 * 1024;
+  const size_t Lp = (static_cast<size_t>(L) + 7) / 8 * 8;
+  // prefer (in order): rows, vote histograms, transitions in shared memory
+  bool placed = false;
+  size_t smem = 0;
+  const bool hist_ok = C0max <= 1024;
+  for (int option = 0; option < 6 && !placed; ++option) {
+    const bool rows = option < 3;
+    const bool hist = hist_ok && (option % 3) < 2;
+    const bool trans = (option % 3) == 0;
+    smem = kgb::evolve_smem_bytes(L, C0max, rows, trans, hist);
+    if (smem <= kSmemBudget) {
+      placed = true;
+      P.smem_rows = rows;
+      P.smem_hist = hist;
+      P.smem_trans = trans;
+    }
+  }
+  if (!placed) fail(KGB_EINVAL, "too many distinct labels for the evolution kernel");
+  P.rows_scratch = P.smem_rows ? nullptr
+                               : ctx.alloc<uint16_t>(static_cast<size_t>(grid) * kgb::kEvolveRowArrays * Lp);
+  P.raw_scratch = ctx.alloc<uint64_t>(static_cast<size_t>(grid) * (L / 2 + 64));
+  if (P.smem_trans) P.trans = nullptr;
+  {
+    int* roff = ctx.alloc<int>(static_cast<size_t>(problems) * (L + 1));
+    uint16_t* ridx = ctx.alloc<uint16_t>(static_cast<size_t>(problems) * L * P.w);
+    kgb::ReverseArgs ra{};
+    ra.problems = problems;
+    ra.L = L;
+    ra.w = P.w;
+    ra.nb = P.nb;
+    ra.rev_off = roff;
+    ra.rev_idx = ridx;
+    ck_launch(kgb::build_reverse_tables(ra, ctx.stream()), "reverse tables");
+    P.rev_off = roff;
+    P.rev_idx = ridx;
+  }
+  {
+    std::vector<double> psq(static_cast<size_t>(L) + 1);
+    const double nd = static_cast<double>(L);
+    for (int c = 0; c <= L; ++c) {
+      const double q = static_cast<double>(c) / nd;
+      psq[c] = q * q;
+    }
+    P.psq = ctx.upload(psq.data(), psq.size());
   }
   ck_launch(kgb::evolve_launch(P, grid, smem, ctx.stream()), "evolution kernel launch");
   return b;
@@ -295,7 +329,7 @@ void validate_matrix_options(const kgb_matrix_options* o) {
 // distances finite >= 0) is resident on the device.
 void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_gidx, float* d_gdist, int K,
                               const kgb_matrix_options* o, kgb_matrix_result* out, Clock& clk, int ev_start,
-                              int ev_graph) {
+                              int ev_graph, std::future<std::vector<kgb::FoldPlan>>& folds_future) {
   const kgb_policy pol = policy_is_zero(o->policy) ? default_policy() : o->policy;
   int landmarks = o->landmarks > 0 ? o->landmarks : 10000;
   if (landmarks >= n) landmarks = static_cast<int>(std::ceil(static_cast<double>(n) * 0.75));
@@ -348,24 +382,23 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   ctx.sync();
   out->timings[2] = clk.lap();
 
-  // per-run landmarks, folds and k-means seeds (host, libstdc++ streams)
+  // per-run landmarks and k-means seeds (host, libstdc++ streams)
   const kgb::Strata strata = kgb::index_strata(atlas, coarse_k);
   const int init_k = std::max(2, std::min(splitting, landmarks));
   const int kk = std::max(1, std::min(init_k, landmarks));
   std::vector<kgb::RunPlan> plans(static_cast<size_t>(M));
+  Clock plan_clock;
   parallel_for(M, host_threads(o->host_threads), [&](int r) {
-    plans[r] = kgb::plan_run(strata, landmarks, init_k, F, seed, r + 1);
+    plans[r] = kgb::plan_run(strata, landmarks, init_k, seed, r + 1);
   });
+  out->timings[5] = plan_clock.lap();
   const int L = static_cast<int>(plans[0].landmarks.size());
   std::vector<int> land(static_cast<size_t>(M) * L), init_rows(static_cast<size_t>(M) * kk);
-  std::vector<uint8_t> folds(static_cast<size_t>(M) * L);
   for (int r = 0; r < M; ++r) {
     std::copy(plans[r].landmarks.begin(), plans[r].landmarks.end(), land.begin() + static_cast<size_t>(r) * L);
     std::copy(plans[r].init_rows.begin(), plans[r].init_rows.end(), init_rows.begin() + static_cast<size_t>(r) * kk);
-    std::copy(plans[r].folds.begin(), plans[r].folds.end(), folds.begin() + static_cast<size_t>(r) * L);
   }
   int* d_land = ctx.upload(land.data(), land.size());
-  uint8_t* d_folds = ctx.upload(folds.data(), folds.size());
   int* d_init_labels = ctx.alloc<int>(static_cast<size_t>(M) * L);
   {
     kgb::KMeansBatch B{};
@@ -389,27 +422,38 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     B.labels = d_init_labels;
     ck_launch(kgb::kmeans_run(B, st), "landmark k-means");
   }
-  std::vector<int> init_labels(static_cast<size_t>(M) * L);
-  ctx.download(init_labels.data(), d_init_labels, init_labels.size());
-  ctx.sync();
-
-  // label coding per run (labels 1..init_k, all inside the bucket range)
-  const uint64_t bc = kgb::unordered_bucket_count(static_cast<size_t>(L));
-  std::vector<Coding> codings(static_cast<size_t>(M));
-  parallel_for(M, host_threads(o->host_threads), [&](int r) {
-    codings[r] = code_labels(init_labels.data() + static_cast<size_t>(r) * L, L, bc);
-  });
-  int C0max = F;
-  for (const auto& c : codings) C0max = std::max<int>(C0max, static_cast<int>(c.code2label.size()));
-  std::vector<uint16_t> codes(static_cast<size_t>(M) * L);
-  std::vector<int> c2l(static_cast<size_t>(M) * C0max, 0), ncodes(static_cast<size_t>(M));
-  std::vector<uint8_t> nocol(static_cast<size_t>(M));
+  // folds were planned on the host while the device worked
+  const std::vector<kgb::FoldPlan> fold_plans = folds_future.get();
+  std::vector<uint8_t> folds(static_cast<size_t>(M) * L);
   for (int r = 0; r < M; ++r) {
-    std::copy(codings[r].codes.begin(), codings[r].codes.end(), codes.begin() + static_cast<size_t>(r) * L);
-    std::copy(codings[r].code2label.begin(), codings[r].code2label.end(), c2l.begin() + static_cast<size_t>(r) * C0max);
-    ncodes[r] = static_cast<int>(codings[r].code2label.size());
-    nocol[r] = codings[r].nocollide ? 1 : 0;
+    std::copy(fold_plans[r].folds.begin(), fold_plans[r].folds.end(), folds.begin() + static_cast<size_t>(r) * L);
   }
+  uint8_t* d_folds = ctx.upload(folds.data(), folds.size());
+  // label coding (labels 1..init_k, all inside the bucket range) and the
+  // initial-label hashes on the device
+  const uint64_t bc = kgb::unordered_bucket_count(static_cast<size_t>(L));
+  const int C0max = std::max(F, kk);
+  uint16_t* d_codes = ctx.alloc<uint16_t>(static_cast<size_t>(M) * L);
+  int* d_c2l = ctx.alloc<int>(static_cast<size_t>(M) * C0max);
+  int* d_ncodes = ctx.alloc<int>(M);
+  uint64_t* d_init_hash = ctx.alloc<uint64_t>(M);
+  {
+    kgb::CodingArgs ca{};
+    ca.problems = M;
+    ca.n = L;
+    ca.k = kk;
+    ca.C0max = C0max;
+    ca.labels = d_init_labels;
+    ca.codes = d_codes;
+    ca.code2label = d_c2l;
+    ca.ncodes = d_ncodes;
+    ck_launch(kgb::code_labels(ca, st), "label coding");
+    ck_launch(kgb::fnv_rows(d_init_labels, M, L, d_init_hash, st), "label hashes");
+  }
+  std::vector<uint64_t> init_hash(static_cast<size_t>(M));
+  ctx.download(init_hash.data(), d_init_hash, init_hash.size());
+  const std::vector<uint8_t> nocol(static_cast<size_t>(M), 1);
+  out->timings[7] = 0.0;
   out->timings[3] = clk.lap();
 
   const int ev_init = ctx.mark();
@@ -463,9 +507,9 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   P.bucket_count = bc;
   P.nb = d_nb;
   P.sc = d_sc;
-  P.init = ctx.upload(codes.data(), codes.size());
-  P.code2label = ctx.upload(c2l.data(), c2l.size());
-  P.ncodes = ctx.upload(ncodes.data(), ncodes.size());
+  P.init = d_codes;
+  P.code2label = d_c2l;
+  P.ncodes = d_ncodes;
   P.nocollide = ctx.upload(nocol.data(), nocol.size());
   P.folds = d_folds;
   P.fixed = nullptr;
@@ -577,8 +621,8 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     out->acc[r] = best[2 * r];
     if (out->run_hashes) {
       out->run_hashes[3 * r + 0] = plans[r].landmark_hash;
-      out->run_hashes[3 * r + 1] = kgb::fnv_hash(init_labels.data() + static_cast<size_t>(r) * L, L);
-      out->run_hashes[3 * r + 2] = plans[r].fold_hash;
+      out->run_hashes[3 * r + 1] = init_hash[r];
+      out->run_hashes[3 * r + 2] = fold_plans[r].fold_hash;
     }
     if (out->run_counters) {
       const int* c = counters.data() + static_cast<size_t>(r) * 16;
@@ -627,6 +671,14 @@ void matrix_entry(const float* x, bool x_on_device, int n, int d, const int32_t*
   const int requested = opt->graph_neighbors > 0 ? opt->graph_neighbors : 100;
   const int neighbors = std::max(1, static_cast<int>(std::floor(std::min(
       {static_cast<double>(landmarks), static_cast<double>(n) * 0.75 - 1.0, static_cast<double>(requested)}))));
+  // fold planning depends only on (seed, run, L): start it on host threads now
+  const int M = opt->runs, F = opt->folds, nthreads = host_threads(opt->host_threads);
+  const uint64_t seed = opt->seed;
+  std::future<std::vector<kgb::FoldPlan>> folds_future = std::async(std::launch::async, [=]() {
+    std::vector<kgb::FoldPlan> plans(static_cast<size_t>(M));
+    parallel_for(M, nthreads, [&](int r) { plans[r] = kgb::plan_folds(landmarks, F, seed, r + 1); });
+    return plans;
+  });
   const int ev_start = ctx.mark();
   const float* d_x = x_on_device ? x : ctx.upload(x, static_cast<size_t>(n) * d);
   int K;
@@ -653,7 +705,7 @@ void matrix_entry(const float* x, bool x_on_device, int n, int d, const int32_t*
   const int ev_graph = ctx.mark();
   ctx.sync();
   out->timings[1] = clk.lap();
-  matrix_from_device_graph(ctx, d_x, n, d, d_gidx, d_gdist, K, opt, out, clk, ev_start, ev_graph);
+  matrix_from_device_graph(ctx, d_x, n, d, d_gidx, d_gdist, K, opt, out, clk, ev_start, ev_graph, folds_future);
   out->timings[0] = total.lap();
 }
 

@@ -35,11 +35,12 @@ namespace {
 constexpr int kThreads = 1024;
 constexpr int kWarps = kThreads / 32;
 constexpr unsigned kFull = 0xffffffffu;
+constexpr int kRowArrays = 8;  // cl, cur, curpred, pred/perm, J, list, 2 x (32-bit scratch)
 
 struct Fixed {
   Mt64State rng;
-  uint16_t jbuf[2 * kMtN];
   int first_reject;
+  int i0;
   int ns;
   int red_i[kWarps];
   int flag;
@@ -60,7 +61,14 @@ struct Smem {
   uint16_t* cur;     // current state (evolutionary) or best state (greedy)
   uint16_t* curpred; // CV predictions of cur
   uint16_t* pred;    // CV predictions of the proposal
-  uint16_t* perm;    // shuffled group ids
+  uint16_t* perm;    // shuffled group ids (first ns positions; aliases pred during the shuffle)
+  uint16_t* jarr;    // swap target of every shuffle step
+  uint16_t* list;    // shuffle steps bucketed by swap target
+  int* scratch32;    // per-position counts / bucket offsets
+  int* trans;        // class x prediction counts (shared or global)
+  unsigned* hist;    // per-warp packed 8-bit vote counters, or nullptr
+  int hist_words;    // words per warp
+  uint64_t* raw;     // engine outputs of one shuffle (global scratch)
   int* cnt;          // per code: count in proposal
   int* firstpos;     // per code: first row
   int* movable;      // per code: non-fixed rows
@@ -93,120 +101,363 @@ __device__ int block_sum(int v, Fixed& f) {
 }
 
 // ---------------------------------------------------------------------------
-// Group shuffle (std::shuffle of iota(G) with a 64-bit engine): for an engine
-// range wider than G^2 the draws come two at a time, one downscaled draw over
-// (i+1)*(i+2) giving the swap targets of positions i and i+1 (quotient and
+// Group shuffle (std::shuffle of iota(G) with a 64-bit engine).  For an engine
+// range wider than G^2 the draws come two at a time: one downscaled draw over
+// (i+1)*(i+2) gives the swap targets of positions i and i+1 (quotient and
 // remainder by i+2); an even G first swaps position 1 with a draw over {0,1}.
-// Positions >= i are untouched before step i, so each swap is "place i at j
-// and move the old occupant of j to i".  Warp 0 computes the targets of up to
-// 312 pairs in parallel from one engine block; lane 0 applies them in order.
+//
+// Only the groups at positions [0, ns) are used, so the permutation is not
+// materialised serially.  Step i (swap of positions i and J[i] <= i) moves
+// group i, which is still at position i, to J[i].  Hence the final occupant of
+// position q is the last step i > q with J[i] == q if there is one; otherwise
+// it is whatever step q pulled into position q, i.e. the occupant of position
+// J[q] just before step q (q itself when J[q] == q; 0 for position 0).  The
+// CTA computes all J[i] in parallel from the engine blocks, buckets the steps
+// by target, and walks each wanted position down this chain.
 // ---------------------------------------------------------------------------
-__device__ void shuffle_groups_warp(Fixed& f, uint16_t* perm, int G, int lane) {
-  int i = 1;
-  if (G >= 2 && (G & 1) == 0) {
-    if (lane == 0) {
-      const int j = static_cast<int>(draw_below_serial(f.rng, 2));
-      const uint16_t t = perm[j];
-      perm[1] = t;
-      perm[j] = 1;
-    }
-    i = 2;
+// Exclusive prefix sum of a[0..n) in place (block-wide).
+__device__ void block_exclusive_scan(int* a, int n, Fixed& f) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int chunk = (n + kThreads - 1) / kThreads;
+  const int b = threadIdx.x * chunk, e = min(n, b + chunk);
+  int local = 0;
+  for (int i = b; i < e; ++i) local += a[i];
+  int incl = local;
+  for (int off = 1; off < 32; off <<= 1) {
+    const int v = __shfl_up_sync(kFull, incl, off);
+    if (lane >= off) incl += v;
   }
-  __syncwarp();
-  while (i < G) {
-    if (f.rng.pos >= kMtN) mt64_refill_warp(f.rng, lane);
-    const int pos = f.rng.pos;
-    const int np = min(kMtN - pos, (G - i) >> 1);
-    if (lane == 0) f.first_reject = np;
-    __syncwarp();
-    for (int p = lane; p < np; p += 32) {
-      const uint64_t b0 = static_cast<uint64_t>(i + 2 * p) + 1ull;
+  if (lane == 31) f.red_i[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    int w = f.red_i[lane];
+    for (int off = 1; off < 32; off <<= 1) {
+      const int v = __shfl_up_sync(kFull, w, off);
+      if (lane >= off) w += v;
+    }
+    f.red_i[lane] = w;  // inclusive warp totals
+  }
+  __syncthreads();
+  int run = (warp > 0 ? f.red_i[warp - 1] : 0) + incl - local;
+  for (int i = b; i < e; ++i) {
+    const int v = a[i];
+    a[i] = run;
+    run += v;
+  }
+  __syncthreads();
+}
+
+// Engine producer group: the first 320 threads (warps 0-9) synchronised by
+// named barrier 1, one state word per thread in each regeneration phase.
+constexpr int kProducerThreads = 320;
+__device__ __forceinline__ void producer_sync() { asm volatile("bar.sync 1, 320;" ::: "memory"); }
+
+__device__ void mt64_refill_group(Mt64State& g, int t) {
+  uint64_t v = 0;
+  if (t < kMtN - kMtM) v = mt64_mix(g.mt[t], g.mt[t + 1], g.mt[t + kMtM]);
+  producer_sync();
+  if (t < kMtN - kMtM) {
+    g.mt[t] = v;
+    g.out[t] = mt64_temper(v);
+  }
+  producer_sync();
+  if (t >= kMtN - kMtM && t < kMtN) {
+    v = t < kMtN - 1 ? mt64_mix(g.mt[t], g.mt[t + 1], g.mt[t - (kMtN - kMtM)])
+                     : mt64_mix(g.mt[kMtN - 1], g.mt[0], g.mt[kMtM - 1]);
+  }
+  producer_sync();
+  if (t >= kMtN - kMtM && t < kMtN) {
+    g.mt[t] = v;
+    g.out[t] = mt64_temper(v);
+  }
+  if (t == 0) g.pos = 0;
+  producer_sync();
+}
+
+// Copy the next `count` engine outputs into raw[start..] (producer group).
+__device__ void produce_outputs_group(Mt64State& g, uint64_t* raw, int start, int count, int t) {
+  int done = 0;
+  while (done < count) {
+    if (g.pos >= kMtN) mt64_refill_group(g, t);
+    const int pos = g.pos;
+    const int take = min(kMtN - pos, count - done);
+    for (int i = t; i < take; i += kProducerThreads) raw[start + done + i] = g.out[pos + i];
+    producer_sync();
+    if (t == 0) g.pos = pos + take;
+    producer_sync();
+    done += take;
+  }
+}
+
+// Swap targets J[i] of every step of the shuffle of G groups.  Warp 0 streams
+// the engine outputs the pair draws consume into `raw`; the whole CTA then
+// downscales them in parallel.  A rejected draw (Lemire resampling, about one
+// in 2^64/G^2) shifts every later pair by one output: the pairs from the
+// rejection on are redone with the next output appended.
+__device__ void shuffle_targets_block(Fixed& f, uint16_t* J, int G, uint64_t* raw) {
+  if (threadIdx.x == 0) {
+    f.i0 = 1;
+    if (G >= 2 && (G & 1) == 0) {
+      J[1] = static_cast<uint16_t>(draw_below_serial(f.rng, 2));
+      f.i0 = 2;
+    }
+  }
+  __syncthreads();
+  const int i0 = f.i0;
+  const int npairs = (G - i0) >> 1;
+  if (npairs <= 0) return;
+  if (threadIdx.x < kProducerThreads) produce_outputs_group(f.rng, raw, 0, npairs, threadIdx.x);
+  __syncthreads();
+  int from = 0, shift = 0;
+  for (;;) {
+    if (threadIdx.x == 0) f.first_reject = npairs;
+    __syncthreads();
+    for (int p = from + threadIdx.x; p < npairs; p += kThreads) {
+      const uint64_t b0 = static_cast<uint64_t>(i0 + 2 * p) + 1ull;
       const uint64_t b1 = b0 + 1ull;
       const uint64_t range = b0 * b1;
-      const uint64_t u = f.rng.out[pos + p];
+      const uint64_t u = raw[p + shift];
       const uint64_t lo = u * range;
-      bool rej = false;
-      if (lo < range) {
-        const uint64_t thr = (0ull - range) % range;
-        rej = lo < thr;
-      }
-      if (rej) {
+      if (lo < range && lo < (0ull - range) % range) {
         atomicMin(&f.first_reject, p);
       } else {
-        const uint64_t x = __umul64hi(u, range);
-        f.jbuf[2 * p] = static_cast<uint16_t>(x / b1);
-        f.jbuf[2 * p + 1] = static_cast<uint16_t>(x % b1);
+        // x < (G-1)*G < 2^32 for G <= 65535: 32-bit quotient and remainder
+        const uint32_t x = static_cast<uint32_t>(__umul64hi(u, range));
+        const uint32_t d1 = static_cast<uint32_t>(b1);
+        const uint32_t qv = x / d1;
+        J[i0 + 2 * p] = static_cast<uint16_t>(qv);
+        J[i0 + 2 * p + 1] = static_cast<uint16_t>(x - qv * d1);
       }
     }
-    __syncwarp();
+    __syncthreads();
     const int r = f.first_reject;
-    if (lane == 0) {
-      for (int p = 0; p < r; ++p) {
-        const int a = i + 2 * p;
-        int j = f.jbuf[2 * p];
-        uint16_t t = perm[j];
-        perm[a] = t;
-        perm[j] = static_cast<uint16_t>(a);
-        j = f.jbuf[2 * p + 1];
-        t = perm[j];
-        perm[a + 1] = t;
-        perm[j] = static_cast<uint16_t>(a + 1);
-      }
-      f.rng.pos = pos + r + (r < np ? 1 : 0);
+    if (r >= npairs) break;
+    // the output at r + shift was rejected: pairs r.. use one output later
+    if (threadIdx.x < kProducerThreads) produce_outputs_group(f.rng, raw, npairs + shift, 1, threadIdx.x);
+    ++shift;
+    from = r;
+    __syncthreads();
+  }
+}
+
+// Bucket the steps by swap target: afterwards cnt[q] is the end of bucket q
+// in `list` and the start of bucket q+1.
+__device__ void bucket_steps_block(const Smem& s, int G) {
+  const uint16_t* J = s.jarr;
+  int* cnt = s.scratch32;
+  uint16_t* list = s.list;
+  for (int q = threadIdx.x; q < G; q += kThreads) cnt[q] = 0;
+  __syncthreads();
+  for (int st = 1 + threadIdx.x; st < G; st += kThreads) atomicAdd(&cnt[J[st]], 1);
+  __syncthreads();
+  block_exclusive_scan(cnt, G, *s.f);
+  for (int st = 1 + threadIdx.x; st < G; st += kThreads) {
+    const int slot = atomicAdd(&cnt[J[st]], 1);
+    list[slot] = static_cast<uint16_t>(st);
+  }
+  __syncthreads();
+}
+
+// Group at final position p: last step > q targeting q, else what step q
+// pulled into q (see above).
+__device__ int occupant_of(const Smem& s, int G, int p) {
+  const uint16_t* J = s.jarr;
+  const int* cnt = s.scratch32;
+  int q = p, t = G - 1;
+  for (;;) {
+    const int b = q > 0 ? cnt[q - 1] : 0, e = cnt[q];
+    int best = -1;
+    for (int k = b; k < e; ++k) {
+      const int st = s.list[k];
+      if (st > q && st <= t && st > best) best = st;
     }
-    i += 2 * r;
-    __syncwarp();
+    if (best >= 0) return best;
+    if (q == 0) return 0;
+    const int jq = J[q];
+    if (jq == q) return q;
+    t = q - 1;
+    q = jq;
+  }
+}
+
+// Final position of group e: it lands on J[e] at step e (group 0 starts at
+// 0), then every later step targeting its position moves it to that step's
+// own position.
+__device__ int final_position_of(const Smem& s, int e) {
+  const int* cnt = s.scratch32;
+  int pos = e == 0 ? 0 : s.jarr[e];
+  int time = e;
+  for (;;) {
+    const int b = pos > 0 ? cnt[pos - 1] : 0, en = cnt[pos];
+    int next = 0x7fffffff;
+    for (int k = b; k < en; ++k) {
+      const int st = s.list[k];
+      if (st > time && st < next) next = st;
+    }
+    if (next == 0x7fffffff) return pos;
+    pos = next;
+    time = next;
   }
 }
 
 // ---------------------------------------------------------------------------
-// Fold vote: one warp per row, one lane per neighbour slot.  Winner: largest
-// count, then largest double score sum (neighbour order), then smallest code.
-// Rows with no out-of-fold neighbour take the majority label of their
-// training folds (ties to the smaller label).
+// Tie-break of a vote among the labels reaching the top count `maxc`
+// (`tied`: one lane per such label).  The larger (less negative) double score
+// sum wins, then the smaller code.  Scores are -(d*d) <= 0; with
+// |s| = mant * 2^ex, if the non-zero magnitudes of the row span at most 24
+// binades every sequential double partial sum of <= 32 of them is exact, so
+// exact integer sums order the tied labels exactly as the reference's double
+// sums do; otherwise the double sums are formed in neighbour order.
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ int vote_tiebreak(int code, unsigned tied, const float* scrow, int w, int lane) {
+  const float my = lane < w ? scrow[lane] : 0.0f;
+  const uint32_t bits = __float_as_uint(my);
+  const uint32_t ef = (bits >> 23) & 0xffu;
+  const uint32_t mant = ef ? ((bits & 0x7fffffu) | 0x800000u) : (bits & 0x7fffffu);
+  const int ex = ef ? static_cast<int>(ef) - 150 : -149;
+  const bool live = code >= 0 && mant != 0u;
+  const bool bad = code >= 0 && ef == 0xffu;
+  const int emin = __reduce_min_sync(kFull, live ? ex : 0x7fffffff);
+  const int emax = __reduce_max_sync(kFull, live ? ex : -0x7fffffff);
+  const bool exact_ok = !__any_sync(kFull, bad) && (emin == 0x7fffffff || emax - emin <= 24);
+  uint32_t p0 = 0, p1 = 0, p2 = 0;
+  if (exact_ok && live) {
+    const uint64_t contrib = static_cast<uint64_t>(mant) << (ex - emin);
+    p0 = static_cast<uint32_t>(contrib & 0x1fffffu);
+    p1 = static_cast<uint32_t>((contrib >> 21) & 0x1fffffu);
+    p2 = static_cast<uint32_t>(contrib >> 42);
+  }
+  uint64_t bmag = ~0ull;
+  double bsum = -INFINITY;
+  int bc = 0x7fffffff;
+  unsigned rem = tied;
+  while (rem) {
+    const int ld = __ffs(rem) - 1;
+    rem &= rem - 1;
+    const int v = __shfl_sync(kFull, code, ld);
+    const bool in = code == v;
+    if (exact_ok) {
+      const uint64_t s0 = __reduce_add_sync(kFull, in ? p0 : 0u);
+      const uint64_t s1 = __reduce_add_sync(kFull, in ? p1 : 0u);
+      const uint64_t s2 = __reduce_add_sync(kFull, in ? p2 : 0u);
+      const uint64_t mag = s0 + (s1 << 21) + (s2 << 42);
+      if (mag < bmag || (mag == bmag && v < bc)) {
+        bmag = mag;
+        bc = v;
+      }
+    } else {
+      const unsigned msk = __ballot_sync(kFull, in);
+      double sum = 0.0;
+      for (int t = 0; t < w; ++t) {
+        const float st = __shfl_sync(kFull, my, t);
+        if ((msk >> t) & 1u) sum = __dadd_rn(sum, static_cast<double>(st));
+      }
+      if (sum > bsum || (sum == bsum && v < bc)) {
+        bsum = sum;
+        bc = v;
+      }
+    }
+  }
+  return bc;
+}
+
+// Fold vote of one row with a per-warp histogram of packed 8-bit counters in
+// shared memory (hist: ceil(C0/4) zeroed words, left zeroed on return).
+__device__ __forceinline__ int vote_row_hist(const uint16_t* lab, uint16_t id, const float* scrow, int w, int lane,
+                                             unsigned* hist) {
+  const int code = id != kNoRow ? static_cast<int>(lab[id]) : -1;
+  if (__ballot_sync(kFull, code >= 0) == 0u) return -1;
+  const int sh = (code & 3) * 8;
+  unsigned old = 0;
+  if (code >= 0) old = atomicAdd(&hist[code >> 2], 1u << sh);
+  __syncwarp();
+  const int cnt = code >= 0 ? static_cast<int>((hist[code >> 2] >> sh) & 0xffu) : 0;
+  const bool first = code >= 0 && ((old >> sh) & 0xffu) == 0u;
+  const int maxc = __reduce_max_sync(kFull, cnt);
+  const bool top = code >= 0 && cnt == maxc;
+  const int bestc = static_cast<int>(__reduce_min_sync(kFull, top ? static_cast<unsigned>(code) : 0xffffffffu));
+  const unsigned tied = __ballot_sync(kFull, top && first);
+  __syncwarp();
+  if (code >= 0) hist[code >> 2] = 0u;
+  __syncwarp();
+  if (__popc(tied) == 1) return bestc;
+  return vote_tiebreak(code, tied, scrow, w, lane);
+}
+
+// ---------------------------------------------------------------------------
+// Fold vote of one row by one warp (lane j holds neighbour slot j).  Winner:
+// largest count, then largest double score sum (neighbour order), then the
+// smallest code.  Returns -1 for a row without valid neighbours.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int vote_row(const uint16_t* lab, uint16_t id, const float* scrow, int w, int lane) {
+  const int code = id != kNoRow ? static_cast<int>(lab[id]) : -1;
+  const unsigned valid = __ballot_sync(kFull, code >= 0);
+  if (valid == 0u) return -1;
+  // pass 1: the distinct labels of the row (warp-uniform loop): the largest
+  // count and the smallest code reaching it; note ties
+  int maxc = 0, bestc = 0x7fffffff, nmax = 0;
+  unsigned rem = valid;
+  while (rem) {
+    const int ld = __ffs(rem) - 1;
+    const int v = __shfl_sync(kFull, code, ld);
+    const unsigned msk = __ballot_sync(kFull, code == v);
+    rem &= ~msk;
+    const int c = __popc(msk);
+    if (c > maxc) {
+      maxc = c;
+      bestc = v;
+      nmax = 1;
+    } else if (c == maxc) {
+      ++nmax;
+      if (v < bestc) bestc = v;
+    }
+  }
+  if (nmax == 1) return bestc;
+  // one lane per label reaching the top count
+  unsigned tied = 0u;
+  rem = valid;
+  while (rem) {
+    const int ld = __ffs(rem) - 1;
+    const int v = __shfl_sync(kFull, code, ld);
+    const unsigned msk = __ballot_sync(kFull, code == v);
+    rem &= ~msk;
+    if (__popc(msk) == maxc) tied |= 1u << ld;
+  }
+  return vote_tiebreak(code, tied, scrow, w, lane);
+}
+
+// Vote rows into `out`: every row (rows == nullptr) or the nrows rows listed
+// in `rows` (the caller has filled the others).  Rows with no out-of-fold
+// neighbour take the majority label of their training folds (ties to the
+// smaller label).  Neighbour ids are fetched 8 rows at a time per warp so the
+// memory latency is paid once per batch; scores only for tied rows.
 __device__ void vote_block(const EvolveParams& P, const Smem& s, int prob, const uint16_t* lab,
-                           uint16_t* out, int C0, bool has_empty) {
+                           uint16_t* out, int C0, bool has_empty, const uint16_t* rows = nullptr,
+                           int nrows = -1) {
   const int L = P.L, w = P.w;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint16_t* nbp = P.nb + static_cast<size_t>(prob) * L * w;
   const float* scp = P.sc + static_cast<size_t>(prob) * L * w;
-  for (int r = warp; r < L; r += kWarps) {
-    const uint16_t id = lane < w ? nbp[static_cast<size_t>(r) * w + lane] : kNoRow;
-    const int code = id != kNoRow ? static_cast<int>(lab[id]) : -1;
-    const unsigned valid = __ballot_sync(kFull, code >= 0);
-    if (valid == 0u) continue;  // empty row, fallback below
-    const unsigned m = __match_any_sync(kFull, code);
-    const int cnt = code >= 0 ? __popc(m) : 0;
-    const int maxc = __reduce_max_sync(kFull, cnt);
-    const bool leader = code >= 0 && cnt == maxc && (__ffs(m) - 1) == lane;
-    const unsigned leaders = __ballot_sync(kFull, leader);
-    int best;
-    if (__popc(leaders) == 1) {
-      best = __shfl_sync(kFull, code, __ffs(leaders) - 1);
-    } else {
-      const float my = lane < w ? scp[static_cast<size_t>(r) * w + lane] : 0.0f;
-      double sum = 0.0;
-      for (int t = 0; t < w; ++t) {
-        const float st = __shfl_sync(kFull, my, t);
-        if (leader && ((m >> t) & 1u)) sum = __dadd_rn(sum, static_cast<double>(st));
-      }
-      double bs = sum;
-      int bc = leader ? code : 0x7fffffff;
-      int bv = leader ? 1 : 0;
-      for (int off = 16; off > 0; off >>= 1) {
-        const double os = __shfl_xor_sync(kFull, bs, off);
-        const int oc = __shfl_xor_sync(kFull, bc, off);
-        const int ov = __shfl_xor_sync(kFull, bv, off);
-        if (ov && (!bv || os > bs || (os == bs && oc < bc))) {
-          bs = os;
-          bc = oc;
-          bv = 1;
-        }
-      }
-      best = bc;
+  const int count = rows ? nrows : L;
+  constexpr int kB = 16;
+  for (int i0 = warp * kB; i0 < count; i0 += kWarps * kB) {
+    uint16_t ids[kB];
+#pragma unroll
+    for (int u = 0; u < kB; ++u) {
+      const int i = i0 + u;
+      const int r = i < count ? (rows ? static_cast<int>(rows[i]) : i) : 0;
+      ids[u] = (i < count && lane < w) ? nbp[static_cast<size_t>(r) * w + lane] : kNoRow;
     }
-    if (lane == 0) out[r] = static_cast<uint16_t>(best);
+#pragma unroll
+    for (int u = 0; u < kB; ++u) {
+      const int i = i0 + u;
+      if (i >= count) break;
+      const int r = rows ? static_cast<int>(rows[i]) : i;
+      const int best = s.hist ? vote_row_hist(lab, ids[u], scp + static_cast<size_t>(r) * w, w, lane,
+                                              s.hist + warp * s.hist_words)
+                              : vote_row(lab, ids[u], scp + static_cast<size_t>(r) * w, w, lane);
+      if (best >= 0 && lane == 0) out[r] = static_cast<uint16_t>(best);
+    }
   }
   if (has_empty) {
     // per-fold training majority (codes in [0, C0))
@@ -223,10 +474,10 @@ __device__ void vote_block(const EvolveParams& P, const Smem& s, int prob, const
     for (int fo_i = threadIdx.x; fo_i < P.F; fo_i += kThreads) {
       int bl = 0, bcount = -1;
       for (int c = 0; c < C0; ++c) {
-        const int count = s.aux[c] - fc[fo_i * P.C0max + c];
-        if (count > bcount) {  // ascending codes: ties keep the smaller label
+        const int cnt = s.aux[c] - fc[fo_i * P.C0max + c];
+        if (cnt > bcount) {  // ascending codes: ties keep the smaller label
           bl = c;
-          bcount = count;
+          bcount = cnt;
         }
       }
       s.order[fo_i] = bl;  // order[] is free here; F <= C0max guaranteed by host
@@ -239,6 +490,47 @@ __device__ void vote_block(const EvolveParams& P, const Smem& s, int prob, const
   __syncthreads();
 }
 
+// Rows whose vote may differ from the current state's: reverse neighbours of
+// the rows whose label changed.  Returns the number listed in s.list, or -1
+// when so many rows changed that a full vote is cheaper.
+__device__ int dirty_rows_block(const EvolveParams& P, const Smem& s, int prob) {
+  Fixed& f = *s.f;
+  const int L = P.L;
+  uint8_t* flag = reinterpret_cast<uint8_t*>(s.scratch32);
+  const int* roff = P.rev_off + static_cast<size_t>(prob) * (L + 1);
+  const uint16_t* ridx = P.rev_idx + static_cast<size_t>(prob) * L * P.w;
+  int changed = 0;
+  for (int r = threadIdx.x; r < L; r += kThreads) {
+    flag[r] = 0;
+    changed += s.cl[r] != s.cur[r];
+  }
+  changed = block_sum(changed, f);
+  // expected dirty rows = changed * mean in-degree; past half of the rows a
+  // full vote is cheaper than gathering the reverse lists
+  if (2ll * changed * roff[L] > static_cast<long long>(L) * L) return -1;
+  for (int r = threadIdx.x; r < L; r += kThreads) {
+    if (s.cl[r] == s.cur[r]) continue;
+    const int b = roff[r], e = roff[r + 1];
+    for (int k = b; k < e; ++k) flag[ridx[k]] = 1;
+  }
+  if (threadIdx.x == 0) f.flag = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  for (int base = threadIdx.x - lane; base < L; base += kThreads) {
+    const int r = base + lane;
+    const bool d = r < L && flag[r];
+    const unsigned bm = __ballot_sync(kFull, d);
+    int slot0 = 0;
+    if (lane == 0 && bm) slot0 = atomicAdd(&f.flag, __popc(bm));
+    slot0 = __shfl_sync(kFull, slot0, 0);
+    if (d) s.list[slot0 + __popc(bm & ((1u << lane) - 1u))] = static_cast<uint16_t>(r);
+  }
+  __syncthreads();
+  const int n = f.flag;
+  __syncthreads();
+  return n;
+}
+
 // Count labels of `lab` per code, first positions and distinct count.
 __device__ int label_census(const EvolveParams& P, const Smem& s, const uint16_t* lab, int C0) {
   for (int c = threadIdx.x; c < C0; c += kThreads) {
@@ -247,8 +539,9 @@ __device__ int label_census(const EvolveParams& P, const Smem& s, const uint16_t
   }
   __syncthreads();
   for (int r = threadIdx.x; r < P.L; r += kThreads) {
-    atomicAdd(&s.cnt[lab[r]], 1);
-    atomicMin(&s.firstpos[lab[r]], r);
+    const int code = lab[r];
+    atomicAdd(&s.cnt[code], 1);
+    atomicMin(&s.firstpos[code], r);
   }
   __syncthreads();
   int local = 0;
@@ -312,12 +605,9 @@ __device__ double objective(const EvolveParams& P, const Smem& s, int prob, doub
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    const double n = static_cast<double>(P.L);
+    // psq[c] = (c/L)*(c/L) rounded as the reference rounds each step
     double same = 0.0;
-    for (int q = 0; q < nc; ++q) {
-      const double p = __ddiv_rn(static_cast<double>(s.cnt[s.order[q]]), n);
-      same = __dadd_rn(same, __dmul_rn(p, p));
-    }
+    for (int q = 0; q < nc; ++q) same = __dadd_rn(same, P.psq[s.cnt[s.order[q]]]);
     const double diff = __dsub_rn(1.0, same);
     const double dlp = (0.0 < diff) ? diff : 0.0;
     s.f->score = __dmul_rn(acc, __dsqrt_rn(dlp));
@@ -332,9 +622,9 @@ __device__ double objective(const EvolveParams& P, const Smem& s, int prob, doub
 // Returns 1 if the labels changed.
 __device__ int absorption_block(const EvolveParams& P, const Smem& s, int prob, const uint16_t* pp, int C0) {
   Fixed& f = *s.f;
-  int* tr = P.trans + static_cast<size_t>(prob) * P.C0max * P.C0max;
+  int* tr = s.trans;
   const int C = P.C0max;
-  for (int i = threadIdx.x; i < C0 * C; i += kThreads) tr[(i / C) * C + (i % C)] = 0;
+  for (int i = threadIdx.x; i < C0 * C; i += kThreads) tr[i] = 0;
   for (int c = threadIdx.x; c < C0; c += kThreads) {
     s.cnt[c] = 0;
     s.movable[c] = 0;
@@ -361,11 +651,24 @@ __device__ int absorption_block(const EvolveParams& P, const Smem& s, int prob, 
     const int stay = row[src];
     int bt = src, bcount = 0, bsize = ssize;
     double bsur = 0.0;
+    // exact surplus x n = cnt*n - ssize*dsize; only the candidates at the
+    // exact maximum can win the double comparison chain below (double
+    // rounding is far below the 1/n spacing of distinct exact surpluses)
+    long long kmax = -0x7fffffffffffffffll;
     for (int dst = 0; dst < C0; ++dst) {
       const int cntd = row[dst];
       if (dst == src || cntd == 0) continue;
       const int dsize = s.cnt[dst];
       if (dsize == 0) continue;
+      const long long kx = static_cast<long long>(cntd) * P.L - static_cast<long long>(ssize) * dsize;
+      if (kx > kmax) kmax = kx;
+    }
+    for (int dst = 0; dst < C0; ++dst) {
+      const int cntd = row[dst];
+      if (dst == src || cntd == 0) continue;
+      const int dsize = s.cnt[dst];
+      if (dsize == 0) continue;
+      if (static_cast<long long>(cntd) * P.L - static_cast<long long>(ssize) * dsize != kmax) continue;
       const double expected = __ddiv_rn(__dmul_rn(static_cast<double>(ssize), static_cast<double>(dsize)), nmax);
       const double sur = __dsub_rn(static_cast<double>(cntd), expected);
       if (sur > bsur || (sur == bsur && cntd > bcount) ||
@@ -552,7 +855,6 @@ __device__ void evolve_problem(const EvolveParams& P, const Smem& s, int prob) {
   for (int cycle = 0; cycle < T; ++cycle) {
     // proposal = current (evolutionary) or best (greedy) state; s.cur holds it
     for (int r = threadIdx.x; r < L; r += kThreads) s.cl[r] = s.cur[r];
-    for (int g = threadIdx.x; g < G; g += kThreads) s.perm[g] = static_cast<uint16_t>(g);
     __syncthreads();
     if (warp == 0) {
       if (lane == 0) {
@@ -573,19 +875,28 @@ __device__ void evolve_problem(const EvolveParams& P, const Smem& s, int prob) {
         f.ns = ns;
       }
       __syncwarp();
-      shuffle_groups_warp(f, s.perm, G, lane);
     }
     __syncthreads();
+    shuffle_targets_block(f, s.jarr, G, s.raw);
     const int ns = f.ns;
-    psize[cycle] = ns;  // every thread writes the same value
-    if (P.singleton && P.pol_guidance) {
-      for (int q = threadIdx.x; q < ns; q += kThreads) {
-        const int row = P.gmem[s.perm[q]];
-        if (P.fixed != nullptr && P.fixed[row] == 1) continue;
-        s.cl[row] = s.curpred[row];
+    if (threadIdx.x == 0) psize[cycle] = ns;
+    if (ns > 0) {
+      bucket_steps_block(s, G);
+      if (P.singleton && P.pol_guidance) {
+        // Each sampled group takes its own CV prediction; only groups whose
+        // prediction differs from their label can change, so walk just those
+        // forward to their final shuffled position.
+        for (int g = threadIdx.x; g < G; g += kThreads) {
+          const int row = P.gmem[g];
+          if (s.curpred[row] == s.cur[row]) continue;
+          if (P.fixed != nullptr && P.fixed[row] == 1) continue;
+          if (final_position_of(s, g) < ns) s.cl[row] = s.curpred[row];
+        }
+      } else {
+        for (int p = threadIdx.x; p < ns; p += kThreads) s.perm[p] = static_cast<uint16_t>(occupant_of(s, G, p));
+        __syncthreads();
+        if (threadIdx.x == 0) relabel_serial(P, s, s.curpred, ns, C0);
       }
-    } else if (threadIdx.x == 0) {
-      relabel_serial(P, s, s.curpred, ns, C0);
     }
     __syncthreads();
 
@@ -596,7 +907,16 @@ __device__ void evolve_problem(const EvolveParams& P, const Smem& s, int prob) {
       absorb_moves += absorbed;
     }
 
-    vote_block(P, s, prob, s.cl, s.pred, C0, has_empty);
+    {
+      const int nd = dirty_rows_block(P, s, prob);
+      if (nd < 0) {
+        vote_block(P, s, prob, s.cl, s.pred, C0, has_empty);
+      } else {
+        for (int r = threadIdx.x; r < L; r += kThreads) s.pred[r] = s.curpred[r];
+        __syncthreads();
+        vote_block(P, s, prob, s.cl, s.pred, C0, has_empty, s.list, nd);
+      }
+    }
     ok = 0;
     for (int r = threadIdx.x; r < L; r += kThreads) ok += s.cl[r] == s.pred[r];
     ok = block_sum(ok, f);
@@ -718,30 +1038,47 @@ __global__ void __launch_bounds__(kThreads, 1) evolve_kernel(EvolveParams P) {
   s.weight = reinterpret_cast<double*>(smem_raw + off); off += align_up(sizeof(double) * C, 16);
   s.cp = reinterpret_cast<double*>(smem_raw + off); off += align_up(sizeof(double) * 2 * C, 16);
   const size_t Lp = align_up(static_cast<size_t>(P.L), 8);
+  s.hist_words = (C + 3) / 4;
+  if (P.smem_hist) {
+    s.hist = reinterpret_cast<unsigned*>(smem_raw + off);
+    off += align_up(sizeof(unsigned) * kWarps * s.hist_words, 16);
+    for (int i = threadIdx.x; i < kWarps * s.hist_words; i += kThreads) s.hist[i] = 0u;
+  } else {
+    s.hist = nullptr;
+  }
+  s.raw = P.raw_scratch + static_cast<size_t>(blockIdx.x) * (P.L / 2 + 64);
+  if (P.smem_trans) {
+    s.trans = reinterpret_cast<int*>(smem_raw + off);
+    off += align_up(sizeof(int) * static_cast<size_t>(C) * C, 16);
+  } else {
+    s.trans = nullptr;
+  }
+  uint16_t* rows = P.smem_rows ? reinterpret_cast<uint16_t*>(smem_raw + off)
+                               : P.rows_scratch + static_cast<size_t>(blockIdx.x) * kRowArrays * Lp;
+  s.cl = rows;
+  s.cur = rows + Lp;
+  s.curpred = rows + 2 * Lp;
+  s.pred = rows + 3 * Lp;
+  s.perm = s.pred;
+  s.jarr = rows + 4 * Lp;
+  s.list = rows + 5 * Lp;
+  s.scratch32 = reinterpret_cast<int*>(rows + 6 * Lp);  // 2 * Lp u16 = Lp ints
   for (int prob = blockIdx.x; prob < P.problems; prob += gridDim.x) {
-    uint16_t* rows;
-    if (P.smem_rows) {
-      rows = reinterpret_cast<uint16_t*>(smem_raw + off);
-    } else {
-      rows = P.rows_scratch + static_cast<size_t>(blockIdx.x) * 5 * Lp;
-    }
-    s.cl = rows;
-    s.cur = rows + Lp;
-    s.curpred = rows + 2 * Lp;
-    s.pred = rows + 3 * Lp;
-    s.perm = rows + 4 * Lp;
+    if (!P.smem_trans) s.trans = P.trans + static_cast<size_t>(prob) * C * C;
     evolve_problem(P, s, prob);
   }
 }
 
 }  // namespace
 
-size_t evolve_smem_bytes(int L, int C0max, bool rows_in_smem) {
+size_t evolve_smem_bytes(int L, int C0max, bool rows_in_smem, bool trans_in_smem, bool hist_in_smem) {
   auto al = [](size_t v) { return (v + 15) / 16 * 16; };
   size_t b = al(sizeof(Fixed));
+  if (hist_in_smem) b += al(sizeof(unsigned) * kWarps * ((C0max + 3) / 4));
   b += 6 * al(sizeof(int) * C0max) + al(sizeof(int) * (C0max + 1));
   b += 2 * al(sizeof(double) * C0max) + al(sizeof(double) * 2 * C0max);
-  if (rows_in_smem) b += 5 * ((static_cast<size_t>(L) + 7) / 8 * 8) * sizeof(uint16_t);
+  if (trans_in_smem) b += al(sizeof(int) * static_cast<size_t>(C0max) * C0max);
+  if (rows_in_smem) b += kRowArrays * ((static_cast<size_t>(L) + 7) / 8 * 8) * sizeof(uint16_t);
   return b;
 }
 

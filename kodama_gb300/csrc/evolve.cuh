@@ -21,7 +21,9 @@ struct EvolveParams {
   int evolutionary, guarded, absorption, adaptive;
   int pol_guidance, pol_adaptive, pol_transition, pol_stochastic, pol_diversity, pol_reject1;
   uint64_t bucket_count;   // libstdc++ bucket count after reserve(L)
-  int smem_rows;           // 1 = label arrays in shared memory
+  int smem_rows;           // 1 = per-row arrays in shared memory
+  int smem_trans;          // 1 = class x prediction counts in shared memory
+  int smem_hist;           // 1 = per-warp vote histograms in shared memory
   // inputs
   const uint16_t* nb;      // problems x L x w local neighbour ids (kNoRow = none)
   const float* sc;         // problems x L x w scores -(d*d)
@@ -34,6 +36,9 @@ struct EvolveParams {
   const int* goff;         // G+1 group offsets
   const int* gmem;         // L group members (rows), ascending within a group
   const uint64_t* seeds;   // problems
+  const double* psq;       // L+1: (c/L)*(c/L) as two rounded double operations
+  const int* rev_off;      // problems x (L+1): reverse neighbour lists of the vote tables
+  const uint16_t* rev_idx; // problems x L x w
   // outputs
   uint16_t* clbest;        // problems x L
   uint16_t* cvpredbest;    // problems x L
@@ -48,10 +53,12 @@ struct EvolveParams {
   // scratch
   int* trans;              // problems x C0max x C0max
   int* foldcnt;            // problems x F x C0max
-  uint16_t* rows_scratch;  // problems x 5 x L (when label arrays do not fit in shared memory)
+  uint16_t* rows_scratch;  // grid x 8 x L (when the per-row arrays do not fit in shared memory)
+  uint64_t* raw_scratch;   // grid x (L/2 + 64) engine outputs of one shuffle
 };
 
-size_t evolve_smem_bytes(int L, int C0max, bool rows_in_smem);
+constexpr int kEvolveRowArrays = 8;
+size_t evolve_smem_bytes(int L, int C0max, bool rows_in_smem, bool trans_in_smem, bool hist_in_smem);
 int evolve_launch(const EvolveParams& p, int grid, size_t smem, void* stream);
 
 }  // namespace kgb

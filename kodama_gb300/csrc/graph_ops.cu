@@ -171,6 +171,85 @@ __global__ void project_kernel(ProjectArgs a) {
   a.res[t] = c2l[code];
 }
 
+// Reverse adjacency of each problem's vote table: rev_idx[rev_off[v] ..
+// rev_off[v+1]) lists the rows r whose table contains v.  One CTA per problem.
+__global__ void reverse_table_kernel(ReverseArgs a) {
+  extern __shared__ int deg[];
+  const int p = blockIdx.x;
+  const uint16_t* nb = a.nb + static_cast<size_t>(p) * a.L * a.w;
+  int* off = a.rev_off + static_cast<size_t>(p) * (a.L + 1);
+  uint16_t* idx = a.rev_idx + static_cast<size_t>(p) * a.L * a.w;
+  for (int v = threadIdx.x; v <= a.L; v += blockDim.x) deg[v] = 0;
+  __syncthreads();
+  const size_t total = static_cast<size_t>(a.L) * a.w;
+  for (size_t e = threadIdx.x; e < total; e += blockDim.x) {
+    const uint16_t v = nb[e];
+    if (v != 0xFFFFu) atomicAdd(&deg[v], 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int run = 0;
+    for (int v = 0; v < a.L; ++v) {
+      const int c = deg[v];
+      deg[v] = run;
+      off[v] = run;
+      run += c;
+    }
+    off[a.L] = run;
+  }
+  __syncthreads();
+  for (size_t e = threadIdx.x; e < total; e += blockDim.x) {
+    const uint16_t v = nb[e];
+    if (v == 0xFFFFu) continue;
+    const int slot = atomicAdd(&deg[v], 1);
+    idx[slot] = static_cast<uint16_t>(e / a.w);
+  }
+}
+
+// Label coding of k-means labels 1..k (one CTA per problem): codes are the
+// ranks of the labels present, code2label the labels in ascending order.
+__global__ void code_labels_kernel(CodingArgs a) {
+  extern __shared__ int cmap[];  // k+1 entries
+  const int p = blockIdx.x;
+  const int* lab = a.labels + static_cast<size_t>(p) * a.n;
+  for (int v = threadIdx.x; v <= a.k; v += blockDim.x) cmap[v] = 0;
+  __syncthreads();
+  for (int r = threadIdx.x; r < a.n; r += blockDim.x) cmap[lab[r]] = 1;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int run = 0;
+    int* c2l = a.code2label + static_cast<size_t>(p) * a.C0max;
+    for (int v = 0; v <= a.k; ++v) {
+      if (cmap[v]) {
+        c2l[run] = v;
+        cmap[v] = run++;
+      }
+    }
+    a.ncodes[p] = run;
+  }
+  __syncthreads();
+  uint16_t* codes = a.codes + static_cast<size_t>(p) * a.n;
+  for (int r = threadIdx.x; r < a.n; r += blockDim.x) codes[r] = static_cast<uint16_t>(cmap[lab[r]]);
+}
+
+// FNV-1a over the little-endian bytes of each row of a rows x n int matrix
+// (hash_integer_vector, kodama_matrix.cpp:1689-1699); one thread per row.
+__global__ void fnv_rows_kernel(const int* __restrict__ data, int rows, int n, uint64_t* __restrict__ out) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= rows) return;
+  const int* v = data + static_cast<size_t>(r) * n;
+  uint64_t h = 1469598103934665603ull;
+  for (int i = 0; i < n; ++i) {
+    const uint32_t b = static_cast<uint32_t>(v[i]);
+#pragma unroll
+    for (int s = 0; s < 32; s += 8) {
+      h ^= static_cast<uint8_t>((b >> s) & 0xffu);
+      h *= 1099511628211ull;
+    }
+  }
+  out[r] = h;
+}
+
 __global__ void transpose_kernel(const int* __restrict__ res, int runs, int n, int* __restrict__ out) {
   __shared__ int tile[32][33];
   const int r0 = blockIdx.y * 32, s0 = blockIdx.x * 32;
@@ -289,9 +368,35 @@ int build_vote_tables(const VoteTableArgs& a, cudaStream_t st) {
   return static_cast<int>(cudaGetLastError());
 }
 
+int build_reverse_tables(const ReverseArgs& a, cudaStream_t st) {
+  const size_t smem = sizeof(int) * (static_cast<size_t>(a.L) + 1);
+  if (smem > 48 * 1024) {
+    cudaFuncSetAttribute(reverse_table_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  }
+  reverse_table_kernel<<<a.problems, 1024, smem, st>>>(a);
+  count_launch();
+  return static_cast<int>(cudaGetLastError());
+}
+
 int project_labels(const ProjectArgs& a, cudaStream_t st) {
   const size_t total = static_cast<size_t>(a.problems) * a.n;
   project_kernel<<<static_cast<unsigned>((total + 255) / 256), 256, 0, st>>>(a);
+  count_launch();
+  return static_cast<int>(cudaGetLastError());
+}
+
+int code_labels(const CodingArgs& a, cudaStream_t st) {
+  const size_t smem = sizeof(int) * (static_cast<size_t>(a.k) + 1);
+  if (smem > 48 * 1024) {
+    cudaFuncSetAttribute(code_labels_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  }
+  code_labels_kernel<<<a.problems, 1024, smem, st>>>(a);
+  count_launch();
+  return static_cast<int>(cudaGetLastError());
+}
+
+int fnv_rows(const int* data, int rows, int n, uint64_t* out, cudaStream_t st) {
+  fnv_rows_kernel<<<(rows + 63) / 64, 64, 0, st>>>(data, rows, n, out);
   count_launch();
   return static_cast<int>(cudaGetLastError());
 }

@@ -20,6 +20,13 @@ struct VoteTableArgs {
   float* sc;              // problems x L x w
 };
 
+struct ReverseArgs {
+  int problems, L, w;
+  const uint16_t* nb;     // problems x L x w
+  int* rev_off;           // problems x (L+1)
+  uint16_t* rev_idx;      // problems x L x w
+};
+
 struct ProjectArgs {
   int problems, L, n, K, pk, C0max;
   const int* gidx;        // n x K zero-based
@@ -27,6 +34,14 @@ struct ProjectArgs {
   const uint16_t* clbest; // problems x L codes
   const int* code2label;  // problems x C0max
   int* res;               // problems x n labels
+};
+
+struct CodingArgs {
+  int problems, n, k, C0max;
+  const int* labels;      // problems x n, values 1..k
+  uint16_t* codes;        // problems x n
+  int* code2label;        // problems x C0max
+  int* ncodes;            // problems
 };
 
 struct DissimArgs {
@@ -46,7 +61,10 @@ int normalize_indices(const int* in_idx, const float* in_dist, size_t total, int
                       int* out_idx, float* out_dist, cudaStream_t st);
 int build_g2l(const int* land, int problems, int L, int n, int* g2l, cudaStream_t st);
 int build_vote_tables(const VoteTableArgs& a, cudaStream_t st);
+int build_reverse_tables(const ReverseArgs& a, cudaStream_t st);
 int project_labels(const ProjectArgs& a, cudaStream_t st);
+int code_labels(const CodingArgs& a, cudaStream_t st);
+int fnv_rows(const int* data, int rows, int n, uint64_t* out, cudaStream_t st);
 int transpose_runs(const int* res, int runs, int n, int* out, cudaStream_t st);
 int dissimilarity(const DissimArgs& a, cudaStream_t st);
 

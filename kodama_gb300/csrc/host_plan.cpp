@@ -199,7 +199,7 @@ std::vector<int> make_folds(const std::vector<int>& labels, const std::vector<in
   return out;
 }
 
-RunPlan plan_run(const Strata& strata, int landmarks, int init_k, int folds, uint64_t seed, int run) {
+RunPlan plan_run(const Strata& strata, int landmarks, int init_k, uint64_t seed, int run) {
   RunPlan p;
   std::mt19937_64 rng(seed + static_cast<uint64_t>(run));
   (void)rng();
@@ -207,7 +207,12 @@ RunPlan plan_run(const Strata& strata, int landmarks, int init_k, int folds, uin
   const int L = static_cast<int>(p.landmarks.size());
   const int k = std::max(1, std::min(init_k, L));
   p.init_rows = permutation_head(L, kmeans_seed_from_draw(rng()), k);
-  // identity constraint 1..L, not stratified: one shuffle of the row order
+  p.landmark_hash = fnv_hash(p.landmarks.data(), p.landmarks.size());
+  return p;
+}
+
+FoldPlan plan_folds(int L, int folds, uint64_t seed, int run) {
+  FoldPlan p;
   std::vector<int> order(static_cast<std::size_t>(L));
   std::iota(order.begin(), order.end(), 0);
   std::mt19937_64 frng(seed + static_cast<uint64_t>(run));
@@ -218,7 +223,6 @@ RunPlan plan_run(const Strata& strata, int landmarks, int init_k, int folds, uin
     fo[order[i]] = static_cast<int>(i % static_cast<std::size_t>(folds));
     p.folds[order[i]] = static_cast<uint8_t>(fo[order[i]]);
   }
-  p.landmark_hash = fnv_hash(p.landmarks.data(), p.landmarks.size());
   p.fold_hash = fnv_hash(fo.data(), fo.size());
   return p;
 }

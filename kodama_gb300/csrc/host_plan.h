@@ -26,12 +26,20 @@ Strata index_strata(const std::vector<int>& labels, int strata);
 struct RunPlan {
   std::vector<int> landmarks;       // sorted global rows, size L
   std::vector<int> init_rows;       // init_k initial centroid rows (indices into landmarks)
-  std::vector<uint8_t> folds;       // L fold ids (identity constraint, not stratified)
   uint64_t landmark_hash = 0;
-  uint64_t fold_hash = 0;
 };
 
-RunPlan plan_run(const Strata& strata, int landmarks, int init_k, int folds, uint64_t seed, int run);
+// Landmarks and initial centroid rows of one run (needs the atlas strata).
+RunPlan plan_run(const Strata& strata, int landmarks, int init_k, uint64_t seed, int run);
+
+// Folds of one run over L landmarks with the identity constraint, not
+// stratified (make_folds, common.cpp:180-189): independent of the data, so
+// they can be planned while the device builds the graph and the atlas.
+struct FoldPlan {
+  std::vector<uint8_t> folds;
+  uint64_t fold_hash = 0;
+};
+FoldPlan plan_folds(int L, int folds, uint64_t seed, int run);
 
 // quota_sample_landmarks (kodama_matrix.cpp:856-944, preserve_strata_order=false).
 std::vector<int> quota_sample(const Strata& st, int target, std::mt19937_64& rng);

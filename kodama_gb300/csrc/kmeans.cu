@@ -79,6 +79,32 @@ __global__ void centroid_norms_kernel(KMeansBatch B, int final_pass) {
       dot_x86([&](int j) { return cent[j]; }, [&](int j) { return cent[j]; }, B.d);
 }
 
+// dot_x86 with the point in registers (NB*16 >= d); every register index is
+// a compile-time constant, predicated on d.
+template <int NB>
+__device__ __forceinline__ float dot_x86_reg(const float (&a)[16 * NB], const float* b, int d) {
+  float p[16];
+#pragma unroll
+  for (int l = 0; l < 16; ++l) p[l] = 0.0f;
+  const int nfull = d >> 4;
+#pragma unroll
+  for (int blk = 0; blk < NB; ++blk) {
+    if (blk < nfull) {
+#pragma unroll
+      for (int l = 0; l < 16; ++l) p[l] = fadd(p[l], fmul(a[16 * blk + l], b[16 * blk + l]));
+    }
+  }
+  float lane[4];
+#pragma unroll
+  for (int l = 0; l < 4; ++l) lane[l] = fadd(fadd(p[l], p[4 + l]), fadd(p[8 + l], p[12 + l]));
+  float sum = fadd(fadd(fadd(lane[0], lane[1]), lane[2]), lane[3]);
+#pragma unroll
+  for (int i = 0; i < 16 * NB; ++i) {
+    if (i >= 16 * nfull && i < d) sum = fadd(sum, fmul(a[i], b[i]));
+  }
+  return sum;
+}
+
 // One thread per row; centroids of the problem staged in shared memory.
 template <int NB>
 __global__ void assign_kernel(KMeansBatch B, int final_pass) {
@@ -94,7 +120,7 @@ __global__ void assign_kernel(KMeansBatch B, int final_pass) {
   const int grow = B.rows ? B.rows[static_cast<size_t>(p) * B.n + r] : r;
   const float* xr = B.x + static_cast<size_t>(grow) * d;
   float pt[NB > 0 ? 16 * NB : 1];
-  if (NB > 0) {
+  if constexpr (NB > 0) {
 #pragma unroll
     for (int j = 0; j < 16 * NB; ++j) pt[j] = j < d ? xr[j] : 0.0f;
   }
@@ -105,8 +131,8 @@ __global__ void assign_kernel(KMeansBatch B, int final_pass) {
   for (int c = 0; c < k; ++c) {
     const float* cc = cs + static_cast<size_t>(c) * d;
     float dt;
-    if (NB > 0) {
-      dt = dot_x86([&](int j) { return pt[j]; }, [&](int j) { return cc[j]; }, d);
+    if constexpr (NB > 0) {
+      dt = dot_x86_reg<NB>(pt, cc, d);
     } else {
       dt = dot_x86([&](int j) { return xr[j]; }, [&](int j) { return cc[j]; }, d);
     }
@@ -213,7 +239,7 @@ __global__ void __launch_bounds__(1024) update_kernel(KMeansBatch B) {
     const unsigned m = __match_any_sync(kFull, c);
     if (c >= 0) {
       const int rank = __popc(m & ((1u << lane) - 1u));
-      mem[whist[warp * k + c] + rank] = r;
+      mem[whist[warp * k + c] + rank] = B.rows ? B.rows[static_cast<size_t>(p) * n + r] : r;
     }
     __syncwarp();
     if (c >= 0 && (__ffs(m) - 1) == lane) whist[warp * k + c] += __popc(m);
@@ -221,18 +247,31 @@ __global__ void __launch_bounds__(1024) update_kernel(KMeansBatch B) {
   }
   __syncthreads();
   float* cent = B.cent + static_cast<size_t>(p) * k * d;
-  for (int i = threadIdx.x; i < k * d; i += blockDim.x) {
-    const int c = i / d, j = i % d;
-    float s = 0.0f;
+  // one warp per cluster, lanes over features; members (global rows, in
+  // ascending row order) are fetched eight at a time so their loads overlap,
+  // and each lane adds its feature in member order
+  constexpr int kPref = 8;
+  for (int c = warp; c < k; c += 32) {
     const int b0 = cbase[c], b1 = cbase[c + 1];
-    for (int q = b0; q < b1; ++q) {
-      const int r = mem[q];
-      const int grow = B.rows ? B.rows[static_cast<size_t>(p) * n + r] : r;
-      s = fadd(s, B.x[static_cast<size_t>(grow) * d + j]);
+    for (int j0 = 0; j0 < d; j0 += 32) {
+      const int j = j0 + lane;
+      float s = 0.0f;
+      for (int q = b0; q < b1; q += kPref) {
+        float v[kPref];
+#pragma unroll
+        for (int t = 0; t < kPref; ++t) {
+          const int qq = q + t;
+          v[t] = (qq < b1 && j < d) ? B.x[static_cast<size_t>(mem[qq]) * d + j] : 0.0f;
+        }
+#pragma unroll
+        for (int t = 0; t < kPref; ++t) {
+          if (q + t < b1) s = fadd(s, v[t]);
+        }
+      }
+      const int cnt = b1 - b0;
+      if (cnt != 0) s = fmul(s, __fdiv_rn(1.0f, static_cast<float>(cnt)));
+      if (j < d) cent[static_cast<size_t>(c) * d + j] = s;
     }
-    const int cnt = b1 - b0;
-    if (cnt != 0) s = fmul(s, __fdiv_rn(1.0f, static_cast<float>(cnt)));
-    cent[i] = s;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
