@@ -65,6 +65,9 @@ typedef struct kgb_matrix_options {
   int32_t metric;            /* 2 = Euclidean (the only metric of the path) */
   int32_t device;            /* CUDA device ordinal */
   int32_t host_threads;      /* host worker threads for per-run set-up, 0 = auto */
+  int32_t first_run;         /* id of the first run (default 1): runs first_run .. first_run+runs-1
+                                use seeds seed+id, so runs can be sharded across devices */
+  int32_t reserved;
   uint64_t seed;             /* default 1234 */
   kgb_policy policy;
 } kgb_matrix_options;

@@ -98,19 +98,20 @@ _KERNEL_NAMES = ("knn_graph", "atlas_kmeans", "landmark_kmeans", "vote_tables", 
 
 
 def _matrix_options(runs, cycles, landmarks, splitting, graph_neighbors, folds, knn_k, seed,
-                    materialize_graph, apply_dissimilarity, device, host_threads, policy):
+                    materialize_graph, apply_dissimilarity, device, host_threads, policy, first_run=1):
     pol = policy if isinstance(policy, EvolutionPolicy) else EvolutionPolicy.from_name(policy or "full")
     return N.MatrixOptions(runs=runs, cycles=cycles, landmarks=landmarks, splitting=splitting,
                            graph_neighbors=graph_neighbors, folds=folds, knn_k=knn_k, classifier=0,
                            components=50, materialize_graph=int(materialize_graph),
                            apply_dissimilarity=int(apply_dissimilarity), metric=2, device=device,
-                           host_threads=host_threads, seed=seed, policy=pol._c())
+                           host_threads=host_threads, first_run=first_run, reserved=0, seed=seed,
+                           policy=pol._c())
 
 
 def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitting=0,
                   graph_neighbors=100, folds=5, knn_k=30, seed=1234, materialize_graph=False,
                   apply_dissimilarity=True, index_base=-1, device=0, host_threads=0,
-                  policy="full", res_out=None) -> MatrixResult:
+                  policy="full", res_out=None, first_run=1) -> MatrixResult:
     """KODAMA.matrix with the kNN classifier on the GPU.
 
     ``graph`` = (indices, distances) of shape (n, K) runs the graph-input path
@@ -134,7 +135,7 @@ def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitt
             raise ValueError("x must be a 2-D matrix")
         n, d = x.shape
     opt = _matrix_options(runs, cycles, landmarks, splitting, graph_neighbors, folds, knn_k, seed,
-                          materialize_graph, apply_dissimilarity, device, host_threads, policy)
+                          materialize_graph, apply_dissimilarity, device, host_threads, policy, first_run)
     res = np.zeros((runs, n), np.int32)
     acc = np.zeros(runs, np.float64)
     v = np.zeros((runs, max(cycles, 0)), np.float64)

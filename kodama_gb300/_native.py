@@ -40,7 +40,7 @@ class MatrixOptions(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int32) for n in (
         "runs", "cycles", "landmarks", "splitting", "graph_neighbors", "folds", "knn_k",
         "classifier", "components", "materialize_graph", "apply_dissimilarity", "metric",
-        "device", "host_threads")] + [("seed", ctypes.c_uint64), ("policy", Policy)]
+        "device", "host_threads", "first_run", "reserved")] + [("seed", ctypes.c_uint64), ("policy", Policy)]
 
 
 class MatrixResult(ctypes.Structure):

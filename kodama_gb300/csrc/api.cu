@@ -84,6 +84,7 @@ class Ctx {
     if (device < 0 || device >= count) fail(KGB_EINVAL, "CUDA device ordinal out of range");
     ck(cudaSetDevice(device), "cudaSetDevice");
     ck(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+    ck(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking), "cudaStreamCreate");
     ck(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, device), "device attribute");
     cudaMemPool_t pool;
     if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
@@ -92,10 +93,19 @@ class Ctx {
     }
   }
   ~Ctx() {
+    cudaStreamSynchronize(side_);  // side-stream work reads buffers freed below
     for (void* p : bufs_) cudaFreeAsync(p, stream_);
     cudaStreamSynchronize(stream_);
     for (int i = 0; i < nev_; ++i) cudaEventDestroy(ev_[i]);
+    cudaStreamDestroy(side_);
     cudaStreamDestroy(stream_);
+  }
+  // side stream for work that overlaps the main stream: fork() makes it wait
+  // for everything queued on the main stream so far.
+  cudaStream_t side() const { return side_; }
+  void fork() {
+    const int e = mark();
+    ck(cudaStreamWaitEvent(side_, ev_[e], 0), "cudaStreamWaitEvent");
   }
   // CUDA events on the call's stream, for per-stage device timings.
   int mark() {
@@ -130,18 +140,48 @@ class Ctx {
   void download(T* host, const T* dev, size_t count) {
     if (count) ck(cudaMemcpyAsync(host, dev, count * sizeof(T), cudaMemcpyDeviceToHost, stream_), "D2H");
   }
-  void sync() { ck(cudaStreamSynchronize(stream_), "stream synchronize"); }
+  void sync() {
+    ck(cudaStreamSynchronize(stream_), "stream synchronize");
+    ck(cudaStreamSynchronize(side_), "stream synchronize");
+  }
   cudaStream_t stream() const { return stream_; }
   int sms() const { return sms_; }
 
  private:
   static constexpr int kMaxEvents = 32;
   cudaStream_t stream_ = nullptr;
+  cudaStream_t side_ = nullptr;
   int sms_ = 1;
   std::vector<void*> bufs_;
   cudaEvent_t ev_[kMaxEvents];
   int nev_ = 0;
 };
+
+// Pinned host staging for large device-to-host results (one buffer per host
+// thread, grown on demand and kept): copying into pageable user memory
+// directly is several times slower than a pinned copy plus a host memcpy.
+class PinnedStage {
+ public:
+  ~PinnedStage() {
+    if (p_) cudaFreeHost(p_);
+  }
+  void* get(size_t bytes) {
+    if (bytes > cap_) {
+      if (p_) cudaFreeHost(p_);
+      p_ = nullptr;
+      cap_ = 0;
+      ck(cudaMallocHost(&p_, bytes), "cudaMallocHost");
+      cap_ = bytes;
+    }
+    return p_;
+  }
+
+ private:
+  void* p_ = nullptr;
+  size_t cap_ = 0;
+};
+
+thread_local PinnedStage g_stage;
 
 struct Clock {
   std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
@@ -370,10 +410,12 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     B.cnorm = ctx.alloc<float>(ck_atlas);
     B.assign = ctx.alloc<int>(n);
     ck(cudaMemsetAsync(B.assign, 0xff, sizeof(int) * n, st), "memset");
-    B.members = ctx.alloc<int>(n);
     B.active = ctx.alloc<int>(1);
     B.changed = ctx.alloc<int>(1);
     B.labels = d_atlas_labels;
+    B.members = ctx.alloc<int>(n);
+    B.offsets = ctx.alloc<int>(ck_atlas + 1);
+    B.fscratch = ctx.alloc<float>(3 * ck_atlas + 1);
     ck_launch(kgb::kmeans_run(B, st), "atlas k-means");
   }
   const int ev_atlas = ctx.mark();
@@ -388,8 +430,9 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   const int kk = std::max(1, std::min(init_k, landmarks));
   std::vector<kgb::RunPlan> plans(static_cast<size_t>(M));
   Clock plan_clock;
+  const int r0 = o->first_run > 0 ? o->first_run : 1;
   parallel_for(M, host_threads(o->host_threads), [&](int r) {
-    plans[r] = kgb::plan_run(strata, landmarks, init_k, seed, r + 1);
+    plans[r] = kgb::plan_run(strata, landmarks, init_k, seed, r0 + r);
   });
   out->timings[5] = plan_clock.lap();
   const int L = static_cast<int>(plans[0].landmarks.size());
@@ -416,10 +459,12 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     B.cnorm = ctx.alloc<float>(static_cast<size_t>(M) * kk);
     B.assign = ctx.alloc<int>(static_cast<size_t>(M) * L);
     ck(cudaMemsetAsync(B.assign, 0xff, sizeof(int) * static_cast<size_t>(M) * L, st), "memset");
-    B.members = ctx.alloc<int>(static_cast<size_t>(M) * L);
     B.active = ctx.alloc<int>(M);
     B.changed = ctx.alloc<int>(M);
     B.labels = d_init_labels;
+    B.members = ctx.alloc<int>(static_cast<size_t>(M) * L);
+    B.offsets = ctx.alloc<int>(static_cast<size_t>(M) * (kk + 1));
+    B.fscratch = ctx.alloc<float>(static_cast<size_t>(M) * (3 * kk + 1));
     ck_launch(kgb::kmeans_run(B, st), "landmark k-means");
   }
   // folds were planned on the host while the device worked
@@ -448,10 +493,13 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     ca.code2label = d_c2l;
     ca.ncodes = d_ncodes;
     ck_launch(kgb::code_labels(ca, st), "label coding");
-    ck_launch(kgb::fnv_rows(d_init_labels, M, L, d_init_hash, st), "label hashes");
+    // the serial FNV hashes overlap the evolution on the side stream
+    ctx.fork();
+    ck_launch(kgb::fnv_rows(d_init_labels, M, L, d_init_hash, ctx.side()), "label hashes");
   }
   std::vector<uint64_t> init_hash(static_cast<size_t>(M));
-  ctx.download(init_hash.data(), d_init_hash, init_hash.size());
+  ck(cudaMemcpyAsync(init_hash.data(), d_init_hash, sizeof(uint64_t) * M, cudaMemcpyDeviceToHost, ctx.side()),
+     "D2H");
   const std::vector<uint8_t> nocol(static_cast<size_t>(M), 1);
   out->timings[7] = 0.0;
   out->timings[3] = clk.lap();
@@ -484,7 +532,7 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   std::vector<int> goff(static_cast<size_t>(L) + 1);
   for (int i = 0; i <= L; ++i) goff[i] = i;
   std::vector<uint64_t> seeds(static_cast<size_t>(M));
-  for (int r = 0; r < M; ++r) seeds[r] = seed + static_cast<uint64_t>(r + 1);
+  for (int r = 0; r < M; ++r) seeds[r] = seed + static_cast<uint64_t>(r0 + r);
 
   kgb::EvolveParams P{};
   P.problems = M;
@@ -542,11 +590,13 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   out->timings[4] = clk.lap();
 
   // outputs
+  const size_t res_bytes = sizeof(int) * static_cast<size_t>(M) * n;
+  void* res_stage = nullptr;
   if (out->res_on_device) {
-    ck(cudaMemcpyAsync(out->res, d_res, sizeof(int) * static_cast<size_t>(M) * n, cudaMemcpyDeviceToDevice, st),
-       "D2D");
+    ck(cudaMemcpyAsync(out->res, d_res, res_bytes, cudaMemcpyDeviceToDevice, st), "D2D");
   } else {
-    ctx.download(out->res, d_res, static_cast<size_t>(M) * n);
+    res_stage = g_stage.get(res_bytes);
+    ck(cudaMemcpyAsync(res_stage, d_res, res_bytes, cudaMemcpyDeviceToHost, st), "D2H");
   }
   std::vector<double> best(static_cast<size_t>(M) * 2);
   ctx.download(best.data(), eb.best, best.size());
@@ -584,6 +634,7 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   }
   const int ev_dis = ctx.mark();
   ctx.sync();
+  if (res_stage != nullptr) std::memcpy(out->res, res_stage, res_bytes);
   const double t_dl = clk.lap();
   out->kernel_ms[0] = ctx.ms(ev_start, ev_graph);
   out->kernel_ms[1] = ctx.ms(ev_graph, ev_atlas);
@@ -627,7 +678,7 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     if (out->run_counters) {
       const int* c = counters.data() + static_cast<size_t>(r) * 16;
       int* rc = out->run_counters + 8 * r;
-      rc[0] = r + 1;
+      rc[0] = r0 + r;
       rc[1] = c[0];
       rc[2] = c[9];
       rc[3] = c[10];
@@ -673,10 +724,11 @@ void matrix_entry(const float* x, bool x_on_device, int n, int d, const int32_t*
       {static_cast<double>(landmarks), static_cast<double>(n) * 0.75 - 1.0, static_cast<double>(requested)}))));
   // fold planning depends only on (seed, run, L): start it on host threads now
   const int M = opt->runs, F = opt->folds, nthreads = host_threads(opt->host_threads);
+  const int first_run = opt->first_run > 0 ? opt->first_run : 1;
   const uint64_t seed = opt->seed;
   std::future<std::vector<kgb::FoldPlan>> folds_future = std::async(std::launch::async, [=]() {
     std::vector<kgb::FoldPlan> plans(static_cast<size_t>(M));
-    parallel_for(M, nthreads, [&](int r) { plans[r] = kgb::plan_folds(landmarks, F, seed, r + 1); });
+    parallel_for(M, nthreads, [&](int r) { plans[r] = kgb::plan_folds(landmarks, F, seed, first_run + r); });
     return plans;
   });
   const int ev_start = ctx.mark();

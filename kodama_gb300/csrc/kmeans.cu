@@ -105,51 +105,140 @@ __device__ __forceinline__ float dot_x86_reg(const float (&a)[16 * NB], const fl
   return sum;
 }
 
-// One thread per row; centroids of the problem staged in shared memory.
+// Two rows per thread; centroids of the problem staged in shared memory with
+// rows padded to a multiple of 4 floats so they are read with 128-bit loads.
+constexpr int kAssignRows = 2;
+
+template <int NB>
+__device__ __forceinline__ void dot2_x86(const float (&a)[kAssignRows][16 * NB], const float (&at)[kAssignRows][16],
+                                         const float* b, int d, int nfull, float (&out)[kAssignRows]) {
+  float p[kAssignRows][16];
+#pragma unroll
+  for (int q = 0; q < kAssignRows; ++q)
+#pragma unroll
+    for (int l = 0; l < 16; ++l) p[q][l] = 0.0f;
+#pragma unroll
+  for (int blk = 0; blk < NB; ++blk) {
+    if (blk < nfull) {
+#pragma unroll
+      for (int l4 = 0; l4 < 4; ++l4) {
+        const float4 c = *reinterpret_cast<const float4*>(b + 16 * blk + 4 * l4);
+        const float cv[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+#pragma unroll
+          for (int q = 0; q < kAssignRows; ++q)
+            p[q][4 * l4 + e] = fadd(p[q][4 * l4 + e], fmul(a[q][16 * blk + 4 * l4 + e], cv[e]));
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < kAssignRows; ++q) {
+    float lane[4];
+#pragma unroll
+    for (int l = 0; l < 4; ++l) lane[l] = fadd(fadd(p[q][l], p[q][4 + l]), fadd(p[q][8 + l], p[q][12 + l]));
+    out[q] = fadd(fadd(fadd(lane[0], lane[1]), lane[2]), lane[3]);
+  }
+  // tail d - 16*nfull < 16 elements, held separately so indices stay static
+  const int tn = d - 16 * nfull;
+  const float* bt = b + 16 * nfull;
+#pragma unroll
+  for (int t = 0; t < 16; ++t) {
+    if (t < tn) {
+      const float bv = bt[t];
+#pragma unroll
+      for (int q = 0; q < kAssignRows; ++q) out[q] = fadd(out[q], fmul(at[q][t], bv));
+    }
+  }
+}
+
 template <int NB>
 __global__ void assign_kernel(KMeansBatch B, int final_pass) {
   extern __shared__ float cs[];
   const int p = blockIdx.y;
   if (!final_pass && !B.active[p]) return;
   const int k = B.k, d = B.d;
+  const int dp = (d + 3) & ~3;
   const float* cent = B.cent + static_cast<size_t>(p) * k * d;
-  for (int i = threadIdx.x; i < k * d; i += blockDim.x) cs[i] = cent[i];
-  __syncthreads();
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= B.n) return;
-  const int grow = B.rows ? B.rows[static_cast<size_t>(p) * B.n + r] : r;
-  const float* xr = B.x + static_cast<size_t>(grow) * d;
-  float pt[NB > 0 ? 16 * NB : 1];
-  if constexpr (NB > 0) {
-#pragma unroll
-    for (int j = 0; j < 16 * NB; ++j) pt[j] = j < d ? xr[j] : 0.0f;
+  float* cn = cs + static_cast<size_t>(k) * dp;  // centroid norms, staged after the centroids
+  for (int i = threadIdx.x; i < k * dp; i += blockDim.x) {
+    const int c = i / dp, j = i % dp;
+    cs[i] = j < d ? cent[static_cast<size_t>(c) * d + j] : 0.0f;
   }
-  const float pn = B.pnorm[grow];
-  const float* cn = B.cnorm + static_cast<size_t>(p) * k;
-  int best = 0;
-  float bestd = INFINITY;
-  for (int c = 0; c < k; ++c) {
-    const float* cc = cs + static_cast<size_t>(c) * d;
-    float dt;
-    if constexpr (NB > 0) {
-      dt = dot_x86_reg<NB>(pt, cc, d);
-    } else {
-      dt = dot_x86([&](int j) { return xr[j]; }, [&](int j) { return cc[j]; }, d);
+  for (int c = threadIdx.x; c < k; c += blockDim.x) cn[c] = B.cnorm[static_cast<size_t>(p) * k + c];
+  __syncthreads();
+  const int r0 = (blockIdx.x * blockDim.x + threadIdx.x) * kAssignRows;
+  if (r0 >= B.n) return;
+  int grow[kAssignRows];
+  bool live[kAssignRows];
+#pragma unroll
+  for (int q = 0; q < kAssignRows; ++q) {
+    live[q] = r0 + q < B.n;
+    const int r = live[q] ? r0 + q : r0;
+    grow[q] = B.rows ? B.rows[static_cast<size_t>(p) * B.n + r] : r;
+  }
+  int best[kAssignRows];
+  float bestd[kAssignRows];
+  float pn[kAssignRows];
+#pragma unroll
+  for (int q = 0; q < kAssignRows; ++q) {
+    best[q] = 0;
+    bestd[q] = INFINITY;
+    pn[q] = B.pnorm[grow[q]];
+  }
+  if constexpr (NB > 0) {
+    const int nfull = d >> 4;
+    float pt[kAssignRows][16 * NB];
+    float ptail[kAssignRows][16];
+#pragma unroll
+    for (int q = 0; q < kAssignRows; ++q) {
+#pragma unroll
+      for (int j = 0; j < 16 * NB; ++j) pt[q][j] = j < 16 * nfull ? B.x[static_cast<size_t>(grow[q]) * d + j] : 0.0f;
+#pragma unroll
+      for (int t = 0; t < 16; ++t) {
+        const int j = 16 * nfull + t;
+        ptail[q][t] = j < d ? B.x[static_cast<size_t>(grow[q]) * d + j] : 0.0f;
+      }
     }
-    const float dist = __fsub_rn(fadd(pn, cn[c]), fmul(2.0f, dt));
-    if (dist < bestd || (dist == bestd && c < best)) {
-      bestd = dist;
-      best = c;
+    for (int c = 0; c < k; ++c) {
+      float dt[kAssignRows];
+      dot2_x86<NB>(pt, ptail, cs + static_cast<size_t>(c) * dp, d, nfull, dt);
+#pragma unroll
+      for (int q = 0; q < kAssignRows; ++q) {
+        const float dist = __fsub_rn(fadd(pn[q], cn[c]), fmul(2.0f, dt[q]));
+        if (dist < bestd[q] || (dist == bestd[q] && c < best[q])) {
+          bestd[q] = dist;
+          best[q] = c;
+        }
+      }
+    }
+  } else {
+    for (int c = 0; c < k; ++c) {
+      const float* cc = cs + static_cast<size_t>(c) * dp;
+#pragma unroll
+      for (int q = 0; q < kAssignRows; ++q) {
+        const float* xr = B.x + static_cast<size_t>(grow[q]) * d;
+        const float dt = dot_x86([&](int j) { return xr[j]; }, [&](int j) { return cc[j]; }, d);
+        const float dist = __fsub_rn(fadd(pn[q], cn[c]), fmul(2.0f, dt));
+        if (dist < bestd[q] || (dist == bestd[q] && c < best[q])) {
+          bestd[q] = dist;
+          best[q] = c;
+        }
+      }
     }
   }
   int* as = B.assign + static_cast<size_t>(p) * B.n;
-  if (final_pass) {
-    B.labels[static_cast<size_t>(p) * B.n + r] = best + 1;
-    return;
-  }
-  if (as[r] != best) {
-    as[r] = best;
-    atomicAdd(&B.changed[p], 1);
+#pragma unroll
+  for (int q = 0; q < kAssignRows; ++q) {
+    if (!live[q]) continue;
+    const int r = r0 + q;
+    if (final_pass) {
+      B.labels[static_cast<size_t>(p) * B.n + r] = best[q] + 1;
+    } else if (as[r] != best[q]) {
+      as[r] = best[q];
+      atomicAdd(&B.changed[p], 1);
+    }
   }
 }
 
@@ -185,22 +274,21 @@ struct Fenwick {
   }
 };
 
-// Update step of one problem per CTA (1024 threads): stable grouping of rows
-// by cluster, row-ordered centroid sums, scaling, empty-cluster splitting.
-__global__ void __launch_bounds__(1024) update_kernel(KMeansBatch B) {
+// Update step, part 1 (one CTA of 1024 threads per problem): stable grouping
+// of the rows by cluster.  Each warp takes a contiguous range of rows, counts
+// its clusters, then places its rows in order at per-(warp, cluster) offsets;
+// members[] holds global row ids grouped by cluster in ascending row order.
+__global__ void __launch_bounds__(1024) sort_kernel(KMeansBatch B) {
   extern __shared__ int sm[];
   const int p = blockIdx.x;
   if (!B.active[p]) return;
-  const int k = B.k, d = B.d, n = B.n;
+  const int k = B.k, n = B.n;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int* whist = sm;              // 32 x k
-  int* csize = sm + 32 * k;     // k
-  int* cbase = csize + k;       // k+1
-  float* ftree = reinterpret_cast<float*>(cbase + k + 1);  // k+1
-  float* fvals = ftree + k + 1;                           // k
-  float* fsize = fvals + k;                               // k
+  int* whist = sm;             // 32 x k
+  int* cbase = whist + 32 * k; // k+1
   const int* as = B.assign + static_cast<size_t>(p) * n;
   int* mem = B.members + static_cast<size_t>(p) * n;
+  int* off = B.offsets + static_cast<size_t>(p) * (k + 1);
   for (int i = threadIdx.x; i < 32 * k; i += blockDim.x) whist[i] = 0;
   __syncthreads();
   const int per = (n + 31) / 32;
@@ -219,109 +307,129 @@ __global__ void __launch_bounds__(1024) update_kernel(KMeansBatch B) {
       whist[w * k + c] = run;
       run += v;
     }
-    csize[c] = run;
+    cbase[c] = run;  // size for now
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     int run = 0;
     for (int c = 0; c < k; ++c) {
+      const int sz = cbase[c];
       cbase[c] = run;
-      run += csize[c];
+      off[c] = run;
+      run += sz;
     }
     cbase[k] = run;
+    off[k] = run;
   }
   __syncthreads();
   for (int i = threadIdx.x; i < 32 * k; i += blockDim.x) whist[i] += cbase[i % k];
   __syncthreads();
+  const int* rows = B.rows ? B.rows + static_cast<size_t>(p) * n : nullptr;
   for (int base = beg; base < end; base += 32) {
     const int r = base + lane;
     const int c = r < end ? as[r] : -1;
     const unsigned m = __match_any_sync(kFull, c);
     if (c >= 0) {
       const int rank = __popc(m & ((1u << lane) - 1u));
-      mem[whist[warp * k + c] + rank] = B.rows ? B.rows[static_cast<size_t>(p) * n + r] : r;
+      mem[whist[warp * k + c] + rank] = rows ? rows[r] : r;
     }
     __syncwarp();
     if (c >= 0 && (__ffs(m) - 1) == lane) whist[warp * k + c] += __popc(m);
     __syncwarp();
   }
-  __syncthreads();
-  float* cent = B.cent + static_cast<size_t>(p) * k * d;
-  // one warp per cluster, lanes over features; members (global rows, in
-  // ascending row order) are fetched eight at a time so their loads overlap,
-  // and each lane adds its feature in member order
+}
+
+// Update step, part 2 (one warp per problem and cluster, lanes over
+// features): centroid sums in ascending row order, scaled by 1/size.
+__global__ void sums_kernel(KMeansBatch B) {
+  const int lane = threadIdx.x & 31;
+  const int gw = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int p = gw / B.k, c = gw % B.k;
+  if (p >= B.problems || !B.active[p]) return;
+  const int d = B.d;
+  const int* mem = B.members + static_cast<size_t>(p) * B.n;
+  const int* off = B.offsets + static_cast<size_t>(p) * (B.k + 1);
+  const int b0 = off[c], b1 = off[c + 1];
+  float* cent = B.cent + (static_cast<size_t>(p) * B.k + c) * d;
   constexpr int kPref = 8;
-  for (int c = warp; c < k; c += 32) {
-    const int b0 = cbase[c], b1 = cbase[c + 1];
-    for (int j0 = 0; j0 < d; j0 += 32) {
-      const int j = j0 + lane;
-      float s = 0.0f;
-      for (int q = b0; q < b1; q += kPref) {
-        float v[kPref];
+  for (int j0 = 0; j0 < d; j0 += 32) {
+    const int j = j0 + lane;
+    float s = 0.0f;
+    for (int q = b0; q < b1; q += kPref) {
+      float v[kPref];
 #pragma unroll
-        for (int t = 0; t < kPref; ++t) {
-          const int qq = q + t;
-          v[t] = (qq < b1 && j < d) ? B.x[static_cast<size_t>(mem[qq]) * d + j] : 0.0f;
-        }
-#pragma unroll
-        for (int t = 0; t < kPref; ++t) {
-          if (q + t < b1) s = fadd(s, v[t]);
-        }
+      for (int t = 0; t < kPref; ++t) {
+        const int qq = q + t;
+        v[t] = (qq < b1 && j < d) ? B.x[static_cast<size_t>(mem[qq]) * d + j] : 0.0f;
       }
-      const int cnt = b1 - b0;
-      if (cnt != 0) s = fmul(s, __fdiv_rn(1.0f, static_cast<float>(cnt)));
-      if (j < d) cent[static_cast<size_t>(c) * d + j] = s;
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    bool any_empty = false;
-    for (int c = 0; c < k; ++c) {
-      fsize[c] = static_cast<float>(csize[c]);
-      any_empty |= csize[c] == 0;
-    }
-    if (any_empty && n > k) {
-      const float eps = 1.0f / 1024.0f;
-      Fenwick fw{ftree, fvals, k};
-      for (int i = 0; i <= k; ++i) ftree[i] = 0.0f;
-      for (int i = 0; i < k; ++i) fvals[i] = 0.0f;
-      for (int c = 0; c < k; ++c) fw.set(c, pos_part(__fsub_rn(fsize[c], 1.0f)));
-      int u = 0;
-      for (int e = 0; e < k; ++e) {
-        if (fsize[e] != 0.0f) continue;
-        const float total = fw.total();
-        int donor = -1;
-        if (total > 0.0f) donor = fw.select(fmul(B.split_uniform[u++], total));
-        if (donor < 0) {
-          donor = 0;
-          for (int c = 1; c < k; ++c) if (fsize[c] > fsize[donor]) donor = c;
-        }
-        float* ec = cent + static_cast<size_t>(e) * d;
-        float* dc = cent + static_cast<size_t>(donor) * d;
-        for (int j = 0; j < d; ++j) ec[j] = dc[j];
-        for (int j = 0; j < d; ++j) {
-          if ((j & 1) == 0) {
-            ec[j] = fmul(ec[j], fadd(1.0f, eps));
-            dc[j] = fmul(dc[j], __fsub_rn(1.0f, eps));
-          } else {
-            ec[j] = fmul(ec[j], __fsub_rn(1.0f, eps));
-            dc[j] = fmul(dc[j], fadd(1.0f, eps));
-          }
-        }
-        fsize[e] = __fdiv_rn(fsize[donor], 2.0f);
-        fsize[donor] = __fsub_rn(fsize[donor], fsize[e]);
-        fw.set(e, pos_part(__fsub_rn(fsize[e], 1.0f)));
-        fw.set(donor, pos_part(__fsub_rn(fsize[donor], 1.0f)));
+#pragma unroll
+      for (int t = 0; t < kPref; ++t) {
+        if (q + t < b1) s = fadd(s, v[t]);
       }
     }
-    if (B.changed[p] == 0) B.active[p] = 0;
-    B.changed[p] = 0;
+    const int cnt = b1 - b0;
+    if (cnt != 0) s = fmul(s, __fdiv_rn(1.0f, static_cast<float>(cnt)));
+    if (j < d) cent[j] = s;
   }
+}
+
+// Update step, part 3 (one thread per problem): empty-cluster splitting and
+// the early-exit flag.
+__global__ void finalize_kernel(KMeansBatch B) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= B.problems || !B.active[p]) return;
+  const int k = B.k, d = B.d, n = B.n;
+  const int* off = B.offsets + static_cast<size_t>(p) * (k + 1);
+  float* cent = B.cent + static_cast<size_t>(p) * k * d;
+  float* fsize = B.fscratch + static_cast<size_t>(p) * (3 * k + 1);
+  float* ftree = fsize + k;
+  float* fvals = ftree + k + 1;
+  bool any_empty = false;
+  for (int c = 0; c < k; ++c) {
+    fsize[c] = static_cast<float>(off[c + 1] - off[c]);
+    any_empty |= off[c + 1] == off[c];
+  }
+  if (any_empty && n > k) {
+    const float eps = 1.0f / 1024.0f;
+    Fenwick fw{ftree, fvals, k};
+    for (int i = 0; i <= k; ++i) ftree[i] = 0.0f;
+    for (int i = 0; i < k; ++i) fvals[i] = 0.0f;
+    for (int c = 0; c < k; ++c) fw.set(c, pos_part(__fsub_rn(fsize[c], 1.0f)));
+    int u = 0;
+    for (int e = 0; e < k; ++e) {
+      if (fsize[e] != 0.0f) continue;
+      const float total = fw.total();
+      int donor = -1;
+      if (total > 0.0f) donor = fw.select(fmul(B.split_uniform[u++], total));
+      if (donor < 0) {
+        donor = 0;
+        for (int c = 1; c < k; ++c) if (fsize[c] > fsize[donor]) donor = c;
+      }
+      float* ec = cent + static_cast<size_t>(e) * d;
+      float* dc = cent + static_cast<size_t>(donor) * d;
+      for (int j = 0; j < d; ++j) ec[j] = dc[j];
+      for (int j = 0; j < d; ++j) {
+        if ((j & 1) == 0) {
+          ec[j] = fmul(ec[j], fadd(1.0f, eps));
+          dc[j] = fmul(dc[j], __fsub_rn(1.0f, eps));
+        } else {
+          ec[j] = fmul(ec[j], __fsub_rn(1.0f, eps));
+          dc[j] = fmul(dc[j], fadd(1.0f, eps));
+        }
+      }
+      fsize[e] = __fdiv_rn(fsize[donor], 2.0f);
+      fsize[donor] = __fsub_rn(fsize[donor], fsize[e]);
+      fw.set(e, pos_part(__fsub_rn(fsize[e], 1.0f)));
+      fw.set(donor, pos_part(__fsub_rn(fsize[donor], 1.0f)));
+    }
+  }
+  if (B.changed[p] == 0) B.active[p] = 0;
+  B.changed[p] = 0;
 }
 
 }  // namespace
 
-size_t kmeans_update_smem(int k) { return sizeof(int) * (32 * k + k + k + 1) + sizeof(float) * (k + 1 + k + k); }
+size_t kmeans_sort_smem(int k) { return sizeof(int) * (33 * static_cast<size_t>(k) + 1); }
 
 int kmeans_row_norms(const float* x, int n, int d, float* out, cudaStream_t st) {
   row_norms_kernel<<<(n + 255) / 256, 256, 0, st>>>(x, n, d, out);
@@ -332,10 +440,12 @@ int kmeans_row_norms(const float* x, int n, int d, float* out, cudaStream_t st) 
 int kmeans_run(const KMeansBatch& B, cudaStream_t st) {
   if (B.problems <= 0) return 0;
   init_centroids_kernel<<<dim3(B.k, B.problems), 64, 0, st>>>(B);
-  const size_t cs_bytes = sizeof(float) * static_cast<size_t>(B.k) * B.d;
-  const size_t up_bytes = kmeans_update_smem(B.k);
-  const dim3 agrid((B.n + 127) / 128, B.problems);
+  const size_t cs_bytes = sizeof(float) * (static_cast<size_t>(B.k) * ((B.d + 3) & ~3) + B.k);
+  const size_t sort_bytes = kmeans_sort_smem(B.k);
+  const dim3 agrid((B.n + 128 * kAssignRows - 1) / (128 * kAssignRows), B.problems);
   const dim3 ngrid((B.k + 127) / 128, B.problems);
+  const int sum_warps = B.problems * B.k;
+  const int sum_blocks = (sum_warps + 7) / 8;
   auto launch_assign = [&](int final_pass) {
     if (B.d <= 16) assign_kernel<1><<<agrid, 128, cs_bytes, st>>>(B, final_pass);
     else if (B.d <= 32) assign_kernel<2><<<agrid, 128, cs_bytes, st>>>(B, final_pass);
@@ -346,16 +456,18 @@ int kmeans_run(const KMeansBatch& B, cudaStream_t st) {
   cudaFuncSetAttribute(assign_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(cs_bytes));
   cudaFuncSetAttribute(assign_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(cs_bytes));
   cudaFuncSetAttribute(assign_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(cs_bytes));
-  cudaFuncSetAttribute(update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(up_bytes));
+  cudaFuncSetAttribute(sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sort_bytes));
   const int iters = B.max_iter > 1 ? B.max_iter : 1;
   for (int it = 0; it < iters; ++it) {
     centroid_norms_kernel<<<ngrid, 128, 0, st>>>(B, 0);
     launch_assign(0);
-    update_kernel<<<B.problems, 1024, up_bytes, st>>>(B);
+    sort_kernel<<<B.problems, 1024, sort_bytes, st>>>(B);
+    sums_kernel<<<sum_blocks, 256, 0, st>>>(B);
+    finalize_kernel<<<(B.problems + 63) / 64, 64, 0, st>>>(B);
   }
   centroid_norms_kernel<<<ngrid, 128, 0, st>>>(B, 1);
   launch_assign(1);
-  count_launch(1 + 3 * iters + 2);
+  count_launch(1 + 5 * iters + 2);
   return static_cast<int>(cudaGetLastError());
 }
 

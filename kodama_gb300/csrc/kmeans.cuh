@@ -20,13 +20,15 @@ struct KMeansBatch {
   float* cent;              // problems x k x d
   float* cnorm;             // problems x k
   int* assign;              // problems x n (must start at -1)
-  int* members;             // problems x n scratch
   int* active;              // problems
   int* changed;             // problems
   int* labels;              // problems x n output, 1-based
+  int* members;             // problems x n scratch: rows grouped by cluster
+  int* offsets;             // problems x (k+1) scratch: cluster offsets in members
+  float* fscratch;          // problems x (3k+1) scratch for empty-cluster splitting
 };
 
-size_t kmeans_update_smem(int k);
+size_t kmeans_sort_smem(int k);
 int kmeans_row_norms(const float* x, int n, int d, float* out, cudaStream_t st);
 int kmeans_run(const KMeansBatch& b, cudaStream_t st);
 

@@ -20,7 +20,7 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 
 OPT_FIELDS = ("runs", "cycles", "landmarks", "splitting", "graph_neighbors", "folds",
-              "knn_k", "threads", "materialize", "classifier", "components", "apply_dissim")
+              "knn_k", "threads", "materialize", "classifier", "components", "apply_dissim", "first_run")
 
 _i32p = np.ctypeslib.ndpointer(np.int32, flags="C")
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C")
@@ -70,7 +70,7 @@ class MatrixResult:
 def matrix_options(**kw) -> np.ndarray:
     defaults = dict(runs=100, cycles=20, landmarks=10000, splitting=0, graph_neighbors=100,
                     folds=5, knn_k=30, threads=1, materialize=0, classifier=0, components=50,
-                    apply_dissim=1)
+                    apply_dissim=1, first_run=1)
     defaults.update(kw)
     return np.array([defaults[f] for f in OPT_FIELDS], dtype=np.int32)
 

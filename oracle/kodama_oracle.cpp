@@ -877,7 +877,7 @@ uint64_t fnv_hash(const std::vector<int>& v) {
 
 struct MatrixOpts {
   int runs, cycles, landmarks, splitting, graph_neighbors, folds, knn_k, threads, materialize,
-      classifier, components, apply_dissim;
+      classifier, components, apply_dissim, first_run;
 };
 
 int majority_of(const std::vector<int>& v) {
@@ -994,9 +994,10 @@ void kodama_matrix(const float* x, int n, int d, const int* gidx_in, const float
   std::atomic<int> next{1};
   auto worker = [&]() {
     for (;;) {
-      const int run = next.fetch_add(1);
-      if (run > o.runs) break;
-      RunOut& ro = outs[static_cast<size_t>(run - 1)];
+      const int slot = next.fetch_add(1);
+      if (slot > o.runs) break;
+      RunOut& ro = outs[static_cast<size_t>(slot - 1)];
+      const int run = slot - 1 + (o.first_run > 0 ? o.first_run : 1);
       std::mt19937_64 rng(seed + static_cast<uint64_t>(run));
       (void)rng();
       const std::vector<int> land = quota_sample(strata, landmarks, rng);
@@ -1150,6 +1151,46 @@ int orc_kmeans(const float* x, int n, int p, int k, unsigned long long rng_seed,
   }
 }
 
+// Self-check of the x87 extended-precision model against the native
+// long double on an x86-64 host (returns the number of mismatches, -1 where
+// long double is not the x87 format).
+int orc_ext80_selftest(int n, unsigned long long seed) {
+#if defined(__x86_64__) && (__LDBL_MANT_DIG__ == 64)
+  std::mt19937_64 g(seed);
+  int bad = 0;
+  auto to_ld = [](Ext80 v) { return v.m == 0 ? 0.0L : std::ldexp(static_cast<long double>(v.m), v.e); };
+  for (int i = 0; i < n; ++i) {
+    const uint64_t t = 1 + g() % 20000, c = 1 + g() % 20000, smp = 1 + g() % 200000;
+    const Ext80 e1 = ext80_div(ext80_from_u64(t * c), ext80_from_u64(smp));
+    const long double l1 = static_cast<long double>(t) * static_cast<long double>(c) / static_cast<long double>(smp);
+    bad += to_ld(e1) != l1;
+    const int base = ext80_floor_int(e1);
+    bad += base != static_cast<int>(std::floor(l1));
+    const Ext80 f1 = ext80_sub(e1, ext80_from_u64(static_cast<uint64_t>(base)));
+    const long double lf = l1 - static_cast<long double>(base);
+    bad += to_ld(f1) != lf;
+    const uint64_t u = g();
+    const Ext80 off = ext80_canonical(u);
+    const long double loff = static_cast<long double>(u) / 18446744073709551616.0L;
+    bad += to_ld(off) != loff;
+    const uint64_t sel = g() % 20000;
+    const Ext80 nx = ext80_add(off, ext80_from_u64(sel));
+    const long double lnx = loff + static_cast<long double>(sel);
+    bad += to_ld(nx) != lnx;
+    const Ext80 cum = ext80_add(f1, ext80_add(off, f1));
+    const long double lcum = lf + (loff + lf);
+    bad += to_ld(cum) != lcum;
+    bad += ext80_lt(nx, cum) != (lnx < lcum);
+    bad += ext80_lt(f1, off) != (lf < loff);
+  }
+  return bad;
+#else
+  (void)n;
+  (void)seed;
+  return -1;
+#endif
+}
+
 int orc_dot_x86(const float* a, const float* b, int n, float* out) {
   *out = orc::dot_x86_order(a, b, n);
   return 0;
@@ -1225,7 +1266,7 @@ int orc_kodama_matrix_graph_data(
   int* cycle_diag, int* out_idx, float* out_dist, int* out_k, double* timings
 ) {
   try {
-    orc::MatrixOpts mo{o[0], o[1], o[2], o[3], o[4], o[5], o[6], o[7], o[8], o[9], o[10], o[11]};
+    orc::MatrixOpts mo{o[0], o[1], o[2], o[3], o[4], o[5], o[6], o[7], o[8], o[9], o[10], o[11], o[12]};
     if (timings) for (int i = 0; i < 6; ++i) timings[i] = 0.0;
     orc::kodama_matrix(x, n, d, gidx, gdist, gk, index_base, mo, seed, res, acc, v,
                        reinterpret_cast<uint64_t*>(hashes), run_counters, cycle_diag, out_idx, out_dist, out_k,

@@ -1,0 +1,87 @@
+"""Generate tests/golden/*.json from the reference's own CPU core.
+
+Runs oracle/_ref/libkodama_ref.so (the reference compiled from its sources by
+oracle/build_ref.sh) on seeded synthetic inputs and records its outputs:
+small arrays in full, large arrays as SHA-256 of their little-endian bytes.
+The neighbour graphs fed to the reference are the canonical exact graphs
+(float32, coordinate order, index tie-break), whose SHA-256 is recorded too.
+
+Usage (where the reference checkout exists):  python tests/golden/make_golden.py
+"""
+
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from kodama_gb300 import datasets  # noqa: E402
+from oracle import oracle, ref  # noqa: E402
+
+
+def sha(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def matrix_case(name, x, K, index_base, **kw):
+    gi, gd = oracle.exact_knn(x, K, threads=8)
+    g_in = gi + 1 if index_base == 1 else gi
+    r = ref.kodama_matrix_graph_data(x, g_in, gd, index_base, threads=8, materialize=1, **kw)
+    return {
+        "kind": "kodama_matrix", "name": name, "K": K, "index_base": index_base, "options": kw,
+        "graph_sha256": sha(gi) + ":" + sha(gd),
+        "acc": r.acc.tolist(), "v_sha256": sha(r.v), "res_sha256": sha(r.res),
+        "hashes": [[int(v) for v in row] for row in r.hashes], "run_counters": r.run_counters.tolist(),
+        "cycle_diag_sha256": sha(r.cycle_diag), "knn_idx_sha256": sha(r.knn_idx),
+        "knn_dist_sha256": sha(r.knn_dist), "res_head": r.res[:, :16].tolist(),
+    }
+
+
+def core_case(name, x, K, labels, **kw):
+    gi, gd = oracle.exact_knn(x, K, threads=8)
+    r = ref.core_knn_graph(gi, gd, labels, index_base=0, **kw)
+    kw_json = {k: (v.tolist() if isinstance(v, np.ndarray) else v) for k, v in kw.items()}
+    return {
+        "kind": "core_knn_graph", "name": name, "K": K, "options": kw_json, "labels_sha256": sha(labels),
+        "graph_sha256": sha(gi) + ":" + sha(gd),
+        "clbest_sha256": sha(r.clbest), "cvpredbest_sha256": sha(r.cvpredbest), "folds_sha256": sha(r.folds),
+        "vect_acc": r.vect_acc.tolist(), "vect_score": r.vect_score.tolist(),
+        "proposal_size": r.proposal_size.tolist(), "active_classes": r.active_classes.tolist(),
+        "flags": r.flags.tolist(), "accbest": r.accbest, "scorebest": r.scorebest,
+        "counters": r.counters.tolist(),
+    }
+
+
+def main():
+    if not ref.available():
+        raise SystemExit("build oracle/_ref first (oracle/build_ref.sh)")
+    if not oracle.available():
+        oracle.build()
+    cases = []
+    xs = datasets.spirals()[0].astype(np.float32)
+    cases.append(matrix_case("spirals_N1000_M20_T20", xs, 50, 1, seed=1234, runs=20, cycles=20,
+                             landmarks=10000, splitting=0, graph_neighbors=50, folds=10, knn_k=10))
+    xg, _ = datasets.gaussian_mixture(n=3000, d=50, seed=21)
+    cases.append(matrix_case("mixture_N3000_d50_M6_T30", xg, 30, 0, seed=7, runs=6, cycles=30,
+                             landmarks=10000, splitting=40, graph_neighbors=30, folds=10, knn_k=30))
+    xc, _ = datasets.gaussian_mixture(n=2000, d=20, seed=5)
+    rng = np.random.default_rng(3)
+    labels = (rng.integers(1, 9, 2000) * 3 - 5).astype(np.int32)
+    cases.append(core_case("core_evolutionary", xc, 40, labels, cycles=25, k=10, folds=7, seed=5, cv_seed=11,
+                           evolutionary=True, guarded=True, absorption=True, stratified=False))
+    cases.append(core_case("core_greedy_stratified", xc, 40, labels, cycles=25, k=10, folds=7, seed=5,
+                           cv_seed=11, evolutionary=False, guarded=False, absorption=False, stratified=True))
+    with open(os.path.join(HERE, "golden.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py", "cases": cases}, f, indent=1)
+    print(f"wrote {len(cases)} cases")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,65 @@
+"""Replay of the cases in tests/golden/golden.json (made from the reference's
+own CPU core by tests/golden/make_golden.py) through any implementation with
+the oracle's calling convention."""
+
+import hashlib
+import json
+import os
+
+import numpy as np
+
+from kodama_gb300 import datasets
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def sha(a) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def cases():
+    with open(os.path.join(HERE, "golden", "golden.json")) as f:
+        return json.load(f)["cases"]
+
+
+def inputs(case):
+    name = case["name"]
+    if name.startswith("spirals"):
+        return datasets.spirals()[0].astype(np.float32)
+    if name.startswith("mixture"):
+        return datasets.gaussian_mixture(n=3000, d=50, seed=21)[0]
+    return datasets.gaussian_mixture(n=2000, d=20, seed=5)[0]
+
+
+def core_labels():
+    rng = np.random.default_rng(3)
+    return (rng.integers(1, 9, 2000) * 3 - 5).astype(np.int32)
+
+
+def check_matrix(case, r):
+    """r: object with res, acc, v, hashes/run_hashes, run_counters, cycle_diag, knn_idx, knn_dist."""
+    hashes = getattr(r, "run_hashes", None)
+    if hashes is None:
+        hashes = r.hashes
+    assert [[int(v) for v in row] for row in hashes] == case["hashes"], "per-run hashes"
+    assert np.asarray(r.run_counters).tolist() == case["run_counters"], "run counters"
+    assert sha(r.cycle_diag) == case["cycle_diag_sha256"], "cycle diagnostics"
+    assert np.asarray(r.acc).tolist() == case["acc"], "accuracies"
+    assert sha(r.v) == case["v_sha256"], "accuracy trace"
+    assert np.asarray(r.res)[:, :16].tolist() == case["res_head"], "label matrix head"
+    assert sha(r.res) == case["res_sha256"], "label matrix"
+    assert sha(r.knn_idx) == case["knn_idx_sha256"], "corrected graph indices"
+    assert sha(r.knn_dist) == case["knn_dist_sha256"], "corrected graph distances"
+
+
+def check_core(case, r, folds_attr="folds"):
+    assert sha(getattr(r, folds_attr)) == case["folds_sha256"], "folds"
+    assert sha(r.clbest) == case["clbest_sha256"], "clbest"
+    assert sha(r.cvpredbest) == case["cvpredbest_sha256"], "cvpredbest"
+    assert np.asarray(r.vect_acc).tolist() == case["vect_acc"], "vect_acc"
+    assert np.asarray(r.vect_score).tolist() == case["vect_score"], "vect_score"
+    assert np.asarray(r.proposal_size).tolist() == case["proposal_size"], "proposal sizes"
+    assert np.asarray(r.active_classes).tolist() == case["active_classes"], "active classes"
+    assert np.asarray(r.flags).tolist() == case["flags"], "accept flags"
+    assert r.accbest == case["accbest"] and r.scorebest == case["scorebest"], "best scalars"
+    assert np.asarray(r.counters).tolist() == case["counters"], "counters"

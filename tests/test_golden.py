@@ -1,0 +1,58 @@
+"""The CPU restatement and the CUDA path against the reference's recorded
+outputs (tests/golden/golden.json)."""
+
+import numpy as np
+import pytest
+
+import golden_util as G
+
+
+def _matrix_args(case):
+    o = dict(case["options"])
+    return o
+
+
+@pytest.mark.parametrize("case", [c for c in G.cases() if c["kind"] == "kodama_matrix"], ids=lambda c: c["name"])
+def test_oracle_matrix_golden(orc, case):
+    x = G.inputs(case)
+    gi, gd = orc.exact_knn(x, case["K"], threads=8)
+    assert G.sha(gi) + ":" + G.sha(gd) == case["graph_sha256"], "canonical exact graph"
+    g_in = gi + 1 if case["index_base"] == 1 else gi
+    r = orc.kodama_matrix_graph_data(x, g_in, gd, case["index_base"], threads=8, materialize=1, **case["options"])
+    G.check_matrix(case, r)
+
+
+@pytest.mark.parametrize("case", [c for c in G.cases() if c["kind"] == "core_knn_graph"], ids=lambda c: c["name"])
+def test_oracle_core_golden(orc, case):
+    x = G.inputs(case)
+    labels = G.core_labels()
+    assert G.sha(labels) == case["labels_sha256"]
+    gi, gd = orc.exact_knn(x, case["K"], threads=8)
+    r = orc.core_knn_graph(gi, gd, labels, index_base=0, **case["options"])
+    G.check_core(case, r)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", [c for c in G.cases() if c["kind"] == "kodama_matrix"], ids=lambda c: c["name"])
+def test_gpu_matrix_golden(kg, case):
+    x = G.inputs(case)
+    o = dict(case["options"])
+    r = kg.KODAMA_matrix(x, materialize_graph=True, **o)
+    gi, gd = kg.knn_graph(x, case["K"])
+    assert G.sha(gi) + ":" + G.sha(gd) == case["graph_sha256"], "device exact graph"
+    G.check_matrix(case, r)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", [c for c in G.cases() if c["kind"] == "core_knn_graph"], ids=lambda c: c["name"])
+def test_gpu_core_golden(kg, case):
+    x = G.inputs(case)
+    labels = G.core_labels()
+    gi, gd = kg.knn_graph(x, case["K"])
+    o = case["options"]
+    out = kg.CoreKNNGraph_batch(gi, gd, labels[None, :], np.array([o["seed"]], np.uint64),
+                                np.array([o["cv_seed"]], np.uint64), cycles=o["cycles"], k=o["k"],
+                                folds=o["folds"], stratified=o["stratified"],
+                                evolutionary_search=o["evolutionary"], guarded_diversity=o["guarded"],
+                                many_to_one_absorption=o["absorption"], index_base=0)
+    G.check_core(case, out[0], folds_attr="fold_assignments")

@@ -127,3 +127,15 @@ def test_dissimilarity_inplace(kg, orc):
     kg.KODAMADissimilarityInPlace(a, b, res)
     assert np.array_equal(a, ri)
     assert np.array_equal(b, rd)
+
+
+def test_matrix_first_run_shard(kg):
+    x = datasets.spirals()[0].astype(np.float32)
+    kw = _matrix_kw(cycles=12)
+    kw.pop("runs")
+    full = kg.KODAMA_matrix(x, runs=6, **kw)
+    part = kg.KODAMA_matrix(x, runs=3, first_run=3, **kw)
+    assert np.array_equal(part.res, full.res[2:5])
+    assert np.array_equal(part.acc, full.acc[2:5])
+    assert np.array_equal(part.run_hashes, full.run_hashes[2:5])
+    assert np.array_equal(part.run_counters, full.run_counters[2:5])
