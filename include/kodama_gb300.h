@@ -182,6 +182,22 @@ int kgb_knn_graph(const float* x, int32_t n, int32_t d, int32_t K, int32_t devic
 int kgb_dissimilarity_inplace(int32_t* gidx, float* gdist, int32_t samples, int32_t gk,
                               const int32_t* res, int32_t runs, int32_t device);
 
+/* The same co-label proximity as kgb_dissimilarity_inplace, on DEVICE
+ * pointers (gidx, gdist: samples x gk one-based graph, rewritten in place;
+ * res: runs x samples labels) and on the caller's `stream` (a cudaStream_t;
+ * NULL = the legacy default stream) of `device`; it returns after that work
+ * has finished.  It allocates no device memory: for callers that cannot call
+ * cudaMalloc/cudaFree, such as a process whose caching allocator already
+ * holds the GPU, or a serving loop where cudaFree would stall the device.
+ * Its scratch is a fixed 16 MiB array inside the library, so
+ * samples * runs <= 4194240 and gk <= 2048; larger inputs return KGB_EINVAL
+ * (use kgb_dissimilarity_inplace).  The first call on each device resolves
+ * that array's address and may load the module; make it before any stream
+ * capture.  Calls that overlap on one device share the scratch and race:
+ * serialise them.  No counterpart in the reference. */
+int kgb_dissimilarity_inplace_device(int32_t* gidx, float* gdist, int32_t samples, int32_t gk,
+                                     const int32_t* res, int32_t runs, int32_t device, void* stream);
+
 /* Number of kernels this library has launched since it was loaded. */
 int64_t kgb_launch_count(void);
 

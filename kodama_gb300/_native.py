@@ -24,6 +24,7 @@ EXPORTED = (
     "kgb_core_knn_graph_batch",
     "kgb_knn_graph",
     "kgb_dissimilarity_inplace",
+    "kgb_dissimilarity_inplace_device",
     "kgb_last_error",
     "kgb_version",
 )
@@ -114,6 +115,7 @@ def load():
                                              ctypes.POINTER(CoreResult)]
     lib.kgb_knn_graph.argtypes = [P, i32, i32, i32, i32, P, P]
     lib.kgb_dissimilarity_inplace.argtypes = [P, P, i32, i32, P, i32, i32]
+    lib.kgb_dissimilarity_inplace_device.argtypes = [P, P, i32, i32, P, i32, i32, P]
     lib.kgb_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     lib.kgb_version.restype = ctypes.c_char_p
     for name in EXPORTED:

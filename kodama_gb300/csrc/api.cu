@@ -763,6 +763,12 @@ void matrix_entry(const float* x, bool x_on_device, int n, int d, const int32_t*
 
 }  // namespace
 
+namespace kgb {
+// Lets entry points defined in other translation units report a message
+// through kgb_last_error().
+void set_last_error(const char* msg) { g_error = msg; }
+}  // namespace kgb
+
 extern "C" {
 
 int kgb_last_error(char* buf, size_t len) {
