@@ -65,6 +65,7 @@ class MatrixResult:
     knn_idx: np.ndarray | None
     knn_dist: np.ndarray | None
     timings: np.ndarray      # runtime, graph, optimisation, dissimilarity, atlas, wall
+    pls_counters: np.ndarray # (runs, 2) int32: PLS coarsening attempted / accepted
 
 
 def matrix_options(**kw) -> np.ndarray:
@@ -83,7 +84,7 @@ def _alloc_matrix(n, opts):
         v=np.zeros(runs * cycles, np.float64), hashes=np.zeros(runs * 3, np.uint64),
         run_counters=np.zeros(runs * 8, np.int32), cycle_diag=np.zeros(runs * cycles * 5, np.int32),
         out_idx=np.zeros(n * k_cap, np.int32), out_dist=np.zeros(n * k_cap, np.float32),
-        out_k=ctypes.c_int(0), timings=np.zeros(6, np.float64))
+        out_k=ctypes.c_int(0), timings=np.zeros(6, np.float64), pls=np.zeros(runs * 2, np.int32))
 
 
 def _wrap(n, opts, b) -> MatrixResult:
@@ -96,7 +97,7 @@ def _wrap(n, opts, b) -> MatrixResult:
         cycle_diag=b["cycle_diag"].reshape(runs, cycles, 5),
         knn_idx=b["out_idx"][: n * k].reshape(n, k).copy() if has_graph else None,
         knn_dist=b["out_dist"][: n * k].reshape(n, k).copy() if has_graph else None,
-        timings=b["timings"])
+        timings=b["timings"], pls_counters=b["pls"].reshape(runs, 2))
 
 
 def kodama_matrix_graph_data(L, x: np.ndarray, gidx: np.ndarray, gdist: np.ndarray,
@@ -115,7 +116,8 @@ def kodama_matrix_graph_data(L, x: np.ndarray, gidx: np.ndarray, gdist: np.ndarr
         opts.ctypes.data_as(ctypes.c_void_p), ctypes.c_ulonglong(seed),
         *[b[f].ctypes.data_as(ctypes.c_void_p) for f in
           ("res", "acc", "v", "hashes", "run_counters", "cycle_diag", "out_idx", "out_dist")],
-        ctypes.byref(b["out_k"]), b["timings"].ctypes.data_as(ctypes.c_void_p))
+        ctypes.byref(b["out_k"]), b["timings"].ctypes.data_as(ctypes.c_void_p),
+        b["pls"].ctypes.data_as(ctypes.c_void_p))
     if rc != 0:
         raise RuntimeError(_err(L))
     return _wrap(n, opts, b)
@@ -133,7 +135,8 @@ def kodama_matrix_raw(L, x: np.ndarray, seed: int = 1234, **kw) -> MatrixResult:
         ctypes.c_ulonglong(seed),
         *[b[f].ctypes.data_as(ctypes.c_void_p) for f in
           ("res", "acc", "v", "hashes", "run_counters", "cycle_diag", "out_idx", "out_dist")],
-        ctypes.byref(b["out_k"]), b["timings"].ctypes.data_as(ctypes.c_void_p))
+        ctypes.byref(b["out_k"]), b["timings"].ctypes.data_as(ctypes.c_void_p),
+        b["pls"].ctypes.data_as(ctypes.c_void_p))
     if rc != 0:
         raise RuntimeError(_err(L))
     return _wrap(n, opts, b)
@@ -151,7 +154,7 @@ class CoreResult:
     flags: np.ndarray        # (cycles, 3): accepted, improving, temperature
     accbest: float
     scorebest: float
-    counters: np.ndarray     # 16 ints
+    counters: np.ndarray     # 16 ints (18 for core_plslda)
 
 
 def core_knn_graph(L, gidx, gdist, labels, *, index_base=-1, constrain=None, fixed=None, cycles=20,
@@ -176,6 +179,43 @@ def core_knn_graph(L, gidx, gdist, labels, *, index_base=-1, constrain=None, fix
         con.ctypes.data_as(ctypes.c_void_p), int(constrain is not None),
         fix.ctypes.data_as(ctypes.c_void_p), int(fixed is not None),
         copts.ctypes.data_as(ctypes.c_void_p), ctypes.c_ulonglong(seed), ctypes.c_ulonglong(cv_seed),
+        *[out[f].ctypes.data_as(ctypes.c_void_p) for f in
+          ("clbest", "cvpredbest", "folds", "vect_acc", "vect_score", "proposal_size",
+           "active_classes", "flags", "scal", "counters")])
+    if rc != 0:
+        raise RuntimeError(_err(L))
+    return CoreResult(out["clbest"], out["cvpredbest"], out["folds"], out["vect_acc"],
+                      out["vect_score"], out["proposal_size"], out["active_classes"],
+                      out["flags"].reshape(cycles, 3), float(out["scal"][0]),
+                      float(out["scal"][1]), out["counters"])
+
+
+def core_plslda(L, x, labels, *, constrain=None, fixed=None, cycles=20, folds=10, stratified=True,
+                components=5, fixed_components=None, center=True, scale=True, threads=1,
+                evolutionary=False, guarded=False, absorption=False, adaptive=True,
+                coarsening=False, seed=1, cv_seed=1) -> CoreResult:
+    """CorePLSLDA_CPU; counters has 18 entries (16 of CoreKNNGraph, then PLS
+    coarsening attempted / accepted)."""
+    x = np.ascontiguousarray(x, np.float32)
+    samples, d = x.shape
+    lab = np.ascontiguousarray(labels, np.int32)
+    con = np.ascontiguousarray(constrain if constrain is not None else np.zeros(samples), np.int32)
+    fix = np.ascontiguousarray(fixed if fixed is not None else np.zeros(samples), np.int32)
+    fc = components if fixed_components is None else fixed_components
+    copts = np.array([cycles, 0, folds, int(stratified), int(evolutionary), int(guarded),
+                      int(absorption), int(adaptive), int(coarsening)], np.int32)
+    popts = np.array([folds, int(stratified), components, fc, int(center), int(scale), threads], np.int32)
+    out = dict(clbest=np.zeros(samples, np.int32), cvpredbest=np.zeros(samples, np.int32),
+               folds=np.zeros(samples, np.int32), vect_acc=np.zeros(cycles, np.float64),
+               vect_score=np.zeros(cycles, np.float64), proposal_size=np.zeros(cycles, np.int32),
+               active_classes=np.zeros(cycles, np.int32), flags=np.zeros(cycles * 3, np.uint8),
+               scal=np.zeros(2, np.float64), counters=np.zeros(18, np.int32))
+    rc = L.core_plslda(
+        x.ctypes.data_as(ctypes.c_void_p), samples, d, lab.ctypes.data_as(ctypes.c_void_p),
+        con.ctypes.data_as(ctypes.c_void_p), int(constrain is not None),
+        fix.ctypes.data_as(ctypes.c_void_p), int(fixed is not None),
+        copts.ctypes.data_as(ctypes.c_void_p), popts.ctypes.data_as(ctypes.c_void_p),
+        ctypes.c_ulonglong(seed), ctypes.c_ulonglong(cv_seed),
         *[out[f].ctypes.data_as(ctypes.c_void_p) for f in
           ("clbest", "cvpredbest", "folds", "vect_acc", "vect_score", "proposal_size",
            "active_classes", "flags", "scal", "counters")])

@@ -24,6 +24,7 @@
 // Build with -ffp-contract=off so no multiply-add is fused.
 
 #include "../kodama_gb300/csrc/ext80.h"
+#include "pls_oracle.h"
 
 #include <algorithm>
 #include <atomic>
@@ -553,13 +554,18 @@ std::vector<int> vote_predict(const VoteTable& t, const std::vector<int>& labels
 // ---------------------------------------------------------------------------
 struct Policy {
   bool prediction_guidance = true, adaptive_proposal_size = true, transition_proposal = true,
-       stochastic_acceptance = true, diversity_multiplier = true, reject_single_class = true;
+       stochastic_acceptance = true, diversity_multiplier = true, pls_transition_coarsening = true,
+       pls_fragmentation_penalty = true, reject_single_class = true;
 };
 
-double objective(const std::vector<int>& labels, double acc, bool guarded, const Policy& pol) {
+// core_objective_score (core.cpp:916-972).  `fragmentation` is
+// auto_class_coarsening with the PLS-LDA classifier.
+double objective(const std::vector<int>& labels, double acc, bool guarded, const Policy& pol,
+                 bool fragmentation = false) {
   const bool use_div = guarded && pol.diversity_multiplier;
+  const bool use_frag = fragmentation && pol.pls_fragmentation_penalty;
   const bool reject1 = guarded && pol.reject_single_class;
-  if (!use_div && !reject1) return acc;
+  if (!use_div && !use_frag && !reject1) return acc;
   if (labels.empty()) return acc;
   std::unordered_map<int, int> counts;
   counts.reserve(labels.size());
@@ -577,7 +583,104 @@ double objective(const std::vector<int>& labels, double acc, bool guarded, const
     }
     score *= std::sqrt(std::max(0.0, 1.0 - same));
   }
+  if (use_frag && nc > 1) {
+    double entropy = 0.0;
+    for (const auto& kv : counts) {
+      const double p = static_cast<double>(kv.second) / n;
+      if (p > 0.0) entropy -= p * std::log(p);
+    }
+    const double max_entropy = n > 1.0 ? std::log(n) : 0.0;
+    const double code_cost = max_entropy > 0.0 ? std::clamp(entropy / max_entropy, 0.0, 1.0) : 0.0;
+    const double keff = std::exp(entropy);
+    const double frag = std::max(0.0, std::log(static_cast<double>(nc) / std::max(1.0, keff)));
+    const double frag_cost = frag / (1.0 + frag);
+    score -= (1.0 - acc) * std::max(code_cost, frag_cost);
+  }
   return score;
+}
+
+// propose_auto_class_coarsening (core.cpp:995-1108) over the transition
+// statistics of build_class_transition_stats (:980-993).
+bool coarsening(std::vector<int>& labels, const std::vector<int>& prev, const std::vector<int>& fixed,
+                std::mt19937_64& rng) {
+  std::map<int, int> sizes, movable;
+  std::map<int, std::map<int, int>> trans;
+  for (size_t i = 0; i < labels.size(); ++i) {
+    ++sizes[labels[i]];
+    ++trans[labels[i]][prev[i]];
+    if (fixed[i] != 1) ++movable[labels[i]];
+  }
+  const int nc = static_cast<int>(sizes.size());
+  if (nc <= 2) return false;
+  const double n = static_cast<double>(labels.size());
+  double class_entropy = 0.0;
+  for (const auto& kv : sizes) {
+    const double p = static_cast<double>(kv.second) / n;
+    if (p > 0.0) class_entropy -= p * std::log(p);
+  }
+  const double keff = std::exp(class_entropy);
+  const double frag = std::max(0.0, std::log(static_cast<double>(nc) / std::max(1.0, keff)));
+  double wte = 0.0;
+  struct Cand { int source, destination; double score; };
+  std::vector<Cand> cands;
+  for (const auto& kv : sizes) {
+    const int src = kv.first, ssize = kv.second;
+    const auto mv = movable.find(src);
+    const int mov = mv == movable.end() ? 0 : mv->second;
+    if (mov <= 0) continue;
+    int dst_best = src, dsize = ssize, bcount = 0;
+    double te = 0.0;
+    const auto& row = trans.at(src);
+    for (const auto& dst : row) {
+      const double p = static_cast<double>(dst.second) / static_cast<double>(ssize);
+      if (p > 0.0) te -= p * std::log(p);
+      const auto cs = sizes.find(dst.first);
+      if (dst.first != src && cs != sizes.end() &&
+          (dst.second > bcount || (dst.second == bcount && cs->second > dsize) ||
+           (dst.second == bcount && cs->second == dsize && dst.first < dst_best))) {
+        dst_best = dst.first;
+        dsize = cs->second;
+        bcount = dst.second;
+      }
+    }
+    wte += (static_cast<double>(ssize) / n) * te;
+    if (dst_best == src || bcount == 0) continue;
+    const double stay = static_cast<double>(row.count(src) ? row.at(src) : 0) / static_cast<double>(ssize);
+    cands.push_back(Cand{src, dst_best, (1.0 / std::sqrt(static_cast<double>(mov))) * (1.0 - stay)});
+  }
+  if (cands.empty()) return false;
+  const double temperature = frag / (frag + wte + 1.0);
+  const double redundant = std::max(0.0, static_cast<double>(nc) - keff);
+  int budget = static_cast<int>(std::ceil(temperature * redundant));
+  if (budget < 1 && frag > 0.0) budget = 1;
+  budget = std::min(budget, nc - 2);
+  if (budget <= 0) return false;
+  std::shuffle(cands.begin(), cands.end(), rng);
+  std::stable_sort(cands.begin(), cands.end(), [](const Cand& a, const Cand& b) { return a.score > b.score; });
+  std::map<int, int> remap;
+  for (const auto& kv : sizes) remap[kv.first] = kv.first;
+  int merged = 0;
+  for (const Cand& c : cands) {
+    if (merged >= budget) break;
+    if (remap[c.source] != c.source) continue;
+    int d = c.destination;
+    while (remap[d] != d) d = remap[d];
+    if (d == c.source) continue;
+    remap[c.source] = d;
+    ++merged;
+  }
+  if (merged == 0) return false;
+  bool changed = false;
+  for (size_t i = 0; i < labels.size(); ++i) {
+    if (fixed[i] == 1) continue;
+    int d = labels[i];
+    while (remap[d] != d) d = remap[d];
+    if (d != labels[i]) {
+      labels[i] = d;
+      changed = true;
+    }
+  }
+  return changed;
 }
 
 // Many-to-one absorption (core.cpp:980-993 build_class_transition_stats,
@@ -679,6 +782,7 @@ int proposal_count(int G, int cycle, int cycles, bool adaptive, std::mt19937_64&
 struct CoreOpts {
   int cycles = 100, k = 30, folds = 10;
   bool stratified = true, evolutionary = false, guarded = false, absorption = false, adaptive = true;
+  bool coarsening = false;  // auto_class_coarsening (PLS-LDA classifier)
   uint64_t seed = 1, cv_seed = 1;
   Policy policy;
 };
@@ -689,20 +793,19 @@ struct CoreOut {
   std::vector<int> proposal_size, active_classes;
   std::vector<unsigned char> accepted, improving, temperature;
   double accbest = 0.0, scorebest = 0.0;
-  int counters[16] = {0};
+  // cycles_completed, proposals_evaluated, best_state_updates, current_state_accepts,
+  // stochastic attempts / accepts, rejections, coarsening_moves, absorption_moves,
+  // transition attempted / accepted, many_to_one attempted / accepted, cv_evaluations,
+  // success, pls_coarsening_attempted, pls_coarsening_accepted
+  int counters[18] = {0};
 };
 
-// maximize_core (core.cpp:1269-1549) with the kNN graph predictor
-// (core_knn_graph_backend :1574-1620).
-CoreOut core_knn_graph(const int* gidx, const float* gdist, int samples, int gk, int index_base,
-                       const std::vector<int>& init, const std::vector<int>& constrain,
-                       const std::vector<int>& fixed_in, const CoreOpts& o) {
+// maximize_core (core.cpp:1269-1549) for any predictor labels -> CV predictions.
+template <class Predict>
+CoreOut core_run(int samples, const std::vector<int>& init, const std::vector<int>& constrain,
+                 const std::vector<int>& fixed_in, const CoreOpts& o, Predict&& predict) {
   CoreOut r;
   const int T = o.cycles;
-  r.folds = make_folds(init, constrain, o.folds, o.stratified, o.cv_seed);
-  const VoteTable table = build_vote_table(gidx, gdist, samples, gk, index_base, r.folds, o.k);
-  int nfold = 0;
-  for (int f : r.folds) nfold = std::max(nfold, f + 1);
   std::vector<int> fixed = fixed_in.empty() ? std::vector<int>(static_cast<size_t>(samples), 0) : fixed_in;
   r.vect_acc.assign(T, -1.0);
   r.vect_score.assign(T, -1.0);
@@ -731,16 +834,14 @@ CoreOut core_knn_graph(const int* gidx, const float* gdist, int samples, int gk,
     return static_cast<int>(std::unique(u.begin(), u.end()) - u.begin());
   };
   std::mt19937_64 rng(o.seed);
-  std::vector<int> universe = init;
-  std::sort(universe.begin(), universe.end());
-  universe.erase(std::unique(universe.begin(), universe.end()), universe.end());
   r.clbest = init;
-  r.cvpredbest = vote_predict(table, r.clbest, universe, nfold);
+  r.cvpredbest = predict(r.clbest);
   int cv_evals = 1, proposals = 0, best_updates = 0, accepts = 0, st_attempts = 0, st_accepts = 0,
-      rejections = 0, absorb_moves = 0, tr_attempted = 0, tr_accepted = 0, m1_att = 0, m1_acc = 0;
+      rejections = 0, absorb_moves = 0, tr_attempted = 0, tr_accepted = 0, m1_att = 0, m1_acc = 0,
+      co_moves = 0, co_att = 0, co_acc = 0;
   bool success = false;
   r.accbest = accuracy(r.clbest, r.cvpredbest);
-  r.scorebest = objective(r.clbest, r.accbest, o.guarded, o.policy);
+  r.scorebest = objective(r.clbest, r.accbest, o.guarded, o.policy, o.coarsening);
   std::vector<int> cur = r.clbest, curpred = r.cvpredbest;
   double cur_acc = r.accbest, cur_score = r.scorebest;
   std::vector<int> groups(static_cast<size_t>(G));
@@ -796,19 +897,25 @@ CoreOut core_knn_graph(const int* gidx, const float* gdist, int samples, int gk,
         for (int idx : eligible) cl[idx] = rep;
       }
     }
-    bool absorbed = false;
+    bool absorbed = false, coarsened = false;
+    const bool attempt_co = o.policy.transition_proposal && o.coarsening && o.policy.pls_transition_coarsening;
     const bool attempt = o.policy.transition_proposal && o.absorption;
+    if (attempt_co || attempt) ++tr_attempted;
+    if (attempt_co) {
+      ++co_att;
+      coarsened = coarsening(cl, pp, fixed, rng);
+      if (coarsened) ++co_moves;
+    }
     if (attempt) {
-      ++tr_attempted;
       ++m1_att;
       absorbed = absorption(cl, pp, fixed, rng);
       if (absorbed) ++absorb_moves;
     }
-    const std::vector<int> pred = vote_predict(table, cl, universe, nfold);
+    const std::vector<int> pred = predict(cl);
     ++cv_evals;
     ++proposals;
     const double acc = accuracy(cl, pred);
-    const double score = objective(cl, acc, o.guarded, o.policy);
+    const double score = objective(cl, acc, o.guarded, o.policy, o.coarsening);
     const bool improves = score > r.scorebest;
     if (improves) {
       r.cvpredbest = pred;
@@ -844,18 +951,62 @@ CoreOut core_knn_graph(const int* gidx, const float* gdist, int samples, int gk,
     r.accepted[cycle] = accepted ? 1 : 0;
     r.improving[cycle] = accepted && improving ? 1 : 0;
     r.temperature[cycle] = stoch ? 1 : 0;
-    if (accepted && absorbed) {
+    if (accepted && (coarsened || absorbed)) {
       ++tr_accepted;
-      ++m1_acc;
+      if (coarsened) ++co_acc;
+      if (absorbed) ++m1_acc;
     }
     r.active_classes[cycle] = distinct(o.evolutionary ? cur : r.clbest);
     r.vect_acc[cycle] = r.accbest;
     r.vect_score[cycle] = r.scorebest;
     if (acc == 1.0 && std::isfinite(score)) success = true;
   }
-  const int c[16] = {T, proposals, best_updates, accepts, st_attempts, st_accepts, rejections, 0,
-                     absorb_moves, tr_attempted, tr_accepted, m1_att, m1_acc, cv_evals, success ? 1 : 0, 0};
+  const int c[18] = {T, proposals, best_updates, accepts, st_attempts, st_accepts, rejections, co_moves,
+                     absorb_moves, tr_attempted, tr_accepted, m1_att, m1_acc, cv_evals, success ? 1 : 0, 0,
+                     co_att, co_acc};
   std::memcpy(r.counters, c, sizeof(c));
+  return r;
+}
+
+// CoreKNNGraph_CPU: maximize_core with the kNN graph predictor
+// (core_knn_graph_backend, core.cpp:1574-1620).
+CoreOut core_knn_graph(const int* gidx, const float* gdist, int samples, int gk, int index_base,
+                       const std::vector<int>& init, const std::vector<int>& constrain,
+                       const std::vector<int>& fixed_in, const CoreOpts& o) {
+  const std::vector<int> folds = make_folds(init, constrain, o.folds, o.stratified, o.cv_seed);
+  const VoteTable table = build_vote_table(gidx, gdist, samples, gk, index_base, folds, o.k);
+  int nfold = 0;
+  for (int f : folds) nfold = std::max(nfold, f + 1);
+  std::vector<int> universe = init;
+  std::sort(universe.begin(), universe.end());
+  universe.erase(std::unique(universe.begin(), universe.end()), universe.end());
+  CoreOut r = core_run(samples, init, constrain, fixed_in, o, [&](const std::vector<int>& labels) {
+    return vote_predict(table, labels, universe, nfold);
+  });
+  r.folds = folds;
+  return r;
+}
+
+// CorePLSLDA_CPU (core.cpp:1626-1646): maximize_core with PLSLDACV_CPU as the
+// predictor under a fresh data epoch.  Non-stratified folds use the fold cache
+// of plscv.cpp:593-667: the first evaluation computes loadings through the
+// scores, later ones through the fold Gram (built on the second evaluation).
+CoreOut core_plslda(const float* x, int samples, int p, const std::vector<int>& init,
+                    const std::vector<int>& constrain, const std::vector<int>& fixed_in, const CoreOpts& o,
+                    const PLSOpts& po) {
+  PLSFoldCache cache;
+  bool have_cache = false;
+  CoreOut r = core_run(samples, init, constrain, fixed_in, o, [&](const std::vector<int>& labels) {
+    if (po.stratified) return plsldacv(x, samples, p, labels, constrain, po).predicted;
+    if (!have_cache) {
+      cache = pls_fold_cache(x, samples, p, make_folds(labels, constrain, po.folds, false, po.cv_seed), po);
+      have_cache = true;
+      return plsldacv_on_cache(cache, samples, p, labels, po, false).predicted;
+    }
+    if (!cache.gram_built) pls_build_grams(cache, p);
+    return plsldacv_on_cache(cache, samples, p, labels, po, true).predicted;
+  });
+  r.folds = make_folds(init, constrain, po.folds, po.stratified, po.cv_seed);
   return r;
 }
 
@@ -936,20 +1087,50 @@ struct RunOut {
   double accbest = 0.0;
   uint64_t hashes[3] = {0, 0, 0};
   int counters[8] = {0};
+  int pls[2] = {0, 0};          // pls_coarsening attempted / accepted
   std::vector<int> cycle_diag;  // cycles x 5
 };
+
+// Run diagnostics of run_iteration (kodama_matrix.cpp:3290-3316).
+void fill_run(RunOut& ro, const CoreOut& core, int run, const std::vector<int>& land, const std::vector<int>& init,
+              int L, int cycles) {
+  ro.vect_acc = core.vect_acc;
+  ro.accbest = core.accbest;
+  ro.hashes[0] = fnv_hash(land);
+  ro.hashes[1] = fnv_hash(init);
+  ro.hashes[2] = fnv_hash(core.folds);
+  ro.counters[0] = run;
+  ro.counters[1] = core.counters[0];
+  ro.counters[2] = core.counters[9];
+  ro.counters[3] = core.counters[10];
+  ro.counters[4] = core.counters[11];
+  ro.counters[5] = core.counters[12];
+  ro.counters[6] = core.counters[13];
+  ro.counters[7] = L;
+  ro.pls[0] = core.counters[16];
+  ro.pls[1] = core.counters[17];
+  ro.cycle_diag.resize(static_cast<size_t>(cycles) * 5);
+  for (int c = 0; c < cycles; ++c) {
+    int* cd = ro.cycle_diag.data() + 5 * c;
+    cd[0] = core.proposal_size[c];
+    cd[1] = core.active_classes[c];
+    cd[2] = core.accepted[c];
+    cd[3] = core.improving[c];
+    cd[4] = core.temperature[c];
+  }
+}
 
 void kodama_matrix(const float* x, int n, int d, const int* gidx_in, const float* gdist_in, int gk_in,
                    int index_base, const MatrixOpts& o, uint64_t seed,
                    int* res_out, double* acc_out, double* v_out, uint64_t* hashes_out, int* counters_out,
-                   int* cycle_out, int* knn_idx_out, float* knn_dist_out, int* knn_k_out, double* timings) {
+                   int* cycle_out, int* knn_idx_out, float* knn_dist_out, int* knn_k_out, double* timings,
+                   int* pls_out) {
   const auto t0 = std::chrono::steady_clock::now();
   auto since = [](std::chrono::steady_clock::time_point a) {
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - a).count();
   };
   if (n < 3) throw std::invalid_argument("KODAMAMatrix requires at least 3 rows.");
   if (o.runs < 1 || o.cycles < 0 || o.folds < 2) throw std::invalid_argument("invalid KODAMA.matrix options");
-  if (o.classifier != 0) throw std::invalid_argument("oracle restates the kNN classifier only");
   int landmarks = o.landmarks > 0 ? o.landmarks : 10000;
   if (landmarks >= n) landmarks = static_cast<int>(std::ceil(static_cast<double>(n) * 0.75));
   landmarks = std::max(2, std::min(landmarks, n - 1));
@@ -1026,6 +1207,41 @@ void kodama_matrix(const float* x, int n, int d, const int* gidx_in, const float
       }
       std::vector<int> constrain(static_cast<size_t>(L));
       std::iota(constrain.begin(), constrain.end(), 1);
+      if (o.classifier == 1) {
+        // PLS-LDA classifier (run_iteration, kodama_matrix.cpp:3105-3158, 3262-3276)
+        CoreOpts co;
+        co.cycles = o.cycles;
+        co.evolutionary = true;
+        co.guarded = true;
+        co.absorption = true;
+        co.adaptive = true;
+        co.coarsening = true;
+        co.seed = seed + static_cast<uint64_t>(run);
+        PLSOpts po;
+        po.folds = o.folds;
+        po.stratified = false;
+        po.cv_seed = seed + static_cast<uint64_t>(run);
+        po.max_components = o.components;
+        po.fixed_components = o.components;
+        const CoreOut core = core_plslda(xl.data(), L, d, init, constrain,
+                                         std::vector<int>(static_cast<size_t>(L), 0), co, po);
+        ro.res.assign(static_cast<size_t>(n), 0);
+        for (int i = 0; i < L; ++i) ro.res[land[i]] = core.clbest[i];
+        std::vector<char> is_land(static_cast<size_t>(n), 0);
+        for (int r : land) is_land[r] = 1;
+        std::vector<int> tpoints;
+        for (int t = 0; t < n; ++t) if (!is_land[t]) tpoints.push_back(t);
+        if (!tpoints.empty()) {
+          std::vector<float> xt(tpoints.size() * static_cast<size_t>(d));
+          for (size_t i = 0; i < tpoints.size(); ++i)
+            std::copy_n(x + static_cast<size_t>(tpoints[i]) * d, d, xt.data() + i * d);
+          const std::vector<int> proj =
+              plslda_predict(xl.data(), L, d, core.clbest, xt.data(), static_cast<int>(tpoints.size()), po);
+          for (size_t i = 0; i < tpoints.size(); ++i) ro.res[tpoints[i]] = proj[i];
+        }
+        fill_run(ro, core, run, land, init, L, o.cycles);
+        continue;
+      }
       CoreOpts co;
       co.cycles = o.cycles;
       co.k = std::max(o.knn_k, 1);
@@ -1057,28 +1273,7 @@ void kodama_matrix(const float* x, int n, int d, const int* gidx_in, const float
         }
         ro.res[t] = votes.empty() ? core.clbest.front() : majority_of(votes);
       }
-      ro.vect_acc = core.vect_acc;
-      ro.accbest = core.accbest;
-      ro.hashes[0] = fnv_hash(land);
-      ro.hashes[1] = fnv_hash(init);
-      ro.hashes[2] = fnv_hash(core.folds);
-      ro.counters[0] = run;
-      ro.counters[1] = core.counters[0];
-      ro.counters[2] = core.counters[9];
-      ro.counters[3] = core.counters[10];
-      ro.counters[4] = core.counters[11];
-      ro.counters[5] = core.counters[12];
-      ro.counters[6] = core.counters[13];
-      ro.counters[7] = L;
-      ro.cycle_diag.resize(static_cast<size_t>(o.cycles) * 5);
-      for (int c = 0; c < o.cycles; ++c) {
-        int* cd = ro.cycle_diag.data() + 5 * c;
-        cd[0] = core.proposal_size[c];
-        cd[1] = core.active_classes[c];
-        cd[2] = core.accepted[c];
-        cd[3] = core.improving[c];
-        cd[4] = core.temperature[c];
-      }
+      fill_run(ro, core, run, land, init, L, o.cycles);
     }
   };
   const int workers = std::max(1, std::min(o.threads, o.runs));
@@ -1094,6 +1289,10 @@ void kodama_matrix(const float* x, int n, int d, const int* gidx_in, const float
     for (int c = 0; c < o.cycles; ++c) v_out[static_cast<size_t>(r) * o.cycles + c] = ro.vect_acc[c];
     for (int h = 0; h < 3; ++h) hashes_out[3 * r + h] = ro.hashes[h];
     for (int c = 0; c < 8; ++c) counters_out[8 * r + c] = ro.counters[c];
+    if (pls_out) {
+      pls_out[2 * r] = ro.pls[0];
+      pls_out[2 * r + 1] = ro.pls[1];
+    }
     std::copy(ro.cycle_diag.begin(), ro.cycle_diag.end(), cycle_out + static_cast<size_t>(r) * o.cycles * 5);
   }
   *knn_k_out = o.materialize ? K : 0;
@@ -1251,7 +1450,7 @@ int orc_core_knn_graph(
     }
     scal_out[0] = r.accbest;
     scal_out[1] = r.scorebest;
-    std::memcpy(int_out, r.counters, sizeof(r.counters));
+    std::memcpy(int_out, r.counters, sizeof(int) * 16);
     return 0;
   } catch (const std::exception& e) {
     orc::g_error = e.what();
@@ -1263,14 +1462,108 @@ int orc_kodama_matrix_graph_data(
   const float* x, int n, int d, const int* gidx, const float* gdist, int gk, int index_base,
   const int* o, unsigned long long seed,
   int* res, double* acc, double* v, unsigned long long* hashes, int* run_counters,
-  int* cycle_diag, int* out_idx, float* out_dist, int* out_k, double* timings
+  int* cycle_diag, int* out_idx, float* out_dist, int* out_k, double* timings, int* pls_counters
 ) {
   try {
     orc::MatrixOpts mo{o[0], o[1], o[2], o[3], o[4], o[5], o[6], o[7], o[8], o[9], o[10], o[11], o[12]};
     if (timings) for (int i = 0; i < 6; ++i) timings[i] = 0.0;
     orc::kodama_matrix(x, n, d, gidx, gdist, gk, index_base, mo, seed, res, acc, v,
                        reinterpret_cast<uint64_t*>(hashes), run_counters, cycle_diag, out_idx, out_dist, out_k,
-                       timings);
+                       timings, pls_counters);
+    return 0;
+  } catch (const std::exception& e) {
+    orc::g_error = e.what();
+    return 1;
+  }
+}
+
+namespace {
+orc::PLSOpts pls_opts(const int* popts, unsigned long long cv_seed) {
+  orc::PLSOpts o;
+  o.folds = popts[0];
+  o.stratified = popts[1] != 0;
+  o.max_components = popts[2];
+  o.fixed_components = popts[3];
+  o.center = popts[4] != 0;
+  o.scale = popts[5] != 0;
+  o.cv_seed = cv_seed;
+  return o;
+}
+}  // namespace
+
+// Same conventions as ref_plsldacv (oracle/ref_driver.cpp).
+int orc_plsldacv(const float* x, int n, int d, const int* labels, const int* constrain, int has_constrain,
+                 const int* popts, unsigned long long cv_seed, int* predicted, int* folds,
+                 int* selected_components, double* accuracy_by_components, double* seconds) {
+  try {
+    const orc::PLSOpts o = pls_opts(popts, cv_seed);
+    std::vector<int> lab(labels, labels + n);
+    std::vector<int> con = has_constrain ? std::vector<int>(constrain, constrain + n) : std::vector<int>();
+    const auto t0 = std::chrono::steady_clock::now();
+    const auto r = orc::plsldacv(x, n, d, lab, con, o);
+    *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    std::memcpy(predicted, r.predicted.data(), sizeof(int) * n);
+    std::memcpy(folds, r.folds.data(), sizeof(int) * n);
+    *selected_components = r.selected_components;
+    for (int i = 0; i < o.max_components; ++i) accuracy_by_components[i] = r.accuracy_by_components[i];
+    return 0;
+  } catch (const std::exception& e) {
+    orc::g_error = e.what();
+    return 1;
+  }
+}
+
+int orc_plsldapredict(const float* train, int n, int d, const int* labels, const float* test, int nt,
+                       const int* popts, int* predicted) {
+  try {
+    const orc::PLSOpts o = pls_opts(popts, 1);
+    std::vector<int> lab(labels, labels + n);
+    const auto r = orc::plslda_predict(train, n, d, lab, test, nt, o);
+    std::memcpy(predicted, r.data(), sizeof(int) * r.size());
+    return 0;
+  } catch (const std::exception& e) {
+    orc::g_error = e.what();
+    return 1;
+  }
+}
+
+// CorePLSLDA_CPU.  copts as orc_core_knn_graph plus copts[8] =
+// auto_class_coarsening; popts as orc_plsldacv; int_out has 18 counters.
+int orc_core_plslda(
+  const float* x, int samples, int d, const int* labels, const int* constrain, int has_constrain,
+  const int* fixed, int has_fixed, const int* copts, const int* popts, unsigned long long seed,
+  unsigned long long cv_seed, int* clbest, int* cvpredbest, int* folds, double* vect_acc, double* vect_score,
+  int* proposal_size, int* active_classes, unsigned char* flags3, double* scal_out, int* int_out
+) {
+  try {
+    orc::CoreOpts o;
+    o.cycles = copts[0];
+    o.evolutionary = copts[4] != 0;
+    o.guarded = copts[5] != 0;
+    o.absorption = copts[6] != 0;
+    o.adaptive = copts[7] != 0;
+    o.coarsening = copts[8] != 0;
+    o.seed = seed;
+    const orc::PLSOpts po = pls_opts(popts, cv_seed);
+    std::vector<int> lab(labels, labels + samples);
+    std::vector<int> con = has_constrain ? std::vector<int>(constrain, constrain + samples) : std::vector<int>();
+    std::vector<int> fix = has_fixed ? std::vector<int>(fixed, fixed + samples) : std::vector<int>();
+    const auto r = orc::core_plslda(x, samples, d, lab, con, fix, o, po);
+    std::memcpy(clbest, r.clbest.data(), sizeof(int) * samples);
+    std::memcpy(cvpredbest, r.cvpredbest.data(), sizeof(int) * samples);
+    std::memcpy(folds, r.folds.data(), sizeof(int) * samples);
+    for (int c = 0; c < o.cycles; ++c) {
+      vect_acc[c] = r.vect_acc[c];
+      vect_score[c] = r.vect_score[c];
+      proposal_size[c] = r.proposal_size[c];
+      active_classes[c] = r.active_classes[c];
+      flags3[3 * c + 0] = r.accepted[c];
+      flags3[3 * c + 1] = r.improving[c];
+      flags3[3 * c + 2] = r.temperature[c];
+    }
+    scal_out[0] = r.accbest;
+    scal_out[1] = r.scorebest;
+    std::memcpy(int_out, r.counters, sizeof(r.counters));
     return 0;
   } catch (const std::exception& e) {
     orc::g_error = e.what();

@@ -35,3 +35,6 @@ exact_knn = _bind(_b.exact_knn)
 kmeans = _bind(_b.kmeans)
 dot_x86 = _bind(_b.dot_x86)
 quota_sample = _bind(_b.quota_sample)
+core_plslda = _bind(_b.core_plslda)
+plsldacv = _bind(_b.plsldacv)
+plsldapredict = _bind(_b.plsldapredict)

@@ -28,3 +28,4 @@ dissimilarity = _bind(_b.dissimilarity)
 plsldacv = _bind(_b.plsldacv)
 plsldapredict = _bind(_b.plsldapredict)
 knncv = _bind(_b.knncv)
+core_plslda = _bind(_b.core_plslda)

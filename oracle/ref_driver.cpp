@@ -53,7 +53,7 @@ kodama::KODAMAMatrixOptions matrix_options(const int* o, unsigned long long seed
 void export_matrix_result(
   const kodama::KODAMAMatrixResult& r, int n, int runs, int cycles,
   int* res, double* acc, double* v, unsigned long long* hashes, int* run_counters,
-  int* cycle_diag, int* out_idx, float* out_dist, int* out_k, double* timings
+  int* cycle_diag, int* out_idx, float* out_dist, int* out_k, double* timings, int* pls_counters
 ) {
   std::memcpy(res, r.res.data(), sizeof(int) * static_cast<size_t>(runs) * n);
   std::memcpy(acc, r.acc.data(), sizeof(double) * runs);
@@ -68,6 +68,10 @@ void export_matrix_result(
     c[3] = d.transition_accepted; c[4] = d.many_to_one_attempted;
     c[5] = d.many_to_one_accepted; c[6] = d.cv_evaluations;
     c[7] = r.effective_landmarks;
+    if (pls_counters) {
+      pls_counters[2 * i] = d.pls_coarsening_attempted;
+      pls_counters[2 * i + 1] = d.pls_coarsening_accepted;
+    }
   }
   for (size_t i = 0; i < r.cycle_diagnostics.size(); ++i) {
     const auto& d = r.cycle_diagnostics[i];
@@ -105,7 +109,7 @@ int ref_kodama_matrix_graph_data(
   const float* x, int n, int d, const int* gidx, const float* gdist, int gk, int index_base,
   const int* o, unsigned long long seed,
   int* res, double* acc, double* v, unsigned long long* hashes, int* run_counters,
-  int* cycle_diag, int* out_idx, float* out_dist, int* out_k, double* timings
+  int* cycle_diag, int* out_idx, float* out_dist, int* out_k, double* timings, int* pls_counters
 ) {
   try {
     kodama::MatrixView view(x, static_cast<size_t>(n), static_cast<size_t>(d));
@@ -120,7 +124,7 @@ int ref_kodama_matrix_graph_data(
     const auto r = kodama::KODAMAMatrixFromGraphData_CPU(view, g, {}, {}, {}, opt);
     const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     export_matrix_result(r, n, opt.runs, opt.cycles, res, acc, v, hashes, run_counters,
-                         cycle_diag, out_idx, out_dist, out_k, timings);
+                         cycle_diag, out_idx, out_dist, out_k, timings, pls_counters);
     if (timings) timings[5] = wall;
     return 0;
   } catch (const std::exception& e) {
@@ -133,7 +137,7 @@ int ref_kodama_matrix_graph_data(
 int ref_kodama_matrix_raw(
   const float* x, int n, int d, const int* o, unsigned long long seed,
   int* res, double* acc, double* v, unsigned long long* hashes, int* run_counters,
-  int* cycle_diag, int* out_idx, float* out_dist, int* out_k, double* timings
+  int* cycle_diag, int* out_idx, float* out_dist, int* out_k, double* timings, int* pls_counters
 ) {
   try {
     kodama::MatrixView view(x, static_cast<size_t>(n), static_cast<size_t>(d));
@@ -142,7 +146,7 @@ int ref_kodama_matrix_raw(
     const auto r = kodama::KODAMAMatrix_CPU(view, {}, {}, {}, opt);
     const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     export_matrix_result(r, n, opt.runs, opt.cycles, res, acc, v, hashes, run_counters,
-                         cycle_diag, out_idx, out_dist, out_k, timings);
+                         cycle_diag, out_idx, out_dist, out_k, timings, pls_counters);
     if (timings) timings[5] = wall;
     return 0;
   } catch (const std::exception& e) {
@@ -283,6 +287,67 @@ int ref_plsldapredict(
     std::vector<int> lab(labels, labels + n);
     const auto r = kodama::PLSLDAPredict_CPU(tv, lab, qv, opt);
     std::memcpy(predicted, r.data(), sizeof(int) * nt);
+    return 0;
+  } catch (const std::exception& e) {
+    g_error = e.what();
+    return 1;
+  }
+}
+
+// CorePLSLDA_CPU (kodama.hpp:986).  copts as ref_core_knn_graph plus
+// copts[8] = auto_class_coarsening; popts as ref_plsldacv; int_out has 18
+// counters (the 16 of ref_core_knn_graph, then pls_coarsening attempted /
+// accepted).
+int ref_core_plslda(
+  const float* x, int samples, int d, const int* labels, const int* constrain, int has_constrain,
+  const int* fixed, int has_fixed, const int* copts, const int* popts, unsigned long long seed,
+  unsigned long long cv_seed, int* clbest, int* cvpredbest, int* folds, double* vect_acc, double* vect_score,
+  int* proposal_size, int* active_classes, unsigned char* flags3, double* scal_out, int* int_out
+) {
+  try {
+    kodama::MatrixView view(x, static_cast<size_t>(samples), static_cast<size_t>(d));
+    kodama::CoreOptions opt;
+    opt.classifier = kodama::CoreClassifier::PLS_LDA;
+    opt.cycles = copts[0];
+    opt.evolutionary_search = copts[4] != 0;
+    opt.guarded_diversity = copts[5] != 0;
+    opt.many_to_one_absorption = copts[6] != 0;
+    opt.adaptive_proposal_size = copts[7] != 0;
+    opt.auto_class_coarsening = copts[8] != 0;
+    opt.seed = seed;
+    opt.pls.cv.folds = popts[0];
+    opt.pls.cv.stratified = popts[1] != 0;
+    opt.pls.cv.seed = cv_seed;
+    opt.pls.max_components = popts[2];
+    opt.pls.fixed_components = popts[3];
+    opt.pls.center = popts[4] != 0;
+    opt.pls.scale = popts[5] != 0;
+    opt.pls.n_threads = popts[6];
+    std::vector<int> lab(labels, labels + samples);
+    std::vector<int> con = has_constrain ? std::vector<int>(constrain, constrain + samples) : std::vector<int>();
+    std::vector<int> fix = has_fixed ? std::vector<int>(fixed, fixed + samples) : std::vector<int>();
+    const auto r = kodama::CorePLSLDA_CPU(view, lab, con, fix, opt);
+    std::memcpy(clbest, r.clbest.data(), sizeof(int) * samples);
+    std::memcpy(cvpredbest, r.cvpredbest.data(), sizeof(int) * samples);
+    std::memcpy(folds, r.fold_assignments.data(), sizeof(int) * samples);
+    for (int c = 0; c < opt.cycles; ++c) {
+      vect_acc[c] = r.vect_acc[c];
+      vect_score[c] = r.vect_score[c];
+      proposal_size[c] = r.proposal_size[c];
+      active_classes[c] = r.active_classes[c];
+      flags3[3 * c + 0] = r.accepted[c];
+      flags3[3 * c + 1] = r.improving_acceptance[c];
+      flags3[3 * c + 2] = r.temperature_acceptance[c];
+    }
+    scal_out[0] = r.accbest;
+    scal_out[1] = r.scorebest;
+    const int counters[18] = {
+      r.cycles_completed, r.proposals_evaluated, r.best_state_updates, r.current_state_accepts,
+      r.stochastic_state_attempts, r.stochastic_state_accepts, r.current_state_rejections,
+      r.coarsening_moves, r.absorption_moves, r.transition_attempted, r.transition_accepted,
+      r.many_to_one_attempted, r.many_to_one_accepted, r.cv_evaluations, r.success ? 1 : 0, 0,
+      r.pls_coarsening_attempted, r.pls_coarsening_accepted};
+    std::memcpy(int_out, counters, sizeof(counters));
     return 0;
   } catch (const std::exception& e) {
     g_error = e.what();

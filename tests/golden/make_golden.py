@@ -59,6 +59,56 @@ def core_case(name, x, K, labels, **kw):
     }
 
 
+def pls_inputs(spec):
+    x, y = datasets.low_rank(n=spec["n"], d=spec["d"], seed=spec["seed"])
+    rng = np.random.default_rng(spec["seed"] + 1000)
+    labels = y.copy()
+    flip = rng.random(len(y)) < spec.get("flip", 0.0)
+    labels[flip] = rng.integers(1, 9, int(flip.sum()))
+    if spec.get("random_labels"):
+        labels = rng.integers(1, spec["random_labels"] + 1, len(y)).astype(np.int32)
+    return x, labels.astype(np.int32)
+
+
+def plsldacv_case(name, spec, **kw):
+    x, labels = pls_inputs(spec)
+    pred, folds, sel, abc, _ = ref.plsldacv(x, labels, **kw)
+    return {"kind": "plsldacv", "name": name, "input": spec, "options": kw, "labels_sha256": sha(labels),
+            "predicted_sha256": sha(pred), "folds_sha256": sha(folds), "selected_components": sel,
+            "accuracy_by_components": abc.tolist(), "predicted_head": pred[:32].tolist()}
+
+
+def plsldapredict_case(name, spec, n_train, **kw):
+    x, labels = pls_inputs(spec)
+    pred = ref.plsldapredict(x[:n_train], labels[:n_train], x[n_train:], **kw)
+    return {"kind": "plsldapredict", "name": name, "input": spec, "n_train": n_train, "options": kw,
+            "predicted_sha256": sha(pred), "predicted_head": pred[:32].tolist()}
+
+
+def core_plslda_case(name, spec, **kw):
+    x, labels = pls_inputs(spec)
+    n = len(labels)
+    r = ref.core_plslda(x, labels, constrain=np.arange(1, n + 1, dtype=np.int32), **kw)
+    return {
+        "kind": "core_plslda", "name": name, "input": spec, "options": kw, "labels_sha256": sha(labels),
+        "clbest_sha256": sha(r.clbest), "cvpredbest_sha256": sha(r.cvpredbest), "folds_sha256": sha(r.folds),
+        "vect_acc": r.vect_acc.tolist(), "vect_score": r.vect_score.tolist(),
+        "proposal_size": r.proposal_size.tolist(), "active_classes": r.active_classes.tolist(),
+        "flags": r.flags.tolist(), "accbest": r.accbest, "scorebest": r.scorebest,
+        "counters": r.counters.tolist(),
+    }
+
+
+def pls_matrix_case(name, spec, K, **kw):
+    x, _ = pls_inputs(spec)
+    case = matrix_case(name, x, K, 0, classifier=1, **kw)
+    r = ref.kodama_matrix_graph_data(x, *oracle.exact_knn(x, K, threads=8), 0, threads=8, materialize=1,
+                                     classifier=1, **kw)
+    case["input"] = spec
+    case["pls_counters"] = r.pls_counters.tolist()
+    return case
+
+
 def main():
     if not ref.available():
         raise SystemExit("build oracle/_ref first (oracle/build_ref.sh)")
@@ -78,6 +128,18 @@ def main():
                            evolutionary=True, guarded=True, absorption=True, stratified=False))
     cases.append(core_case("core_greedy_stratified", xc, 40, labels, cycles=25, k=10, folds=7, seed=5,
                            cv_seed=11, evolutionary=False, guarded=False, absorption=False, stratified=True))
+    cases.append(plsldacv_case("plsldacv_stratified", dict(n=1200, d=60, seed=31, flip=0.3),
+                               folds=10, stratified=True, max_components=6, fixed_components=0, cv_seed=7))
+    cases.append(plsldacv_case("plsldacv_fixed5", dict(n=1000, d=80, seed=32, flip=0.4),
+                               folds=8, stratified=False, max_components=5, fixed_components=5, cv_seed=9))
+    cases.append(plsldapredict_case("plsldapredict_c5", dict(n=1500, d=50, seed=33, flip=0.2), 1000,
+                                    components=5))
+    cases.append(core_plslda_case("core_plslda_evolutionary", dict(n=900, d=40, seed=34, random_labels=10),
+                                  cycles=20, folds=5, stratified=False, components=5, evolutionary=True,
+                                  guarded=True, absorption=True, coarsening=True, seed=13, cv_seed=14))
+    cases.append(pls_matrix_case("pls_matrix_N1500_d50_M4_T12", dict(n=1500, d=50, seed=35), 20,
+                                 seed=99, runs=4, cycles=12, landmarks=10000, splitting=20,
+                                 graph_neighbors=20, folds=5, knn_k=10, components=5))
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py", "cases": cases}, f, indent=1)
     print(f"wrote {len(cases)} cases")

@@ -22,7 +22,21 @@ def cases():
         return json.load(f)["cases"]
 
 
+def pls_inputs(spec):
+    """Low-rank PLS workload of a case spec: (x, labels) with optional label noise."""
+    x, y = datasets.low_rank(n=spec["n"], d=spec["d"], seed=spec["seed"])
+    rng = np.random.default_rng(spec["seed"] + 1000)
+    labels = y.copy()
+    flip = rng.random(len(y)) < spec.get("flip", 0.0)
+    labels[flip] = rng.integers(1, 9, int(flip.sum()))
+    if spec.get("random_labels"):
+        labels = rng.integers(1, spec["random_labels"] + 1, len(y)).astype(np.int32)
+    return x, labels.astype(np.int32)
+
+
 def inputs(case):
+    if "input" in case:
+        return pls_inputs(case["input"])[0]
     name = case["name"]
     if name.startswith("spirals"):
         return datasets.spirals()[0].astype(np.float32)
@@ -63,3 +77,8 @@ def check_core(case, r, folds_attr="folds"):
     assert np.asarray(r.flags).tolist() == case["flags"], "accept flags"
     assert r.accbest == case["accbest"] and r.scorebest == case["scorebest"], "best scalars"
     assert np.asarray(r.counters).tolist() == case["counters"], "counters"
+
+
+def check_pls_matrix(case, r):
+    check_matrix(case, r)
+    assert np.asarray(r.pls_counters).tolist() == case["pls_counters"], "PLS coarsening counters"

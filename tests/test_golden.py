@@ -19,7 +19,10 @@ def test_oracle_matrix_golden(orc, case):
     assert G.sha(gi) + ":" + G.sha(gd) == case["graph_sha256"], "canonical exact graph"
     g_in = gi + 1 if case["index_base"] == 1 else gi
     r = orc.kodama_matrix_graph_data(x, g_in, gd, case["index_base"], threads=8, materialize=1, **case["options"])
-    G.check_matrix(case, r)
+    if "pls_counters" in case:
+        G.check_pls_matrix(case, r)
+    else:
+        G.check_matrix(case, r)
 
 
 @pytest.mark.parametrize("case", [c for c in G.cases() if c["kind"] == "core_knn_graph"], ids=lambda c: c["name"])
@@ -29,6 +32,37 @@ def test_oracle_core_golden(orc, case):
     assert G.sha(labels) == case["labels_sha256"]
     gi, gd = orc.exact_knn(x, case["K"], threads=8)
     r = orc.core_knn_graph(gi, gd, labels, index_base=0, **case["options"])
+    G.check_core(case, r)
+
+
+def _cases(kind):
+    return [c for c in G.cases() if c["kind"] == kind]
+
+
+@pytest.mark.parametrize("case", _cases("plsldacv"), ids=lambda c: c["name"])
+def test_oracle_plsldacv_golden(orc, case):
+    x, labels = G.pls_inputs(case["input"])
+    assert G.sha(labels) == case["labels_sha256"]
+    pred, folds, sel, abc, _ = orc.plsldacv(x, labels, **case["options"])
+    assert pred[:32].tolist() == case["predicted_head"]
+    assert G.sha(pred) == case["predicted_sha256"] and G.sha(folds) == case["folds_sha256"]
+    assert sel == case["selected_components"] and abc.tolist() == case["accuracy_by_components"]
+
+
+@pytest.mark.parametrize("case", _cases("plsldapredict"), ids=lambda c: c["name"])
+def test_oracle_plsldapredict_golden(orc, case):
+    x, labels = G.pls_inputs(case["input"])
+    t = case["n_train"]
+    pred = orc.plsldapredict(x[:t], labels[:t], x[t:], **case["options"])
+    assert pred[:32].tolist() == case["predicted_head"] and G.sha(pred) == case["predicted_sha256"]
+
+
+@pytest.mark.parametrize("case", _cases("core_plslda"), ids=lambda c: c["name"])
+def test_oracle_core_plslda_golden(orc, case):
+    x, labels = G.pls_inputs(case["input"])
+    assert G.sha(labels) == case["labels_sha256"]
+    n = len(labels)
+    r = orc.core_plslda(x, labels, constrain=np.arange(1, n + 1, dtype=np.int32), **case["options"])
     G.check_core(case, r)
 
 

@@ -56,3 +56,56 @@ def test_dissimilarity_vs_reference(orc):
     a = ref.dissimilarity(gi1, gd, res)
     b = orc.dissimilarity(gi1, gd, res)
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def _low_rank_noisy(n, d, seed, flip=0.3):
+    x, y = datasets.low_rank(n=n, d=d, seed=seed)
+    rng = np.random.default_rng(seed)
+    lab = y.copy()
+    f = rng.random(n) < flip
+    lab[f] = rng.integers(1, 9, int(f.sum()))
+    return x, lab.astype(np.int32)
+
+
+@needs_ref
+@pytest.mark.parametrize("n,d,stratified,maxc,fixc", [(300, 20, True, 5, 0), (500, 40, False, 5, 5),
+                                                       (200, 300, False, 4, 4), (120, 10, True, 12, 0)])
+def test_plsldacv_vs_reference(orc, n, d, stratified, maxc, fixc):
+    x, lab = _low_rank_noisy(n, d, seed=n + d)
+    kw = dict(folds=10, stratified=stratified, max_components=maxc, fixed_components=fixc, cv_seed=7)
+    a = ref.plsldacv(x, lab, **kw)
+    b = orc.plsldacv(x, lab, **kw)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    assert a[2] == b[2] and np.array_equal(a[3], b[3])
+    half = n // 2
+    pa = ref.plsldapredict(x[:half], lab[:half], x[half:], components=maxc)
+    pb = orc.plsldapredict(x[:half], lab[:half], x[half:], components=maxc)
+    assert np.array_equal(pa, pb)
+
+
+@needs_ref
+@pytest.mark.parametrize("stratified,coarsening", [(False, True), (True, True), (False, False)])
+def test_core_plslda_vs_reference(orc, stratified, coarsening):
+    x, _ = datasets.low_rank(n=400, d=30, seed=5)
+    labels = np.random.default_rng(6).integers(1, 12, 400).astype(np.int32)
+    kw = dict(cycles=15, folds=5, stratified=stratified, components=4, evolutionary=True, guarded=True,
+              absorption=True, coarsening=coarsening, seed=11, cv_seed=12,
+              constrain=np.arange(1, 401, dtype=np.int32))
+    a = ref.core_plslda(x, labels, **kw)
+    b = orc.core_plslda(x, labels, **kw)
+    for f in ("clbest", "cvpredbest", "folds", "vect_acc", "vect_score", "proposal_size",
+              "active_classes", "flags", "counters"):
+        assert np.array_equal(getattr(a, f), getattr(b, f)), f
+    assert a.accbest == b.accbest and a.scorebest == b.scorebest
+
+
+@needs_ref
+def test_pls_matrix_vs_reference(orc):
+    x, _ = datasets.low_rank(n=800, d=30, seed=3)
+    gi, gd = orc.exact_knn(x, 20, threads=8)
+    kw = dict(runs=3, cycles=8, landmarks=600, splitting=12, graph_neighbors=20, folds=5, knn_k=10,
+              threads=3, materialize=1, classifier=1, components=4)
+    a = ref.kodama_matrix_graph_data(x, gi, gd, 0, seed=77, **kw)
+    b = orc.kodama_matrix_graph_data(x, gi, gd, 0, seed=77, **kw)
+    for f in ("res", "acc", "v", "hashes", "run_counters", "cycle_diag", "knn_idx", "knn_dist", "pls_counters"):
+        assert np.array_equal(getattr(a, f), getattr(b, f)), f
