@@ -94,6 +94,7 @@ typedef struct kgb_matrix_result {
                                 dissimilarity, whole device span */
   int32_t res_on_device;     /* in: 1 = `res` is a device pointer (the label matrix stays in HBM) */
   int32_t reserved;
+  int32_t* pls_counters;     /* runs x 2: PLS coarsening attempted / accepted (classifier 1), or NULL */
 } kgb_matrix_result;
 
 /* Replaces KODAMAMatrix_CUDA (kodama.hpp:1077-1083; dispatch
@@ -126,7 +127,7 @@ typedef struct kgb_core_options {
   int32_t many_to_one_absorption;
   int32_t adaptive_proposal_size;
   int32_t device;
-  int32_t reserved;
+  int32_t auto_class_coarsening; /* CoreOptions::auto_class_coarsening (PLS-LDA classifier only) */
   uint64_t seed;
   uint64_t cv_seed;
   kgb_policy policy;
@@ -144,11 +145,12 @@ typedef struct kgb_core_result {
   uint8_t* flags;            /* cycles x 3: accepted, improving, temperature */
   double accbest;            /* out */
   double scorebest;          /* out */
-  int32_t counters[16];      /* out: cycles_completed, proposals_evaluated, best_state_updates,
+  int32_t counters[18];      /* out: cycles_completed, proposals_evaluated, best_state_updates,
                                 current_state_accepts, stochastic_attempts, stochastic_accepts,
                                 current_state_rejections, coarsening_moves, absorption_moves,
                                 transition_attempted, transition_accepted, many_to_one_attempted,
-                                many_to_one_accepted, cv_evaluations, success, 0 */
+                                many_to_one_accepted, cv_evaluations, success, 0,
+                                pls_coarsening_attempted, pls_coarsening_accepted */
 } kgb_core_result;
 
 /* Replaces CoreKNNGraph_CUDA (kodama.hpp:1043-1050, core.cpp:1684-1700):
@@ -167,6 +169,41 @@ int kgb_core_knn_graph_batch(const int32_t* gidx, const float* gdist, int32_t sa
                              int32_t index_base, int32_t problems, const int32_t* labels,
                              const uint64_t* seeds, const uint64_t* cv_seeds,
                              const kgb_core_options* opt, kgb_core_result* out);
+
+/* PLS options (kodama.hpp:177-188 PLSOptions / CorePLSLDAOptions). */
+typedef struct kgb_pls_options {
+  int32_t folds;             /* cv.folds (default 10) */
+  int32_t stratified;        /* cv.stratified (default 1) */
+  int32_t max_components;    /* default 10 */
+  int32_t fixed_components;  /* default 0 = evaluate max_components */
+  int32_t center;            /* default 1 */
+  int32_t scale;             /* default 1 */
+  int32_t device;
+  int32_t reserved;
+  uint64_t cv_seed;          /* cv.seed (default 1) */
+} kgb_pls_options;
+
+/* Replaces PLSLDACV_CUDA (kodama.hpp:920; CPU semantics of run_plscv_host,
+ * plscv.cpp:2293-2507): cross-validated PLS-LDA predictions of `labels` from
+ * x (n x p).  constrain may be NULL.  accuracy_by_components has
+ * max_components entries (only the selected one is non-zero, as in the
+ * reference). */
+int kgb_plsldacv(const float* x, int32_t n, int32_t p, const int32_t* labels, const int32_t* constrain,
+                 const kgb_pls_options* opt, int32_t* predicted, int32_t* fold_assignments,
+                 int32_t* selected_components, double* accuracy_by_components);
+
+/* Replaces PLSLDAPredict_CUDA (kodama.hpp:941; CPU semantics
+ * plscv.cpp:2976-3005): fit PLS-LDA on train (n x p, labels) and predict
+ * test (nt x p). */
+int kgb_plslda_predict(const float* train, int32_t n, int32_t p, const int32_t* labels, const float* test,
+                       int32_t nt, const kgb_pls_options* opt, int32_t* predicted);
+
+/* Replaces CorePLSLDA_CUDA (kodama.hpp:1002; CPU semantics core.cpp:1626-1646):
+ * label evolution with PLSLDACV as the predictor.  Non-stratified folds only
+ * (the fold cache of plscv.cpp:593-667 applies); constrain / fixed may be NULL. */
+int kgb_core_plslda(const float* x, int32_t n, int32_t p, const int32_t* labels, const int32_t* constrain,
+                    const int32_t* fixed, const kgb_core_options* opt, const kgb_pls_options* pls,
+                    kgb_core_result* out);
 
 /* Exact kNN graph on the device: for each row its K nearest other rows by
  * squared Euclidean distance (float32, coordinate order, no FMA), ties by

@@ -11,6 +11,9 @@ library; there is no CPU fallback.
     CoreKNNGraph_batch(...)             M independent CoreKNNGraph problems, one launch
     knn_graph(x, K)                     exact kNN graph (native_cuda_exact_knn_search)
     KODAMADissimilarityInPlace(...)     KODAMADissimilarityInPlace(backend=CUDA)
+    PLSLDACV(x, labels, ...)            PLSLDACV_CUDA
+    PLSLDAPredict(train, labels, test)  PLSLDAPredict_CUDA
+    CorePLSLDA(x, labels, ...)          CorePLSLDA_CUDA
 """
 
 from __future__ import annotations
@@ -23,7 +26,7 @@ import numpy as np
 from . import _native as N
 
 __all__ = ["KODAMA_matrix", "CoreKNNGraph", "CoreKNNGraph_batch", "knn_graph",
-           "KODAMADissimilarityInPlace", "MatrixResult", "CoreResult", "EvolutionPolicy",
+           "KODAMADissimilarityInPlace", "PLSLDACV", "PLSLDAPredict", "CorePLSLDA", "PLSCVResult", "MatrixResult", "CoreResult", "EvolutionPolicy",
            "library_path", "version", "launch_count"]
 
 
@@ -89,6 +92,7 @@ class MatrixResult:
     effective_landmarks: int
     timings: dict = field(default_factory=dict)
     kernel_ms: dict = field(default_factory=dict)
+    pls_counters: np.ndarray | None = None   # (runs, 2): PLS coarsening attempted / accepted
 
 
 _TIMING_NAMES = ("total", "knn_graph", "shared_landmark_partition", "landmark_initialization",
@@ -98,11 +102,13 @@ _KERNEL_NAMES = ("knn_graph", "atlas_kmeans", "landmark_kmeans", "vote_tables", 
 
 
 def _matrix_options(runs, cycles, landmarks, splitting, graph_neighbors, folds, knn_k, seed,
-                    materialize_graph, apply_dissimilarity, device, host_threads, policy, first_run=1):
+                    materialize_graph, apply_dissimilarity, device, host_threads, policy, first_run=1,
+                    classifier=0, components=50):
     pol = policy if isinstance(policy, EvolutionPolicy) else EvolutionPolicy.from_name(policy or "full")
     return N.MatrixOptions(runs=runs, cycles=cycles, landmarks=landmarks, splitting=splitting,
-                           graph_neighbors=graph_neighbors, folds=folds, knn_k=knn_k, classifier=0,
-                           components=50, materialize_graph=int(materialize_graph),
+                           graph_neighbors=graph_neighbors, folds=folds, knn_k=knn_k,
+                           classifier=classifier, components=components,
+                           materialize_graph=int(materialize_graph),
                            apply_dissimilarity=int(apply_dissimilarity), metric=2, device=device,
                            host_threads=host_threads, first_run=first_run, reserved=0, seed=seed,
                            policy=pol._c())
@@ -111,8 +117,10 @@ def _matrix_options(runs, cycles, landmarks, splitting, graph_neighbors, folds, 
 def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitting=0,
                   graph_neighbors=100, folds=5, knn_k=30, seed=1234, materialize_graph=False,
                   apply_dissimilarity=True, index_base=-1, device=0, host_threads=0,
-                  policy="full", res_out=None, first_run=1) -> MatrixResult:
-    """KODAMA.matrix with the kNN classifier on the GPU.
+                  policy="full", res_out=None, first_run=1, classifier="knn",
+                  components=50) -> MatrixResult:
+    """KODAMA.matrix on the GPU with the kNN (``classifier="knn"``) or PLS-LDA
+    (``classifier="pls"``, ``components`` latent components) classifier.
 
     ``graph`` = (indices, distances) of shape (n, K) runs the graph-input path
     (KODAMAMatrixFromGraphData_CUDA); without it the exact kNN graph is built
@@ -134,14 +142,19 @@ def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitt
         if x.ndim != 2:
             raise ValueError("x must be a 2-D matrix")
         n, d = x.shape
+    cls = {"knn": 0, "pls": 1, "pls-lda": 1, 0: 0, 1: 1}.get(classifier)
+    if cls is None:
+        raise ValueError("Unsupported KODAMA.matrix classifier.")
     opt = _matrix_options(runs, cycles, landmarks, splitting, graph_neighbors, folds, knn_k, seed,
-                          materialize_graph, apply_dissimilarity, device, host_threads, policy, first_run)
+                          materialize_graph, apply_dissimilarity, device, host_threads, policy, first_run,
+                          cls, components)
     res = np.zeros((runs, n), np.int32)
     acc = np.zeros(runs, np.float64)
     v = np.zeros((runs, max(cycles, 0)), np.float64)
     hashes = np.zeros((runs, 3), np.uint64)
     counters = np.zeros((runs, 8), np.int32)
     cdiag = np.zeros((runs, max(cycles, 0), 5), np.int32)
+    plsc = np.zeros((runs, 2), np.int32)
     cap = max(1, graph_neighbors if graph is None else np.asarray(graph[0]).shape[1])
     kidx = np.zeros((n, cap), np.int32) if materialize_graph else None
     kdist = np.zeros((n, cap), np.float32) if materialize_graph else None
@@ -158,6 +171,7 @@ def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitt
     out.run_hashes = hashes.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))
     out.run_counters = counters.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
     out.cycle_diag = cdiag.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+    out.pls_counters = plsc.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
     if materialize_graph:
         out.knn_idx = kidx.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
         out.knn_dist = kdist.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
@@ -183,7 +197,7 @@ def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitt
         knn_dist=kdist[:, :k].copy() if (materialize_graph and k) else None,
         effective_landmarks=out.effective_landmarks,
         timings=dict(zip(_TIMING_NAMES, list(out.timings))),
-        kernel_ms=dict(zip(_KERNEL_NAMES, list(out.kernel_ms))))
+        kernel_ms=dict(zip(_KERNEL_NAMES, list(out.kernel_ms))), pls_counters=plsc)
 
 
 def launch_count() -> int:
@@ -215,7 +229,7 @@ def _core_options(cycles, k, folds, stratified, evolutionary_search, guarded_div
                          guarded_diversity=int(guarded_diversity),
                          many_to_one_absorption=int(many_to_one_absorption),
                          adaptive_proposal_size=int(adaptive_proposal_size), device=device,
-                         reserved=0, seed=seed, cv_seed=cv_seed, policy=pol._c())
+                         auto_class_coarsening=0, seed=seed, cv_seed=cv_seed, policy=pol._c())
 
 
 def _alloc_core(samples, cycles):
@@ -314,3 +328,76 @@ def KODAMADissimilarityInPlace(graph_idx: np.ndarray, graph_dist: np.ndarray, ru
     samples, gk = graph_idx.shape
     N.check(N.load().kgb_dissimilarity_inplace(_ptr(graph_idx), _ptr(graph_dist), samples, gk, _ptr(res),
                                                res.shape[0], device))
+
+
+def _pls_options(folds, stratified, max_components, fixed_components, center, scale, cv_seed, device):
+    return N.PlsOptions(folds=folds, stratified=int(stratified), max_components=max_components,
+                        fixed_components=fixed_components, center=int(center), scale=int(scale),
+                        device=device, reserved=0, cv_seed=cv_seed)
+
+
+@dataclass
+class PLSCVResult:
+    """The PLSCVResult fields of the path (kodama.hpp:263-275)."""
+    predicted_labels: np.ndarray
+    fold_assignments: np.ndarray
+    selected_components: int
+    accuracy_by_components: np.ndarray
+    global_accuracy: float
+
+
+def PLSLDACV(x, labels, *, constrain=None, folds=10, stratified=True, max_components=10,
+             fixed_components=0, center=True, scale=True, cv_seed=1, device=0) -> PLSCVResult:
+    """PLSLDACV: cross-validated PLS-LDA predictions (plscv.cpp:2920)."""
+    xa = np.ascontiguousarray(x, dtype=np.float32)
+    n, p = xa.shape
+    lab = np.ascontiguousarray(labels, dtype=np.int32)
+    con = None if constrain is None else np.ascontiguousarray(constrain, dtype=np.int32)
+    pred = np.zeros(n, np.int32)
+    fo = np.zeros(n, np.int32)
+    sel = ctypes.c_int32(0)
+    abc = np.zeros(max(1, max_components), np.float64)
+    opt = _pls_options(folds, stratified, max_components, fixed_components, center, scale, cv_seed, device)
+    N.check(N.load().kgb_plsldacv(_ptr(xa), n, p, _ptr(lab), _ptr(con), ctypes.byref(opt), _ptr(pred),
+                                  _ptr(fo), ctypes.byref(sel), _ptr(abc)))
+    return PLSCVResult(pred, fo, int(sel.value), abc, float(np.mean(pred == lab)))
+
+
+def PLSLDAPredict(train, labels, test, *, max_components=10, fixed_components=0, center=True,
+                  scale=True, device=0) -> np.ndarray:
+    """PLSLDAPredict: fit on (train, labels), predict test (plscv.cpp:3068)."""
+    tr = np.ascontiguousarray(train, dtype=np.float32)
+    te = np.ascontiguousarray(test, dtype=np.float32)
+    n, p = tr.shape
+    if te.ndim != 2 or te.shape[1] != p:
+        raise ValueError("PLSLDAPredict train/test column mismatch.")
+    if len(labels) != n:
+        raise ValueError("PLSLDAPredict labels size must match training rows.")
+    lab = np.ascontiguousarray(labels, dtype=np.int32)
+    out = np.zeros(te.shape[0], np.int32)
+    opt = _pls_options(2, False, max_components, fixed_components, center, scale, 1, device)
+    N.check(N.load().kgb_plslda_predict(_ptr(tr), n, p, _ptr(lab), _ptr(te), te.shape[0],
+                                        ctypes.byref(opt), _ptr(out)))
+    return out
+
+
+def CorePLSLDA(x, labels, *, constrain=None, fixed=None, cycles=100, folds=10, stratified=False,
+               max_components=10, fixed_components=0, center=True, scale=True,
+               evolutionary_search=False, guarded_diversity=False, many_to_one_absorption=False,
+               adaptive_proposal_size=True, auto_class_coarsening=False, seed=1, cv_seed=1,
+               device=0, policy="full") -> CoreResult:
+    """CorePLSLDA: label evolution with PLSLDACV as the predictor (core.cpp:1626).
+    counters has 18 entries: CoreResult's 16, then PLS coarsening attempted / accepted."""
+    xa = np.ascontiguousarray(x, dtype=np.float32)
+    n, p = xa.shape
+    lab = np.ascontiguousarray(labels, dtype=np.int32)
+    con = None if constrain is None else np.ascontiguousarray(constrain, dtype=np.int32)
+    fix = None if fixed is None else np.ascontiguousarray(fixed, dtype=np.int32)
+    opt = _core_options(cycles, 1, folds, stratified, evolutionary_search, guarded_diversity,
+                        many_to_one_absorption, adaptive_proposal_size, seed, cv_seed, device, policy)
+    opt.auto_class_coarsening = int(auto_class_coarsening)
+    popt = _pls_options(folds, stratified, max_components, fixed_components, center, scale, cv_seed, device)
+    r, bufs = _alloc_core(n, cycles)
+    N.check(N.load().kgb_core_plslda(_ptr(xa), n, p, _ptr(lab), _ptr(con), _ptr(fix), ctypes.byref(opt),
+                                     ctypes.byref(popt), ctypes.byref(r)))
+    return _wrap_core(r, bufs, cycles)

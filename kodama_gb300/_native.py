@@ -22,6 +22,9 @@ EXPORTED = (
     "kgb_launch_count",
     "kgb_core_knn_graph",
     "kgb_core_knn_graph_batch",
+    "kgb_plsldacv",
+    "kgb_plslda_predict",
+    "kgb_core_plslda",
     "kgb_knn_graph",
     "kgb_dissimilarity_inplace",
     "kgb_dissimilarity_inplace_device",
@@ -61,13 +64,14 @@ class MatrixResult(ctypes.Structure):
         ("kernel_ms", ctypes.c_double * 8),
         ("res_on_device", ctypes.c_int32),
         ("reserved", ctypes.c_int32),
+        ("pls_counters", ctypes.POINTER(ctypes.c_int32)),
     ]
 
 
 class CoreOptions(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int32) for n in (
         "cycles", "k", "folds", "stratified", "evolutionary_search", "guarded_diversity",
-        "many_to_one_absorption", "adaptive_proposal_size", "device", "reserved")] + [
+        "many_to_one_absorption", "adaptive_proposal_size", "device", "auto_class_coarsening")] + [
         ("seed", ctypes.c_uint64), ("cv_seed", ctypes.c_uint64), ("policy", Policy)]
 
 
@@ -83,8 +87,14 @@ class CoreResult(ctypes.Structure):
         ("flags", ctypes.POINTER(ctypes.c_uint8)),
         ("accbest", ctypes.c_double),
         ("scorebest", ctypes.c_double),
-        ("counters", ctypes.c_int32 * 16),
+        ("counters", ctypes.c_int32 * 18),
     ]
+
+
+class PlsOptions(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int32) for n in (
+        "folds", "stratified", "max_components", "fixed_components", "center", "scale", "device",
+        "reserved")] + [("cv_seed", ctypes.c_uint64)]
 
 
 _lib = None
@@ -115,6 +125,10 @@ def load():
                                              ctypes.POINTER(CoreResult)]
     lib.kgb_knn_graph.argtypes = [P, i32, i32, i32, i32, P, P]
     lib.kgb_dissimilarity_inplace.argtypes = [P, P, i32, i32, P, i32, i32]
+    lib.kgb_plsldacv.argtypes = [P, i32, i32, P, P, ctypes.POINTER(PlsOptions), P, P, P, P]
+    lib.kgb_plslda_predict.argtypes = [P, i32, i32, P, P, i32, ctypes.POINTER(PlsOptions), P]
+    lib.kgb_core_plslda.argtypes = [P, i32, i32, P, P, P, ctypes.POINTER(CoreOptions),
+                                    ctypes.POINTER(PlsOptions), ctypes.POINTER(CoreResult)]
     lib.kgb_dissimilarity_inplace_device.argtypes = [P, P, i32, i32, P, i32, i32, P]
     lib.kgb_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     lib.kgb_version.restype = ctypes.c_char_p

@@ -11,6 +11,7 @@
 #include "kmeans.cuh"
 #include "knn.cuh"
 #include "launch_count.cuh"
+#include "pls.cuh"
 
 #include <cuda_runtime.h>
 
@@ -21,7 +22,9 @@
 #include <cstring>
 #include <exception>
 #include <future>
+#include <limits>
 #include <map>
+#include <random>
 #include <stdexcept>
 #include <string>
 #include <thread>
@@ -355,13 +358,308 @@ EvolveBuffers run_evolution(Ctx& ctx, kgb::EvolveParams P, int C0max) {
   return b;
 }
 
+// ---------------------------------------------------------------------------
+// PLS-LDA (pls.cu): fold slices, device buffers, the evolution cycle loop
+// ---------------------------------------------------------------------------
+
+// The SIMPLS start vector (plscv.cpp:833-838): the reference's own engine and
+// distribution from the same libstdc++, hence the same floats.
+std::vector<float> pls_start_vector(int p) {
+  std::mt19937 gen(1u);
+  std::normal_distribution<float> nd(0.0f, 1.0f);
+  std::vector<float> w(static_cast<size_t>(p));
+  for (float& v : w) v = nd(gen);
+  return w;
+}
+
+// Slices of R problems of L rows: fold ids renumbered densely per problem (the
+// reference visits only the fold ids that occur), training and validation
+// rows of each slice ascending.  Predict mode: one slice per problem, every
+// row trains.
+struct PlsSlices {
+  int F = 1;
+  std::vector<int> train_off, train_idx, val_off, val_idx, ntrain, present;
+  std::vector<uint8_t> folds8;
+};
+
+PlsSlices pls_slices(const std::vector<std::vector<int>>& folds, int R, int L, bool predict) {
+  PlsSlices sl;
+  std::vector<std::vector<int>> dense(static_cast<size_t>(R));
+  std::vector<int> nf(static_cast<size_t>(R), 1);
+  if (!predict) {
+    sl.F = 0;
+    for (int r = 0; r < R; ++r) {
+      std::vector<int> ids = folds[r];
+      std::sort(ids.begin(), ids.end());
+      ids.erase(std::unique(ids.begin(), ids.end()), ids.end());
+      nf[r] = static_cast<int>(ids.size());
+      sl.F = std::max(sl.F, nf[r]);
+      dense[r].resize(static_cast<size_t>(L));
+      for (int i = 0; i < L; ++i)
+        dense[r][i] = static_cast<int>(std::lower_bound(ids.begin(), ids.end(), folds[r][i]) - ids.begin());
+    }
+    if (sl.F > 255) fail(KGB_EINVAL, "at most 255 folds are supported");
+    sl.folds8.resize(static_cast<size_t>(R) * L);
+  }
+  sl.train_off.push_back(0);
+  sl.val_off.push_back(0);
+  for (int r = 0; r < R; ++r) {
+    for (int f = 0; f < sl.F; ++f) {
+      for (int i = 0; i < L; ++i) {
+        const bool val = !predict && dense[r][i] == f;
+        (val ? sl.val_idx : sl.train_idx).push_back(i);
+      }
+      sl.train_off.push_back(static_cast<int>(sl.train_idx.size()));
+      sl.val_off.push_back(static_cast<int>(sl.val_idx.size()));
+      sl.ntrain.push_back(sl.train_off.back() - sl.train_off[sl.train_off.size() - 2]);
+      sl.present.push_back(f < nf[r] ? 1 : 0);
+    }
+    if (!predict)
+      for (int i = 0; i < L; ++i) sl.folds8[static_cast<size_t>(r) * L + i] = static_cast<uint8_t>(dense[r][i]);
+  }
+  return sl;
+}
+
+struct PlsBuffers {
+  kgb::PlsPrepArgs prep{};
+  kgb::PlsEvalArgs ev{};
+  int S = 0;
+  std::vector<int> ntrain, present;
+};
+
+// Statistics, standardised rows and evaluation scratch of a set of slices.
+// d_X: R x L x p rows; d_Xv: R x NV x p rows to predict (predict mode) or null.
+PlsBuffers pls_buffers(Ctx& ctx, const float* d_X, int R, int L, int p, const PlsSlices& sl, int C0max,
+                       int max_components, int requested, bool center, bool scale, const float* d_Xv, int NV) {
+  PlsBuffers b;
+  const int F = sl.F, S = R * F;
+  b.S = S;
+  b.ntrain = sl.ntrain;
+  b.present = sl.present;
+  if (kgb::pls_eval_smem(p, C0max, requested) > 200 * 1024)
+    fail(KGB_EINVAL, "too many features, classes or components for the PLS-LDA kernel");
+  cudaStream_t st = ctx.stream();
+  kgb::PlsPrepArgs& a = b.prep;
+  a.problems = R;
+  a.F = F;
+  a.L = L;
+  a.p = p;
+  a.center = center;
+  a.scale = scale;
+  a.X = d_X;
+  int* d_toff = ctx.upload(sl.train_off.data(), sl.train_off.size());
+  int* d_tidx = sl.train_idx.empty() ? ctx.alloc<int>(1) : ctx.upload(sl.train_idx.data(), sl.train_idx.size());
+  a.train_off = d_toff;
+  a.train_idx = d_tidx;
+  a.mean = ctx.alloc<float>(static_cast<size_t>(S) * p);
+  a.sdev = ctx.alloc<float>(static_cast<size_t>(S) * p);
+  a.Z = ctx.alloc<float>(static_cast<size_t>(S) * L * p);
+  a.xsum = ctx.alloc<float>(static_cast<size_t>(S) * p);
+  a.Xv = d_Xv;
+  a.NV = NV;
+  a.Zv = d_Xv != nullptr ? ctx.alloc<float>(static_cast<size_t>(R) * NV * p) : nullptr;
+  a.gram = nullptr;
+  ck_launch(kgb::pls_prepare(a, st), "PLS fold preparation");
+
+  kgb::PlsEvalArgs& e = b.ev;
+  e.problems = R;
+  e.F = F;
+  e.L = L;
+  e.p = p;
+  e.C0max = C0max;
+  e.max_components = max_components;
+  e.requested = requested;
+  e.predict_mode = d_Xv != nullptr;
+  e.Z = a.Z;
+  e.xsum = a.xsum;
+  e.gram = nullptr;
+  e.use_gram = ctx.alloc<uint8_t>(S);
+  ck(cudaMemsetAsync(const_cast<uint8_t*>(e.use_gram), 0, S, st), "memset");
+  e.folds = e.predict_mode ? nullptr : ctx.upload(sl.folds8.data(), sl.folds8.size());
+  e.train_off = d_toff;
+  e.train_idx = d_tidx;
+  e.val_off = ctx.upload(sl.val_off.data(), sl.val_off.size());
+  e.val_idx = sl.val_idx.empty() ? ctx.alloc<int>(1) : ctx.upload(sl.val_idx.data(), sl.val_idx.size());
+  e.Zv = a.Zv;
+  e.NV = NV;
+  const std::vector<float> w0 = pls_start_vector(p);
+  e.w0 = ctx.upload(w0.data(), w0.size());
+  // logf(max(k / nt, FLT_MIN)) for every count k of a class of the slice
+  std::map<int, int> table_of;
+  std::vector<float> tables;
+  std::vector<int> lp_off(static_cast<size_t>(S));
+  for (int s2 = 0; s2 < S; ++s2) {
+    const int nt = sl.ntrain[s2];
+    auto it = table_of.find(nt);
+    if (it == table_of.end()) {
+      it = table_of.emplace(nt, static_cast<int>(tables.size())).first;
+      const float den = static_cast<float>(std::max(1, nt));
+      for (int k = 0; k <= nt; ++k)
+        tables.push_back(std::log(std::max(static_cast<float>(k) / den, std::numeric_limits<float>::min())));
+    }
+    lp_off[s2] = it->second;
+  }
+  e.logprior = ctx.upload(tables.data(), tables.size());
+  e.lp_off = ctx.upload(lp_off.data(), lp_off.size());
+  e.pred = ctx.alloc<uint16_t>(static_cast<size_t>(R) * (e.predict_mode ? NV : L));
+  e.eval_comp = ctx.alloc<int>(S);
+  e.status = ctx.alloc<int>(S);
+  e.s_scr = ctx.alloc<float>(static_cast<size_t>(S) * p * C0max);
+  e.W = ctx.alloc<float>(static_cast<size_t>(S) * p * max_components);
+  e.V = ctx.alloc<float>(static_cast<size_t>(S) * p * max_components);
+  e.T = ctx.alloc<float>(static_cast<size_t>(S) * L * requested);
+  e.sc = ctx.alloc<float>(static_cast<size_t>(S) * L);
+  return b;
+}
+
+// Builds the fold Gram matrices (slices with at least p training rows) and
+// switches the evaluation to the Gram loadings, as the reference's fold cache
+// does from the second evaluation of a data epoch on.
+void pls_enable_gram(Ctx& ctx, PlsBuffers& b) {
+  const int S = b.S, p = b.prep.p;
+  std::vector<uint8_t> want(static_cast<size_t>(S));
+  for (int s2 = 0; s2 < S; ++s2) want[s2] = p <= b.ntrain[s2] ? 1 : 0;
+  uint8_t* d_want = const_cast<uint8_t*>(b.ev.use_gram);
+  ck(cudaMemcpyAsync(d_want, want.data(), want.size(), cudaMemcpyHostToDevice, ctx.stream()), "H2D");
+  b.prep.gram = ctx.alloc<float>(static_cast<size_t>(S) * p * p);
+  ck_launch(kgb::pls_build_gram(b.prep, d_want, ctx.stream()), "fold Gram");
+  b.ev.gram = b.prep.gram;
+  ctx.sync();  // `want` is a host temporary
+}
+
+// Host class lists of coded labels: rows grouped by code, ascending within.
+void class_lists_host(const std::vector<uint16_t>& codes, int C0max, std::vector<int>& off,
+                      std::vector<uint16_t>& rows) {
+  off.assign(static_cast<size_t>(C0max) + 1, 0);
+  for (uint16_t c : codes) off[c + 1]++;
+  for (int c = 0; c < C0max; ++c) off[c + 1] += off[c];
+  std::vector<int> pos(off.begin(), off.end() - 1);
+  rows.resize(codes.size());
+  for (size_t i = 0; i < codes.size(); ++i) rows[pos[codes[i]]++] = static_cast<uint16_t>(i);
+}
+
+void pls_check_status(Ctx& ctx, const PlsBuffers& b) {
+  std::vector<int> status(static_cast<size_t>(b.S));
+  ctx.download(status.data(), b.ev.status, status.size());
+  ctx.sync();
+  for (int s2 = 0; s2 < b.S; ++s2) {
+    if (!b.present[s2]) continue;
+    if (status[s2] == 1) fail(KGB_EINTERNAL, "CPU float32 SIMPLS found no supervised latent direction.");
+    if (status[s2] == 2) fail(KGB_EINTERNAL, "Float32 PLS-LDA Cholesky factorization failed.");
+  }
+}
+
+// maximize_core with the PLS-LDA predictor for P.problems problems whose
+// slices are in `b`: the cycle loop of alternating evolution steps and CV
+// evaluations.  P carries everything but the outputs and scratch.
+EvolveBuffers run_pls_evolution(Ctx& ctx, kgb::EvolveParams P, PlsBuffers& b, int C0max, bool coarsening,
+                                const kgb_policy& pol) {
+  const int problems = P.problems, L = P.L, T = P.T;
+  cudaStream_t st = ctx.stream();
+  EvolveBuffers eb;
+  eb.clbest = ctx.alloc<uint16_t>(static_cast<size_t>(problems) * L);
+  eb.cvpredbest = ctx.alloc<uint16_t>(static_cast<size_t>(problems) * L);
+  eb.vect_acc = ctx.alloc<double>(static_cast<size_t>(problems) * std::max(T, 1));
+  eb.vect_score = ctx.alloc<double>(static_cast<size_t>(problems) * std::max(T, 1));
+  eb.psize = ctx.alloc<int>(static_cast<size_t>(problems) * std::max(T, 1));
+  eb.active = ctx.alloc<int>(static_cast<size_t>(problems) * std::max(T, 1));
+  eb.flags = ctx.alloc<uint8_t>(static_cast<size_t>(problems) * std::max(T, 1) * 3);
+  eb.counters = ctx.alloc<int>(static_cast<size_t>(problems) * 18);
+  eb.best = ctx.alloc<double>(static_cast<size_t>(problems) * 2);
+  eb.status = ctx.alloc<int>(static_cast<size_t>(problems));
+  P.clbest = eb.clbest;
+  P.cvpredbest = eb.cvpredbest;
+  P.vect_acc = eb.vect_acc;
+  P.vect_score = eb.vect_score;
+  P.proposal_size = eb.psize;
+  P.active = eb.active;
+  P.flags = eb.flags;
+  P.counters = eb.counters;
+  P.best = eb.best;
+  P.status = eb.status;
+  P.C0max = C0max;
+  P.w = 1;
+  P.trans = ctx.alloc<int>(static_cast<size_t>(problems) * C0max * C0max);
+  const int grid = problems;
+  constexpr size_t kSmemBudget = 200 * 1024;
+  const size_t Lp = (static_cast<size_t>(L) + 7) / 8 * 8;
+  bool placed = false;
+  size_t smem = 0;
+  for (int option = 0; option < 4 && !placed; ++option) {
+    const bool rows = option < 2;
+    const bool trans = (option % 2) == 0;
+    smem = kgb::evolve_smem_bytes(L, C0max, rows, trans, false);
+    if (smem <= kSmemBudget) {
+      placed = true;
+      P.smem_rows = rows;
+      P.smem_hist = 0;
+      P.smem_trans = trans;
+    }
+  }
+  if (!placed) fail(KGB_EINVAL, "too many distinct labels for the evolution kernel");
+  P.rows_scratch = P.smem_rows ? nullptr
+                               : ctx.alloc<uint16_t>(static_cast<size_t>(grid) * kgb::kEvolveRowArrays * Lp);
+  P.raw_scratch = ctx.alloc<uint64_t>(static_cast<size_t>(grid) * (L / 2 + 64));
+  if (P.smem_trans) P.trans = nullptr;
+  {
+    std::vector<double> psq(static_cast<size_t>(L) + 1);
+    const double nd = static_cast<double>(L);
+    for (int c = 0; c <= L; ++c) {
+      const double q = static_cast<double>(c) / nd;
+      psq[c] = q * q;
+    }
+    P.psq = ctx.upload(psq.data(), psq.size());
+  }
+  kgb::EvolvePlsParams Q{};
+  Q.base = P;
+  Q.state = ctx.alloc<kgb::PlsRunState>(problems);
+  Q.rng = ctx.alloc<kgb::Mt64State>(problems);
+  Q.cur = ctx.alloc<uint16_t>(static_cast<size_t>(problems) * L);
+  Q.curpred = ctx.alloc<uint16_t>(static_cast<size_t>(problems) * L);
+  Q.cl = ctx.alloc<uint16_t>(static_cast<size_t>(problems) * L);
+  Q.pred = b.ev.pred;
+  Q.class_off = ctx.alloc<int>(static_cast<size_t>(problems) * (C0max + 1));
+  Q.class_rows = ctx.alloc<uint16_t>(static_cast<size_t>(problems) * L);
+  {
+    // entropy terms p*log(p), p = k/L, rounded as core_objective_score does
+    std::vector<double> plogp(static_cast<size_t>(L) + 1, 0.0);
+    const double nd = static_cast<double>(L);
+    for (int k = 1; k <= L; ++k) {
+      const double q = static_cast<double>(k) / nd;
+      plogp[k] = q * std::log(q);
+    }
+    Q.plogp = ctx.upload(plogp.data(), plogp.size());
+    Q.logn = std::log(nd);
+  }
+  Q.coarsening = coarsening;
+  Q.pol_coarsen = pol.pls_transition_coarsening != 0;
+  Q.pol_frag = pol.pls_fragmentation_penalty != 0;
+  b.ev.labels = Q.cl;
+  b.ev.class_off = Q.class_off;
+  b.ev.class_rows = Q.class_rows;
+  Q.phase = 0;
+  Q.cycle = 0;
+  ck_launch(kgb::evolve_pls_launch(Q, grid, smem, st), "PLS evolution step");
+  for (int cycle = 0; cycle <= T; ++cycle) {
+    if (cycle == 1) pls_enable_gram(ctx, b);
+    ck_launch(kgb::pls_evaluate(b.ev, st), "PLS-LDA evaluation");
+    Q.phase = 1;
+    Q.cycle = cycle;
+    ck_launch(kgb::evolve_pls_launch(Q, grid, smem, st), "PLS evolution step");
+  }
+  pls_check_status(ctx, b);
+  // leave the best labels' class lists in b.ev for a projection
+  b.ev.labels = eb.clbest;
+  return eb;
+}
+
+
 void validate_matrix_options(const kgb_matrix_options* o) {
   if (o == nullptr) fail(KGB_EINVAL, "options pointer is null");
   if (o->runs < 1) fail(KGB_EINVAL, "KODAMAMatrixOptions::runs must be positive.");
   if (o->cycles < 0) fail(KGB_EINVAL, "KODAMAMatrixOptions::cycles must be non-negative.");
   if (o->folds < 2) fail(KGB_EINVAL, "KODAMAMatrixOptions::folds must be at least two.");
   if (o->folds > 255) fail(KGB_EINVAL, "at most 255 folds are supported");
-  if (o->classifier != 0) fail(KGB_EINVAL, "only the kNN classifier is implemented by this entry point");
   if (o->metric != 2 && o->metric != 0) fail(KGB_EINVAL, "only the Euclidean metric is supported");
 }
 
@@ -380,8 +678,11 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   const uint64_t seed = o->seed;
   const int knn_k = std::max(o->knn_k, 1);
   const int w = std::max(1, std::min(knn_k, K));
-  if (w > 32) fail(KGB_EINVAL, "knn.k above 32 is not supported by the vote kernel");
-  if (knn_k > kgb::kMaxProjectK) fail(KGB_EINVAL, "knn.k too large for the projection kernel");
+  const bool pls = o->classifier == 1;
+  if (o->classifier != 0 && o->classifier != 1) fail(KGB_EINVAL, "Unsupported KODAMA.matrix classifier.");
+  if (!pls && w > 32) fail(KGB_EINVAL, "knn.k above 32 is not supported by the vote kernel");
+  if (!pls && knn_k > kgb::kMaxProjectK) fail(KGB_EINVAL, "knn.k too large for the projection kernel");
+  if (pls && o->components < 1) fail(KGB_EINVAL, "PLSOptions::max_components must be positive.");
   cudaStream_t st = ctx.stream();
 
   // shared landmark atlas (kodama_matrix.cpp:3662-3734)
@@ -505,6 +806,92 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   out->timings[3] = clk.lap();
 
   const int ev_init = ctx.mark();
+  std::vector<uint64_t> seeds(static_cast<size_t>(M));
+  for (int r = 0; r < M; ++r) seeds[r] = seed + static_cast<uint64_t>(r0 + r);
+  std::vector<int> identity(static_cast<size_t>(L));
+  for (int i = 0; i < L; ++i) identity[i] = i;
+  std::vector<int> goff(static_cast<size_t>(L) + 1);
+  for (int i = 0; i <= L; ++i) goff[i] = i;
+  kgb::EvolveParams P{};
+  P.problems = M;
+  P.L = L;
+  P.w = w;
+  P.T = T;
+  P.F = F;
+  P.G = L;
+  P.singleton = 1;
+  P.evolutionary = 1;
+  P.guarded = 1;
+  P.absorption = 1;
+  P.adaptive = 1;
+  P.pol_guidance = pol.prediction_guidance != 0;
+  P.pol_adaptive = pol.adaptive_proposal_size != 0;
+  P.pol_transition = pol.transition_proposal != 0;
+  P.pol_stochastic = pol.stochastic_acceptance != 0;
+  P.pol_diversity = pol.diversity_multiplier != 0;
+  P.pol_reject1 = pol.reject_single_class != 0;
+  P.bucket_count = bc;
+  P.init = d_codes;
+  P.code2label = d_c2l;
+  P.ncodes = d_ncodes;
+  P.nocollide = ctx.upload(nocol.data(), nocol.size());
+  P.folds = d_folds;
+  P.fixed = nullptr;
+  P.goff = ctx.upload(goff.data(), goff.size());
+  P.gmem = ctx.upload(identity.data(), identity.size());
+  P.seeds = ctx.upload(seeds.data(), seeds.size());
+  EvolveBuffers eb{};
+  int* d_res = nullptr;
+  int ev_tables = 0, ev_evo0 = 0, ev_evo1 = 0, ev_proj = 0;
+  int cstride = 16;
+  if (pls) {
+    // PLS-LDA classifier (run_iteration, kodama_matrix.cpp:3105-3158, 3262-3276):
+    // CorePLSLDA on the landmark rows of every run, PLSLDAPredict for the rest
+    cstride = 18;
+    const int p = d;
+    float* d_xl = ctx.alloc<float>(static_cast<size_t>(M) * L * p);
+    ck_launch(kgb::pls_gather_rows(d_x, p, d_land, static_cast<size_t>(M) * L, d_xl, st), "landmark rows");
+    std::vector<std::vector<int>> fl(static_cast<size_t>(M));
+    for (int r = 0; r < M; ++r) fl[r].assign(fold_plans[r].folds.begin(), fold_plans[r].folds.end());
+    const PlsSlices sl = pls_slices(fl, M, L, false);
+    const int comps = o->components;
+    PlsBuffers b = pls_buffers(ctx, d_xl, M, L, p, sl, C0max, comps, comps, true, true, nullptr, 0);
+    ev_tables = ctx.mark();
+    ev_evo0 = ev_tables;
+    eb = run_pls_evolution(ctx, P, b, C0max, true, pol);
+    ev_evo1 = ctx.mark();
+    const int NV = n - L;
+    std::vector<int> test_rows(static_cast<size_t>(M) * std::max(NV, 0));
+    for (int r = 0; r < M; ++r) {
+      std::vector<char> is_land(static_cast<size_t>(n), 0);
+      for (int i = 0; i < L; ++i) is_land[land[static_cast<size_t>(r) * L + i]] = 1;
+      size_t q = static_cast<size_t>(r) * NV;
+      for (int t = 0; t < n; ++t)
+        if (!is_land[t]) test_rows[q++] = t;
+    }
+    int* d_test = test_rows.empty() ? ctx.alloc<int>(1) : ctx.upload(test_rows.data(), test_rows.size());
+    d_res = ctx.alloc<int>(static_cast<size_t>(M) * n);
+    uint16_t* d_proj = ctx.alloc<uint16_t>(static_cast<size_t>(M) * std::max(NV, 1));
+    if (NV > 0) {
+      float* d_xt = ctx.alloc<float>(static_cast<size_t>(M) * NV * p);
+      ck_launch(kgb::pls_gather_rows(d_x, p, d_test, static_cast<size_t>(M) * NV, d_xt, st), "test rows");
+      const int ncomp = std::max(1, std::min({comps, p, std::max(1, L - 1)}));
+      const PlsSlices sp = pls_slices({}, M, L, true);
+      PlsBuffers pb = pls_buffers(ctx, d_xl, M, L, p, sp, C0max, ncomp, ncomp, true, true, d_xt, NV);
+      pb.ev.labels = eb.clbest;
+      pb.ev.class_off = b.ev.class_off;
+      pb.ev.class_rows = b.ev.class_rows;
+      ck_launch(kgb::pls_evaluate(pb.ev, st), "PLS-LDA projection");
+      pls_check_status(ctx, pb);
+      d_proj = pb.ev.pred;
+    }
+    ck_launch(kgb::pls_assemble_result(M, n, L, std::max(NV, 0), d_land, d_test, eb.clbest, d_proj, d_c2l, C0max,
+                                       d_res, st),
+              "result rows");
+    ev_proj = ctx.mark();
+    ctx.sync();
+    out->timings[4] = clk.lap();
+  } else {
   // per-run fold-filtered vote tables over the landmark subgraph
   int* d_g2l = ctx.alloc<int>(static_cast<size_t>(M) * n);
   ck_launch(kgb::build_g2l(d_land, M, L, n, d_g2l, st), "landmark index");
@@ -526,50 +913,15 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     a.sc = d_sc;
     ck_launch(kgb::build_vote_tables(a, st), "vote tables");
   }
-  const int ev_tables = ctx.mark();
-  std::vector<int> identity(static_cast<size_t>(L));
-  for (int i = 0; i < L; ++i) identity[i] = i;
-  std::vector<int> goff(static_cast<size_t>(L) + 1);
-  for (int i = 0; i <= L; ++i) goff[i] = i;
-  std::vector<uint64_t> seeds(static_cast<size_t>(M));
-  for (int r = 0; r < M; ++r) seeds[r] = seed + static_cast<uint64_t>(r0 + r);
-
-  kgb::EvolveParams P{};
-  P.problems = M;
-  P.L = L;
-  P.w = w;
-  P.T = T;
-  P.F = F;
-  P.G = L;
-  P.singleton = 1;
-  P.evolutionary = 1;
-  P.guarded = 1;
-  P.absorption = 1;
-  P.adaptive = 1;
-  P.pol_guidance = pol.prediction_guidance != 0;
-  P.pol_adaptive = pol.adaptive_proposal_size != 0;
-  P.pol_transition = pol.transition_proposal != 0;
-  P.pol_stochastic = pol.stochastic_acceptance != 0;
-  P.pol_diversity = pol.diversity_multiplier != 0;
-  P.pol_reject1 = pol.reject_single_class != 0;
-  P.bucket_count = bc;
+  ev_tables = ctx.mark();
   P.nb = d_nb;
   P.sc = d_sc;
-  P.init = d_codes;
-  P.code2label = d_c2l;
-  P.ncodes = d_ncodes;
-  P.nocollide = ctx.upload(nocol.data(), nocol.size());
-  P.folds = d_folds;
-  P.fixed = nullptr;
-  P.goff = ctx.upload(goff.data(), goff.size());
-  P.gmem = ctx.upload(identity.data(), identity.size());
-  P.seeds = ctx.upload(seeds.data(), seeds.size());
-  const int ev_evo0 = ctx.mark();
-  const EvolveBuffers eb = run_evolution(ctx, P, C0max);
-  const int ev_evo1 = ctx.mark();
+  ev_evo0 = ctx.mark();
+  eb = run_evolution(ctx, P, C0max);
+  ev_evo1 = ctx.mark();
 
   // projection of non-landmarks and result matrix
-  int* d_res = ctx.alloc<int>(static_cast<size_t>(M) * n);
+  d_res = ctx.alloc<int>(static_cast<size_t>(M) * n);
   {
     kgb::ProjectArgs a{};
     a.problems = M;
@@ -585,9 +937,10 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     a.res = d_res;
     ck_launch(kgb::project_labels(a, st), "projection");
   }
-  const int ev_proj = ctx.mark();
+  ev_proj = ctx.mark();
   ctx.sync();
   out->timings[4] = clk.lap();
+  }
 
   // outputs
   const size_t res_bytes = sizeof(int) * static_cast<size_t>(M) * n;
@@ -602,7 +955,7 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   ctx.download(best.data(), eb.best, best.size());
   ctx.download(out->v, eb.vect_acc, static_cast<size_t>(M) * T);
   std::vector<int> psize(static_cast<size_t>(M) * T), active(static_cast<size_t>(M) * T),
-      counters(static_cast<size_t>(M) * 16);
+      counters(static_cast<size_t>(M) * cstride);
   std::vector<uint8_t> flags(static_cast<size_t>(M) * T * 3);
   ctx.download(psize.data(), eb.psize, psize.size());
   ctx.download(active.data(), eb.active, active.size());
@@ -675,8 +1028,13 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
       out->run_hashes[3 * r + 1] = init_hash[r];
       out->run_hashes[3 * r + 2] = fold_plans[r].fold_hash;
     }
+    if (out->pls_counters) {
+      const int* c = counters.data() + static_cast<size_t>(r) * cstride;
+      out->pls_counters[2 * r] = pls ? c[16] : 0;
+      out->pls_counters[2 * r + 1] = pls ? c[17] : 0;
+    }
     if (out->run_counters) {
-      const int* c = counters.data() + static_cast<size_t>(r) * 16;
+      const int* c = counters.data() + static_cast<size_t>(r) * cstride;
       int* rc = out->run_counters + 8 * r;
       rc[0] = r0 + r;
       rc[1] = c[0];
@@ -949,7 +1307,8 @@ int kgb_core_knn_graph_batch(const int32_t* gidx, const float* gdist, int32_t sa
       }
       r.accbest = best[2 * p];
       r.scorebest = best[2 * p + 1];
-      std::memcpy(r.counters, counters.data() + static_cast<size_t>(p) * 16, sizeof(r.counters));
+      std::memset(r.counters, 0, sizeof(r.counters));
+      std::memcpy(r.counters, counters.data() + static_cast<size_t>(p) * 16, sizeof(int) * 16);
     }
   });
 }
@@ -1008,6 +1367,207 @@ int kgb_dissimilarity_inplace(int32_t* gidx, float* gdist, int32_t samples, int3
     ctx.download(gidx, d_oidx, total);
     ctx.download(gdist, d_odist, total);
     ctx.sync();
+  });
+}
+
+namespace {
+void check_pls_options(const kgb_pls_options* o) {
+  if (o->max_components < 1) fail(KGB_EINVAL, "PLSOptions::max_components must be positive.");
+  if (o->fixed_components < 0) fail(KGB_EINVAL, "PLSOptions::fixed_components must be non-negative.");
+  if (o->fixed_components > o->max_components)
+    fail(KGB_EINVAL, "PLSOptions::fixed_components cannot exceed max_components.");
+}
+}  // namespace
+
+int kgb_plsldacv(const float* x, int32_t n, int32_t p, const int32_t* labels, const int32_t* constrain,
+                 const kgb_pls_options* opt, int32_t* predicted, int32_t* fold_assignments,
+                 int32_t* selected_components, double* accuracy_by_components) {
+  return guarded([&]() {
+    if (x == nullptr || labels == nullptr || opt == nullptr || predicted == nullptr) fail(KGB_EINVAL, "null pointer");
+    if (n < 1 || p < 1) fail(KGB_EINVAL, "PLSLDACV requires a non-empty matrix.");
+    if (n > 65535) fail(KGB_EINVAL, "at most 65535 rows are supported");
+    check_pls_options(opt);
+    const std::vector<int> lab(labels, labels + n);
+    const std::vector<int> con = constrain ? std::vector<int>(constrain, constrain + n) : std::vector<int>();
+    const std::vector<int> folds = kgb::make_folds(lab, con, opt->folds, opt->stratified != 0, opt->cv_seed);
+    const Coding cd = code_labels(labels, n, 1);
+    const int C0max = std::max(2, static_cast<int>(cd.code2label.size()));
+    const int requested = opt->fixed_components > 0 ? opt->fixed_components : opt->max_components;
+    Ctx ctx(opt->device);
+    const float* d_x = ctx.upload(x, static_cast<size_t>(n) * p);
+    const PlsSlices sl = pls_slices({folds}, 1, n, false);
+    PlsBuffers b = pls_buffers(ctx, d_x, 1, n, p, sl, C0max, opt->max_components, requested, opt->center != 0,
+                               opt->scale != 0, nullptr, 0);
+    std::vector<int> off;
+    std::vector<uint16_t> rows;
+    class_lists_host(cd.codes, C0max, off, rows);
+    b.ev.labels = ctx.upload(cd.codes.data(), cd.codes.size());
+    b.ev.class_off = ctx.upload(off.data(), off.size());
+    b.ev.class_rows = ctx.upload(rows.data(), rows.size());
+    ck_launch(kgb::pls_evaluate(b.ev, ctx.stream()), "PLS-LDA evaluation");
+    std::vector<uint16_t> pc(static_cast<size_t>(n));
+    std::vector<int> comp(static_cast<size_t>(b.S));
+    ctx.download(pc.data(), b.ev.pred, pc.size());
+    ctx.download(comp.data(), b.ev.eval_comp, comp.size());
+    pls_check_status(ctx, b);
+    int evaluated = requested;
+    for (int s2 = 0; s2 < b.S; ++s2)
+      if (b.present[s2]) evaluated = std::min(evaluated, comp[s2]);
+    const int best = std::min(evaluated, opt->max_components);
+    int ok = 0;
+    for (int i = 0; i < n; ++i) {
+      predicted[i] = cd.code2label[pc[i]];
+      ok += predicted[i] == labels[i];
+    }
+    if (fold_assignments) std::copy(folds.begin(), folds.end(), fold_assignments);
+    if (selected_components) *selected_components = best;
+    if (accuracy_by_components) {
+      for (int c = 0; c < opt->max_components; ++c) accuracy_by_components[c] = 0.0;
+      accuracy_by_components[best - 1] = static_cast<double>(ok) / static_cast<double>(n);
+    }
+  });
+}
+
+int kgb_plslda_predict(const float* train, int32_t n, int32_t p, const int32_t* labels, const float* test,
+                       int32_t nt, const kgb_pls_options* opt, int32_t* predicted) {
+  return guarded([&]() {
+    if (train == nullptr || labels == nullptr || opt == nullptr || (nt > 0 && (test == nullptr || predicted == nullptr)))
+      fail(KGB_EINVAL, "PLSLDAPredict input matrix pointer is null.");
+    if (n <= 0 || nt <= 0 || p <= 0) return;
+    if (n > 65535) fail(KGB_EINVAL, "at most 65535 training rows are supported");
+    const Coding cd = code_labels(labels, n, 1);
+    if (cd.code2label.size() == 1) {
+      for (int i = 0; i < nt; ++i) predicted[i] = cd.code2label[0];
+      return;
+    }
+    const int C0max = static_cast<int>(cd.code2label.size());
+    const int requested = opt->fixed_components > 0 ? opt->fixed_components : opt->max_components;
+    const int ncomp = std::max(1, std::min({requested, static_cast<int>(p), std::max(1, static_cast<int>(n) - 1)}));
+    Ctx ctx(opt->device);
+    const float* d_x = ctx.upload(train, static_cast<size_t>(n) * p);
+    const float* d_t = ctx.upload(test, static_cast<size_t>(nt) * p);
+    const PlsSlices sl = pls_slices({}, 1, n, true);
+    PlsBuffers b = pls_buffers(ctx, d_x, 1, n, p, sl, C0max, ncomp, ncomp, opt->center != 0, opt->scale != 0, d_t, nt);
+    std::vector<int> off;
+    std::vector<uint16_t> rows;
+    class_lists_host(cd.codes, C0max, off, rows);
+    b.ev.labels = ctx.upload(cd.codes.data(), cd.codes.size());
+    b.ev.class_off = ctx.upload(off.data(), off.size());
+    b.ev.class_rows = ctx.upload(rows.data(), rows.size());
+    ck_launch(kgb::pls_evaluate(b.ev, ctx.stream()), "PLS-LDA evaluation");
+    std::vector<uint16_t> pc(static_cast<size_t>(nt));
+    ctx.download(pc.data(), b.ev.pred, pc.size());
+    pls_check_status(ctx, b);
+    for (int i = 0; i < nt; ++i) predicted[i] = cd.code2label[pc[i]];
+  });
+}
+
+int kgb_core_plslda(const float* x, int32_t n, int32_t p, const int32_t* labels, const int32_t* constrain,
+                    const int32_t* fixed, const kgb_core_options* opt, const kgb_pls_options* pls,
+                    kgb_core_result* out) {
+  return guarded([&]() {
+    if (x == nullptr || labels == nullptr || opt == nullptr || pls == nullptr || out == nullptr)
+      fail(KGB_EINVAL, "null pointer");
+    if (n < 2 || p < 1) fail(KGB_EINVAL, "CorePLSLDA requires at least two rows.");
+    if (n > 65535) fail(KGB_EINVAL, "at most 65535 rows are supported");
+    if (opt->cycles < 0) fail(KGB_EINVAL, "Core cycles must be non-negative.");
+    check_pls_options(pls);
+    if (pls->stratified)
+      fail(KGB_EINVAL, "stratified folds are not supported by the CUDA CorePLSLDA entry point (set stratified = 0)");
+    const kgb_policy pol = policy_is_zero(opt->policy) ? default_policy() : opt->policy;
+    const std::vector<int> lab(labels, labels + n);
+    const std::vector<int> con = constrain ? std::vector<int>(constrain, constrain + n) : std::vector<int>();
+    const std::vector<int> folds = kgb::make_folds(lab, con, pls->folds, false, pls->cv_seed);
+    const uint64_t bc = kgb::unordered_bucket_count(static_cast<size_t>(n));
+    const Coding cd = code_labels(labels, n, bc);
+    const int C0 = static_cast<int>(cd.code2label.size());
+    const int C0max = std::max(2, C0);
+    // groups: singletons without a constraint, else ascending constrain values
+    std::vector<int> goff, gmem;
+    int G = n;
+    if (con.empty()) {
+      for (int i = 0; i <= n; ++i) goff.push_back(i);
+      for (int i = 0; i < n; ++i) gmem.push_back(i);
+    } else {
+      std::map<int, std::vector<int>> members;
+      for (int i = 0; i < n; ++i) members[con[i]].push_back(i);
+      goff.push_back(0);
+      for (const auto& kv : members) {
+        gmem.insert(gmem.end(), kv.second.begin(), kv.second.end());
+        goff.push_back(static_cast<int>(gmem.size()));
+      }
+      G = static_cast<int>(members.size());
+    }
+    const int requested = pls->fixed_components > 0 ? pls->fixed_components : pls->max_components;
+    Ctx ctx(pls->device);
+    const float* d_x = ctx.upload(x, static_cast<size_t>(n) * p);
+    const PlsSlices sl = pls_slices({folds}, 1, n, false);
+    PlsBuffers b = pls_buffers(ctx, d_x, 1, n, p, sl, C0max, pls->max_components, requested, pls->center != 0,
+                               pls->scale != 0, nullptr, 0);
+    std::vector<int> c2l(static_cast<size_t>(C0max), 0);
+    std::copy(cd.code2label.begin(), cd.code2label.end(), c2l.begin());
+    const int nco = C0;
+    const uint8_t nocol = cd.nocollide ? 1 : 0;
+    const uint64_t seed = opt->seed;
+    kgb::EvolveParams P{};
+    P.problems = 1;
+    P.L = n;
+    P.T = opt->cycles;
+    P.F = sl.F;
+    P.G = G;
+    P.singleton = con.empty() ? 1 : 0;
+    P.evolutionary = opt->evolutionary_search != 0;
+    P.guarded = opt->guarded_diversity != 0;
+    P.absorption = opt->many_to_one_absorption != 0;
+    P.adaptive = opt->adaptive_proposal_size != 0;
+    P.pol_guidance = pol.prediction_guidance != 0;
+    P.pol_adaptive = pol.adaptive_proposal_size != 0;
+    P.pol_transition = pol.transition_proposal != 0;
+    P.pol_stochastic = pol.stochastic_acceptance != 0;
+    P.pol_diversity = pol.diversity_multiplier != 0;
+    P.pol_reject1 = pol.reject_single_class != 0;
+    P.bucket_count = bc;
+    P.init = ctx.upload(cd.codes.data(), cd.codes.size());
+    P.code2label = ctx.upload(c2l.data(), c2l.size());
+    P.ncodes = ctx.upload(&nco, 1);
+    P.nocollide = ctx.upload(&nocol, 1);
+    P.folds = b.ev.folds;
+    P.fixed = fixed ? ctx.upload(fixed, static_cast<size_t>(n)) : nullptr;
+    P.goff = ctx.upload(goff.data(), goff.size());
+    P.gmem = ctx.upload(gmem.data(), gmem.size());
+    P.seeds = ctx.upload(&seed, 1);
+    const EvolveBuffers eb = run_pls_evolution(ctx, P, b, C0max, opt->auto_class_coarsening != 0, pol);
+    const int T = opt->cycles;
+    std::vector<uint16_t> cb(static_cast<size_t>(n)), cp(static_cast<size_t>(n));
+    std::vector<double> va(static_cast<size_t>(std::max(T, 1))), vs(va.size()), best(2);
+    std::vector<int> ps(va.size()), ac(va.size()), counters(18);
+    std::vector<uint8_t> fl(va.size() * 3);
+    ctx.download(cb.data(), eb.clbest, cb.size());
+    ctx.download(cp.data(), eb.cvpredbest, cp.size());
+    ctx.download(va.data(), eb.vect_acc, va.size());
+    ctx.download(vs.data(), eb.vect_score, vs.size());
+    ctx.download(ps.data(), eb.psize, ps.size());
+    ctx.download(ac.data(), eb.active, ac.size());
+    ctx.download(fl.data(), eb.flags, fl.size());
+    ctx.download(counters.data(), eb.counters, counters.size());
+    ctx.download(best.data(), eb.best, best.size());
+    ctx.sync();
+    for (int i = 0; i < n; ++i) {
+      if (out->clbest) out->clbest[i] = cd.code2label[cb[i]];
+      if (out->cvpredbest) out->cvpredbest[i] = cd.code2label[cp[i]];
+      if (out->fold_assignments) out->fold_assignments[i] = folds[i];
+    }
+    for (int c = 0; c < T; ++c) {
+      if (out->vect_acc) out->vect_acc[c] = va[c];
+      if (out->vect_score) out->vect_score[c] = vs[c];
+      if (out->proposal_size) out->proposal_size[c] = ps[c];
+      if (out->active_classes) out->active_classes[c] = ac[c];
+      if (out->flags)
+        for (int q = 0; q < 3; ++q) out->flags[3 * c + q] = fl[3 * c + q];
+    }
+    out->accbest = best[0];
+    out->scorebest = best[1];
+    for (int q = 0; q < 18; ++q) out->counters[q] = counters[q];
   });
 }
 

@@ -23,6 +23,7 @@
 #include "evolve.cuh"
 #include "launch_count.cuh"
 #include "rng.cuh"
+#include "crmath.cuh"
 
 #include <cuda_runtime.h>
 #include <float.h>
@@ -549,15 +550,9 @@ __device__ int label_census(const EvolveParams& P, const Smem& s, const uint16_t
   return block_sum(local, *s.f);
 }
 
-// core_objective_score for the kNN classifier; census must be current.
-__device__ double objective(const EvolveParams& P, const Smem& s, int prob, double acc, int nc, int C0) {
-  const bool use_div = P.guarded && P.pol_diversity;
-  const bool reject1 = P.guarded && P.pol_reject1;
-  if (!use_div && !reject1) return acc;
-  if (reject1 && nc == 1) return -INFINITY;
-  if (!use_div) return acc;
-  // iteration order of std::unordered_map<int,int> after reserve(L) and
-  // insertion in row order
+// s.order[0..nc) = the codes of the census in the iteration order of
+// std::unordered_map<int,int> after reserve(L) and insertion in row order.
+__device__ void map_order(const EvolveParams& P, const Smem& s, int prob, int C0) {
   const bool nocollide = P.nocollide[prob] != 0;
   if (nocollide) {
     // every key has its own bucket: each new key goes to the list front
@@ -604,6 +599,16 @@ __device__ double objective(const EvolveParams& P, const Smem& s, int prob, doub
     }
   }
   __syncthreads();
+}
+
+// core_objective_score for the kNN classifier; census must be current.
+__device__ double objective(const EvolveParams& P, const Smem& s, int prob, double acc, int nc, int C0) {
+  const bool use_div = P.guarded && P.pol_diversity;
+  const bool reject1 = P.guarded && P.pol_reject1;
+  if (!use_div && !reject1) return acc;
+  if (reject1 && nc == 1) return -INFINITY;
+  if (!use_div) return acc;
+  map_order(P, s, prob, C0);
   if (threadIdx.x == 0) {
     // psq[c] = (c/L)*(c/L) rounded as the reference rounds each step
     double same = 0.0;
@@ -1021,8 +1026,7 @@ __device__ void evolve_problem(const EvolveParams& P, const Smem& s, int prob) {
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(kThreads, 1) evolve_kernel(EvolveParams P) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ Smem carve_smem(const EvolveParams& P, unsigned char* smem_raw) {
   Smem s;
   size_t off = 0;
   s.f = reinterpret_cast<Fixed*>(smem_raw);
@@ -1063,9 +1067,521 @@ __global__ void __launch_bounds__(kThreads, 1) evolve_kernel(EvolveParams P) {
   s.jarr = rows + 4 * Lp;
   s.list = rows + 5 * Lp;
   s.scratch32 = reinterpret_cast<int*>(rows + 6 * Lp);  // 2 * Lp u16 = Lp ints
+  return s;
+}
+
+__global__ void __launch_bounds__(kThreads, 1) evolve_kernel(EvolveParams P) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Smem s = carve_smem(P, smem_raw);
+  const int C = P.C0max;
   for (int prob = blockIdx.x; prob < P.problems; prob += gridDim.x) {
     if (!P.smem_trans) s.trans = P.trans + static_cast<size_t>(prob) * C * C;
     evolve_problem(P, s, prob);
+  }
+}
+
+// ===========================================================================
+// PLS-LDA evolution: maximize_core (core.cpp:1269-1549) with PLSLDACV as the
+// predictor.  The predictor runs as separate launches over all problems and
+// folds (pls.cu), so each cycle is split in two: this kernel accepts the
+// previous proposal (its CV predictions are in Q.pred) and builds the next
+// one, keeping the engine, the current state and the counters in global
+// memory between launches.  PLS adds to the kNN cycle:
+//   propose_auto_class_coarsening   core.cpp:995-1108
+//   the fragmentation penalty       core.cpp:954-968
+// ===========================================================================
+
+// Serial std::shuffle of a[0..n) with the libstdc++ 64-bit-engine algorithm
+// (pair draws, see shuffle_targets_block); a holds (a0, a1) int pairs and a
+// double key, swapped together.
+__device__ void shuffle_triples_serial(Mt64State& g, int* a0, int* a1, double* key, int n) {
+  auto swap3 = [&](int i, int j) {
+    const int t0 = a0[i], t1 = a1[i];
+    const double tk = key[i];
+    a0[i] = a0[j];
+    a1[i] = a1[j];
+    key[i] = key[j];
+    a0[j] = t0;
+    a1[j] = t1;
+    key[j] = tk;
+  };
+  if (n <= 1) return;
+  int i = 1;
+  if ((n & 1) == 0) {
+    swap3(1, static_cast<int>(draw_below_serial(g, 2)));
+    i = 2;
+  }
+  while (i < n) {
+    const uint64_t b0 = static_cast<uint64_t>(i) + 1ull, b1 = b0 + 1ull;
+    const uint64_t x = draw_below_serial(g, b0 * b1);
+    swap3(i, static_cast<int>(x / b1));
+    swap3(i + 1, static_cast<int>(x % b1));
+    i += 2;
+  }
+}
+
+// Class sizes, movable sizes and class x prediction counts of s.cl against pp
+// (build_class_transition_stats, core.cpp:980-993).  Returns the class count.
+__device__ int transition_stats(const EvolveParams& P, const Smem& s, const uint16_t* pp, int C0) {
+  int* tr = s.trans;
+  const int C = P.C0max;
+  for (int i = threadIdx.x; i < C0 * C; i += kThreads) tr[i] = 0;
+  for (int c = threadIdx.x; c < C0; c += kThreads) {
+    s.cnt[c] = 0;
+    s.movable[c] = 0;
+  }
+  __syncthreads();
+  for (int r = threadIdx.x; r < P.L; r += kThreads) {
+    const int a = s.cl[r];
+    atomicAdd(&s.cnt[a], 1);
+    atomicAdd(&tr[a * C + pp[r]], 1);
+    if (P.fixed == nullptr || P.fixed[r] != 1) atomicAdd(&s.movable[a], 1);
+  }
+  __syncthreads();
+  int local = 0;
+  for (int c = threadIdx.x; c < C0; c += kThreads) local += s.cnt[c] > 0;
+  return block_sum(local, *s.f);
+}
+
+// propose_auto_class_coarsening on s.cl.  plogp[k] = (k/L) * log(k/L) as the
+// reference rounds it.  Returns 1 if the labels changed.
+__device__ int coarsening_block(const EvolvePlsParams& Q, const Smem& s, int prob, const uint16_t* pp, int C0) {
+  const EvolveParams& P = Q.base;
+  Fixed& f = *s.f;
+  const int nc = transition_stats(P, s, pp, C0);
+  if (nc <= 2) return 0;
+  const int C = P.C0max;
+  if (threadIdx.x == 0) {
+    const double n = static_cast<double>(P.L);
+    double ce = 0.0;
+    for (int c = 0; c < C0; ++c)
+      if (s.cnt[c] > 0) ce = __dsub_rn(ce, Q.plogp[s.cnt[c]]);
+    const double keff = cr_exp(ce);
+    const double lr = cr_log(__ddiv_rn(static_cast<double>(nc), 1.0 < keff ? keff : 1.0));
+    const double frag = 0.0 < lr ? lr : 0.0;
+    double wte = 0.0;
+    int K = 0;
+    int* csrc = s.order;   // candidates: source, destination, score
+    int* cdst = s.bt;
+    double* cscore = s.weight;
+    for (int src = 0; src < C0; ++src) {
+      const int ssize = s.cnt[src];
+      if (ssize == 0) continue;
+      const int mov = s.movable[src];
+      if (mov <= 0) continue;
+      const int* row = s.trans + src * C;
+      int dbest = src, dsize = ssize, bcount = 0;
+      double te = 0.0;
+      for (int dst = 0; dst < C0; ++dst) {
+        const int cntd = row[dst];
+        if (cntd == 0) continue;
+        const double pr = __ddiv_rn(static_cast<double>(cntd), static_cast<double>(ssize));
+        if (pr > 0.0) te = __dsub_rn(te, __dmul_rn(pr, cr_log(pr)));
+        const int sz = s.cnt[dst];
+        if (dst != src && sz > 0 &&
+            (cntd > bcount || (cntd == bcount && sz > dsize) || (cntd == bcount && sz == dsize && dst < dbest))) {
+          dbest = dst;
+          dsize = sz;
+          bcount = cntd;
+        }
+      }
+      wte = __dadd_rn(wte, __dmul_rn(__ddiv_rn(static_cast<double>(ssize), n), te));
+      if (dbest == src || bcount == 0) continue;
+      const double stay = __ddiv_rn(static_cast<double>(row[src]), static_cast<double>(ssize));
+      csrc[K] = src;
+      cdst[K] = dbest;
+      cscore[K] = __dmul_rn(__ddiv_rn(1.0, __dsqrt_rn(static_cast<double>(mov))), __dsub_rn(1.0, stay));
+      ++K;
+    }
+    int budget = 0;
+    if (K > 0) {
+      const double temperature = __ddiv_rn(frag, __dadd_rn(__dadd_rn(frag, wte), 1.0));
+      const double rd = __dsub_rn(static_cast<double>(nc), keff);
+      const double redundant = 0.0 < rd ? rd : 0.0;
+      budget = static_cast<int>(ceil(__dmul_rn(temperature, redundant)));
+      if (budget < 1 && frag > 0.0) budget = 1;
+      budget = min(budget, nc - 2);
+    }
+    int merged = 0;
+    if (K > 0 && budget > 0) {
+      shuffle_triples_serial(f.rng, csrc, cdst, cscore, K);
+      for (int a = 1; a < K; ++a) {  // stable sort by score, descending
+        const int v0 = csrc[a], v1 = cdst[a];
+        const double vk = cscore[a];
+        int b = a - 1;
+        while (b >= 0 && vk > cscore[b]) {
+          csrc[b + 1] = csrc[b];
+          cdst[b + 1] = cdst[b];
+          cscore[b + 1] = cscore[b];
+          --b;
+        }
+        csrc[b + 1] = v0;
+        cdst[b + 1] = v1;
+        cscore[b + 1] = vk;
+      }
+      int* remap = s.aux;
+      for (int c = 0; c < C0; ++c) remap[c] = c;
+      for (int q = 0; q < K && merged < budget; ++q) {
+        const int src = csrc[q];
+        if (remap[src] != src) continue;
+        int d = cdst[q];
+        while (remap[d] != d) d = remap[d];
+        if (d == src) continue;
+        remap[src] = d;
+        ++merged;
+      }
+    }
+    f.flag = merged;
+  }
+  __syncthreads();
+  if (f.flag == 0) return 0;
+  int changed = 0;
+  const int* remap = s.aux;
+  for (int r = threadIdx.x; r < P.L; r += kThreads) {
+    if (P.fixed != nullptr && P.fixed[r] == 1) continue;
+    const int a = s.cl[r];
+    int d = a;
+    while (remap[d] != d) d = remap[d];
+    if (d != a) {
+      s.cl[r] = static_cast<uint16_t>(d);
+      changed = 1;
+    }
+  }
+  return block_sum(changed, f) > 0 ? 1 : 0;
+}
+
+// core_objective_score with the PLS fragmentation penalty; census current.
+__device__ double objective_pls(const EvolvePlsParams& Q, const Smem& s, int prob, double acc, int nc, int C0) {
+  const EvolveParams& P = Q.base;
+  const bool use_div = P.guarded && P.pol_diversity;
+  const bool use_frag = Q.coarsening && Q.pol_frag;
+  const bool reject1 = P.guarded && P.pol_reject1;
+  if (!use_div && !use_frag && !reject1) return acc;
+  if (reject1 && nc == 1) return -INFINITY;
+  if (!use_div && !(use_frag && nc > 1)) return acc;
+  map_order(P, s, prob, C0);
+  if (threadIdx.x == 0) {
+    double score = acc;
+    if (use_div) {
+      double same = 0.0;
+      for (int q = 0; q < nc; ++q) same = __dadd_rn(same, P.psq[s.cnt[s.order[q]]]);
+      const double diff = __dsub_rn(1.0, same);
+      score = __dmul_rn(score, __dsqrt_rn(0.0 < diff ? diff : 0.0));
+    }
+    if (use_frag && nc > 1) {
+      double entropy = 0.0;
+      for (int q = 0; q < nc; ++q) entropy = __dsub_rn(entropy, Q.plogp[s.cnt[s.order[q]]]);
+      const double mse = P.L > 1 ? Q.logn : 0.0;
+      double code_cost = 0.0;
+      if (mse > 0.0) {
+        const double v = __ddiv_rn(entropy, mse);
+        code_cost = v < 0.0 ? 0.0 : (1.0 < v ? 1.0 : v);
+      }
+      const double keff = cr_exp(entropy);
+      const double lr = cr_log(__ddiv_rn(static_cast<double>(nc), 1.0 < keff ? keff : 1.0));
+      const double frag = 0.0 < lr ? lr : 0.0;
+      const double frag_cost = __ddiv_rn(frag, __dadd_rn(1.0, frag));
+      const double pc = code_cost < frag_cost ? frag_cost : code_cost;
+      score = __dsub_rn(score, __dmul_rn(__dsub_rn(1.0, acc), pc));
+    }
+    s.f->score = score;
+  }
+  __syncthreads();
+  const double out = s.f->score;
+  __syncthreads();
+  return out;
+}
+
+// Rows of s.cl grouped by code, ascending rows within a code, for the
+// cross-product chains of the PLS predictor: one warp per code.
+__device__ void class_lists(const EvolvePlsParams& Q, const Smem& s, int prob, int C0) {
+  const int L = Q.base.L, C = Q.base.C0max;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int c = threadIdx.x; c < C0; c += kThreads) s.cnt[c] = 0;
+  __syncthreads();
+  for (int r = threadIdx.x; r < L; r += kThreads) atomicAdd(&s.cnt[s.cl[r]], 1);
+  __syncthreads();
+  int* coff = Q.class_off + static_cast<size_t>(prob) * (C + 1);
+  if (threadIdx.x == 0) {
+    int run = 0;
+    for (int c = 0; c < C; ++c) {
+      coff[c] = run;
+      s.aux[c] = run;
+      run += c < C0 ? s.cnt[c] : 0;
+    }
+    coff[C] = run;
+  }
+  __syncthreads();
+  uint16_t* rows = Q.class_rows + static_cast<size_t>(prob) * L;
+  for (int c = warp; c < C0; c += kWarps) {
+    if (s.cnt[c] == 0) continue;
+    int pos = s.aux[c];
+    for (int base = 0; base < L; base += 32) {
+      const int r = base + lane;
+      const bool hit = r < L && s.cl[r] == c;
+      const unsigned m = __ballot_sync(kFull, hit);
+      if (hit) rows[pos + __popc(m & ((1u << lane) - 1u))] = static_cast<uint16_t>(r);
+      pos += __popc(m);
+    }
+  }
+  __syncthreads();
+}
+
+__device__ void pls_propose(const EvolvePlsParams& Q, const Smem& s, int prob, int cycle, PlsRunState& st, int C0) {
+  const EvolveParams& P = Q.base;
+  Fixed& f = *s.f;
+  const int L = P.L, T = P.T, G = P.G;
+  for (int r = threadIdx.x; r < L; r += kThreads) s.cl[r] = s.cur[r];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ns;
+    if (G <= 1) {
+      ns = G > 0 ? G : 0;
+    } else if (!(P.adaptive && P.pol_adaptive) || T <= 1) {
+      ns = uniform_int_serial(f.rng, 1, G);
+    } else {
+      double progress = __ddiv_rn(static_cast<double>(cycle + 1), static_cast<double>(T + 1));
+      progress = progress < 0.0 ? 0.0 : (progress > 1.0 ? 1.0 : progress);
+      const double smooth = __dmul_rn(__dmul_rn(progress, progress), __dsub_rn(3.0, __dmul_rn(2.0, progress)));
+      double temp = __dsub_rn(1.0, smooth);
+      temp = temp < 0.0 ? 0.0 : (temp > 1.0 ? 1.0 : temp);
+      const int mc = 1 + static_cast<int>(floor(__dmul_rn(static_cast<double>(G - 1), temp)));
+      ns = uniform_int_serial(f.rng, 1, mc > 1 ? mc : 1);
+    }
+    f.ns = ns;
+    P.proposal_size[static_cast<size_t>(prob) * T + cycle] = ns;
+  }
+  __syncthreads();
+  shuffle_targets_block(f, s.jarr, G, s.raw);
+  const int ns = f.ns;
+  if (ns > 0) {
+    bucket_steps_block(s, G);
+    if (P.singleton && P.pol_guidance) {
+      for (int g = threadIdx.x; g < G; g += kThreads) {
+        const int row = P.gmem[g];
+        if (s.curpred[row] == s.cur[row]) continue;
+        if (P.fixed != nullptr && P.fixed[row] == 1) continue;
+        if (final_position_of(s, g) < ns) s.cl[row] = s.curpred[row];
+      }
+    } else {
+      for (int q = threadIdx.x; q < ns; q += kThreads) s.perm[q] = static_cast<uint16_t>(occupant_of(s, G, q));
+      __syncthreads();
+      if (threadIdx.x == 0) relabel_serial(P, s, s.curpred, ns, C0);
+    }
+  }
+  __syncthreads();
+  const bool attempt_co = P.pol_transition && Q.coarsening && Q.pol_coarsen;
+  const bool attempt_ab = P.pol_transition && P.absorption;
+  int coarsened = 0, absorbed = 0;
+  if (attempt_co) coarsened = coarsening_block(Q, s, prob, s.curpred, C0);
+  if (attempt_ab) absorbed = absorption_block(P, s, prob, s.curpred, C0);
+  if (threadIdx.x == 0) {
+    if (attempt_co || attempt_ab) ++st.tr_att;
+    if (attempt_co) {
+      ++st.co_att;
+      st.co_moves += coarsened;
+    }
+    if (attempt_ab) {
+      ++st.m1_att;
+      st.absorb_moves += absorbed;
+    }
+    st.coarsened = coarsened;
+    st.absorbed = absorbed;
+  }
+  __syncthreads();
+  class_lists(Q, s, prob, C0);
+}
+
+__device__ void pls_step(const EvolvePlsParams& Q, const Smem& s, int prob) {
+  const EvolveParams& P = Q.base;
+  Fixed& f = *s.f;
+  const int L = P.L, T = P.T;
+  const int C0 = P.ncodes[prob];
+  const size_t ro = static_cast<size_t>(prob) * L;
+  PlsRunState& gst = Q.state[prob];
+  __shared__ PlsRunState st;
+  if (Q.phase == 0) {
+    if (threadIdx.x == 0) {
+      mt64_seed(f.rng, P.seeds[prob]);
+      st = PlsRunState{};
+    }
+    for (int r = threadIdx.x; r < L; r += kThreads) {
+      s.cl[r] = P.init[ro + r];
+      Q.cl[ro + r] = s.cl[r];
+    }
+    __syncthreads();
+    class_lists(Q, s, prob, C0);
+  } else {
+    const int cycle = Q.cycle;  // proposal `cycle - 1` was evaluated (cycle 0: the initial labels)
+    const Mt64State& g = Q.rng[prob];
+    for (int i = threadIdx.x; i < kMtN; i += kThreads) {
+      f.rng.mt[i] = g.mt[i];
+      f.rng.out[i] = g.out[i];
+    }
+    if (threadIdx.x == 0) {
+      f.rng.pos = g.pos;
+      st = gst;
+    }
+    for (int r = threadIdx.x; r < L; r += kThreads) {
+      s.cl[r] = Q.cl[ro + r];
+      s.pred[r] = Q.pred[ro + r];
+      if (cycle > 0) {
+        s.cur[r] = Q.cur[ro + r];
+        s.curpred[r] = Q.curpred[ro + r];
+      }
+    }
+    __syncthreads();
+    uint16_t* gbest = P.clbest + ro;
+    uint16_t* gbestpred = P.cvpredbest + ro;
+    int ok = 0;
+    for (int r = threadIdx.x; r < L; r += kThreads) ok += s.cl[r] == s.pred[r];
+    ok = block_sum(ok, f);
+    const double acc = __ddiv_rn(static_cast<double>(ok), static_cast<double>(L));
+    const int nc = label_census(P, s, s.cl, C0);
+    const double score = objective_pls(Q, s, prob, acc, nc, C0);
+    if (cycle == 0) {
+      for (int r = threadIdx.x; r < L; r += kThreads) {
+        s.cur[r] = s.cl[r];
+        s.curpred[r] = s.pred[r];
+        gbest[r] = s.cl[r];
+        gbestpred[r] = s.pred[r];
+      }
+      if (threadIdx.x == 0) {
+        st.accbest = st.cur_acc = acc;
+        st.scorebest = st.cur_score = score;
+        st.nc_cur = st.nc_best = nc;
+      }
+    } else {
+      const int c = cycle - 1;
+      if (threadIdx.x == 0) {
+        ++st.proposals;
+        const bool improves = score > st.scorebest;
+        int accepted = improves, improving = improves, stoch = 0;
+        if (P.evolutionary) {
+          const double cooling = __dsub_rn(1.0, __ddiv_rn(static_cast<double>(c + 1), static_cast<double>(T > 1 ? T : 1)));
+          const double one_minus = __dsub_rn(1.0, st.cur_acc);
+          const double clipped = (0.0 < one_minus) ? one_minus : 0.0;
+          const double t0 = __dmul_rn(__dmul_rn(0.10, clipped), cooling);
+          const double temperature = (1.0e-9 < t0) ? t0 : 1.0e-9;
+          int acc_cur = score >= st.cur_score;
+          improving = acc_cur;
+          if (!acc_cur && P.pol_stochastic && temperature > 1.0e-9) {
+            ++st.st_att;
+            const double u = canonical_serial(f.rng);
+            acc_cur = u < exp(__ddiv_rn(__dsub_rn(score, st.cur_score), temperature));
+            stoch = acc_cur;
+          }
+          accepted = acc_cur;
+        }
+        f.accept = accepted | (improves << 1) | (stoch << 2) | (improving << 3);
+        if (improves) {
+          st.accbest = acc;
+          st.scorebest = score;
+          ++st.best_updates;
+          st.nc_best = nc;
+        }
+        if (P.evolutionary) {
+          if (accepted) {
+            st.cur_acc = acc;
+            st.cur_score = score;
+            st.nc_cur = nc;
+            ++st.accepts;
+            if (stoch) ++st.st_acc;
+          } else {
+            ++st.rejections;
+          }
+        }
+        if (accepted && (st.coarsened || st.absorbed)) {
+          ++st.tr_acc;
+          if (st.coarsened) ++st.co_acc;
+          if (st.absorbed) ++st.m1_acc;
+        }
+        uint8_t* fl = P.flags + (static_cast<size_t>(prob) * T + c) * 3;
+        fl[0] = accepted ? 1 : 0;
+        fl[1] = (accepted && improving) ? 1 : 0;
+        fl[2] = stoch ? 1 : 0;
+        P.active[static_cast<size_t>(prob) * T + c] = P.evolutionary ? st.nc_cur : st.nc_best;
+        P.vect_acc[static_cast<size_t>(prob) * T + c] = st.accbest;
+        P.vect_score[static_cast<size_t>(prob) * T + c] = st.scorebest;
+        if (acc == 1.0 && isfinite(score)) st.success = 1;
+      }
+      __syncthreads();
+      const int code = f.accept;
+      const bool improves = (code >> 1) & 1;
+      const bool take = P.evolutionary ? (code & 1) : improves;
+      if (improves) {
+        for (int r = threadIdx.x; r < L; r += kThreads) {
+          gbest[r] = s.cl[r];
+          gbestpred[r] = s.pred[r];
+        }
+      }
+      if (take) {
+        for (int r = threadIdx.x; r < L; r += kThreads) {
+          s.cur[r] = s.cl[r];
+          s.curpred[r] = s.pred[r];
+        }
+      }
+      __syncthreads();
+    }
+    if (cycle == T) {
+      // the rows of the best labels by code, for the projection
+      __syncthreads();
+      for (int r = threadIdx.x; r < L; r += kThreads) s.cl[r] = gbest[r];
+      __syncthreads();
+      class_lists(Q, s, prob, C0);
+    }
+    if (cycle < T) {
+      pls_propose(Q, s, prob, cycle, st, C0);
+      for (int r = threadIdx.x; r < L; r += kThreads) Q.cl[ro + r] = s.cl[r];
+    } else if (threadIdx.x == 0) {
+      int* c = P.counters + static_cast<size_t>(prob) * 18;
+      c[0] = T;
+      c[1] = st.proposals;
+      c[2] = st.best_updates;
+      c[3] = st.accepts;
+      c[4] = st.st_att;
+      c[5] = st.st_acc;
+      c[6] = st.rejections;
+      c[7] = st.co_moves;
+      c[8] = st.absorb_moves;
+      c[9] = st.tr_att;
+      c[10] = st.tr_acc;
+      c[11] = st.m1_att;
+      c[12] = st.m1_acc;
+      c[13] = st.proposals + 1;
+      c[14] = st.success;
+      c[15] = 0;
+      c[16] = st.co_att;
+      c[17] = st.co_acc;
+      P.best[2 * prob] = st.accbest;
+      P.best[2 * prob + 1] = st.scorebest;
+      P.status[prob] = 0;
+    }
+    for (int r = threadIdx.x; r < L; r += kThreads) {
+      Q.cur[ro + r] = s.cur[r];
+      Q.curpred[ro + r] = s.curpred[r];
+    }
+  }
+  __syncthreads();
+  Mt64State& g = Q.rng[prob];
+  for (int i = threadIdx.x; i < kMtN; i += kThreads) {
+    g.mt[i] = f.rng.mt[i];
+    g.out[i] = f.rng.out[i];
+  }
+  if (threadIdx.x == 0) {
+    g.pos = f.rng.pos;
+    gst = st;
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kThreads, 1) evolve_pls_kernel(EvolvePlsParams Q) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Smem s = carve_smem(Q.base, smem_raw);
+  const int C = Q.base.C0max;
+  for (int prob = blockIdx.x; prob < Q.base.problems; prob += gridDim.x) {
+    if (!Q.base.smem_trans) s.trans = Q.base.trans + static_cast<size_t>(prob) * C * C;
+    pls_step(Q, s, prob);
   }
 }
 
@@ -1080,6 +1596,15 @@ size_t evolve_smem_bytes(int L, int C0max, bool rows_in_smem, bool trans_in_smem
   if (trans_in_smem) b += al(sizeof(int) * static_cast<size_t>(C0max) * C0max);
   if (rows_in_smem) b += kRowArrays * ((static_cast<size_t>(L) + 7) / 8 * 8) * sizeof(uint16_t);
   return b;
+}
+
+int evolve_pls_launch(const EvolvePlsParams& q, int grid, size_t smem, void* stream) {
+  cudaError_t e = cudaFuncSetAttribute(evolve_pls_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(smem));
+  if (e != cudaSuccess) return static_cast<int>(e);
+  evolve_pls_kernel<<<grid, kThreads, smem, static_cast<cudaStream_t>(stream)>>>(q);
+  count_launch();
+  return static_cast<int>(cudaGetLastError());
 }
 
 int evolve_launch(const EvolveParams& p, int grid, size_t smem, void* stream) {

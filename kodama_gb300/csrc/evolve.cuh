@@ -3,6 +3,8 @@
 
 #include <stdint.h>
 
+#include "rng.cuh"
+
 namespace kgb {
 
 constexpr uint16_t kNoRow = 0xFFFFu;
@@ -57,8 +59,36 @@ struct EvolveParams {
   uint64_t* raw_scratch;   // grid x (L/2 + 64) engine outputs of one shuffle
 };
 
+// Per-problem state of the PLS-LDA evolution kept between cycle launches.
+struct PlsRunState {
+  double accbest, scorebest, cur_acc, cur_score;
+  int nc_cur, nc_best;
+  int coarsened, absorbed;  // moves of the pending proposal
+  int proposals, best_updates, accepts, st_att, st_acc, rejections;
+  int co_moves, absorb_moves, tr_att, tr_acc, m1_att, m1_acc, co_att, co_acc, success;
+};
+
+struct EvolvePlsParams {
+  EvolveParams base;       // counters has stride 18 here
+  PlsRunState* state;      // problems
+  Mt64State* rng;          // problems: the run's engine between launches
+  uint16_t* cur;           // problems x L current state
+  uint16_t* curpred;       // problems x L its CV predictions
+  uint16_t* cl;            // problems x L labels to evaluate (proposal)
+  const uint16_t* pred;    // problems x L CV predictions of cl
+  int* class_off;          // problems x (C0max + 1)
+  uint16_t* class_rows;    // problems x L rows of cl grouped by code
+  const double* plogp;     // L + 1: (k/L) * log(k/L)
+  double logn;             // log(L)
+  int coarsening;          // auto_class_coarsening
+  int pol_coarsen, pol_frag;
+  int phase;               // 0: initial labels; 1: accept cycle-1 / propose cycle
+  int cycle;
+};
+
 constexpr int kEvolveRowArrays = 8;
 size_t evolve_smem_bytes(int L, int C0max, bool rows_in_smem, bool trans_in_smem, bool hist_in_smem);
 int evolve_launch(const EvolveParams& p, int grid, size_t smem, void* stream);
+int evolve_pls_launch(const EvolvePlsParams& q, int grid, size_t smem, void* stream);
 
 }  // namespace kgb

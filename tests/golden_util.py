@@ -76,7 +76,10 @@ def check_core(case, r, folds_attr="folds"):
     assert np.asarray(r.active_classes).tolist() == case["active_classes"], "active classes"
     assert np.asarray(r.flags).tolist() == case["flags"], "accept flags"
     assert r.accbest == case["accbest"] and r.scorebest == case["scorebest"], "best scalars"
-    assert np.asarray(r.counters).tolist() == case["counters"], "counters"
+    got = np.asarray(r.counters).tolist()
+    want = case["counters"]
+    # the kNN core has no PLS coarsening: counters beyond the recorded ones are zero
+    assert got[:len(want)] == want and not any(got[len(want):]), "counters"
 
 
 def check_pls_matrix(case, r):
