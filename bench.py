@@ -39,6 +39,11 @@ METRIC = "KODAMA.matrix wall-s at N=20k,d=50,M=100: learned vs plain GPU at equa
 WORKLOAD = dict(n=20000, d=50, runs=100, cycles=100, graph_neighbors=30, knn_k=30, folds=10,
                 splitting=50, landmarks=10000, seed=1234)
 CPU_SAMPLE_RUNS = 16
+# --workload pls: the PLS-LDA configuration (CorePLSLDA inside KODAMA.matrix)
+PLS_METRIC = "KODAMA.matrix PLS-LDA wall-s at N=10k,d=200,ncomp=5,F=10,M=50,Tcycle=50"
+PLS_WORKLOAD = dict(n=10000, d=200, runs=50, cycles=50, graph_neighbors=30, knn_k=30, folds=10,
+                    splitting=0, landmarks=10000, seed=1234, components=5)
+PLS_CPU_SAMPLE_RUNS = 16
 # DRAM bytes (read + write) of one evolution-kernel launch, scaled from the
 # ncu capture summarised in profiles/evolve_kernel_cfg2.md (None until captured).
 EVOLVE_TRAFFIC_BYTES = 280837120
@@ -160,6 +165,128 @@ def cpu_baseline(x, threads=None):
                       f"({t_graph + t_matrix:.2f} s), runs scaled x{WORKLOAD['runs'] / CPU_SAMPLE_RUNS:g}",
             "stages_s": {"graph": round(t_graph, 3), "atlas": round(t_atlas, 3),
                          "runs_sample": round(t_runs, 3)}}
+
+
+def _pls_data():
+    from kodama_gb300 import datasets
+    x, _ = datasets.low_rank(n=PLS_WORKLOAD["n"], d=PLS_WORKLOAD["d"], seed=3)
+    return np.ascontiguousarray(x, np.float32)
+
+
+def _pls_kw():
+    w = PLS_WORKLOAD
+    return dict(runs=w["runs"], cycles=w["cycles"], landmarks=w["landmarks"], splitting=w["splitting"],
+                graph_neighbors=w["graph_neighbors"], folds=w["folds"], knn_k=w["knn_k"], seed=w["seed"],
+                components=w["components"])
+
+
+def _pls_config(extra=None):
+    c = {"workload": "KODAMA.matrix PLS-LDA N=10000 d=200 (low-rank X=ZW+E, 8 classes), M=50 runs, "
+                     "Tcycle=50, ncomp=5, folds=10, landmarks=10000 (L=7500), splitting=100",
+         "global_batch": PLS_WORKLOAD["runs"], "seq_len": PLS_WORKLOAD["cycles"],
+         "parallelism": "replicas", "l2": "flushed between steps (512 MB write)",
+         "data": "synthetic low_rank(seed=3)"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+def pls_cpu_baseline(x, threads=None):
+    """The CPU restatement of the PLS-LDA path on a bounded sample: exact graph,
+    atlas and PLS_CPU_SAMPLE_RUNS runs (one per thread), scaled to M=50."""
+    from oracle import oracle
+    if not oracle.available():
+        oracle.build()
+    threads = threads or os.cpu_count() or 1
+    w = PLS_WORKLOAD
+    t0 = time.perf_counter()
+    gi, gd = oracle.exact_knn(x, w["graph_neighbors"], threads=threads)
+    t_graph = time.perf_counter() - t0
+    kw = _pls_kw()
+    kw["runs"] = PLS_CPU_SAMPLE_RUNS
+    seed = kw.pop("seed")
+    t1 = time.perf_counter()
+    r = oracle.kodama_matrix_graph_data(x, gi, gd, 0, seed=seed, threads=threads, materialize=0,
+                                        classifier=1, **kw)
+    t_matrix = time.perf_counter() - t1
+    t_atlas, t_runs = float(r.timings[4]), float(r.timings[2])
+    # runs are independent; with `threads` workers the sample wall time covers
+    # ceil(sample / threads) waves of runs
+    waves_sample = -(-PLS_CPU_SAMPLE_RUNS // threads)
+    waves_full = -(-w["runs"] // threads)
+    total = t_graph + t_atlas + t_runs * (waves_full / waves_sample) + max(0.0, t_matrix - t_atlas - t_runs)
+    return {"value": round(total, 4), "unit": "s", "cores": threads, "kind": "port",
+            "sample": f"exact graph + atlas + {PLS_CPU_SAMPLE_RUNS} of {w['runs']} runs timed "
+                      f"({t_graph + t_matrix:.2f} s), run waves scaled x{waves_full / waves_sample:g}",
+            "stages_s": {"graph": round(t_graph, 3), "atlas": round(t_atlas, 3), "runs_sample": round(t_runs, 3)},
+            "mean_final_cv_acc_sample": round(float(np.mean(r.acc)), 6)}
+
+
+def run_gpu_pls(args):
+    import torch
+
+    import kodama_gb300 as kg
+    from kodama_gb300 import build as kbuild
+
+    kbuild.build()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    x = _pls_data()
+    kw = _pls_kw()
+    w = PLS_WORKLOAD
+    n, runs, cycles = w["n"], w["runs"], w["cycles"]
+    x_dev = torch.from_numpy(x).to(f"cuda:{local}")
+    res_dev = torch.empty((runs, n), dtype=torch.int32, device=f"cuda:{local}")
+    x_pin = torch.from_numpy(x).pin_memory()
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    for _ in range(args.warmup):
+        kg.KODAMA_matrix(x_dev, res_out=res_dev, device=local, classifier="pls", **kw)
+    spans, evo, accs = [], [], []
+    launches0 = kg.launch_count()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            r = kg.KODAMA_matrix(x_dev, res_out=res_dev, device=local, classifier="pls", **kw)
+            spans.append(r.kernel_ms["device_span"] / 1000.0)
+            evo.append(r.kernel_ms["evolution"] / 1000.0)
+            accs.append(float(r.acc.mean()))
+        torch.cuda.synchronize()
+    launches = (kg.launch_count() - launches0) // max(1, args.steps)
+    e2e = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        kg.KODAMA_matrix(x_pin.numpy(), device=local, classifier="pls", **kw)
+        e2e.append(time.perf_counter() - t0)
+    value = float(np.mean(spans))
+    L = int(np.ceil(0.75 * n)) if w["landmarks"] >= n else w["landmarks"]
+    F, p = w["folds"], w["d"]
+    # one evaluation streams, per (run, fold), the standardised training rows
+    # twice (cross-product, scores) and the validation rows once
+    nt = L - L // F
+    bytes_eval = runs * F * (2 * nt + (L - nt)) * p * 4
+    evo_s = float(np.mean(evo))
+    peak, peak_kind = _peaks()
+    achieved = bytes_eval * (cycles + 1) / evo_s / 1e9
+    line = {"metric": PLS_METRIC, "value": round(value, 5), "unit": "s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(value * 1000, 3), "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic",
+            "config": _pls_config(),
+            "e2e": {"value": round(float(np.mean(e2e)), 5), "unit": "s", "h2d_bytes_per_step": x.nbytes,
+                    "d2h_bytes_per_step": runs * n * 4 + runs * cycles * 8},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                         "kernel": "PLS evolution span (eval_kernel x (T+1) + evolution steps + Gram)",
+                         "algorithmic_bytes_per_eval": bytes_eval, "traffic": None},
+            "gpu_launches": int(launches), "clocks": clocks.summary(),
+            "stage_ms": {k: round(v, 3) for k, v in r.kernel_ms.items()},
+            "mean_final_cv_acc": round(float(np.mean(accs)), 6)}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = pls_cpu_baseline(x)
+    print(json.dumps(line))
 
 
 def run_reference(args):
@@ -295,9 +422,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="knn", choices=["knn", "pls"],
+                    help="knn: the headline configuration; pls: the PLS-LDA configuration")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "pls":
+        run_gpu_pls(args)
     else:
         run_gpu(args)
 

@@ -436,7 +436,13 @@ PlsBuffers pls_buffers(Ctx& ctx, const float* d_X, int R, int L, int p, const Pl
   b.S = S;
   b.ntrain = sl.ntrain;
   b.present = sl.present;
-  if (kgb::pls_eval_smem(p, C0max, requested) > 200 * 1024)
+  if (requested > kgb::kPlsMaxComponents || max_components > kgb::kPlsMaxComponents)
+    fail(KGB_EINVAL, "at most 64 PLS components are supported by the CUDA PLS-LDA kernel");
+  // the cross-product in shared memory when two CTAs still fit on an SM for
+  // the Gram evaluations and one CTA for those that compute scores in the fit
+  const bool s_in_smem = kgb::pls_eval_smem(p, C0max, requested, max_components, true, false) <= 110 * 1024 &&
+                         kgb::pls_eval_smem(p, C0max, requested, max_components, true, true) <= 200 * 1024;
+  if (kgb::pls_eval_smem(p, C0max, requested, max_components, s_in_smem, true) > 200 * 1024)
     fail(KGB_EINVAL, "too many features, classes or components for the PLS-LDA kernel");
   cudaStream_t st = ctx.stream();
   kgb::PlsPrepArgs& a = b.prep;
@@ -470,6 +476,8 @@ PlsBuffers pls_buffers(Ctx& ctx, const float* d_X, int R, int L, int p, const Pl
   e.max_components = max_components;
   e.requested = requested;
   e.predict_mode = d_Xv != nullptr;
+  e.s_in_smem = s_in_smem ? 1 : 0;
+  e.tiles_after_s = 1;  // no fold Gram yet: every slice computes scores in the fit
   e.Z = a.Z;
   e.xsum = a.xsum;
   e.gram = nullptr;
@@ -524,6 +532,7 @@ void pls_enable_gram(Ctx& ctx, PlsBuffers& b) {
   b.prep.gram = ctx.alloc<float>(static_cast<size_t>(S) * p * p);
   ck_launch(kgb::pls_build_gram(b.prep, d_want, ctx.stream()), "fold Gram");
   b.ev.gram = b.prep.gram;
+  b.ev.tiles_after_s = std::all_of(want.begin(), want.end(), [](uint8_t v) { return v != 0; }) ? 0 : 1;
   ctx.sync();  // `want` is a host temporary
 }
 
@@ -630,6 +639,13 @@ EvolveBuffers run_pls_evolution(Ctx& ctx, kgb::EvolveParams P, PlsBuffers& b, in
     }
     Q.plogp = ctx.upload(plogp.data(), plogp.size());
     Q.logn = std::log(nd);
+    std::vector<double> klogk(static_cast<size_t>(L) + 1, 0.0), logk(static_cast<size_t>(L) + 1, 0.0);
+    for (int k = 1; k <= L; ++k) {
+      logk[k] = std::log(static_cast<double>(k));
+      klogk[k] = static_cast<double>(k) * logk[k];
+    }
+    Q.klogk = ctx.upload(klogk.data(), klogk.size());
+    Q.logk = ctx.upload(logk.data(), logk.size());
   }
   Q.coarsening = coarsening;
   Q.pol_coarsen = pol.pls_transition_coarsening != 0;

@@ -1144,13 +1144,49 @@ __device__ int transition_stats(const EvolveParams& P, const Smem& s, const uint
 }
 
 // propose_auto_class_coarsening on s.cl.  plogp[k] = (k/L) * log(k/L) as the
-// reference rounds it.  Returns 1 if the labels changed.
+// reference rounds it.  One thread per source class computes its transition
+// entropy, its destination and its candidate score; the transition entropy
+// is formed as log(s) - sum_c c log(c) / s from host tables of k log k and
+// log k: it only feeds ceil(temperature * redundant), which an ulp-level
+// difference cannot move unless that product lies within an ulp of an
+// integer.  Returns 1 if the labels changed.
 __device__ int coarsening_block(const EvolvePlsParams& Q, const Smem& s, int prob, const uint16_t* pp, int C0) {
   const EvolveParams& P = Q.base;
   Fixed& f = *s.f;
   const int nc = transition_stats(P, s, pp, C0);
   if (nc <= 2) return 0;
   const int C = P.C0max;
+  double* te_of = s.bsur;     // per source: transition entropy
+  int* dst_of = s.bt;         // per source: destination, -1 = not a candidate
+  double* score_of = s.cp;    // per source: candidate score
+  for (int src = threadIdx.x; src < C0; src += kThreads) {
+    const int ssize = s.cnt[src];
+    dst_of[src] = -1;
+    te_of[src] = 0.0;
+    if (ssize == 0 || s.movable[src] <= 0) continue;
+    const int* row = s.trans + src * C;
+    int dbest = src, dsize = ssize, bcount = 0;
+    double clc = 0.0;
+    for (int dst = 0; dst < C0; ++dst) {
+      const int cntd = row[dst];
+      if (cntd == 0) continue;
+      clc = __dadd_rn(clc, Q.klogk[cntd]);
+      const int sz = s.cnt[dst];
+      if (dst != src && sz > 0 &&
+          (cntd > bcount || (cntd == bcount && sz > dsize) || (cntd == bcount && sz == dsize && dst < dbest))) {
+        dbest = dst;
+        dsize = sz;
+        bcount = cntd;
+      }
+    }
+    te_of[src] = __dsub_rn(Q.logk[ssize], __ddiv_rn(clc, static_cast<double>(ssize)));
+    if (dbest == src || bcount == 0) continue;
+    const double stay = __ddiv_rn(static_cast<double>(row[src]), static_cast<double>(ssize));
+    dst_of[src] = dbest;
+    score_of[src] =
+        __dmul_rn(__ddiv_rn(1.0, __dsqrt_rn(static_cast<double>(s.movable[src]))), __dsub_rn(1.0, stay));
+  }
+  __syncthreads();
   if (threadIdx.x == 0) {
     const double n = static_cast<double>(P.L);
     double ce = 0.0;
@@ -1161,36 +1197,16 @@ __device__ int coarsening_block(const EvolvePlsParams& Q, const Smem& s, int pro
     const double frag = 0.0 < lr ? lr : 0.0;
     double wte = 0.0;
     int K = 0;
-    int* csrc = s.order;   // candidates: source, destination, score
-    int* cdst = s.bt;
+    int* csrc = s.order;   // candidates in ascending source order: source, destination, score
+    int* cdst = s.firstpos;
     double* cscore = s.weight;
     for (int src = 0; src < C0; ++src) {
-      const int ssize = s.cnt[src];
-      if (ssize == 0) continue;
-      const int mov = s.movable[src];
-      if (mov <= 0) continue;
-      const int* row = s.trans + src * C;
-      int dbest = src, dsize = ssize, bcount = 0;
-      double te = 0.0;
-      for (int dst = 0; dst < C0; ++dst) {
-        const int cntd = row[dst];
-        if (cntd == 0) continue;
-        const double pr = __ddiv_rn(static_cast<double>(cntd), static_cast<double>(ssize));
-        if (pr > 0.0) te = __dsub_rn(te, __dmul_rn(pr, cr_log(pr)));
-        const int sz = s.cnt[dst];
-        if (dst != src && sz > 0 &&
-            (cntd > bcount || (cntd == bcount && sz > dsize) || (cntd == bcount && sz == dsize && dst < dbest))) {
-          dbest = dst;
-          dsize = sz;
-          bcount = cntd;
-        }
-      }
-      wte = __dadd_rn(wte, __dmul_rn(__ddiv_rn(static_cast<double>(ssize), n), te));
-      if (dbest == src || bcount == 0) continue;
-      const double stay = __ddiv_rn(static_cast<double>(row[src]), static_cast<double>(ssize));
+      if (s.cnt[src] == 0 || s.movable[src] <= 0) continue;
+      wte = __dadd_rn(wte, __dmul_rn(__ddiv_rn(static_cast<double>(s.cnt[src]), n), te_of[src]));
+      if (dst_of[src] < 0) continue;
       csrc[K] = src;
-      cdst[K] = dbest;
-      cscore[K] = __dmul_rn(__ddiv_rn(1.0, __dsqrt_rn(static_cast<double>(mov))), __dsub_rn(1.0, stay));
+      cdst[K] = dst_of[src];
+      cscore[K] = score_of[src];
       ++K;
     }
     int budget = 0;

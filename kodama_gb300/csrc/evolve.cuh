@@ -79,6 +79,8 @@ struct EvolvePlsParams {
   int* class_off;          // problems x (C0max + 1)
   uint16_t* class_rows;    // problems x L rows of cl grouped by code
   const double* plogp;     // L + 1: (k/L) * log(k/L)
+  const double* klogk;     // L + 1: k * log(k) (0 for k = 0)
+  const double* logk;      // L + 1: log(k)
   double logn;             // log(L)
   int coarsening;          // auto_class_coarsening
   int pol_coarsen, pol_frag;

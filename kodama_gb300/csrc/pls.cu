@@ -13,11 +13,14 @@
 //
 // Every float accumulation of the reference is a sequential chain in a fixed
 // order (rows ascending, features ascending, classes ascending); each chain
-// here runs in one thread in that order, and the parallelism is across
-// chains: slices x features x classes x rows.  Double accumulators of the
-// reference (dot_float, mat_vec_float, t_mat_vec_float, power_norm2_float)
-// sum exact float products, so each step is one fma(a, b, acc) in double.
-// Built with --fmad=false: no other multiply-add is fused.
+// runs in one thread (or one warp feeding one accumulator) in that order, and
+// the parallelism is across chains: slices x features x classes x rows.
+// Double accumulators of the reference (dot_float, mat_vec_float,
+// t_mat_vec_float, power_norm2_float) sum exact float products; they are
+// reproduced by an exact integer sum with a rounding-safety check, and by
+// the sequential double sum only when that check cannot decide
+// (warp_exact_dot below).  Built with --fmad=false: no multiply-add is fused
+// unless written as one.
 #include "pls.cuh"
 #include "launch_count.cuh"
 
@@ -169,10 +172,148 @@ __global__ void __launch_bounds__(1024) gram_kernel(PlsPrepArgs a, const uint8_t
 // Evaluation: one CTA per slice
 // ---------------------------------------------------------------------------
 
+constexpr int kMaxNC = 8;      // components per register pass over the rows
+constexpr int kMaxComp = 64;   // components of a fit held per row (local array)
+constexpr int kTile = 32 * 33; // per-warp transposing tile (floats)
+
 struct EvalShared {
-  int m, nt, maxr, fitted, nc, stop, best, lab;
+  int m, nt, stop, best, lab, fail;
   float rn, inv;
 };
+
+// ---------------------------------------------------------------------------
+// float(sum_k double(a_k) * double(b_k)) summed sequentially in double, as the
+// reference's dot_float / mat_vec_float / t_mat_vec_float / power_norm2_float
+// do, without double arithmetic on the common path.
+//
+// Each product of two floats is exact in double, so the sequential sum S_seq
+// differs from the exact sum S by at most n * 2^-53 * sum|t_k| (recursive
+// summation of exact terms; 2^-52 is used below).  A warp forms S exactly as
+// a 64-bit fixed-point integer from the 24-bit mantissas (terms below the
+// fixed point truncated: at most n units of error), rounds it to float and
+// checks that the rounding interval of that float contains S widened by both
+// error bounds; then float(S_seq) is that float.  When the check cannot
+// decide (S close to a rounding boundary, massive cancellation, non-finite
+// or extreme values), lane 0 runs the sequential double sum.  The point:
+// this GPU issues a dependent double FMA only every 64-152 cycles.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ int clog2i(int n) { return n <= 1 ? 0 : 32 - __clz(n - 1); }
+
+__device__ __forceinline__ float warp_sum_ru(float v) {
+  for (int o = 16; o > 0; o >>= 1) v = __fadd_ru(v, __shfl_xor_sync(kFull, v, o));
+  return v;
+}
+
+__device__ __forceinline__ long long warp_sum_i64(long long v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+
+// The float nearest to V * 2^LSB, if S_seq provably rounds to it (see above).
+__device__ __forceinline__ bool round_check(long long V, int LSB, float A, int n, float& out) {
+  if (V == 0) {
+    if (A == 0.0f) {
+      out = 0.0f;
+      return true;
+    }
+    return false;
+  }
+  const bool neg = V < 0;
+  const unsigned long long mag = neg ? 0ull - static_cast<unsigned long long>(V) : static_cast<unsigned long long>(V);
+  const int e = 63 - __clzll(static_cast<long long>(mag));
+  const int shift = e - 23;
+  if (shift <= 0) return false;
+  const float bu = __fadd_ru(__fmul_ru(ldexpf(A, -52 - LSB), static_cast<float>(n)), static_cast<float>(n + 1));
+  if (!(bu < 1e30f)) return false;
+  const unsigned long long one = 1ull;
+  unsigned long long m = mag >> shift;
+  const unsigned long long rem = mag & ((one << shift) - 1ull), half = one << (shift - 1);
+  const bool up = rem > half || (rem == half && (m & 1ull));
+  unsigned long long dlo, dhi;
+  if (!up) {
+    if (rem == half) return false;
+    dhi = half - rem;
+    dlo = rem + (m == 0x800000ull ? (half >> 1) : half);
+  } else {
+    dlo = rem - half;
+    dhi = ((one << shift) - rem) + half;
+  }
+  const float dmin = __ull2float_rz(dlo < dhi ? dlo : dhi);
+  if (!(dmin > bu)) return false;
+  if (up) ++m;
+  int ex = shift + LSB;
+  if (m == 0x1000000ull) {
+    m >>= 1;
+    ++ex;
+  }
+  if (ex + 23 > 126 || ex + 23 < -126) return false;
+  const float fv = ldexpf(static_cast<float>(m), ex);
+  out = neg ? -fv : fv;
+  return true;
+}
+
+// Exact fixed-point sum over the warp; returns whether `out` is float(S_seq).
+template <class Term>
+__device__ bool warp_exact_dot(int n, Term term, int lane, float& out) {
+  int top = -100000, bad = 0;
+  float A = 0.0f;
+  for (int k = lane; k < n; k += 32) {
+    float x, y;
+    term(k, x, y);
+    const unsigned ux = __float_as_uint(x), uy = __float_as_uint(y);
+    const int ex = static_cast<int>((ux >> 23) & 0xffu), ey = static_cast<int>((uy >> 23) & 0xffu);
+    bad |= (ex == 0xff) | (ey == 0xff);
+    if ((ux << 1) != 0u && (uy << 1) != 0u) top = max(top, max(ex, 1) + max(ey, 1) - 252);
+    A = __fadd_ru(A, __fmul_ru(fabsf(x), fabsf(y)));
+  }
+  bad = __reduce_or_sync(kFull, bad);
+  top = __reduce_max_sync(kFull, top);
+  if (bad) return false;
+  A = warp_sum_ru(A);
+  if (top == -100000) {  // every term is zero
+    out = 0.0f;
+    return true;
+  }
+  const int LSB = top + clog2i(n) - 62;
+  long long acc = 0;
+  for (int k = lane; k < n; k += 32) {
+    float x, y;
+    term(k, x, y);
+    const unsigned ux = __float_as_uint(x), uy = __float_as_uint(y);
+    const unsigned bx = (ux >> 23) & 0xffu, by = (uy >> 23) & 0xffu;
+    const unsigned mx = (ux & 0x7fffffu) | (bx ? 0x800000u : 0u), my = (uy & 0x7fffffu) | (by ? 0x800000u : 0u);
+    const unsigned long long P = static_cast<unsigned long long>(mx) * my;
+    if (P == 0ull) continue;
+    const int E = (bx ? static_cast<int>(bx) - 150 : -149) + (by ? static_cast<int>(by) - 150 : -149);
+    const int sh = E - LSB;
+    unsigned long long v;
+    if (sh >= 0) v = P << sh;
+    else v = -sh >= 64 ? 0ull : P >> (-sh);
+    acc += ((ux ^ uy) >> 31) ? -static_cast<long long>(v) : static_cast<long long>(v);
+  }
+  acc = warp_sum_i64(acc);
+  return round_check(acc, LSB, A, n, out);
+}
+
+// dot_float / mat_vec_float / t_mat_vec_float element: float(S_seq).
+template <class Term>
+__device__ float warp_seq_dot(int n, Term term, int lane) {
+  float out = 0.0f;
+  if (!warp_exact_dot(n, term, lane, out)) {
+    if (lane == 0) {
+      double acc = 0.0;
+      for (int k = 0; k < n; ++k) {
+        float x, y;
+        term(k, x, y);
+        acc = fma(static_cast<double>(x), static_cast<double>(y), acc);
+      }
+      out = __double2float_rn(acc);
+    }
+    out = __shfl_sync(kFull, out, 0);
+  }
+  return out;
+}
 
 __device__ __forceinline__ float power_norm2(double sum) {
   if (!isfinite(sum) || sum < 0.0) return INFINITY;
@@ -180,85 +321,74 @@ __device__ __forceinline__ float power_norm2(double sum) {
   return __double2float_rn(__dsqrt_rn(sum));
 }
 
-// Block-wide: out[c] = float(sum_j S[j + c*p] * w[j]) (double chain over j).
-__device__ void t_mat_vec(const float* S, int p, int m, const float* w, float* out) {
-  for (int c = threadIdx.x; c < m; c += kEvalThreads) {
-    const float* col = S + static_cast<size_t>(c) * p;
+// power_norm2_float of v[0..n) by one warp.
+__device__ float warp_power_norm(const float* v, int n, int lane) {
+  float out = 0.0f;
+  auto t = [&](int k, float& x, float& y) {
+    x = v[k];
+    y = v[k];
+  };
+  if (warp_exact_dot(n, t, lane, out)) return __fsqrt_rn(out);
+  if (lane == 0) {
     double acc = 0.0;
-    for (int j = 0; j < p; ++j) acc = fma(static_cast<double>(col[j]), static_cast<double>(w[j]), acc);
-    out[c] = __double2float_rn(acc);
+    for (int k = 0; k < n; ++k) acc = fma(static_cast<double>(v[k]), static_cast<double>(v[k]), acc);
+    out = power_norm2(acc);
   }
+  return __shfl_sync(kFull, out, 0);
 }
 
-// Block-wide: out[j] = float(sum_c S[j + c*p] * t[c]) (double chain over c).
-__device__ void mat_vec(const float* S, int p, int m, const float* t, float* out) {
-  for (int j = threadIdx.x; j < p; j += kEvalThreads) {
-    double acc = 0.0;
-    for (int c = 0; c < m; ++c)
-      acc = fma(static_cast<double>(S[j + static_cast<size_t>(c) * p]), static_cast<double>(t[c]), acc);
-    out[j] = __double2float_rn(acc);
-  }
-}
-
-__device__ void power_refresh(const float* S, int p, int m, float* w, float* tv) {
-  for (int it = 0; it < 2; ++it) {
-    t_mat_vec(S, p, m, w, tv);
-    __syncthreads();
-    mat_vec(S, p, m, tv, w);
-    __syncthreads();
-  }
-}
-
-// Serial double sum of squares (dot_float(x, x) and power_norm2_float).
-__device__ double sumsq_serial(const float* x, int n) {
-  double acc = 0.0;
-  for (int i = 0; i < n; ++i) acc = fma(static_cast<double>(x[i]), static_cast<double>(x[i]), acc);
-  return acc;
-}
-
-// cholesky_solve_float on an n x n matrix A (row-major) for rhs n x m; one thread.
-__device__ bool chol_solve(const float* A, int n, const float* rhs, int m, float* Lc, float* sol) {
-  for (int row = 0; row < n; ++row) {
-    for (int col = 0; col <= row; ++col) {
-      float v = A[row * n + col];
-      for (int k = 0; k < col; ++k) v = __fsub_rn(v, __fmul_rn(Lc[row * n + k], Lc[col * n + k]));
-      if (row == col) {
-        if (!isfinite(v) || v <= 0.0f) return false;
-        Lc[row * n + col] = __fsqrt_rn(v);
-      } else {
-        const float d = Lc[col * n + col];
-        if (!isfinite(d) || d <= 0.0f) return false;
-        Lc[row * n + col] = __fdiv_rn(v, d);
-      }
+// Scores of 32 rows (one per lane; row < 0 = none) for components
+// q0 .. q0+nq-1 (nq <= kMaxNC): acc[q] = sum over features in order of
+// z(row, j) * W(j, q0+q).  The rows come in through the warp's transposing
+// tile with 128-byte loads.
+__device__ __forceinline__ void warp_scores(const float* __restrict__ base, int p, int myrow, const float* W, int ldw,
+                                            int q0, int nq, float* tile, int lane, float* acc) {
+#pragma unroll
+  for (int q = 0; q < kMaxNC; ++q) acc[q] = 0.0f;
+  for (int j0 = 0; j0 < p; j0 += 32) {
+    const int jl = j0 + lane;
+#pragma unroll 8
+    for (int i = 0; i < 32; ++i) {
+      const int ri = __shfl_sync(kFull, myrow, i);
+      tile[i * 33 + lane] = (ri >= 0 && jl < p) ? base[static_cast<size_t>(ri) * p + jl] : 0.0f;
     }
-  }
-  for (int i = 0; i < n * m; ++i) sol[i] = rhs[i];
-  for (int c = 0; c < m; ++c) {
-    for (int row = 0; row < n; ++row) {
-      float v = sol[row * m + c];
-      for (int k = 0; k < row; ++k) v = __fsub_rn(v, __fmul_rn(Lc[row * n + k], sol[k * m + c]));
-      sol[row * m + c] = __fdiv_rn(v, Lc[row * n + row]);
+    __syncwarp();
+    const int jn = min(32, p - j0);
+    for (int jj = 0; jj < jn; ++jj) {
+      const float v = tile[lane * 33 + jj];
+      const float* wr = W + static_cast<size_t>(j0 + jj) * ldw + q0;
+#pragma unroll
+      for (int q = 0; q < kMaxNC; ++q)
+        if (q < nq) acc[q] = __fadd_rn(acc[q], __fmul_rn(v, wr[q]));
     }
-    for (int row = n - 1; row >= 0; --row) {
-      float v = sol[row * m + c];
-      for (int k = row + 1; k < n; ++k) v = __fsub_rn(v, __fmul_rn(Lc[k * n + row], sol[k * m + c]));
-      sol[row * m + c] = __fdiv_rn(v, Lc[row * n + row]);
-    }
+    __syncwarp();
   }
-  return true;
 }
 
-// Score of one standardised row for component q: sum over features in order.
-__device__ __forceinline__ float row_score(const float* z, const float* W, int ldw, int p, int q) {
+// Sequential float chain over list entries b..e-1, warp-cooperative: lanes
+// fetch 32 entries at a time, then every lane adds them in list order.
+// val(i, v) stores the term of entry i and returns whether it counts.
+template <class Val>
+__device__ float warp_chain(int b, int e, Val val, int lane) {
   float acc = 0.0f;
-  for (int j = 0; j < p; ++j) acc = __fadd_rn(acc, __fmul_rn(z[j], W[static_cast<size_t>(j) * ldw + q]));
+  for (int base = b; base < e; base += 32) {
+    const int i = base + lane;
+    float v = 0.0f;
+    const bool ok = i < e && val(i, v);
+    const unsigned msk = __ballot_sync(kFull, ok);
+#pragma unroll 8
+    for (int q = 0; q < 32; ++q) {
+      const float t = __shfl_sync(kFull, v, q);
+      if ((msk >> q) & 1u) acc = __fadd_rn(acc, t);
+    }
+  }
   return acc;
 }
 
-__global__ void __launch_bounds__(kEvalThreads) eval_kernel(PlsEvalArgs a) {
+__global__ void __launch_bounds__(kEvalThreads, 2) eval_kernel(PlsEvalArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int s = blockIdx.x, r = s / a.F, f = s % a.F;
-  const int p = a.p, L = a.L, C = a.C0max, NCm = a.requested;
+  const int p = a.p, L = a.L, C = a.C0max, NCm = a.requested, ldw = a.max_components;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   EvalShared& sh = *reinterpret_cast<EvalShared*>(smem);
   size_t off = 64;
@@ -273,15 +403,20 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(PlsEvalArgs a) {
   float* ld = reinterpret_cast<float*>(carve(sizeof(float) * p));
   float* pw = reinterpret_cast<float*>(carve(sizeof(float) * p));
   float* tv = reinterpret_cast<float*>(carve(sizeof(float) * C));
+  float* Wsm = reinterpret_cast<float*>(carve(sizeof(float) * p * ldw));
+  float* Vsm = reinterpret_cast<float*>(carve(sizeof(float) * p * ldw));
   float* cs = reinterpret_cast<float*>(carve(sizeof(float) * C * NCm));
   float* cp = reinterpret_cast<float*>(carve(sizeof(float) * NCm * NCm));
   float* pooled = reinterpret_cast<float*>(carve(sizeof(float) * NCm * NCm));
-  float* cov = reinterpret_cast<float*>(carve(sizeof(float) * NCm * NCm));
   float* Lc = reinterpret_cast<float*>(carve(sizeof(float) * NCm * NCm));
-  float* rhs = reinterpret_cast<float*>(carve(sizeof(float) * NCm * C));
   float* sol = reinterpret_cast<float*>(carve(sizeof(float) * NCm * C));
   float* lin = reinterpret_cast<float*>(carve(sizeof(float) * C * NCm));
   float* cst = reinterpret_cast<float*>(carve(sizeof(float) * C));
+  // shared region: the cross-product (when it fits) and the score tiles,
+  // which overlap it unless a slice of the launch computes scores during the
+  // fit (no fold Gram)
+  float* region = reinterpret_cast<float*>(carve(0));
+  float* tiles = (a.s_in_smem && a.tiles_after_s) ? region + static_cast<size_t>(p) * C : region;
 
   const uint16_t* lab = a.labels + static_cast<size_t>(r) * L;
   const int* coff = a.class_off + static_cast<size_t>(r) * (C + 1);
@@ -292,10 +427,7 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(PlsEvalArgs a) {
   const int nv = a.predict_mode ? a.NV : a.val_off[s + 1] - a.val_off[s];
   const int* vidx = a.predict_mode ? nullptr : a.val_idx + a.val_off[s];
   uint16_t* pred = a.pred + static_cast<size_t>(r) * (a.predict_mode ? a.NV : L);
-  auto val_row = [&](int v) -> const float* {
-    return a.predict_mode ? a.Zv + (static_cast<size_t>(r) * a.NV + v) * p : Zs + static_cast<size_t>(vidx[v]) * p;
-  };
-  auto val_out = [&](int v) -> int { return a.predict_mode ? v : vidx[v]; };
+  const float* vbase = a.predict_mode ? a.Zv + static_cast<size_t>(r) * a.NV * p : Zs;
 
   // --- fold classes: codes with training rows, ascending -------------------
   for (int c = threadIdx.x; c < C; c += kEvalThreads) cnt[c] = coff[c + 1] - coff[c];
@@ -316,13 +448,14 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(PlsEvalArgs a) {
   if (m <= 1) {
     // one training class: it is every prediction (labels.front() without one)
     const int only = m == 1 ? klist[0] : lab[0];
-    for (int v = threadIdx.x; v < nv; v += kEvalThreads) pred[val_out(v)] = static_cast<uint16_t>(only);
+    for (int v = threadIdx.x; v < nv; v += kEvalThreads)
+      pred[a.predict_mode ? v : vidx[v]] = static_cast<uint16_t>(only);
     if (threadIdx.x == 0) a.eval_comp[s] = 1;
     return;
   }
 
   // --- label cross-product S (p x m), column k = fold class k -------------
-  float* S = a.s_scr + static_cast<size_t>(s) * p * C;
+  float* S = a.s_in_smem ? region : a.s_scr + static_cast<size_t>(s) * p * C;
   {
     const int JB = (p + 31) / 32;
     const float inv_n = nt > 0 ? __fdiv_rn(1.0f, static_cast<float>(nt)) : 0.0f;
@@ -356,42 +489,63 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(PlsEvalArgs a) {
 
   // --- SIMPLS weights ------------------------------------------------------
   const int maxr = min(min(a.max_components, p), max(1, nt - 1));
-  const int ldw = a.max_components;
-  float* Wg = a.W + static_cast<size_t>(s) * p * ldw;
-  float* Vg = a.V + static_cast<size_t>(s) * p * ldw;
   const bool gram = a.gram != nullptr && a.use_gram[s];
   const float* G = gram ? a.gram + static_cast<size_t>(s) * p * p : nullptr;
   float* scv = a.sc + static_cast<size_t>(s) * L;
+  const int* tix = a.train_idx + tb;
   int fitted = 0;
   for (int comp = 0; comp < maxr; ++comp) {
     for (int j = threadIdx.x; j < p; j += kEvalThreads) w[j] = comp == 0 ? a.w0[j] : pw[j];
     __syncthreads();
-    power_refresh(S, p, m, w, tv);
-    if (threadIdx.x == 0) {
-      float rn = power_norm2(sumsq_serial(w, p));
-      int best = -1;
-      if (comp == 0 && !(isfinite(rn) && rn > 1.0e-10f)) {
-        // retry on the response column with the largest norm
-        double bn = 0.0;
-        for (int k = 0; k < m; ++k) {
-          const double ns = sumsq_serial(S + static_cast<size_t>(k) * p, p);
-          if (isfinite(ns) && ns > bn) {
-            bn = ns;
-            best = k;
+    // two power iterations (a second pass only for the strongest-column retry)
+    for (int pass = 0; pass < 2; ++pass) {
+      for (int it = 0; it < 2; ++it) {
+        for (int c = warp; c < m; c += kEvalWarps) {
+          const float* col = S + static_cast<size_t>(c) * p;
+          const float v = warp_seq_dot(p, [&](int k, float& x, float& y) {
+            x = col[k];
+            y = w[k];
+          }, lane);
+          if (lane == 0) tv[c] = v;
+        }
+        __syncthreads();
+        for (int j = warp; j < p; j += kEvalWarps) {
+          const float v = warp_seq_dot(m, [&](int k, float& x, float& y) {
+            x = S[j + static_cast<size_t>(k) * p];
+            y = tv[k];
+          }, lane);
+          if (lane == 0) w[j] = v;
+        }
+        __syncthreads();
+      }
+      if (warp == 0) {
+        const float rn = warp_power_norm(w, p, lane);
+        if (lane == 0) {
+          sh.rn = rn;
+          sh.best = -1;
+          if (pass == 0 && comp == 0 && !(isfinite(rn) && rn > 1.0e-10f)) {
+            // retry on the response column with the largest norm (rare: double sums)
+            double bn = 0.0;
+            int best = -1;
+            for (int k = 0; k < m; ++k) {
+              double ns = 0.0;
+              for (int j = 0; j < p; ++j) {
+                const double v = static_cast<double>(S[j + static_cast<size_t>(k) * p]);
+                ns = fma(v, v, ns);
+              }
+              if (isfinite(ns) && ns > bn) {
+                bn = ns;
+                best = k;
+              }
+            }
+            if (best >= 0 && bn > 1.0e-20) sh.best = best;
           }
         }
-        if (!(best >= 0 && bn > 1.0e-20)) best = -1;
       }
-      sh.rn = rn;
-      sh.best = best;
-    }
-    __syncthreads();
-    if (sh.best >= 0) {
+      __syncthreads();
+      if (sh.best < 0) break;
       const int best = sh.best;
       for (int j = threadIdx.x; j < p; j += kEvalThreads) w[j] = S[j + static_cast<size_t>(best) * p];
-      __syncthreads();
-      power_refresh(S, p, m, w, tv);
-      if (threadIdx.x == 0) sh.rn = power_norm2(sumsq_serial(w, p));
       __syncthreads();
     }
     const float rn = sh.rn;
@@ -399,19 +553,24 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(PlsEvalArgs a) {
     for (int j = threadIdx.x; j < p; j += kEvalThreads) w[j] = __fdiv_rn(w[j], rn);
     __syncthreads();
     if (gram) {
-      for (int i = threadIdx.x; i < p; i += kEvalThreads) {
-        double acc = 0.0;
-        for (int j = 0; j < p; ++j)
-          acc = fma(static_cast<double>(G[static_cast<size_t>(j) * p + i]), static_cast<double>(w[j]), acc);
-        ld[i] = __double2float_rn(acc);
+      for (int i = warp; i < p; i += kEvalWarps) {
+        const float* gi = G + static_cast<size_t>(i) * p;
+        const float v = warp_seq_dot(p, [&](int k, float& x, float& y) {
+          x = gi[k];
+          y = w[k];
+        }, lane);
+        if (lane == 0) ld[i] = v;
       }
       __syncthreads();
-      if (threadIdx.x == 0) {
-        double acc = 0.0;
-        for (int j = 0; j < p; ++j) acc = fma(static_cast<double>(w[j]), static_cast<double>(ld[j]), acc);
-        const float sns = __double2float_rn(acc);
-        sh.stop = !(isfinite(sns) && sns > 1.0e-20f);
-        sh.inv = sh.stop ? 0.0f : __fdiv_rn(1.0f, __fsqrt_rn(sns));
+      if (warp == 0) {
+        const float sns = warp_seq_dot(p, [&](int k, float& x, float& y) {
+          x = w[k];
+          y = ld[k];
+        }, lane);
+        if (lane == 0) {
+          sh.stop = !(isfinite(sns) && sns > 1.0e-20f);
+          sh.inv = sh.stop ? 0.0f : __fdiv_rn(1.0f, __fsqrt_rn(sns));
+        }
       }
       __syncthreads();
       if (sh.stop) break;
@@ -423,18 +582,25 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(PlsEvalArgs a) {
       __syncthreads();
     } else {
       // scores of the training rows, their norm, loading = X^T scores
-      for (int t = threadIdx.x; t < nt; t += kEvalThreads) {
-        const float* z = Zs + static_cast<size_t>(a.train_idx[tb + t]) * p;
-        float acc = 0.0f;
-        for (int j = 0; j < p; ++j) acc = __fadd_rn(acc, __fmul_rn(z[j], w[j]));
-        scv[t] = acc;
+      float* tile = tiles + warp * kTile;
+      for (int b0 = warp * 32; b0 < nt; b0 += kEvalWarps * 32) {
+        const int t = b0 + lane;
+        const int row = t < nt ? tix[t] : -1;
+        float acc[kMaxNC];
+        warp_scores(Zs, p, row, w, 1, 0, 1, tile, lane, acc);
+        if (t < nt) scv[t] = acc[0];
       }
       __syncthreads();
-      if (threadIdx.x == 0) {
-        const float d = __double2float_rn(sumsq_serial(scv, nt));
-        const float sn = __fsqrt_rn(0.0f < d ? d : 0.0f);
-        sh.stop = !(isfinite(sn) && sn > 1.0e-10f);
-        sh.inv = sh.stop ? 0.0f : __fdiv_rn(1.0f, sn);
+      if (warp == 0) {
+        const float d = warp_seq_dot(nt, [&](int k, float& x, float& y) {
+          x = scv[k];
+          y = scv[k];
+        }, lane);
+        if (lane == 0) {
+          const float sn = __fsqrt_rn(0.0f < d ? d : 0.0f);
+          sh.stop = !(isfinite(sn) && sn > 1.0e-10f);
+          sh.inv = sh.stop ? 0.0f : __fdiv_rn(1.0f, sn);
+        }
       }
       __syncthreads();
       if (sh.stop) break;
@@ -442,21 +608,12 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(PlsEvalArgs a) {
       for (int t = threadIdx.x; t < nt; t += kEvalThreads) scv[t] = __fmul_rn(scv[t], inv);
       for (int j = threadIdx.x; j < p; j += kEvalThreads) w[j] = __fmul_rn(w[j], inv);
       __syncthreads();
-      for (int j = threadIdx.x; j < p; j += kEvalThreads) {
-        double acc = 0.0;
-        for (int t = 0; t < nt; t += 8) {
-          float zv[8], sv[8];
-#pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            const bool in = t + q < nt;
-            zv[q] = in ? Zs[static_cast<size_t>(a.train_idx[tb + t + q]) * p + j] : 0.0f;
-            sv[q] = in ? scv[t + q] : 0.0f;
-          }
-#pragma unroll
-          for (int q = 0; q < 8; ++q)
-            if (t + q < nt) acc = fma(static_cast<double>(zv[q]), static_cast<double>(sv[q]), acc);
-        }
-        ld[j] = __double2float_rn(acc);
+      for (int j = warp; j < p; j += kEvalWarps) {
+        const float v = warp_seq_dot(nt, [&](int k, float& x, float& y) {
+          x = Zs[static_cast<size_t>(tix[k]) * p + j];
+          y = scv[k];
+        }, lane);
+        if (lane == 0) ld[j] = v;
       }
       __syncthreads();
     }
@@ -465,34 +622,40 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(PlsEvalArgs a) {
     for (int q = 0; q < comp; ++q) {
       if (threadIdx.x == 0) {
         float proj = 0.0f;
-        for (int j = 0; j < p; ++j) proj = __fadd_rn(proj, __fmul_rn(Vg[static_cast<size_t>(j) * ldw + q], ld[j]));
+        for (int j = 0; j < p; ++j) proj = __fadd_rn(proj, __fmul_rn(Vsm[static_cast<size_t>(j) * ldw + q], ld[j]));
         sh.inv = proj;
       }
       __syncthreads();
       const float proj = sh.inv;
       for (int j = threadIdx.x; j < p; j += kEvalThreads)
-        ld[j] = __fsub_rn(ld[j], __fmul_rn(proj, Vg[static_cast<size_t>(j) * ldw + q]));
+        ld[j] = __fsub_rn(ld[j], __fmul_rn(proj, Vsm[static_cast<size_t>(j) * ldw + q]));
       __syncthreads();
     }
-    if (threadIdx.x == 0) {
-      const float d = __double2float_rn(sumsq_serial(ld, p));
-      const float ln = __fsqrt_rn(0.0f < d ? d : 0.0f);
-      sh.stop = !(isfinite(ln) && ln > 1.0e-10f);
-      sh.inv = ln;
+    if (warp == 0) {
+      const float d = warp_seq_dot(p, [&](int k, float& x, float& y) {
+        x = ld[k];
+        y = ld[k];
+      }, lane);
+      if (lane == 0) {
+        const float ln = __fsqrt_rn(0.0f < d ? d : 0.0f);
+        sh.stop = !(isfinite(ln) && ln > 1.0e-10f);
+        sh.inv = ln;
+      }
     }
     __syncthreads();
     if (sh.stop) break;
     const float ln = sh.inv;
     for (int j = threadIdx.x; j < p; j += kEvalThreads) {
       ld[j] = __fdiv_rn(ld[j], ln);
-      Wg[static_cast<size_t>(j) * ldw + comp] = w[j];
-      Vg[static_cast<size_t>(j) * ldw + comp] = ld[j];
+      Wsm[static_cast<size_t>(j) * ldw + comp] = w[j];
+      Vsm[static_cast<size_t>(j) * ldw + comp] = ld[j];
     }
     __syncthreads();
     // deflate the cross-product
     for (int k = threadIdx.x; k < m; k += kEvalThreads) {
       float acc = 0.0f;
-      for (int j = 0; j < p; ++j) acc = __fadd_rn(acc, __fmul_rn(ld[j], S[j + static_cast<size_t>(k) * p]));
+      const float* col = S + static_cast<size_t>(k) * p;
+      for (int j = 0; j < p; ++j) acc = __fadd_rn(acc, __fmul_rn(ld[j], col[j]));
       tv[k] = acc;
     }
     __syncthreads();
@@ -522,130 +685,179 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(PlsEvalArgs a) {
       a.eval_comp[s] = 1;
     }
     __syncthreads();
-    for (int v = threadIdx.x; v < nv; v += kEvalThreads) pred[val_out(v)] = static_cast<uint16_t>(sh.lab);
+    for (int v = threadIdx.x; v < nv; v += kEvalThreads)
+      pred[a.predict_mode ? v : vidx[v]] = static_cast<uint16_t>(sh.lab);
     return;
   }
 
   // --- LDA on the first nc score columns -----------------------------------
   const int nc = a.predict_mode ? fitted : min(a.requested, fitted);
   float* Ts = a.T + static_cast<size_t>(s) * L * NCm;  // by row: Ts[row * nc + q]
-  for (int t = threadIdx.x; t < nt; t += kEvalThreads) {
-    const int row = a.train_idx[tb + t];
-    const float* z = Zs + static_cast<size_t>(row) * p;
-    for (int q = 0; q < nc; ++q) Ts[static_cast<size_t>(row) * nc + q] = row_score(z, Wg, ldw, p, q);
+  {
+    float* tile = tiles + warp * kTile;
+    for (int b0 = warp * 32; b0 < nt; b0 += kEvalWarps * 32) {
+      const int t = b0 + lane;
+      const int row = t < nt ? tix[t] : -1;
+      for (int q0 = 0; q0 < nc; q0 += kMaxNC) {
+        const int nq = min(kMaxNC, nc - q0);
+        float acc[kMaxNC];
+        warp_scores(Zs, p, row, Wsm, ldw, q0, nq, tile, lane, acc);
+        if (row >= 0) {
+#pragma unroll
+          for (int q = 0; q < kMaxNC; ++q)
+            if (q < nq) Ts[static_cast<size_t>(row) * nc + q0 + q] = acc[q];
+        }
+      }
+    }
   }
   __syncthreads();
   // class sums (rows of each class in order) and score cross-products (all
-  // training rows in order): independent chains
+  // training rows in order): one warp per chain
   const int ncs = m * nc, ncp = nc * (nc + 1) / 2;
-  for (int it = threadIdx.x; it < ncs + ncp; it += kEvalThreads) {
+  for (int it = warp; it < ncs + ncp; it += kEvalWarps) {
+    float acc;
+    int k = 0, q = 0, rr = 0, col = 0;
     if (it < ncs) {
-      const int k = it / nc, q = it % nc;
+      k = it / nc;
+      q = it % nc;
       const int code = klist[k];
-      float acc = 0.0f;
-      for (int i = coff[code]; i < coff[code + 1]; ++i) {
+      acc = warp_chain(coff[code], coff[code + 1], [&](int i, float& v) {
         const int row = crow[i];
-        if (fold != nullptr && fold[row] == f) continue;
-        acc = __fadd_rn(acc, Ts[static_cast<size_t>(row) * nc + q]);
-      }
-      cs[k * nc + q] = acc;
+        if (fold != nullptr && fold[row] == f) return false;
+        v = Ts[static_cast<size_t>(row) * nc + q];
+        return true;
+      }, lane);
     } else {
-      int pr = it - ncs, rr = 0;
+      int pr = it - ncs;
       while (pr > rr) {
         pr -= rr + 1;
         ++rr;
       }
-      const int col = pr;
-      float acc = 0.0f;
-      for (int t = tb; t < te; t += 8) {
-        float x0[8], x1[8];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const int row = t + q < te ? a.train_idx[t + q] : 0;
-          x0[q] = Ts[static_cast<size_t>(row) * nc + rr];
-          x1[q] = Ts[static_cast<size_t>(row) * nc + col];
-        }
-#pragma unroll
-        for (int q = 0; q < 8; ++q)
-          if (t + q < te) acc = __fadd_rn(acc, __fmul_rn(x0[q], x1[q]));
+      col = pr;
+      acc = warp_chain(0, nt, [&](int i, float& v) {
+        const float* tr = Ts + static_cast<size_t>(tix[i]) * nc;
+        v = __fmul_rn(tr[rr], tr[col]);
+        return true;
+      }, lane);
+    }
+    if (lane == 0) {
+      if (it < ncs) {
+        cs[k * nc + q] = acc;
+      } else {
+        cp[rr * nc + col] = acc;
+        cp[col * nc + rr] = acc;
       }
-      cp[rr * nc + col] = acc;
-      cp[col * nc + rr] = acc;
     }
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int k = 0; k < m; ++k) {
-      const int c = cnt[klist[k]];
-      const float inv = c > 0 ? __fdiv_rn(1.0f, static_cast<float>(c)) : 0.0f;
-      for (int q = 0; q < nc; ++q) cs[k * nc + q] = __fmul_rn(cs[k * nc + q], inv);
+  // fit_lda_from_score_statistics_float, parallel where the reference's loops
+  // are independent of one another
+  for (int it = threadIdx.x; it < m * nc; it += kEvalThreads) {
+    const int k = it / nc, c = cnt[klist[k]];
+    const float inv = c > 0 ? __fdiv_rn(1.0f, static_cast<float>(c)) : 0.0f;
+    cs[it] = __fmul_rn(cs[it], inv);
+  }
+  __syncthreads();
+  const float df = static_cast<float>(max(1, nt - m));
+  for (int it = threadIdx.x; it < ncp; it += kEvalThreads) {
+    int pr = it, rr = 0;
+    while (pr > rr) {
+      pr -= rr + 1;
+      ++rr;
     }
-    const float df = static_cast<float>(max(1, nt - m));
-    float trace = 0.0f;
-    for (int rr = 0; rr < nc; ++rr) {
-      for (int col = 0; col <= rr; ++col) {
-        float between = 0.0f;
-        for (int k = 0; k < m; ++k)
-          between = __fadd_rn(between, __fmul_rn(__fmul_rn(static_cast<float>(cnt[klist[k]]), cs[k * nc + rr]),
-                                                 cs[k * nc + col]));
-        const float cv = __fdiv_rn(__fsub_rn(cp[rr * nc + col], between), df);
-        pooled[rr * nc + col] = cv;
-        pooled[col * nc + rr] = cv;
-      }
-      trace = __fadd_rn(trace, pooled[rr * nc + rr]);
-    }
+    const int col = pr;
+    float between = 0.0f;
     for (int k = 0; k < m; ++k)
-      for (int q = 0; q < nc; ++q) rhs[q * m + k] = cs[k * nc + q];
+      between = __fadd_rn(between, __fmul_rn(__fmul_rn(static_cast<float>(cnt[klist[k]]), cs[k * nc + rr]),
+                                             cs[k * nc + col]));
+    const float cv = __fdiv_rn(__fsub_rn(cp[rr * nc + col], between), df);
+    pooled[rr * nc + col] = cv;
+    pooled[col * nc + rr] = cv;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    // the ridge grid and the Cholesky factor (independent of the right-hand sides)
+    float trace = 0.0f;
+    for (int rr = 0; rr < nc; ++rr) trace = __fadd_rn(trace, pooled[rr * nc + rr]);
     const float ridge_scale =
         (isfinite(trace) && trace > 0.0f) ? __fdiv_rn(trace, static_cast<float>(max(1, nc))) : 1.0f;
     const float grid[6] = {1e-8f, 1e-6f, 1e-5f, 1e-4f, 1e-3f, 1e-2f};
     bool ok = false;
     for (int g = 0; g < 6 && !ok; ++g) {
       const float lambda = __fmul_rn(grid[g], ridge_scale);
-      for (int i = 0; i < nc * nc; ++i) cov[i] = pooled[i];
-      for (int q = 0; q < nc; ++q) cov[q * nc + q] = __fadd_rn(cov[q * nc + q], lambda);
-      ok = chol_solve(cov, nc, rhs, m, Lc, sol);
-    }
-    if (!ok) {
-      a.status[s] = 2;
-      sh.stop = 1;
-    } else {
-      const float* lp = a.logprior + a.lp_off[s];
-      for (int k = 0; k < m; ++k) {
-        float dot_mu = 0.0f;
-        for (int q = 0; q < nc; ++q) {
-          lin[k * nc + q] = sol[q * m + k];
-          dot_mu = __fadd_rn(dot_mu, __fmul_rn(cs[k * nc + q], lin[k * nc + q]));
+      ok = true;
+      for (int row = 0; row < nc && ok; ++row) {
+        for (int col = 0; col <= row && ok; ++col) {
+          float v = pooled[row * nc + col];
+          if (row == col) v = __fadd_rn(v, lambda);
+          for (int q = 0; q < col; ++q) v = __fsub_rn(v, __fmul_rn(Lc[row * nc + q], Lc[col * nc + q]));
+          if (row == col) {
+            if (!isfinite(v) || v <= 0.0f) ok = false;
+            else Lc[row * nc + col] = __fsqrt_rn(v);
+          } else {
+            const float dgl = Lc[col * nc + col];
+            if (!isfinite(dgl) || dgl <= 0.0f) ok = false;
+            else Lc[row * nc + col] = __fdiv_rn(v, dgl);
+          }
         }
-        cst[k] = __fadd_rn(__fmul_rn(-0.5f, dot_mu), lp[cnt[klist[k]]]);
       }
-      sh.stop = 0;
     }
+    sh.fail = ok ? 0 : 1;
+    if (!ok) a.status[s] = 2;
     a.eval_comp[s] = nc;
   }
   __syncthreads();
-  if (sh.stop) return;
-  for (int v = threadIdx.x; v < nv; v += kEvalThreads) {
-    const float* z = val_row(v);
-    float sr[16];
-    int best = 0;
-    float bs = -INFINITY;
-    // scores in chunks of 16 components (one chain per component)
-    for (int k = 0; k < m; ++k) {
-      float sc = cst[k];
-      for (int q0 = 0; q0 < nc; q0 += 16) {
-        const int cntq = min(16, nc - q0);
-        if (k == 0 || nc > 16) {
-          for (int q = 0; q < cntq; ++q) sr[q] = row_score(z, Wg, ldw, p, q0 + q);
-        }
-        for (int q = 0; q < cntq; ++q) sc = __fadd_rn(sc, __fmul_rn(sr[q], lin[k * nc + q0 + q]));
+  if (sh.fail) return;
+  const float* lp = a.logprior + a.lp_off[s];
+  for (int k = threadIdx.x; k < m; k += kEvalThreads) {
+    // forward and backward substitution for the right-hand side of class k
+    for (int row = 0; row < nc; ++row) {
+      float v = cs[k * nc + row];
+      for (int q = 0; q < row; ++q) v = __fsub_rn(v, __fmul_rn(Lc[row * nc + q], sol[q * m + k]));
+      sol[row * m + k] = __fdiv_rn(v, Lc[row * nc + row]);
+    }
+    for (int row = nc - 1; row >= 0; --row) {
+      float v = sol[row * m + k];
+      for (int q = row + 1; q < nc; ++q) v = __fsub_rn(v, __fmul_rn(Lc[q * nc + row], sol[q * m + k]));
+      sol[row * m + k] = __fdiv_rn(v, Lc[row * nc + row]);
+    }
+    float dot_mu = 0.0f;
+    for (int q = 0; q < nc; ++q) {
+      lin[k * nc + q] = sol[q * m + k];
+      dot_mu = __fadd_rn(dot_mu, __fmul_rn(cs[k * nc + q], lin[k * nc + q]));
+    }
+    cst[k] = __fadd_rn(__fmul_rn(-0.5f, dot_mu), lp[cnt[klist[k]]]);
+  }
+  __syncthreads();
+  // --- predictions ---------------------------------------------------------
+  {
+    float* tile = tiles + warp * kTile;
+    for (int b0 = warp * 32; b0 < nv; b0 += kEvalWarps * 32) {
+      const int v = b0 + lane;
+      const int row = v < nv ? (a.predict_mode ? v : vidx[v]) : -1;
+      float sr[kMaxComp];
+      for (int q0 = 0; q0 < nc; q0 += kMaxNC) {
+        const int nq = min(kMaxNC, nc - q0);
+        float acc[kMaxNC];
+        warp_scores(vbase, p, row, Wsm, ldw, q0, nq, tile, lane, acc);
+#pragma unroll
+        for (int q = 0; q < kMaxNC; ++q)
+          if (q < nq) sr[q0 + q] = acc[q];
       }
-      if (sc > bs) {
-        bs = sc;
-        best = k;
+      if (row >= 0) {
+        int best = 0;
+        float bs = -INFINITY;
+        for (int k = 0; k < m; ++k) {
+          float sc = cst[k];
+          for (int q = 0; q < nc; ++q) sc = __fadd_rn(sc, __fmul_rn(sr[q], lin[k * nc + q]));
+          if (sc > bs) {
+            bs = sc;
+            best = k;
+          }
+        }
+        pred[row] = static_cast<uint16_t>(klist[best]);
       }
     }
-    pred[val_out(v)] = static_cast<uint16_t>(klist[best]);
   }
 }
 
@@ -718,20 +930,26 @@ int pls_build_gram(const PlsPrepArgs& a, const uint8_t* want, cudaStream_t st) {
   return static_cast<int>(cudaGetLastError());
 }
 
-size_t pls_eval_smem(int p, int C0max, int requested) {
+size_t pls_eval_smem(int p, int C0max, int requested, int max_components, bool s_in_smem, bool tiles_after_s) {
   auto al = [](size_t v) { return (v + 15) / 16 * 16; };
   const size_t C = static_cast<size_t>(C0max), N = static_cast<size_t>(requested);
   size_t b = 64;
   b += 2 * al(sizeof(int) * C);
   b += 3 * al(sizeof(float) * p) + al(sizeof(float) * C);
-  b += al(sizeof(float) * C * N) + 4 * al(sizeof(float) * N * N) + 2 * al(sizeof(float) * N * C);
+  b += 2 * al(sizeof(float) * p * max_components);
+  b += al(sizeof(float) * C * N) + 3 * al(sizeof(float) * N * N) + al(sizeof(float) * N * C);
   b += al(sizeof(float) * C * N) + al(sizeof(float) * C);
+  const size_t cross = s_in_smem ? sizeof(float) * static_cast<size_t>(p) * C : 0;
+  const size_t tiles = sizeof(float) * static_cast<size_t>(kEvalWarps) * kTile;
+  b += tiles_after_s ? cross + tiles : (cross > tiles ? cross : tiles);
   return b;
 }
 
 int pls_evaluate(const PlsEvalArgs& a, cudaStream_t st) {
   const int S = a.problems * a.F;
-  const size_t smem = pls_eval_smem(a.p, a.C0max, a.requested);
+  if (a.requested > kMaxComp || a.max_components > kMaxComp) return static_cast<int>(cudaErrorInvalidValue);
+  const size_t smem =
+      pls_eval_smem(a.p, a.C0max, a.requested, a.max_components, a.s_in_smem != 0, a.tiles_after_s != 0);
   if (smem > 48 * 1024) {
     const cudaError_t e =
         cudaFuncSetAttribute(eval_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));

@@ -47,6 +47,8 @@ struct PlsEvalArgs {
   int max_components;    // SIMPLS rank limit
   int requested;         // components evaluated: min(requested, fitted rank)
   int predict_mode;      // 1: rows to predict are Zv rows 0..NV-1
+  int s_in_smem;         // 1: the label cross-product of a slice lives in shared memory
+  int tiles_after_s;     // 1: some slice computes training scores during the fit (no fold Gram)
   const float* Z;        // S x L x p
   const float* xsum;     // S x p
   const float* gram;     // S x p x p, or nullptr
@@ -76,7 +78,10 @@ struct PlsEvalArgs {
 };
 
 int pls_evaluate(const PlsEvalArgs& a, cudaStream_t st);
-size_t pls_eval_smem(int p, int C0max, int requested);
+// Dynamic shared memory of the evaluation kernel; components are limited to 64.
+size_t pls_eval_smem(int p, int C0max, int requested, int max_components, bool s_in_smem,
+                     bool tiles_after_s);
+constexpr int kPlsMaxComponents = 64;
 
 // out[i] = x row rows[i] (p columns), i < nrows.
 int pls_gather_rows(const float* x, int p, const int* rows, size_t nrows, float* out, cudaStream_t st);
