@@ -70,6 +70,12 @@ typedef struct kgb_matrix_options {
   int32_t reserved;
   uint64_t seed;             /* default 1234 */
   kgb_policy policy;
+  /* Learned relabelling proposal (kNN classifier): NULL = the plain proposal
+   * of the reference; else the 4801 network parameters of
+   * kgb_proposal_train.  No counterpart in the reference. */
+  const float* proposal_weights;
+  int32_t snapshot_cycle;    /* cycle whose starting state kgb_matrix_result.snapshot_* record */
+  int32_t reserved2;
 } kgb_matrix_options;
 
 /* Caller-allocated outputs of a KODAMA.matrix call. NULL = not wanted
@@ -95,6 +101,13 @@ typedef struct kgb_matrix_result {
   int32_t res_on_device;     /* in: 1 = `res` is a device pointer (the label matrix stays in HBM) */
   int32_t reserved;
   int32_t* pls_counters;     /* runs x 2: PLS coarsening attempted / accepted (classifier 1), or NULL */
+  /* Training data for the learned proposal (kNN classifier), or NULL: the
+   * state at the start of cycle opt->snapshot_cycle of every run, per
+   * landmark 8 features (runs x L x 8, L = effective_landmarks) and flags
+   * (runs x L): bit 0 = candidate (label differs from its CV prediction),
+   * bit 1 = the run's final best label equals that prediction. */
+  float* snapshot_features;
+  uint8_t* snapshot_flags;
 } kgb_matrix_result;
 
 /* Replaces KODAMAMatrix_CUDA (kodama.hpp:1077-1083; dispatch
@@ -204,6 +217,30 @@ int kgb_plslda_predict(const float* train, int32_t n, int32_t p, const int32_t* 
 int kgb_core_plslda(const float* x, int32_t n, int32_t p, const int32_t* labels, const int32_t* constrain,
                     const int32_t* fixed, const kgb_core_options* opt, const kgb_pls_options* pls,
                     kgb_core_result* out);
+
+/* ---- Learned relabelling proposal (no counterpart in the reference) ------
+ * A 3-layer perceptron (8 -> 64 -> 64 -> 1, bfloat16 weights and
+ * activations, float accumulation) that ranks the landmarks whose label
+ * differs from their CV prediction; kgb_matrix_options.proposal_weights makes
+ * a KODAMA.matrix run relabel the best-ranked candidates instead of uniformly
+ * drawn ones, every move still accepted or rejected by the exact CV accuracy.
+ * Parameters: 4801 floats (W1 8x64, b1 64, W2 64x64, b2 64, w3 64, b3). */
+#define KGB_PROPOSAL_PARAMS 4801
+
+/* Trains the network on n rows of features (n x 8) and 0/1 targets with
+ * Adam (mean binary cross-entropy), minibatches drawn in a seeded order.
+ * weights_init may be NULL (seeded He-uniform start).  loss_per_epoch has
+ * `epochs` entries (may be NULL). */
+int kgb_proposal_train(const float* features, const uint8_t* targets, int32_t n, int32_t epochs, int32_t batch,
+                       float learning_rate, uint64_t seed, const float* weights_init, int32_t device,
+                       float* weights_out, float* loss_per_epoch);
+
+/* Gradient of the mean loss over n rows at `weights` (4801 floats) and the loss. */
+int kgb_proposal_gradient(const float* weights, const float* features, const uint8_t* targets, int32_t n,
+                          int32_t device, float* grad, float* loss);
+
+/* Logits of n rows. */
+int kgb_proposal_predict(const float* weights, const float* features, int32_t n, int32_t device, float* logits);
 
 /* Exact kNN graph on the device: for each row its K nearest other rows by
  * squared Euclidean distance (float32, coordinate order, no FMA), ties by

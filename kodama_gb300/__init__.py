@@ -25,7 +25,7 @@ import numpy as np
 
 from . import _native as N
 
-__all__ = ["KODAMA_matrix", "CoreKNNGraph", "CoreKNNGraph_batch", "knn_graph",
+__all__ = ["train_proposal", "proposal_gradient", "proposal_predict", "KODAMA_matrix", "CoreKNNGraph", "CoreKNNGraph_batch", "knn_graph",
            "KODAMADissimilarityInPlace", "PLSLDACV", "PLSLDAPredict", "CorePLSLDA", "PLSCVResult", "MatrixResult", "CoreResult", "EvolutionPolicy",
            "library_path", "version", "launch_count"]
 
@@ -93,6 +93,8 @@ class MatrixResult:
     timings: dict = field(default_factory=dict)
     kernel_ms: dict = field(default_factory=dict)
     pls_counters: np.ndarray | None = None   # (runs, 2): PLS coarsening attempted / accepted
+    snapshot_features: np.ndarray | None = None  # (runs, L, 8) learned-proposal training features
+    snapshot_flags: np.ndarray | None = None     # (runs, L): bit 0 candidate, bit 1 target
 
 
 _TIMING_NAMES = ("total", "knn_graph", "shared_landmark_partition", "landmark_initialization",
@@ -118,9 +120,12 @@ def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitt
                   graph_neighbors=100, folds=5, knn_k=30, seed=1234, materialize_graph=False,
                   apply_dissimilarity=True, index_base=-1, device=0, host_threads=0,
                   policy="full", res_out=None, first_run=1, classifier="knn",
-                  components=50) -> MatrixResult:
+                  components=50, proposal_weights=None, snapshot_cycle=None) -> MatrixResult:
     """KODAMA.matrix on the GPU with the kNN (``classifier="knn"``) or PLS-LDA
     (``classifier="pls"``, ``components`` latent components) classifier.
+    ``proposal_weights`` (the 4801 parameters of ``train_proposal``) selects
+    the learned relabelling proposal; ``snapshot_cycle`` records its training
+    data (``snapshot_features`` / ``snapshot_flags``) at that cycle.
 
     ``graph`` = (indices, distances) of shape (n, K) runs the graph-input path
     (KODAMAMatrixFromGraphData_CUDA); without it the exact kNN graph is built
@@ -172,6 +177,21 @@ def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitt
     out.run_counters = counters.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
     out.cycle_diag = cdiag.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
     out.pls_counters = plsc.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+    wts = None
+    if proposal_weights is not None:
+        wts = np.ascontiguousarray(proposal_weights, dtype=np.float32)
+        if wts.shape != (N.PROPOSAL_PARAMS,):
+            raise ValueError(f"proposal_weights must hold {N.PROPOSAL_PARAMS} floats")
+        opt.proposal_weights = wts.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    snap_f = snap_g = None
+    if snapshot_cycle is not None:
+        if not 0 <= snapshot_cycle < cycles:
+            raise ValueError("snapshot_cycle must lie in [0, cycles)")
+        opt.snapshot_cycle = int(snapshot_cycle)
+        snap_f = np.zeros(runs * n * 8, np.float32)  # the landmarks are fewer than n
+        snap_g = np.zeros(runs * n, np.uint8)
+        out.snapshot_features = snap_f.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        out.snapshot_flags = snap_g.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
     if materialize_graph:
         out.knn_idx = kidx.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
         out.knn_dist = kdist.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
@@ -197,7 +217,11 @@ def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitt
         knn_dist=kdist[:, :k].copy() if (materialize_graph and k) else None,
         effective_landmarks=out.effective_landmarks,
         timings=dict(zip(_TIMING_NAMES, list(out.timings))),
-        kernel_ms=dict(zip(_KERNEL_NAMES, list(out.kernel_ms))), pls_counters=plsc)
+        kernel_ms=dict(zip(_KERNEL_NAMES, list(out.kernel_ms))), pls_counters=plsc,
+        snapshot_features=None if snap_f is None else
+        snap_f[: runs * out.effective_landmarks * 8].reshape(runs, out.effective_landmarks, 8),
+        snapshot_flags=None if snap_g is None else
+        snap_g[: runs * out.effective_landmarks].reshape(runs, out.effective_landmarks))
 
 
 def launch_count() -> int:
@@ -401,3 +425,42 @@ def CorePLSLDA(x, labels, *, constrain=None, fixed=None, cycles=100, folds=10, s
     N.check(N.load().kgb_core_plslda(_ptr(xa), n, p, _ptr(lab), _ptr(con), _ptr(fix), ctypes.byref(opt),
                                      ctypes.byref(popt), ctypes.byref(r)))
     return _wrap_core(r, bufs, cycles)
+
+
+# ---------------------------------------------------------------------------
+# Learned relabelling proposal (no counterpart in the reference)
+# ---------------------------------------------------------------------------
+
+def train_proposal(features, targets, *, epochs=20, batch=4096, learning_rate=2e-3, seed=1,
+                   weights_init=None, device=0):
+    """Trains the proposal network (kgb_proposal_train): returns (weights, loss per epoch)."""
+    f = np.ascontiguousarray(features, dtype=np.float32).reshape(-1, 8)
+    t = np.ascontiguousarray(targets, dtype=np.uint8).reshape(-1)
+    if len(t) != len(f):
+        raise ValueError("one target per feature row")
+    w = np.zeros(N.PROPOSAL_PARAMS, np.float32)
+    losses = np.zeros(max(epochs, 1), np.float32)
+    init = None if weights_init is None else np.ascontiguousarray(weights_init, dtype=np.float32)
+    N.check(N.load().kgb_proposal_train(_ptr(f), _ptr(t), len(f), epochs, batch, learning_rate, seed, _ptr(init),
+                                        device, _ptr(w), _ptr(losses)))
+    return w, losses[:epochs]
+
+
+def proposal_gradient(weights, features, targets, *, device=0):
+    """Mean-loss gradient of the proposal network on the GPU: (grad, loss)."""
+    w = np.ascontiguousarray(weights, dtype=np.float32)
+    f = np.ascontiguousarray(features, dtype=np.float32).reshape(-1, 8)
+    t = np.ascontiguousarray(targets, dtype=np.uint8).reshape(-1)
+    g = np.zeros(N.PROPOSAL_PARAMS, np.float32)
+    loss = ctypes.c_float(0.0)
+    N.check(N.load().kgb_proposal_gradient(_ptr(w), _ptr(f), _ptr(t), len(f), device, _ptr(g), ctypes.byref(loss)))
+    return g, float(loss.value)
+
+
+def proposal_predict(weights, features, *, device=0):
+    """Logits of the proposal network on the GPU."""
+    w = np.ascontiguousarray(weights, dtype=np.float32)
+    f = np.ascontiguousarray(features, dtype=np.float32).reshape(-1, 8)
+    out = np.zeros(len(f), np.float32)
+    N.check(N.load().kgb_proposal_predict(_ptr(w), _ptr(f), len(f), device, _ptr(out)))
+    return out

@@ -13,6 +13,7 @@ import os
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libkodama_gb300.so")
 
+PROPOSAL_PARAMS = 4801
 KGB_OK, KGB_EINVAL, KGB_ENOMEM, KGB_ECUDA, KGB_ETIMEOUT, KGB_EINTERNAL = range(6)
 
 EXPORTED = (
@@ -25,6 +26,9 @@ EXPORTED = (
     "kgb_plsldacv",
     "kgb_plslda_predict",
     "kgb_core_plslda",
+    "kgb_proposal_train",
+    "kgb_proposal_gradient",
+    "kgb_proposal_predict",
     "kgb_knn_graph",
     "kgb_dissimilarity_inplace",
     "kgb_dissimilarity_inplace_device",
@@ -44,7 +48,9 @@ class MatrixOptions(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int32) for n in (
         "runs", "cycles", "landmarks", "splitting", "graph_neighbors", "folds", "knn_k",
         "classifier", "components", "materialize_graph", "apply_dissimilarity", "metric",
-        "device", "host_threads", "first_run", "reserved")] + [("seed", ctypes.c_uint64), ("policy", Policy)]
+        "device", "host_threads", "first_run", "reserved")] + [
+        ("seed", ctypes.c_uint64), ("policy", Policy), ("proposal_weights", ctypes.POINTER(ctypes.c_float)),
+        ("snapshot_cycle", ctypes.c_int32), ("reserved2", ctypes.c_int32)]
 
 
 class MatrixResult(ctypes.Structure):
@@ -65,6 +71,8 @@ class MatrixResult(ctypes.Structure):
         ("res_on_device", ctypes.c_int32),
         ("reserved", ctypes.c_int32),
         ("pls_counters", ctypes.POINTER(ctypes.c_int32)),
+        ("snapshot_features", ctypes.POINTER(ctypes.c_float)),
+        ("snapshot_flags", ctypes.POINTER(ctypes.c_uint8)),
     ]
 
 
@@ -125,6 +133,9 @@ def load():
                                              ctypes.POINTER(CoreResult)]
     lib.kgb_knn_graph.argtypes = [P, i32, i32, i32, i32, P, P]
     lib.kgb_dissimilarity_inplace.argtypes = [P, P, i32, i32, P, i32, i32]
+    lib.kgb_proposal_train.argtypes = [P, P, i32, i32, i32, ctypes.c_float, ctypes.c_uint64, P, i32, P, P]
+    lib.kgb_proposal_gradient.argtypes = [P, P, P, i32, i32, P, P]
+    lib.kgb_proposal_predict.argtypes = [P, P, i32, i32, P]
     lib.kgb_plsldacv.argtypes = [P, i32, i32, P, P, ctypes.POINTER(PlsOptions), P, P, P, P]
     lib.kgb_plslda_predict.argtypes = [P, i32, i32, P, P, i32, ctypes.POINTER(PlsOptions), P]
     lib.kgb_core_plslda.argtypes = [P, i32, i32, P, P, P, ctypes.POINTER(CoreOptions),

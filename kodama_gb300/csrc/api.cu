@@ -12,6 +12,7 @@
 #include "knn.cuh"
 #include "launch_count.cuh"
 #include "pls.cuh"
+#include "mlp.cuh"
 
 #include <cuda_runtime.h>
 
@@ -24,6 +25,7 @@
 #include <future>
 #include <limits>
 #include <map>
+#include <numeric>
 #include <random>
 #include <stdexcept>
 #include <string>
@@ -932,9 +934,36 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   ev_tables = ctx.mark();
   P.nb = d_nb;
   P.sc = d_sc;
+  if (o->proposal_weights != nullptr) {
+    float* master = ctx.upload(o->proposal_weights, kgb::kMlpParams);
+    float* rounded = ctx.alloc<float>(kgb::kMlpParams);
+    ck_launch(kgb::mlp_round_params(master, rounded, st), "proposal weights");
+    P.mlp = rounded;
+  }
+  const bool snap = out->snapshot_features != nullptr && out->snapshot_flags != nullptr;
+  if (snap) {
+    P.snap_cycle = o->snapshot_cycle;
+    P.snap_feat = ctx.alloc<float>(static_cast<size_t>(M) * L * kgb::kMlpIn);
+    P.snap_cur = ctx.alloc<uint16_t>(static_cast<size_t>(M) * L);
+    P.snap_pred = ctx.alloc<uint16_t>(static_cast<size_t>(M) * L);
+    ck(cudaMemsetAsync(P.snap_feat, 0, sizeof(float) * M * L * kgb::kMlpIn, st), "memset");
+    ck(cudaMemsetAsync(P.snap_cur, 0, sizeof(uint16_t) * M * L, st), "memset");
+    ck(cudaMemsetAsync(P.snap_pred, 0, sizeof(uint16_t) * M * L, st), "memset");
+  }
   ev_evo0 = ctx.mark();
   eb = run_evolution(ctx, P, C0max);
   ev_evo1 = ctx.mark();
+  if (snap) {
+    const size_t ML = static_cast<size_t>(M) * L;
+    std::vector<uint16_t> scur(ML), spred(ML), best(ML);
+    ctx.download(out->snapshot_features, P.snap_feat, ML * kgb::kMlpIn);
+    ctx.download(scur.data(), P.snap_cur, ML);
+    ctx.download(spred.data(), P.snap_pred, ML);
+    ctx.download(best.data(), eb.clbest, ML);
+    ctx.sync();
+    for (size_t i = 0; i < ML; ++i)
+      out->snapshot_flags[i] = static_cast<uint8_t>((scur[i] != spred[i] ? 1 : 0) | (best[i] == spred[i] ? 2 : 0));
+  }
 
   // projection of non-landmarks and result matrix
   d_res = ctx.alloc<int>(static_cast<size_t>(M) * n);
@@ -1584,6 +1613,117 @@ int kgb_core_plslda(const float* x, int32_t n, int32_t p, const int32_t* labels,
     out->accbest = best[0];
     out->scorebest = best[1];
     for (int q = 0; q < 18; ++q) out->counters[q] = counters[q];
+  });
+}
+
+int kgb_proposal_train(const float* features, const uint8_t* targets, int32_t n, int32_t epochs, int32_t batch,
+                       float learning_rate, uint64_t seed, const float* weights_init, int32_t device,
+                       float* weights_out, float* loss_per_epoch) {
+  return guarded([&]() {
+    if (features == nullptr || targets == nullptr || weights_out == nullptr) fail(KGB_EINVAL, "null pointer");
+    if (n < 1 || epochs < 0 || batch < 1) fail(KGB_EINVAL, "invalid training sizes");
+    std::vector<float> w(kgb::kMlpParams, 0.0f);
+    if (weights_init != nullptr) {
+      std::copy(weights_init, weights_init + kgb::kMlpParams, w.begin());
+    } else {
+      // He-uniform weights, zero biases, from a seeded engine
+      std::mt19937_64 rng(seed);
+      auto fill = [&](int off, int count, int fan_in) {
+        const float a = std::sqrt(6.0f / static_cast<float>(fan_in));
+        std::uniform_real_distribution<float> u(-a, a);
+        for (int i = 0; i < count; ++i) w[off + i] = u(rng);
+      };
+      fill(kgb::kMlpW1, kgb::kMlpIn * kgb::kMlpHidden, kgb::kMlpIn);
+      fill(kgb::kMlpW2, kgb::kMlpHidden * kgb::kMlpHidden, kgb::kMlpHidden);
+      fill(kgb::kMlpW3, kgb::kMlpHidden, kgb::kMlpHidden);
+    }
+    Ctx ctx(device);
+    cudaStream_t st = ctx.stream();
+    const float* d_feat = ctx.upload(features, static_cast<size_t>(n) * kgb::kMlpIn);
+    const uint8_t* d_tgt = ctx.upload(targets, static_cast<size_t>(n));
+    float* master = ctx.upload(w.data(), w.size());
+    float* rounded = ctx.alloc<float>(kgb::kMlpParams);
+    float* m = ctx.alloc<float>(kgb::kMlpParams);
+    float* v = ctx.alloc<float>(kgb::kMlpParams);
+    float* grad = ctx.alloc<float>(kgb::kMlpParams);
+    ck(cudaMemsetAsync(m, 0, sizeof(float) * kgb::kMlpParams, st), "memset");
+    ck(cudaMemsetAsync(v, 0, sizeof(float) * kgb::kMlpParams, st), "memset");
+    const int bsz = std::min(batch, n);
+    const int nb = (n + bsz - 1) / bsz;
+    float* partial = ctx.alloc<float>(static_cast<size_t>((bsz + kgb::kMlpGradBlock - 1) / kgb::kMlpGradBlock) *
+                                      (kgb::kMlpParams + 1));
+    float* d_loss = ctx.alloc<float>(nb);
+    int* d_idx = ctx.alloc<int>(n);
+    std::vector<int> order(static_cast<size_t>(n));
+    std::vector<float> losses(static_cast<size_t>(nb));
+    int step = 0;
+    for (int ep = 0; ep < epochs; ++ep) {
+      std::iota(order.begin(), order.end(), 0);
+      std::mt19937_64 rng(seed + 1000003ull * static_cast<uint64_t>(ep + 1));
+      std::shuffle(order.begin(), order.end(), rng);
+      ck(cudaMemcpyAsync(d_idx, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st), "H2D");
+      for (int b = 0; b < nb; ++b) {
+        const int rows = std::min(bsz, n - b * bsz);
+        ck_launch(kgb::mlp_round_params(master, rounded, st), "round");
+        ck_launch(kgb::mlp_gradient(rounded, d_feat, d_tgt, d_idx + static_cast<size_t>(b) * bsz, rows, partial, grad,
+                                    d_loss + b, st),
+                  "gradient");
+        ck_launch(kgb::mlp_adam(master, m, v, grad, learning_rate, ++step, st), "adam");
+      }
+      ctx.download(losses.data(), d_loss, losses.size());
+      ctx.sync();  // `order` is rewritten next epoch
+      if (loss_per_epoch) {
+        double acc = 0.0;
+        for (float l : losses) acc += l;
+        loss_per_epoch[ep] = static_cast<float>(acc / nb);
+      }
+    }
+    ctx.download(weights_out, master, kgb::kMlpParams);
+    ctx.sync();
+  });
+}
+
+int kgb_proposal_gradient(const float* weights, const float* features, const uint8_t* targets, int32_t n,
+                          int32_t device, float* grad, float* loss) {
+  return guarded([&]() {
+    if (weights == nullptr || features == nullptr || targets == nullptr || grad == nullptr || loss == nullptr)
+      fail(KGB_EINVAL, "null pointer");
+    if (n < 1) fail(KGB_EINVAL, "no rows");
+    Ctx ctx(device);
+    cudaStream_t st = ctx.stream();
+    float* master = ctx.upload(weights, kgb::kMlpParams);
+    float* rounded = ctx.alloc<float>(kgb::kMlpParams);
+    ck_launch(kgb::mlp_round_params(master, rounded, st), "round");
+    std::vector<int> idx(static_cast<size_t>(n));
+    std::iota(idx.begin(), idx.end(), 0);
+    float* partial = ctx.alloc<float>(static_cast<size_t>((n + kgb::kMlpGradBlock - 1) / kgb::kMlpGradBlock) *
+                                      (kgb::kMlpParams + 1));
+    float* d_grad = ctx.alloc<float>(kgb::kMlpParams);
+    float* d_loss = ctx.alloc<float>(1);
+    ck_launch(kgb::mlp_gradient(rounded, ctx.upload(features, static_cast<size_t>(n) * kgb::kMlpIn),
+                                ctx.upload(targets, static_cast<size_t>(n)), ctx.upload(idx.data(), idx.size()), n,
+                                partial, d_grad, d_loss, st),
+              "gradient");
+    ctx.download(grad, d_grad, kgb::kMlpParams);
+    ctx.download(loss, d_loss, 1);
+    ctx.sync();
+  });
+}
+
+int kgb_proposal_predict(const float* weights, const float* features, int32_t n, int32_t device, float* logits) {
+  return guarded([&]() {
+    if (weights == nullptr || features == nullptr || logits == nullptr) fail(KGB_EINVAL, "null pointer");
+    if (n < 1) return;
+    Ctx ctx(device);
+    cudaStream_t st = ctx.stream();
+    float* master = ctx.upload(weights, kgb::kMlpParams);
+    float* rounded = ctx.alloc<float>(kgb::kMlpParams);
+    ck_launch(kgb::mlp_round_params(master, rounded, st), "round");
+    float* d_out = ctx.alloc<float>(n);
+    ck_launch(kgb::mlp_predict(rounded, ctx.upload(features, static_cast<size_t>(n) * kgb::kMlpIn), n, d_out, st),
+              "predict");
+    ctx.download(logits, d_out, n);
+    ctx.sync();
   });
 }
 

@@ -24,6 +24,7 @@
 #include "launch_count.cuh"
 #include "rng.cuh"
 #include "crmath.cuh"
+#include "mlp.cuh"
 
 #include <cuda_runtime.h>
 #include <float.h>
@@ -815,6 +816,105 @@ __device__ void relabel_serial(const EvolveParams& P, const Smem& s, const uint1
   }
 }
 
+// ---------------------------------------------------------------------------
+// Learned relabelling proposal (mlp.cuh)
+// ---------------------------------------------------------------------------
+
+// Features of `row` in the current state (s.cur / s.curpred), census of
+// s.cur in `cnt_cur`: among the row's fold-filtered neighbours, the fractions
+// sharing its label, holding its prediction as label, predicting its
+// prediction and whose label equals their prediction; the sizes of its label
+// and prediction classes; the run's progress; the fraction of valid
+// neighbours.
+__device__ void proposal_features(const EvolveParams& P, const Smem& s, int prob, int row, const int* cnt_cur,
+                                  float progress, float* f) {
+  const uint16_t* nbr = P.nb + (static_cast<size_t>(prob) * P.L + row) * P.w;
+  const int c = s.cur[row], q = s.curpred[row];
+  int nv = 0, same_cur = 0, same_pred = 0, pred_pred = 0, stable = 0;
+  for (int j = 0; j < P.w; ++j) {
+    const int id = nbr[j];
+    if (id == kNoRow) break;
+    ++nv;
+    const int lc = s.cur[id], lp = s.curpred[id];
+    same_cur += lc == c;
+    same_pred += lc == q;
+    pred_pred += lp == q;
+    stable += lc == lp;
+  }
+  const float inv = nv > 0 ? 1.0f / static_cast<float>(nv) : 0.0f;
+  const float invL = 1.0f / static_cast<float>(P.L);
+  f[0] = same_cur * inv;
+  f[1] = same_pred * inv;
+  f[2] = pred_pred * inv;
+  f[3] = stable * inv;
+  f[4] = cnt_cur[c] * invL;
+  f[5] = cnt_cur[q] * invL;
+  f[6] = progress;
+  f[7] = static_cast<float>(nv) / static_cast<float>(P.w);
+}
+
+// Census of s.cur into s.aux (per code).
+__device__ void census_cur(const EvolveParams& P, const Smem& s, int C0) {
+  for (int c = threadIdx.x; c < C0; c += kThreads) s.aux[c] = 0;
+  __syncthreads();
+  for (int r = threadIdx.x; r < P.L; r += kThreads) atomicAdd(&s.aux[s.cur[r]], 1);
+  __syncthreads();
+}
+
+// Relabels to their prediction the `take` candidates (label != prediction,
+// not fixed) with the highest scores, ties to the smaller row: keys are the
+// score's top 16 bits over (65535 - row), all distinct, and the threshold is
+// the take-th largest key, found bit by bit.
+__device__ void learned_flip(const EvolveParams& P, const Smem& s, int prob, int cycle, int take, int C0) {
+  Fixed& f = *s.f;
+  if (take <= 0) return;
+  census_cur(P, s, C0);
+  unsigned* key = reinterpret_cast<unsigned*>(s.scratch32);
+  const float progress = static_cast<float>(cycle) / static_cast<float>(P.T > 0 ? P.T : 1);
+  for (int r = threadIdx.x; r < P.L; r += kThreads) {
+    unsigned k = 0u;
+    if (s.cur[r] != s.curpred[r] && (P.fixed == nullptr || P.fixed[r] != 1)) {
+      float x[kMlpIn];
+      proposal_features(P, s, prob, r, s.aux, progress, x);
+      const float z = mlp_logit(P.mlp, x);
+      // order-preserving map of the float to an unsigned, top 16 bits kept
+      const unsigned u = __float_as_uint(z);
+      const unsigned ord = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+      k = (ord & 0xffff0000u) | (0xffffu - static_cast<unsigned>(r));
+      if (k == 0u) k = 1u;
+    }
+    key[r] = k;
+  }
+  __syncthreads();
+  unsigned thr = 0u;
+  for (int bit = 31; bit >= 0; --bit) {
+    const unsigned cand = thr | (1u << bit);
+    int cntge = 0;
+    for (int r = threadIdx.x; r < P.L; r += kThreads) cntge += key[r] >= cand;
+    cntge = block_sum(cntge, f);
+    if (cntge >= take) thr = cand;
+  }
+  for (int r = threadIdx.x; r < P.L; r += kThreads)
+    if (key[r] != 0u && key[r] >= thr) s.cl[r] = s.curpred[r];
+  __syncthreads();
+}
+
+// Training snapshot of the current state: features of every row and its
+// label / prediction codes.
+__device__ void snapshot_state(const EvolveParams& P, const Smem& s, int prob, int cycle, int C0) {
+  census_cur(P, s, C0);
+  const float progress = static_cast<float>(cycle) / static_cast<float>(P.T > 0 ? P.T : 1);
+  for (int r = threadIdx.x; r < P.L; r += kThreads) {
+    const size_t o = static_cast<size_t>(prob) * P.L + r;
+    float x[kMlpIn];
+    proposal_features(P, s, prob, r, s.aux, progress, x);
+    for (int i = 0; i < kMlpIn; ++i) P.snap_feat[o * kMlpIn + i] = x[i];
+    P.snap_cur[o] = s.cur[r];
+    P.snap_pred[o] = s.curpred[r];
+  }
+  __syncthreads();
+}
+
 __device__ void evolve_problem(const EvolveParams& P, const Smem& s, int prob) {
   Fixed& f = *s.f;
   const int L = P.L, T = P.T, G = P.G;
@@ -858,6 +958,7 @@ __device__ void evolve_problem(const EvolveParams& P, const Smem& s, int prob) {
       absorb_moves = 0, tr_att = 0, tr_acc = 0, success = 0;
 
   for (int cycle = 0; cycle < T; ++cycle) {
+    if (P.snap_feat != nullptr && cycle == P.snap_cycle) snapshot_state(P, s, prob, cycle, C0);
     // proposal = current (evolutionary) or best (greedy) state; s.cur holds it
     for (int r = threadIdx.x; r < L; r += kThreads) s.cl[r] = s.cur[r];
     __syncthreads();
@@ -887,7 +988,19 @@ __device__ void evolve_problem(const EvolveParams& P, const Smem& s, int prob) {
     if (threadIdx.x == 0) psize[cycle] = ns;
     if (ns > 0) {
       bucket_steps_block(s, G);
-      if (P.singleton && P.pol_guidance) {
+      if (P.singleton && P.pol_guidance && P.mlp != nullptr) {
+        // learned proposal: as many relabellings as the plain draw would make,
+        // given to the candidates the network scores highest
+        int take = 0;
+        for (int g = threadIdx.x; g < G; g += kThreads) {
+          const int row = P.gmem[g];
+          if (s.curpred[row] == s.cur[row]) continue;
+          if (P.fixed != nullptr && P.fixed[row] == 1) continue;
+          take += final_position_of(s, g) < ns;
+        }
+        take = block_sum(take, f);
+        learned_flip(P, s, prob, cycle, take, C0);
+      } else if (P.singleton && P.pol_guidance) {
         // Each sampled group takes its own CV prediction; only groups whose
         // prediction differs from their label can change, so walk just those
         // forward to their final shuffled position.

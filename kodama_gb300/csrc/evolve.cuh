@@ -57,6 +57,13 @@ struct EvolveParams {
   int* foldcnt;            // problems x F x C0max
   uint16_t* rows_scratch;  // grid x 8 x L (when the per-row arrays do not fit in shared memory)
   uint64_t* raw_scratch;   // grid x (L/2 + 64) engine outputs of one shuffle
+  // learned proposal (kNN singleton path): bfloat16-rounded network parameters, or nullptr
+  const float* mlp;
+  // training snapshot of the state at the start of cycle snap_cycle (snap_feat nullptr = none)
+  int snap_cycle;
+  float* snap_feat;        // problems x L x 8
+  uint16_t* snap_cur;      // problems x L
+  uint16_t* snap_pred;     // problems x L
 };
 
 // Per-problem state of the PLS-LDA evolution kept between cycle launches.
