@@ -75,7 +75,8 @@ typedef struct kgb_matrix_options {
    * kgb_proposal_train.  No counterpart in the reference. */
   const float* proposal_weights;
   int32_t snapshot_cycle;    /* cycle whose starting state kgb_matrix_result.snapshot_* record */
-  int32_t reserved2;
+  int32_t proposal_greedy;   /* 0 = sample the relabelled candidates from the network's softmax
+                                (Gumbel top-k, default); 1 = take the top-scored ones */
 } kgb_matrix_options;
 
 /* Caller-allocated outputs of a KODAMA.matrix call. NULL = not wanted

@@ -120,12 +120,15 @@ def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitt
                   graph_neighbors=100, folds=5, knn_k=30, seed=1234, materialize_graph=False,
                   apply_dissimilarity=True, index_base=-1, device=0, host_threads=0,
                   policy="full", res_out=None, first_run=1, classifier="knn",
-                  components=50, proposal_weights=None, snapshot_cycle=None) -> MatrixResult:
+                  components=50, proposal_weights=None, snapshot_cycle=None,
+                  proposal_greedy=False) -> MatrixResult:
     """KODAMA.matrix on the GPU with the kNN (``classifier="knn"``) or PLS-LDA
     (``classifier="pls"``, ``components`` latent components) classifier.
     ``proposal_weights`` (the 4801 parameters of ``train_proposal``) selects
-    the learned relabelling proposal; ``snapshot_cycle`` records its training
-    data (``snapshot_features`` / ``snapshot_flags``) at that cycle.
+    the learned relabelling proposal, which samples the relabelled candidates
+    from the network's softmax (``proposal_greedy=True``: takes the
+    top-scored ones); ``snapshot_cycle`` records its training data
+    (``snapshot_features`` / ``snapshot_flags``) at that cycle.
 
     ``graph`` = (indices, distances) of shape (n, K) runs the graph-input path
     (KODAMAMatrixFromGraphData_CUDA); without it the exact kNN graph is built
@@ -183,6 +186,7 @@ def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitt
         if wts.shape != (N.PROPOSAL_PARAMS,):
             raise ValueError(f"proposal_weights must hold {N.PROPOSAL_PARAMS} floats")
         opt.proposal_weights = wts.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        opt.proposal_greedy = 1 if proposal_greedy else 0
     snap_f = snap_g = None
     if snapshot_cycle is not None:
         if not 0 <= snapshot_cycle < cycles:

@@ -937,8 +937,11 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   if (o->proposal_weights != nullptr) {
     float* master = ctx.upload(o->proposal_weights, kgb::kMlpParams);
     float* rounded = ctx.alloc<float>(kgb::kMlpParams);
+    uint32_t* frag = ctx.alloc<uint32_t>(kgb::kMlpFragWords);
     ck_launch(kgb::mlp_round_params(master, rounded, st), "proposal weights");
-    P.mlp = rounded;
+    ck_launch(kgb::mlp_pack_params(rounded, frag, st), "proposal weights");
+    P.mlp = frag;
+    P.mlp_greedy = o->proposal_greedy != 0;
   }
   const bool snap = out->snapshot_features != nullptr && out->snapshot_flags != nullptr;
   if (snap) {
@@ -1718,9 +1721,11 @@ int kgb_proposal_predict(const float* weights, const float* features, int32_t n,
     cudaStream_t st = ctx.stream();
     float* master = ctx.upload(weights, kgb::kMlpParams);
     float* rounded = ctx.alloc<float>(kgb::kMlpParams);
+    uint32_t* frag = ctx.alloc<uint32_t>(kgb::kMlpFragWords);
     ck_launch(kgb::mlp_round_params(master, rounded, st), "round");
+    ck_launch(kgb::mlp_pack_params(rounded, frag, st), "pack");
     float* d_out = ctx.alloc<float>(n);
-    ck_launch(kgb::mlp_predict(rounded, ctx.upload(features, static_cast<size_t>(n) * kgb::kMlpIn), n, d_out, st),
+    ck_launch(kgb::mlp_predict(frag, ctx.upload(features, static_cast<size_t>(n) * kgb::kMlpIn), n, d_out, st),
               "predict");
     ctx.download(logits, d_out, n);
     ctx.sync();

@@ -55,6 +55,11 @@ struct Fixed {
   double score;
   int accept;
   int improves;
+  // learned proposal: candidate count and radix-select state
+  int sel_count;
+  int sel_digit;
+  int sel_need;
+  int sel_hist[256];
 };
 
 struct Smem {
@@ -861,41 +866,120 @@ __device__ void census_cur(const EvolveParams& P, const Smem& s, int C0) {
   __syncthreads();
 }
 
-// Relabels to their prediction the `take` candidates (label != prediction,
-// not fixed) with the highest scores, ties to the smaller row: keys are the
-// score's top 16 bits over (65535 - row), all distinct, and the threshold is
-// the take-th largest key, found bit by bit.
+// Gumbel(0, 1) noise of (run seed, cycle, row): a splitmix64 hash of the
+// three (Steele, Lea and Flood, "Fast splittable pseudorandom number
+// generators", 2014) mapped to u in (0, 1), then -log(-log u).
+__device__ __forceinline__ float gumbel_noise(uint64_t seed, int cycle, int row) {
+  uint64_t z = seed + 0x9e3779b97f4a7c15ull * (static_cast<uint64_t>(cycle) * 65536ull + static_cast<uint64_t>(row) + 1ull);
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  z ^= z >> 31;
+  const float u = (static_cast<float>(z >> 40) + 0.5f) * (1.0f / 16777216.0f);
+  return -__logf(-__logf(u));
+}
+
+// Relabels to their prediction `take` of the candidates (label != prediction,
+// not fixed).  The candidates are compacted into keys whose low 16 bits are
+// 65535 - row; each warp scores 32 of them on the tensor pipe
+// (mlp_logit_warp) and puts the top 16 bits of the order-preserving image of
+// the score (plus Gumbel noise unless P.mlp_greedy: sampling without
+// replacement from the network's softmax over the candidates) above the row,
+// so all keys are distinct and ties go to the smaller row.  The take-th
+// largest key is found by a 4-pass radix select with 8-bit digits.
 __device__ void learned_flip(const EvolveParams& P, const Smem& s, int prob, int cycle, int take, int C0) {
   Fixed& f = *s.f;
   if (take <= 0) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   census_cur(P, s, C0);
   unsigned* key = reinterpret_cast<unsigned*>(s.scratch32);
-  const float progress = static_cast<float>(cycle) / static_cast<float>(P.T > 0 ? P.T : 1);
-  for (int r = threadIdx.x; r < P.L; r += kThreads) {
-    unsigned k = 0u;
-    if (s.cur[r] != s.curpred[r] && (P.fixed == nullptr || P.fixed[r] != 1)) {
-      float x[kMlpIn];
-      proposal_features(P, s, prob, r, s.aux, progress, x);
-      const float z = mlp_logit(P.mlp, x);
-      // order-preserving map of the float to an unsigned, top 16 bits kept
-      const unsigned u = __float_as_uint(z);
-      const unsigned ord = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-      k = (ord & 0xffff0000u) | (0xffffu - static_cast<unsigned>(r));
-      if (k == 0u) k = 1u;
-    }
-    key[r] = k;
+  if (threadIdx.x == 0) f.sel_count = 0;
+  __syncthreads();
+  for (int base = warp * 32; base < P.L; base += kThreads) {
+    const int r = base + lane;
+    const bool c = r < P.L && s.cur[r] != s.curpred[r] && (P.fixed == nullptr || P.fixed[r] != 1);
+    const unsigned b = __ballot_sync(kFull, c);
+    int at = 0;
+    if (lane == 0 && b != 0u) at = atomicAdd(&f.sel_count, __popc(b));
+    at = __shfl_sync(kFull, at, 0);
+    if (c) key[at + __popc(b & ((1u << lane) - 1u))] = 0xffffu - static_cast<unsigned>(r);
   }
   __syncthreads();
-  unsigned thr = 0u;
-  for (int bit = 31; bit >= 0; --bit) {
-    const unsigned cand = thr | (1u << bit);
-    int cntge = 0;
-    for (int r = threadIdx.x; r < P.L; r += kThreads) cntge += key[r] >= cand;
-    cntge = block_sum(cntge, f);
-    if (cntge >= take) thr = cand;
+  const int count = f.sel_count;
+  if (take >= count) {
+    for (int i = threadIdx.x; i < count; i += kThreads) {
+      const int r = 0xffff - static_cast<int>(key[i] & 0xffffu);
+      s.cl[r] = s.curpred[r];
+    }
+    __syncthreads();
+    return;
   }
-  for (int r = threadIdx.x; r < P.L; r += kThreads)
-    if (key[r] != 0u && key[r] >= thr) s.cl[r] = s.curpred[r];
+  const float progress = static_cast<float>(cycle) / static_cast<float>(P.T > 0 ? P.T : 1);
+  const uint64_t seed = P.seeds[prob];
+  for (int base = warp * 32; base < count; base += kThreads) {
+    const int i = base + lane;
+    uint32_t fw[4] = {0u, 0u, 0u, 0u};
+    int r = -1;
+    if (i < count) {
+      r = 0xffff - static_cast<int>(key[i] & 0xffffu);
+      float x[kMlpIn];
+      proposal_features(P, s, prob, r, s.aux, progress, x);
+      mlp_pack_row(x, fw);
+    }
+    float z = mlp_logit_warp(P.mlp, fw, min(32, count - base));
+    if (i < count) {
+      if (!P.mlp_greedy) z += gumbel_noise(seed, cycle, r);
+      const unsigned u = __float_as_uint(z);
+      const unsigned ord = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+      key[i] = (ord & 0xffff0000u) | (0xffffu - static_cast<unsigned>(r));
+    }
+  }
+  __syncthreads();
+  unsigned prefix = 0u;
+  int need = take;
+  for (int pass = 3; pass >= 0; --pass) {
+    const int shift = 8 * pass;
+    const unsigned hmask = pass == 3 ? 0u : (0xffffffffu << (shift + 8));
+    for (int b = threadIdx.x; b < 256; b += kThreads) f.sel_hist[b] = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < count; i += kThreads) {
+      const unsigned k = key[i];
+      if ((k & hmask) == prefix) atomicAdd(&f.sel_hist[(k >> shift) & 255u], 1);
+    }
+    __syncthreads();
+    if (warp == 0) {
+      // lane l holds digits 8 l .. 8 l + 7; find the largest digit whose
+      // count of keys at or above it reaches `need`
+      int c[8], tot = 0;
+#pragma unroll
+      for (int d = 0; d < 8; ++d) {
+        c[d] = f.sel_hist[8 * lane + d];
+        tot += c[d];
+      }
+      int suf = tot;  // keys in lanes >= this lane
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_down_sync(kFull, suf, o);
+        if (lane + o < 32) suf += v;
+      }
+      const unsigned ball = __ballot_sync(kFull, suf >= need);
+      if (lane == 31 - __clz(ball)) {
+        int above = suf - tot, d = 7;
+        while (d > 0 && above + c[d] < need) above += c[d--];
+        f.sel_digit = 8 * lane + d;
+        f.sel_need = need - above;
+      }
+    }
+    __syncthreads();
+    prefix |= static_cast<unsigned>(f.sel_digit) << shift;
+    need = f.sel_need;
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < count; i += kThreads) {
+    if (key[i] >= prefix) {
+      const int r = 0xffff - static_cast<int>(key[i] & 0xffffu);
+      s.cl[r] = s.curpred[r];
+    }
+  }
   __syncthreads();
 }
 

@@ -57,8 +57,9 @@ struct EvolveParams {
   int* foldcnt;            // problems x F x C0max
   uint16_t* rows_scratch;  // grid x 8 x L (when the per-row arrays do not fit in shared memory)
   uint64_t* raw_scratch;   // grid x (L/2 + 64) engine outputs of one shuffle
-  // learned proposal (kNN singleton path): bfloat16-rounded network parameters, or nullptr
-  const float* mlp;
+  // learned proposal (kNN singleton path): network packed by mlp_pack_params, or nullptr
+  const uint32_t* mlp;
+  int mlp_greedy;          // 1 = relabel the top-scored candidates; 0 = sample them (Gumbel top-k)
   // training snapshot of the state at the start of cycle snap_cycle (snap_feat nullptr = none)
   int snap_cycle;
   float* snap_feat;        // problems x L x 8

@@ -1,7 +1,8 @@
 // Training and batch inference of the learned relabelling proposal (mlp.cuh).
 //
 // Forward: BF16 inputs, weights and activations with FP32 accumulation, the
-// same arithmetic as mlp_logit().  Backward: FP32 gradients of the mean binary
+// arithmetic of the warp-tile tensor-pipe path mlp_logit_warp() (inference)
+// up to the order of the float sums.  Backward: FP32 gradients of the mean binary
 // cross-entropy, one row per thread for the activations, then one thread per
 // parameter summing the block's rows in order; blocks write partial sums that
 // a second kernel adds in block order, so training is deterministic.
@@ -119,9 +120,48 @@ __global__ void adam_kernel(float* master, float* m, float* v, const float* grad
   }
 }
 
-__global__ void predict_kernel(const float* __restrict__ p, const float* __restrict__ feat, int n, float* out) {
-  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
-    out[r] = mlp_logit(p, feat + static_cast<size_t>(r) * kMlpIn);
+__global__ void pack_kernel(const float* __restrict__ p, uint32_t* __restrict__ frag) {
+  for (int e = threadIdx.x; e < kMlpFragWords; e += blockDim.x) {
+    uint32_t v = 0u;
+    if (e < kMlpFragW2) {
+      // layer 1 B fragment: n-tile nt, lane (g, tig): W1[2 tig][8 nt + g], W1[2 tig + 1][8 nt + g]
+      const int nt = e / 32, lane = e % 32, g = lane >> 2, tig = lane & 3;
+      v = bf16_pack(p[kMlpW1 + (2 * tig) * kH + 8 * nt + g], p[kMlpW1 + (2 * tig + 1) * kH + 8 * nt + g]);
+    } else if (e < kMlpFragB1) {
+      // layer 2 B fragments: (k-slice s, n-tile j), lane, word w = rows 16 s + 8 w + 2 tig (+1)
+      const int q = e - kMlpFragW2, w = q & 1, lane = (q >> 1) & 31, sj = q >> 6;
+      const int s = sj / 8, j = sj % 8, g = lane >> 2, tig = lane & 3;
+      const int k = 16 * s + 8 * w + 2 * tig, col = 8 * j + g;
+      v = bf16_pack(p[kMlpW2 + k * kH + col], p[kMlpW2 + (k + 1) * kH + col]);
+    } else if (e < kMlpFragB2) {
+      v = __float_as_uint(p[kMlpB1 + e - kMlpFragB1]);
+    } else if (e < kMlpFragW3) {
+      v = __float_as_uint(p[kMlpB2 + e - kMlpFragB2]);
+    } else if (e < kMlpFragB3) {
+      v = __float_as_uint(bf16_round(p[kMlpW3 + e - kMlpFragW3]));
+    } else if (e == kMlpFragB3) {
+      v = __float_as_uint(p[kMlpB3]);
+    }
+    frag[e] = v;
+  }
+}
+
+// one warp per 32 rows
+__global__ void predict_kernel(const uint32_t* __restrict__ frag, const float* __restrict__ feat, int n,
+                               float* out) {
+  const int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int base = (blockIdx.x * blockDim.x + threadIdx.x) >> 5 << 5; base < n; base += warps * 32) {
+    const int r = base + lane;
+    uint32_t fw[4] = {0u, 0u, 0u, 0u};
+    if (r < n) {
+      float x[kMlpIn];
+      for (int i = 0; i < kMlpIn; ++i) x[i] = feat[static_cast<size_t>(r) * kMlpIn + i];
+      mlp_pack_row(x, fw);
+    }
+    const float z = mlp_logit_warp(frag, fw, min(32, n - base));
+    if (r < n) out[r] = z;
+  }
 }
 
 }  // namespace
@@ -149,9 +189,15 @@ int mlp_adam(float* master, float* m, float* v, const float* grad, float lr, int
   return static_cast<int>(cudaGetLastError());
 }
 
-int mlp_predict(const float* rounded, const float* feat, int n, float* out, cudaStream_t st) {
-  const int blocks = (n + 255) / 256 < 1024 ? (n + 255) / 256 + 1 : 1024;
-  predict_kernel<<<blocks, 256, 0, st>>>(rounded, feat, n, out);
+int mlp_pack_params(const float* rounded, uint32_t* frag, cudaStream_t st) {
+  pack_kernel<<<1, 512, 0, st>>>(rounded, frag);
+  count_launch();
+  return static_cast<int>(cudaGetLastError());
+}
+
+int mlp_predict(const uint32_t* frag, const float* feat, int n, float* out, cudaStream_t st) {
+  const int blocks = (n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024;
+  predict_kernel<<<blocks, 256, 0, st>>>(frag, feat, n, out);
   count_launch();
   return static_cast<int>(cudaGetLastError());
 }
