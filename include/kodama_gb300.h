@@ -36,6 +36,11 @@ extern "C" {
 #define KGB_ETIMEOUT 4  /* a bounded device-side wait gave up */
 #define KGB_EINTERNAL 5 /* internal consistency check failed (std::runtime_error) */
 
+/* DistanceMetric (kodama.hpp:27-31). */
+#define KGB_METRIC_COSINE 0
+#define KGB_METRIC_INNER_PRODUCT 1
+#define KGB_METRIC_EUCLIDEAN 2
+
 /* Evolution-policy switches (kodama.hpp:49-61 EvolutionPolicy). 1 = on. */
 typedef struct kgb_policy {
   int32_t prediction_guidance;
@@ -173,6 +178,40 @@ typedef struct kgb_core_result {
 int kgb_core_knn_graph(const int32_t* gidx, const float* gdist, int32_t samples, int32_t gk,
                        int32_t index_base, const int32_t* labels, const int32_t* constrain,
                        const int32_t* fixed, const kgb_core_options* opt, kgb_core_result* out);
+
+/* ---- Raw-data fold-wise kNN (KNNCV, CoreKNN) ------------------------------
+ * The exact search of the CUDA backend (KNNIndexType::CudaExact): for each
+ * row the k nearest rows of the other folds by the internal distance
+ * (squared L2 for KGB_METRIC_EUCLIDEAN; minus the inner product for
+ * KGB_METRIC_INNER_PRODUCT and for KGB_METRIC_COSINE on rows scaled to unit
+ * norm), float32 chains in coordinate order, ties to the smaller row; vote
+ * score = -distance (native_knn.cpp:1153).  At most 65535 rows. */
+
+/* KNNOptions (kodama.hpp:151-166) as KNNCV uses them. */
+typedef struct kgb_knn_options {
+  int32_t folds;             /* cv.folds (default 10) */
+  int32_t stratified;        /* cv.stratified (default 1) */
+  int32_t k;                 /* default 10 */
+  int32_t metric;            /* KGB_METRIC_* (default cosine) */
+  int32_t device;
+  int32_t reserved;
+  uint64_t cv_seed;          /* cv.seed (default 1) */
+} kgb_knn_options;
+
+/* Replaces KNNCV_CUDA (kodama.hpp:871, knncv.cpp:421-488): cross-validated
+ * kNN predictions of `labels` from x (n x d); majority vote by count, then
+ * score sum, then the smaller label (knncv.cpp:111-131).  constrain may be
+ * NULL.  predicted and fold_assignments have n entries. */
+int kgb_knncv(const float* x, int32_t n, int32_t d, const int32_t* labels, const int32_t* constrain,
+              const kgb_knn_options* opt, int32_t* predicted, int32_t* fold_assignments);
+
+/* Replaces CoreKNN_CUDA (kodama.hpp:1036, core.cpp:1782-1808): label
+ * evolution over the fold-wise neighbour tables of x (precompute_knn_cv_cuda,
+ * core.cpp:695-782); metric is KGB_METRIC_*.  opt->k <= 32.  constrain /
+ * fixed may be NULL. */
+int kgb_core_knn(const float* x, int32_t n, int32_t d, int32_t metric, const int32_t* labels,
+                 const int32_t* constrain, const int32_t* fixed, const kgb_core_options* opt,
+                 kgb_core_result* out);
 
 /* Batched CoreKNNGraph: `problems` independent evolutions over ONE graph
  * (labels is problems x samples; seeds[p] / cv_seeds[p] per problem; out is

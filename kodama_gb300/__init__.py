@@ -335,6 +335,111 @@ def CoreKNNGraph(graph_idx, graph_dist, labels, *, constrain=None, fixed=None, c
     return _wrap_core(r, bufs, cycles)
 
 
+@dataclass
+class FoldResult:
+    """FoldResult (kodama.hpp:222-227)."""
+    fold: int
+    n_train: int
+    n_validation: int
+    accuracy: float
+
+
+@dataclass
+class ConfusionMatrix:
+    """ConfusionMatrix (kodama.hpp:229-237): counts[truth, predicted] over the
+    sorted distinct true labels; predictions outside them are not counted."""
+    labels: np.ndarray
+    counts: np.ndarray
+
+
+@dataclass
+class KNNCVResult:
+    """The KNNCVResult fields of the path (kodama.hpp:256-266)."""
+    predicted_labels: np.ndarray
+    true_labels: np.ndarray
+    fold_assignments: np.ndarray
+    folds: list
+    global_accuracy: float
+    confusion: ConfusionMatrix
+
+
+def _metric(metric) -> int:
+    if isinstance(metric, str):
+        if metric not in N.METRICS:
+            raise ValueError(f"unknown metric {metric!r}")
+        return N.METRICS[metric]
+    return int(metric)
+
+
+def _cv_summary(truth, pred, folds):
+    """Fold results, global accuracy and confusion (knncv.cpp:462-485,
+    common.cpp:226-255)."""
+    out = []
+    for f in np.unique(folds):
+        val = folds == f
+        out.append(FoldResult(int(f), int((~val).sum()), int(val.sum()), float(np.mean(truth[val] == pred[val]))))
+    labels = np.unique(truth)
+    pos = {int(v): i for i, v in enumerate(labels)}
+    counts = np.zeros((len(labels), len(labels)), np.int64)
+    for t, p in zip(truth.tolist(), pred.tolist()):
+        if p in pos:
+            counts[pos[t], pos[p]] += 1
+    return out, float(np.mean(truth == pred)), ConfusionMatrix(labels, counts)
+
+
+def KNNCV(x, labels, *, constrain=None, folds=10, stratified=True, seed=1, k=10, metric="cosine",
+          device=0) -> KNNCVResult:
+    """KNNCV with backend "cuda" (R/kodama.R:160, knncv.cpp:421-488): fold-wise
+    exact kNN votes; ``seed`` is cv.seed."""
+    xa = np.ascontiguousarray(x, dtype=np.float32)
+    if xa.ndim != 2:
+        raise ValueError("x must be a 2-D matrix")
+    n, d = xa.shape
+    lab = np.ascontiguousarray(labels, dtype=np.int32)
+    if lab.shape[0] != n:
+        raise ValueError("labels size must match number of rows.")
+    con = None if constrain is None else np.ascontiguousarray(constrain, dtype=np.int32)
+    if con is not None and con.shape[0] != n:
+        raise ValueError("constrain size must be zero or match number of rows.")
+    pred = np.zeros(n, np.int32)
+    fo = np.zeros(n, np.int32)
+    opt = N.KnnOptions(folds=folds, stratified=int(stratified), k=k, metric=_metric(metric), device=device,
+                       reserved=0, cv_seed=seed)
+    N.check(N.load().kgb_knncv(_ptr(xa), n, d, _ptr(lab), _ptr(con), ctypes.byref(opt), _ptr(pred), _ptr(fo)))
+    fr, acc, cm = _cv_summary(lab, pred, fo)
+    return KNNCVResult(pred, lab, fo, fr, acc, cm)
+
+
+def CoreKNN(x, labels, *, constrain=None, fixed=None, cycles=100, folds=10, stratified=True, seed=1, k=30,
+            metric="euclidean", evolutionary_search=False, guarded_diversity=False,
+            many_to_one_absorption=False, adaptive_proposal_size=True, cv_seed=None, device=0,
+            policy="full") -> CoreResult:
+    """CoreKNN with backend "cuda" (R/kodama.R:266, core.cpp:1782-1808): label
+    evolution over the fold-wise exact kNN tables of x.  ``seed`` seeds both
+    the evolution and the folds unless ``cv_seed`` is given (core_impl_cpp,
+    kodama_r.cpp:1140-1145)."""
+    xa = np.ascontiguousarray(x, dtype=np.float32)
+    if xa.ndim != 2:
+        raise ValueError("x must be a 2-D matrix")
+    n, d = xa.shape
+    lab = np.ascontiguousarray(labels, dtype=np.int32)
+    if lab.shape[0] != n:
+        raise ValueError("labels size must match number of rows.")
+    con = None if constrain is None else np.ascontiguousarray(constrain, dtype=np.int32)
+    fix = None if fixed is None else np.ascontiguousarray(fixed, dtype=np.int32)
+    if con is not None and con.shape[0] != n:
+        raise ValueError("constrain size must be zero or match number of rows.")
+    if fix is not None and fix.shape[0] != n:
+        raise ValueError("fixed size must be zero or match number of rows.")
+    opt = _core_options(cycles, k, folds, stratified, evolutionary_search, guarded_diversity,
+                        many_to_one_absorption, adaptive_proposal_size, seed,
+                        seed if cv_seed is None else cv_seed, device, policy)
+    r, bufs = _alloc_core(n, cycles)
+    N.check(N.load().kgb_core_knn(_ptr(xa), n, d, _metric(metric), _ptr(lab), _ptr(con), _ptr(fix),
+                                  ctypes.byref(opt), ctypes.byref(r)))
+    return _wrap_core(r, bufs, cycles)
+
+
 def knn_graph(x, K: int, *, device: int = 0):
     """Exact kNN graph: zero-based (n, K) indices and sqrt distances."""
     x = np.ascontiguousarray(x, dtype=np.float32)

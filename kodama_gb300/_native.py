@@ -23,6 +23,8 @@ EXPORTED = (
     "kgb_launch_count",
     "kgb_core_knn_graph",
     "kgb_core_knn_graph_batch",
+    "kgb_knncv",
+    "kgb_core_knn",
     "kgb_plsldacv",
     "kgb_plslda_predict",
     "kgb_core_plslda",
@@ -99,6 +101,14 @@ class CoreResult(ctypes.Structure):
     ]
 
 
+class KnnOptions(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int32) for n in (
+        "folds", "stratified", "k", "metric", "device", "reserved")] + [("cv_seed", ctypes.c_uint64)]
+
+
+METRICS = {"cosine": 0, "inner_product": 1, "euclidean": 2}
+
+
 class PlsOptions(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int32) for n in (
         "folds", "stratified", "max_components", "fixed_components", "center", "scale", "device",
@@ -132,6 +142,8 @@ def load():
     lib.kgb_core_knn_graph_batch.argtypes = [P, P, i32, i32, i32, i32, P, P, P, ctypes.POINTER(CoreOptions),
                                              ctypes.POINTER(CoreResult)]
     lib.kgb_knn_graph.argtypes = [P, i32, i32, i32, i32, P, P]
+    lib.kgb_knncv.argtypes = [P, i32, i32, P, P, ctypes.POINTER(KnnOptions), P, P]
+    lib.kgb_core_knn.argtypes = [P, i32, i32, i32, P, P, P, ctypes.POINTER(CoreOptions), ctypes.POINTER(CoreResult)]
     lib.kgb_dissimilarity_inplace.argtypes = [P, P, i32, i32, P, i32, i32]
     lib.kgb_proposal_train.argtypes = [P, P, i32, i32, i32, ctypes.c_float, ctypes.c_uint64, P, i32, P, P]
     lib.kgb_proposal_gradient.argtypes = [P, P, P, i32, i32, P, P]

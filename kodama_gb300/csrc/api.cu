@@ -1167,6 +1167,202 @@ void matrix_entry(const float* x, bool x_on_device, int n, int d, const int32_t*
   out->timings[0] = total.lap();
 }
 
+// Label evolution of `problems` problems over the same `samples` rows
+// (maximize_core, core.cpp:1269-1549, with predict_precomputed_knn): folds
+// from each problem's labels (make_folds, common.cpp:108-214), groups from
+// `constrain` (ascending values, members in row order; nullptr = singletons)
+// and `fixed` flags shared by all problems, vote tables of width w filled by
+// tables(folds, d_folds, d_nb, d_sc), all problems in one persistent launch.
+template <class Tables>
+void core_knn_run(Ctx& ctx, int samples, int problems, const int32_t* labels, const uint64_t* seeds,
+                  const uint64_t* cv_seeds, const int32_t* constrain, const int32_t* fixed,
+                  const kgb_core_options* opt, int w, kgb_core_result* out, Tables&& tables) {
+  if (samples > 65535) fail(KGB_EINVAL, "at most 65535 samples per problem are supported");
+  if (problems < 1) fail(KGB_EINVAL, "problems must be positive");
+  if (opt->cycles < 0) fail(KGB_EINVAL, "Core cycles must be non-negative.");
+  if (opt->k < 1) fail(KGB_EINVAL, "KNNOptions::k must be positive.");
+  if (opt->folds < 2) fail(KGB_EINVAL, "Number of folds must be at least 2.");
+  if (opt->folds > 255) fail(KGB_EINVAL, "at most 255 folds are supported");
+  if (w > 32) fail(KGB_EINVAL, "knn.k above 32 is not supported by the vote kernel");
+  const kgb_policy pol = policy_is_zero(opt->policy) ? default_policy() : opt->policy;
+  cudaStream_t st = ctx.stream();
+  std::vector<int> goff, gmem;
+  if (constrain == nullptr) {
+    goff.reserve(static_cast<size_t>(samples) + 1);
+    for (int i = 0; i <= samples; ++i) goff.push_back(i);
+    for (int i = 0; i < samples; ++i) gmem.push_back(i);
+  } else {
+    std::map<int, std::vector<int>> members;
+    for (int i = 0; i < samples; ++i) members[constrain[i]].push_back(i);
+    goff.push_back(0);
+    for (const auto& kv : members) {
+      gmem.insert(gmem.end(), kv.second.begin(), kv.second.end());
+      goff.push_back(static_cast<int>(gmem.size()));
+    }
+  }
+  const std::vector<int> con = constrain ? std::vector<int>(constrain, constrain + samples) : std::vector<int>();
+  const uint64_t bc = kgb::unordered_bucket_count(static_cast<size_t>(samples));
+  std::vector<Coding> codings(static_cast<size_t>(problems));
+  std::vector<std::vector<int>> folds(static_cast<size_t>(problems));
+  parallel_for(problems, host_threads(0), [&](int p) {
+    const int* lab = labels + static_cast<size_t>(p) * samples;
+    codings[p] = code_labels(lab, samples, bc);
+    folds[p] = kgb::make_folds(std::vector<int>(lab, lab + samples), con, opt->folds, opt->stratified != 0,
+                               cv_seeds[p]);
+  });
+  int C0max = opt->folds;
+  for (const auto& c : codings) C0max = std::max<int>(C0max, static_cast<int>(c.code2label.size()));
+  std::vector<uint16_t> codes(static_cast<size_t>(problems) * samples);
+  std::vector<int> c2l(static_cast<size_t>(problems) * C0max, 0), ncodes(static_cast<size_t>(problems));
+  std::vector<uint8_t> nocol(static_cast<size_t>(problems)), fo8(static_cast<size_t>(problems) * samples);
+  for (int p = 0; p < problems; ++p) {
+    std::copy(codings[p].codes.begin(), codings[p].codes.end(), codes.begin() + static_cast<size_t>(p) * samples);
+    std::copy(codings[p].code2label.begin(), codings[p].code2label.end(), c2l.begin() + static_cast<size_t>(p) * C0max);
+    ncodes[p] = static_cast<int>(codings[p].code2label.size());
+    nocol[p] = codings[p].nocollide ? 1 : 0;
+    for (int i = 0; i < samples; ++i) fo8[static_cast<size_t>(p) * samples + i] = static_cast<uint8_t>(folds[p][i]);
+  }
+  uint8_t* d_folds = ctx.upload(fo8.data(), fo8.size());
+  uint16_t* d_nb = ctx.alloc<uint16_t>(static_cast<size_t>(problems) * samples * w);
+  float* d_sc = ctx.alloc<float>(static_cast<size_t>(problems) * samples * w);
+  tables(folds, d_folds, d_nb, d_sc);
+  kgb::EvolveParams P{};
+  P.problems = problems;
+  P.L = samples;
+  P.w = w;
+  P.T = opt->cycles;
+  P.F = opt->folds;
+  P.G = static_cast<int>(goff.size()) - 1;
+  P.singleton = constrain == nullptr;
+  P.evolutionary = opt->evolutionary_search != 0;
+  P.guarded = opt->guarded_diversity != 0;
+  P.absorption = opt->many_to_one_absorption != 0;
+  P.adaptive = opt->adaptive_proposal_size != 0;
+  P.pol_guidance = pol.prediction_guidance != 0;
+  P.pol_adaptive = pol.adaptive_proposal_size != 0;
+  P.pol_transition = pol.transition_proposal != 0;
+  P.pol_stochastic = pol.stochastic_acceptance != 0;
+  P.pol_diversity = pol.diversity_multiplier != 0;
+  P.pol_reject1 = pol.reject_single_class != 0;
+  P.bucket_count = bc;
+  P.nb = d_nb;
+  P.sc = d_sc;
+  P.init = ctx.upload(codes.data(), codes.size());
+  P.code2label = ctx.upload(c2l.data(), c2l.size());
+  P.ncodes = ctx.upload(ncodes.data(), ncodes.size());
+  P.nocollide = ctx.upload(nocol.data(), nocol.size());
+  P.folds = d_folds;
+  P.fixed = fixed != nullptr ? ctx.upload(fixed, static_cast<size_t>(samples)) : nullptr;
+  P.goff = ctx.upload(goff.data(), goff.size());
+  P.gmem = ctx.upload(gmem.data(), gmem.size());
+  P.seeds = ctx.upload(seeds, static_cast<size_t>(problems));
+  const EvolveBuffers eb = run_evolution(ctx, P, C0max);
+  const int T = opt->cycles;
+  std::vector<uint16_t> hb(static_cast<size_t>(problems) * samples), hp(hb.size());
+  std::vector<double> best(static_cast<size_t>(problems) * 2);
+  std::vector<int> counters(static_cast<size_t>(problems) * 16);
+  ctx.download(hb.data(), eb.clbest, hb.size());
+  ctx.download(hp.data(), eb.cvpredbest, hp.size());
+  ctx.download(best.data(), eb.best, best.size());
+  ctx.download(counters.data(), eb.counters, counters.size());
+  std::vector<double> va(static_cast<size_t>(problems) * T), vs(va.size());
+  std::vector<int> ps(va.size()), ac(va.size());
+  std::vector<uint8_t> fl(va.size() * 3);
+  ctx.download(va.data(), eb.vect_acc, va.size());
+  ctx.download(vs.data(), eb.vect_score, vs.size());
+  ctx.download(ps.data(), eb.psize, ps.size());
+  ctx.download(ac.data(), eb.active, ac.size());
+  ctx.download(fl.data(), eb.flags, fl.size());
+  ctx.sync();
+  for (int p = 0; p < problems; ++p) {
+    kgb_core_result& r = out[p];
+    const int* map = c2l.data() + static_cast<size_t>(p) * C0max;
+    for (int i = 0; i < samples; ++i) {
+      const size_t o1 = static_cast<size_t>(p) * samples + i;
+      if (r.clbest) r.clbest[i] = map[hb[o1]];
+      if (r.cvpredbest) r.cvpredbest[i] = map[hp[o1]];
+      if (r.fold_assignments) r.fold_assignments[i] = folds[p][i];
+    }
+    for (int c = 0; c < T; ++c) {
+      const size_t o1 = static_cast<size_t>(p) * T + c;
+      if (r.vect_acc) r.vect_acc[c] = va[o1];
+      if (r.vect_score) r.vect_score[c] = vs[o1];
+      if (r.proposal_size) r.proposal_size[c] = ps[o1];
+      if (r.active_classes) r.active_classes[c] = ac[o1];
+      if (r.flags) {
+        r.flags[3 * c] = fl[3 * o1];
+        r.flags[3 * c + 1] = fl[3 * o1 + 1];
+        r.flags[3 * c + 2] = fl[3 * o1 + 2];
+      }
+    }
+    r.accbest = best[2 * p];
+    r.scorebest = best[2 * p + 1];
+    std::memset(r.counters, 0, sizeof(r.counters));
+    std::memcpy(r.counters, counters.data() + static_cast<size_t>(p) * 16, sizeof(int) * 16);
+  }
+}
+
+// CoreKNNGraph over one graph for `problems` label vectors: the graph's
+// fold-filtered neighbours as vote tables (precompute_knn_cv_graph,
+// core.cpp:624-688).
+void core_graph_problems(const int32_t* gidx, const float* gdist, int samples, int gk, int index_base, int problems,
+                         const int32_t* labels, const uint64_t* seeds, const uint64_t* cv_seeds,
+                         const int32_t* constrain, const int32_t* fixed, const kgb_core_options* opt,
+                         kgb_core_result* out) {
+  Ctx ctx(opt->device);
+  cudaStream_t st = ctx.stream();
+  const size_t total = static_cast<size_t>(samples) * gk;
+  const int* d_in_idx = ctx.upload(gidx, total);
+  const float* d_in_dist = ctx.upload(gdist, total);
+  int* d_mm = ctx.alloc<int>(2);
+  ck_launch(kgb::graph_minmax(d_in_idx, total, d_mm, st), "graph min/max");
+  int* d_gidx = ctx.alloc<int>(total);
+  float* d_gdist = ctx.alloc<float>(total);
+  ck_launch(kgb::normalize_indices(d_in_idx, d_in_dist, total, samples, index_base, d_mm, d_gidx, d_gdist, st),
+            "graph normalisation");
+  const int w = std::max(1, std::min(opt->k, gk));
+  core_knn_run(ctx, samples, problems, labels, seeds, cv_seeds, constrain, fixed, opt, w, out,
+               [&](const std::vector<std::vector<int>>&, uint8_t* d_folds, uint16_t* d_nb, float* d_sc) {
+                 kgb::VoteTableArgs a{};
+                 a.problems = problems;
+                 a.L = samples;
+                 a.n = samples;
+                 a.K = gk;
+                 a.w = w;
+                 a.gidx = d_gidx;
+                 a.gdist = d_gdist;
+                 a.land = nullptr;
+                 a.g2l = nullptr;
+                 a.folds = d_folds;
+                 a.nb = d_nb;
+                 a.sc = d_sc;
+                 ck_launch(kgb::build_vote_tables(a, st), "vote tables");
+               });
+}
+
+// Every fold keeps training rows (knncv.cpp:142, core.cpp:705; a
+// std::runtime_error there).
+void check_training_rows(const std::vector<int>& folds) {
+  std::map<int, int> size;
+  for (int f : folds) size[f]++;
+  for (const auto& kv : size)
+    if (kv.second == static_cast<int>(folds.size())) fail(KGB_EINTERNAL, "KNN fold has no training samples.");
+}
+
+// The search matrix of a metric on the device: cosine rows normalised
+// (mode 0 = knncv.cpp:85-108, 1 = core.cpp:166-195), else x itself.
+const float* search_matrix(Ctx& ctx, const float* d_x, int n, int d, int metric, int mode) {
+  if (metric != KGB_METRIC_COSINE) return d_x;
+  float* xs = ctx.alloc<float>(static_cast<size_t>(n) * d);
+  ck_launch(kgb::normalize_rows(d_x, n, d, mode, xs, ctx.stream()), "search matrix");
+  return xs;
+}
+
+void check_metric(int metric) {
+  if (metric != KGB_METRIC_COSINE && metric != KGB_METRIC_INNER_PRODUCT && metric != KGB_METRIC_EUCLIDEAN)
+    fail(KGB_EINVAL, "unknown distance metric");
+}
+
 }  // namespace
 
 namespace kgb {
@@ -1218,146 +1414,9 @@ int kgb_core_knn_graph_batch(const int32_t* gidx, const float* gdist, int32_t sa
       fail(KGB_EINVAL, "null pointer");
     }
     if (samples < 2) fail(KGB_EINVAL, "CoreKNNGraph requires at least two samples.");
-    if (samples > 65535) fail(KGB_EINVAL, "at most 65535 samples per problem are supported");
     if (gk <= 0) fail(KGB_EINVAL, "NeighborGraph.neighbors must be positive.");
-    if (problems < 1) fail(KGB_EINVAL, "problems must be positive");
-    if (opt->cycles < 0) fail(KGB_EINVAL, "Core cycles must be non-negative.");
-    if (opt->k < 1) fail(KGB_EINVAL, "KNNOptions::k must be positive.");
-    if (opt->folds < 2) fail(KGB_EINVAL, "Number of folds must be at least 2.");
-    if (opt->folds > 255) fail(KGB_EINVAL, "at most 255 folds are supported");
-    const int w = std::max(1, std::min(opt->k, gk));
-    if (w > 32) fail(KGB_EINVAL, "knn.k above 32 is not supported by the vote kernel");
-    const kgb_policy pol = policy_is_zero(opt->policy) ? default_policy() : opt->policy;
-    Ctx ctx(opt->device);
-    cudaStream_t st = ctx.stream();
-    const size_t total = static_cast<size_t>(samples) * gk;
-    const int* d_in_idx = ctx.upload(gidx, total);
-    const float* d_in_dist = ctx.upload(gdist, total);
-    int* d_mm = ctx.alloc<int>(2);
-    ck_launch(kgb::graph_minmax(d_in_idx, total, d_mm, st), "graph min/max");
-    int* d_gidx = ctx.alloc<int>(total);
-    float* d_gdist = ctx.alloc<float>(total);
-    ck_launch(kgb::normalize_indices(d_in_idx, d_in_dist, total, samples, index_base, d_mm, d_gidx, d_gdist, st),
-              "graph normalisation");
-    // singleton groups (no constraint)
-    std::vector<int> goff, gmem;
-    goff.reserve(static_cast<size_t>(samples) + 1);
-    for (int i = 0; i <= samples; ++i) goff.push_back(i);
-    for (int i = 0; i < samples; ++i) gmem.push_back(i);
-    const uint64_t bc = kgb::unordered_bucket_count(static_cast<size_t>(samples));
-    std::vector<Coding> codings(static_cast<size_t>(problems));
-    std::vector<std::vector<int>> folds(static_cast<size_t>(problems));
-    parallel_for(problems, host_threads(0), [&](int p) {
-      const int* lab = labels + static_cast<size_t>(p) * samples;
-      codings[p] = code_labels(lab, samples, bc);
-      folds[p] = kgb::make_folds(std::vector<int>(lab, lab + samples), {}, opt->folds, opt->stratified != 0,
-                                 cv_seeds[p]);
-    });
-    int C0max = opt->folds;
-    for (const auto& c : codings) C0max = std::max<int>(C0max, static_cast<int>(c.code2label.size()));
-    std::vector<uint16_t> codes(static_cast<size_t>(problems) * samples);
-    std::vector<int> c2l(static_cast<size_t>(problems) * C0max, 0), ncodes(static_cast<size_t>(problems));
-    std::vector<uint8_t> nocol(static_cast<size_t>(problems)), fo8(static_cast<size_t>(problems) * samples);
-    for (int p = 0; p < problems; ++p) {
-      std::copy(codings[p].codes.begin(), codings[p].codes.end(), codes.begin() + static_cast<size_t>(p) * samples);
-      std::copy(codings[p].code2label.begin(), codings[p].code2label.end(), c2l.begin() + static_cast<size_t>(p) * C0max);
-      ncodes[p] = static_cast<int>(codings[p].code2label.size());
-      nocol[p] = codings[p].nocollide ? 1 : 0;
-      for (int i = 0; i < samples; ++i) fo8[static_cast<size_t>(p) * samples + i] = static_cast<uint8_t>(folds[p][i]);
-    }
-    uint8_t* d_folds = ctx.upload(fo8.data(), fo8.size());
-    uint16_t* d_nb = ctx.alloc<uint16_t>(static_cast<size_t>(problems) * samples * w);
-    float* d_sc = ctx.alloc<float>(static_cast<size_t>(problems) * samples * w);
-    {
-      kgb::VoteTableArgs a{};
-      a.problems = problems;
-      a.L = samples;
-      a.n = samples;
-      a.K = gk;
-      a.w = w;
-      a.gidx = d_gidx;
-      a.gdist = d_gdist;
-      a.land = nullptr;
-      a.g2l = nullptr;
-      a.folds = d_folds;
-      a.nb = d_nb;
-      a.sc = d_sc;
-      ck_launch(kgb::build_vote_tables(a, st), "vote tables");
-    }
-    kgb::EvolveParams P{};
-    P.problems = problems;
-    P.L = samples;
-    P.w = w;
-    P.T = opt->cycles;
-    P.F = opt->folds;
-    P.G = samples;
-    P.singleton = 1;
-    P.evolutionary = opt->evolutionary_search != 0;
-    P.guarded = opt->guarded_diversity != 0;
-    P.absorption = opt->many_to_one_absorption != 0;
-    P.adaptive = opt->adaptive_proposal_size != 0;
-    P.pol_guidance = pol.prediction_guidance != 0;
-    P.pol_adaptive = pol.adaptive_proposal_size != 0;
-    P.pol_transition = pol.transition_proposal != 0;
-    P.pol_stochastic = pol.stochastic_acceptance != 0;
-    P.pol_diversity = pol.diversity_multiplier != 0;
-    P.pol_reject1 = pol.reject_single_class != 0;
-    P.bucket_count = bc;
-    P.nb = d_nb;
-    P.sc = d_sc;
-    P.init = ctx.upload(codes.data(), codes.size());
-    P.code2label = ctx.upload(c2l.data(), c2l.size());
-    P.ncodes = ctx.upload(ncodes.data(), ncodes.size());
-    P.nocollide = ctx.upload(nocol.data(), nocol.size());
-    P.folds = d_folds;
-    P.fixed = nullptr;
-    P.goff = ctx.upload(goff.data(), goff.size());
-    P.gmem = ctx.upload(gmem.data(), gmem.size());
-    P.seeds = ctx.upload(seeds, static_cast<size_t>(problems));
-    const EvolveBuffers eb = run_evolution(ctx, P, C0max);
-    const int T = opt->cycles;
-    std::vector<uint16_t> hb(static_cast<size_t>(problems) * samples), hp(hb.size());
-    std::vector<double> best(static_cast<size_t>(problems) * 2);
-    std::vector<int> counters(static_cast<size_t>(problems) * 16);
-    ctx.download(hb.data(), eb.clbest, hb.size());
-    ctx.download(hp.data(), eb.cvpredbest, hp.size());
-    ctx.download(best.data(), eb.best, best.size());
-    ctx.download(counters.data(), eb.counters, counters.size());
-    std::vector<double> va(static_cast<size_t>(problems) * T), vs(va.size());
-    std::vector<int> ps(va.size()), ac(va.size());
-    std::vector<uint8_t> fl(va.size() * 3);
-    ctx.download(va.data(), eb.vect_acc, va.size());
-    ctx.download(vs.data(), eb.vect_score, vs.size());
-    ctx.download(ps.data(), eb.psize, ps.size());
-    ctx.download(ac.data(), eb.active, ac.size());
-    ctx.download(fl.data(), eb.flags, fl.size());
-    ctx.sync();
-    for (int p = 0; p < problems; ++p) {
-      kgb_core_result& r = out[p];
-      const int* map = c2l.data() + static_cast<size_t>(p) * C0max;
-      for (int i = 0; i < samples; ++i) {
-        const size_t o1 = static_cast<size_t>(p) * samples + i;
-        if (r.clbest) r.clbest[i] = map[hb[o1]];
-        if (r.cvpredbest) r.cvpredbest[i] = map[hp[o1]];
-        if (r.fold_assignments) r.fold_assignments[i] = folds[p][i];
-      }
-      for (int c = 0; c < T; ++c) {
-        const size_t o1 = static_cast<size_t>(p) * T + c;
-        if (r.vect_acc) r.vect_acc[c] = va[o1];
-        if (r.vect_score) r.vect_score[c] = vs[o1];
-        if (r.proposal_size) r.proposal_size[c] = ps[o1];
-        if (r.active_classes) r.active_classes[c] = ac[o1];
-        if (r.flags) {
-          r.flags[3 * c] = fl[3 * o1];
-          r.flags[3 * c + 1] = fl[3 * o1 + 1];
-          r.flags[3 * c + 2] = fl[3 * o1 + 2];
-        }
-      }
-      r.accbest = best[2 * p];
-      r.scorebest = best[2 * p + 1];
-      std::memset(r.counters, 0, sizeof(r.counters));
-      std::memcpy(r.counters, counters.data() + static_cast<size_t>(p) * 16, sizeof(int) * 16);
-    }
+    core_graph_problems(gidx, gdist, samples, gk, index_base, problems, labels, seeds, cv_seeds, nullptr, nullptr,
+                        opt, out);
   });
 }
 
@@ -1735,16 +1794,86 @@ int kgb_proposal_predict(const float* weights, const float* features, int32_t n,
 int kgb_core_knn_graph(const int32_t* gidx, const float* gdist, int32_t samples, int32_t gk, int32_t index_base,
                        const int32_t* labels, const int32_t* constrain, const int32_t* fixed,
                        const kgb_core_options* opt, kgb_core_result* out) {
-  if (constrain != nullptr || fixed != nullptr) {
-    g_error = "constrain / fixed are not supported yet by the CUDA CoreKNNGraph entry point";
-    return KGB_EINVAL;
-  }
-  if (opt == nullptr) {
-    g_error = "null options";
-    return KGB_EINVAL;
-  }
-  const uint64_t s = opt->seed, cs = opt->cv_seed;
-  return kgb_core_knn_graph_batch(gidx, gdist, samples, gk, index_base, 1, labels, &s, &cs, opt, out);
+  return guarded([&]() {
+    if (gidx == nullptr || gdist == nullptr || labels == nullptr || opt == nullptr || out == nullptr)
+      fail(KGB_EINVAL, "null pointer");
+    if (samples < 2) fail(KGB_EINVAL, "NeighborGraph samples must be at least 2.");
+    if (gk <= 0) fail(KGB_EINVAL, "NeighborGraph.neighbors must be positive.");
+    const uint64_t s = opt->seed, cs = opt->cv_seed;
+    core_graph_problems(gidx, gdist, samples, gk, index_base, 1, labels, &s, &cs, constrain, fixed, opt, out);
+  });
+}
+
+int kgb_knncv(const float* x, int32_t n, int32_t d, const int32_t* labels, const int32_t* constrain,
+              const kgb_knn_options* opt, int32_t* predicted, int32_t* fold_assignments) {
+  return guarded([&]() {
+    if (x == nullptr) fail(KGB_EINVAL, "MatrixView data pointer is null.");
+    if (labels == nullptr || opt == nullptr || predicted == nullptr) fail(KGB_EINVAL, "null pointer");
+    if (n < 1 || d < 1) fail(KGB_EINVAL, "Input matrix must have at least one row and one column.");
+    if (opt->k < 1) fail(KGB_EINVAL, "KNNOptions::k must be positive.");
+    if (opt->folds < 2) fail(KGB_EINVAL, "Number of folds must be at least 2.");
+    if (n > 65535) fail(KGB_EINVAL, "at most 65535 rows are supported");
+    check_metric(opt->metric);
+    const std::vector<int> lab(labels, labels + n);
+    const std::vector<int> con = constrain ? std::vector<int>(constrain, constrain + n) : std::vector<int>();
+    const std::vector<int> folds = kgb::make_folds(lab, con, opt->folds, opt->stratified != 0, opt->cv_seed);
+    check_training_rows(folds);
+    const int K = std::min(opt->k, n - 1);
+    Ctx ctx(opt->device);
+    cudaStream_t st = ctx.stream();
+    const float* d_x = ctx.upload(x, static_cast<size_t>(n) * d);
+    const float* xs = search_matrix(ctx, d_x, n, d, opt->metric, 0);
+    const int* d_folds = ctx.upload(folds.data(), folds.size());
+    int* d_idx = ctx.alloc<int>(static_cast<size_t>(n) * K);
+    float* d_dist = ctx.alloc<float>(static_cast<size_t>(n) * K);
+    const int segments = 4;
+    void* scratch = ctx.alloc<unsigned char>(kgb::knn_bruteforce_scratch(n, K, segments));
+    ck_launch(kgb::knn_fold_search(xs, n, d, K, opt->metric != KGB_METRIC_EUCLIDEAN, d_folds, segments, scratch,
+                                   d_idx, d_dist, st),
+              "fold-wise kNN");
+    int* d_pred = ctx.alloc<int>(static_cast<size_t>(n));
+    ck_launch(kgb::knn_vote(d_idx, d_dist, n, K, ctx.upload(labels, static_cast<size_t>(n)), d_pred, st), "vote");
+    ctx.download(predicted, d_pred, static_cast<size_t>(n));
+    ctx.sync();
+    if (fold_assignments) std::copy(folds.begin(), folds.end(), fold_assignments);
+  });
+}
+
+int kgb_core_knn(const float* x, int32_t n, int32_t d, int32_t metric, const int32_t* labels,
+                 const int32_t* constrain, const int32_t* fixed, const kgb_core_options* opt,
+                 kgb_core_result* out) {
+  return guarded([&]() {
+    if (x == nullptr) fail(KGB_EINVAL, "MatrixView data pointer is null.");
+    if (labels == nullptr || opt == nullptr || out == nullptr) fail(KGB_EINVAL, "null pointer");
+    if (n < 1 || d < 1) fail(KGB_EINVAL, "Input matrix must have at least one row and one column.");
+    if (n < 2) fail(KGB_EINVAL, "CoreKNN requires at least two samples.");
+    check_metric(metric);
+    if (opt->k < 1) fail(KGB_EINVAL, "KNNOptions::k must be positive.");
+    if (opt->folds < 2) fail(KGB_EINVAL, "Number of folds must be at least 2.");
+    {
+      const std::vector<int> con = constrain ? std::vector<int>(constrain, constrain + n) : std::vector<int>();
+      check_training_rows(kgb::make_folds(std::vector<int>(labels, labels + n), con, opt->folds,
+                                          opt->stratified != 0, opt->cv_seed));
+    }
+    const int w = std::min(opt->k, n - 1);
+    const uint64_t s = opt->seed, cs = opt->cv_seed;
+    Ctx ctx(opt->device);
+    cudaStream_t st = ctx.stream();
+    const float* d_x = ctx.upload(x, static_cast<size_t>(n) * d);
+    const float* xs = search_matrix(ctx, d_x, n, d, metric, 1);
+    core_knn_run(ctx, n, 1, labels, &s, &cs, constrain, fixed, opt, w, out,
+                 [&](const std::vector<std::vector<int>>& folds, uint8_t*, uint16_t* d_nb, float* d_sc) {
+                   const int* d_folds = ctx.upload(folds[0].data(), folds[0].size());
+                   int* d_idx = ctx.alloc<int>(static_cast<size_t>(n) * w);
+                   float* d_dist = ctx.alloc<float>(static_cast<size_t>(n) * w);
+                   const int segments = 4;
+                   void* scratch = ctx.alloc<unsigned char>(kgb::knn_bruteforce_scratch(n, w, segments));
+                   ck_launch(kgb::knn_fold_search(xs, n, d, w, metric != KGB_METRIC_EUCLIDEAN, d_folds, segments,
+                                                  scratch, d_idx, d_dist, st),
+                             "fold-wise kNN");
+                   ck_launch(kgb::knn_fold_tables(d_idx, d_dist, n, w, w, d_nb, d_sc, st), "vote tables");
+                 });
+  });
 }
 
 }  // extern "C"

@@ -309,12 +309,14 @@ __device__ int final_position_of(const Smem& s, int e) {
 
 // ---------------------------------------------------------------------------
 // Tie-break of a vote among the labels reaching the top count `maxc`
-// (`tied`: one lane per such label).  The larger (less negative) double score
-// sum wins, then the smaller code.  Scores are -(d*d) <= 0; with
-// |s| = mant * 2^ex, if the non-zero magnitudes of the row span at most 24
-// binades every sequential double partial sum of <= 32 of them is exact, so
-// exact integer sums order the tied labels exactly as the reference's double
-// sums do; otherwise the double sums are formed in neighbour order.
+// (`tied`: one lane per such label).  The larger double score sum wins, then
+// the smaller code.  With |s| = mant * 2^ex, if the non-zero magnitudes of the
+// row span at most 24 binades every sequential double partial sum of <= 32 of
+// them is exact, so when all scores share a sign (-(d*d) <= 0 for squared L2,
+// inner products >= 0 among near neighbours) exact integer sums of the
+// magnitudes order the tied labels exactly as the reference's double sums do
+// (smaller magnitude first for non-positive scores, larger for non-negative);
+// otherwise the double sums are formed in neighbour order.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ int vote_tiebreak(int code, unsigned tied, const float* scrow, int w, int lane) {
   const float my = lane < w ? scrow[lane] : 0.0f;
@@ -326,7 +328,10 @@ __device__ __forceinline__ int vote_tiebreak(int code, unsigned tied, const floa
   const bool bad = code >= 0 && ef == 0xffu;
   const int emin = __reduce_min_sync(kFull, live ? ex : 0x7fffffff);
   const int emax = __reduce_max_sync(kFull, live ? ex : -0x7fffffff);
-  const bool exact_ok = !__any_sync(kFull, bad) && (emin == 0x7fffffff || emax - emin <= 24);
+  const bool any_neg = __any_sync(kFull, live && (bits >> 31) != 0u);
+  const bool any_pos = __any_sync(kFull, live && (bits >> 31) == 0u);
+  const bool exact_ok = !__any_sync(kFull, bad) && !(any_neg && any_pos) &&
+                        (emin == 0x7fffffff || emax - emin <= 24);
   uint32_t p0 = 0, p1 = 0, p2 = 0;
   if (exact_ok && live) {
     const uint64_t contrib = static_cast<uint64_t>(mant) << (ex - emin);
@@ -334,7 +339,7 @@ __device__ __forceinline__ int vote_tiebreak(int code, unsigned tied, const floa
     p1 = static_cast<uint32_t>((contrib >> 21) & 0x1fffffu);
     p2 = static_cast<uint32_t>(contrib >> 42);
   }
-  uint64_t bmag = ~0ull;
+  uint64_t bmag = any_pos ? 0ull : ~0ull;
   double bsum = -INFINITY;
   int bc = 0x7fffffff;
   unsigned rem = tied;
@@ -348,7 +353,7 @@ __device__ __forceinline__ int vote_tiebreak(int code, unsigned tied, const floa
       const uint64_t s1 = __reduce_add_sync(kFull, in ? p1 : 0u);
       const uint64_t s2 = __reduce_add_sync(kFull, in ? p2 : 0u);
       const uint64_t mag = s0 + (s1 << 21) + (s2 << 42);
-      if (mag < bmag || (mag == bmag && v < bc)) {
+      if ((any_pos ? mag > bmag : mag < bmag) || (mag == bmag && v < bc)) {
         bmag = mag;
         bc = v;
       }

@@ -1,7 +1,8 @@
 // Software model of x86 80-bit extended precision (64-bit significand,
-// round-to-nearest-even) for the few non-negative operations the landmark
-// quota allocation performs in `long double`
-// (kodama_matrix.cpp:856-944 quota_sample_landmarks).
+// round-to-nearest-even) for the few non-negative operations the reference
+// performs in `long double`: the landmark quota allocation
+// (kodama_matrix.cpp:856-944 quota_sample_landmarks) and the squared row
+// norms of the cosine search matrix (core.cpp:182-188).
 //
 // The reference is built with g++ on x86-64, where `long double` is the x87
 // 80-bit format; on aarch64 it is IEEE binary128, which would round the
@@ -135,4 +136,47 @@ EXT80_HD int ext80_floor_int(Ext80 v) {
   if (v.e >= 0) return static_cast<int>(v.m << v.e);
   if (v.e <= -64) return 0;
   return static_cast<int>(v.m >> (-v.e));
+}
+
+// The square of a finite float, exactly (at most 48 significant bits).
+EXT80_HD Ext80 ext80_float_square(float v) {
+#if defined(__CUDA_ARCH__)
+  const uint32_t u = __float_as_uint(v) & 0x7fffffffu;
+#else
+  uint32_t u;
+  __builtin_memcpy(&u, &v, sizeof(u));
+  u &= 0x7fffffffu;
+#endif
+  const int be = static_cast<int>(u >> 23);
+  uint64_t m = u & 0x7fffffu;
+  int e = -149;
+  if (be != 0) {
+    m |= 0x800000u;
+    e = be - 150;
+  }
+  return ext80_round(static_cast<unsigned __int128>(m * m), 2 * e, false);
+}
+
+// static_cast<double>(long double): nearest-even rounding of the 64-bit
+// significand to 53 bits (values within the normal double range).
+EXT80_HD double ext80_to_double(Ext80 a) {
+  if (a.m == 0) return 0.0;
+  uint64_t q = a.m >> 11;
+  const uint64_t rem = a.m & 0x7ffu;
+  int e = a.e + 11;
+  if (rem > 0x400u || (rem == 0x400u && (q & 1u))) {
+    ++q;
+    if (q == (1ull << 53)) {
+      q >>= 1;
+      ++e;
+    }
+  }
+  const uint64_t bits = (static_cast<uint64_t>(e + 52 + 1023) << 52) | (q & ((1ull << 52) - 1));
+#if defined(__CUDA_ARCH__)
+  return __longlong_as_double(static_cast<long long>(bits));
+#else
+  double out;
+  __builtin_memcpy(&out, &bits, sizeof(out));
+  return out;
+#endif
 }

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 #include <stddef.h>
+#include <stdint.h>
 
 namespace kgb {
 
@@ -11,5 +12,23 @@ constexpr int kMaxSegments = 16;
 size_t knn_bruteforce_scratch(int n, int K, int segments);
 int knn_bruteforce(const float* x, int n, int d, int K, int segments, void* scratch, int* idx, float* dist,
                    cudaStream_t st);
+
+// Fold-wise search: for each row the K nearest rows of other folds (folds[n]),
+// ranked by (internal distance, row); inner = minus the inner product instead
+// of the squared L2 distance.  idx -1 / dist +inf where fewer rows qualify;
+// dist is the internal distance.  Scratch as knn_bruteforce_scratch.
+int knn_fold_search(const float* x, int n, int d, int K, bool inner, const int* folds, int segments, void* scratch,
+                    int* idx, float* dist, cudaStream_t st);
+
+// Cosine search matrix: mode 0 = knncv.cpp:85-108, mode 1 = core.cpp:166-195.
+int normalize_rows(const float* x, int n, int d, int mode, float* out, cudaStream_t st);
+
+// Majority vote of every row over its K fold-wise neighbours (knncv.cpp:111-131).
+int knn_vote(const int* idx, const float* dist, int n, int K, const int* labels, int* pred, cudaStream_t st);
+
+// Evolution vote tables (n x w, 16-bit ids, score = -distance) from the
+// fold-wise neighbours (n x K, w <= K).
+int knn_fold_tables(const int* idx, const float* dist, int n, int K, int w, uint16_t* nb, float* sc,
+                    cudaStream_t st);
 
 }  // namespace kgb

@@ -280,20 +280,63 @@ def plsldapredict(L, train, labels, test, *, components=5, center=True, scale=Tr
     return pred
 
 
-def knncv(L, x, labels, *, k=10, folds=10, stratified=True, metric=0, cv_seed=1, threads=1):
+def knncv(L, x, labels, *, constrain=None, k=10, folds=10, stratified=True, metric=0, cv_seed=1, threads=1):
+    """KNNCV: predictions and fold assignments (and, from the reference, its
+    runtime in seconds; 0.0 from the restatement)."""
     x = np.ascontiguousarray(x, np.float32)
     n, d = x.shape
     pred = np.zeros(n, np.int32)
     fo = np.zeros(n, np.int32)
+    con = np.ascontiguousarray(constrain if constrain is not None else np.zeros(n), np.int32)
+    lab = np.ascontiguousarray(labels, np.int32)
     sec = ctypes.c_double(0)
-    rc = L.knncv(x.ctypes.data_as(ctypes.c_void_p), n, d,
-                         np.ascontiguousarray(labels, np.int32).ctypes.data_as(ctypes.c_void_p),
-                         k, folds, int(stratified), metric, ctypes.c_ulonglong(cv_seed), threads,
-                         pred.ctypes.data_as(ctypes.c_void_p), fo.ctypes.data_as(ctypes.c_void_p),
-                         ctypes.byref(sec))
+    if L.prefix == "orc_":
+        rc = L.knncv(x.ctypes.data_as(ctypes.c_void_p), n, d, lab.ctypes.data_as(ctypes.c_void_p),
+                     con.ctypes.data_as(ctypes.c_void_p), int(constrain is not None), k, folds,
+                     int(stratified), metric, ctypes.c_ulonglong(cv_seed),
+                     pred.ctypes.data_as(ctypes.c_void_p), fo.ctypes.data_as(ctypes.c_void_p))
+    else:
+        if constrain is not None:
+            raise ValueError("the reference shim takes no constrain")
+        rc = L.knncv(x.ctypes.data_as(ctypes.c_void_p), n, d, lab.ctypes.data_as(ctypes.c_void_p),
+                     k, folds, int(stratified), metric, ctypes.c_ulonglong(cv_seed), threads,
+                     pred.ctypes.data_as(ctypes.c_void_p), fo.ctypes.data_as(ctypes.c_void_p),
+                     ctypes.byref(sec))
     if rc != 0:
         raise RuntimeError(_err(L))
     return pred, fo, sec.value
+
+
+def core_knn(L, x, labels, *, metric=2, constrain=None, fixed=None, cycles=20, k=30, folds=10,
+             stratified=True, evolutionary=False, guarded=False, absorption=False, adaptive=True,
+             seed=1, cv_seed=1) -> CoreResult:
+    """CoreKNN on raw data (metric 0 cosine, 1 inner product, 2 Euclidean)."""
+    x = np.ascontiguousarray(x, np.float32)
+    samples, d = x.shape
+    lab = np.ascontiguousarray(labels, np.int32)
+    con = np.ascontiguousarray(constrain if constrain is not None else np.zeros(samples), np.int32)
+    fix = np.ascontiguousarray(fixed if fixed is not None else np.zeros(samples), np.int32)
+    copts = np.array([cycles, k, folds, int(stratified), int(evolutionary), int(guarded),
+                      int(absorption), int(adaptive)], np.int32)
+    out = dict(clbest=np.zeros(samples, np.int32), cvpredbest=np.zeros(samples, np.int32),
+               folds=np.zeros(samples, np.int32), vect_acc=np.zeros(cycles, np.float64),
+               vect_score=np.zeros(cycles, np.float64), proposal_size=np.zeros(cycles, np.int32),
+               active_classes=np.zeros(cycles, np.int32), flags=np.zeros(cycles * 3, np.uint8),
+               scal=np.zeros(2, np.float64), counters=np.zeros(16, np.int32))
+    rc = L.core_knn(
+        x.ctypes.data_as(ctypes.c_void_p), samples, d, metric, lab.ctypes.data_as(ctypes.c_void_p),
+        con.ctypes.data_as(ctypes.c_void_p), int(constrain is not None),
+        fix.ctypes.data_as(ctypes.c_void_p), int(fixed is not None),
+        copts.ctypes.data_as(ctypes.c_void_p), ctypes.c_ulonglong(seed), ctypes.c_ulonglong(cv_seed),
+        *[out[f].ctypes.data_as(ctypes.c_void_p) for f in
+          ("clbest", "cvpredbest", "folds", "vect_acc", "vect_score", "proposal_size",
+           "active_classes", "flags", "scal", "counters")])
+    if rc != 0:
+        raise RuntimeError(_err(L))
+    return CoreResult(out["clbest"], out["cvpredbest"], out["folds"], out["vect_acc"],
+                      out["vect_score"], out["proposal_size"], out["active_classes"],
+                      out["flags"].reshape(cycles, 3), float(out["scal"][0]),
+                      float(out["scal"][1]), out["counters"])
 
 
 def exact_knn(L, x, K, threads=1):

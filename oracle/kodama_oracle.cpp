@@ -987,6 +987,164 @@ CoreOut core_knn_graph(const int* gidx, const float* gdist, int samples, int gk,
   return r;
 }
 
+// ---------------------------------------------------------------------------
+// Raw-data fold-wise kNN: KNNCV_CUDA (knncv.cpp:421-488) and CoreKNN_CUDA
+// (core.cpp:1782-1808 via precompute_knn_cv_cuda :695-782) with the exact
+// search.  The reference's exact CUDA search (native_cuda_backend.hpp:165) has
+// no source in the checkout and its CPU paths use approximate HNSW, so the
+// exact search is defined here as on the device: the canonical distance below,
+// neighbours ranked by (distance, row).
+// ---------------------------------------------------------------------------
+
+constexpr int kMetricCosine = 0, kMetricInner = 1, kMetricEuclidean = 2;
+
+// Rows as searched (make_search_matrix): cosine rows multiplied in double by
+// 1 / ||row|| (when finite and positive) and rounded to float; other metrics
+// unchanged.  mode 0 sums the squares sequentially in double
+// (knncv.cpp:85-108); mode 1 is core.cpp:166-195's long double sum in the x86
+// 80-bit format (ext80.h: exact float squares, 64-bit significand sums)
+// rounded to double.
+std::vector<float> search_matrix(const float* x, int n, int d, int metric, int mode) {
+  std::vector<float> out(x, x + static_cast<size_t>(n) * d);
+  if (metric != kMetricCosine) return out;
+  for (int r = 0; r < n; ++r) {
+    const float* row = x + static_cast<size_t>(r) * d;
+    double ss;
+    if (mode == 0) {
+      ss = 0.0;
+      for (int j = 0; j < d; ++j) ss += static_cast<double>(row[j]) * static_cast<double>(row[j]);
+    } else {
+      Ext80 acc{0, 0};
+      bool finite = true;
+      for (int j = 0; j < d; ++j) {
+        finite = finite && std::isfinite(row[j]);
+        acc = ext80_add(acc, ext80_float_square(row[j]));
+      }
+      ss = finite ? ext80_to_double(acc) : std::numeric_limits<double>::infinity();
+    }
+    const double nrm = std::sqrt(ss);
+    const double scale = nrm > 0.0 && std::isfinite(nrm) ? 1.0 / nrm : 1.0;
+    for (int j = 0; j < d; ++j)
+      out[static_cast<size_t>(r) * d + j] = static_cast<float>(static_cast<double>(row[j]) * scale);
+  }
+  return out;
+}
+
+// Canonical internal distance: squared L2 as a float chain of separately
+// rounded (a - b)^2 terms in coordinate order; for the inner product and
+// cosine, minus the float chain of the a * b products (the internal
+// representation of native_knn.cpp:40-95, score = -distance, :1153).
+float canon_distance(const float* a, const float* b, int d, bool inner) {
+  float acc = 0.0f;
+  if (inner) {
+    for (int j = 0; j < d; ++j) acc = acc + a[j] * b[j];
+    return -acc;
+  }
+  for (int j = 0; j < d; ++j) {
+    const float diff = a[j] - b[j];
+    acc = acc + diff * diff;
+  }
+  return acc;
+}
+
+// Every fold must keep training rows (knncv.cpp:142, core.cpp:705).
+void check_training_rows(const std::vector<int>& folds) {
+  std::map<int, int> size;
+  for (int f : folds) size[f]++;
+  for (const auto& kv : size)
+    if (kv.second == static_cast<int>(folds.size())) throw std::runtime_error("KNN fold has no training samples.");
+}
+
+// For each row its k nearest rows of the other folds by (distance, row), as a
+// vote table with score = -distance.  Fewer than k candidates leave -1 slots
+// (k = min(k, training rows) per fold).
+VoteTable fold_knn_table(const std::vector<float>& xs, int n, int d, bool inner, const std::vector<int>& folds, int k) {
+  VoteTable t;
+  t.samples = n;
+  t.width = std::max(1, k);
+  t.folds = folds;
+  t.nb.assign(static_cast<size_t>(n) * t.width, -1);
+  t.score.assign(static_cast<size_t>(n) * t.width, -std::numeric_limits<float>::infinity());
+  std::vector<std::pair<float, int>> cand;
+  for (int r = 0; r < n; ++r) {
+    cand.clear();
+    for (int j = 0; j < n; ++j) {
+      if (folds[j] == folds[r]) continue;
+      cand.emplace_back(canon_distance(&xs[static_cast<size_t>(r) * d], &xs[static_cast<size_t>(j) * d], d, inner), j);
+    }
+    const int m = std::min<int>(t.width, static_cast<int>(cand.size()));
+    std::partial_sort(cand.begin(), cand.begin() + m, cand.end(), [](const auto& a, const auto& b) {
+      return a.first < b.first || (a.first == b.first && a.second < b.second);
+    });
+    for (int c = 0; c < m; ++c) {
+      t.nb[static_cast<size_t>(r) * t.width + c] = cand[c].second;
+      t.score[static_cast<size_t>(r) * t.width + c] = -cand[c].first;
+    }
+  }
+  return t;
+}
+
+// majority_vote (knncv.cpp:111-131) of every row over its table row: per label
+// the count and the double sum of the scores in neighbour order; the largest
+// count, then the larger sum, then the smaller label.
+std::vector<int> majority_votes(const VoteTable& t, const std::vector<int>& labels) {
+  std::vector<int> pred(static_cast<size_t>(t.samples), 0);
+  for (int r = 0; r < t.samples; ++r) {
+    std::map<int, std::pair<int, double>> votes;
+    for (int j = 0; j < t.width; ++j) {
+      const int nb = t.nb[static_cast<size_t>(r) * t.width + j];
+      if (nb < 0) continue;
+      auto& v = votes[labels[nb]];
+      v.first += 1;
+      v.second += static_cast<double>(t.score[static_cast<size_t>(r) * t.width + j]);
+    }
+    if (votes.empty()) continue;
+    int bl = votes.begin()->first, bc = votes.begin()->second.first;
+    double bs = votes.begin()->second.second;
+    for (const auto& kv : votes) {
+      if (kv.second.first > bc || (kv.second.first == bc && kv.second.second > bs) ||
+          (kv.second.first == bc && kv.second.second == bs && kv.first < bl)) {
+        bl = kv.first;
+        bc = kv.second.first;
+        bs = kv.second.second;
+      }
+    }
+    pred[r] = bl;
+  }
+  return pred;
+}
+
+// KNNCV with the exact search: predictions and fold assignments.
+std::vector<int> knncv(const float* x, int n, int d, const std::vector<int>& labels, const std::vector<int>& constrain,
+                       int k, int nfolds, bool stratified, int metric, uint64_t cv_seed, std::vector<int>& folds) {
+  if (k < 1) throw std::invalid_argument("KNNOptions::k must be positive.");
+  folds = make_folds(labels, constrain, nfolds, stratified, cv_seed);
+  check_training_rows(folds);
+  const std::vector<float> xs = search_matrix(x, n, d, metric, 0);
+  const VoteTable t = fold_knn_table(xs, n, d, metric != kMetricEuclidean, folds, k);
+  return majority_votes(t, labels);
+}
+
+// CoreKNN with the exact search: maximize_core over the fold-wise tables.
+CoreOut core_knn(const float* x, int n, int d, const std::vector<int>& init, const std::vector<int>& constrain,
+                 const std::vector<int>& fixed_in, const CoreOpts& o, int metric) {
+  if (o.k < 1) throw std::invalid_argument("KNNOptions::k must be positive.");
+  const std::vector<int> folds = make_folds(init, constrain, o.folds, o.stratified, o.cv_seed);
+  check_training_rows(folds);
+  const std::vector<float> xs = search_matrix(x, n, d, metric, 1);
+  const VoteTable table = fold_knn_table(xs, n, d, metric != kMetricEuclidean, folds, o.k);
+  int nfold = 0;
+  for (int f : folds) nfold = std::max(nfold, f + 1);
+  std::vector<int> universe = init;
+  std::sort(universe.begin(), universe.end());
+  universe.erase(std::unique(universe.begin(), universe.end()), universe.end());
+  CoreOut r = core_run(n, init, constrain, fixed_in, o, [&](const std::vector<int>& labels) {
+    return vote_predict(table, labels, universe, nfold);
+  });
+  r.folds = folds;
+  return r;
+}
+
 // CorePLSLDA_CPU (core.cpp:1626-1646): maximize_core with PLSLDACV_CPU as the
 // predictor under a fresh data epoch.  Non-stratified folds use the fold cache
 // of plscv.cpp:593-667: the first evaluation computes loadings through the
@@ -1439,6 +1597,69 @@ int orc_core_knn_graph(
     std::memcpy(clbest, r.clbest.data(), sizeof(int) * samples);
     std::memcpy(cvpredbest, r.cvpredbest.data(), sizeof(int) * samples);
     std::memcpy(folds, r.folds.data(), sizeof(int) * samples);
+    for (int c = 0; c < o.cycles; ++c) {
+      vect_acc[c] = r.vect_acc[c];
+      vect_score[c] = r.vect_score[c];
+      proposal_size[c] = r.proposal_size[c];
+      active_classes[c] = r.active_classes[c];
+      flags3[3 * c + 0] = r.accepted[c];
+      flags3[3 * c + 1] = r.improving[c];
+      flags3[3 * c + 2] = r.temperature[c];
+    }
+    scal_out[0] = r.accbest;
+    scal_out[1] = r.scorebest;
+    std::memcpy(int_out, r.counters, sizeof(int) * 16);
+    return 0;
+  } catch (const std::exception& e) {
+    orc::g_error = e.what();
+    return 1;
+  }
+}
+
+// KNNCV (exact search); predicted and fold_out have n entries.
+int orc_knncv(const float* x, int n, int d, const int* labels, const int* constrain, int has_constrain, int k,
+              int folds, int stratified, int metric, unsigned long long cv_seed, int* predicted, int* fold_out) {
+  try {
+    std::vector<int> lab(labels, labels + n);
+    std::vector<int> con = has_constrain ? std::vector<int>(constrain, constrain + n) : std::vector<int>();
+    std::vector<int> fo;
+    const std::vector<int> pred = orc::knncv(x, n, d, lab, con, k, folds, stratified != 0, metric, cv_seed, fo);
+    std::memcpy(predicted, pred.data(), sizeof(int) * n);
+    std::memcpy(fold_out, fo.data(), sizeof(int) * n);
+    return 0;
+  } catch (const std::exception& e) {
+    orc::g_error = e.what();
+    return 1;
+  }
+}
+
+// CoreKNN (exact search); outputs as orc_core_knn_graph.
+int orc_core_knn(
+  const float* x, int n, int d, int metric,
+  const int* labels, const int* constrain, int has_constrain, const int* fixed, int has_fixed,
+  const int* copts, unsigned long long seed, unsigned long long cv_seed,
+  int* clbest, int* cvpredbest, int* folds, double* vect_acc, double* vect_score,
+  int* proposal_size, int* active_classes, unsigned char* flags3, double* scal_out, int* int_out
+) {
+  try {
+    orc::CoreOpts o;
+    o.cycles = copts[0];
+    o.k = copts[1];
+    o.folds = copts[2];
+    o.stratified = copts[3] != 0;
+    o.evolutionary = copts[4] != 0;
+    o.guarded = copts[5] != 0;
+    o.absorption = copts[6] != 0;
+    o.adaptive = copts[7] != 0;
+    o.seed = seed;
+    o.cv_seed = cv_seed;
+    std::vector<int> lab(labels, labels + n);
+    std::vector<int> con = has_constrain ? std::vector<int>(constrain, constrain + n) : std::vector<int>();
+    std::vector<int> fix = has_fixed ? std::vector<int>(fixed, fixed + n) : std::vector<int>();
+    const auto r = orc::core_knn(x, n, d, lab, con, fix, o, metric);
+    std::memcpy(clbest, r.clbest.data(), sizeof(int) * n);
+    std::memcpy(cvpredbest, r.cvpredbest.data(), sizeof(int) * n);
+    std::memcpy(folds, r.folds.data(), sizeof(int) * n);
     for (int c = 0; c < o.cycles; ++c) {
       vect_acc[c] = r.vect_acc[c];
       vect_score[c] = r.vect_score[c];

@@ -38,3 +38,5 @@ quota_sample = _bind(_b.quota_sample)
 core_plslda = _bind(_b.core_plslda)
 plsldacv = _bind(_b.plsldacv)
 plsldapredict = _bind(_b.plsldapredict)
+knncv = _bind(_b.knncv)
+core_knn = _bind(_b.core_knn)

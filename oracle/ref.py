@@ -29,3 +29,4 @@ plsldacv = _bind(_b.plsldacv)
 plsldapredict = _bind(_b.plsldapredict)
 knncv = _bind(_b.knncv)
 core_plslda = _bind(_b.core_plslda)
+core_knn = _bind(_b.core_knn)

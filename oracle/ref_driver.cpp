@@ -383,4 +383,60 @@ int ref_knncv(
   }
 }
 
+// CoreKNN_CPU (core.cpp:1648-1667): the reference's HNSW fold-wise kNN under
+// maximize_core.  Outputs as ref_core_knn_graph.
+int ref_core_knn(
+  const float* x, int n, int d, int metric,
+  const int* labels, const int* constrain, int has_constrain, const int* fixed, int has_fixed,
+  const int* copts, unsigned long long seed, unsigned long long cv_seed,
+  int* clbest, int* cvpredbest, int* folds, double* vect_acc, double* vect_score,
+  int* proposal_size, int* active_classes, unsigned char* flags3, double* scal_out, int* int_out
+) {
+  try {
+    kodama::MatrixView view(x, static_cast<size_t>(n), static_cast<size_t>(d));
+    kodama::CoreOptions opt;
+    opt.cycles = copts[0];
+    opt.knn.k = copts[1];
+    opt.knn.cv.folds = copts[2];
+    opt.knn.cv.stratified = copts[3] != 0;
+    opt.evolutionary_search = copts[4] != 0;
+    opt.guarded_diversity = copts[5] != 0;
+    opt.many_to_one_absorption = copts[6] != 0;
+    opt.adaptive_proposal_size = copts[7] != 0;
+    opt.knn.metric = metric == 2 ? kodama::DistanceMetric::Euclidean :
+      (metric == 1 ? kodama::DistanceMetric::InnerProduct : kodama::DistanceMetric::Cosine);
+    opt.knn.hnsw_tune_k = std::max(50, opt.knn.k);
+    opt.seed = seed;
+    opt.knn.cv.seed = cv_seed;
+    std::vector<int> lab(labels, labels + n);
+    std::vector<int> con = has_constrain ? std::vector<int>(constrain, constrain + n) : std::vector<int>();
+    std::vector<int> fix = has_fixed ? std::vector<int>(fixed, fixed + n) : std::vector<int>();
+    const auto r = kodama::CoreKNN_CPU(view, lab, con, fix, opt);
+    std::memcpy(clbest, r.clbest.data(), sizeof(int) * n);
+    std::memcpy(cvpredbest, r.cvpredbest.data(), sizeof(int) * n);
+    std::memcpy(folds, r.fold_assignments.data(), sizeof(int) * n);
+    for (int c = 0; c < opt.cycles; ++c) {
+      vect_acc[c] = r.vect_acc[c];
+      vect_score[c] = r.vect_score[c];
+      proposal_size[c] = r.proposal_size[c];
+      active_classes[c] = r.active_classes[c];
+      flags3[3 * c + 0] = r.accepted[c];
+      flags3[3 * c + 1] = r.improving_acceptance[c];
+      flags3[3 * c + 2] = r.temperature_acceptance[c];
+    }
+    scal_out[0] = r.accbest;
+    scal_out[1] = r.scorebest;
+    const int counters[16] = {
+      r.cycles_completed, r.proposals_evaluated, r.best_state_updates, r.current_state_accepts,
+      r.stochastic_state_attempts, r.stochastic_state_accepts, r.current_state_rejections,
+      r.coarsening_moves, r.absorption_moves, r.transition_attempted, r.transition_accepted,
+      r.many_to_one_attempted, r.many_to_one_accepted, r.cv_evaluations, r.success ? 1 : 0, 0};
+    std::memcpy(int_out, counters, sizeof(counters));
+    return 0;
+  } catch (const std::exception& e) {
+    g_error = e.what();
+    return 1;
+  }
+}
+
 }  // extern "C"

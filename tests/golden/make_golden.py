@@ -22,6 +22,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+from golden_util import knn_inputs  # noqa: E402
 from kodama_gb300 import datasets  # noqa: E402
 from oracle import oracle, ref  # noqa: E402
 
@@ -109,6 +112,45 @@ def pls_matrix_case(name, spec, K, **kw):
     return case
 
 
+def knncv_case(name, spec, **kw):
+    x, labels, con, _ = knn_inputs(spec)
+    if con is not None:
+        raise ValueError("the reference shim of KNNCV takes no constraint")
+    pred, folds, _ = ref.knncv(x, labels, threads=8, **kw)
+    return {"kind": "knncv", "name": name, "input": spec, "options": kw, "labels_sha256": sha(labels),
+            "predicted_sha256": sha(pred), "folds_sha256": sha(folds), "predicted_head": pred[:32].tolist()}
+
+
+def core_knn_case(name, spec, **kw):
+    x, labels, con, fix = knn_inputs(spec)
+    r = ref.core_knn(x, labels, constrain=con, fixed=fix, **kw)
+    return {
+        "kind": "core_knn", "name": name, "input": spec, "options": kw, "labels_sha256": sha(labels),
+        "clbest_sha256": sha(r.clbest), "cvpredbest_sha256": sha(r.cvpredbest), "folds_sha256": sha(r.folds),
+        "vect_acc": r.vect_acc.tolist(), "vect_score": r.vect_score.tolist(),
+        "proposal_size": r.proposal_size.tolist(), "active_classes": r.active_classes.tolist(),
+        "flags": r.flags.tolist(), "accbest": r.accbest, "scorebest": r.scorebest,
+        "counters": r.counters.tolist(),
+    }
+
+
+def core_graph_case(name, spec, K, **kw):
+    """CoreKNNGraph on the canonical exact graph of knn_inputs(spec), with its
+    constraint / fixed flags."""
+    x, labels, con, fix = knn_inputs(spec)
+    gi, gd = oracle.exact_knn(x, K, threads=8)
+    r = ref.core_knn_graph(gi, gd, labels, index_base=0, constrain=con, fixed=fix, **kw)
+    return {
+        "kind": "core_knn_graph_input", "name": name, "input": spec, "K": K, "options": kw,
+        "graph_sha256": sha(gi) + ":" + sha(gd), "labels_sha256": sha(labels),
+        "clbest_sha256": sha(r.clbest), "cvpredbest_sha256": sha(r.cvpredbest), "folds_sha256": sha(r.folds),
+        "vect_acc": r.vect_acc.tolist(), "vect_score": r.vect_score.tolist(),
+        "proposal_size": r.proposal_size.tolist(), "active_classes": r.active_classes.tolist(),
+        "flags": r.flags.tolist(), "accbest": r.accbest, "scorebest": r.scorebest,
+        "counters": r.counters.tolist(),
+    }
+
+
 def main():
     if not ref.available():
         raise SystemExit("build oracle/_ref first (oracle/build_ref.sh)")
@@ -140,6 +182,23 @@ def main():
     cases.append(pls_matrix_case("pls_matrix_N1500_d50_M4_T12", dict(n=1500, d=50, seed=35), 20,
                                  seed=99, runs=4, cycles=12, landmarks=10000, splitting=20,
                                  graph_neighbors=20, folds=5, knn_k=10, components=5))
+    cases.append(knncv_case("knncv_cosine_stratified", dict(n=900, d=20, seed=41, flip=0.2),
+                            k=10, folds=10, stratified=True, metric=0, cv_seed=3))
+    cases.append(knncv_case("knncv_euclidean", dict(n=700, d=12, seed=42, flip=0.3),
+                            k=7, folds=5, stratified=False, metric=2, cv_seed=4))
+    cases.append(knncv_case("knncv_inner_product", dict(n=600, d=24, seed=44, flip=0.1),
+                            k=15, folds=8, stratified=True, metric=1, cv_seed=5))
+    cases.append(core_knn_case("core_knn_cosine_evolutionary", dict(n=800, d=16, seed=43, random_labels=6),
+                               metric=0, cycles=20, k=10, folds=5, stratified=True, evolutionary=True,
+                               guarded=True, absorption=True, seed=4, cv_seed=6))
+    cases.append(core_knn_case("core_knn_euclidean_constrained_fixed",
+                               dict(n=800, d=16, seed=45, random_labels=6, groups_of=3, fixed_frac=0.1),
+                               metric=2, cycles=20, k=30, folds=10, stratified=False, evolutionary=False,
+                               guarded=False, absorption=False, seed=7, cv_seed=8))
+    cases.append(core_graph_case("core_graph_constrained_fixed",
+                                 dict(n=900, d=16, seed=46, random_labels=7, groups_of=2, fixed_frac=0.15),
+                                 30, cycles=20, k=10, folds=5, stratified=True, evolutionary=True, guarded=True,
+                                 absorption=True, seed=9, cv_seed=10))
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py", "cases": cases}, f, indent=1)
     print(f"wrote {len(cases)} cases")

@@ -34,6 +34,32 @@ def pls_inputs(spec):
     return x, labels.astype(np.int32)
 
 
+def knn_inputs(spec):
+    """Mixture workload of a KNNCV / CoreKNN case spec: (x, labels, constrain,
+    fixed) -- the cluster labels with a fraction replaced, or random start
+    labels; constrain groups of `groups_of` rows; a `fixed_frac` of fixed rows."""
+    x, y = datasets.gaussian_mixture(n=spec["n"], d=spec["d"], seed=spec["seed"])
+    rng = np.random.default_rng(spec["seed"] + 2000)
+    labels = (y + 1).astype(np.int32)
+    flip = rng.random(len(y)) < spec.get("flip", 0.0)
+    labels[flip] = rng.integers(1, 9, int(flip.sum()))
+    if spec.get("random_labels"):
+        labels = rng.integers(1, spec["random_labels"] + 1, len(y)).astype(np.int32)
+    con = fix = None
+    if spec.get("groups_of"):
+        g = spec["groups_of"]
+        con = (np.arange(len(y)) // g * 7 + 5).astype(np.int32)[rng.permutation(len(y))]
+    if spec.get("fixed_frac"):
+        fix = (rng.random(len(y)) < spec["fixed_frac"]).astype(np.int32)
+    return np.ascontiguousarray(x, np.float32), labels.astype(np.int32), con, fix
+
+
+def check_knncv(case, pred, folds):
+    assert sha(folds) == case["folds_sha256"], "folds"
+    assert np.asarray(pred)[:32].tolist() == case["predicted_head"], "predictions head"
+    assert sha(pred) == case["predicted_sha256"], "predictions"
+
+
 def inputs(case):
     if "input" in case:
         return pls_inputs(case["input"])[0]

@@ -39,6 +39,38 @@ def _cases(kind):
     return [c for c in G.cases() if c["kind"] == kind]
 
 
+def _core_kw(o):
+    return dict(cycles=o["cycles"], k=o["k"], folds=o["folds"], stratified=o["stratified"],
+                evolutionary=o["evolutionary"], guarded=o["guarded"], absorption=o["absorption"],
+                seed=o["seed"], cv_seed=o["cv_seed"])
+
+
+@pytest.mark.parametrize("case", _cases("knncv"), ids=lambda c: c["name"])
+def test_oracle_knncv_golden(orc, case):
+    x, labels, _, _ = G.knn_inputs(case["input"])
+    assert G.sha(labels) == case["labels_sha256"]
+    pred, folds, _ = orc.knncv(x, labels, **case["options"])
+    G.check_knncv(case, pred, folds)
+
+
+@pytest.mark.parametrize("case", _cases("core_knn"), ids=lambda c: c["name"])
+def test_oracle_core_knn_golden(orc, case):
+    x, labels, con, fix = G.knn_inputs(case["input"])
+    assert G.sha(labels) == case["labels_sha256"]
+    o = case["options"]
+    r = orc.core_knn(x, labels, metric=o["metric"], constrain=con, fixed=fix, **_core_kw(o))
+    G.check_core(case, r)
+
+
+@pytest.mark.parametrize("case", _cases("core_knn_graph_input"), ids=lambda c: c["name"])
+def test_oracle_core_graph_input_golden(orc, case):
+    x, labels, con, fix = G.knn_inputs(case["input"])
+    gi, gd = orc.exact_knn(x, case["K"], threads=8)
+    assert G.sha(gi) + ":" + G.sha(gd) == case["graph_sha256"], "canonical exact graph"
+    r = orc.core_knn_graph(gi, gd, labels, index_base=0, constrain=con, fixed=fix, **_core_kw(case["options"]))
+    G.check_core(case, r)
+
+
 @pytest.mark.parametrize("case", _cases("plsldacv"), ids=lambda c: c["name"])
 def test_oracle_plsldacv_golden(orc, case):
     x, labels = G.pls_inputs(case["input"])
@@ -91,3 +123,38 @@ def test_gpu_core_golden(kg, case):
                                 evolutionary_search=o["evolutionary"], guarded_diversity=o["guarded"],
                                 many_to_one_absorption=o["absorption"], index_base=0)
     G.check_core(case, out[0], folds_attr="fold_assignments")
+
+
+def _gpu_core_kw(o):
+    return dict(cycles=o["cycles"], k=o["k"], folds=o["folds"], stratified=o["stratified"],
+                evolutionary_search=o["evolutionary"], guarded_diversity=o["guarded"],
+                many_to_one_absorption=o["absorption"], seed=o["seed"], cv_seed=o["cv_seed"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", _cases("knncv"), ids=lambda c: c["name"])
+def test_gpu_knncv_golden(kg, case):
+    x, labels, _, _ = G.knn_inputs(case["input"])
+    o = case["options"]
+    r = kg.KNNCV(x, labels, k=o["k"], folds=o["folds"], stratified=o["stratified"], metric=o["metric"],
+                 seed=o["cv_seed"])
+    G.check_knncv(case, r.predicted_labels, r.fold_assignments)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", _cases("core_knn"), ids=lambda c: c["name"])
+def test_gpu_core_knn_golden(kg, case):
+    x, labels, con, fix = G.knn_inputs(case["input"])
+    o = case["options"]
+    r = kg.CoreKNN(x, labels, metric=o["metric"], constrain=con, fixed=fix, **_gpu_core_kw(o))
+    G.check_core(case, r, folds_attr="fold_assignments")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", _cases("core_knn_graph_input"), ids=lambda c: c["name"])
+def test_gpu_core_graph_input_golden(kg, case):
+    x, labels, con, fix = G.knn_inputs(case["input"])
+    gi, gd = kg.knn_graph(x, case["K"])
+    assert G.sha(gi) + ":" + G.sha(gd) == case["graph_sha256"], "exact graph"
+    r = kg.CoreKNNGraph(gi, gd, labels, index_base=0, constrain=con, fixed=fix, **_gpu_core_kw(case["options"]))
+    G.check_core(case, r, folds_attr="fold_assignments")

@@ -109,3 +109,40 @@ def test_pls_matrix_vs_reference(orc):
     b = orc.kodama_matrix_graph_data(x, gi, gd, 0, seed=77, **kw)
     for f in ("res", "acc", "v", "hashes", "run_counters", "cycle_diag", "knn_idx", "knn_dist", "pls_counters"):
         assert np.array_equal(getattr(a, f), getattr(b, f)), f
+
+
+def _clustered(n, d, seed):
+    rng = np.random.default_rng(seed)
+    sizes = [n // 3, n // 3, n - 2 * (n // 3)]
+    centres = rng.standard_normal((3, d)) * 1.5
+    x = (rng.standard_normal((n, d)) + np.repeat(centres, sizes, axis=0)).astype(np.float32)
+    return x, np.repeat([1, 2, 3], sizes).astype(np.int32)
+
+
+@needs_ref
+@pytest.mark.parametrize("metric", [0, 1, 2])
+@pytest.mark.parametrize("stratified", [False, True])
+def test_knncv_vs_reference(orc, metric, stratified):
+    # small folds: the reference's HNSW search is exact here
+    x, y = _clustered(300, 10, 3)
+    a, fa, _ = ref.knncv(x, y, k=10, folds=10, stratified=stratified, metric=metric, cv_seed=5)
+    b, fb, _ = orc.knncv(x, y, k=10, folds=10, stratified=stratified, metric=metric, cv_seed=5)
+    assert np.array_equal(fa, fb) and np.array_equal(a, b)
+
+
+@needs_ref
+@pytest.mark.parametrize("metric", [0, 2])
+@pytest.mark.parametrize("constrained", [False, True])
+def test_core_knn_vs_reference(orc, metric, constrained):
+    x, _ = _clustered(600, 20, 4)
+    rng = np.random.default_rng(9)
+    init = rng.integers(1, 7, 600).astype(np.int32)
+    con = (np.arange(600) // 3 * 7 + 5).astype(np.int32)[rng.permutation(600)] if constrained else None
+    fix = (rng.random(600) < 0.1).astype(np.int32) if constrained else None
+    kw = dict(metric=metric, constrain=con, fixed=fix, cycles=15, k=10, folds=5, seed=4, cv_seed=6,
+              evolutionary=constrained, guarded=constrained, absorption=constrained)
+    a = ref.core_knn(x, init, **kw)
+    b = orc.core_knn(x, init, **kw)
+    for f in ("clbest", "cvpredbest", "folds", "vect_acc", "vect_score", "proposal_size",
+              "active_classes", "flags", "counters"):
+        assert np.array_equal(getattr(a, f), getattr(b, f)), f
