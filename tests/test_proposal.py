@@ -83,3 +83,24 @@ def test_snapshot_leaves_plain_run_unchanged(kg):
     assert np.array_equal(a.res, b.res) and np.array_equal(a.acc, b.acc)
     assert b.snapshot_features.shape == (4, 2000, 8)
     assert (b.snapshot_flags & 1).any()
+
+
+def test_default_weights_ship():
+    from kodama_gb300 import proposal_training as PT
+    w = PT.load_default()
+    assert w.shape == (M.PARAMS,) and np.isfinite(w).all()
+
+
+@pytest.mark.gpu
+def test_trained_network_gains_over_plain(kg):
+    # shipped weights, trained on plain-run moves of other workloads; at equal
+    # cycle counts the learned proposal reaches a higher mean final CV accuracy
+    from kodama_gb300 import proposal_training as PT
+    w = PT.load_default()
+    x, _ = datasets.gaussian_mixture(n=6000, d=30, seed=13)
+    kw = dict(runs=16, landmarks=4000, splitting=30, graph_neighbors=20, knn_k=20, folds=10, seed=5)
+    for T in (8, 12):
+        plain = kg.KODAMA_matrix(x, cycles=T, **kw)
+        learned = kg.KODAMA_matrix(x, cycles=T, proposal_weights=w, **kw)
+        assert learned.acc.mean() > plain.acc.mean() + 0.01, (T, plain.acc.mean(), learned.acc.mean())
+        assert (learned.acc > plain.acc).sum() > kw["runs"] // 2
