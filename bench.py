@@ -49,7 +49,7 @@ PLS_WORKLOAD = dict(n=10000, d=200, runs=50, cycles=50, graph_neighbors=30, knn_
 PLS_CPU_SAMPLE_RUNS = 16
 # DRAM bytes (read + write) of one evolution-kernel launch, scaled from the
 # ncu capture summarised in profiles/evolve_kernel_cfg2.md (None until captured).
-EVOLVE_TRAFFIC_BYTES = 280837120
+EVOLVE_TRAFFIC_BYTES = 457883648
 
 
 def _config(extra=None):
