@@ -284,11 +284,23 @@ int kgb_proposal_predict(const float* weights, const float* features, int32_t n,
 
 /* Exact kNN graph on the device: for each row its K nearest other rows by
  * squared Euclidean distance (float32, coordinate order, no FMA), ties by
- * index; idx zero-based, dist = sqrtf(d2).  Replaces
+ * index; idx zero-based, dist = sqrtf(d2).  Built by bf16 tensor-core
+ * candidate search with an exact re-rank where it applies (KGB_KNN_*).  Replaces
  * native_cuda_exact_knn_search (native_cuda_backend.hpp:165) as used by
  * self_knn_graph (kodama_matrix.cpp:391-533). */
 int kgb_knn_graph(const float* x, int32_t n, int32_t d, int32_t K, int32_t device, int32_t* idx,
                   float* dist);
+
+/* Search methods of the exact graph (all give the same result). */
+#define KGB_KNN_AUTO 0        /* the tensor-core search where it applies, else the brute force */
+#define KGB_KNN_BRUTE_FORCE 1 /* float32 brute force in the canonical order */
+#define KGB_KNN_TENSOR 2      /* bf16 hi+lo tensor-core candidates, canonical re-rank, per-row
+                                 certificate, brute force for uncertified rows; d <= 64, K <= 96 */
+
+/* kgb_knn_graph with an explicit method; fallback_rows (may be NULL) receives
+ * how many rows were computed by the brute force. */
+int kgb_knn_graph_ex(const float* x, int32_t n, int32_t d, int32_t K, int32_t device, int32_t method,
+                     int32_t* idx, float* dist, int32_t* fallback_rows);
 
 /* Replaces the Backend::CUDA branch of KODAMADissimilarityInPlace
  * (kodama.hpp:1181-1189, kodama_matrix.cpp:4383-4463): co-label proximity on a

@@ -440,14 +440,21 @@ def CoreKNN(x, labels, *, constrain=None, fixed=None, cycles=100, folds=10, stra
     return _wrap_core(r, bufs, cycles)
 
 
-def knn_graph(x, K: int, *, device: int = 0):
-    """Exact kNN graph: zero-based (n, K) indices and sqrt distances."""
+KNN_METHODS = {"auto": 0, "brute_force": 1, "tensor": 2}
+
+
+def knn_graph(x, K: int, *, device: int = 0, method: str = "auto", return_fallback: bool = False):
+    """Exact kNN graph: zero-based (n, K) indices and sqrt distances.
+    ``method``: "auto", "brute_force" or "tensor" (same result);
+    ``return_fallback`` adds the number of rows the brute force computed."""
     x = np.ascontiguousarray(x, dtype=np.float32)
     n, d = x.shape
     idx = np.zeros((n, K), np.int32)
     dist = np.zeros((n, K), np.float32)
-    N.check(N.load().kgb_knn_graph(_ptr(x), n, d, K, device, _ptr(idx), _ptr(dist)))
-    return idx, dist
+    fb = ctypes.c_int32(0)
+    N.check(N.load().kgb_knn_graph_ex(_ptr(x), n, d, K, device, KNN_METHODS[method], _ptr(idx), _ptr(dist),
+                                      ctypes.byref(fb)))
+    return (idx, dist, int(fb.value)) if return_fallback else (idx, dist)
 
 
 def KODAMADissimilarityInPlace(graph_idx: np.ndarray, graph_dist: np.ndarray, run_labels: np.ndarray,

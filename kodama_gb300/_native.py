@@ -24,6 +24,7 @@ EXPORTED = (
     "kgb_core_knn_graph",
     "kgb_core_knn_graph_batch",
     "kgb_knncv",
+    "kgb_knn_graph_ex",
     "kgb_core_knn",
     "kgb_plsldacv",
     "kgb_plslda_predict",
@@ -142,6 +143,7 @@ def load():
     lib.kgb_core_knn_graph_batch.argtypes = [P, P, i32, i32, i32, i32, P, P, P, ctypes.POINTER(CoreOptions),
                                              ctypes.POINTER(CoreResult)]
     lib.kgb_knn_graph.argtypes = [P, i32, i32, i32, i32, P, P]
+    lib.kgb_knn_graph_ex.argtypes = [P, i32, i32, i32, i32, i32, P, P, P]
     lib.kgb_knncv.argtypes = [P, i32, i32, P, P, ctypes.POINTER(KnnOptions), P, P]
     lib.kgb_core_knn.argtypes = [P, i32, i32, i32, P, P, P, ctypes.POINTER(CoreOptions), ctypes.POINTER(CoreResult)]
     lib.kgb_dissimilarity_inplace.argtypes = [P, P, i32, i32, P, i32, i32]

@@ -1111,6 +1111,32 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
 // Shared body of the KODAMA.matrix entry points: x on the host (copied in) or
 // already on the device; a caller graph (normalised like
 // normalize_external_graph) or the exact graph built on the device.
+// The exact kNN graph of d_x (n x d, device) into d_idx / d_dist (n x K):
+// the tensor-core candidate search with its certificate where it applies
+// (knn_tc.cu), else the brute force.  fallback_rows (host, may be null)
+// receives how many rows the certificate sent to the brute force.
+void exact_graph(Ctx& ctx, const float* d_x, int n, int d, int K, int method, int* d_idx, float* d_dist,
+                 int* fallback_rows) {
+  const int segments = 4;
+  const bool tc = method == KGB_KNN_TENSOR || (method == KGB_KNN_AUTO && kgb::knn_tc_supported(n, d, K));
+  if (method == KGB_KNN_TENSOR && !kgb::knn_tc_supported(n, d, K))
+    fail(KGB_EINVAL, "the tensor-core kNN search needs d <= 64, K <= 96 and n > 2 * (K + 16) + 64");
+  if (tc) {
+    void* scratch = ctx.alloc<unsigned char>(kgb::knn_tc_scratch(n, d, K, segments));
+    ck_launch(kgb::knn_tc_graph(d_x, n, d, K, segments, scratch, d_idx, d_dist, ctx.stream()), "kNN graph");
+    if (fallback_rows != nullptr) {
+      int count = 0;
+      ck_launch(kgb::knn_tc_fallback_count(scratch, n, d, K, segments, &count, ctx.stream()), "kNN graph");
+      ctx.sync();
+      *fallback_rows = count;
+    }
+  } else {
+    void* scratch = ctx.alloc<unsigned char>(kgb::knn_bruteforce_scratch(n, K, segments));
+    ck_launch(kgb::knn_bruteforce(d_x, n, d, K, segments, scratch, d_idx, d_dist, ctx.stream()), "kNN graph");
+    if (fallback_rows != nullptr) *fallback_rows = n;
+  }
+}
+
 void matrix_entry(const float* x, bool x_on_device, int n, int d, const int32_t* gidx, const float* gdist, int gk,
                   int index_base, const kgb_matrix_options* opt, kgb_matrix_result* out) {
   if (x == nullptr || out == nullptr) fail(KGB_EINVAL, "null pointer");
@@ -1156,9 +1182,7 @@ void matrix_entry(const float* x, bool x_on_device, int n, int d, const int32_t*
     K = neighbors;
     d_gidx = ctx.alloc<int>(static_cast<size_t>(n) * K);
     d_gdist = ctx.alloc<float>(static_cast<size_t>(n) * K);
-    const int segments = 4;
-    void* scratch = ctx.alloc<unsigned char>(kgb::knn_bruteforce_scratch(n, K, segments));
-    ck_launch(kgb::knn_bruteforce(d_x, n, d, K, segments, scratch, d_gidx, d_gdist, ctx.stream()), "kNN graph");
+    exact_graph(ctx, d_x, n, d, K, KGB_KNN_AUTO, d_gidx, d_gdist, nullptr);
   }
   const int ev_graph = ctx.mark();
   ctx.sync();
@@ -1421,19 +1445,26 @@ int kgb_core_knn_graph_batch(const int32_t* gidx, const float* gdist, int32_t sa
 }
 
 int kgb_knn_graph(const float* x, int32_t n, int32_t d, int32_t K, int32_t device, int32_t* idx, float* dist) {
+  return kgb_knn_graph_ex(x, n, d, K, device, KGB_KNN_AUTO, idx, dist, nullptr);
+}
+
+int kgb_knn_graph_ex(const float* x, int32_t n, int32_t d, int32_t K, int32_t device, int32_t method,
+                     int32_t* idx, float* dist, int32_t* fallback_rows) {
   return guarded([&]() {
     if (x == nullptr || idx == nullptr || dist == nullptr) fail(KGB_EINVAL, "null pointer");
     if (n < 1 || d < 1 || K < 1) fail(KGB_EINVAL, "invalid kNN graph dimensions");
+    if (method != KGB_KNN_AUTO && method != KGB_KNN_BRUTE_FORCE && method != KGB_KNN_TENSOR)
+      fail(KGB_EINVAL, "unknown kNN search method");
     Ctx ctx(device);
     const float* d_x = ctx.upload(x, static_cast<size_t>(n) * d);
     int* d_idx = ctx.alloc<int>(static_cast<size_t>(n) * K);
     float* d_dist = ctx.alloc<float>(static_cast<size_t>(n) * K);
-    const int segments = 4;
-    void* scratch = ctx.alloc<unsigned char>(kgb::knn_bruteforce_scratch(n, K, segments));
-    ck_launch(kgb::knn_bruteforce(d_x, n, d, K, segments, scratch, d_idx, d_dist, ctx.stream()), "kNN graph");
+    int fb = 0;
+    exact_graph(ctx, d_x, n, d, K, method, d_idx, d_dist, &fb);
     ctx.download(idx, d_idx, static_cast<size_t>(n) * K);
     ctx.download(dist, d_dist, static_cast<size_t>(n) * K);
     ctx.sync();
+    if (fallback_rows != nullptr) *fallback_rows = fb;
   });
 }
 

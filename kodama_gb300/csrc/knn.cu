@@ -85,23 +85,33 @@ __device__ __forceinline__ void topk_insert(float* bd, int* bi, int K, int& cnt,
 
 // FOLD: candidates are the rows whose fold differs from the query's (which
 // excludes the query itself); otherwise every row but the query.
+// Query slot qi is row qrows[qi] for qi < *nq (a row list, e.g. the rows a
+// faster search could not certify), or row qi when qrows is null.
+__device__ __forceinline__ int query_row(const int* qrows, const int* nq, int n, int qi) {
+  if (qrows == nullptr) return qi < n ? qi : -1;
+  return qi < *nq ? qrows[qi] : -1;
+}
+
 template <int NB, bool IP, bool FOLD>
 __global__ void __launch_bounds__(kQ) knn_segment_kernel(const float* __restrict__ x, int n, int d, int K,
                                                          int seg_len, const int* __restrict__ folds,
+                                                         const int* __restrict__ qrows, const int* __restrict__ nq,
                                                          float* __restrict__ pd, int* __restrict__ pi) {
   extern __shared__ float tile[];
   __shared__ int tfold[kTile];
+  if (qrows != nullptr && static_cast<int>(blockIdx.x) * kQ >= *nq) return;
   const int dp = (d + 3) & ~3;
-  const int q = blockIdx.x * kQ + threadIdx.x;
+  const int qi = blockIdx.x * kQ + threadIdx.x;
+  const int q = query_row(qrows, nq, n, qi);
   const int seg = blockIdx.y;
   const int c0 = seg * seg_len, c1 = min(n, c0 + seg_len);
   float qv[16 * NB];
-  const bool active = q < n;
+  const bool active = q >= 0;
 #pragma unroll
   for (int j = 0; j < 16 * NB; ++j) qv[j] = (active && j < d) ? x[static_cast<size_t>(q) * d + j] : 0.0f;
   const int fq = (FOLD && active) ? folds[q] : -1;
-  float* bd = pd + (static_cast<size_t>(seg) * n + (active ? q : 0)) * K;
-  int* bi = pi + (static_cast<size_t>(seg) * n + (active ? q : 0)) * K;
+  float* bd = pd + (static_cast<size_t>(seg) * n + (active ? qi : 0)) * K;
+  int* bi = pi + (static_cast<size_t>(seg) * n + (active ? qi : 0)) * K;
   int cnt = 0;
   float worst = INFINITY;
   for (int t0 = c0; t0 < c1; t0 += kTile) {
@@ -138,16 +148,20 @@ __global__ void __launch_bounds__(kQ) knn_segment_kernel(const float* __restrict
 template <bool IP, bool FOLD>
 __global__ void __launch_bounds__(kQ) knn_segment_generic_kernel(const float* __restrict__ x, int n, int d, int K,
                                                                  int seg_len, const int* __restrict__ folds,
+                                                                 const int* __restrict__ qrows,
+                                                                 const int* __restrict__ nq,
                                                                  float* __restrict__ pd, int* __restrict__ pi) {
   extern __shared__ float tile[];
   __shared__ int tfold[kTile];
-  const int q = blockIdx.x * kQ + threadIdx.x;
+  if (qrows != nullptr && static_cast<int>(blockIdx.x) * kQ >= *nq) return;
+  const int qi = blockIdx.x * kQ + threadIdx.x;
+  const int q = query_row(qrows, nq, n, qi);
   const int seg = blockIdx.y;
   const int c0 = seg * seg_len, c1 = min(n, c0 + seg_len);
-  const bool active = q < n;
+  const bool active = q >= 0;
   const int fq = (FOLD && active) ? folds[q] : -1;
-  float* bd = pd + (static_cast<size_t>(seg) * n + (active ? q : 0)) * K;
-  int* bi = pi + (static_cast<size_t>(seg) * n + (active ? q : 0)) * K;
+  float* bd = pd + (static_cast<size_t>(seg) * n + (active ? qi : 0)) * K;
+  int* bi = pi + (static_cast<size_t>(seg) * n + (active ? qi : 0)) * K;
   int cnt = 0;
   float worst = INFINITY;
   for (int t0 = c0; t0 < c1; t0 += kTile) {
@@ -184,9 +198,11 @@ __global__ void __launch_bounds__(kQ) knn_segment_generic_kernel(const float* __
 }
 
 __global__ void knn_merge_kernel(int n, int K, int segs, const float* __restrict__ pd, const int* __restrict__ pi,
-                                 bool raw, int* __restrict__ idx, float* __restrict__ dist) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= n) return;
+                                 const int* __restrict__ qrows, const int* __restrict__ nq, bool raw,
+                                 int* __restrict__ idx, float* __restrict__ dist) {
+  const int qi = blockIdx.x * blockDim.x + threadIdx.x;
+  const int qrow = query_row(qrows, nq, n, qi);
+  if (qrow < 0) return;
   int head[kMaxSegments];
   for (int s = 0; s < segs; ++s) head[s] = 0;
   for (int o = 0; o < K; ++o) {
@@ -195,7 +211,7 @@ __global__ void knn_merge_kernel(int n, int K, int segs, const float* __restrict
     int biv = 0x7fffffff;
     for (int s = 0; s < segs; ++s) {
       if (head[s] >= K) continue;
-      const size_t off = (static_cast<size_t>(s) * n + q) * K + head[s];
+      const size_t off = (static_cast<size_t>(s) * n + qi) * K + head[s];
       const float dv = pd[off];
       const int iv = pi[off];
       if (iv == 0x7fffffff) continue;
@@ -205,7 +221,7 @@ __global__ void knn_merge_kernel(int n, int K, int segs, const float* __restrict
         biv = iv;
       }
     }
-    const size_t out = static_cast<size_t>(q) * K + o;
+    const size_t out = static_cast<size_t>(qrow) * K + o;
     if (bs < 0) {
       idx[out] = -1;
       dist[out] = INFINITY;
@@ -295,24 +311,24 @@ __global__ void knn_fold_tables_kernel(const int* __restrict__ idx, const float*
 }
 
 template <bool IP, bool FOLD>
-int launch_segments(const float* x, int n, int d, int K, int segments, const int* folds, float* pd, int* pi,
-                    cudaStream_t st) {
+int launch_segments(const float* x, int n, int d, int K, int segments, const int* folds, const int* qrows,
+                    const int* nq, float* pd, int* pi, cudaStream_t st) {
   const int seg_len = (n + segments - 1) / segments;
   const dim3 grid((n + kQ - 1) / kQ, segments);
   const size_t smem = sizeof(float) * kTile * ((d + 3) & ~3);
   if (d <= 16) {
-    knn_segment_kernel<1, IP, FOLD><<<grid, kQ, smem, st>>>(x, n, d, K, seg_len, folds, pd, pi);
+    knn_segment_kernel<1, IP, FOLD><<<grid, kQ, smem, st>>>(x, n, d, K, seg_len, folds, qrows, nq, pd, pi);
   } else if (d <= 32) {
-    knn_segment_kernel<2, IP, FOLD><<<grid, kQ, smem, st>>>(x, n, d, K, seg_len, folds, pd, pi);
+    knn_segment_kernel<2, IP, FOLD><<<grid, kQ, smem, st>>>(x, n, d, K, seg_len, folds, qrows, nq, pd, pi);
   } else if (d <= 64) {
-    knn_segment_kernel<4, IP, FOLD><<<grid, kQ, smem, st>>>(x, n, d, K, seg_len, folds, pd, pi);
+    knn_segment_kernel<4, IP, FOLD><<<grid, kQ, smem, st>>>(x, n, d, K, seg_len, folds, qrows, nq, pd, pi);
   } else {
     if (smem > 48 * 1024) {
       const cudaError_t e = cudaFuncSetAttribute(knn_segment_generic_kernel<IP, FOLD>,
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
       if (e != cudaSuccess) return static_cast<int>(e);
     }
-    knn_segment_generic_kernel<IP, FOLD><<<grid, kQ, smem, st>>>(x, n, d, K, seg_len, folds, pd, pi);
+    knn_segment_generic_kernel<IP, FOLD><<<grid, kQ, smem, st>>>(x, n, d, K, seg_len, folds, qrows, nq, pd, pi);
   }
   count_launch();
   return static_cast<int>(cudaGetLastError());
@@ -330,9 +346,22 @@ int knn_bruteforce(const float* x, int n, int d, int K, int segments, void* scra
   if (segments > kMaxSegments) segments = kMaxSegments;
   float* pd = static_cast<float*>(scratch);
   int* pi = reinterpret_cast<int*>(pd + static_cast<size_t>(segments) * n * K);
-  const int e = launch_segments<false, false>(x, n, d, K, segments, nullptr, pd, pi, st);
+  const int e = launch_segments<false, false>(x, n, d, K, segments, nullptr, nullptr, nullptr, pd, pi, st);
   if (e != 0) return e;
-  knn_merge_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, K, segments, pd, pi, false, idx, dist);
+  knn_merge_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, K, segments, pd, pi, nullptr, nullptr, false, idx, dist);
+  count_launch();
+  return static_cast<int>(cudaGetLastError());
+}
+
+int knn_bruteforce_rows(const float* x, int n, int d, int K, int segments, const int* rows, const int* nrows,
+                        void* scratch, int* idx, float* dist, cudaStream_t st) {
+  if (segments < 1) segments = 1;
+  if (segments > kMaxSegments) segments = kMaxSegments;
+  float* pd = static_cast<float*>(scratch);
+  int* pi = reinterpret_cast<int*>(pd + static_cast<size_t>(segments) * n * K);
+  const int e = launch_segments<false, false>(x, n, d, K, segments, nullptr, rows, nrows, pd, pi, st);
+  if (e != 0) return e;
+  knn_merge_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, K, segments, pd, pi, rows, nrows, false, idx, dist);
   count_launch();
   return static_cast<int>(cudaGetLastError());
 }
@@ -343,10 +372,10 @@ int knn_fold_search(const float* x, int n, int d, int K, bool inner, const int* 
   if (segments > kMaxSegments) segments = kMaxSegments;
   float* pd = static_cast<float*>(scratch);
   int* pi = reinterpret_cast<int*>(pd + static_cast<size_t>(segments) * n * K);
-  const int e = inner ? launch_segments<true, true>(x, n, d, K, segments, folds, pd, pi, st)
-                      : launch_segments<false, true>(x, n, d, K, segments, folds, pd, pi, st);
+  const int e = inner ? launch_segments<true, true>(x, n, d, K, segments, folds, nullptr, nullptr, pd, pi, st)
+                      : launch_segments<false, true>(x, n, d, K, segments, folds, nullptr, nullptr, pd, pi, st);
   if (e != 0) return e;
-  knn_merge_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, K, segments, pd, pi, true, idx, dist);
+  knn_merge_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, K, segments, pd, pi, nullptr, nullptr, true, idx, dist);
   count_launch();
   return static_cast<int>(cudaGetLastError());
 }

@@ -13,6 +13,22 @@ size_t knn_bruteforce_scratch(int n, int K, int segments);
 int knn_bruteforce(const float* x, int n, int d, int K, int segments, void* scratch, int* idx, float* dist,
                    cudaStream_t st);
 
+// knn_bruteforce restricted to the *nrows rows listed in rows (read on the
+// device): their results are written, the other rows' left untouched.
+int knn_bruteforce_rows(const float* x, int n, int d, int K, int segments, const int* rows, const int* nrows,
+                        void* scratch, int* idx, float* dist, cudaStream_t st);
+
+// The same exact graph as knn_bruteforce through a tensor-core candidate
+// search with an exact re-rank and a per-row certificate (knn_tc.cu); rows
+// whose certificate fails are recomputed by knn_bruteforce_rows.
+bool knn_tc_supported(int n, int d, int K);
+size_t knn_tc_scratch(int n, int d, int K, int segments);
+int knn_tc_graph(const float* x, int n, int d, int K, int segments, void* scratch, int* idx, float* dist,
+                 cudaStream_t st);
+// Rows of the last knn_tc_graph on this scratch that went to the fallback
+// (asynchronous copy into host memory).
+int knn_tc_fallback_count(const void* scratch, int n, int d, int K, int segments, int* out, cudaStream_t st);
+
 // Fold-wise search: for each row the K nearest rows of other folds (folds[n]),
 // ranked by (internal distance, row); inner = minus the inner product instead
 // of the squared L2 distance.  idx -1 / dist +inf where fewer rows qualify;

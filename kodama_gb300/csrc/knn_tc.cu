@@ -1,0 +1,458 @@
+// Exact kNN graph through a tensor-core candidate search (knn.cuh).
+//
+// The canonical result (knn.cu: squared L2 as a float32 chain over the
+// coordinates in order, each term separately rounded, ties by index) is
+// found in three steps:
+//
+//  1. candidates: every row is split once into bfloat16 hi + lo parts
+//     (x = hi + lo + r, |r| <= 2^-16 |x|); a warp computes the approximate
+//     distances a = |q|^2 + |c|^2 - 2 (hi.hi + hi.lo + lo.hi) of 16 queries
+//     to a 64-row candidate tile with mma.sync (bf16 in, f32 accumulate);
+//     every query keeps the kp smallest approximate distances in a sorted
+//     list in shared memory.  Lanes flag the values of their accumulator
+//     fragments below their rows' thresholds, and the warp inserts the
+//     flagged values one at a time, all lanes together (position by a warp
+//     reduction, parallel shift), so the selection never diverges.  Each
+//     CTA walks the candidate tiles in a scattered order, so data sorted by
+//     cluster does not turn every value of a query's own cluster into an
+//     insertion;
+//  2. re-rank: one warp per query computes the canonical distances of its kp
+//     candidates and takes the K smallest by (distance, index);
+//  3. certificate: every row left out of a query's list has a >= B, the
+//     list's final threshold; with |a - e| <= delta for every row (delta from
+//     the error bound below), e_K < B - delta proves that no excluded row
+//     can enter the top K or tie with it.  Rows whose certificate fails are
+//     listed and recomputed by the brute-force kernels (knn.cu).
+//
+// Error bound (u = 2^-24): with D the true squared distance and e its
+// canonical value, |e - D| <= (d + 4) u D <= 2 (d + 4) u (|q|^2 + |c|^2);
+// the split drops hi.hi residuals of at most ~3.1 * 2^-16 sum|q_i c_i|, the
+// f32 accumulation of 3 dp products adds at most 3 dp 2^-22 sum|q_i c_i|
+// (tensor-core accumulation allowed two ulps per add), and
+// sum|q_i c_i| <= (|q|^2 + |c|^2) / 2; the f32 norms and the final
+// combination add (d + 8) u (|q|^2 + |c|^2).  So
+// delta <= (|q|^2 + max |c|^2) * (1e-4 + 2e-6 dp), a safe over-estimate.
+#include "knn.cuh"
+#include "launch_count.cuh"
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+namespace kgb {
+
+namespace {
+
+constexpr int kTcWarps = 4;            // warps per CTA, 16 queries each
+constexpr int kTcQ = 16 * kTcWarps;    // queries per CTA
+constexpr int kTcN = 64;               // candidates per tile
+constexpr int kTcMaxKs = 4;            // k-steps of 16 held in registers (dp <= 64)
+constexpr int kTileStride = kTcN + 8;  // floats per row of a warp's distance tile
+
+__device__ __forceinline__ uint32_t bf16_bits(float v) {
+  // round to the nearest bfloat16 (ties to even); inf / nan kept
+  const uint32_t u = __float_as_uint(v);
+  if ((u & 0x7f800000u) == 0x7f800000u) return u >> 16;
+  return (u + 0x7fffu + ((u >> 16) & 1u)) >> 16;
+}
+
+// Position of coordinate k inside its 16-block: the four values a lane feeds
+// to one m16n8k16 fragment (k = 2t, 2t+1, 2t+8, 2t+9) are contiguous at 4t.
+__device__ __forceinline__ int perm16(int k) {
+  const int kk = k & 15;
+  return (k & ~15) | (4 * ((kk & 7) >> 1) + ((kk & 1) | ((kk >> 3) << 1)));
+}
+
+__global__ void tc_prep_kernel(const float* __restrict__ x, int n, int d, int dp, uint16_t* __restrict__ xh,
+                               uint16_t* __restrict__ xl, float* __restrict__ nrm, unsigned* __restrict__ nrm_max,
+                               int* __restrict__ nonfinite) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  float s = 0.0f;
+  bool fin = true;
+  for (int k = 0; k < dp; ++k) {
+    const float v = k < d ? x[static_cast<size_t>(r) * d + k] : 0.0f;
+    fin = fin && isfinite(v);
+    const uint32_t hb = bf16_bits(v);
+    const float h = __uint_as_float(hb << 16);
+    const uint32_t lb = bf16_bits(__fsub_rn(v, h));
+    const size_t o = static_cast<size_t>(r) * dp + perm16(k);
+    xh[o] = static_cast<uint16_t>(hb);
+    xl[o] = static_cast<uint16_t>(lb);
+    s = __fadd_rn(s, __fmul_rn(v, v));
+  }
+  nrm[r] = s;
+  if (fin) atomicMax(nrm_max, __float_as_uint(s));
+  else atomicExch(nonfinite, 1);
+}
+
+__device__ __forceinline__ void mma16816(float* c, const uint32_t* a, uint2 b) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b.x), "r"(b.y));
+}
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
+}
+
+struct TcArgs {
+  const uint16_t* xh;   // n x dp, permuted 16-blocks
+  const uint16_t* xl;
+  const float* nrm;     // n
+  int n, dp, kp;
+  int row_words;        // 32-bit words per candidate row in shared memory (= 8 mod 16)
+  int* cand;            // n x kp candidate rows (-1 = none)
+  float* bound;         // n: the list's final threshold (+inf = nothing excluded)
+};
+
+constexpr int kMaxPer = 4;  // list entries per lane (kp <= 128)
+
+// Shared memory: 2 x (hi, lo) candidate tiles, 2 x tile norms, per warp a
+// 16 x kTileStride distance tile, 16 sorted lists of kp (distance, row)
+// entries, their lengths and thresholds.
+size_t tc_smem_bytes(int row_words, int kp) {
+  return 2 * 2 * static_cast<size_t>(kTcN) * row_words * 4 + 2 * kTcN * 4 +
+         kTcWarps * (16 * kTileStride * 4 + 16 * static_cast<size_t>(kp) * 8 + 16 * 8);
+}
+
+__global__ void __launch_bounds__(32 * kTcWarps) tc_candidates_kernel(TcArgs A) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
+  const int n = A.n, dp = A.dp, kp = A.kp, rw = A.row_words, ksn = dp >> 4;
+  uint32_t* cbuf = reinterpret_cast<uint32_t*>(smem);  // [buf][hi/lo][kTcN][rw]
+  float* cnb = reinterpret_cast<float*>(cbuf + 2 * 2 * kTcN * rw);  // [buf][kTcN]
+  float* wbase = cnb + 2 * kTcN + warp * (16 * kTileStride + 16 * kp * 2 + 16 * 2);
+  float* dt = wbase;                                   // [16][kTileStride]
+  float* lv = dt + 16 * kTileStride;                   // [16][kp] distances
+  int* lj = reinterpret_cast<int*>(lv + 16 * kp);      // [16][kp] rows
+  int* lcnt = lj + 16 * kp;                            // [16]
+  float* ltau = reinterpret_cast<float*>(lcnt + 16);   // [16]
+  if (lane < 16) {
+    lcnt[lane] = 0;
+    ltau[lane] = INFINITY;
+  }
+
+  const int q0 = blockIdx.x * kTcQ + warp * 16;
+  // query fragments: rows g and g + 8 of the warp's 16 queries
+  uint32_t ah[kTcMaxKs][4], al[kTcMaxKs][4];
+  {
+    const int ra = min(q0 + g, n - 1), rb = min(q0 + g + 8, n - 1);
+#pragma unroll
+    for (int ks = 0; ks < kTcMaxKs; ++ks) {
+      uint2 pa = make_uint2(0u, 0u), pb = pa, qa = pa, qb = pa;
+      if (ks < ksn) {
+        pa = *reinterpret_cast<const uint2*>(A.xh + static_cast<size_t>(ra) * dp + ks * 16 + 4 * tig);
+        pb = *reinterpret_cast<const uint2*>(A.xh + static_cast<size_t>(rb) * dp + ks * 16 + 4 * tig);
+        qa = *reinterpret_cast<const uint2*>(A.xl + static_cast<size_t>(ra) * dp + ks * 16 + 4 * tig);
+        qb = *reinterpret_cast<const uint2*>(A.xl + static_cast<size_t>(rb) * dp + ks * 16 + 4 * tig);
+      }
+      ah[ks][0] = pa.x; ah[ks][2] = pa.y; ah[ks][1] = pb.x; ah[ks][3] = pb.y;
+      al[ks][0] = qa.x; al[ks][2] = qa.y; al[ks][1] = qb.x; al[ks][3] = qb.y;
+    }
+  }
+  const int qa_row = q0 + g, qb_row = q0 + g + 8;
+  const float nq_g = A.nrm[min(qa_row, n - 1)], nq_g8 = A.nrm[min(qb_row, n - 1)];
+  __syncwarp();
+
+  // scattered tile order: tile t is visited at step (t0 + step * stride) mod ntiles
+  // with stride coprime to ntiles (a prime above any tile count)
+  const int ntiles = (n + kTcN - 1) / kTcN;
+  const int stride = static_cast<int>(1000003ull % static_cast<unsigned long long>(ntiles));
+  const int first = static_cast<int>((static_cast<unsigned long long>(blockIdx.x) * 7919ull) % ntiles);
+  auto tile_at = [&](int step) {
+    return static_cast<int>((static_cast<unsigned long long>(first) +
+                             static_cast<unsigned long long>(step) * stride) % ntiles) * kTcN;
+  };
+
+  auto load_tile = [&](int buf, int base) {
+    const int chunks = dp >> 3;  // 16-byte chunks per row
+    for (int e = threadIdx.x; e < kTcN * chunks; e += 32 * kTcWarps) {
+      const int c = e / chunks, ch = e - c * chunks;
+      const int row = base + c;
+      uint32_t* dh = cbuf + ((buf * 2 + 0) * kTcN + c) * rw + ch * 4;
+      uint32_t* dl = cbuf + ((buf * 2 + 1) * kTcN + c) * rw + ch * 4;
+      if (row < n) {
+        cp_async16(dh, A.xh + static_cast<size_t>(row) * dp + ch * 8);
+        cp_async16(dl, A.xl + static_cast<size_t>(row) * dp + ch * 8);
+      } else {
+        *reinterpret_cast<uint4*>(dh) = make_uint4(0u, 0u, 0u, 0u);
+        *reinterpret_cast<uint4*>(dl) = make_uint4(0u, 0u, 0u, 0u);
+      }
+    }
+    for (int c = threadIdx.x; c < kTcN; c += 32 * kTcWarps) cnb[buf * kTcN + c] = base + c < n ? A.nrm[base + c] : 0.0f;
+    cp_async_commit();
+  };
+
+  load_tile(0, tile_at(0));
+  for (int step = 0; step < ntiles; ++step) {
+    const int buf = step & 1;
+    const int t0 = tile_at(step);
+    if (step + 1 < ntiles) {
+      load_tile(buf ^ 1, tile_at(step + 1));
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    const uint32_t* th = cbuf + (buf * 2 + 0) * kTcN * rw;
+    const uint32_t* tl = cbuf + (buf * 2 + 1) * kTcN * rw;
+    const float* cn = cnb + buf * kTcN;
+    const float tau_a = ltau[g], tau_b = ltau[g + 8];
+    unsigned flags = 0u;  // bit 4 nt + k: value k of n-tile nt is below its row's threshold
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+      float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+      for (int ks = 0; ks < kTcMaxKs; ++ks) {
+        if (ks < ksn) {
+          const int off = (nt * 8 + g) * rw + ks * 8 + 2 * tig;
+          const uint2 bh = *reinterpret_cast<const uint2*>(th + off);
+          const uint2 bl = *reinterpret_cast<const uint2*>(tl + off);
+          mma16816(acc, ah[ks], bh);
+          mma16816(acc, ah[ks], bl);
+          mma16816(acc, al[ks], bh);
+        }
+      }
+      const int col = nt * 8 + 2 * tig;
+      const float c0 = cn[col], c1 = cn[col + 1];
+      const float v0 = nq_g + c0 - 2.0f * acc[0], v1 = nq_g + c1 - 2.0f * acc[1];
+      const float v2 = nq_g8 + c0 - 2.0f * acc[2], v3 = nq_g8 + c1 - 2.0f * acc[3];
+      const int j0 = t0 + col, j1 = j0 + 1;
+      flags |= static_cast<unsigned>(v0 < tau_a && j0 < n && j0 != qa_row && qa_row < n) << (4 * nt + 0);
+      flags |= static_cast<unsigned>(v1 < tau_a && j1 < n && j1 != qa_row && qa_row < n) << (4 * nt + 1);
+      flags |= static_cast<unsigned>(v2 < tau_b && j0 < n && j0 != qb_row && qb_row < n) << (4 * nt + 2);
+      flags |= static_cast<unsigned>(v3 < tau_b && j1 < n && j1 != qb_row && qb_row < n) << (4 * nt + 3);
+      *reinterpret_cast<float2*>(dt + g * kTileStride + col) = make_float2(v0, v1);
+      *reinterpret_cast<float2*>(dt + (g + 8) * kTileStride + col) = make_float2(v2, v3);
+    }
+    __syncwarp();
+    // insert the flagged values, one at a time, the whole warp together
+    for (;;) {
+      const unsigned who = __ballot_sync(0xffffffffu, flags != 0u);
+      if (who == 0u) break;
+      const int src = __ffs(who) - 1;
+      const unsigned sf = __shfl_sync(0xffffffffu, flags, src);
+      const int b = __ffs(sf) - 1;
+      if (lane == src) flags &= flags - 1u;
+      const int sg = src >> 2, stig = src & 3, nt = b >> 2, k = b & 3;
+      const int row = (k & 2) ? sg + 8 : sg;
+      const int col = nt * 8 + 2 * stig + (k & 1);
+      const float v = dt[row * kTileStride + col];
+      const int j = t0 + col;
+      const int cnt = lcnt[row];
+      if (!(v < ltau[row])) continue;  // the threshold fell since the value was flagged
+      float* rv = lv + row * kp;
+      int* rj = lj + row * kp;
+      int below = 0;
+#pragma unroll
+      for (int t = 0; t < kMaxPer; ++t) {
+        const int e = lane + 32 * t;
+        if (e < cnt && rv[e] <= v) ++below;
+      }
+      const int pos = __reduce_add_sync(0xffffffffu, below);
+      const int last = min(cnt, kp - 1);  // entries [pos, last) move one place up
+      float mv[kMaxPer];
+      int mj[kMaxPer];
+#pragma unroll
+      for (int t = 0; t < kMaxPer; ++t) {
+        const int e = lane + 32 * t;
+        if (e >= pos && e < last) {
+          mv[t] = rv[e];
+          mj[t] = rj[e];
+        }
+      }
+      __syncwarp();
+#pragma unroll
+      for (int t = 0; t < kMaxPer; ++t) {
+        const int e = lane + 32 * t;
+        if (e >= pos && e < last) {
+          rv[e + 1] = mv[t];
+          rj[e + 1] = mj[t];
+        }
+      }
+      __syncwarp();
+      if (lane == 0) {
+        rv[pos] = v;
+        rj[pos] = j;
+        const int nc = min(cnt + 1, kp);
+        lcnt[row] = nc;
+        if (nc == kp) ltau[row] = rv[kp - 1];
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+  }
+  // lists out; the bound is the final threshold (+inf while a list is short)
+  for (int r = 0; r < 16; ++r) {
+    const int q = q0 + r;
+    if (q >= n) break;
+    const int cnt = lcnt[r];
+    for (int e = lane; e < kp; e += 32) A.cand[static_cast<size_t>(q) * kp + e] = e < cnt ? lj[r * kp + e] : -1;
+    if (lane == 0) A.bound[q] = cnt == kp ? ltau[r] : INFINITY;
+  }
+}
+
+// One warp per query: canonical distances of the kp candidates, the K
+// smallest by (distance, index), the certificate e_K < B - delta (every row
+// goes to the fallback list when the data hold a non-finite value).
+__global__ void tc_rerank_kernel(const float* __restrict__ x, int n, int d, int K, int kp,
+                                 const int* __restrict__ cand, const float* __restrict__ bound,
+                                 const float* __restrict__ nrm, const unsigned* __restrict__ nrm_max,
+                                 const int* __restrict__ nonfinite, float crel, int* __restrict__ idx,
+                                 float* __restrict__ dist, int* __restrict__ fb_rows, int* __restrict__ fb_count) {
+  constexpr int kPer = kMaxPer;  // candidates per lane (kp <= 128)
+  const int lane = threadIdx.x & 31;
+  const int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (q >= n) return;
+  if (*nonfinite) {
+    if (lane == 0) fb_rows[atomicAdd(fb_count, 1)] = q;
+    return;
+  }
+  const int m = kp;
+  const float* xq = x + static_cast<size_t>(q) * d;
+  // (distance bits, row): canonical distances are >= 0, so their bit
+  // patterns order like the values and the keys order by (distance, row)
+  unsigned long long key[kPer];
+#pragma unroll
+  for (int t = 0; t < kPer; ++t) {
+    const int e = lane + 32 * t;
+    key[t] = ~0ull;
+    if (e < m) {
+      const int j = cand[static_cast<size_t>(q) * m + e];
+      if (j >= 0) {
+        const float* xj = x + static_cast<size_t>(j) * d;
+        float a = 0.0f;
+        for (int k = 0; k < d; ++k) {
+          const float diff = __fsub_rn(xq[k], xj[k]);
+          a = __fadd_rn(a, __fmul_rn(diff, diff));
+        }
+        key[t] = (static_cast<unsigned long long>(__float_as_uint(a)) << 32) | static_cast<unsigned>(j);
+      }
+    }
+  }
+  float eK = INFINITY;
+  for (int o = 0; o < K; ++o) {
+    unsigned long long best = key[0];
+#pragma unroll
+    for (int t = 1; t < kPer; ++t) best = key[t] < best ? key[t] : best;
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) {
+      const unsigned long long other = __shfl_xor_sync(0xffffffffu, best, s);
+      best = other < best ? other : best;
+    }
+#pragma unroll
+    for (int t = 0; t < kPer; ++t)
+      if (key[t] == best) key[t] = ~0ull;
+    if (lane == 0) {
+      const size_t out = static_cast<size_t>(q) * K + o;
+      if (best == ~0ull) {
+        idx[out] = -1;
+        dist[out] = INFINITY;
+        eK = INFINITY;
+      } else {
+        eK = __uint_as_float(static_cast<unsigned>(best >> 32));
+        idx[out] = static_cast<int>(best & 0xffffffffu);
+        dist[out] = __fsqrt_rn(eK);
+      }
+    }
+  }
+  if (lane == 0) {
+    const float delta = (nrm[q] + __uint_as_float(*nrm_max)) * crel;
+    if (!(eK < bound[q] - delta)) fb_rows[atomicAdd(fb_count, 1)] = q;
+  }
+}
+
+}  // namespace
+
+bool knn_tc_supported(int n, int d, int K) {
+  const int kp = (K + 16 + 15) / 16 * 16;
+  return d >= 1 && d <= 16 * kTcMaxKs && K >= 1 && kp <= 32 * kMaxPer && n > 2 * kp + kTcN;
+}
+
+namespace {
+
+struct TcLayout {
+  int dp, kp, rw;
+  size_t o_xh, o_xl, o_nrm, o_flags, o_cand, o_bound, o_fb, o_brute, total;
+};
+
+TcLayout tc_layout(int n, int d, int K, int segments) {
+  TcLayout L{};
+  L.dp = (d + 15) / 16 * 16;
+  L.kp = (K + 16 + 15) / 16 * 16;
+  const int half = L.dp / 2;
+  L.rw = (half % 16 == 8) ? half : half + 8;
+  auto al = [](size_t v) { return (v + 255) / 256 * 256; };
+  size_t o = 0;
+  L.o_xh = o; o = al(o + static_cast<size_t>(n) * L.dp * 2);
+  L.o_xl = o; o = al(o + static_cast<size_t>(n) * L.dp * 2);
+  L.o_nrm = o; o = al(o + static_cast<size_t>(n) * 4);
+  L.o_flags = o; o = al(o + 16);  // nrm_max, nonfinite, fb_count
+  L.o_cand = o; o = al(o + static_cast<size_t>(n) * L.kp * 4);
+  L.o_bound = o; o = al(o + static_cast<size_t>(n) * 4);
+  L.o_fb = o; o = al(o + static_cast<size_t>(n) * 4);
+  L.o_brute = o; o = al(o + knn_bruteforce_scratch(n, K, segments));
+  L.total = o;
+  return L;
+}
+
+}  // namespace
+
+size_t knn_tc_scratch(int n, int d, int K, int segments) { return tc_layout(n, d, K, segments).total; }
+
+int knn_tc_graph(const float* x, int n, int d, int K, int segments, void* scratch, int* idx, float* dist,
+                 cudaStream_t st) {
+  const TcLayout L = tc_layout(n, d, K, segments);
+  unsigned char* b = static_cast<unsigned char*>(scratch);
+  uint16_t* xh = reinterpret_cast<uint16_t*>(b + L.o_xh);
+  uint16_t* xl = reinterpret_cast<uint16_t*>(b + L.o_xl);
+  float* nrm = reinterpret_cast<float*>(b + L.o_nrm);
+  unsigned* flags = reinterpret_cast<unsigned*>(b + L.o_flags);  // [0] nrm_max bits, [1] nonfinite, [2] fallback count
+  int* cand = reinterpret_cast<int*>(b + L.o_cand);
+  float* bound = reinterpret_cast<float*>(b + L.o_bound);
+  int* fb = reinterpret_cast<int*>(b + L.o_fb);
+  cudaError_t e = cudaMemsetAsync(flags, 0, 16, st);
+  if (e != cudaSuccess) return static_cast<int>(e);
+  tc_prep_kernel<<<(n + 127) / 128, 128, 0, st>>>(x, n, d, L.dp, xh, xl, nrm, flags,
+                                                 reinterpret_cast<int*>(flags + 1));
+  TcArgs A{};
+  A.xh = xh;
+  A.xl = xl;
+  A.nrm = nrm;
+  A.n = n;
+  A.dp = L.dp;
+  A.kp = L.kp;
+  A.row_words = L.rw;
+  A.cand = cand;
+  A.bound = bound;
+  const size_t smem = tc_smem_bytes(L.rw, L.kp);
+  e = cudaFuncSetAttribute(tc_candidates_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  if (e != cudaSuccess) return static_cast<int>(e);
+  tc_candidates_kernel<<<(n + kTcQ - 1) / kTcQ, 32 * kTcWarps, smem, st>>>(A);
+  const float crel = 1e-4f + 2e-6f * static_cast<float>(L.dp);
+  tc_rerank_kernel<<<(n + 3) / 4, 128, 0, st>>>(x, n, d, K, L.kp, cand, bound, nrm, flags,
+                                                 reinterpret_cast<const int*>(flags + 1), crel, idx, dist, fb,
+                                                 reinterpret_cast<int*>(flags + 2));
+  count_launch(3);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return static_cast<int>(e);
+  return knn_bruteforce_rows(x, n, d, K, segments, fb, reinterpret_cast<const int*>(flags + 2), b + L.o_brute, idx,
+                             dist, st);
+}
+
+int knn_tc_fallback_count(const void* scratch, int n, int d, int K, int segments, int* out, cudaStream_t st) {
+  const TcLayout L = tc_layout(n, d, K, segments);
+  const unsigned char* b = static_cast<const unsigned char*>(scratch);
+  return static_cast<int>(cudaMemcpyAsync(out, b + L.o_flags + 8, sizeof(int), cudaMemcpyDeviceToHost, st));
+}
+
+}  // namespace kgb
