@@ -8,18 +8,18 @@
 //     (x = hi + lo + r, |r| <= 2^-16 |x|); a warp computes the approximate
 //     distances a = |q|^2 + |c|^2 - 2 (hi.hi + hi.lo + lo.hi) of 16 queries
 //     to a 64-row candidate tile with mma.sync (bf16 in, f32 accumulate);
-//     every query keeps the kp smallest approximate distances in a sorted
-//     list in shared memory.  Lanes flag the values of their accumulator
-//     fragments below their rows' thresholds, and the warp inserts the
-//     flagged values one at a time, all lanes together (position by a warp
-//     reduction, parallel shift), so the selection never diverges.  Each
-//     CTA walks the candidate tiles in a scattered order, so data sorted by
-//     cluster does not turn every value of a query's own cluster into an
-//     insertion;
-//  2. re-rank: one warp per query computes the canonical distances of its kp
-//     candidates and takes the K smallest by (distance, index);
-//  3. certificate: every row left out of a query's list has a >= B, the
-//     list's final threshold; with |a - e| <= delta for every row (delta from
+//     every query keeps the kp smallest approximate distances of each half
+//     of its columns in two max-heaps, one per lane (lanes r and r + 16 own
+//     query row r).  The lanes holding the accumulator fragments flag the
+//     values below their heap's threshold and publish per-row masks; each
+//     owner lane then inserts only its flagged values, so the insertions of
+//     the 32 heaps run side by side.  Each CTA walks the candidate tiles in
+//     a scattered order, so data sorted by cluster does not turn every value
+//     of a query's own cluster into an insertion;
+//  2. re-rank: one warp per query computes the canonical distances of its
+//     2 kp candidates and takes the K smallest by (distance, index);
+//  3. certificate: every row left out of a query's heaps has a >= B, the
+//     smaller final heap threshold; with |a - e| <= delta for every row (delta from
 //     the error bound below), e_K < B - delta proves that no excluded row
 //     can enter the top K or tie with it.  Rows whose certificate fails are
 //     listed and recomputed by the brute-force kernels (knn.cu).
@@ -110,18 +110,18 @@ struct TcArgs {
   const float* nrm;     // n
   int n, dp, kp;
   int row_words;        // 32-bit words per candidate row in shared memory (= 8 mod 16)
-  int* cand;            // n x kp candidate rows (-1 = none)
-  float* bound;         // n: the list's final threshold (+inf = nothing excluded)
+  int* cand;            // n x 2 kp candidate rows (-1 = none)
+  float* bound;         // n: the smaller final heap threshold (+inf = nothing excluded)
 };
 
-constexpr int kMaxPer = 4;  // list entries per lane (kp <= 128)
+constexpr int kMaxPer = 8;  // re-rank candidates per lane (2 kp <= 256)
 
 // Shared memory: 2 x (hi, lo) candidate tiles, 2 x tile norms, per warp a
-// 16 x kTileStride distance tile, 16 sorted lists of kp (distance, row)
-// entries, their lengths and thresholds.
+// 16 x kTileStride distance tile, 16 x 4 flag masks, 32 thresholds and 32
+// lane-interleaved max-heaps of kp (distance, row) entries.
 size_t tc_smem_bytes(int row_words, int kp) {
   return 2 * 2 * static_cast<size_t>(kTcN) * row_words * 4 + 2 * kTcN * 4 +
-         kTcWarps * (16 * kTileStride * 4 + 16 * static_cast<size_t>(kp) * 8 + 16 * 8);
+         kTcWarps * (16 * kTileStride * 4 + 64 * 4 + 32 * 4 + 32 * static_cast<size_t>(kp) * 8);
 }
 
 __global__ void __launch_bounds__(32 * kTcWarps) tc_candidates_kernel(TcArgs A) {
@@ -130,16 +130,12 @@ __global__ void __launch_bounds__(32 * kTcWarps) tc_candidates_kernel(TcArgs A) 
   const int n = A.n, dp = A.dp, kp = A.kp, rw = A.row_words, ksn = dp >> 4;
   uint32_t* cbuf = reinterpret_cast<uint32_t*>(smem);  // [buf][hi/lo][kTcN][rw]
   float* cnb = reinterpret_cast<float*>(cbuf + 2 * 2 * kTcN * rw);  // [buf][kTcN]
-  float* wbase = cnb + 2 * kTcN + warp * (16 * kTileStride + 16 * kp * 2 + 16 * 2);
-  float* dt = wbase;                                   // [16][kTileStride]
-  float* lv = dt + 16 * kTileStride;                   // [16][kp] distances
-  int* lj = reinterpret_cast<int*>(lv + 16 * kp);      // [16][kp] rows
-  int* lcnt = lj + 16 * kp;                            // [16]
-  float* ltau = reinterpret_cast<float*>(lcnt + 16);   // [16]
-  if (lane < 16) {
-    lcnt[lane] = 0;
-    ltau[lane] = INFINITY;
-  }
+  float* dt = cnb + 2 * kTcN + warp * (16 * kTileStride + 64 + 32 + 32 * kp * 2);  // [16][kTileStride]
+  unsigned* fmask = reinterpret_cast<unsigned*>(dt + 16 * kTileStride);            // [16][4]
+  float* htau = reinterpret_cast<float*>(fmask + 64);                              // [32] per heap
+  float* hv = htau + 32;                                                           // [kp][32]
+  int* hj = reinterpret_cast<int*>(hv + 32 * kp);                                  // [kp][32]
+  htau[lane] = INFINITY;
 
   const int q0 = blockIdx.x * kTcQ + warp * 16;
   // query fragments: rows g and g + 8 of the warp's 16 queries
@@ -161,10 +157,16 @@ __global__ void __launch_bounds__(32 * kTcWarps) tc_candidates_kernel(TcArgs A) 
   }
   const int qa_row = q0 + g, qb_row = q0 + g + 8;
   const float nq_g = A.nrm[min(qa_row, n - 1)], nq_g8 = A.nrm[min(qb_row, n - 1)];
+  // the heap this lane owns: query row r, the columns of quad lanes 2 h, 2 h + 1
+  const int r = lane & 15, h = lane >> 4, myq = q0 + r;
+  // the heaps whose thresholds this lane's fragment values are filtered by
+  const int heap_a = g + 16 * (tig >> 1), heap_b = heap_a + 8;
+  int cnt = 0;
+  float tau = INFINITY;
   __syncwarp();
 
-  // scattered tile order: tile t is visited at step (t0 + step * stride) mod ntiles
-  // with stride coprime to ntiles (a prime above any tile count)
+  // scattered tile order: tile t is visited at step (first + step * stride) mod
+  // ntiles, stride coprime to ntiles (1000003 is a prime above any tile count)
   const int ntiles = (n + kTcN - 1) / kTcN;
   const int stride = static_cast<int>(1000003ull % static_cast<unsigned long long>(ntiles));
   const int first = static_cast<int>((static_cast<unsigned long long>(blockIdx.x) * 7919ull) % ntiles);
@@ -206,8 +208,8 @@ __global__ void __launch_bounds__(32 * kTcWarps) tc_candidates_kernel(TcArgs A) 
     const uint32_t* th = cbuf + (buf * 2 + 0) * kTcN * rw;
     const uint32_t* tl = cbuf + (buf * 2 + 1) * kTcN * rw;
     const float* cn = cnb + buf * kTcN;
-    const float tau_a = ltau[g], tau_b = ltau[g + 8];
-    unsigned flags = 0u;  // bit 4 nt + k: value k of n-tile nt is below its row's threshold
+    const float tau_a = htau[heap_a], tau_b = htau[heap_b];
+    unsigned fa = 0u, fb = 0u;  // bit 2 nt + c: column nt * 8 + 2 tig + c of rows g / g + 8
 #pragma unroll
     for (int nt = 0; nt < 8; ++nt) {
       float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
@@ -227,81 +229,82 @@ __global__ void __launch_bounds__(32 * kTcWarps) tc_candidates_kernel(TcArgs A) 
       const float v0 = nq_g + c0 - 2.0f * acc[0], v1 = nq_g + c1 - 2.0f * acc[1];
       const float v2 = nq_g8 + c0 - 2.0f * acc[2], v3 = nq_g8 + c1 - 2.0f * acc[3];
       const int j0 = t0 + col, j1 = j0 + 1;
-      flags |= static_cast<unsigned>(v0 < tau_a && j0 < n && j0 != qa_row && qa_row < n) << (4 * nt + 0);
-      flags |= static_cast<unsigned>(v1 < tau_a && j1 < n && j1 != qa_row && qa_row < n) << (4 * nt + 1);
-      flags |= static_cast<unsigned>(v2 < tau_b && j0 < n && j0 != qb_row && qb_row < n) << (4 * nt + 2);
-      flags |= static_cast<unsigned>(v3 < tau_b && j1 < n && j1 != qb_row && qb_row < n) << (4 * nt + 3);
-      *reinterpret_cast<float2*>(dt + g * kTileStride + col) = make_float2(v0, v1);
-      *reinterpret_cast<float2*>(dt + (g + 8) * kTileStride + col) = make_float2(v2, v3);
+      const bool f0 = v0 < tau_a && j0 < n && j0 != qa_row && qa_row < n;
+      const bool f1 = v1 < tau_a && j1 < n && j1 != qa_row && qa_row < n;
+      const bool f2 = v2 < tau_b && j0 < n && j0 != qb_row && qb_row < n;
+      const bool f3 = v3 < tau_b && j1 < n && j1 != qb_row && qb_row < n;
+      fa |= (static_cast<unsigned>(f0) | (static_cast<unsigned>(f1) << 1)) << (2 * nt);
+      fb |= (static_cast<unsigned>(f2) | (static_cast<unsigned>(f3) << 1)) << (2 * nt);
+      if (f0 | f1) *reinterpret_cast<float2*>(dt + g * kTileStride + col) = make_float2(v0, v1);
+      if (f2 | f3) *reinterpret_cast<float2*>(dt + (g + 8) * kTileStride + col) = make_float2(v2, v3);
     }
+    fmask[g * 4 + tig] = fa;
+    fmask[(g + 8) * 4 + tig] = fb;
     __syncwarp();
-    // insert the flagged values, one at a time, the whole warp together
-    for (;;) {
-      const unsigned who = __ballot_sync(0xffffffffu, flags != 0u);
-      if (who == 0u) break;
-      const int src = __ffs(who) - 1;
-      const unsigned sf = __shfl_sync(0xffffffffu, flags, src);
-      const int b = __ffs(sf) - 1;
-      if (lane == src) flags &= flags - 1u;
-      const int sg = src >> 2, stig = src & 3, nt = b >> 2, k = b & 3;
-      const int row = (k & 2) ? sg + 8 : sg;
-      const int col = nt * 8 + 2 * stig + (k & 1);
-      const float v = dt[row * kTileStride + col];
+    // the owner of each heap inserts its flagged values: 16 bits per quad lane,
+    // quad lanes 2 h and 2 h + 1 feed heap (r, h)
+    unsigned m = fmask[r * 4 + 2 * h] | (fmask[r * 4 + 2 * h + 1] << 16);
+    while (m != 0u) {
+      const int b = __ffs(m) - 1;
+      m &= m - 1u;
+      const int qt = 2 * h + (b >> 4), bb = b & 15;
+      const int col = (bb >> 1) * 8 + 2 * qt + (bb & 1);
+      const float v = dt[r * kTileStride + col];
+      if (!(v < tau)) continue;
       const int j = t0 + col;
-      const int cnt = lcnt[row];
-      if (!(v < ltau[row])) continue;  // the threshold fell since the value was flagged
-      float* rv = lv + row * kp;
-      int* rj = lj + row * kp;
-      int below = 0;
-#pragma unroll
-      for (int t = 0; t < kMaxPer; ++t) {
-        const int e = lane + 32 * t;
-        if (e < cnt && rv[e] <= v) ++below;
-      }
-      const int pos = __reduce_add_sync(0xffffffffu, below);
-      const int last = min(cnt, kp - 1);  // entries [pos, last) move one place up
-      float mv[kMaxPer];
-      int mj[kMaxPer];
-#pragma unroll
-      for (int t = 0; t < kMaxPer; ++t) {
-        const int e = lane + 32 * t;
-        if (e >= pos && e < last) {
-          mv[t] = rv[e];
-          mj[t] = rj[e];
+      if (cnt < kp) {
+        // push: sift up
+        int c = cnt++;
+        while (c > 0) {
+          const int p = (c - 1) >> 1;
+          const float pv = hv[p * 32 + lane];
+          if (!(pv < v)) break;
+          hv[c * 32 + lane] = pv;
+          hj[c * 32 + lane] = hj[p * 32 + lane];
+          c = p;
         }
-      }
-      __syncwarp();
-#pragma unroll
-      for (int t = 0; t < kMaxPer; ++t) {
-        const int e = lane + 32 * t;
-        if (e >= pos && e < last) {
-          rv[e + 1] = mv[t];
-          rj[e + 1] = mj[t];
+        hv[c * 32 + lane] = v;
+        hj[c * 32 + lane] = j;
+        if (cnt == kp) tau = hv[lane];
+      } else {
+        // replace the maximum: sift down
+        int c = 0;
+        for (;;) {
+          const int l = 2 * c + 1;
+          if (l >= kp) break;
+          int big = l;
+          float bv = hv[l * 32 + lane];
+          if (l + 1 < kp) {
+            const float rv = hv[(l + 1) * 32 + lane];
+            if (rv > bv) {
+              big = l + 1;
+              bv = rv;
+            }
+          }
+          if (!(bv > v)) break;
+          hv[c * 32 + lane] = bv;
+          hj[c * 32 + lane] = hj[big * 32 + lane];
+          c = big;
         }
+        hv[c * 32 + lane] = v;
+        hj[c * 32 + lane] = j;
+        tau = hv[lane];
       }
-      __syncwarp();
-      if (lane == 0) {
-        rv[pos] = v;
-        rj[pos] = j;
-        const int nc = min(cnt + 1, kp);
-        lcnt[row] = nc;
-        if (nc == kp) ltau[row] = rv[kp - 1];
-      }
-      __syncwarp();
     }
+    htau[lane] = tau;
     __syncthreads();
   }
-  // lists out; the bound is the final threshold (+inf while a list is short)
-  for (int r = 0; r < 16; ++r) {
-    const int q = q0 + r;
-    if (q >= n) break;
-    const int cnt = lcnt[r];
-    for (int e = lane; e < kp; e += 32) A.cand[static_cast<size_t>(q) * kp + e] = e < cnt ? lj[r * kp + e] : -1;
-    if (lane == 0) A.bound[q] = cnt == kp ? ltau[r] : INFINITY;
+  // heaps out; the bound is the smaller final threshold of the row's two heaps
+  const float mine = cnt == kp ? tau : INFINITY;
+  const float other = __shfl_xor_sync(0xffffffffu, mine, 16);
+  if (myq < n) {
+    int* out = A.cand + static_cast<size_t>(myq) * 2 * kp + h * kp;
+    for (int e = 0; e < kp; ++e) out[e] = e < cnt ? hj[e * 32 + lane] : -1;
+    if (h == 0) A.bound[myq] = fminf(mine, other);
   }
 }
 
-// One warp per query: canonical distances of the kp candidates, the K
+// One warp per query: canonical distances of the 2 kp candidates, the K
 // smallest by (distance, index), the certificate e_K < B - delta (every row
 // goes to the fallback list when the data hold a non-finite value).
 __global__ void tc_rerank_kernel(const float* __restrict__ x, int n, int d, int K, int kp,
@@ -309,7 +312,7 @@ __global__ void tc_rerank_kernel(const float* __restrict__ x, int n, int d, int 
                                  const float* __restrict__ nrm, const unsigned* __restrict__ nrm_max,
                                  const int* __restrict__ nonfinite, float crel, int* __restrict__ idx,
                                  float* __restrict__ dist, int* __restrict__ fb_rows, int* __restrict__ fb_count) {
-  constexpr int kPer = kMaxPer;  // candidates per lane (kp <= 128)
+  constexpr int kPer = kMaxPer;  // candidates per lane (2 kp <= 256)
   const int lane = threadIdx.x & 31;
   const int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (q >= n) return;
@@ -317,7 +320,7 @@ __global__ void tc_rerank_kernel(const float* __restrict__ x, int n, int d, int 
     if (lane == 0) fb_rows[atomicAdd(fb_count, 1)] = q;
     return;
   }
-  const int m = kp;
+  const int m = 2 * kp;
   const float* xq = x + static_cast<size_t>(q) * d;
   // (distance bits, row): canonical distances are >= 0, so their bit
   // patterns order like the values and the keys order by (distance, row)
@@ -375,7 +378,7 @@ __global__ void tc_rerank_kernel(const float* __restrict__ x, int n, int d, int 
 
 bool knn_tc_supported(int n, int d, int K) {
   const int kp = (K + 16 + 15) / 16 * 16;
-  return d >= 1 && d <= 16 * kTcMaxKs && K >= 1 && kp <= 32 * kMaxPer && n > 2 * kp + kTcN;
+  return d >= 1 && d <= 16 * kTcMaxKs && K >= 1 && 2 * kp <= 32 * kMaxPer && n > 2 * kp + kTcN;
 }
 
 namespace {
@@ -397,7 +400,7 @@ TcLayout tc_layout(int n, int d, int K, int segments) {
   L.o_xl = o; o = al(o + static_cast<size_t>(n) * L.dp * 2);
   L.o_nrm = o; o = al(o + static_cast<size_t>(n) * 4);
   L.o_flags = o; o = al(o + 16);  // nrm_max, nonfinite, fb_count
-  L.o_cand = o; o = al(o + static_cast<size_t>(n) * L.kp * 4);
+  L.o_cand = o; o = al(o + static_cast<size_t>(n) * 2 * L.kp * 4);
   L.o_bound = o; o = al(o + static_cast<size_t>(n) * 4);
   L.o_fb = o; o = al(o + static_cast<size_t>(n) * 4);
   L.o_brute = o; o = al(o + knn_bruteforce_scratch(n, K, segments));
