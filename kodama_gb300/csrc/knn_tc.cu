@@ -7,22 +7,24 @@
 //  1. candidates: every row is split once into bfloat16 hi + lo parts
 //     (x = hi + lo + r, |r| <= 2^-16 |x|); a warp computes the approximate
 //     distances a = |q|^2 + |c|^2 - 2 (hi.hi + hi.lo + lo.hi) of 16 queries
-//     to a 64-row candidate tile with mma.sync (bf16 in, f32 accumulate);
-//     every query keeps the kp smallest approximate distances of each half
-//     of its columns in two max-heaps, one per lane (lanes r and r + 16 own
-//     query row r).  The lanes holding the accumulator fragments flag the
-//     values below their heap's threshold and publish per-row masks; each
-//     owner lane then inserts only its flagged values, so the insertions of
-//     the 32 heaps run side by side.  Each CTA walks the candidate tiles in
-//     a scattered order, so data sorted by cluster does not turn every value
-//     of a query's own cluster into an insertion;
-//  2. re-rank: one warp per query computes the canonical distances of its
-//     2 kp candidates and takes the K smallest by (distance, index);
-//  3. certificate: every row left out of a query's heaps has a >= B, the
-//     smaller final heap threshold; with |a - e| <= delta for every row (delta from
-//     the error bound below), e_K < B - delta proves that no excluded row
-//     can enter the top K or tie with it.  Rows whose certificate fails are
-//     listed and recomputed by the brute-force kernels (knn.cu).
+//     to a 64-row candidate tile with mma.sync (bf16 in, f32 accumulate).
+//     The candidate tiles are dealt to S segments (grid.y) in a scattered
+//     order; per segment every query keeps the kp smallest approximate
+//     distances of each half of its columns in two max-heaps, one per lane
+//     (lanes r and r + 16 own query row r).  The lanes holding the
+//     accumulator fragments flag the values below their heap's threshold and
+//     publish per-row masks; each owner lane inserts only its flagged
+//     values, so the 32 heaps of a warp fill side by side;
+//  2. re-rank: one warp per query takes A_K, the K-th smallest approximate
+//     distance over its heaps, computes the canonical distances of the
+//     candidates with a <= A_K + 2 delta, and keeps the K smallest by
+//     (distance, index);
+//  3. certificate: every row left out of the heaps has a >= B, the smallest
+//     final heap threshold.  A row of the true top K (ties by index
+//     included) has e <= e_K <= A_K + delta, hence a <= A_K + 2 delta, so
+//     B > A_K + 2 delta proves it was kept and re-ranked.  Rows whose
+//     certificate fails are listed and recomputed by the brute-force kernels
+//     (knn.cu).  delta bounds |a - e| for every row (below).
 //
 // Error bound (u = 2^-24): with D the true squared distance and e its
 // canonical value, |e - D| <= (d + 4) u D <= 2 (d + 4) u (|q|^2 + |c|^2);
@@ -108,13 +110,15 @@ struct TcArgs {
   const uint16_t* xh;   // n x dp, permuted 16-blocks
   const uint16_t* xl;
   const float* nrm;     // n
-  int n, dp, kp;
+  int n, dp, kp, segs;
   int row_words;        // 32-bit words per candidate row in shared memory (= 8 mod 16)
-  int* cand;            // n x 2 kp candidate rows (-1 = none)
-  float* bound;         // n: the smaller final heap threshold (+inf = nothing excluded)
+  int* cand;            // n x segs x 2 x kp candidate rows (-1 = none)
+  float* cand_a;        // their approximate distances
+  float* bound;         // n x segs: the smaller final heap threshold (+inf = nothing excluded)
 };
 
-constexpr int kMaxPer = 8;  // re-rank candidates per lane (2 kp <= 256)
+constexpr int kMaxPer = 8;   // re-rank candidates per lane (segs x 2 x kp <= 256)
+constexpr int kMaxLoads = 4; // 16-byte tile chunks per thread (kTcN x dp / 8 / 128 <= 4)
 
 // Shared memory: 2 x (hi, lo) candidate tiles, 2 x tile norms, per warp a
 // 16 x kTileStride distance tile, 16 x 4 flag masks, 32 thresholds and 32
@@ -128,6 +132,7 @@ __global__ void __launch_bounds__(32 * kTcWarps) tc_candidates_kernel(TcArgs A) 
   extern __shared__ __align__(16) unsigned char smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
   const int n = A.n, dp = A.dp, kp = A.kp, rw = A.row_words, ksn = dp >> 4;
+  const int seg = blockIdx.y, segs = A.segs;
   uint32_t* cbuf = reinterpret_cast<uint32_t*>(smem);  // [buf][hi/lo][kTcN][rw]
   float* cnb = reinterpret_cast<float*>(cbuf + 2 * 2 * kTcN * rw);  // [buf][kTcN]
   float* dt = cnb + 2 * kTcN + warp * (16 * kTileStride + 64 + 32 + 32 * kp * 2);  // [16][kTileStride]
@@ -163,43 +168,68 @@ __global__ void __launch_bounds__(32 * kTcWarps) tc_candidates_kernel(TcArgs A) 
   const int heap_a = g + 16 * (tig >> 1), heap_b = heap_a + 8;
   int cnt = 0;
   float tau = INFINITY;
+
+  // this thread's 16-byte chunks of a tile (the same every tile): smem word
+  // offset of the hi chunk and element offset inside the tile's rows
+  const int chunks = dp >> 3;
+  int ld_smem[kMaxLoads], ld_row[kMaxLoads], ld_col[kMaxLoads], nld = 0;
+#pragma unroll
+  for (int t = 0; t < kMaxLoads; ++t) {
+    const int e = threadIdx.x + t * 32 * kTcWarps;
+    ld_row[t] = 0;
+    ld_col[t] = 0;
+    ld_smem[t] = 0;
+    if (e < kTcN * chunks) {
+      const int c = e / chunks, ch = e - c * chunks;
+      ld_row[t] = c;
+      ld_col[t] = ch * 8;
+      ld_smem[t] = c * rw + ch * 4;
+      nld = t + 1;
+    }
+  }
   __syncwarp();
 
-  // scattered tile order: tile t is visited at step (first + step * stride) mod
-  // ntiles, stride coprime to ntiles (1000003 is a prime above any tile count)
+  // scattered tile order: the tile at step k is (first + k * stride) mod ntiles,
+  // stride coprime to ntiles (1000003 is a prime above any tile count); this
+  // segment takes the steps seg, seg + segs, ...
   const int ntiles = (n + kTcN - 1) / kTcN;
   const int stride = static_cast<int>(1000003ull % static_cast<unsigned long long>(ntiles));
-  const int first = static_cast<int>((static_cast<unsigned long long>(blockIdx.x) * 7919ull) % ntiles);
-  auto tile_at = [&](int step) {
-    return static_cast<int>((static_cast<unsigned long long>(first) +
-                             static_cast<unsigned long long>(step) * stride) % ntiles) * kTcN;
-  };
+  const int jump = static_cast<int>((static_cast<unsigned long long>(stride) * segs) % ntiles);
+  const int first = static_cast<int>((static_cast<unsigned long long>(blockIdx.x) * 7919ull +
+                                      static_cast<unsigned long long>(seg) * stride) % ntiles);
+  const int nsteps = ntiles > seg ? (ntiles - seg + segs - 1) / segs : 0;
 
-  auto load_tile = [&](int buf, int base) {
-    const int chunks = dp >> 3;  // 16-byte chunks per row
-    for (int e = threadIdx.x; e < kTcN * chunks; e += 32 * kTcWarps) {
-      const int c = e / chunks, ch = e - c * chunks;
-      const int row = base + c;
-      uint32_t* dh = cbuf + ((buf * 2 + 0) * kTcN + c) * rw + ch * 4;
-      uint32_t* dl = cbuf + ((buf * 2 + 1) * kTcN + c) * rw + ch * 4;
-      if (row < n) {
-        cp_async16(dh, A.xh + static_cast<size_t>(row) * dp + ch * 8);
-        cp_async16(dl, A.xl + static_cast<size_t>(row) * dp + ch * 8);
-      } else {
-        *reinterpret_cast<uint4*>(dh) = make_uint4(0u, 0u, 0u, 0u);
-        *reinterpret_cast<uint4*>(dl) = make_uint4(0u, 0u, 0u, 0u);
+  auto load_tile = [&](int buf, int tile) {
+    const int base = tile * kTcN;
+    uint32_t* dh = cbuf + (buf * 2 + 0) * kTcN * rw;
+    uint32_t* dl = cbuf + (buf * 2 + 1) * kTcN * rw;
+#pragma unroll
+    for (int t = 0; t < kMaxLoads; ++t) {
+      if (t < nld) {
+        const int row = base + ld_row[t];
+        if (row < n) {
+          const size_t src = static_cast<size_t>(row) * dp + ld_col[t];
+          cp_async16(dh + ld_smem[t], A.xh + src);
+          cp_async16(dl + ld_smem[t], A.xl + src);
+        } else {
+          *reinterpret_cast<uint4*>(dh + ld_smem[t]) = make_uint4(0u, 0u, 0u, 0u);
+          *reinterpret_cast<uint4*>(dl + ld_smem[t]) = make_uint4(0u, 0u, 0u, 0u);
+        }
       }
     }
     for (int c = threadIdx.x; c < kTcN; c += 32 * kTcWarps) cnb[buf * kTcN + c] = base + c < n ? A.nrm[base + c] : 0.0f;
     cp_async_commit();
   };
 
-  load_tile(0, tile_at(0));
-  for (int step = 0; step < ntiles; ++step) {
+  int tile = first;
+  if (nsteps > 0) load_tile(0, tile);
+  for (int step = 0; step < nsteps; ++step) {
     const int buf = step & 1;
-    const int t0 = tile_at(step);
-    if (step + 1 < ntiles) {
-      load_tile(buf ^ 1, tile_at(step + 1));
+    const int t0 = tile * kTcN;
+    int next = tile + jump;
+    if (next >= ntiles) next -= ntiles;
+    if (step + 1 < nsteps) {
+      load_tile(buf ^ 1, next);
       cp_async_wait<1>();
     } else {
       cp_async_wait<0>();
@@ -208,6 +238,9 @@ __global__ void __launch_bounds__(32 * kTcWarps) tc_candidates_kernel(TcArgs A) 
     const uint32_t* th = cbuf + (buf * 2 + 0) * kTcN * rw;
     const uint32_t* tl = cbuf + (buf * 2 + 1) * kTcN * rw;
     const float* cn = cnb + buf * kTcN;
+    // only the last tile and the tiles holding this warp's queries need the
+    // column checks (past the end, the query itself)
+    const bool edge = t0 + kTcN > n || (t0 < q0 + 16 && q0 < t0 + kTcN) || q0 + 16 > n;
     const float tau_a = htau[heap_a], tau_b = htau[heap_b];
     unsigned fa = 0u, fb = 0u;  // bit 2 nt + c: column nt * 8 + 2 tig + c of rows g / g + 8
 #pragma unroll
@@ -228,11 +261,14 @@ __global__ void __launch_bounds__(32 * kTcWarps) tc_candidates_kernel(TcArgs A) 
       const float c0 = cn[col], c1 = cn[col + 1];
       const float v0 = nq_g + c0 - 2.0f * acc[0], v1 = nq_g + c1 - 2.0f * acc[1];
       const float v2 = nq_g8 + c0 - 2.0f * acc[2], v3 = nq_g8 + c1 - 2.0f * acc[3];
-      const int j0 = t0 + col, j1 = j0 + 1;
-      const bool f0 = v0 < tau_a && j0 < n && j0 != qa_row && qa_row < n;
-      const bool f1 = v1 < tau_a && j1 < n && j1 != qa_row && qa_row < n;
-      const bool f2 = v2 < tau_b && j0 < n && j0 != qb_row && qb_row < n;
-      const bool f3 = v3 < tau_b && j1 < n && j1 != qb_row && qb_row < n;
+      bool f0 = v0 < tau_a, f1 = v1 < tau_a, f2 = v2 < tau_b, f3 = v3 < tau_b;
+      if (edge) {
+        const int j0 = t0 + col, j1 = j0 + 1;
+        f0 = f0 && j0 < n && j0 != qa_row && qa_row < n;
+        f1 = f1 && j1 < n && j1 != qa_row && qa_row < n;
+        f2 = f2 && j0 < n && j0 != qb_row && qb_row < n;
+        f3 = f3 && j1 < n && j1 != qb_row && qb_row < n;
+      }
       fa |= (static_cast<unsigned>(f0) | (static_cast<unsigned>(f1) << 1)) << (2 * nt);
       fb |= (static_cast<unsigned>(f2) | (static_cast<unsigned>(f3) << 1)) << (2 * nt);
       if (f0 | f1) *reinterpret_cast<float2*>(dt + g * kTileStride + col) = make_float2(v0, v1);
@@ -292,27 +328,39 @@ __global__ void __launch_bounds__(32 * kTcWarps) tc_candidates_kernel(TcArgs A) 
       }
     }
     htau[lane] = tau;
+    tile = next;
     __syncthreads();
   }
   // heaps out; the bound is the smaller final threshold of the row's two heaps
   const float mine = cnt == kp ? tau : INFINITY;
   const float other = __shfl_xor_sync(0xffffffffu, mine, 16);
   if (myq < n) {
-    int* out = A.cand + static_cast<size_t>(myq) * 2 * kp + h * kp;
-    for (int e = 0; e < kp; ++e) out[e] = e < cnt ? hj[e * 32 + lane] : -1;
-    if (h == 0) A.bound[myq] = fminf(mine, other);
+    const size_t base = ((static_cast<size_t>(myq) * segs + seg) * 2 + h) * kp;
+    for (int e = 0; e < kp; ++e) {
+      A.cand[base + e] = e < cnt ? hj[e * 32 + lane] : -1;
+      A.cand_a[base + e] = e < cnt ? hv[e * 32 + lane] : INFINITY;
+    }
+    if (h == 0) A.bound[static_cast<size_t>(myq) * segs + seg] = fminf(mine, other);
   }
 }
 
-// One warp per query: canonical distances of the 2 kp candidates, the K
-// smallest by (distance, index), the certificate e_K < B - delta (every row
-// goes to the fallback list when the data hold a non-finite value).
-__global__ void tc_rerank_kernel(const float* __restrict__ x, int n, int d, int K, int kp,
-                                 const int* __restrict__ cand, const float* __restrict__ bound,
-                                 const float* __restrict__ nrm, const unsigned* __restrict__ nrm_max,
-                                 const int* __restrict__ nonfinite, float crel, int* __restrict__ idx,
-                                 float* __restrict__ dist, int* __restrict__ fb_rows, int* __restrict__ fb_count) {
-  constexpr int kPer = kMaxPer;  // candidates per lane (2 kp <= 256)
+// order-preserving image of a float as an unsigned
+__device__ __forceinline__ unsigned ord_float(float v) {
+  const unsigned u = __float_as_uint(v);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+// One warp per query: A_K (the K-th smallest approximate distance of its
+// m = segs x 2 x kp candidates), canonical distances of the candidates with
+// a <= A_K + 2 delta, the K smallest of those by (distance, index), and the
+// certificate B > A_K + 2 delta (every row goes to the fallback list when the
+// data hold a non-finite value).
+__global__ void tc_rerank_kernel(const float* __restrict__ x, int n, int d, int K, int m, int segs,
+                                 const int* __restrict__ cand, const float* __restrict__ cand_a,
+                                 const float* __restrict__ bound, const float* __restrict__ nrm,
+                                 const unsigned* __restrict__ nrm_max, const int* __restrict__ nonfinite,
+                                 float crel, int* __restrict__ idx, float* __restrict__ dist,
+                                 int* __restrict__ fb_rows, int* __restrict__ fb_count) {
   const int lane = threadIdx.x & 31;
   const int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (q >= n) return;
@@ -320,88 +368,141 @@ __global__ void tc_rerank_kernel(const float* __restrict__ x, int n, int d, int 
     if (lane == 0) fb_rows[atomicAdd(fb_count, 1)] = q;
     return;
   }
-  const int m = 2 * kp;
-  const float* xq = x + static_cast<size_t>(q) * d;
-  // (distance bits, row): canonical distances are >= 0, so their bit
-  // patterns order like the values and the keys order by (distance, row)
-  unsigned long long key[kPer];
+  float av[kMaxPer];
+  int jv[kMaxPer];
+  unsigned long long key[kMaxPer];
 #pragma unroll
-  for (int t = 0; t < kPer; ++t) {
+  for (int t = 0; t < kMaxPer; ++t) {
     const int e = lane + 32 * t;
-    key[t] = ~0ull;
+    av[t] = INFINITY;
+    jv[t] = -1;
     if (e < m) {
       const int j = cand[static_cast<size_t>(q) * m + e];
       if (j >= 0) {
-        const float* xj = x + static_cast<size_t>(j) * d;
-        float a = 0.0f;
-        for (int k = 0; k < d; ++k) {
-          const float diff = __fsub_rn(xq[k], xj[k]);
-          a = __fadd_rn(a, __fmul_rn(diff, diff));
-        }
-        key[t] = (static_cast<unsigned long long>(__float_as_uint(a)) << 32) | static_cast<unsigned>(j);
+        jv[t] = j;
+        av[t] = cand_a[static_cast<size_t>(q) * m + e];
       }
     }
   }
-  float eK = INFINITY;
+  float thr = INFINITY;
+  {
+    // A_K: the approximate distance of the K-th smallest (a, row) key
+    unsigned long long k2[kMaxPer];
+#pragma unroll
+    for (int t = 0; t < kMaxPer; ++t)
+      k2[t] = jv[t] >= 0 ? (static_cast<unsigned long long>(ord_float(av[t])) << 32) | static_cast<unsigned>(jv[t])
+                         : ~0ull;
+    unsigned long long kth = ~0ull;
+    for (int o = 0; o < K; ++o) {
+      unsigned long long best = k2[0];
+#pragma unroll
+      for (int t = 1; t < kMaxPer; ++t) best = k2[t] < best ? k2[t] : best;
+#pragma unroll
+      for (int s = 16; s > 0; s >>= 1) {
+        const unsigned long long other = __shfl_xor_sync(0xffffffffu, best, s);
+        best = other < best ? other : best;
+      }
+      kth = best;
+      if (best == ~0ull) break;
+#pragma unroll
+      for (int t = 0; t < kMaxPer; ++t)
+        if (k2[t] == best) k2[t] = ~0ull;
+    }
+    if (kth != ~0ull) {
+      const unsigned o = static_cast<unsigned>(kth >> 32);
+      thr = __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
+    }
+  }
+  const float delta = (nrm[q] + __uint_as_float(*nrm_max)) * crel;
+  const float limit = thr + 2.0f * delta;
+  const float* xq = x + static_cast<size_t>(q) * d;
+  // canonical distances of the candidates within the limit
+#pragma unroll
+  for (int t = 0; t < kMaxPer; ++t) {
+    key[t] = ~0ull;
+    if (jv[t] >= 0 && av[t] <= limit) {
+      const float* xj = x + static_cast<size_t>(jv[t]) * d;
+      float a = 0.0f;
+      for (int k = 0; k < d; ++k) {
+        const float diff = __fsub_rn(xq[k], xj[k]);
+        a = __fadd_rn(a, __fmul_rn(diff, diff));
+      }
+      // canonical distances are >= 0: their bit patterns order like the values
+      key[t] = (static_cast<unsigned long long>(__float_as_uint(a)) << 32) | static_cast<unsigned>(jv[t]);
+    }
+  }
   for (int o = 0; o < K; ++o) {
     unsigned long long best = key[0];
 #pragma unroll
-    for (int t = 1; t < kPer; ++t) best = key[t] < best ? key[t] : best;
+    for (int t = 1; t < kMaxPer; ++t) best = key[t] < best ? key[t] : best;
 #pragma unroll
     for (int s = 16; s > 0; s >>= 1) {
       const unsigned long long other = __shfl_xor_sync(0xffffffffu, best, s);
       best = other < best ? other : best;
     }
 #pragma unroll
-    for (int t = 0; t < kPer; ++t)
+    for (int t = 0; t < kMaxPer; ++t)
       if (key[t] == best) key[t] = ~0ull;
     if (lane == 0) {
       const size_t out = static_cast<size_t>(q) * K + o;
       if (best == ~0ull) {
         idx[out] = -1;
         dist[out] = INFINITY;
-        eK = INFINITY;
       } else {
-        eK = __uint_as_float(static_cast<unsigned>(best >> 32));
         idx[out] = static_cast<int>(best & 0xffffffffu);
-        dist[out] = __fsqrt_rn(eK);
+        dist[out] = __fsqrt_rn(__uint_as_float(static_cast<unsigned>(best >> 32)));
       }
     }
   }
   if (lane == 0) {
-    const float delta = (nrm[q] + __uint_as_float(*nrm_max)) * crel;
-    if (!(eK < bound[q] - delta)) fb_rows[atomicAdd(fb_count, 1)] = q;
+    float B = INFINITY;
+    for (int s = 0; s < segs; ++s) B = fminf(B, bound[static_cast<size_t>(q) * segs + s]);
+    if (!(B > limit)) fb_rows[atomicAdd(fb_count, 1)] = q;
   }
 }
 
 }  // namespace
 
+// Segments and heap size: the K nearest rows spread over segs x 2 heaps,
+// each heap holding about twice its expected share plus a margin.
+void tc_shape(int K, int* segs, int* kp) {
+  *segs = K <= 40 ? 8 : 4;
+  const int share = (K + 2 * *segs - 1) / (2 * *segs);
+  int k = (2 * share + 8 + 7) / 8 * 8;
+  k = k < 16 ? 16 : k;
+  const int cap = kMaxPer * 32 / (2 * *segs);
+  *kp = k > cap ? cap : k;
+}
+
 bool knn_tc_supported(int n, int d, int K) {
-  const int kp = (K + 16 + 15) / 16 * 16;
-  return d >= 1 && d <= 16 * kTcMaxKs && K >= 1 && 2 * kp <= 32 * kMaxPer && n > 2 * kp + kTcN;
+  int segs = 0, kp = 0;
+  tc_shape(K, &segs, &kp);
+  return d >= 1 && d <= 16 * kTcMaxKs && K >= 1 && K <= 96 && n > 2 * kp + kTcN;
 }
 
 namespace {
 
 struct TcLayout {
-  int dp, kp, rw;
-  size_t o_xh, o_xl, o_nrm, o_flags, o_cand, o_bound, o_fb, o_brute, total;
+  int dp, kp, segs, rw;
+  size_t o_xh, o_xl, o_nrm, o_flags, o_cand, o_canda, o_bound, o_fb, o_brute, total;
 };
 
 TcLayout tc_layout(int n, int d, int K, int segments) {
   TcLayout L{};
   L.dp = (d + 15) / 16 * 16;
-  L.kp = (K + 16 + 15) / 16 * 16;
+  tc_shape(K, &L.segs, &L.kp);
   const int half = L.dp / 2;
   L.rw = (half % 16 == 8) ? half : half + 8;
+  const size_t m = static_cast<size_t>(L.segs) * 2 * L.kp;
   auto al = [](size_t v) { return (v + 255) / 256 * 256; };
   size_t o = 0;
   L.o_xh = o; o = al(o + static_cast<size_t>(n) * L.dp * 2);
   L.o_xl = o; o = al(o + static_cast<size_t>(n) * L.dp * 2);
   L.o_nrm = o; o = al(o + static_cast<size_t>(n) * 4);
   L.o_flags = o; o = al(o + 16);  // nrm_max, nonfinite, fb_count
-  L.o_cand = o; o = al(o + static_cast<size_t>(n) * 2 * L.kp * 4);
-  L.o_bound = o; o = al(o + static_cast<size_t>(n) * 4);
+  L.o_cand = o; o = al(o + static_cast<size_t>(n) * m * 4);
+  L.o_canda = o; o = al(o + static_cast<size_t>(n) * m * 4);
+  L.o_bound = o; o = al(o + static_cast<size_t>(n) * L.segs * 4);
   L.o_fb = o; o = al(o + static_cast<size_t>(n) * 4);
   L.o_brute = o; o = al(o + knn_bruteforce_scratch(n, K, segments));
   L.total = o;
@@ -421,6 +522,7 @@ int knn_tc_graph(const float* x, int n, int d, int K, int segments, void* scratc
   float* nrm = reinterpret_cast<float*>(b + L.o_nrm);
   unsigned* flags = reinterpret_cast<unsigned*>(b + L.o_flags);  // [0] nrm_max bits, [1] nonfinite, [2] fallback count
   int* cand = reinterpret_cast<int*>(b + L.o_cand);
+  float* cand_a = reinterpret_cast<float*>(b + L.o_canda);
   float* bound = reinterpret_cast<float*>(b + L.o_bound);
   int* fb = reinterpret_cast<int*>(b + L.o_fb);
   cudaError_t e = cudaMemsetAsync(flags, 0, 16, st);
@@ -434,16 +536,18 @@ int knn_tc_graph(const float* x, int n, int d, int K, int segments, void* scratc
   A.n = n;
   A.dp = L.dp;
   A.kp = L.kp;
+  A.segs = L.segs;
   A.row_words = L.rw;
   A.cand = cand;
+  A.cand_a = cand_a;
   A.bound = bound;
   const size_t smem = tc_smem_bytes(L.rw, L.kp);
   e = cudaFuncSetAttribute(tc_candidates_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   if (e != cudaSuccess) return static_cast<int>(e);
-  tc_candidates_kernel<<<(n + kTcQ - 1) / kTcQ, 32 * kTcWarps, smem, st>>>(A);
+  tc_candidates_kernel<<<dim3((n + kTcQ - 1) / kTcQ, L.segs), 32 * kTcWarps, smem, st>>>(A);
   const float crel = 1e-4f + 2e-6f * static_cast<float>(L.dp);
-  tc_rerank_kernel<<<(n + 3) / 4, 128, 0, st>>>(x, n, d, K, L.kp, cand, bound, nrm, flags,
-                                                 reinterpret_cast<const int*>(flags + 1), crel, idx, dist, fb,
+  tc_rerank_kernel<<<(n + 3) / 4, 128, 0, st>>>(x, n, d, K, L.segs * 2 * L.kp, L.segs, cand, cand_a, bound, nrm,
+                                                 flags, reinterpret_cast<const int*>(flags + 1), crel, idx, dist, fb,
                                                  reinterpret_cast<int*>(flags + 2));
   count_launch(3);
   e = cudaGetLastError();
