@@ -128,7 +128,7 @@ size_t tc_smem_bytes(int row_words, int kp) {
          kTcWarps * (16 * kTileStride * 4 + 64 * 4 + 32 * 4 + 32 * static_cast<size_t>(kp) * 8);
 }
 
-__global__ void __launch_bounds__(32 * kTcWarps) tc_candidates_kernel(TcArgs A) {
+__global__ void __launch_bounds__(32 * kTcWarps, 2) tc_candidates_kernel(TcArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
   const int n = A.n, dp = A.dp, kp = A.kp, rw = A.row_words, ksn = dp >> 4;
@@ -243,20 +243,27 @@ __global__ void __launch_bounds__(32 * kTcWarps) tc_candidates_kernel(TcArgs A) 
     const bool edge = t0 + kTcN > n || (t0 < q0 + 16 && q0 < t0 + kTcN) || q0 + 16 > n;
     const float tau_a = htau[heap_a], tau_b = htau[heap_b];
     unsigned fa = 0u, fb = 0u;  // bit 2 nt + c: column nt * 8 + 2 tig + c of rows g / g + 8
+    // eight independent accumulator chains (one per n-tile) hide the mma latency
+    float accs[8][4];
 #pragma unroll
-    for (int nt = 0; nt < 8; ++nt) {
-      float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    for (int nt = 0; nt < 8; ++nt) accs[nt][0] = accs[nt][1] = accs[nt][2] = accs[nt][3] = 0.0f;
 #pragma unroll
-      for (int ks = 0; ks < kTcMaxKs; ++ks) {
-        if (ks < ksn) {
+    for (int ks = 0; ks < kTcMaxKs; ++ks) {
+      if (ks < ksn) {
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) {
           const int off = (nt * 8 + g) * rw + ks * 8 + 2 * tig;
           const uint2 bh = *reinterpret_cast<const uint2*>(th + off);
           const uint2 bl = *reinterpret_cast<const uint2*>(tl + off);
-          mma16816(acc, ah[ks], bh);
-          mma16816(acc, ah[ks], bl);
-          mma16816(acc, al[ks], bh);
+          mma16816(accs[nt], ah[ks], bh);
+          mma16816(accs[nt], ah[ks], bl);
+          mma16816(accs[nt], al[ks], bh);
         }
       }
+    }
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+      const float* acc = accs[nt];
       const int col = nt * 8 + 2 * tig;
       const float c0 = cn[col], c1 = cn[col + 1];
       const float v0 = nq_g + c0 - 2.0f * acc[0], v1 = nq_g + c1 - 2.0f * acc[1];
