@@ -683,6 +683,29 @@ void validate_matrix_options(const kgb_matrix_options* o) {
 
 // The KODAMA.matrix path after the global graph (n x K zero-based, compacted,
 // distances finite >= 0) is resident on the device.
+// The bf16 hi / lo split of the data matrix, made once per call and shared
+// by the k-means runs that use the tensor-core assignment.
+struct TcSplit {
+  uint16_t* xh = nullptr;
+  uint16_t* xl = nullptr;
+  int dp = 0;
+};
+
+void tc_kmeans_inputs(Ctx& ctx, kgb::KMeansBatch& B, const float* d_x, int n, int d, TcSplit& split) {
+  if (!kgb::kmeans_tc_supported(d, B.k)) return;
+  if (split.xh == nullptr) {
+    split.dp = (d + 15) / 16 * 16;
+    split.xh = ctx.alloc<uint16_t>(static_cast<size_t>(n) * split.dp);
+    split.xl = ctx.alloc<uint16_t>(static_cast<size_t>(n) * split.dp);
+    ck_launch(kgb::bf16_split_rows(d_x, n, d, split.dp, split.xh, split.xl, ctx.stream()), "bf16 split");
+  }
+  B.xh = split.xh;
+  B.xl = split.xl;
+  B.dp = split.dp;
+  B.ch = ctx.alloc<uint16_t>(static_cast<size_t>(B.problems) * B.k * split.dp);
+  B.cl = ctx.alloc<uint16_t>(static_cast<size_t>(B.problems) * B.k * split.dp);
+}
+
 void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_gidx, float* d_gdist, int K,
                               const kgb_matrix_options* o, kgb_matrix_result* out, Clock& clk, int ev_start,
                               int ev_graph, std::future<std::vector<kgb::FoldPlan>>& folds_future) {
@@ -697,6 +720,7 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   const int knn_k = std::max(o->knn_k, 1);
   const int w = std::max(1, std::min(knn_k, K));
   const bool pls = o->classifier == 1;
+  TcSplit tc_split;
   if (o->classifier != 0 && o->classifier != 1) fail(KGB_EINVAL, "Unsupported KODAMA.matrix classifier.");
   if (!pls && w > 32) fail(KGB_EINVAL, "knn.k above 32 is not supported by the vote kernel");
   if (!pls && knn_k > kgb::kMaxProjectK) fail(KGB_EINVAL, "knn.k too large for the projection kernel");
@@ -735,6 +759,7 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     B.members = ctx.alloc<int>(n);
     B.offsets = ctx.alloc<int>(ck_atlas + 1);
     B.fscratch = ctx.alloc<float>(3 * ck_atlas + 1);
+    tc_kmeans_inputs(ctx, B, d_x, n, d, tc_split);
     ck_launch(kgb::kmeans_run(B, st), "atlas k-means");
   }
   const int ev_atlas = ctx.mark();
@@ -784,6 +809,7 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     B.members = ctx.alloc<int>(static_cast<size_t>(M) * L);
     B.offsets = ctx.alloc<int>(static_cast<size_t>(M) * (kk + 1));
     B.fscratch = ctx.alloc<float>(static_cast<size_t>(M) * (3 * kk + 1));
+    tc_kmeans_inputs(ctx, B, d_x, n, d, tc_split);
     ck_launch(kgb::kmeans_run(B, st), "landmark k-means");
   }
   // folds were planned on the host while the device worked

@@ -14,10 +14,13 @@
 //   max(0, size-1) with mt19937(1234) uniforms (:566-662).
 // Every product and sum uses explicit round-to-nearest intrinsics.
 #include "kmeans.cuh"
+#include "knn.cuh"
 #include "launch_count.cuh"
 
 #include <cuda_runtime.h>
 #include <math.h>
+
+#include <cmath>
 
 namespace kgb {
 
@@ -229,6 +232,7 @@ __global__ void assign_kernel(KMeansBatch B, int final_pass) {
     }
   }
   int* as = B.assign + static_cast<size_t>(p) * B.n;
+  bool moved = false;
 #pragma unroll
   for (int q = 0; q < kAssignRows; ++q) {
     if (!live[q]) continue;
@@ -237,8 +241,204 @@ __global__ void assign_kernel(KMeansBatch B, int final_pass) {
       B.labels[static_cast<size_t>(p) * B.n + r] = best[q] + 1;
     } else if (as[r] != best[q]) {
       as[r] = best[q];
-      atomicAdd(&B.changed[p], 1);
+      moved = true;
     }
+  }
+  // the reference only tests whether any assignment changed: one plain store
+  // per warp instead of an atomic per row (per-row atomics on one counter
+  // serialise in L2)
+  const unsigned any = __ballot_sync(__activemask(), moved);
+  if (any != 0u && (threadIdx.x & 31) == __ffs(__activemask()) - 1) B.changed[p] = 1;
+}
+
+// ---------------------------------------------------------------------------
+// Tensor-core assignment.  Approximate distances a_c = (|x|^2 + |c|^2) -
+// 2 dot_tc(x, c), where dot_tc is the bf16 hi + lo product (hi.hi + hi.lo +
+// lo.hi) accumulated in f32 by mma.sync and the norms are the exact ones of
+// the canonical formula; |a_c - dist_c| <= delta = (|x|^2 + max |c|^2) *
+// (1e-4 + 2e-6 dp) (the same bound as the kNN candidate search, knn_tc.cu).
+// The exact nearest centroid has a_c <= min a + 2 delta, so only those
+// centroids get the canonical x86-order distance; the winner among them
+// (ties to the lower cluster) is the canonical winner.  Non-finite values
+// fail no test and send every centroid to the exact distance.
+// ---------------------------------------------------------------------------
+constexpr int kTcAssignWarps = 4;
+
+__device__ __forceinline__ void mma_bf16_16816(float* c, const uint32_t* a, uint2 b) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b.x), "r"(b.y));
+}
+
+__device__ __forceinline__ int tc_row_words(int dp) {
+  const int half = dp / 2;
+  return (half % 16 == 8) ? half : half + 8;
+}
+
+size_t assign_tc_smem(int k, int d, int dp) {
+  const int kpad = (k + 7) / 8 * 8, d4 = (d + 3) & ~3;
+  const int half = dp / 2, rw = (half % 16 == 8) ? half : half + 8;
+  return sizeof(uint32_t) * 2 * kpad * rw + sizeof(float) * (static_cast<size_t>(k) * d4 + kpad + 1) +
+         sizeof(float) * kTcAssignWarps * 16 * (kpad + 1);
+}
+
+__global__ void __launch_bounds__(32 * kTcAssignWarps) assign_tc_kernel(KMeansBatch B, int final_pass) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int p = blockIdx.y;
+  if (!final_pass && !B.active[p]) return;
+  const int k = B.k, d = B.d, dp = B.dp, n = B.n;
+  const int kpad = (k + 7) / 8 * 8, d4 = (d + 3) & ~3, rw = tc_row_words(dp), ksn = dp >> 4;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
+  uint32_t* sch = reinterpret_cast<uint32_t*>(smraw);  // [kpad][rw]
+  uint32_t* scl = sch + kpad * rw;
+  float* scf = reinterpret_cast<float*>(scl + kpad * rw);  // [k][d4]
+  float* scn = scf + static_cast<size_t>(k) * d4;          // [kpad] + max
+  float* sa = scn + kpad + 1 + warp * 16 * (kpad + 1);     // this warp's [16][kpad + 1]
+  const uint16_t* gch = B.ch + static_cast<size_t>(p) * k * dp;
+  const uint16_t* gcl = B.cl + static_cast<size_t>(p) * k * dp;
+  const float* cent = B.cent + static_cast<size_t>(p) * k * d;
+  // centroids staged once per CTA (warps over centroids, lanes over words)
+  for (int c = warp; c < kpad; c += kTcAssignWarps) {
+    const uint32_t* h32 = reinterpret_cast<const uint32_t*>(gch + static_cast<size_t>(c) * dp);
+    const uint32_t* l32 = reinterpret_cast<const uint32_t*>(gcl + static_cast<size_t>(c) * dp);
+    for (int w = lane; w < (dp >> 1); w += 32) {
+      sch[c * rw + w] = c < k ? h32[w] : 0u;
+      scl[c * rw + w] = c < k ? l32[w] : 0u;
+    }
+    if (c < k)
+      for (int j = lane; j < d4; j += 32) scf[c * d4 + j] = j < d ? cent[static_cast<size_t>(c) * d + j] : 0.0f;
+  }
+  for (int c = threadIdx.x; c < kpad; c += blockDim.x)
+    scn[c] = c < k ? B.cnorm[static_cast<size_t>(p) * k + c] : 0.0f;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    float mx = 0.0f;
+    for (int c = lane; c < k; c += 32) mx = fmaxf(mx, scn[c]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(kFull, mx, o));
+    if (lane == 0) scn[kpad] = mx;
+  }
+  __syncthreads();
+  for (int rb = 0; rb < B.tc_blocks; ++rb) {
+    if ((blockIdx.x * B.tc_blocks + rb) * 16 * kTcAssignWarps >= n) break;
+    const int r0 = (blockIdx.x * B.tc_blocks + rb) * 16 * kTcAssignWarps + warp * 16;
+    auto global_row = [&](int i) {
+      const int ii = i < n ? i : n - 1;
+      return B.rows ? B.rows[static_cast<size_t>(p) * n + ii] : ii;
+    };
+    const int ga = global_row(r0 + g), gb = global_row(r0 + g + 8);
+    uint32_t ah[4][4], al[4][4];
+  #pragma unroll
+    for (int ks = 0; ks < 4; ++ks) {
+      uint2 pa = make_uint2(0u, 0u), pb = pa, qa = pa, qb = pa;
+      if (ks < ksn) {
+        pa = *reinterpret_cast<const uint2*>(B.xh + static_cast<size_t>(ga) * dp + ks * 16 + 4 * tig);
+        pb = *reinterpret_cast<const uint2*>(B.xh + static_cast<size_t>(gb) * dp + ks * 16 + 4 * tig);
+        qa = *reinterpret_cast<const uint2*>(B.xl + static_cast<size_t>(ga) * dp + ks * 16 + 4 * tig);
+        qb = *reinterpret_cast<const uint2*>(B.xl + static_cast<size_t>(gb) * dp + ks * 16 + 4 * tig);
+      }
+      ah[ks][0] = pa.x; ah[ks][2] = pa.y; ah[ks][1] = pb.x; ah[ks][3] = pb.y;
+      al[ks][0] = qa.x; al[ks][2] = qa.y; al[ks][1] = qb.x; al[ks][3] = qb.y;
+    }
+    const float pna = B.pnorm[ga], pnb = B.pnorm[gb];
+    // approximate distances, eight centroids per n-tile
+    for (int nt0 = 0; nt0 < kpad / 8; nt0 += 8) {
+      float acc[8][4];
+  #pragma unroll
+      for (int t = 0; t < 8; ++t) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.0f;
+  #pragma unroll
+      for (int ks = 0; ks < 4; ++ks) {
+        if (ks < ksn) {
+  #pragma unroll
+          for (int t = 0; t < 8; ++t) {
+            if (nt0 + t < kpad / 8) {
+              const int off = ((nt0 + t) * 8 + g) * rw + ks * 8 + 2 * tig;
+              const uint2 bh = *reinterpret_cast<const uint2*>(sch + off);
+              const uint2 bl = *reinterpret_cast<const uint2*>(scl + off);
+              mma_bf16_16816(acc[t], ah[ks], bh);
+              mma_bf16_16816(acc[t], ah[ks], bl);
+              mma_bf16_16816(acc[t], al[ks], bh);
+            }
+          }
+        }
+      }
+  #pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        if (nt0 + t < kpad / 8) {
+          const int c = (nt0 + t) * 8 + 2 * tig;
+          sa[g * (kpad + 1) + c] = __fsub_rn(fadd(pna, scn[c]), fmul(2.0f, acc[t][0]));
+          sa[g * (kpad + 1) + c + 1] = __fsub_rn(fadd(pna, scn[c + 1]), fmul(2.0f, acc[t][1]));
+          sa[(g + 8) * (kpad + 1) + c] = __fsub_rn(fadd(pnb, scn[c]), fmul(2.0f, acc[t][2]));
+          sa[(g + 8) * (kpad + 1) + c + 1] = __fsub_rn(fadd(pnb, scn[c + 1]), fmul(2.0f, acc[t][3]));
+        }
+      }
+    }
+    __syncwarp();
+    // exact distances of the centroids within min a + 2 delta: lanes r and
+    // r + 16 take row r, each half of its centroids (by parity)
+    {
+      const int r = lane & 15, half = lane >> 4;
+      const int i = r0 + r;
+      const bool valid = i < n;
+      const int grow = B.rows ? B.rows[static_cast<size_t>(p) * n + (valid ? i : n - 1)] : (valid ? i : n - 1);
+      const float pn = B.pnorm[grow];
+      const float* arow = sa + r * (kpad + 1);
+      float amin = INFINITY;
+      for (int c = half; c < k; c += 2) amin = fminf(amin, arow[c]);
+      amin = fminf(amin, __shfl_xor_sync(kFull, amin, 16));
+      const float thr = amin + 2.0f * fadd(pn, scn[kpad]) * B.tc_crel;
+      float xv[64];
+      const float* xr = B.x + static_cast<size_t>(grow) * d;
+#pragma unroll
+      for (int j = 0; j < 64; ++j) xv[j] = j < d ? xr[j] : 0.0f;
+      int best = k;
+      float bestd = INFINITY;
+      // each lane walks its own candidates; the lanes compute their dots
+      // together (one per lane per round), so the warp never runs a dot for
+      // a single lane
+      int cpos = half;
+      for (;;) {
+        while (cpos < k && arow[cpos] > thr) cpos += 2;
+        const bool have = cpos < k;
+        if (!__any_sync(kFull, have)) break;
+        const int c = have ? cpos : 0;
+        const float dt = dot_x86_reg<4>(xv, scf + static_cast<size_t>(c) * d4, d);
+        if (have) {
+          const float dist = __fsub_rn(fadd(pn, scn[c]), fmul(2.0f, dt));
+          if (dist < bestd || (dist == bestd && c < best)) {
+            bestd = dist;
+            best = c;
+          }
+          cpos += 2;
+        }
+      }
+      // the pair's winner: smaller distance, then smaller cluster (a NaN
+      // distance never wins, as in the full scan; an all-NaN row keeps 0)
+      const float od = __shfl_xor_sync(kFull, bestd, 16);
+      const int oc = __shfl_xor_sync(kFull, best, 16);
+      if (od < bestd || (od == bestd && oc < best)) {
+        bestd = od;
+        best = oc;
+      }
+      if (best >= k) best = 0;
+      bool moved = false;
+      if (valid && half == 0) {
+        if (final_pass) {
+          B.labels[static_cast<size_t>(p) * n + i] = best + 1;
+        } else {
+          int* as = B.assign + static_cast<size_t>(p) * n;
+          if (as[i] != best) {
+            as[i] = best;
+            moved = true;
+          }
+        }
+      }
+      // only whether any assignment changed matters: one store per warp
+      if (__ballot_sync(kFull, moved) != 0u && lane == 0) B.changed[p] = 1;
+    }
+    __syncwarp();
   }
 }
 
@@ -339,37 +539,99 @@ __global__ void __launch_bounds__(1024) sort_kernel(KMeansBatch B) {
   }
 }
 
-// Update step, part 2 (one warp per problem and cluster, lanes over
-// features): centroid sums in ascending row order, scaled by 1/size.
-__global__ void sums_kernel(KMeansBatch B) {
-  const int lane = threadIdx.x & 31;
-  const int gw = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int p = gw / B.k, c = gw % B.k;
+// Update step, part 2 (one CTA per problem and cluster): centroid sums in
+// ascending row order, scaled by 1/size.  A cluster can hold thousands of
+// rows (in high dimension one centroid often takes most of a mixture
+// component), and its features are sequential float chains, so the rows are
+// streamed through a ring of kSumStages chunks of kSumChunk rows in shared
+// memory with cp.async: every thread copies, the member ids of a chunk are
+// read one chunk ahead of its copies, and thread j adds feature j down each
+// landed chunk in row order.  Features go in blocks of kSumCols.
+constexpr int kSumChunk = 128;
+constexpr int kSumStages = 4;
+constexpr int kSumCols = 64;
+constexpr int kSumThreads = 256;
+
+size_t sums_smem(int d) {
+  const int dw = d < kSumCols ? d : kSumCols;
+  return sizeof(float) * kSumStages * kSumChunk * dw + sizeof(int) * kSumStages * kSumChunk;
+}
+
+__device__ __forceinline__ void cp_async4(float* smem, const float* gmem) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit_group() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait_groups() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
+}
+
+__global__ void __launch_bounds__(kSumThreads) sums_kernel(KMeansBatch B) {
+  extern __shared__ float sring[];
+  const int p = blockIdx.x / B.k, c = blockIdx.x % B.k;
   if (p >= B.problems || !B.active[p]) return;
   const int d = B.d;
   const int* mem = B.members + static_cast<size_t>(p) * B.n;
   const int* off = B.offsets + static_cast<size_t>(p) * (B.k + 1);
   const int b0 = off[c], b1 = off[c + 1];
   float* cent = B.cent + (static_cast<size_t>(p) * B.k + c) * d;
-  constexpr int kPref = 8;
-  for (int j0 = 0; j0 < d; j0 += 32) {
-    const int j = j0 + lane;
+  const int cnt = b1 - b0;
+  const float inv = cnt != 0 ? __fdiv_rn(1.0f, static_cast<float>(cnt)) : 0.0f;
+  const int nchunks = (cnt + kSumChunk - 1) / kSumChunk;
+  for (int jb = 0; jb < d; jb += kSumCols) {
+    const int dw = min(kSumCols, d - jb);
+    float* rows_s = sring;                                              // [stage][kSumChunk][dw]
+    int* ids_s = reinterpret_cast<int*>(sring + kSumStages * kSumChunk * dw);  // [stage][kSumChunk]
+    // stage the ids of the first chunks, then copy chunk i while the ids of
+    // chunk i + 1 are read
+    auto load_ids = [&](int ch) {
+      const int base = b0 + ch * kSumChunk;
+      int* ids = ids_s + (ch % kSumStages) * kSumChunk;
+      for (int r = threadIdx.x; r < kSumChunk; r += kSumThreads) ids[r] = base + r < b1 ? mem[base + r] : -1;
+    };
+    auto copy_rows = [&](int ch) {
+      const int* ids = ids_s + (ch % kSumStages) * kSumChunk;
+      float* dst = rows_s + (ch % kSumStages) * kSumChunk * dw;
+      const int m = min(kSumChunk, b1 - (b0 + ch * kSumChunk));
+      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+      for (int r = warp; r < m; r += kSumThreads / 32) {
+        const float* src = B.x + static_cast<size_t>(ids[r]) * d + jb;
+        for (int col = lane; col < dw; col += 32) cp_async4(dst + r * dw + col, src + col);
+      }
+    };
     float s = 0.0f;
-    for (int q = b0; q < b1; q += kPref) {
-      float v[kPref];
-#pragma unroll
-      for (int t = 0; t < kPref; ++t) {
-        const int qq = q + t;
-        v[t] = (qq < b1 && j < d) ? B.x[static_cast<size_t>(mem[qq]) * d + j] : 0.0f;
+    __syncthreads();
+    if (nchunks > 0) load_ids(0);
+    __syncthreads();
+    // prologue: copies of chunks 0 .. kSumStages-2 in flight
+    for (int ch = 0; ch < kSumStages - 1; ++ch) {
+      if (ch < nchunks) {
+        if (ch + 1 < nchunks) load_ids(ch + 1);
+        copy_rows(ch);
       }
-#pragma unroll
-      for (int t = 0; t < kPref; ++t) {
-        if (q + t < b1) s = fadd(s, v[t]);
-      }
+      cp_async_commit_group();
+      __syncthreads();
     }
-    const int cnt = b1 - b0;
-    if (cnt != 0) s = fmul(s, __fdiv_rn(1.0f, static_cast<float>(cnt)));
-    if (j < d) cent[j] = s;
+    for (int ch = 0; ch < nchunks; ++ch) {
+      // keep kSumStages - 1 chunks in flight: issue chunk ch + kSumStages - 1
+      const int nx = ch + kSumStages - 1;
+      if (nx < nchunks) {
+        if (nx + 1 < nchunks) load_ids(nx + 1);
+        copy_rows(nx);
+      }
+      cp_async_commit_group();
+      cp_async_wait_groups<kSumStages - 1>();
+      __syncthreads();
+      if (threadIdx.x < dw) {
+        const int m = min(kSumChunk, b1 - (b0 + ch * kSumChunk));
+        const float* sc = rows_s + (ch % kSumStages) * kSumChunk * dw + threadIdx.x;
+#pragma unroll 8
+        for (int r = 0; r < m; ++r) s = fadd(s, sc[r * dw]);
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x < dw) cent[jb + threadIdx.x] = cnt != 0 ? fmul(s, inv) : s;
   }
 }
 
@@ -429,6 +691,8 @@ __global__ void finalize_kernel(KMeansBatch B) {
 
 }  // namespace
 
+bool kmeans_tc_supported(int d, int k) { return d >= 1 && d <= 64 && k >= 1 && k <= 128; }
+
 size_t kmeans_sort_smem(int k) { return sizeof(int) * (33 * static_cast<size_t>(k) + 1); }
 
 int kmeans_row_norms(const float* x, int n, int d, float* out, cudaStream_t st) {
@@ -444,9 +708,39 @@ int kmeans_run(const KMeansBatch& B, cudaStream_t st) {
   const size_t sort_bytes = kmeans_sort_smem(B.k);
   const dim3 agrid((B.n + 128 * kAssignRows - 1) / (128 * kAssignRows), B.problems);
   const dim3 ngrid((B.k + 127) / 128, B.problems);
-  const int sum_warps = B.problems * B.k;
-  const int sum_blocks = (sum_warps + 7) / 8;
+  const size_t sum_bytes = sums_smem(B.d);
+  const bool tc = B.xh != nullptr && kmeans_tc_supported(B.d, B.k);
+  const size_t tc_bytes = tc ? assign_tc_smem(B.k, B.d, B.dp) : 0;
+  if (tc) cudaFuncSetAttribute(assign_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(tc_bytes));
+  // 64-row blocks per CTA: the centroids are staged once per CTA, but the grid
+  // keeps at least two CTAs per SM
+  KMeansBatch T = B;
+  {
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long blocks = static_cast<long long>((B.n + 16 * kTcAssignWarps - 1) / (16 * kTcAssignWarps)) * B.problems;
+    long long per = blocks / (2LL * sms);
+    T.tc_blocks = static_cast<int>(per < 1 ? 1 : (per > 8 ? 8 : per));
+    // |a - dist| <= (|x|^2 + max |c|^2) * tc_crel: both share RN(|x|^2 + |c|^2);
+    // 2 |dot_tc - dot_x86| <= 2 (3.1 * 2^-16 [the hi + lo split] +
+    // 3 dp * 2^-22 [f32 accumulation of 3 dp products, two ulps per add] +
+    // (d / 16 + 5) 2^-24 [the x86-order dot]) sum|x_i c_i|, with
+    // sum|x_i c_i| <= 0.51 (|x|^2 + |c|^2); the two final subtractions round
+    // values of at most 2.03 (|x|^2 + |c|^2) each
+    const double tc = 3.1 * std::ldexp(1.0, -16) + 3.0 * B.dp * std::ldexp(1.0, -22) +
+                      (B.d / 16 + 5) * std::ldexp(1.0, -24);
+    T.tc_crel = static_cast<float>(1.05 * (1.02 * tc + 4.1 * std::ldexp(1.0, -24)) + 1e-7);
+  }
+  const int rows_per_cta = 16 * kTcAssignWarps * T.tc_blocks;
+  const dim3 tgrid((B.n + rows_per_cta - 1) / rows_per_cta, B.problems);
   auto launch_assign = [&](int final_pass) {
+    if (tc) {
+      // the centroids' bf16 split (its own launch is counted there)
+      bf16_split_rows(B.cent, B.problems * B.k, B.d, B.dp, B.ch, B.cl, st);
+      assign_tc_kernel<<<tgrid, 32 * kTcAssignWarps, tc_bytes, st>>>(T, final_pass);
+      return;
+    }
     if (B.d <= 16) assign_kernel<1><<<agrid, 128, cs_bytes, st>>>(B, final_pass);
     else if (B.d <= 32) assign_kernel<2><<<agrid, 128, cs_bytes, st>>>(B, final_pass);
     else if (B.d <= 64) assign_kernel<4><<<agrid, 128, cs_bytes, st>>>(B, final_pass);
@@ -457,12 +751,13 @@ int kmeans_run(const KMeansBatch& B, cudaStream_t st) {
   cudaFuncSetAttribute(assign_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(cs_bytes));
   cudaFuncSetAttribute(assign_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(cs_bytes));
   cudaFuncSetAttribute(sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sort_bytes));
+  cudaFuncSetAttribute(sums_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sum_bytes));
   const int iters = B.max_iter > 1 ? B.max_iter : 1;
   for (int it = 0; it < iters; ++it) {
     centroid_norms_kernel<<<ngrid, 128, 0, st>>>(B, 0);
     launch_assign(0);
     sort_kernel<<<B.problems, 1024, sort_bytes, st>>>(B);
-    sums_kernel<<<sum_blocks, 256, 0, st>>>(B);
+    sums_kernel<<<B.problems * B.k, kSumThreads, sum_bytes, st>>>(B);
     finalize_kernel<<<(B.problems + 63) / 64, 64, 0, st>>>(B);
   }
   centroid_norms_kernel<<<ngrid, 128, 0, st>>>(B, 1);

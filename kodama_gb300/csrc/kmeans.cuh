@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 #include <stddef.h>
+#include <stdint.h>
 
 namespace kgb {
 
@@ -26,7 +27,20 @@ struct KMeansBatch {
   int* members;             // problems x n scratch: rows grouped by cluster
   int* offsets;             // problems x (k+1) scratch: cluster offsets in members
   float* fscratch;          // problems x (3k+1) scratch for empty-cluster splitting
+  // tensor-core assignment (kmeans_tc_supported): x split into bf16 hi / lo
+  // (bf16_split_rows, dp columns), scratch for the centroids' split; xh null =
+  // every distance computed exactly
+  const uint16_t* xh;
+  const uint16_t* xl;
+  int dp;
+  uint16_t* ch;             // problems x k x dp
+  uint16_t* cl;
+  int tc_blocks;            // set by kmeans_run: 64-row blocks per CTA
+  float tc_crel;            // set by kmeans_run: the error bound's factor
 };
+
+// The tensor-core assignment applies (d <= 64, k <= 128).
+bool kmeans_tc_supported(int d, int k);
 
 size_t kmeans_sort_smem(int k);
 int kmeans_row_norms(const float* x, int n, int d, float* out, cudaStream_t st);

@@ -29,6 +29,11 @@ int knn_tc_graph(const float* x, int n, int d, int K, int segments, void* scratc
 // (asynchronous copy into host memory).
 int knn_tc_fallback_count(const void* scratch, int n, int d, int K, int segments, int* out, cudaStream_t st);
 
+// Rows of x (n x d) split into bfloat16 hi + lo parts (x = hi + lo + r,
+// |r| <= 2^-16 |x|), dp = d rounded up to 16, coordinates permuted inside
+// each 16-block so one lane's m16n8k16 fragment values are contiguous.
+int bf16_split_rows(const float* x, int n, int d, int dp, uint16_t* xh, uint16_t* xl, cudaStream_t st);
+
 // Fold-wise search: for each row the K nearest rows of other folds (folds[n]),
 // ranked by (internal distance, row); inner = minus the inner product instead
 // of the squared L2 distance.  idx -1 / dist +inf where fewer rows qualify;

@@ -88,6 +88,19 @@ __global__ void tc_prep_kernel(const float* __restrict__ x, int n, int d, int dp
   else atomicExch(nonfinite, 1);
 }
 
+__global__ void split_rows_kernel(const float* __restrict__ x, int n, int d, int dp, uint16_t* __restrict__ xh,
+                                  uint16_t* __restrict__ xl) {
+  const size_t e = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= static_cast<size_t>(n) * dp) return;
+  const int r = static_cast<int>(e / dp), k = static_cast<int>(e % dp);
+  const float v = k < d ? x[static_cast<size_t>(r) * d + k] : 0.0f;
+  const uint32_t hb = bf16_bits(v);
+  const uint32_t lb = bf16_bits(__fsub_rn(v, __uint_as_float(hb << 16)));
+  const size_t o = static_cast<size_t>(r) * dp + perm16(k);
+  xh[o] = static_cast<uint16_t>(hb);
+  xl[o] = static_cast<uint16_t>(lb);
+}
+
 __device__ __forceinline__ void mma16816(float* c, const uint32_t* a, uint2 b) {
   asm volatile(
       "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
@@ -479,6 +492,14 @@ void tc_shape(int K, int* segs, int* kp) {
   k = k < 16 ? 16 : k;
   const int cap = kMaxPer * 32 / (2 * *segs);
   *kp = k > cap ? cap : k;
+}
+
+int bf16_split_rows(const float* x, int n, int d, int dp, uint16_t* xh, uint16_t* xl, cudaStream_t st) {
+  const size_t total = static_cast<size_t>(n) * dp;
+  if (total == 0) return 0;
+  split_rows_kernel<<<static_cast<unsigned>((total + 255) / 256), 256, 0, st>>>(x, n, d, dp, xh, xl);
+  count_launch();
+  return static_cast<int>(cudaGetLastError());
 }
 
 bool knn_tc_supported(int n, int d, int K) {
