@@ -22,6 +22,7 @@
 #include <cmath>
 #include <cstring>
 #include <exception>
+#include <functional>
 #include <future>
 #include <limits>
 #include <map>
@@ -111,6 +112,14 @@ class Ctx {
   void fork() {
     const int e = mark();
     ck(cudaStreamWaitEvent(side_, ev_[e], 0), "cudaStreamWaitEvent");
+  }
+  // Copies device memory to the host as soon as event e has completed, on the
+  // side stream, and waits for that copy only (the main stream runs on).
+  template <class T>
+  void download_after(T* host, const T* dev, size_t count, int e) {
+    ck(cudaStreamWaitEvent(side_, ev_[e], 0), "cudaStreamWaitEvent");
+    if (count) ck(cudaMemcpyAsync(host, dev, count * sizeof(T), cudaMemcpyDeviceToHost, side_), "D2H");
+    ck(cudaStreamSynchronize(side_), "stream synchronize");
   }
   // CUDA events on the call's stream, for per-stage device timings.
   int mark() {
@@ -706,9 +715,13 @@ void tc_kmeans_inputs(Ctx& ctx, kgb::KMeansBatch& B, const float* d_x, int n, in
   B.cl = ctx.alloc<uint16_t>(static_cast<size_t>(B.problems) * B.k * split.dp);
 }
 
+// build_graph (may be empty): queues the kNN graph into d_gidx / d_gdist; it
+// runs right after the atlas k-means, so the host plans the runs while the
+// device builds the graph.
 void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_gidx, float* d_gdist, int K,
                               const kgb_matrix_options* o, kgb_matrix_result* out, Clock& clk, int ev_start,
-                              int ev_graph, std::future<std::vector<kgb::FoldPlan>>& folds_future) {
+                              int ev_graph, std::future<std::vector<kgb::FoldPlan>>& folds_future,
+                              const std::function<void()>& build_graph = {}) {
   const kgb_policy pol = policy_is_zero(o->policy) ? default_policy() : o->policy;
   int landmarks = o->landmarks > 0 ? o->landmarks : 10000;
   if (landmarks >= n) landmarks = static_cast<int>(std::ceil(static_cast<double>(n) * 0.75));
@@ -763,9 +776,13 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     ck_launch(kgb::kmeans_run(B, st), "atlas k-means");
   }
   const int ev_atlas = ctx.mark();
+  const bool graph_here = static_cast<bool>(build_graph);
+  if (graph_here) {
+    build_graph();
+    ev_graph = ctx.mark();
+  }
   std::vector<int> atlas(static_cast<size_t>(n));
-  ctx.download(atlas.data(), d_atlas_labels, n);
-  ctx.sync();
+  ctx.download_after(atlas.data(), d_atlas_labels, n, ev_atlas);
   out->timings[2] = clk.lap();
 
   // per-run landmarks and k-means seeds (host, libstdc++ streams)
@@ -1063,9 +1080,16 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   ctx.sync();
   if (res_stage != nullptr) std::memcpy(out->res, res_stage, res_bytes);
   const double t_dl = clk.lap();
-  out->kernel_ms[0] = ctx.ms(ev_start, ev_graph);
-  out->kernel_ms[1] = ctx.ms(ev_graph, ev_atlas);
-  out->kernel_ms[2] = ctx.ms(ev_atlas, ev_init);
+  if (graph_here) {
+    // order on the device: atlas, graph, landmark initialisation
+    out->kernel_ms[0] = ctx.ms(ev_atlas, ev_graph);
+    out->kernel_ms[1] = ctx.ms(ev_start, ev_atlas);
+    out->kernel_ms[2] = ctx.ms(ev_graph, ev_init);
+  } else {
+    out->kernel_ms[0] = ctx.ms(ev_start, ev_graph);
+    out->kernel_ms[1] = ctx.ms(ev_graph, ev_atlas);
+    out->kernel_ms[2] = ctx.ms(ev_atlas, ev_init);
+  }
   out->kernel_ms[3] = ctx.ms(ev_init, ev_tables);
   out->kernel_ms[4] = ctx.ms(ev_evo0, ev_evo1);
   out->kernel_ms[5] = ctx.ms(ev_evo1, ev_proj);
@@ -1205,10 +1229,16 @@ void matrix_entry(const float* x, bool x_on_device, int n, int d, const int32_t*
     ck_launch(kgb::normalize_external(d_in_idx, d_in_dist, n, gk, K, index_base, d_mm, d_gidx, d_gdist,
                                       ctx.stream()), "graph normalisation");
   } else {
+    // raw data: the graph is queued after the atlas k-means (see
+    // matrix_from_device_graph), overlapping the host's run planning
     K = neighbors;
     d_gidx = ctx.alloc<int>(static_cast<size_t>(n) * K);
     d_gdist = ctx.alloc<float>(static_cast<size_t>(n) * K);
-    exact_graph(ctx, d_x, n, d, K, KGB_KNN_AUTO, d_gidx, d_gdist, nullptr);
+    out->timings[1] = clk.lap();
+    matrix_from_device_graph(ctx, d_x, n, d, d_gidx, d_gdist, K, opt, out, clk, ev_start, -1, folds_future,
+                             [&]() { exact_graph(ctx, d_x, n, d, K, KGB_KNN_AUTO, d_gidx, d_gdist, nullptr); });
+    out->timings[0] = total.lap();
+    return;
   }
   const int ev_graph = ctx.mark();
   ctx.sync();
