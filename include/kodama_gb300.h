@@ -82,6 +82,14 @@ typedef struct kgb_matrix_options {
   int32_t snapshot_cycle;    /* cycle whose starting state kgb_matrix_result.snapshot_* record */
   int32_t proposal_greedy;   /* 0 = sample the relabelled candidates from the network's softmax
                                 (Gumbel top-k, default); 1 = take the top-scored ones */
+  /* Semi-supervised inputs of KODAMAMatrix (kodama.hpp:1077-1083), n entries
+   * each or NULL: starting_labels replace the k-means start (and switch the
+   * evolution to greedy acceptance), constrain groups the samples (every
+   * result row takes its group's majority label), fixed (non-zero) rows keep
+   * their labels. */
+  const int32_t* starting_labels;
+  const int32_t* constrain;
+  const int32_t* fixed;
 } kgb_matrix_options;
 
 /* Caller-allocated outputs of a KODAMA.matrix call. NULL = not wanted

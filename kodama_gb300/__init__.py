@@ -121,7 +121,8 @@ def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitt
                   apply_dissimilarity=True, index_base=-1, device=0, host_threads=0,
                   policy="full", res_out=None, first_run=1, classifier="knn",
                   components=50, proposal_weights=None, snapshot_cycle=None,
-                  proposal_greedy=False) -> MatrixResult:
+                  proposal_greedy=False, starting_labels=None, constrain=None,
+                  fixed=None) -> MatrixResult:
     """KODAMA.matrix on the GPU with the kNN (``classifier="knn"``) or PLS-LDA
     (``classifier="pls"``, ``components`` latent components) classifier.
     ``proposal_weights`` (the 4801 parameters of ``train_proposal``) selects
@@ -129,6 +130,12 @@ def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitt
     from the network's softmax (``proposal_greedy=True``: takes the
     top-scored ones); ``snapshot_cycle`` records its training data
     (``snapshot_features`` / ``snapshot_flags``) at that cycle.
+
+    Semi-supervised inputs (n integers each, KODAMAMatrix's starting_labels /
+    constrain / fixed, kodama.hpp:1077-1083): ``starting_labels`` replace the
+    k-means start and make the evolution greedy, ``constrain`` groups the
+    samples (every result row takes its group's majority label), non-zero
+    ``fixed`` rows keep their labels.
 
     ``graph`` = (indices, distances) of shape (n, K) runs the graph-input path
     (KODAMAMatrixFromGraphData_CUDA); without it the exact kNN graph is built
@@ -187,6 +194,18 @@ def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitt
             raise ValueError(f"proposal_weights must hold {N.PROPOSAL_PARAMS} floats")
         opt.proposal_weights = wts.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
         opt.proposal_greedy = 1 if proposal_greedy else 0
+    semi = {}
+    for name, vec, msg in (
+            ("starting_labels", starting_labels, "starting_labels size must match number of rows."),
+            ("constrain", constrain, "constrain size must be zero or match number of rows."),
+            ("fixed", fixed, "fixed size must be zero or match number of rows.")):
+        if vec is None or len(vec) == 0:
+            continue
+        a = np.ascontiguousarray(vec, dtype=np.int32)
+        if a.shape != (n,):
+            raise ValueError(msg)
+        semi[name] = a
+        setattr(opt, name, a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
     snap_f = snap_g = None
     if snapshot_cycle is not None:
         if not 0 <= snapshot_cycle < cycles:

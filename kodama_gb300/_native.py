@@ -53,7 +53,9 @@ class MatrixOptions(ctypes.Structure):
         "classifier", "components", "materialize_graph", "apply_dissimilarity", "metric",
         "device", "host_threads", "first_run", "reserved")] + [
         ("seed", ctypes.c_uint64), ("policy", Policy), ("proposal_weights", ctypes.POINTER(ctypes.c_float)),
-        ("snapshot_cycle", ctypes.c_int32), ("proposal_greedy", ctypes.c_int32)]
+        ("snapshot_cycle", ctypes.c_int32), ("proposal_greedy", ctypes.c_int32),
+        ("starting_labels", ctypes.POINTER(ctypes.c_int32)), ("constrain", ctypes.POINTER(ctypes.c_int32)),
+        ("fixed", ctypes.POINTER(ctypes.c_int32))]
 
 
 class MatrixResult(ctypes.Structure):

@@ -250,6 +250,42 @@ Coding code_labels(const int* labels, int n, uint64_t bucket_count) {
   return c;
 }
 
+// normalize_constrain / factor_subset (kodama_matrix.cpp:183-201, 988-1001):
+// group ids 1.. by first appearance of values[rows[i]].
+std::vector<int> first_appearance_ids(const int* values, const std::vector<int>& rows) {
+  std::map<int, int> ids;
+  std::vector<int> out(rows.size(), 0);
+  for (size_t i = 0; i < rows.size(); ++i) {
+    auto it = ids.find(values[rows[i]]);
+    if (it == ids.end()) it = ids.emplace(values[rows[i]], static_cast<int>(ids.size()) + 1).first;
+    out[i] = it->second;
+  }
+  return out;
+}
+
+// majority_label (kodama_matrix.cpp:169-181): the most frequent value, ties to
+// the smaller value.
+int majority_value(const std::vector<int>& values) {
+  std::map<int, int> counts;
+  for (int v : values) counts[v] += 1;
+  int bl = counts.begin()->first, bc = counts.begin()->second;
+  for (const auto& kv : counts)
+    if (kv.second > bc || (kv.second == bc && kv.first < bl)) {
+      bl = kv.first;
+      bc = kv.second;
+    }
+  return bl;
+}
+
+// constrained_majority (kodama_matrix.cpp:1003-1011), in place on n labels.
+void constrained_majority(int* labels, const int* groups, size_t n) {
+  std::map<int, std::vector<int>> by;
+  for (size_t i = 0; i < n; ++i) by[groups[i]].push_back(labels[i]);
+  std::map<int, int> lab;
+  for (const auto& kv : by) lab[kv.first] = majority_value(kv.second);
+  for (size_t i = 0; i < n; ++i) labels[i] = lab[groups[i]];
+}
+
 int host_threads(int requested) {
   if (requested > 0) return requested;
   const unsigned hc = std::thread::hardware_concurrency();
@@ -804,7 +840,30 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   }
   int* d_land = ctx.upload(land.data(), land.size());
   int* d_init_labels = ctx.alloc<int>(static_cast<size_t>(M) * L);
-  {
+  // semi-supervised inputs (run_kodama_matrix, kodama_matrix.cpp:3405-3420;
+  // run_iteration :3060-3117): starting labels replace the k-means start,
+  // a constraint groups the rows (normalize_constrain), fixed rows keep
+  // their labels
+  const bool has_start = o->starting_labels != nullptr;
+  std::vector<int> groups_all;
+  bool identity_groups = true;
+  if (o->constrain != nullptr) {
+    std::vector<int> all(static_cast<size_t>(n));
+    std::iota(all.begin(), all.end(), 0);
+    groups_all = first_appearance_ids(o->constrain, all);
+    for (int i = 0; i < n && identity_groups; ++i) identity_groups = groups_all[i] == i + 1;
+  }
+  const bool semi = has_start || !identity_groups;
+  std::vector<int> xcon;  // M x L landmark group ids (non-identity constraint)
+  if (!identity_groups) {
+    xcon.resize(static_cast<size_t>(M) * L);
+    parallel_for(M, host_threads(o->host_threads), [&](int r) {
+      const std::vector<int> lr(land.begin() + static_cast<size_t>(r) * L, land.begin() + static_cast<size_t>(r + 1) * L);
+      const std::vector<int> ids = first_appearance_ids(groups_all.data(), lr);
+      std::copy(ids.begin(), ids.end(), xcon.begin() + static_cast<size_t>(r) * L);
+    });
+  }
+  if (!has_start) {
     kgb::KMeansBatch B{};
     B.problems = M;
     B.n = L;
@@ -830,21 +889,67 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     ck_launch(kgb::kmeans_run(B, st), "landmark k-means");
   }
   // folds were planned on the host while the device worked
-  const std::vector<kgb::FoldPlan> fold_plans = folds_future.get();
+  std::vector<kgb::FoldPlan> fold_plans = folds_future.get();
+  // label coding and the initial-label hashes on the device; with
+  // semi-supervised inputs the start labels are built and coded on the host
+  const uint64_t bc = kgb::unordered_bucket_count(static_cast<size_t>(L));
+  std::vector<Coding> semi_codes;
+  int C0max = std::max(F, kk);
+  if (semi) {
+    std::vector<int> init_host(static_cast<size_t>(M) * L);
+    if (has_start) {
+      for (size_t i = 0; i < init_host.size(); ++i) init_host[i] = o->starting_labels[land[i]];
+    } else {
+      ctx.download(init_host.data(), d_init_labels, init_host.size());
+      ctx.sync();
+    }
+    semi_codes.resize(static_cast<size_t>(M));
+    parallel_for(M, host_threads(o->host_threads), [&](int r) {
+      int* lr = init_host.data() + static_cast<size_t>(r) * L;
+      if (!identity_groups) {
+        const int* gr = xcon.data() + static_cast<size_t>(r) * L;
+        constrained_majority(lr, gr, static_cast<size_t>(L));
+        // a constraint keeps every group inside one fold (make_folds,
+        // common.cpp:190-214), so the folds follow the start labels
+        const std::vector<int> fo = kgb::make_folds(std::vector<int>(lr, lr + L), std::vector<int>(gr, gr + L), F,
+                                                    false, seed + static_cast<uint64_t>(r0 + r));
+        fold_plans[r].folds.assign(fo.begin(), fo.end());
+        fold_plans[r].fold_hash = kgb::fnv_hash(fo.data(), fo.size());
+      }
+      semi_codes[r] = code_labels(lr, L, bc);
+    });
+    for (const auto& c : semi_codes) C0max = std::max<int>(C0max, static_cast<int>(c.code2label.size()));
+    ck(cudaMemcpyAsync(d_init_labels, init_host.data(), sizeof(int) * init_host.size(), cudaMemcpyHostToDevice, st),
+       "H2D");
+    ctx.sync();
+  }
   std::vector<uint8_t> folds(static_cast<size_t>(M) * L);
   for (int r = 0; r < M; ++r) {
     std::copy(fold_plans[r].folds.begin(), fold_plans[r].folds.end(), folds.begin() + static_cast<size_t>(r) * L);
   }
   uint8_t* d_folds = ctx.upload(folds.data(), folds.size());
-  // label coding (labels 1..init_k, all inside the bucket range) and the
-  // initial-label hashes on the device
-  const uint64_t bc = kgb::unordered_bucket_count(static_cast<size_t>(L));
-  const int C0max = std::max(F, kk);
   uint16_t* d_codes = ctx.alloc<uint16_t>(static_cast<size_t>(M) * L);
   int* d_c2l = ctx.alloc<int>(static_cast<size_t>(M) * C0max);
   int* d_ncodes = ctx.alloc<int>(M);
   uint64_t* d_init_hash = ctx.alloc<uint64_t>(M);
-  {
+  std::vector<uint8_t> nocol(static_cast<size_t>(M), 1);
+  if (semi) {
+    std::vector<uint16_t> codes(static_cast<size_t>(M) * L);
+    std::vector<int> c2l(static_cast<size_t>(M) * C0max, 0), ncodes(static_cast<size_t>(M));
+    for (int r = 0; r < M; ++r) {
+      std::copy(semi_codes[r].codes.begin(), semi_codes[r].codes.end(), codes.begin() + static_cast<size_t>(r) * L);
+      std::copy(semi_codes[r].code2label.begin(), semi_codes[r].code2label.end(),
+                c2l.begin() + static_cast<size_t>(r) * C0max);
+      ncodes[r] = static_cast<int>(semi_codes[r].code2label.size());
+      nocol[r] = semi_codes[r].nocollide ? 1 : 0;
+    }
+    ck(cudaMemcpyAsync(d_codes, codes.data(), sizeof(uint16_t) * codes.size(), cudaMemcpyHostToDevice, st), "H2D");
+    ck(cudaMemcpyAsync(d_c2l, c2l.data(), sizeof(int) * c2l.size(), cudaMemcpyHostToDevice, st), "H2D");
+    ck(cudaMemcpyAsync(d_ncodes, ncodes.data(), sizeof(int) * ncodes.size(), cudaMemcpyHostToDevice, st), "H2D");
+    ctx.sync();
+    ctx.fork();
+    ck_launch(kgb::fnv_rows(d_init_labels, M, L, d_init_hash, ctx.side()), "label hashes");
+  } else {
     kgb::CodingArgs ca{};
     ca.problems = M;
     ca.n = L;
@@ -862,7 +967,6 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   std::vector<uint64_t> init_hash(static_cast<size_t>(M));
   ck(cudaMemcpyAsync(init_hash.data(), d_init_hash, sizeof(uint64_t) * M, cudaMemcpyDeviceToHost, ctx.side()),
      "D2H");
-  const std::vector<uint8_t> nocol(static_cast<size_t>(M), 1);
   out->timings[7] = 0.0;
   out->timings[3] = clk.lap();
 
@@ -880,8 +984,8 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   P.T = T;
   P.F = F;
   P.G = L;
-  P.singleton = 1;
-  P.evolutionary = 1;
+  P.singleton = identity_groups ? 1 : 0;
+  P.evolutionary = has_start ? 0 : 1;
   P.guarded = 1;
   P.absorption = 1;
   P.adaptive = 1;
@@ -900,6 +1004,40 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   P.fixed = nullptr;
   P.goff = ctx.upload(goff.data(), goff.size());
   P.gmem = ctx.upload(identity.data(), identity.size());
+  if (!identity_groups || o->fixed != nullptr) {
+    // one block of groups and fixed flags per run: groups in ascending id
+    // (maximize_core's std::map), members in landmark order
+    std::vector<int> pg_off(static_cast<size_t>(M) * (L + 1)), pg_mem(static_cast<size_t>(M) * L),
+        pg_cnt(static_cast<size_t>(M));
+    std::vector<int> pfix(o->fixed != nullptr ? static_cast<size_t>(M) * L : 0);
+    parallel_for(M, host_threads(o->host_threads), [&](int r) {
+      int* off = pg_off.data() + static_cast<size_t>(r) * (L + 1);
+      int* mem = pg_mem.data() + static_cast<size_t>(r) * L;
+      if (identity_groups) {
+        for (int i = 0; i <= L; ++i) off[i] = i;
+        for (int i = 0; i < L; ++i) mem[i] = i;
+        pg_cnt[r] = L;
+      } else {
+        std::map<int, std::vector<int>> members;
+        for (int i = 0; i < L; ++i) members[xcon[static_cast<size_t>(r) * L + i]].push_back(i);
+        int g = 0, pos = 0;
+        off[0] = 0;
+        for (const auto& kv : members) {
+          for (int m : kv.second) mem[pos++] = m;
+          off[++g] = pos;
+        }
+        pg_cnt[r] = g;
+      }
+      if (o->fixed != nullptr)
+        for (int i = 0; i < L; ++i)
+          pfix[static_cast<size_t>(r) * L + i] = o->fixed[land[static_cast<size_t>(r) * L + i]] != 0 ? 1 : 0;
+    });
+    P.per_problem_groups = 1;
+    P.goff = ctx.upload(pg_off.data(), pg_off.size());
+    P.gmem = ctx.upload(pg_mem.data(), pg_mem.size());
+    P.gcount = ctx.upload(pg_cnt.data(), pg_cnt.size());
+    if (o->fixed != nullptr) P.fixed = ctx.upload(pfix.data(), pfix.size());
+  }
   P.seeds = ctx.upload(seeds.data(), seeds.size());
   EvolveBuffers eb{};
   int* d_res = nullptr;
@@ -1031,6 +1169,19 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   ev_proj = ctx.mark();
   ctx.sync();
   out->timings[4] = clk.lap();
+  }
+
+  if (!identity_groups) {
+    // the result rows take their groups' majority labels (run_iteration,
+    // kodama_matrix.cpp:3277-3283)
+    std::vector<int> res_host(static_cast<size_t>(M) * n);
+    ctx.download(res_host.data(), d_res, res_host.size());
+    ctx.sync();
+    parallel_for(M, host_threads(o->host_threads), [&](int r) {
+      constrained_majority(res_host.data() + static_cast<size_t>(r) * n, groups_all.data(), static_cast<size_t>(n));
+    });
+    ck(cudaMemcpyAsync(d_res, res_host.data(), sizeof(int) * res_host.size(), cudaMemcpyHostToDevice, st), "H2D");
+    ctx.sync();
   }
 
   // outputs

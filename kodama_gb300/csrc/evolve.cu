@@ -55,6 +55,11 @@ struct Fixed {
   double score;
   int accept;
   int improves;
+  // this problem's groups and fixed flags (bind_groups)
+  const int* goff;
+  const int* gmem;
+  const int* fxd;
+  int G;
   // learned proposal: candidate count and radix-select state
   int sel_count;
   int sel_digit;
@@ -651,7 +656,7 @@ __device__ int absorption_block(const EvolveParams& P, const Smem& s, int prob, 
     const int a = s.cl[r];
     atomicAdd(&s.cnt[a], 1);
     atomicAdd(&tr[a * C + pp[r]], 1);
-    if (P.fixed == nullptr || P.fixed[r] != 1) atomicAdd(&s.movable[a], 1);
+    if (s.f->fxd == nullptr || s.f->fxd[r] != 1) atomicAdd(&s.movable[a], 1);
   }
   __syncthreads();
   int local = 0;
@@ -757,7 +762,7 @@ __device__ int absorption_block(const EvolveParams& P, const Smem& s, int prob, 
   if (apply) {
     for (int r = threadIdx.x; r < P.L; r += kThreads) {
       const int a = s.cl[r];
-      if (P.fixed != nullptr && P.fixed[r] == 1) continue;
+      if (s.f->fxd != nullptr && s.f->fxd[r] == 1) continue;
       if (a != sel && s.bt[a] == sel) s.cl[r] = static_cast<uint16_t>(sel);
     }
   }
@@ -786,17 +791,17 @@ __device__ void relabel_serial(const EvolveParams& P, const Smem& s, const uint1
   }
   for (int q = 0; q < ns; ++q) {
     const int g = s.perm[q];
-    const int beg = P.goff[g], end = P.goff[g + 1];
+    const int beg = s.f->goff[g], end = s.f->goff[g + 1];
     int neligible = 0;
-    for (int a = beg; a < end; ++a) neligible += (P.fixed == nullptr || P.fixed[P.gmem[a]] != 1);
+    for (int a = beg; a < end; ++a) neligible += (s.f->fxd == nullptr || s.f->fxd[s.f->gmem[a]] != 1);
     if (neligible == 0) continue;
     int rep;
     if (P.pol_guidance) {
       // candidate labels: predictions of the eligible members, ascending, with counts
       int k = 0;
       for (int a = beg; a < end; ++a) {
-        const int row = P.gmem[a];
-        if (P.fixed != nullptr && P.fixed[row] == 1) continue;
+        const int row = s.f->gmem[a];
+        if (s.f->fxd != nullptr && s.f->fxd[row] == 1) continue;
         const int c = pp[row];
         if (hist[c]++ == 0) s.bt[k++] = c;
       }
@@ -819,8 +824,8 @@ __device__ void relabel_serial(const EvolveParams& P, const Smem& s, const uint1
       rep = s.order[discrete_serial(f.rng, s.weight, nemp, s.cp)];
     }
     for (int a = beg; a < end; ++a) {
-      const int row = P.gmem[a];
-      if (P.fixed != nullptr && P.fixed[row] == 1) continue;
+      const int row = s.f->gmem[a];
+      if (s.f->fxd != nullptr && s.f->fxd[row] == 1) continue;
       s.cl[row] = static_cast<uint16_t>(rep);
     }
   }
@@ -901,7 +906,7 @@ __device__ void learned_flip(const EvolveParams& P, const Smem& s, int prob, int
   __syncthreads();
   for (int base = warp * 32; base < P.L; base += kThreads) {
     const int r = base + lane;
-    const bool c = r < P.L && s.cur[r] != s.curpred[r] && (P.fixed == nullptr || P.fixed[r] != 1);
+    const bool c = r < P.L && s.cur[r] != s.curpred[r] && (s.f->fxd == nullptr || s.f->fxd[r] != 1);
     const unsigned b = __ballot_sync(kFull, c);
     int at = 0;
     if (lane == 0 && b != 0u) at = atomicAdd(&f.sel_count, __popc(b));
@@ -1004,9 +1009,24 @@ __device__ void snapshot_state(const EvolveParams& P, const Smem& s, int prob, i
   __syncthreads();
 }
 
+// Points the CTA at problem prob's groups and fixed flags: shared by all
+// problems, or one block per problem (per_problem_groups: goff stride L + 1,
+// gmem and fixed stride L, group count gcount[prob]).
+__device__ void bind_groups(const EvolveParams& P, const Smem& s, int prob) {
+  if (threadIdx.x == 0) {
+    const bool per = P.per_problem_groups != 0;
+    s.f->goff = P.goff + (per ? static_cast<size_t>(prob) * (P.L + 1) : 0);
+    s.f->gmem = P.gmem + (per ? static_cast<size_t>(prob) * P.L : 0);
+    s.f->fxd = P.fixed == nullptr ? nullptr : P.fixed + (per ? static_cast<size_t>(prob) * P.L : 0);
+    s.f->G = per ? P.gcount[prob] : P.G;
+  }
+  __syncthreads();
+}
+
 __device__ void evolve_problem(const EvolveParams& P, const Smem& s, int prob) {
   Fixed& f = *s.f;
-  const int L = P.L, T = P.T, G = P.G;
+  bind_groups(P, s, prob);
+  const int L = P.L, T = P.T, G = f.G;
   const int C0 = P.ncodes[prob];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint16_t* init = P.init + static_cast<size_t>(prob) * L;
@@ -1082,9 +1102,9 @@ __device__ void evolve_problem(const EvolveParams& P, const Smem& s, int prob) {
         // given to the candidates the network scores highest
         int take = 0;
         for (int g = threadIdx.x; g < G; g += kThreads) {
-          const int row = P.gmem[g];
+          const int row = s.f->gmem[g];
           if (s.curpred[row] == s.cur[row]) continue;
-          if (P.fixed != nullptr && P.fixed[row] == 1) continue;
+          if (s.f->fxd != nullptr && s.f->fxd[row] == 1) continue;
           take += final_position_of(s, g) < ns;
         }
         take = block_sum(take, f);
@@ -1094,9 +1114,9 @@ __device__ void evolve_problem(const EvolveParams& P, const Smem& s, int prob) {
         // prediction differs from their label can change, so walk just those
         // forward to their final shuffled position.
         for (int g = threadIdx.x; g < G; g += kThreads) {
-          const int row = P.gmem[g];
+          const int row = s.f->gmem[g];
           if (s.curpred[row] == s.cur[row]) continue;
-          if (P.fixed != nullptr && P.fixed[row] == 1) continue;
+          if (s.f->fxd != nullptr && s.f->fxd[row] == 1) continue;
           if (final_position_of(s, g) < ns) s.cl[row] = s.curpred[row];
         }
       } else {
@@ -1337,7 +1357,7 @@ __device__ int transition_stats(const EvolveParams& P, const Smem& s, const uint
     const int a = s.cl[r];
     atomicAdd(&s.cnt[a], 1);
     atomicAdd(&tr[a * C + pp[r]], 1);
-    if (P.fixed == nullptr || P.fixed[r] != 1) atomicAdd(&s.movable[a], 1);
+    if (s.f->fxd == nullptr || s.f->fxd[r] != 1) atomicAdd(&s.movable[a], 1);
   }
   __syncthreads();
   int local = 0;
@@ -1456,7 +1476,7 @@ __device__ int coarsening_block(const EvolvePlsParams& Q, const Smem& s, int pro
   int changed = 0;
   const int* remap = s.aux;
   for (int r = threadIdx.x; r < P.L; r += kThreads) {
-    if (P.fixed != nullptr && P.fixed[r] == 1) continue;
+    if (s.f->fxd != nullptr && s.f->fxd[r] == 1) continue;
     const int a = s.cl[r];
     int d = a;
     while (remap[d] != d) d = remap[d];
@@ -1548,7 +1568,7 @@ __device__ void class_lists(const EvolvePlsParams& Q, const Smem& s, int prob, i
 __device__ void pls_propose(const EvolvePlsParams& Q, const Smem& s, int prob, int cycle, PlsRunState& st, int C0) {
   const EvolveParams& P = Q.base;
   Fixed& f = *s.f;
-  const int L = P.L, T = P.T, G = P.G;
+  const int L = P.L, T = P.T, G = f.G;
   for (int r = threadIdx.x; r < L; r += kThreads) s.cl[r] = s.cur[r];
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -1576,9 +1596,9 @@ __device__ void pls_propose(const EvolvePlsParams& Q, const Smem& s, int prob, i
     bucket_steps_block(s, G);
     if (P.singleton && P.pol_guidance) {
       for (int g = threadIdx.x; g < G; g += kThreads) {
-        const int row = P.gmem[g];
+        const int row = s.f->gmem[g];
         if (s.curpred[row] == s.cur[row]) continue;
-        if (P.fixed != nullptr && P.fixed[row] == 1) continue;
+        if (s.f->fxd != nullptr && s.f->fxd[row] == 1) continue;
         if (final_position_of(s, g) < ns) s.cl[row] = s.curpred[row];
       }
     } else {
@@ -1613,6 +1633,7 @@ __device__ void pls_propose(const EvolvePlsParams& Q, const Smem& s, int prob, i
 __device__ void pls_step(const EvolvePlsParams& Q, const Smem& s, int prob) {
   const EvolveParams& P = Q.base;
   Fixed& f = *s.f;
+  bind_groups(P, s, prob);
   const int L = P.L, T = P.T;
   const int C0 = P.ncodes[prob];
   const size_t ro = static_cast<size_t>(prob) * L;

@@ -34,9 +34,11 @@ struct EvolveParams {
   const int* ncodes;       // problems
   const uint8_t* nocollide;// problems: 1 if all labels lie in [0, bucket_count)
   const uint8_t* folds;    // problems x L
-  const int* fixed;        // L (shared) or nullptr; value 1 = fixed
-  const int* goff;         // G+1 group offsets
-  const int* gmem;         // L group members (rows), ascending within a group
+  const int* fixed;        // L (shared) or problems x L (per_problem_groups), or nullptr; value 1 = fixed
+  const int* goff;         // G+1 group offsets (or problems x (L+1))
+  const int* gmem;         // L group members (rows), ascending within a group (or problems x L)
+  int per_problem_groups;  // 1: goff / gmem / fixed hold one block per problem, group counts in gcount
+  const int* gcount;       // problems (per_problem_groups)
   const uint64_t* seeds;   // problems
   const double* psq;       // L+1: (c/L)*(c/L) as two rounded double operations
   const int* rev_off;      // problems x (L+1): reverse neighbour lists of the vote tables

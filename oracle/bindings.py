@@ -100,16 +100,28 @@ def _wrap(n, opts, b) -> MatrixResult:
         timings=b["timings"], pls_counters=b["pls"].reshape(runs, 2))
 
 
+def _opt_vec(v, n):
+    if v is None:
+        return None, ctypes.c_void_p(0)
+    a = np.ascontiguousarray(v, np.int32)
+    if a.shape != (n,):
+        raise ValueError("starting / constrain / fixed need one entry per row")
+    return a, a.ctypes.data_as(ctypes.c_void_p)
+
+
 def kodama_matrix_graph_data(L, x: np.ndarray, gidx: np.ndarray, gdist: np.ndarray,
-                             index_base: int, seed: int = 1234, **kw) -> MatrixResult:
-    """KODAMAMatrixFromGraphData_CPU: data plus a caller-supplied graph."""
+                             index_base: int, seed: int = 1234, starting=None, constrain=None, fixed=None,
+                             **kw) -> MatrixResult:
+    """KODAMAMatrixFromGraphData_CPU: data plus a caller-supplied graph, with
+    optional starting labels, constraint groups and fixed flags."""
     x = np.ascontiguousarray(x, np.float32)
     n, d = x.shape
     gk = gidx.shape[1]
     opts = matrix_options(**kw)
     opts[4] = opts[4] if opts[4] > 0 else 100
     b = _alloc_matrix(n, opts)
-    rc = L.kodama_matrix_graph_data(
+    keep = [_opt_vec(v, n) for v in (starting, constrain, fixed)]
+    rc = L.kodama_matrix_graph_data_ex(
         x.ctypes.data_as(ctypes.c_void_p), n, d,
         np.ascontiguousarray(gidx, np.int32).ctypes.data_as(ctypes.c_void_p),
         np.ascontiguousarray(gdist, np.float32).ctypes.data_as(ctypes.c_void_p), gk, index_base,
@@ -117,7 +129,7 @@ def kodama_matrix_graph_data(L, x: np.ndarray, gidx: np.ndarray, gdist: np.ndarr
         *[b[f].ctypes.data_as(ctypes.c_void_p) for f in
           ("res", "acc", "v", "hashes", "run_counters", "cycle_diag", "out_idx", "out_dist")],
         ctypes.byref(b["out_k"]), b["timings"].ctypes.data_as(ctypes.c_void_p),
-        b["pls"].ctypes.data_as(ctypes.c_void_p))
+        b["pls"].ctypes.data_as(ctypes.c_void_p), *[k[1] for k in keep])
     if rc != 0:
         raise RuntimeError(_err(L))
     return _wrap(n, opts, b)

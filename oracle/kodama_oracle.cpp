@@ -1197,6 +1197,32 @@ int majority_of(const std::vector<int>& v) {
   return bl;
 }
 
+// Grouping helpers of the semi-supervised KODAMA.matrix (kodama_matrix.cpp):
+// normalize_constrain :183-201 (ids 1.. by first appearance; none = each row
+// its own group), factor_subset :988-1001 (the same over a row subset) and
+// constrained_majority :1003-1011 (every row takes its group's majority label,
+// ties to the smaller label).
+std::vector<int> first_appearance_ids(const int* values, const std::vector<int>& rows) {
+  std::map<int, int> ids;
+  std::vector<int> out(rows.size(), 0);
+  for (size_t i = 0; i < rows.size(); ++i) {
+    auto it = ids.find(values[rows[i]]);
+    if (it == ids.end()) it = ids.emplace(values[rows[i]], static_cast<int>(ids.size()) + 1).first;
+    out[i] = it->second;
+  }
+  return out;
+}
+
+std::vector<int> constrained_majority(const std::vector<int>& labels, const std::vector<int>& groups) {
+  std::map<int, std::vector<int>> by;
+  for (size_t i = 0; i < labels.size(); ++i) by[groups[i]].push_back(labels[i]);
+  std::map<int, int> lab;
+  for (const auto& kv : by) lab[kv.first] = majority_of(kv.second);
+  std::vector<int> out(labels.size());
+  for (size_t i = 0; i < labels.size(); ++i) out[i] = lab[groups[i]];
+  return out;
+}
+
 void dissimilarity(int* idx, float* dist, int samples, int K, const int* res, int runs, bool in1, bool out1) {
   std::vector<int> by(static_cast<size_t>(samples) * runs);
   for (int s = 0; s < samples; ++s)
@@ -1278,11 +1304,15 @@ void fill_run(RunOut& ro, const CoreOut& core, int run, const std::vector<int>& 
   }
 }
 
+// starting / constrain / fixed (n entries each, null = none) are the
+// semi-supervised inputs of run_kodama_matrix (kodama_matrix.cpp:3405-3420,
+// run_iteration :3060-3117, :3277-3283).
 void kodama_matrix(const float* x, int n, int d, const int* gidx_in, const float* gdist_in, int gk_in,
                    int index_base, const MatrixOpts& o, uint64_t seed,
                    int* res_out, double* acc_out, double* v_out, uint64_t* hashes_out, int* counters_out,
                    int* cycle_out, int* knn_idx_out, float* knn_dist_out, int* knn_k_out, double* timings,
-                   int* pls_out) {
+                   int* pls_out, const int* starting = nullptr, const int* constrain_in = nullptr,
+                   const int* fixed_in = nullptr) {
   const auto t0 = std::chrono::steady_clock::now();
   auto since = [](std::chrono::steady_clock::time_point a) {
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - a).count();
@@ -1321,6 +1351,13 @@ void kodama_matrix(const float* x, int n, int d, const int* gidx_in, const float
     }
   }
   const int splitting = o.splitting > 0 ? o.splitting : (n < 40000 ? 100 : 300);
+  std::vector<int> all_rows(static_cast<size_t>(n));
+  std::iota(all_rows.begin(), all_rows.end(), 0);
+  std::vector<int> groups = all_rows;  // normalize_constrain: 1..n without a constraint
+  for (int& g : groups) ++g;
+  if (constrain_in != nullptr) groups = first_appearance_ids(constrain_in, all_rows);
+  bool identity = true;
+  for (int i = 0; i < n; ++i) identity = identity && groups[i] == i + 1;
   // shared landmark atlas (kodama_matrix.cpp:3662-3734)
   const int coarse_k = std::max(2, std::min(splitting, n));
   std::mt19937_64 shared_rng(seed + 1u);
@@ -1343,8 +1380,19 @@ void kodama_matrix(const float* x, int n, int d, const int* gidx_in, const float
       const int L = static_cast<int>(land.size());
       std::vector<float> xl(static_cast<size_t>(L) * d);
       for (int i = 0; i < L; ++i) std::copy_n(x + static_cast<size_t>(land[i]) * d, d, xl.data() + static_cast<size_t>(i) * d);
-      const int init_k = std::max(2, std::min(splitting, L));
-      const std::vector<int> init = kmeans_labels(xl.data(), L, d, init_k, rng, 10);
+      std::vector<int> xcon(static_cast<size_t>(L)), xfix(static_cast<size_t>(L), 0), init;
+      if (identity) std::iota(xcon.begin(), xcon.end(), 1);
+      else xcon = first_appearance_ids(groups.data(), land);
+      if (fixed_in != nullptr)
+        for (int i = 0; i < L; ++i) xfix[i] = fixed_in[land[i]] != 0 ? 1 : 0;
+      if (starting != nullptr) {
+        init.resize(static_cast<size_t>(L));
+        for (int i = 0; i < L; ++i) init[i] = starting[land[i]];
+      } else {
+        const int init_k = std::max(2, std::min(splitting, L));
+        init = kmeans_labels(xl.data(), L, d, init_k, rng, 10);
+      }
+      if (!identity) init = constrained_majority(init, xcon);
       // subset_graph_to_rows (kodama_matrix.cpp:1332-1365): one-based local ids
       std::vector<int> g2l(static_cast<size_t>(n), -1);
       for (int i = 0; i < L; ++i) g2l[land[i]] = i;
@@ -1363,13 +1411,15 @@ void kodama_matrix(const float* x, int n, int d, const int* gidx_in, const float
           ++col;
         }
       }
-      std::vector<int> constrain(static_cast<size_t>(L));
-      std::iota(constrain.begin(), constrain.end(), 1);
+      const std::vector<int>& constrain = xcon;
+      auto finish = [&](RunOut& out_run) {
+        if (!identity) out_run.res = constrained_majority(out_run.res, groups);
+      };
       if (o.classifier == 1) {
         // PLS-LDA classifier (run_iteration, kodama_matrix.cpp:3105-3158, 3262-3276)
         CoreOpts co;
         co.cycles = o.cycles;
-        co.evolutionary = true;
+        co.evolutionary = starting == nullptr;
         co.guarded = true;
         co.absorption = true;
         co.adaptive = true;
@@ -1381,8 +1431,7 @@ void kodama_matrix(const float* x, int n, int d, const int* gidx_in, const float
         po.cv_seed = seed + static_cast<uint64_t>(run);
         po.max_components = o.components;
         po.fixed_components = o.components;
-        const CoreOut core = core_plslda(xl.data(), L, d, init, constrain,
-                                         std::vector<int>(static_cast<size_t>(L), 0), co, po);
+        const CoreOut core = core_plslda(xl.data(), L, d, init, constrain, xfix, co, po);
         ro.res.assign(static_cast<size_t>(n), 0);
         for (int i = 0; i < L; ++i) ro.res[land[i]] = core.clbest[i];
         std::vector<char> is_land(static_cast<size_t>(n), 0);
@@ -1397,6 +1446,7 @@ void kodama_matrix(const float* x, int n, int d, const int* gidx_in, const float
               plslda_predict(xl.data(), L, d, core.clbest, xt.data(), static_cast<int>(tpoints.size()), po);
           for (size_t i = 0; i < tpoints.size(); ++i) ro.res[tpoints[i]] = proj[i];
         }
+        finish(ro);
         fill_run(ro, core, run, land, init, L, o.cycles);
         continue;
       }
@@ -1405,14 +1455,13 @@ void kodama_matrix(const float* x, int n, int d, const int* gidx_in, const float
       co.k = std::max(o.knn_k, 1);
       co.folds = o.folds;
       co.stratified = false;
-      co.evolutionary = true;
+      co.evolutionary = starting == nullptr;
       co.guarded = true;
       co.absorption = true;
       co.adaptive = true;
       co.seed = seed + static_cast<uint64_t>(run);
       co.cv_seed = seed + static_cast<uint64_t>(run);
-      const CoreOut core = core_knn_graph(lidx.data(), ldist.data(), L, K, -1, init, constrain,
-                                          std::vector<int>(static_cast<size_t>(L), 0), co);
+      const CoreOut core = core_knn_graph(lidx.data(), ldist.data(), L, K, -1, init, constrain, xfix, co);
       // projection of non-landmarks (kodama_matrix.cpp:3221-3261, majority_label :169)
       ro.res.assign(static_cast<size_t>(n), 0);
       for (int i = 0; i < L; ++i) ro.res[land[i]] = core.clbest[i];
@@ -1431,6 +1480,7 @@ void kodama_matrix(const float* x, int n, int d, const int* gidx_in, const float
         }
         ro.res[t] = votes.empty() ? core.clbest.front() : majority_of(votes);
       }
+      finish(ro);
       fill_run(ro, core, run, land, init, L, o.cycles);
     }
   };
@@ -1679,23 +1729,36 @@ int orc_core_knn(
   }
 }
 
-int orc_kodama_matrix_graph_data(
+// starting / constrain / fixed: n entries each, or null.
+int orc_kodama_matrix_graph_data_ex(
   const float* x, int n, int d, const int* gidx, const float* gdist, int gk, int index_base,
   const int* o, unsigned long long seed,
   int* res, double* acc, double* v, unsigned long long* hashes, int* run_counters,
-  int* cycle_diag, int* out_idx, float* out_dist, int* out_k, double* timings, int* pls_counters
+  int* cycle_diag, int* out_idx, float* out_dist, int* out_k, double* timings, int* pls_counters,
+  const int* starting, const int* constrain, const int* fixed
 ) {
   try {
     orc::MatrixOpts mo{o[0], o[1], o[2], o[3], o[4], o[5], o[6], o[7], o[8], o[9], o[10], o[11], o[12]};
     if (timings) for (int i = 0; i < 6; ++i) timings[i] = 0.0;
     orc::kodama_matrix(x, n, d, gidx, gdist, gk, index_base, mo, seed, res, acc, v,
                        reinterpret_cast<uint64_t*>(hashes), run_counters, cycle_diag, out_idx, out_dist, out_k,
-                       timings, pls_counters);
+                       timings, pls_counters, starting, constrain, fixed);
     return 0;
   } catch (const std::exception& e) {
     orc::g_error = e.what();
     return 1;
   }
+}
+
+int orc_kodama_matrix_graph_data(
+  const float* x, int n, int d, const int* gidx, const float* gdist, int gk, int index_base,
+  const int* o, unsigned long long seed,
+  int* res, double* acc, double* v, unsigned long long* hashes, int* run_counters,
+  int* cycle_diag, int* out_idx, float* out_dist, int* out_k, double* timings, int* pls_counters
+) {
+  return orc_kodama_matrix_graph_data_ex(x, n, d, gidx, gdist, gk, index_base, o, seed, res, acc, v, hashes,
+                                         run_counters, cycle_diag, out_idx, out_dist, out_k, timings,
+                                         pls_counters, nullptr, nullptr, nullptr);
 }
 
 namespace {

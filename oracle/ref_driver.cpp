@@ -105,13 +105,17 @@ int ref_last_error(char* buf, int len) {
 }
 
 // KODAMAMatrixFromGraphData_CPU (kodama.hpp:1206): data + caller graph.
-int ref_kodama_matrix_graph_data(
+int ref_kodama_matrix_graph_data_ex(
   const float* x, int n, int d, const int* gidx, const float* gdist, int gk, int index_base,
   const int* o, unsigned long long seed,
   int* res, double* acc, double* v, unsigned long long* hashes, int* run_counters,
-  int* cycle_diag, int* out_idx, float* out_dist, int* out_k, double* timings, int* pls_counters
+  int* cycle_diag, int* out_idx, float* out_dist, int* out_k, double* timings, int* pls_counters,
+  const int* starting, const int* constrain, const int* fixed
 ) {
   try {
+    const std::vector<int> st = starting ? std::vector<int>(starting, starting + n) : std::vector<int>();
+    const std::vector<int> co = constrain ? std::vector<int>(constrain, constrain + n) : std::vector<int>();
+    const std::vector<int> fx = fixed ? std::vector<int>(fixed, fixed + n) : std::vector<int>();
     kodama::MatrixView view(x, static_cast<size_t>(n), static_cast<size_t>(d));
     kodama::NeighborGraph g;
     g.neighbors = gk;
@@ -121,7 +125,7 @@ int ref_kodama_matrix_graph_data(
       (index_base == 0 ? kodama::GraphIndexBase::Zero : kodama::GraphIndexBase::Auto);
     const auto opt = matrix_options(o, seed);
     const auto t0 = std::chrono::steady_clock::now();
-    const auto r = kodama::KODAMAMatrixFromGraphData_CPU(view, g, {}, {}, {}, opt);
+    const auto r = kodama::KODAMAMatrixFromGraphData_CPU(view, g, st, co, fx, opt);
     const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     export_matrix_result(r, n, opt.runs, opt.cycles, res, acc, v, hashes, run_counters,
                          cycle_diag, out_idx, out_dist, out_k, timings, pls_counters);
@@ -131,6 +135,17 @@ int ref_kodama_matrix_graph_data(
     g_error = e.what();
     return 1;
   }
+}
+
+int ref_kodama_matrix_graph_data(
+  const float* x, int n, int d, const int* gidx, const float* gdist, int gk, int index_base,
+  const int* o, unsigned long long seed,
+  int* res, double* acc, double* v, unsigned long long* hashes, int* run_counters,
+  int* cycle_diag, int* out_idx, float* out_dist, int* out_k, double* timings, int* pls_counters
+) {
+  return ref_kodama_matrix_graph_data_ex(x, n, d, gidx, gdist, gk, index_base, o, seed, res, acc, v, hashes,
+                                         run_counters, cycle_diag, out_idx, out_dist, out_k, timings,
+                                         pls_counters, nullptr, nullptr, nullptr);
 }
 
 // KODAMAMatrix_CPU (kodama.hpp:1069): raw data, the reference's own HNSW graph.

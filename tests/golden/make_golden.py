@@ -24,7 +24,7 @@ sys.path.insert(0, ROOT)
 
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 
-from golden_util import knn_inputs  # noqa: E402
+from golden_util import knn_inputs, semi_inputs  # noqa: E402
 from kodama_gb300 import datasets  # noqa: E402
 from oracle import oracle, ref  # noqa: E402
 
@@ -151,6 +151,24 @@ def core_graph_case(name, spec, K, **kw):
     }
 
 
+def semi_matrix_case(name, spec, K, **kw):
+    """KODAMAMatrixFromGraphData with starting labels / constraint / fixed
+    flags of semi_inputs(spec), on the canonical exact graph."""
+    x, start, con, fix = semi_inputs(spec)
+    gi, gd = oracle.exact_knn(x, K, threads=8)
+    r = ref.kodama_matrix_graph_data(x, gi, gd, 0, threads=8, materialize=1, starting=start, constrain=con,
+                                     fixed=fix, **kw)
+    return {
+        "kind": "kodama_matrix_semi", "name": name, "input": spec, "K": K, "index_base": 0, "options": kw,
+        "graph_sha256": sha(gi) + ":" + sha(gd),
+        "acc": r.acc.tolist(), "v_sha256": sha(r.v), "res_sha256": sha(r.res),
+        "hashes": [[int(v) for v in row] for row in r.hashes], "run_counters": r.run_counters.tolist(),
+        "cycle_diag_sha256": sha(r.cycle_diag), "knn_idx_sha256": sha(r.knn_idx),
+        "knn_dist_sha256": sha(r.knn_dist), "res_head": r.res[:, :16].tolist(),
+        "pls_counters": r.pls_counters.tolist(),
+    }
+
+
 def main():
     if not ref.available():
         raise SystemExit("build oracle/_ref first (oracle/build_ref.sh)")
@@ -199,6 +217,19 @@ def main():
                                  dict(n=900, d=16, seed=46, random_labels=7, groups_of=2, fixed_frac=0.15),
                                  30, cycles=20, k=10, folds=5, stratified=True, evolutionary=True, guarded=True,
                                  absorption=True, seed=9, cv_seed=10))
+    semi_kw = dict(runs=4, cycles=12, landmarks=1000, splitting=20, graph_neighbors=20, folds=5, knn_k=10)
+    cases.append(semi_matrix_case("semi_knn_start_constrain_fixed",
+                                  dict(n=1500, d=12, seed=47, flip=0.3, use_start=True, groups_of=3,
+                                       fixed_frac=0.1), 20, seed=11, **semi_kw))
+    cases.append(semi_matrix_case("semi_knn_constrain", dict(n=1300, d=10, seed=48, groups_of=2), 20,
+                                  seed=12, **semi_kw))
+    cases.append(semi_matrix_case("semi_knn_start_fixed", dict(n=1200, d=16, seed=49, flip=0.4, use_start=True,
+                                                               fixed_frac=0.2), 20, seed=13, **semi_kw))
+    cases.append(semi_matrix_case("semi_pls_start_constrain",
+                                  dict(n=1400, d=14, seed=50, flip=0.3, use_start=True, groups_of=2), 20,
+                                  seed=14, classifier=1, components=4, **semi_kw))
+    cases.append(semi_matrix_case("semi_pls_fixed", dict(n=1100, d=12, seed=51, fixed_frac=0.15), 20, seed=15,
+                                  classifier=1, components=4, **semi_kw))
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py", "cases": cases}, f, indent=1)
     print(f"wrote {len(cases)} cases")

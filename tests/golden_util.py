@@ -54,6 +54,16 @@ def knn_inputs(spec):
     return np.ascontiguousarray(x, np.float32), labels.astype(np.int32), con, fix
 
 
+def semi_inputs(spec):
+    """Semi-supervised KODAMA.matrix case: (x, starting_labels, constrain,
+    fixed) from knn_inputs(spec), the start labels mapped to 3*label - 7 (so
+    they are neither positive nor consecutive); each of the three is kept
+    only where the spec asks for it (use_start, groups_of, fixed_frac)."""
+    x, labels, con, fix = knn_inputs(spec)
+    start = (labels * 3 - 7).astype(np.int32) if spec.get("use_start") else None
+    return x, start, con, fix
+
+
 def check_knncv(case, pred, folds):
     assert sha(folds) == case["folds_sha256"], "folds"
     assert np.asarray(pred)[:32].tolist() == case["predicted_head"], "predictions head"

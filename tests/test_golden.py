@@ -158,3 +158,27 @@ def test_gpu_core_graph_input_golden(kg, case):
     assert G.sha(gi) + ":" + G.sha(gd) == case["graph_sha256"], "exact graph"
     r = kg.CoreKNNGraph(gi, gd, labels, index_base=0, constrain=con, fixed=fix, **_gpu_core_kw(case["options"]))
     G.check_core(case, r, folds_attr="fold_assignments")
+
+
+@pytest.mark.parametrize("case", _cases("kodama_matrix_semi"), ids=lambda c: c["name"])
+def test_oracle_semi_matrix_golden(orc, case):
+    x, start, con, fix = G.semi_inputs(case["input"])
+    gi, gd = orc.exact_knn(x, case["K"], threads=8)
+    assert G.sha(gi) + ":" + G.sha(gd) == case["graph_sha256"], "canonical exact graph"
+    r = orc.kodama_matrix_graph_data(x, gi, gd, 0, threads=8, materialize=1, starting=start, constrain=con,
+                                     fixed=fix, **case["options"])
+    G.check_pls_matrix(case, r)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("raw", [False, True], ids=["graph_input", "raw_data"])
+@pytest.mark.parametrize("case", _cases("kodama_matrix_semi"), ids=lambda c: c["name"])
+def test_gpu_semi_matrix_golden(kg, case, raw):
+    x, start, con, fix = G.semi_inputs(case["input"])
+    graph = None
+    if not raw:
+        graph = kg.knn_graph(x, case["K"])
+        assert G.sha(graph[0]) + ":" + G.sha(graph[1]) == case["graph_sha256"], "exact graph"
+    r = kg.KODAMA_matrix(x, graph, index_base=0, materialize_graph=True, starting_labels=start, constrain=con,
+                         fixed=fix, **case["options"])
+    G.check_pls_matrix(case, r)

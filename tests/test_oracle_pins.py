@@ -111,6 +111,30 @@ def test_pls_matrix_vs_reference(orc):
         assert np.array_equal(getattr(a, f), getattr(b, f)), f
 
 
+@needs_ref
+@pytest.mark.parametrize("classifier", [0, 1])
+@pytest.mark.parametrize("inputs", ["start", "constrain", "fixed", "all"])
+def test_semi_matrix_vs_reference(orc, classifier, inputs):
+    x, y = datasets.gaussian_mixture(n=1500, d=12, seed=8)
+    gi, gd = orc.exact_knn(x, 20, threads=8)
+    rng = np.random.default_rng(3)
+    n = len(x)
+    start = (y % 5 + 1).astype(np.int32)
+    flip = rng.random(n) < 0.3
+    start[flip] = rng.integers(1, 6, int(flip.sum()))
+    con = (rng.integers(0, 600, n) * 3 + 7).astype(np.int32)
+    fix = (rng.random(n) < 0.1).astype(np.int32)
+    extra = dict(starting=start if inputs in ("start", "all") else None,
+                 constrain=con if inputs in ("constrain", "all") else None,
+                 fixed=fix if inputs in ("fixed", "all") else None)
+    kw = dict(runs=4, cycles=10, landmarks=1000, splitting=20, graph_neighbors=20, folds=5, knn_k=10, threads=4,
+              materialize=1, classifier=classifier, components=4)
+    a = ref.kodama_matrix_graph_data(x, gi, gd, 0, seed=11, **extra, **kw)
+    b = orc.kodama_matrix_graph_data(x, gi, gd, 0, seed=11, **extra, **kw)
+    for f in ("res", "acc", "v", "hashes", "run_counters", "cycle_diag", "knn_idx", "knn_dist", "pls_counters"):
+        assert np.array_equal(getattr(a, f), getattr(b, f)), f
+
+
 def _clustered(n, d, seed):
     rng = np.random.default_rng(seed)
     sizes = [n // 3, n // 3, n - 2 * (n // 3)]
