@@ -13,6 +13,7 @@
 #include "launch_count.cuh"
 #include "pls.cuh"
 #include "mlp.cuh"
+#include "plan.cuh"
 
 #include <cuda_runtime.h>
 
@@ -103,6 +104,7 @@ class Ctx {
     for (void* p : bufs_) cudaFreeAsync(p, stream_);
     cudaStreamSynchronize(stream_);
     for (int i = 0; i < nev_; ++i) cudaEventDestroy(ev_[i]);
+    for (int i = 0; i < njoin_; ++i) cudaEventDestroy(join_[i]);
     cudaStreamDestroy(side_);
     cudaStreamDestroy(stream_);
   }
@@ -112,6 +114,16 @@ class Ctx {
   void fork() {
     const int e = mark();
     ck(cudaStreamWaitEvent(side_, ev_[e], 0), "cudaStreamWaitEvent");
+  }
+  // side stream waits for event e only; join() makes the main stream wait for
+  // everything queued on the side stream so far.
+  void fork_after(int e) { ck(cudaStreamWaitEvent(side_, ev_[e], 0), "cudaStreamWaitEvent"); }
+  void join() {
+    if (njoin_ >= kMaxEvents) fail(KGB_EINTERNAL, "too many stream joins");
+    ck(cudaEventCreateWithFlags(&join_[njoin_], cudaEventDisableTiming), "cudaEventCreate");
+    ck(cudaEventRecord(join_[njoin_], side_), "cudaEventRecord");
+    ck(cudaStreamWaitEvent(stream_, join_[njoin_], 0), "cudaStreamWaitEvent");
+    ++njoin_;
   }
   // Copies device memory to the host as soon as event e has completed, on the
   // side stream, and waits for that copy only (the main stream runs on).
@@ -169,6 +181,8 @@ class Ctx {
   std::vector<void*> bufs_;
   cudaEvent_t ev_[kMaxEvents];
   int nev_ = 0;
+  cudaEvent_t join_[kMaxEvents];
+  int njoin_ = 0;
 };
 
 // Pinned host staging for large device-to-host results (one buffer per host
@@ -284,6 +298,14 @@ void constrained_majority(int* labels, const int* groups, size_t n) {
   std::map<int, int> lab;
   for (const auto& kv : by) lab[kv.first] = majority_value(kv.second);
   for (size_t i = 0; i < n; ++i) labels[i] = lab[groups[i]];
+}
+
+// Status word of the device landmark planning (plan.cu): non-zero when the
+// atlas labels or the quota allocation were inconsistent.
+void check_plan_status(const int* d_status) {
+  int v = 0;
+  ck(cudaMemcpy(&v, d_status, sizeof(int), cudaMemcpyDeviceToHost), "D2H");
+  if (v != 0) fail(KGB_EINTERNAL, "Landmark quota allocation produced the wrong sample size.");
 }
 
 int host_threads(int requested) {
@@ -817,28 +839,49 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     build_graph();
     ev_graph = ctx.mark();
   }
-  std::vector<int> atlas(static_cast<size_t>(n));
-  ctx.download_after(atlas.data(), d_atlas_labels, n, ev_atlas);
   out->timings[2] = clk.lap();
 
-  // per-run landmarks and k-means seeds (host, libstdc++ streams)
-  const kgb::Strata strata = kgb::index_strata(atlas, coarse_k);
+  // per-run landmarks and k-means seeds, drawn on the device from the atlas
+  // (side stream, beside the graph build); quota_sample returns exactly
+  // min(target, n) rows
   const int init_k = std::max(2, std::min(splitting, landmarks));
   const int kk = std::max(1, std::min(init_k, landmarks));
-  std::vector<kgb::RunPlan> plans(static_cast<size_t>(M));
-  Clock plan_clock;
   const int r0 = o->first_run > 0 ? o->first_run : 1;
-  parallel_for(M, host_threads(o->host_threads), [&](int r) {
-    plans[r] = kgb::plan_run(strata, landmarks, init_k, seed, r0 + r);
-  });
-  out->timings[5] = plan_clock.lap();
-  const int L = static_cast<int>(plans[0].landmarks.size());
-  std::vector<int> land(static_cast<size_t>(M) * L), init_rows(static_cast<size_t>(M) * kk);
-  for (int r = 0; r < M; ++r) {
-    std::copy(plans[r].landmarks.begin(), plans[r].landmarks.end(), land.begin() + static_cast<size_t>(r) * L);
-    std::copy(plans[r].init_rows.begin(), plans[r].init_rows.end(), init_rows.begin() + static_cast<size_t>(r) * kk);
+  const int L = landmarks;
+  int* d_land = ctx.alloc<int>(static_cast<size_t>(M) * L);
+  int* d_nonland = pls && n > L ? ctx.alloc<int>(static_cast<size_t>(M) * (n - L)) : nullptr;
+  int* d_plan_init = ctx.alloc<int>(static_cast<size_t>(M) * kk);
+  uint64_t* d_land_hash = ctx.alloc<uint64_t>(M);
+  int* d_plan_status = ctx.alloc<int>(1);
+  {
+    ck(cudaMemsetAsync(d_plan_status, 0, sizeof(int), st), "memset");
+    kgb::PlanArgs pa;
+    pa.n = n;
+    pa.strata = coarse_k;
+    pa.target = L;
+    pa.init_k = kk;
+    pa.runs = M;
+    pa.first_run = r0;
+    pa.seed = seed;
+    pa.atlas = d_atlas_labels;
+    pa.land = d_land;
+    pa.nonland = d_nonland;
+    pa.init_rows = d_plan_init;
+    pa.land_hash = d_land_hash;
+    pa.status = d_plan_status;
+    pa.scratch = ctx.alloc<char>(kgb::plan_scratch_bytes(n, coarse_k, L, M));
+    ctx.fork_after(ev_atlas);
+    ck_launch(kgb::plan_landmarks(pa, ctx.side()), "landmark planning");
+    ctx.join();
   }
-  int* d_land = ctx.upload(land.data(), land.size());
+  out->timings[5] = 0.0;
+  std::vector<int> land;  // host copy, semi-supervised inputs only
+  if (o->starting_labels != nullptr || o->constrain != nullptr || o->fixed != nullptr) {
+    land.resize(static_cast<size_t>(M) * L);
+    ctx.download(land.data(), d_land, land.size());
+    ctx.sync();
+    check_plan_status(d_plan_status);
+  }
   int* d_init_labels = ctx.alloc<int>(static_cast<size_t>(M) * L);
   // semi-supervised inputs (run_kodama_matrix, kodama_matrix.cpp:3405-3420;
   // run_iteration :3060-3117): starting labels replace the k-means start,
@@ -873,7 +916,7 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     B.x = d_x;
     B.rows = d_land;
     B.pnorm = d_pnorm;
-    B.init_rows = ctx.upload(init_rows.data(), init_rows.size());
+    B.init_rows = d_plan_init;
     B.split_uniform = d_split;
     B.cent = ctx.alloc<float>(static_cast<size_t>(M) * kk * d);
     B.cnorm = ctx.alloc<float>(static_cast<size_t>(M) * kk);
@@ -1060,15 +1103,7 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     eb = run_pls_evolution(ctx, P, b, C0max, true, pol);
     ev_evo1 = ctx.mark();
     const int NV = n - L;
-    std::vector<int> test_rows(static_cast<size_t>(M) * std::max(NV, 0));
-    for (int r = 0; r < M; ++r) {
-      std::vector<char> is_land(static_cast<size_t>(n), 0);
-      for (int i = 0; i < L; ++i) is_land[land[static_cast<size_t>(r) * L + i]] = 1;
-      size_t q = static_cast<size_t>(r) * NV;
-      for (int t = 0; t < n; ++t)
-        if (!is_land[t]) test_rows[q++] = t;
-    }
-    int* d_test = test_rows.empty() ? ctx.alloc<int>(1) : ctx.upload(test_rows.data(), test_rows.size());
+    int* d_test = d_nonland != nullptr ? d_nonland : ctx.alloc<int>(1);
     d_res = ctx.alloc<int>(static_cast<size_t>(M) * n);
     uint16_t* d_proj = ctx.alloc<uint16_t>(static_cast<size_t>(M) * std::max(NV, 1));
     if (NV > 0) {
@@ -1228,7 +1263,12 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     }
   }
   const int ev_dis = ctx.mark();
+  std::vector<uint64_t> land_hash(static_cast<size_t>(M));
+  int plan_status = 0;
+  ctx.download(land_hash.data(), d_land_hash, land_hash.size());
+  ctx.download(&plan_status, d_plan_status, 1);
   ctx.sync();
+  if (plan_status != 0) fail(KGB_EINTERNAL, "Landmark quota allocation produced the wrong sample size.");
   if (res_stage != nullptr) std::memcpy(out->res, res_stage, res_bytes);
   const double t_dl = clk.lap();
   if (graph_here) {
@@ -1273,7 +1313,7 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   for (int r = 0; r < M; ++r) {
     out->acc[r] = best[2 * r];
     if (out->run_hashes) {
-      out->run_hashes[3 * r + 0] = plans[r].landmark_hash;
+      out->run_hashes[3 * r + 0] = land_hash[r];
       out->run_hashes[3 * r + 1] = init_hash[r];
       out->run_hashes[3 * r + 2] = fold_plans[r].fold_hash;
     }

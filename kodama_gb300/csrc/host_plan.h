@@ -1,9 +1,9 @@
-// Host-side planning of the per-run random choices that precede the device
-// work: landmark atlas strata, landmark quota sampling, fold assignment and
-// k-means seeding.  These are serial draws from the reference's per-run
-// std::mt19937_64 streams and are made here with the same libstdc++ engines
-// and algorithms the reference uses, so each run sees the reference's exact
-// landmark rows, folds and initial centroids.
+// Host-side planning of the data-independent random choices that precede the
+// device work: fold assignment and the atlas k-means seeding.  These are
+// serial draws from the reference's std::mt19937_64 streams and are made here
+// with the same libstdc++ engines and algorithms the reference uses.  The
+// per-run landmark quota sample depends on the atlas and is drawn on the
+// device (plan.cu).
 #pragma once
 
 #include <cstddef>
@@ -13,25 +13,6 @@
 
 namespace kgb {
 
-struct Strata {
-  std::vector<int> offsets, rows;
-};
-
-// index_strata (kodama_matrix.cpp:806-828); labels are 1..strata.
-Strata index_strata(const std::vector<int>& labels, int strata);
-
-// One KODAMA.matrix run's plan (run_iteration, kodama_matrix.cpp:2897-2939 and
-// :3091-3103): rng(seed+run); discard one draw; quota-sample landmarks; then
-// the init k-means seed.
-struct RunPlan {
-  std::vector<int> landmarks;       // sorted global rows, size L
-  std::vector<int> init_rows;       // init_k initial centroid rows (indices into landmarks)
-  uint64_t landmark_hash = 0;
-};
-
-// Landmarks and initial centroid rows of one run (needs the atlas strata).
-RunPlan plan_run(const Strata& strata, int landmarks, int init_k, uint64_t seed, int run);
-
 // Folds of one run over L landmarks with the identity constraint, not
 // stratified (make_folds, common.cpp:180-189): independent of the data, so
 // they can be planned while the device builds the graph and the atlas.
@@ -40,9 +21,6 @@ struct FoldPlan {
   uint64_t fold_hash = 0;
 };
 FoldPlan plan_folds(int L, int folds, uint64_t seed, int run);
-
-// quota_sample_landmarks (kodama_matrix.cpp:856-944, preserve_strata_order=false).
-std::vector<int> quota_sample(const Strata& st, int target, std::mt19937_64& rng);
 
 // First `needed` entries of the FAISS-compatible permutation
 // (kodama_matrix.cpp:535-564) seeded with `seed`.
