@@ -136,6 +136,40 @@ int kgb_kodama_matrix(const float* x, int32_t n, int32_t d, const kgb_matrix_opt
 int kgb_kodama_matrix_resident(const float* x_device, int32_t n, int32_t d, const kgb_matrix_options* opt,
                                kgb_matrix_result* out);
 
+/* A batch of independent KODAMA.matrix problems (each as kgb_kodama_matrix
+ * with raw data; no semi-supervised inputs, learned proposal or snapshots).
+ * Not a reference entry point: the reference runs such a batch as separate
+ * KODAMAMatrix calls, and every problem's result here equals that call's.
+ * All problems are captured into one CUDA graph of `lanes` independent
+ * chains; the schedule is autotuned on the first call for a batch shape
+ * (lanes/order 0) and the graph is replayed while the shape stays. */
+typedef struct kgb_matrix_problem {
+  const float* x;               /* n x d, row-major, host memory */
+  int32_t n, d;
+  kgb_matrix_options options;   /* options.device is ignored (the batch's device is used) */
+  kgb_matrix_result* result;    /* host buffers, as for kgb_kodama_matrix */
+} kgb_matrix_problem;
+
+typedef struct kgb_batch_options {
+  int32_t device;
+  int32_t lanes;                /* concurrent chains, 1..64; 0 = autotuned */
+  int32_t order;                /* 1 = longest first to the least loaded lane, 2 = round robin; 0 = autotuned */
+  int32_t reserved;
+} kgb_batch_options;
+
+typedef struct kgb_batch_report {
+  int32_t lanes, order;         /* the schedule used */
+  int32_t graph_nodes;          /* nodes of the captured graph */
+  int32_t kernel_nodes;         /* kernel launches per replay */
+  int32_t rebuilt;              /* 1 = this call captured (and possibly tuned) the graph */
+  int32_t reserved;
+  double device_ms;             /* CUDA-event time of the graph launch */
+  double tune_ms;               /* host wall time spent autotuning in this call */
+} kgb_batch_report;
+
+int kgb_kodama_matrix_batch(const kgb_matrix_problem* problems, int32_t count, const kgb_batch_options* options,
+                            kgb_batch_report* report);
+
 /* Replaces KODAMAMatrixFromGraphData_CUDA (kodama.hpp:1215-1222,
  * kodama_matrix.cpp:4676-4699): data plus a caller graph (n x gk, indices
  * zero- or one-based: index_base 0, 1, or -1 = auto as GraphIndexBase::Auto). */

@@ -25,7 +25,7 @@ import numpy as np
 
 from . import _native as N
 
-__all__ = ["train_proposal", "proposal_gradient", "proposal_predict", "KODAMA_matrix", "CoreKNNGraph", "CoreKNNGraph_batch", "knn_graph",
+__all__ = ["KODAMA_matrix_batch", "train_proposal", "proposal_gradient", "proposal_predict", "KODAMA_matrix", "CoreKNNGraph", "CoreKNNGraph_batch", "knn_graph",
            "KODAMADissimilarityInPlace", "PLSLDACV", "PLSLDAPredict", "CorePLSLDA", "PLSCVResult", "MatrixResult", "CoreResult", "EvolutionPolicy",
            "library_path", "version", "launch_count"]
 
@@ -245,6 +245,95 @@ def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitt
         snap_f[: runs * out.effective_landmarks * 8].reshape(runs, out.effective_landmarks, 8),
         snapshot_flags=None if snap_g is None else
         snap_g[: runs * out.effective_landmarks].reshape(runs, out.effective_landmarks))
+
+
+@dataclass
+class BatchReport:
+    """Schedule and timing of one kgb_kodama_matrix_batch call."""
+    lanes: int
+    order: int
+    graph_nodes: int
+    kernel_nodes: int
+    rebuilt: bool
+    device_ms: float
+    tune_ms: float
+
+
+def KODAMA_matrix_batch(problems, *, runs=100, cycles=20, landmarks=10000, splitting=0, graph_neighbors=100,
+                        folds=5, knn_k=30, seed=1234, components=50, policy="full", device=0, lanes=0,
+                        order=0, materialize_graph=False, apply_dissimilarity=True):
+    """Independent KODAMA.matrix problems in one captured CUDA graph.
+
+    ``problems``: list of dicts with ``x`` (n x d float32) and optionally
+    ``classifier`` ("knn" / "pls") and any per-problem override of the
+    keyword options.  Returns (list of MatrixResult, BatchReport); each result
+    equals KODAMA_matrix on that problem alone.  ``lanes`` / ``order`` fix the
+    schedule (0 = autotuned on the first call for this batch shape)."""
+    count = len(problems)
+    if count < 1:
+        raise ValueError("a batch needs at least one problem")
+    base = dict(runs=runs, cycles=cycles, landmarks=landmarks, splitting=splitting,
+                graph_neighbors=graph_neighbors, folds=folds, knn_k=knn_k, seed=seed, components=components)
+    arr = (N.MatrixProblem * count)()
+    keep, outs = [], []
+    for i, pr in enumerate(problems):
+        x = np.ascontiguousarray(pr["x"], dtype=np.float32)
+        if x.ndim != 2:
+            raise ValueError("x must be a 2-D matrix")
+        n, d = x.shape
+        kw = {k: pr.get(k, v) for k, v in base.items()}
+        cls = {"knn": 0, "pls": 1, "pls-lda": 1, 0: 0, 1: 1}.get(pr.get("classifier", "knn"))
+        if cls is None:
+            raise ValueError("Unsupported KODAMA.matrix classifier.")
+        opt = _matrix_options(kw["runs"], kw["cycles"], kw["landmarks"], kw["splitting"], kw["graph_neighbors"],
+                              kw["folds"], kw["knn_k"], kw["seed"], materialize_graph, apply_dissimilarity,
+                              device, 0, policy, 1, cls, kw["components"])
+        M, T = kw["runs"], kw["cycles"]
+        b = dict(x=x, res=np.zeros((M, n), np.int32), acc=np.zeros(M, np.float64),
+                 v=np.zeros((M, max(T, 0)), np.float64), hashes=np.zeros((M, 3), np.uint64),
+                 counters=np.zeros((M, 8), np.int32), cdiag=np.zeros((M, max(T, 0), 5), np.int32),
+                 plsc=np.zeros((M, 2), np.int32))
+        cap = max(1, min(kw["graph_neighbors"] if kw["graph_neighbors"] > 0 else 100, n))
+        if materialize_graph:
+            b["kidx"] = np.zeros((n, cap), np.int32)
+            b["kdist"] = np.zeros((n, cap), np.float32)
+        out = N.MatrixResult()
+        out.res = b["res"].ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+        out.acc = b["acc"].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        out.v = b["v"].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        out.run_hashes = b["hashes"].ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))
+        out.run_counters = b["counters"].ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+        out.cycle_diag = b["cdiag"].ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+        out.pls_counters = b["plsc"].ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+        if materialize_graph:
+            out.knn_idx = b["kidx"].ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+            out.knn_dist = b["kdist"].ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        out.knn_cap = cap
+        b["out"] = out
+        arr[i].x = x.ctypes.data
+        arr[i].n = n
+        arr[i].d = d
+        arr[i].options = opt
+        arr[i].result = ctypes.pointer(out)
+        keep.append(b)
+    bo = N.BatchOptions(device=device, lanes=lanes, order=order, reserved=0)
+    rep = N.BatchReport()
+    N.check(N.load().kgb_kodama_matrix_batch(arr, count, ctypes.byref(bo), ctypes.byref(rep)))
+    for b in keep:
+        out = b["out"]
+        k = out.knn_k
+        outs.append(MatrixResult(
+            res=b["res"], acc=b["acc"], v=b["v"], run_hashes=b["hashes"], run_counters=b["counters"],
+            cycle_diag=b["cdiag"],
+            knn_idx=b["kidx"][:, :k].copy() if (materialize_graph and k) else None,
+            knn_dist=b["kdist"][:, :k].copy() if (materialize_graph and k) else None,
+            effective_landmarks=out.effective_landmarks,
+            timings=dict(zip(_TIMING_NAMES, list(out.timings))),
+            kernel_ms=dict(zip(_KERNEL_NAMES, list(out.kernel_ms))), pls_counters=b["plsc"],
+            snapshot_features=None, snapshot_flags=None))
+    return outs, BatchReport(lanes=rep.lanes, order=rep.order, graph_nodes=rep.graph_nodes,
+                             kernel_nodes=rep.kernel_nodes, rebuilt=bool(rep.rebuilt), device_ms=rep.device_ms,
+                             tune_ms=rep.tune_ms)
 
 
 def launch_count() -> int:

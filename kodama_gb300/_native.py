@@ -20,6 +20,7 @@ EXPORTED = (
     "kgb_kodama_matrix",
     "kgb_kodama_matrix_from_graph_data",
     "kgb_kodama_matrix_resident",
+    "kgb_kodama_matrix_batch",
     "kgb_launch_count",
     "kgb_core_knn_graph",
     "kgb_core_knn_graph_batch",
@@ -81,6 +82,21 @@ class MatrixResult(ctypes.Structure):
     ]
 
 
+class MatrixProblem(ctypes.Structure):
+    _fields_ = [("x", ctypes.c_void_p), ("n", ctypes.c_int32), ("d", ctypes.c_int32),
+                ("options", MatrixOptions), ("result", ctypes.POINTER(MatrixResult))]
+
+
+class BatchOptions(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int32) for n in ("device", "lanes", "order", "reserved")]
+
+
+class BatchReport(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int32) for n in ("lanes", "order", "graph_nodes", "kernel_nodes", "rebuilt",
+                                              "reserved")] + [("device_ms", ctypes.c_double),
+                                                              ("tune_ms", ctypes.c_double)]
+
+
 class CoreOptions(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int32) for n in (
         "cycles", "k", "folds", "stratified", "evolutionary_search", "guarded_diversity",
@@ -136,6 +152,8 @@ def load():
     lib.kgb_kodama_matrix.argtypes = [P, i32, i32, ctypes.POINTER(MatrixOptions), ctypes.POINTER(MatrixResult)]
     lib.kgb_kodama_matrix_resident.argtypes = [P, i32, i32, ctypes.POINTER(MatrixOptions),
                                                ctypes.POINTER(MatrixResult)]
+    lib.kgb_kodama_matrix_batch.argtypes = [ctypes.POINTER(MatrixProblem), i32, ctypes.POINTER(BatchOptions),
+                                            ctypes.POINTER(BatchReport)]
     lib.kgb_launch_count.restype = ctypes.c_int64
     lib.kgb_launch_count.argtypes = []
     lib.kgb_kodama_matrix_from_graph_data.argtypes = [

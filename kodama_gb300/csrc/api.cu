@@ -22,6 +22,9 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <cstdio>
+#include <memory>
+#include <mutex>
 #include <exception>
 #include <functional>
 #include <future>
@@ -81,10 +84,71 @@ int guarded(F&& f) {
   }
 }
 
+// Pinned host memory of a captured batch.  A CUDA graph replays its copies at
+// every launch, so the host side of each copy must outlive the capture: the
+// sources of host-to-device copies are kept here, and device-to-host copies
+// land here and are delivered to their host destinations after each launch.
+class CaptureArena {
+ public:
+  CaptureArena() = default;
+  CaptureArena(const CaptureArena&) = delete;
+  CaptureArena& operator=(const CaptureArena&) = delete;
+  ~CaptureArena() {
+    for (void* p : blocks_) cudaFreeHost(p);
+  }
+  void* keep(const void* src, size_t bytes) {
+    void* p = get(bytes);
+    if (bytes) std::memcpy(p, src, bytes);
+    return p;
+  }
+  void* slot(void* dst, size_t bytes) {
+    void* p = get(bytes);
+    posts_.push_back(Post{dst, p, bytes});
+    return p;
+  }
+  void deliver() const {
+    for (const Post& q : posts_) std::memcpy(q.dst, q.src, q.bytes);
+  }
+
+ private:
+  void* get(size_t bytes) {
+    bytes = (std::max<size_t>(bytes, 1) + 63) / 64 * 64;
+    if (bytes > left_) {
+      const size_t cap = std::max<size_t>(bytes, size_t(8) << 20);
+      void* p = nullptr;
+      ck(cudaMallocHost(&p, cap), "cudaMallocHost");
+      blocks_.push_back(p);
+      cur_ = static_cast<char*>(p);
+      left_ = cap;
+    }
+    void* p = cur_;
+    cur_ += bytes;
+    left_ -= bytes;
+    return p;
+  }
+  struct Post {
+    void* dst;
+    const void* src;
+    size_t bytes;
+  };
+  std::vector<void*> blocks_;
+  std::vector<Post> posts_;
+  char* cur_ = nullptr;
+  size_t left_ = 0;
+};
+
 // Per-call device context: device selection, one stream, stream-ordered
-// allocations released when the call ends.
+// allocations released when the call ends.  In capture mode the context
+// enqueues into two streams of a batch being captured into a CUDA graph: no
+// host synchronisation, host copies through the batch's pinned arena, and the
+// allocations freed inside the graph (release()).
 class Ctx {
  public:
+  Ctx(int device, cudaStream_t main, cudaStream_t side, CaptureArena* arena)
+      : stream_(main), side_(side), arena_(arena), owns_streams_(false) {
+    ck(cudaSetDevice(device), "cudaSetDevice");
+    ck(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, device), "device attribute");
+  }
   explicit Ctx(int device) {
     int count = 0;
     if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) fail(KGB_ECUDA, "no CUDA device is available");
@@ -100,13 +164,29 @@ class Ctx {
     }
   }
   ~Ctx() {
-    cudaStreamSynchronize(side_);  // side-stream work reads buffers freed below
-    for (void* p : bufs_) cudaFreeAsync(p, stream_);
-    cudaStreamSynchronize(stream_);
+    if (owns_streams_) {
+      cudaStreamSynchronize(side_);  // side-stream work reads buffers freed below
+      for (void* p : bufs_) cudaFreeAsync(p, stream_);
+      cudaStreamSynchronize(stream_);
+    }
     for (int i = 0; i < nev_; ++i) cudaEventDestroy(ev_[i]);
     for (int i = 0; i < njoin_; ++i) cudaEventDestroy(join_[i]);
-    cudaStreamDestroy(side_);
-    cudaStreamDestroy(stream_);
+    if (owns_streams_) {
+      cudaStreamDestroy(side_);
+      cudaStreamDestroy(stream_);
+    }
+  }
+  bool capturing() const { return arena_ != nullptr; }
+  // Capture mode: joins the side stream and frees every allocation inside the
+  // graph, after all the work queued so far.
+  void release() {
+    join();
+    for (void* p : bufs_) ck(cudaFreeAsync(p, stream_), "cudaFreeAsync");
+    bufs_.clear();
+  }
+  // A host wait for timing or for host-side steps; skipped inside a capture.
+  void checkpoint() {
+    if (!capturing()) sync();
   }
   // side stream for work that overlaps the main stream: fork() makes it wait
   // for everything queued on the main stream so far.
@@ -142,7 +222,7 @@ class Ctx {
   }
   double ms(int a, int b) {
     float v = 0.0f;
-    if (a < 0 || b < 0 || cudaEventElapsedTime(&v, ev_[a], ev_[b]) != cudaSuccess) return 0.0;
+    if (capturing() || a < 0 || b < 0 || cudaEventElapsedTime(&v, ev_[a], ev_[b]) != cudaSuccess) return 0.0;
     return static_cast<double>(v);
   }
   Ctx(const Ctx&) = delete;
@@ -159,14 +239,26 @@ class Ctx {
   template <class T>
   T* upload(const T* host, size_t count) {
     T* d = alloc<T>(count);
-    if (count) ck(cudaMemcpyAsync(d, host, count * sizeof(T), cudaMemcpyHostToDevice, stream_), "H2D");
+    h2d(d, host, count);
     return d;
+  }
+  // host -> existing device buffer, on the main stream
+  template <class T>
+  void h2d(T* dev, const T* host, size_t count) {
+    if (!count) return;
+    const void* src = capturing() ? arena_->keep(host, count * sizeof(T)) : static_cast<const void*>(host);
+    ck(cudaMemcpyAsync(dev, src, count * sizeof(T), cudaMemcpyHostToDevice, stream_), "H2D");
   }
   template <class T>
   void download(T* host, const T* dev, size_t count) {
-    if (count) ck(cudaMemcpyAsync(host, dev, count * sizeof(T), cudaMemcpyDeviceToHost, stream_), "D2H");
+    download_on(stream_, host, dev, count);
+  }
+  template <class T>
+  void download_side(T* host, const T* dev, size_t count) {
+    download_on(side_, host, dev, count);
   }
   void sync() {
+    if (capturing()) fail(KGB_EINTERNAL, "host synchronisation inside a captured batch");
     ck(cudaStreamSynchronize(stream_), "stream synchronize");
     ck(cudaStreamSynchronize(side_), "stream synchronize");
   }
@@ -174,9 +266,17 @@ class Ctx {
   int sms() const { return sms_; }
 
  private:
+  template <class T>
+  void download_on(cudaStream_t s, T* host, const T* dev, size_t count) {
+    if (!count) return;
+    void* dst = capturing() ? arena_->slot(host, count * sizeof(T)) : static_cast<void*>(host);
+    ck(cudaMemcpyAsync(dst, dev, count * sizeof(T), cudaMemcpyDeviceToHost, s), "D2H");
+  }
   static constexpr int kMaxEvents = 32;
   cudaStream_t stream_ = nullptr;
   cudaStream_t side_ = nullptr;
+  CaptureArena* arena_ = nullptr;
+  bool owns_streams_ = true;
   int sms_ = 1;
   std::vector<void*> bufs_;
   cudaEvent_t ev_[kMaxEvents];
@@ -597,12 +697,11 @@ void pls_enable_gram(Ctx& ctx, PlsBuffers& b) {
   std::vector<uint8_t> want(static_cast<size_t>(S));
   for (int s2 = 0; s2 < S; ++s2) want[s2] = p <= b.ntrain[s2] ? 1 : 0;
   uint8_t* d_want = const_cast<uint8_t*>(b.ev.use_gram);
-  ck(cudaMemcpyAsync(d_want, want.data(), want.size(), cudaMemcpyHostToDevice, ctx.stream()), "H2D");
+  ctx.h2d(d_want, want.data(), want.size());
   b.prep.gram = ctx.alloc<float>(static_cast<size_t>(S) * p * p);
   ck_launch(kgb::pls_build_gram(b.prep, d_want, ctx.stream()), "fold Gram");
   b.ev.gram = b.prep.gram;
   b.ev.tiles_after_s = std::all_of(want.begin(), want.end(), [](uint8_t v) { return v != 0; }) ? 0 : 1;
-  ctx.sync();  // `want` is a host temporary
 }
 
 // Host class lists of coded labels: rows grouped by code, ascending within.
@@ -616,22 +715,39 @@ void class_lists_host(const std::vector<uint16_t>& codes, int C0max, std::vector
   for (size_t i = 0; i < codes.size(); ++i) rows[pos[codes[i]]++] = static_cast<uint16_t>(i);
 }
 
-void pls_check_status(Ctx& ctx, const PlsBuffers& b) {
-  std::vector<int> status(static_cast<size_t>(b.S));
-  ctx.download(status.data(), b.ev.status, status.size());
-  ctx.sync();
-  for (int s2 = 0; s2 < b.S; ++s2) {
-    if (!b.present[s2]) continue;
+// Status words of PLS-LDA fits read back after the call's work: with a sink
+// the check is deferred to pls_status_check (the captured batch path).
+struct PlsStatusSink {
+  std::vector<std::vector<int>> status;
+  std::vector<std::vector<uint8_t>> present;
+};
+
+void pls_status_check(const std::vector<int>& status, const std::vector<uint8_t>& present) {
+  for (size_t s2 = 0; s2 < status.size(); ++s2) {
+    if (!present[s2]) continue;
     if (status[s2] == 1) fail(KGB_EINTERNAL, "CPU float32 SIMPLS found no supervised latent direction.");
     if (status[s2] == 2) fail(KGB_EINTERNAL, "Float32 PLS-LDA Cholesky factorization failed.");
   }
+}
+
+void pls_check_status(Ctx& ctx, const PlsBuffers& b, PlsStatusSink* sink = nullptr) {
+  if (sink != nullptr) {
+    sink->status.emplace_back(static_cast<size_t>(b.S));
+    sink->present.emplace_back(b.present.begin(), b.present.end());
+    ctx.download(sink->status.back().data(), b.ev.status, static_cast<size_t>(b.S));
+    return;
+  }
+  std::vector<int> status(static_cast<size_t>(b.S));
+  ctx.download(status.data(), b.ev.status, status.size());
+  ctx.sync();
+  pls_status_check(status, std::vector<uint8_t>(b.present.begin(), b.present.end()));
 }
 
 // maximize_core with the PLS-LDA predictor for P.problems problems whose
 // slices are in `b`: the cycle loop of alternating evolution steps and CV
 // evaluations.  P carries everything but the outputs and scratch.
 EvolveBuffers run_pls_evolution(Ctx& ctx, kgb::EvolveParams P, PlsBuffers& b, int C0max, bool coarsening,
-                                const kgb_policy& pol) {
+                                const kgb_policy& pol, PlsStatusSink* sink = nullptr) {
   const int problems = P.problems, L = P.L, T = P.T;
   cudaStream_t st = ctx.stream();
   EvolveBuffers eb;
@@ -732,7 +848,7 @@ EvolveBuffers run_pls_evolution(Ctx& ctx, kgb::EvolveParams P, PlsBuffers& b, in
     Q.cycle = cycle;
     ck_launch(kgb::evolve_pls_launch(Q, grid, smem, st), "PLS evolution step");
   }
-  pls_check_status(ctx, b);
+  pls_check_status(ctx, b, sink);
   // leave the best labels' class lists in b.ev for a projection
   b.ev.labels = eb.clbest;
   return eb;
@@ -773,13 +889,34 @@ void tc_kmeans_inputs(Ctx& ctx, kgb::KMeansBatch& B, const float* d_x, int n, in
   B.cl = ctx.alloc<uint16_t>(static_cast<size_t>(B.problems) * B.k * split.dp);
 }
 
+// Host side of one KODAMA.matrix call between its enqueue and its finalize:
+// where the results land when the device work completes, and what the
+// finalize needs to fill kgb_matrix_result.
+struct MatrixTail {
+  int n = 0, K = 0, M = 0, T = 0, L = 0, r0 = 1, cstride = 16;
+  bool pls = false, want_graph = false, apply_dissimilarity = false, graph_here = false;
+  void* res_stage = nullptr;  // pinned copy of res (host results only)
+  size_t res_bytes = 0;
+  std::vector<double> best, v;
+  std::vector<int> psize, active, counters;
+  std::vector<uint8_t> flags;
+  std::vector<uint64_t> land_hash, init_hash, fold_hash;
+  int plan_status = 0;
+  PlsStatusSink pls_status;
+  std::vector<int> gi;
+  std::vector<float> gd;
+  int ev_start = -1, ev_atlas = -1, ev_graph = -1, ev_init = -1, ev_tables = -1, ev_evo0 = -1, ev_evo1 = -1,
+      ev_proj = -1, ev_dis = -1;
+};
+
 // build_graph (may be empty): queues the kNN graph into d_gidx / d_gdist; it
-// runs right after the atlas k-means, so the host plans the runs while the
-// device builds the graph.
+// runs right after the atlas k-means, beside the landmark planning.  Queues
+// the whole call; the results are read by matrix_finalize once the device
+// work is done (no host wait on the plain path, so a batch can capture it).
 void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_gidx, float* d_gdist, int K,
                               const kgb_matrix_options* o, kgb_matrix_result* out, Clock& clk, int ev_start,
                               int ev_graph, std::future<std::vector<kgb::FoldPlan>>& folds_future,
-                              const std::function<void()>& build_graph = {}) {
+                              MatrixTail& tail, const std::function<void()>& build_graph = {}) {
   const kgb_policy pol = policy_is_zero(o->policy) ? default_policy() : o->policy;
   int landmarks = o->landmarks > 0 ? o->landmarks : 10000;
   if (landmarks >= n) landmarks = static_cast<int>(std::ceil(static_cast<double>(n) * 0.75));
@@ -1007,9 +1144,8 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     ctx.fork();
     ck_launch(kgb::fnv_rows(d_init_labels, M, L, d_init_hash, ctx.side()), "label hashes");
   }
-  std::vector<uint64_t> init_hash(static_cast<size_t>(M));
-  ck(cudaMemcpyAsync(init_hash.data(), d_init_hash, sizeof(uint64_t) * M, cudaMemcpyDeviceToHost, ctx.side()),
-     "D2H");
+  tail.init_hash.assign(static_cast<size_t>(M), 0);
+  ctx.download_side(tail.init_hash.data(), d_init_hash, static_cast<size_t>(M));
   out->timings[7] = 0.0;
   out->timings[3] = clk.lap();
 
@@ -1100,7 +1236,7 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     PlsBuffers b = pls_buffers(ctx, d_xl, M, L, p, sl, C0max, comps, comps, true, true, nullptr, 0);
     ev_tables = ctx.mark();
     ev_evo0 = ev_tables;
-    eb = run_pls_evolution(ctx, P, b, C0max, true, pol);
+    eb = run_pls_evolution(ctx, P, b, C0max, true, pol, &tail.pls_status);
     ev_evo1 = ctx.mark();
     const int NV = n - L;
     int* d_test = d_nonland != nullptr ? d_nonland : ctx.alloc<int>(1);
@@ -1116,14 +1252,14 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
       pb.ev.class_off = b.ev.class_off;
       pb.ev.class_rows = b.ev.class_rows;
       ck_launch(kgb::pls_evaluate(pb.ev, st), "PLS-LDA projection");
-      pls_check_status(ctx, pb);
+      pls_check_status(ctx, pb, &tail.pls_status);
       d_proj = pb.ev.pred;
     }
     ck_launch(kgb::pls_assemble_result(M, n, L, std::max(NV, 0), d_land, d_test, eb.clbest, d_proj, d_c2l, C0max,
                                        d_res, st),
               "result rows");
     ev_proj = ctx.mark();
-    ctx.sync();
+    ctx.checkpoint();
     out->timings[4] = clk.lap();
   } else {
   // per-run fold-filtered vote tables over the landmark subgraph
@@ -1202,7 +1338,7 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     ck_launch(kgb::project_labels(a, st), "projection");
   }
   ev_proj = ctx.mark();
-  ctx.sync();
+  ctx.checkpoint();
   out->timings[4] = clk.lap();
   }
 
@@ -1219,35 +1355,46 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     ctx.sync();
   }
 
-  // outputs
-  const size_t res_bytes = sizeof(int) * static_cast<size_t>(M) * n;
-  void* res_stage = nullptr;
+  // outputs: queued here, read by matrix_finalize
+  tail.n = n;
+  tail.K = K;
+  tail.M = M;
+  tail.T = T;
+  tail.L = L;
+  tail.r0 = r0;
+  tail.cstride = cstride;
+  tail.pls = pls;
+  tail.res_bytes = sizeof(int) * static_cast<size_t>(M) * n;
   if (out->res_on_device) {
-    ck(cudaMemcpyAsync(out->res, d_res, res_bytes, cudaMemcpyDeviceToDevice, st), "D2D");
+    ck(cudaMemcpyAsync(out->res, d_res, tail.res_bytes, cudaMemcpyDeviceToDevice, st), "D2D");
   } else {
-    res_stage = g_stage.get(res_bytes);
-    ck(cudaMemcpyAsync(res_stage, d_res, res_bytes, cudaMemcpyDeviceToHost, st), "D2H");
+    if (ctx.capturing()) fail(KGB_EINTERNAL, "a captured batch keeps its label matrices on the device");
+    tail.res_stage = g_stage.get(tail.res_bytes);
+    ck(cudaMemcpyAsync(tail.res_stage, d_res, tail.res_bytes, cudaMemcpyDeviceToHost, st), "D2H");
   }
-  std::vector<double> best(static_cast<size_t>(M) * 2);
-  ctx.download(best.data(), eb.best, best.size());
-  ctx.download(out->v, eb.vect_acc, static_cast<size_t>(M) * T);
-  std::vector<int> psize(static_cast<size_t>(M) * T), active(static_cast<size_t>(M) * T),
-      counters(static_cast<size_t>(M) * cstride);
-  std::vector<uint8_t> flags(static_cast<size_t>(M) * T * 3);
-  ctx.download(psize.data(), eb.psize, psize.size());
-  ctx.download(active.data(), eb.active, active.size());
-  ctx.download(flags.data(), eb.flags, flags.size());
-  ctx.download(counters.data(), eb.counters, counters.size());
-  int* d_oidx = nullptr;
-  float* d_odist = nullptr;
-  const bool want_graph = o->materialize_graph && out->knn_idx != nullptr && out->knn_dist != nullptr;
-  if (want_graph) {
+  tail.best.assign(static_cast<size_t>(M) * 2, 0.0);
+  tail.v.assign(static_cast<size_t>(M) * T, 0.0);
+  tail.psize.assign(static_cast<size_t>(M) * T, 0);
+  tail.active.assign(static_cast<size_t>(M) * T, 0);
+  tail.counters.assign(static_cast<size_t>(M) * cstride, 0);
+  tail.flags.assign(static_cast<size_t>(M) * T * 3, 0);
+  ctx.download(tail.best.data(), eb.best, tail.best.size());
+  ctx.download(tail.v.data(), eb.vect_acc, tail.v.size());
+  ctx.download(tail.psize.data(), eb.psize, tail.psize.size());
+  ctx.download(tail.active.data(), eb.active, tail.active.size());
+  ctx.download(tail.flags.data(), eb.flags, tail.flags.size());
+  ctx.download(tail.counters.data(), eb.counters, tail.counters.size());
+  tail.want_graph = o->materialize_graph && out->knn_idx != nullptr && out->knn_dist != nullptr;
+  tail.apply_dissimilarity = o->apply_dissimilarity != 0;
+  if (tail.want_graph) {
     if (out->knn_cap < K) fail(KGB_EINVAL, "knn_cap is smaller than the graph width");
+    tail.gi.assign(static_cast<size_t>(n) * K, 0);
+    tail.gd.assign(static_cast<size_t>(n) * K, 0.0f);
     if (o->apply_dissimilarity) {
       int* d_lbs = ctx.alloc<int>(static_cast<size_t>(M) * n);
       ck_launch(kgb::transpose_runs(d_res, M, n, d_lbs, st), "transpose");
-      d_oidx = ctx.alloc<int>(static_cast<size_t>(n) * K);
-      d_odist = ctx.alloc<float>(static_cast<size_t>(n) * K);
+      int* d_oidx = ctx.alloc<int>(static_cast<size_t>(n) * K);
+      float* d_odist = ctx.alloc<float>(static_cast<size_t>(n) * K);
       kgb::DissimArgs a{};
       a.n = n;
       a.K = K;
@@ -1260,49 +1407,62 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
       a.out_idx = d_oidx;
       a.out_dist = d_odist;
       ck_launch(kgb::dissimilarity(a, st), "dissimilarity");
-    }
-  }
-  const int ev_dis = ctx.mark();
-  std::vector<uint64_t> land_hash(static_cast<size_t>(M));
-  int plan_status = 0;
-  ctx.download(land_hash.data(), d_land_hash, land_hash.size());
-  ctx.download(&plan_status, d_plan_status, 1);
-  ctx.sync();
-  if (plan_status != 0) fail(KGB_EINTERNAL, "Landmark quota allocation produced the wrong sample size.");
-  if (res_stage != nullptr) std::memcpy(out->res, res_stage, res_bytes);
-  const double t_dl = clk.lap();
-  if (graph_here) {
-    // order on the device: atlas, graph, landmark initialisation
-    out->kernel_ms[0] = ctx.ms(ev_atlas, ev_graph);
-    out->kernel_ms[1] = ctx.ms(ev_start, ev_atlas);
-    out->kernel_ms[2] = ctx.ms(ev_graph, ev_init);
-  } else {
-    out->kernel_ms[0] = ctx.ms(ev_start, ev_graph);
-    out->kernel_ms[1] = ctx.ms(ev_graph, ev_atlas);
-    out->kernel_ms[2] = ctx.ms(ev_atlas, ev_init);
-  }
-  out->kernel_ms[3] = ctx.ms(ev_init, ev_tables);
-  out->kernel_ms[4] = ctx.ms(ev_evo0, ev_evo1);
-  out->kernel_ms[5] = ctx.ms(ev_evo1, ev_proj);
-  out->kernel_ms[6] = ctx.ms(ev_proj, ev_dis);
-  out->kernel_ms[7] = ctx.ms(ev_start, ev_dis);
-  if (want_graph) {
-    std::vector<int> gi(static_cast<size_t>(n) * K);
-    std::vector<float> gd(static_cast<size_t>(n) * K);
-    if (o->apply_dissimilarity) {
-      ctx.download(gi.data(), d_oidx, gi.size());
-      ctx.download(gd.data(), d_odist, gd.size());
+      ctx.download(tail.gi.data(), d_oidx, tail.gi.size());
+      ctx.download(tail.gd.data(), d_odist, tail.gd.size());
     } else {
-      ctx.download(gi.data(), d_gidx, gi.size());
-      ctx.download(gd.data(), d_gdist, gd.size());
+      ctx.download(tail.gi.data(), d_gidx, tail.gi.size());
+      ctx.download(tail.gd.data(), d_gdist, tail.gd.size());
     }
-    ctx.sync();
+  }
+  tail.ev_dis = ctx.mark();
+  tail.land_hash.assign(static_cast<size_t>(M), 0);
+  ctx.download(tail.land_hash.data(), d_land_hash, tail.land_hash.size());
+  ctx.download(&tail.plan_status, d_plan_status, 1);
+  tail.fold_hash.resize(static_cast<size_t>(M));
+  for (int r = 0; r < M; ++r) tail.fold_hash[r] = fold_plans[r].fold_hash;
+  tail.graph_here = graph_here;
+  tail.ev_start = ev_start;
+  tail.ev_atlas = ev_atlas;
+  tail.ev_graph = ev_graph;
+  tail.ev_init = ev_init;
+  tail.ev_tables = ev_tables;
+  tail.ev_evo0 = ev_evo0;
+  tail.ev_evo1 = ev_evo1;
+  tail.ev_proj = ev_proj;
+}
+
+// Fills kgb_matrix_result from a completed call's tail (ctx null: no stage
+// timings, as for a captured batch).
+void matrix_finalize(Ctx* ctx, MatrixTail& t, kgb_matrix_result* out, Clock& clk) {
+  if (t.plan_status != 0) fail(KGB_EINTERNAL, "Landmark quota allocation produced the wrong sample size.");
+  for (size_t i = 0; i < t.pls_status.status.size(); ++i) pls_status_check(t.pls_status.status[i], t.pls_status.present[i]);
+  const int M = t.M, T = t.T, n = t.n, K = t.K, L = t.L;
+  if (t.res_stage != nullptr) std::memcpy(out->res, t.res_stage, t.res_bytes);
+  if (!t.v.empty()) std::memcpy(out->v, t.v.data(), sizeof(double) * t.v.size());
+  const double t_dl = clk.lap();
+  auto ms = [&](int a, int b) { return ctx == nullptr ? 0.0 : ctx->ms(a, b); };
+  if (t.graph_here) {
+    // order on the device: atlas, graph, landmark initialisation
+    out->kernel_ms[0] = ms(t.ev_atlas, t.ev_graph);
+    out->kernel_ms[1] = ms(t.ev_start, t.ev_atlas);
+    out->kernel_ms[2] = ms(t.ev_graph, t.ev_init);
+  } else {
+    out->kernel_ms[0] = ms(t.ev_start, t.ev_graph);
+    out->kernel_ms[1] = ms(t.ev_graph, t.ev_atlas);
+    out->kernel_ms[2] = ms(t.ev_atlas, t.ev_init);
+  }
+  out->kernel_ms[3] = ms(t.ev_init, t.ev_tables);
+  out->kernel_ms[4] = ms(t.ev_evo0, t.ev_evo1);
+  out->kernel_ms[5] = ms(t.ev_evo1, t.ev_proj);
+  out->kernel_ms[6] = ms(t.ev_proj, t.ev_dis);
+  out->kernel_ms[7] = ms(t.ev_start, t.ev_dis);
+  if (t.want_graph) {
     for (int i = 0; i < n; ++i) {
       for (int j = 0; j < K; ++j) {
-        int v = gi[static_cast<size_t>(i) * K + j];
-        if (!o->apply_dissimilarity && v >= 0) v += 1;
+        int v = t.gi[static_cast<size_t>(i) * K + j];
+        if (!t.apply_dissimilarity && v >= 0) v += 1;
         out->knn_idx[static_cast<size_t>(i) * out->knn_cap + j] = v;
-        out->knn_dist[static_cast<size_t>(i) * out->knn_cap + j] = gd[static_cast<size_t>(i) * K + j];
+        out->knn_dist[static_cast<size_t>(i) * out->knn_cap + j] = t.gd[static_cast<size_t>(i) * K + j];
       }
     }
     out->knn_k = K;
@@ -1311,21 +1471,20 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   }
   out->timings[6] = clk.lap() + t_dl;
   for (int r = 0; r < M; ++r) {
-    out->acc[r] = best[2 * r];
+    out->acc[r] = t.best[2 * r];
     if (out->run_hashes) {
-      out->run_hashes[3 * r + 0] = land_hash[r];
-      out->run_hashes[3 * r + 1] = init_hash[r];
-      out->run_hashes[3 * r + 2] = fold_plans[r].fold_hash;
+      out->run_hashes[3 * r + 0] = t.land_hash[r];
+      out->run_hashes[3 * r + 1] = t.init_hash[r];
+      out->run_hashes[3 * r + 2] = t.fold_hash[r];
     }
+    const int* c = t.counters.data() + static_cast<size_t>(r) * t.cstride;
     if (out->pls_counters) {
-      const int* c = counters.data() + static_cast<size_t>(r) * cstride;
-      out->pls_counters[2 * r] = pls ? c[16] : 0;
-      out->pls_counters[2 * r + 1] = pls ? c[17] : 0;
+      out->pls_counters[2 * r] = t.pls ? c[16] : 0;
+      out->pls_counters[2 * r + 1] = t.pls ? c[17] : 0;
     }
     if (out->run_counters) {
-      const int* c = counters.data() + static_cast<size_t>(r) * cstride;
       int* rc = out->run_counters + 8 * r;
-      rc[0] = r0 + r;
+      rc[0] = t.r0 + r;
       rc[1] = c[0];
       rc[2] = c[9];
       rc[3] = c[10];
@@ -1335,14 +1494,14 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
       rc[7] = L;
     }
     if (out->cycle_diag) {
-      for (int c = 0; c < T; ++c) {
-        int* cd = out->cycle_diag + (static_cast<size_t>(r) * T + c) * 5;
-        const size_t o1 = static_cast<size_t>(r) * T + c;
-        cd[0] = psize[o1];
-        cd[1] = active[o1];
-        cd[2] = flags[3 * o1 + 0];
-        cd[3] = flags[3 * o1 + 1];
-        cd[4] = flags[3 * o1 + 2];
+      for (int cy = 0; cy < T; ++cy) {
+        int* cd = out->cycle_diag + (static_cast<size_t>(r) * T + cy) * 5;
+        const size_t o1 = static_cast<size_t>(r) * T + cy;
+        cd[0] = t.psize[o1];
+        cd[1] = t.active[o1];
+        cd[2] = t.flags[3 * o1 + 0];
+        cd[3] = t.flags[3 * o1 + 1];
+        cd[4] = t.flags[3 * o1 + 2];
       }
     }
   }
@@ -1375,6 +1534,338 @@ void exact_graph(Ctx& ctx, const float* d_x, int n, int d, int K, int method, in
     void* scratch = ctx.alloc<unsigned char>(kgb::knn_bruteforce_scratch(n, K, segments));
     ck_launch(kgb::knn_bruteforce(d_x, n, d, K, segments, scratch, d_idx, d_dist, ctx.stream()), "kNN graph");
     if (fallback_rows != nullptr) *fallback_rows = n;
+  }
+}
+
+// Landmarks and graph width of a call (run_kodama_matrix,
+// kodama_matrix.cpp:3340-3350, and the graph width rule).
+struct MatrixSizes {
+  int landmarks, neighbors;
+};
+MatrixSizes matrix_sizes(int n, const kgb_matrix_options* opt) {
+  int landmarks = opt->landmarks > 0 ? opt->landmarks : 10000;
+  if (landmarks >= n) landmarks = static_cast<int>(std::ceil(static_cast<double>(n) * 0.75));
+  landmarks = std::max(2, std::min(landmarks, n - 1));
+  const int requested = opt->graph_neighbors > 0 ? opt->graph_neighbors : 100;
+  const int neighbors = std::max(1, static_cast<int>(std::floor(std::min(
+      {static_cast<double>(landmarks), static_cast<double>(n) * 0.75 - 1.0, static_cast<double>(requested)}))));
+  return MatrixSizes{landmarks, neighbors};
+}
+
+// ---------------------------------------------------------------------------
+// Batches of independent KODAMA.matrix problems in one captured CUDA graph.
+//
+// Every problem's plain raw-data path (matrix_from_device_graph) is queued,
+// with no host synchronisation, into one of `lanes` stream pairs of a capture;
+// the graph therefore holds `lanes` independent chains that the device runs
+// side by side, and each problem's allocations are graph memory nodes freed
+// at the end of its chain, so memory is reused along a chain.  The problems'
+// data sit in one persistent device buffer and their label matrices in
+// persistent device buffers; everything else goes through the capture arena.
+// The schedule (lanes, and the order problems are dealt to the lanes) is
+// picked by timing candidate graphs on the first call for a batch shape and
+// kept for later calls; the last graph is replayed while the shape stays.
+// ---------------------------------------------------------------------------
+struct BatchProblem {
+  MatrixTail tail;
+  kgb_matrix_result shadow{};  // the capture's view of the result (label matrix on the device)
+  int* d_res = nullptr;
+  size_t x_off = 0;
+  double cost = 0.0;
+};
+
+struct BatchGraph {
+  std::string key;
+  int device = 0, lanes = 0, order = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t root = nullptr;
+  std::vector<cudaStream_t> streams;
+  CaptureArena arena;
+  std::vector<std::unique_ptr<BatchProblem>> problems;
+  float* d_x = nullptr;
+  size_t nodes = 0, kernel_nodes = 0;
+  BatchGraph() = default;
+  BatchGraph(const BatchGraph&) = delete;
+  BatchGraph& operator=(const BatchGraph&) = delete;
+  ~BatchGraph() {
+    if (root) cudaStreamSynchronize(root);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    for (auto& p : problems)
+      if (p->d_res) cudaFree(p->d_res);
+    if (d_x) cudaFree(d_x);
+    for (cudaStream_t st : streams) cudaStreamDestroy(st);
+    if (root) cudaStreamDestroy(root);
+  }
+};
+
+std::mutex g_batch_mu;
+std::unique_ptr<BatchGraph> g_batch;                  // the last captured batch
+std::map<std::string, std::pair<int, int>> g_tuned;   // batch shape -> (lanes, order)
+
+void check_batch_problem(const kgb_matrix_problem& q) {
+  if (q.x == nullptr || q.result == nullptr) fail(KGB_EINVAL, "null pointer");
+  if (q.n < 3) fail(KGB_EINVAL, "KODAMAMatrix requires at least 3 rows.");
+  if (q.d < 1) fail(KGB_EINVAL, "Input matrix must have at least one column.");
+  validate_matrix_options(&q.options);
+  const kgb_matrix_result* r = q.result;
+  if (r->res == nullptr || r->acc == nullptr || r->v == nullptr) fail(KGB_EINVAL, "null result buffer");
+  if (r->res_on_device) fail(KGB_EINVAL, "a batch returns the label matrices in host memory");
+  if (q.options.starting_labels != nullptr || q.options.constrain != nullptr || q.options.fixed != nullptr)
+    fail(KGB_EINVAL, "semi-supervised inputs are not supported in a batch");
+  if (q.options.proposal_weights != nullptr) fail(KGB_EINVAL, "the learned proposal is not supported in a batch");
+  if (r->snapshot_features != nullptr || r->snapshot_flags != nullptr)
+    fail(KGB_EINVAL, "proposal snapshots are not supported in a batch");
+}
+
+// Everything the captured work depends on, so a replay is only taken for the
+// same shapes and options.
+std::string batch_key(const kgb_matrix_problem* probs, int count, int device) {
+  std::string k = std::to_string(device) + ":" + std::to_string(count);
+  for (int i = 0; i < count; ++i) {
+    const kgb_matrix_problem& q = probs[i];
+    const kgb_matrix_options& o = q.options;
+    char buf[512];
+    std::snprintf(buf, sizeof(buf), "|%d,%d,%d,%d,%d,%d,%d,%d,%d,%d,%d,%d,%d,%d,%d,%llu,%d%d%d%d%d%d%d%d,%d,%d,%d",
+                  q.n, q.d, o.runs, o.cycles, o.landmarks, o.splitting, o.graph_neighbors, o.folds, o.knn_k,
+                  o.classifier, o.components, o.materialize_graph, o.apply_dissimilarity, o.metric, o.first_run,
+                  static_cast<unsigned long long>(o.seed), o.policy.prediction_guidance,
+                  o.policy.adaptive_proposal_size, o.policy.transition_proposal, o.policy.stochastic_acceptance,
+                  o.policy.diversity_multiplier, o.policy.pls_transition_coarsening,
+                  o.policy.pls_fragmentation_penalty, o.policy.reject_single_class,
+                  q.result->knn_idx != nullptr && q.result->knn_dist != nullptr ? q.result->knn_cap : -1,
+                  q.result->run_hashes != nullptr, q.result->cycle_diag != nullptr);
+    k += buf;
+  }
+  return k;
+}
+
+// Relative device cost of a problem, for dealing the longest first: the
+// graph (n^2 d), the k-means and the evolution (M T L per cycle, with PLS
+// heavier by its per-cycle fits over d features).
+double batch_cost(const kgb_matrix_problem& q) {
+  const double n = q.n, d = q.d, M = q.options.runs, T = q.options.cycles + 1;
+  const double L = matrix_sizes(q.n, &q.options).landmarks;
+  const double graph = n * n * d * 1e-9;
+  const double evolve = q.options.classifier == 1 ? M * T * L * (d + 20.0) * 2e-9 : M * T * L * 4e-9;
+  return graph + evolve + M * L * d * 1e-8;
+}
+
+std::unique_ptr<BatchGraph> build_batch(const kgb_matrix_problem* probs, int count, int device, int lanes,
+                                        int order, const std::string& key) {
+  auto g = std::make_unique<BatchGraph>();
+  g->key = key;
+  g->device = device;
+  g->lanes = lanes;
+  g->order = order;
+  ck(cudaSetDevice(device), "cudaSetDevice");
+  ck(cudaStreamCreateWithFlags(&g->root, cudaStreamNonBlocking), "cudaStreamCreate");
+  for (int l = 0; l < 2 * lanes; ++l) {
+    cudaStream_t st;
+    ck(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
+    g->streams.push_back(st);
+  }
+  size_t xf = 0;
+  for (int i = 0; i < count; ++i) {
+    auto bp = std::make_unique<BatchProblem>();
+    bp->x_off = xf;
+    xf += static_cast<size_t>(probs[i].n) * probs[i].d;
+    bp->cost = batch_cost(probs[i]);
+    ck(cudaMalloc(&bp->d_res, sizeof(int) * static_cast<size_t>(probs[i].options.runs) * probs[i].n), "cudaMalloc");
+    bp->shadow = *probs[i].result;
+    bp->shadow.res = bp->d_res;
+    bp->shadow.res_on_device = 1;
+    g->problems.push_back(std::move(bp));
+  }
+  ck(cudaMalloc(&g->d_x, sizeof(float) * std::max<size_t>(xf, 1)), "cudaMalloc");
+  // deal the problems to the lanes: longest first to the least loaded lane,
+  // or in the given order round robin
+  std::vector<int> idx(static_cast<size_t>(count));
+  std::iota(idx.begin(), idx.end(), 0);
+  std::vector<std::vector<int>> lane_of(static_cast<size_t>(lanes));
+  if (order == 1) {
+    std::stable_sort(idx.begin(), idx.end(),
+                     [&](int a, int b) { return g->problems[a]->cost > g->problems[b]->cost; });
+    std::vector<double> load(static_cast<size_t>(lanes), 0.0);
+    for (int i : idx) {
+      const int l = static_cast<int>(std::min_element(load.begin(), load.end()) - load.begin());
+      lane_of[l].push_back(i);
+      load[l] += g->problems[i]->cost;
+    }
+  } else {
+    for (int i : idx) lane_of[i % lanes].push_back(i);
+  }
+  std::vector<std::unique_ptr<Ctx>> ctxs;
+  std::vector<cudaEvent_t> evs;
+  auto event = [&]() {
+    cudaEvent_t e;
+    ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+    evs.push_back(e);
+    return e;
+  };
+  ck(cudaStreamBeginCapture(g->root, cudaStreamCaptureModeRelaxed), "cudaStreamBeginCapture");
+  try {
+    const cudaEvent_t e0 = event();
+    ck(cudaEventRecord(e0, g->root), "cudaEventRecord");
+    for (int l = 0; l < lanes; ++l) {
+      cudaStream_t mainst = g->streams[2 * l], sidest = g->streams[2 * l + 1];
+      ck(cudaStreamWaitEvent(mainst, e0, 0), "cudaStreamWaitEvent");
+      ck(cudaStreamWaitEvent(sidest, e0, 0), "cudaStreamWaitEvent");
+      for (int i : lane_of[l]) {
+        const kgb_matrix_problem& q = probs[i];
+        BatchProblem& bp = *g->problems[i];
+        ctxs.push_back(std::make_unique<Ctx>(device, mainst, sidest, &g->arena));
+        Ctx& ctx = *ctxs.back();
+        const MatrixSizes sz = matrix_sizes(q.n, &q.options);
+        const int K = sz.neighbors, landmarks = sz.landmarks;
+        const int M = q.options.runs, F = q.options.folds;
+        const int first_run = q.options.first_run > 0 ? q.options.first_run : 1;
+        const uint64_t seed = q.options.seed;
+        std::future<std::vector<kgb::FoldPlan>> folds = std::async(std::launch::deferred, [=]() {
+          std::vector<kgb::FoldPlan> plans(static_cast<size_t>(M));
+          for (int r = 0; r < M; ++r) plans[r] = kgb::plan_folds(landmarks, F, seed, first_run + r);
+          return plans;
+        });
+        const float* d_x = g->d_x + bp.x_off;
+        const int ev_start = ctx.mark();
+        int* d_gidx = ctx.alloc<int>(static_cast<size_t>(q.n) * K);
+        float* d_gdist = ctx.alloc<float>(static_cast<size_t>(q.n) * K);
+        kgb_matrix_options o = q.options;
+        o.device = device;
+        Clock clk;
+        matrix_from_device_graph(ctx, d_x, q.n, q.d, d_gidx, d_gdist, K, &o, &bp.shadow, clk, ev_start, -1, folds,
+                                 bp.tail, [&]() {
+                                   exact_graph(ctx, d_x, q.n, q.d, K, KGB_KNN_AUTO, d_gidx, d_gdist, nullptr);
+                                 });
+        ctx.release();
+      }
+      const cudaEvent_t done = event();
+      ck(cudaEventRecord(done, mainst), "cudaEventRecord");
+      ck(cudaStreamWaitEvent(g->root, done, 0), "cudaStreamWaitEvent");
+    }
+    ck(cudaStreamEndCapture(g->root, &g->graph), "cudaStreamEndCapture");
+  } catch (...) {
+    cudaGraph_t broken = nullptr;
+    cudaStreamEndCapture(g->root, &broken);
+    if (broken) cudaGraphDestroy(broken);
+    cudaGetLastError();
+    ctxs.clear();
+    for (cudaEvent_t e : evs) cudaEventDestroy(e);
+    throw;
+  }
+  ctxs.clear();
+  for (cudaEvent_t e : evs) cudaEventDestroy(e);
+  ck(cudaGraphInstantiate(&g->exec, g->graph, 0), "cudaGraphInstantiate");
+  size_t nn = 0;
+  ck(cudaGraphGetNodes(g->graph, nullptr, &nn), "cudaGraphGetNodes");
+  std::vector<cudaGraphNode_t> nodes(nn);
+  if (nn) ck(cudaGraphGetNodes(g->graph, nodes.data(), &nn), "cudaGraphGetNodes");
+  g->nodes = nn;
+  for (cudaGraphNode_t nd : nodes) {
+    cudaGraphNodeType ty;
+    if (cudaGraphNodeGetType(nd, &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel) ++g->kernel_nodes;
+  }
+  return g;
+}
+
+// One replay: data in, graph, label matrices out; returns the graph's device
+// time in ms.
+double run_batch(BatchGraph& g, const kgb_matrix_problem* probs, int count) {
+  ck(cudaSetDevice(g.device), "cudaSetDevice");
+  cudaEvent_t e0, e1;
+  ck(cudaEventCreate(&e0), "cudaEventCreate");
+  ck(cudaEventCreate(&e1), "cudaEventCreate");
+  for (int i = 0; i < count; ++i)
+    ck(cudaMemcpyAsync(g.d_x + g.problems[i]->x_off, probs[i].x, sizeof(float) * static_cast<size_t>(probs[i].n) * probs[i].d,
+                       cudaMemcpyHostToDevice, g.root),
+       "H2D");
+  ck(cudaEventRecord(e0, g.root), "cudaEventRecord");
+  ck(cudaGraphLaunch(g.exec, g.root), "cudaGraphLaunch");
+  ck(cudaEventRecord(e1, g.root), "cudaEventRecord");
+  for (int i = 0; i < count; ++i)
+    ck(cudaMemcpyAsync(probs[i].result->res, g.problems[i]->d_res,
+                       sizeof(int) * static_cast<size_t>(probs[i].options.runs) * probs[i].n, cudaMemcpyDeviceToHost,
+                       g.root),
+       "D2H");
+  const cudaError_t e = cudaStreamSynchronize(g.root);
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  ck(e, "batch graph");
+  g.arena.deliver();
+  return static_cast<double>(ms);
+}
+
+void batch_entry(const kgb_matrix_problem* probs, int count, const kgb_batch_options* bo, kgb_batch_report* rep) {
+  if (probs == nullptr || count < 1) fail(KGB_EINVAL, "a batch needs at least one problem");
+  for (int i = 0; i < count; ++i) check_batch_problem(probs[i]);
+  const int device = bo != nullptr ? bo->device : 0;
+  int devcount = 0;
+  if (cudaGetDeviceCount(&devcount) != cudaSuccess || devcount <= 0) fail(KGB_ECUDA, "no CUDA device is available");
+  if (device < 0 || device >= devcount) fail(KGB_EINVAL, "CUDA device ordinal out of range");
+  std::lock_guard<std::mutex> lock(g_batch_mu);
+  const std::string key = batch_key(probs, count, device);
+  Clock clk;
+  double tune_ms = 0.0;
+  bool rebuilt = false;
+  int lanes = bo != nullptr ? bo->lanes : 0, order = bo != nullptr ? bo->order : 0;
+  if (lanes < 0 || lanes > 64) fail(KGB_EINVAL, "lanes must lie in [0, 64]");
+  if (order < 0 || order > 2) fail(KGB_EINVAL, "order must be 0, 1 or 2");
+  if (lanes == 0 || order == 0) {
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) {
+      if (lanes == 0) lanes = it->second.first;
+      if (order == 0) order = it->second.second;
+    } else {
+      // autotune: time each candidate schedule once on this batch
+      const int cand_lanes[] = {4, 8, 16, 32};
+      double best = 0.0;
+      int bl = 0, bo2 = 0;
+      for (int cl : cand_lanes) {
+        if (lanes != 0 && cl != lanes) continue;
+        if (cl > 2 * count && cl != 4) continue;
+        for (int co = 1; co <= 2; ++co) {
+          if (order != 0 && co != order) continue;
+          g_batch.reset();
+          g_batch = build_batch(probs, count, device, cl, co, key);
+          const double ms = run_batch(*g_batch, probs, count);
+          if (bl == 0 || ms < best) {
+            best = ms;
+            bl = cl;
+            bo2 = co;
+          }
+        }
+      }
+      g_tuned[key] = {bl, bo2};
+      lanes = bl;
+      order = bo2;
+      tune_ms = clk.lap();
+      rebuilt = true;
+    }
+  }
+  if (!g_batch || g_batch->key != key || g_batch->lanes != lanes || g_batch->order != order) {
+    g_batch.reset();
+    g_batch = build_batch(probs, count, device, lanes, order, key);
+    rebuilt = true;
+  }
+  const double dev_ms = run_batch(*g_batch, probs, count);
+  for (int i = 0; i < count; ++i) {
+    kgb_matrix_result* out = probs[i].result;
+    for (double& t : out->timings) t = 0.0;
+    for (double& t : out->kernel_ms) t = 0.0;
+    Clock fclk;
+    matrix_finalize(nullptr, g_batch->problems[i]->tail, out, fclk);
+  }
+  if (rep != nullptr) {
+    rep->lanes = lanes;
+    rep->order = order;
+    rep->graph_nodes = static_cast<int32_t>(g_batch->nodes);
+    rep->kernel_nodes = static_cast<int32_t>(g_batch->kernel_nodes);
+    rep->rebuilt = rebuilt ? 1 : 0;
+    rep->device_ms = dev_ms;
+    rep->tune_ms = tune_ms;
   }
 }
 
@@ -1421,20 +1912,27 @@ void matrix_entry(const float* x, bool x_on_device, int n, int d, const int32_t*
                                       ctx.stream()), "graph normalisation");
   } else {
     // raw data: the graph is queued after the atlas k-means (see
-    // matrix_from_device_graph), overlapping the host's run planning
+    // matrix_from_device_graph), beside the landmark planning
     K = neighbors;
     d_gidx = ctx.alloc<int>(static_cast<size_t>(n) * K);
     d_gdist = ctx.alloc<float>(static_cast<size_t>(n) * K);
     out->timings[1] = clk.lap();
-    matrix_from_device_graph(ctx, d_x, n, d, d_gidx, d_gdist, K, opt, out, clk, ev_start, -1, folds_future,
+    MatrixTail tail;
+    matrix_from_device_graph(ctx, d_x, n, d, d_gidx, d_gdist, K, opt, out, clk, ev_start, -1, folds_future, tail,
                              [&]() { exact_graph(ctx, d_x, n, d, K, KGB_KNN_AUTO, d_gidx, d_gdist, nullptr); });
+    ctx.sync();
+    matrix_finalize(&ctx, tail, out, clk);
     out->timings[0] = total.lap();
     return;
   }
   const int ev_graph = ctx.mark();
   ctx.sync();
   out->timings[1] = clk.lap();
-  matrix_from_device_graph(ctx, d_x, n, d, d_gidx, d_gdist, K, opt, out, clk, ev_start, ev_graph, folds_future);
+  MatrixTail tail;
+  matrix_from_device_graph(ctx, d_x, n, d, d_gidx, d_gdist, K, opt, out, clk, ev_start, ev_graph, folds_future,
+                           tail);
+  ctx.sync();
+  matrix_finalize(&ctx, tail, out, clk);
   out->timings[0] = total.lap();
 }
 
@@ -1671,6 +2169,11 @@ int kgb_kodama_matrix(const float* x, int32_t n, int32_t d, const kgb_matrix_opt
 int kgb_kodama_matrix_resident(const float* x_device, int32_t n, int32_t d, const kgb_matrix_options* opt,
                                kgb_matrix_result* out) {
   return guarded([&]() { matrix_entry(x_device, true, n, d, nullptr, nullptr, 0, -1, opt, out); });
+}
+
+int kgb_kodama_matrix_batch(const kgb_matrix_problem* problems, int32_t count, const kgb_batch_options* options,
+                            kgb_batch_report* report) {
+  return guarded([&]() { batch_entry(problems, count, options, report); });
 }
 
 int64_t kgb_launch_count(void) { return kgb::g_launches_value(); }

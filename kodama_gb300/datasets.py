@@ -81,3 +81,21 @@ def pca_mixture(n: int = 100000, d: int = 50, clusters: int = 30, seed: int = 5
         pos += cnt
     order = rng.permutation(n)
     return x[order], y[order]
+
+
+def uneven_batch(count: int = 256, seed: int = 4) -> list[dict]:
+    """Independent KODAMA.matrix problems of uneven size: problem i draws, from
+    its own generator seeded seed + i, N log-uniform in [500, 20000],
+    d uniform in {10, 50, 100} and a Gaussian mixture of 3-20 clusters with
+    means ~ N(0, 3^2 I) and unit covariance; even problems use the kNN
+    classifier, odd ones PLS-LDA.  Returns dicts with x (float32), classifier."""
+    out = []
+    for i in range(count):
+        rng = np.random.default_rng(seed + i)
+        n = int(round(float(np.exp(rng.uniform(np.log(500.0), np.log(20000.0))))))
+        d = int(rng.choice([10, 50, 100]))
+        clusters = int(rng.integers(3, 21))
+        x, _ = gaussian_mixture(n=n, d=d, clusters=clusters, mean_scale=3.0, seed=int(rng.integers(1 << 31)))
+        out.append({"x": x, "classifier": "knn" if i % 2 == 0 else "pls"})
+    return out
+
