@@ -1520,7 +1520,7 @@ void exact_graph(Ctx& ctx, const float* d_x, int n, int d, int K, int method, in
   const int segments = 4;
   const bool tc = method == KGB_KNN_TENSOR || (method == KGB_KNN_AUTO && kgb::knn_tc_supported(n, d, K));
   if (method == KGB_KNN_TENSOR && !kgb::knn_tc_supported(n, d, K))
-    fail(KGB_EINVAL, "the tensor-core kNN search needs d <= 64, K <= 96 and n > 2 * (K + 16) + 64");
+    fail(KGB_EINVAL, "the tensor-core kNN search needs d <= 128, K <= 96 and n > 2 * (K + 16) + 64");
   if (tc) {
     void* scratch = ctx.alloc<unsigned char>(kgb::knn_tc_scratch(n, d, K, segments));
     ck_launch(kgb::knn_tc_graph(d_x, n, d, K, segments, scratch, d_idx, d_dist, ctx.stream()), "kNN graph");
@@ -1819,25 +1819,38 @@ void batch_entry(const kgb_matrix_problem* probs, int count, const kgb_batch_opt
       if (lanes == 0) lanes = it->second.first;
       if (order == 0) order = it->second.second;
     } else {
-      // autotune: time each candidate schedule once on this batch
-      const int cand_lanes[] = {4, 8, 16, 32};
+      // autotune on a sample of at most 64 problems spread over the cost
+      // range: the lane count first (longest-first dealing), then the order
+      // at that lane count; each candidate graph is captured and timed once
+      std::vector<int> byc(static_cast<size_t>(count));
+      std::iota(byc.begin(), byc.end(), 0);
+      std::stable_sort(byc.begin(), byc.end(),
+                       [&](int a, int b) { return batch_cost(probs[a]) > batch_cost(probs[b]); });
+      const int ns = std::min(count, 64);
+      std::vector<kgb_matrix_problem> sample;
+      for (int i = 0; i < ns; ++i) sample.push_back(probs[byc[static_cast<size_t>(i) * count / ns]]);
+      const std::string skey = "tune:" + batch_key(sample.data(), ns, device);
+      auto time_schedule = [&](int cl, int co) {
+        g_batch.reset();
+        g_batch = build_batch(sample.data(), ns, device, cl, co, skey);
+        return run_batch(*g_batch, sample.data(), ns);
+      };
       double best = 0.0;
-      int bl = 0, bo2 = 0;
-      for (int cl : cand_lanes) {
+      int bl = 0, bo2 = order != 0 ? order : 1;
+      for (int cl : {4, 8, 16, 32}) {
         if (lanes != 0 && cl != lanes) continue;
-        if (cl > 2 * count && cl != 4) continue;
-        for (int co = 1; co <= 2; ++co) {
-          if (order != 0 && co != order) continue;
-          g_batch.reset();
-          g_batch = build_batch(probs, count, device, cl, co, key);
-          const double ms = run_batch(*g_batch, probs, count);
-          if (bl == 0 || ms < best) {
-            best = ms;
-            bl = cl;
-            bo2 = co;
-          }
+        if (lanes == 0 && cl > ns && cl != 4) continue;
+        const double ms = time_schedule(cl, bo2);
+        if (bl == 0 || ms < best) {
+          best = ms;
+          bl = cl;
         }
       }
+      if (order == 0) {
+        const double ms = time_schedule(bl, 2);
+        if (ms < best) bo2 = 2;
+      }
+      g_batch.reset();
       g_tuned[key] = {bl, bo2};
       lanes = bl;
       order = bo2;

@@ -284,6 +284,8 @@ size_t assign_tc_smem(int k, int d, int dp) {
          sizeof(float) * kTcAssignWarps * 16 * (kpad + 1);
 }
 
+// KS: k-steps of 16 coordinates held in registers (dp <= 16 KS).
+template <int KS>
 __global__ void __launch_bounds__(32 * kTcAssignWarps) assign_tc_kernel(KMeansBatch B, int final_pass) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int p = blockIdx.y;
@@ -329,9 +331,9 @@ __global__ void __launch_bounds__(32 * kTcAssignWarps) assign_tc_kernel(KMeansBa
       return B.rows ? B.rows[static_cast<size_t>(p) * n + ii] : ii;
     };
     const int ga = global_row(r0 + g), gb = global_row(r0 + g + 8);
-    uint32_t ah[4][4], al[4][4];
+    uint32_t ah[KS][4], al[KS][4];
   #pragma unroll
-    for (int ks = 0; ks < 4; ++ks) {
+    for (int ks = 0; ks < KS; ++ks) {
       uint2 pa = make_uint2(0u, 0u), pb = pa, qa = pa, qb = pa;
       if (ks < ksn) {
         pa = *reinterpret_cast<const uint2*>(B.xh + static_cast<size_t>(ga) * dp + ks * 16 + 4 * tig);
@@ -349,7 +351,7 @@ __global__ void __launch_bounds__(32 * kTcAssignWarps) assign_tc_kernel(KMeansBa
   #pragma unroll
       for (int t = 0; t < 8; ++t) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.0f;
   #pragma unroll
-      for (int ks = 0; ks < 4; ++ks) {
+      for (int ks = 0; ks < KS; ++ks) {
         if (ks < ksn) {
   #pragma unroll
           for (int t = 0; t < 8; ++t) {
@@ -389,10 +391,10 @@ __global__ void __launch_bounds__(32 * kTcAssignWarps) assign_tc_kernel(KMeansBa
       for (int c = half; c < k; c += 2) amin = fminf(amin, arow[c]);
       amin = fminf(amin, __shfl_xor_sync(kFull, amin, 16));
       const float thr = amin + 2.0f * fadd(pn, scn[kpad]) * B.tc_crel;
-      float xv[64];
+      float xv[16 * KS];
       const float* xr = B.x + static_cast<size_t>(grow) * d;
 #pragma unroll
-      for (int j = 0; j < 64; ++j) xv[j] = j < d ? xr[j] : 0.0f;
+      for (int j = 0; j < 16 * KS; ++j) xv[j] = j < d ? xr[j] : 0.0f;
       int best = k;
       float bestd = INFINITY;
       // each lane walks its own candidates; the lanes compute their dots
@@ -404,7 +406,7 @@ __global__ void __launch_bounds__(32 * kTcAssignWarps) assign_tc_kernel(KMeansBa
         const bool have = cpos < k;
         if (!__any_sync(kFull, have)) break;
         const int c = have ? cpos : 0;
-        const float dt = dot_x86_reg<4>(xv, scf + static_cast<size_t>(c) * d4, d);
+        const float dt = dot_x86_reg<KS>(xv, scf + static_cast<size_t>(c) * d4, d);
         if (have) {
           const float dist = __fsub_rn(fadd(pn, scn[c]), fmul(2.0f, dt));
           if (dist < bestd || (dist == bestd && c < best)) {
@@ -691,7 +693,7 @@ __global__ void finalize_kernel(KMeansBatch B) {
 
 }  // namespace
 
-bool kmeans_tc_supported(int d, int k) { return d >= 1 && d <= 64 && k >= 1 && k <= 128; }
+bool kmeans_tc_supported(int d, int k) { return d >= 1 && d <= 128 && k >= 1 && k <= 128; }
 
 size_t kmeans_sort_smem(int k) { return sizeof(int) * (33 * static_cast<size_t>(k) + 1); }
 
@@ -711,7 +713,11 @@ int kmeans_run(const KMeansBatch& B, cudaStream_t st) {
   const size_t sum_bytes = sums_smem(B.d);
   const bool tc = B.xh != nullptr && kmeans_tc_supported(B.d, B.k);
   const size_t tc_bytes = tc ? assign_tc_smem(B.k, B.d, B.dp) : 0;
-  if (tc) cudaFuncSetAttribute(assign_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(tc_bytes));
+  const bool tc_wide = B.dp > 64;
+  if (tc) {
+    cudaFuncSetAttribute(assign_tc_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(tc_bytes));
+    cudaFuncSetAttribute(assign_tc_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(tc_bytes));
+  }
   // 64-row blocks per CTA: the centroids are staged once per CTA, but the grid
   // keeps at least two CTAs per SM
   KMeansBatch T = B;
@@ -738,7 +744,8 @@ int kmeans_run(const KMeansBatch& B, cudaStream_t st) {
     if (tc) {
       // the centroids' bf16 split (its own launch is counted there)
       bf16_split_rows(B.cent, B.problems * B.k, B.d, B.dp, B.ch, B.cl, st);
-      assign_tc_kernel<<<tgrid, 32 * kTcAssignWarps, tc_bytes, st>>>(T, final_pass);
+      if (tc_wide) assign_tc_kernel<8><<<tgrid, 32 * kTcAssignWarps, tc_bytes, st>>>(T, final_pass);
+      else assign_tc_kernel<4><<<tgrid, 32 * kTcAssignWarps, tc_bytes, st>>>(T, final_pass);
       return;
     }
     if (B.d <= 16) assign_kernel<1><<<agrid, 128, cs_bytes, st>>>(B, final_pass);

@@ -48,7 +48,7 @@ namespace {
 constexpr int kTcWarps = 4;            // warps per CTA, 16 queries each
 constexpr int kTcQ = 16 * kTcWarps;    // queries per CTA
 constexpr int kTcN = 64;               // candidates per tile
-constexpr int kTcMaxKs = 4;            // k-steps of 16 held in registers (dp <= 64)
+constexpr int kTcMaxKs = 8;            // k-steps of 16 held in registers (dp <= 128)
 constexpr int kTileStride = kTcN + 8;  // floats per row of a warp's distance tile
 
 __device__ __forceinline__ uint32_t bf16_bits(float v) {
@@ -131,7 +131,6 @@ struct TcArgs {
 };
 
 constexpr int kMaxPer = 8;   // re-rank candidates per lane (segs x 2 x kp <= 256)
-constexpr int kMaxLoads = 4; // 16-byte tile chunks per thread (kTcN x dp / 8 / 128 <= 4)
 
 // Shared memory: 2 x (hi, lo) candidate tiles, 2 x tile norms, per warp a
 // 16 x kTileStride distance tile, 16 x 4 flag masks, 32 thresholds and 32
@@ -141,7 +140,11 @@ size_t tc_smem_bytes(int row_words, int kp) {
          kTcWarps * (16 * kTileStride * 4 + 64 * 4 + 32 * 4 + 32 * static_cast<size_t>(kp) * 8);
 }
 
+// KS: k-steps of 16 coordinates in the query fragments (dp <= 16 KS); each
+// thread copies 2 KS 16-byte chunks of a candidate tile (kTcN x dp / 8 / 128).
+template <int KS>
 __global__ void __launch_bounds__(32 * kTcWarps, 2) tc_candidates_kernel(TcArgs A) {
+  constexpr int kMaxLoads = 2 * KS;
   extern __shared__ __align__(16) unsigned char smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
   const int n = A.n, dp = A.dp, kp = A.kp, rw = A.row_words, ksn = dp >> 4;
@@ -157,11 +160,11 @@ __global__ void __launch_bounds__(32 * kTcWarps, 2) tc_candidates_kernel(TcArgs 
 
   const int q0 = blockIdx.x * kTcQ + warp * 16;
   // query fragments: rows g and g + 8 of the warp's 16 queries
-  uint32_t ah[kTcMaxKs][4], al[kTcMaxKs][4];
+  uint32_t ah[KS][4], al[KS][4];
   {
     const int ra = min(q0 + g, n - 1), rb = min(q0 + g + 8, n - 1);
 #pragma unroll
-    for (int ks = 0; ks < kTcMaxKs; ++ks) {
+    for (int ks = 0; ks < KS; ++ks) {
       uint2 pa = make_uint2(0u, 0u), pb = pa, qa = pa, qb = pa;
       if (ks < ksn) {
         pa = *reinterpret_cast<const uint2*>(A.xh + static_cast<size_t>(ra) * dp + ks * 16 + 4 * tig);
@@ -261,7 +264,7 @@ __global__ void __launch_bounds__(32 * kTcWarps, 2) tc_candidates_kernel(TcArgs 
 #pragma unroll
     for (int nt = 0; nt < 8; ++nt) accs[nt][0] = accs[nt][1] = accs[nt][2] = accs[nt][3] = 0.0f;
 #pragma unroll
-    for (int ks = 0; ks < kTcMaxKs; ++ks) {
+    for (int ks = 0; ks < KS; ++ks) {
       if (ks < ksn) {
 #pragma unroll
         for (int nt = 0; nt < 8; ++nt) {
@@ -570,9 +573,18 @@ int knn_tc_graph(const float* x, int n, int d, int K, int segments, void* scratc
   A.cand_a = cand_a;
   A.bound = bound;
   const size_t smem = tc_smem_bytes(L.rw, L.kp);
-  e = cudaFuncSetAttribute(tc_candidates_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-  if (e != cudaSuccess) return static_cast<int>(e);
-  tc_candidates_kernel<<<dim3((n + kTcQ - 1) / kTcQ, L.segs), 32 * kTcWarps, smem, st>>>(A);
+  const dim3 grid((n + kTcQ - 1) / kTcQ, L.segs);
+  if (L.dp <= 64) {
+    e = cudaFuncSetAttribute(tc_candidates_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(smem));
+    if (e != cudaSuccess) return static_cast<int>(e);
+    tc_candidates_kernel<4><<<grid, 32 * kTcWarps, smem, st>>>(A);
+  } else {
+    e = cudaFuncSetAttribute(tc_candidates_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(smem));
+    if (e != cudaSuccess) return static_cast<int>(e);
+    tc_candidates_kernel<8><<<grid, 32 * kTcWarps, smem, st>>>(A);
+  }
   const float crel = 1e-4f + 2e-6f * static_cast<float>(L.dp);
   tc_rerank_kernel<<<(n + 3) / 4, 128, 0, st>>>(x, n, d, K, L.segs * 2 * L.kp, L.segs, cand, cand_a, bound, nrm,
                                                  flags, reinterpret_cast<const int*>(flags + 1), crel, idx, dist, fb,

@@ -15,7 +15,8 @@ def _same(a, b):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("n,d,K", [(300, 3, 1), (1000, 10, 50), (2500, 16, 30), (3000, 17, 10), (4000, 33, 96),
-                                   (6000, 50, 30), (5000, 64, 20), (20000, 50, 30)])
+                                   (6000, 50, 30), (5000, 64, 20), (20000, 50, 30), (3000, 65, 30),
+                                   (4000, 100, 30), (2500, 128, 64), (12000, 100, 30)])
 def test_tensor_search_matches_oracle(kg, orc, n, d, K):
     x, _ = datasets.gaussian_mixture(n=n, d=d, seed=n + d)
     t = kg.knn_graph(x, K, method="tensor", return_fallback=True)
@@ -54,7 +55,7 @@ def test_tensor_search_non_finite_falls_back(kg):
 
 @pytest.mark.gpu
 def test_tensor_search_limits(kg):
-    x, _ = datasets.gaussian_mixture(n=500, d=80, seed=1)
+    x, _ = datasets.gaussian_mixture(n=500, d=129, seed=1)
     with pytest.raises(ValueError, match="tensor-core"):
         kg.knn_graph(x, 10, method="tensor")
     idx, _ = kg.knn_graph(x, 10)  # auto: the brute force

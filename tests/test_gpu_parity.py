@@ -80,6 +80,17 @@ def test_matrix_raw_mixture(kg, orc):
     _assert_matrix_equal(gpu, ref)
 
 
+@pytest.mark.parametrize("d", [72, 100, 128])
+def test_matrix_raw_high_dim(kg, orc, d):
+    # tensor-core graph and k-means with 16-coordinate k-steps up to 8
+    x, _ = datasets.gaussian_mixture(n=2500, d=d, clusters=9, mean_scale=3.0, seed=d)
+    kw = _matrix_kw(runs=3, cycles=8, graph_neighbors=30, knn_k=10, splitting=100)
+    gpu = kg.KODAMA_matrix(x, materialize_graph=True, **kw)
+    gi, gd = orc.exact_knn(x, 30, threads=8)
+    ref = _oracle_matrix(orc, x, gi, gd, 0, kw)
+    _assert_matrix_equal(gpu, ref)
+
+
 @pytest.mark.parametrize("mode", [
     dict(evolutionary_search=False, guarded_diversity=False, many_to_one_absorption=False, stratified=True),
     dict(evolutionary_search=True, guarded_diversity=True, many_to_one_absorption=True, stratified=False),
