@@ -47,6 +47,12 @@ PLS_METRIC = "KODAMA.matrix PLS-LDA wall-s at N=10k,d=200,ncomp=5,F=10,M=50,Tcyc
 PLS_WORKLOAD = dict(n=10000, d=200, runs=50, cycles=50, graph_neighbors=30, knn_k=30, folds=10,
                     splitting=0, landmarks=10000, seed=1234, components=5)
 PLS_CPU_SAMPLE_RUNS = 16
+# --workload batch: 256 independent KODAMA.matrix problems of uneven size
+# (datasets.uneven_batch: N log-uniform in [500, 20000], d in {10, 50, 100},
+# Gaussian mixtures of 3-20 clusters, half kNN k=10, half PLS-LDA ncomp=5),
+# M=50 runs x Tcycle=50 each, in one captured CUDA graph
+BATCH_METRIC = "256-problem uneven KODAMA.matrix batch wall-s (M=50, Tcycle=50 each, one captured CUDA graph)"
+BATCH_KW = dict(runs=50, cycles=50, knn_k=10, components=5, graph_neighbors=30, folds=10, seed=1234)
 # DRAM bytes (read + write) of one evolution-kernel launch, scaled from the
 # ncu capture summarised in profiles/evolve_kernel_cfg2.md (None until captured).
 EVOLVE_TRAFFIC_BYTES = 457883648
@@ -292,9 +298,160 @@ def run_gpu_pls(args):
     print(json.dumps(line))
 
 
+def _batch_config(extra=None):
+    c = {"workload": "256 independent KODAMA.matrix problems: N log-uniform [500, 20000], d in {10, 50, 100}, "
+                     "Gaussian mixtures of 3-20 clusters (means ~ N(0, 9 I)), even problems kNN (knn.k=10), odd "
+                     "PLS-LDA (ncomp=5); M=50 runs x Tcycle=50 each, exact graph K=30, folds=10, default "
+                     "landmarks/splitting; one captured CUDA graph, schedule autotuned",
+         "global_batch": 256 * BATCH_KW["runs"], "seq_len": BATCH_KW["cycles"], "parallelism": "replicas",
+         "l2": "inputs (1.6 M rows) larger than L2", "data": "synthetic uneven_batch(seed=4)"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+def _batch_cost(n, d, L, cls, runs, cycles):
+    # the library's own dealing estimate (api.cu batch_cost), used to scale
+    # the CPU sample to the whole batch
+    graph = n * n * d * 1e-9
+    evolve = runs * (cycles + 1) * L * ((d + 20.0) * 2e-9 if cls == "pls" else 4e-9)
+    return graph + evolve + runs * L * d * 1e-8
+
+
+def batch_cpu_baseline(problems, threads=None):
+    """The CPU restatement on a bounded sample of the batch: per classifier
+    the three problems nearest that classifier's median cost, each timed as the
+    exact graph, the atlas and min(threads, 16) runs (run waves scaled to
+    M=50); the per-classifier seconds-per-cost ratio then prices every
+    problem of the batch."""
+    from oracle import oracle
+    if not oracle.available():
+        oracle.build()
+    threads = threads or os.cpu_count() or 1
+    kw = dict(BATCH_KW)
+    seed = kw.pop("seed")
+    runs = kw["runs"]
+    costs = []
+    for pr in problems:
+        n, d = pr["x"].shape
+        L = int(np.ceil(0.75 * n)) if 10000 >= n else 10000
+        costs.append(_batch_cost(n, d, L, pr["classifier"], runs, kw["cycles"]))
+    ratio, timed = {}, []
+    for cls in ("knn", "pls"):
+        idx = [i for i, pr in enumerate(problems) if pr["classifier"] == cls]
+        med = float(np.median([costs[i] for i in idx]))
+        pick = sorted(idx, key=lambda i: abs(costs[i] - med))[:3]
+        tsum, csum = 0.0, 0.0
+        for i in pick:
+            x = np.ascontiguousarray(problems[i]["x"], np.float32)
+            sample_runs = min(threads, 16)
+            t0 = time.perf_counter()
+            gi, gd = oracle.exact_knn(x, kw["graph_neighbors"], threads=threads)
+            t_graph = time.perf_counter() - t0
+            r = oracle.kodama_matrix_graph_data(
+                x, gi, gd, 0, seed=seed, threads=threads, materialize=0, classifier=1 if cls == "pls" else 0,
+                runs=sample_runs, cycles=kw["cycles"], graph_neighbors=kw["graph_neighbors"], folds=kw["folds"],
+                knn_k=kw["knn_k"], components=kw["components"], landmarks=10000, splitting=0)
+            t_atlas, t_runs = float(r.timings[4]), float(r.timings[2])
+            waves = -(-runs // threads) / -(-sample_runs // threads)
+            t = t_graph + t_atlas + t_runs * waves
+            timed.append({"problem": i, "classifier": cls, "n": int(x.shape[0]), "d": int(x.shape[1]),
+                          "seconds": round(t, 3)})
+            tsum += t
+            csum += costs[i]
+        ratio[cls] = tsum / csum
+    total = sum(ratio[pr["classifier"]] * c for pr, c in zip(problems, costs))
+    return {"value": round(total, 3), "unit": "s", "cores": threads, "kind": "port",
+            "sample": "3 kNN + 3 PLS-LDA problems nearest their classifier's median cost, each graph + atlas + "
+                      f"min(threads,16) runs (waves scaled to M={runs}); batch priced by seconds per cost unit",
+            "timed": timed}
+
+
+def run_gpu_batch(args):
+    import torch
+
+    import kodama_gb300 as kg
+    from kodama_gb300 import build as kbuild
+    from kodama_gb300 import datasets
+
+    kbuild.build()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    problems = datasets.uneven_batch()
+    kw = dict(BATCH_KW)
+    t0 = time.perf_counter()
+    res, rep = kg.KODAMA_matrix_batch(problems, device=local, **kw)
+    first_call = time.perf_counter() - t0
+    tune_s = rep.tune_ms / 1000.0 if rep.rebuilt else 0.0
+    for _ in range(max(0, args.warmup - 1)):
+        kg.KODAMA_matrix_batch(problems, device=local, **kw)
+    dev, e2e, accs = [], [], []
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            res, rep = kg.KODAMA_matrix_batch(problems, device=local, **kw)
+            e2e.append(time.perf_counter() - t0)
+            dev.append(rep.device_ms / 1000.0)
+            accs.append(float(np.mean([r.acc.mean() for r in res])))
+        torch.cuda.synchronize()
+    value = float(np.mean(dev))
+    runs, cycles = kw["runs"], kw["cycles"]
+    h2d = int(sum(p["x"].nbytes for p in problems))
+    d2h = int(sum(runs * p["x"].shape[0] * 4 + runs * cycles * (8 + 20) + runs * 72 for p in problems))
+    # algorithmic bytes of the evolution of every problem: kNN vote tables
+    # per CV evaluation, PLS standardised rows streamed per evaluation
+    algo = 0
+    for p in problems:
+        n, d = p["x"].shape
+        L = int(np.ceil(0.75 * n)) if 10000 >= n else 10000
+        if p["classifier"] == "knn":
+            algo += evolve_bytes_per_launch(L, min(kw["knn_k"], kw["graph_neighbors"]), runs, cycles)
+        else:
+            F = kw["folds"]
+            nt = L - L // F
+            algo += runs * F * (2 * nt + (L - nt)) * d * 4 * (cycles + 1)
+    peak, peak_kind = _peaks()
+    achieved = algo / value / 1e9
+    line = {"metric": BATCH_METRIC, "value": round(value, 4), "unit": "s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(value * 1000, 2), "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32/f32/f64", "data": "synthetic",
+            "config": _batch_config({"lanes": rep.lanes, "order": "longest first" if rep.order == 1 else "round robin"}),
+            "e2e": {"value": round(float(np.mean(e2e)), 4), "unit": "s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                         "kernel": "whole batch graph (evolution traffic of all 256 problems over the graph time; "
+                                   "the PLS eval_kernel dominates and is issue-bound)",
+                         "algorithmic_bytes_per_launch": int(algo), "traffic": None},
+            "gpu_launches": int(rep.kernel_nodes), "graph_nodes": int(rep.graph_nodes),
+            "clocks": clocks.summary(),
+            "first_call_s": round(first_call, 2), "autotune_s": round(tune_s, 2),
+            "mean_final_cv_acc": round(float(np.mean(accs)), 6)}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = batch_cpu_baseline(problems)
+    print(json.dumps(line))
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
+        return
+    if args.workload == "batch":
+        from kodama_gb300 import datasets
+        problems = datasets.uneven_batch()
+        vals, last = [], None
+        for _ in range(args.steps):
+            last = batch_cpu_baseline(problems)
+            vals.append(last["value"])
+        v = float(np.mean(vals))
+        print(json.dumps({"metric": BATCH_METRIC, "value": round(v, 3), "unit": "s", "n_gpus": args.gpus,
+                          "steps": args.steps, "warmup": 0, "ms_per_step": round(v * 1000, 1),
+                          "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+                          "dtype": "int32/f32/f64", "data": "synthetic", "config": _batch_config(),
+                          "impl": "reference", "cpu_baseline": dict(last, value=round(v, 3)),
+                          "e2e": {"value": round(v, 3), "unit": "s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}))
         return
     x = _data()
     for _ in range(args.warmup):
@@ -485,13 +642,16 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-proposal comparison")
-    ap.add_argument("--workload", default="knn", choices=["knn", "pls"],
-                    help="knn: the headline configuration; pls: the PLS-LDA configuration")
+    ap.add_argument("--workload", default="knn", choices=["knn", "pls", "batch"],
+                    help="knn: the headline configuration; pls: the PLS-LDA configuration; batch: 256 uneven "
+                         "problems in one captured CUDA graph")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "pls":
         run_gpu_pls(args)
+    elif args.workload == "batch":
+        run_gpu_batch(args)
     else:
         run_gpu(args)
 

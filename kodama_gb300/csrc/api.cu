@@ -1854,7 +1854,7 @@ void batch_entry(const kgb_matrix_problem* probs, int count, const kgb_batch_opt
       g_tuned[key] = {bl, bo2};
       lanes = bl;
       order = bo2;
-      tune_ms = clk.lap();
+      tune_ms = clk.lap() * 1000.0;
       rebuilt = true;
     }
   }
