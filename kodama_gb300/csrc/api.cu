@@ -685,6 +685,9 @@ PlsBuffers pls_buffers(Ctx& ctx, const float* d_X, int R, int L, int p, const Pl
   e.W = ctx.alloc<float>(static_cast<size_t>(S) * p * max_components);
   e.V = ctx.alloc<float>(static_cast<size_t>(S) * p * max_components);
   e.T = ctx.alloc<float>(static_cast<size_t>(S) * L * requested);
+  e.Tt = ctx.alloc<float>(static_cast<size_t>(S) * L * requested);
+  e.pos = ctx.alloc<uint16_t>(static_cast<size_t>(S) * L);
+  e.posok = ctx.alloc<uint8_t>(static_cast<size_t>(S) * L);
   e.sc = ctx.alloc<float>(static_cast<size_t>(S) * L);
   return b;
 }

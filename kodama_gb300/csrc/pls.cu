@@ -365,21 +365,71 @@ __device__ __forceinline__ void warp_scores(const float* __restrict__ base, int 
   }
 }
 
-// Sequential float chain over list entries b..e-1, warp-cooperative: lanes
-// fetch 32 entries at a time, then every lane adds them in list order.
-// val(i, v) stores the term of entry i and returns whether it counts.
-template <class Val>
-__device__ float warp_chain(int b, int e, Val val, int lane) {
+// Sequential float chain over positions b..e-1 of a row-major matrix
+// (stride ld, column c) counting only the positions whose flag is set,
+// warp-cooperative: each 32-position group is loaded D groups ahead, then
+// every lane adds the group's values in position order.
+template <int D>
+__device__ float warp_masked_chain(const float* __restrict__ m, int ld, int c, const uint8_t* __restrict__ ok, int b,
+                                   int e, int lane) {
   float acc = 0.0f;
-  for (int base = b; base < e; base += 32) {
-    const int i = base + lane;
-    float v = 0.0f;
-    const bool ok = i < e && val(i, v);
-    const unsigned msk = __ballot_sync(kFull, ok);
+  float v[D];
+  bool f[D];
+#pragma unroll
+  for (int g = 0; g < D; ++g) {
+    const int i = b + g * 32 + lane;
+    v[g] = i < e ? m[static_cast<size_t>(i) * ld + c] : 0.0f;
+    f[g] = i < e && ok[i] != 0;
+  }
+  for (int base = b; base < e; base += 32 * D) {
+#pragma unroll
+    for (int g = 0; g < D; ++g) {
+      const int gb = base + g * 32;
+      if (gb >= e) break;
+      const unsigned msk = __ballot_sync(kFull, f[g]);
+      const float cur = v[g];
+      const int i = gb + D * 32 + lane;
+      v[g] = i < e ? m[static_cast<size_t>(i) * ld + c] : 0.0f;
+      f[g] = i < e && ok[i] != 0;
 #pragma unroll 8
-    for (int q = 0; q < 32; ++q) {
-      const float t = __shfl_sync(kFull, v, q);
-      if ((msk >> q) & 1u) acc = __fadd_rn(acc, t);
+      for (int q = 0; q < 32; ++q) {
+        const float t = __shfl_sync(kFull, cur, q);
+        if ((msk >> q) & 1u) acc = __fadd_rn(acc, t);
+      }
+    }
+  }
+  return acc;
+}
+
+// Sequential float chain sum_i a_i * b_i over i = 0..n-1 (rows of a
+// row-major matrix with stride ld, columns ca and cb), warp-cooperative like
+// warp_chain; each 32-row group's operands are loaded D groups ahead of its
+// products and adds, so nothing waits on a fresh load.
+template <int D>
+__device__ float warp_product_chain(const float* __restrict__ m, int n, int ld, int ca, int cb, int lane) {
+  float acc = 0.0f;
+  float va[D], vb[D];
+#pragma unroll
+  for (int g = 0; g < D; ++g) {
+    const int i = g * 32 + lane;
+    va[g] = i < n ? m[static_cast<size_t>(i) * ld + ca] : 0.0f;
+    vb[g] = i < n ? m[static_cast<size_t>(i) * ld + cb] : 0.0f;
+  }
+  for (int base = 0; base < n; base += 32 * D) {
+#pragma unroll
+    for (int g = 0; g < D; ++g) {
+      const int gb = base + g * 32;
+      if (gb >= n) break;
+      const float prod = __fmul_rn(va[g], vb[g]);
+      const int i = gb + D * 32 + lane;
+      va[g] = i < n ? m[static_cast<size_t>(i) * ld + ca] : 0.0f;
+      vb[g] = i < n ? m[static_cast<size_t>(i) * ld + cb] : 0.0f;
+      const int cnt = min(32, n - gb);
+#pragma unroll 8
+      for (int q = 0; q < 32; ++q) {
+        const float t = __shfl_sync(kFull, prod, q);
+        if (q < cnt) acc = __fadd_rn(acc, t);
+      }
     }
   }
   return acc;
@@ -442,6 +492,14 @@ __global__ void __launch_bounds__(kEvalThreads, 2) eval_kernel(PlsEvalArgs a) {
     sh.m = m;
     sh.nt = te - tb;
     a.status[s] = 0;
+  }
+  // class-list position of every row, and whether that position trains the slice
+  uint16_t* posof = a.pos + static_cast<size_t>(s) * L;
+  uint8_t* posok = a.posok + static_cast<size_t>(s) * L;
+  for (int i = threadIdx.x; i < L; i += kEvalThreads) {
+    const int row = crow[i];
+    posof[row] = static_cast<uint16_t>(i);
+    posok[i] = (fold == nullptr || fold[row] != f) ? 1 : 0;
   }
   __syncthreads();
   const int m = sh.m, nt = sh.nt;
@@ -692,7 +750,8 @@ __global__ void __launch_bounds__(kEvalThreads, 2) eval_kernel(PlsEvalArgs a) {
 
   // --- LDA on the first nc score columns -----------------------------------
   const int nc = a.predict_mode ? fitted : min(a.requested, fitted);
-  float* Ts = a.T + static_cast<size_t>(s) * L * NCm;  // by row: Ts[row * nc + q]
+  float* Ts = a.T + static_cast<size_t>(s) * L * NCm;   // by class-list position: Ts[pos * nc + q]
+  float* Tt = a.Tt + static_cast<size_t>(s) * L * NCm;  // by training position: Tt[t * nc + q]
   {
     float* tile = tiles + warp * kTile;
     for (int b0 = warp * 32; b0 < nt; b0 += kEvalWarps * 32) {
@@ -703,50 +762,40 @@ __global__ void __launch_bounds__(kEvalThreads, 2) eval_kernel(PlsEvalArgs a) {
         float acc[kMaxNC];
         warp_scores(Zs, p, row, Wsm, ldw, q0, nq, tile, lane, acc);
         if (row >= 0) {
+          const size_t ps = static_cast<size_t>(posof[row]) * nc;
 #pragma unroll
-          for (int q = 0; q < kMaxNC; ++q)
-            if (q < nq) Ts[static_cast<size_t>(row) * nc + q0 + q] = acc[q];
+          for (int q = 0; q < kMaxNC; ++q) {
+            if (q < nq) {
+              Ts[ps + q0 + q] = acc[q];
+              Tt[static_cast<size_t>(t) * nc + q0 + q] = acc[q];
+            }
+          }
         }
       }
     }
   }
   __syncthreads();
-  // class sums (rows of each class in order) and score cross-products (all
-  // training rows in order): one warp per chain
+  // class sums (the training rows of each class in row order, i.e. the
+  // flagged class-list positions in order): one warp per chain
   const int ncs = m * nc, ncp = nc * (nc + 1) / 2;
-  for (int it = warp; it < ncs + ncp; it += kEvalWarps) {
-    float acc;
-    int k = 0, q = 0, rr = 0, col = 0;
-    if (it < ncs) {
-      k = it / nc;
-      q = it % nc;
-      const int code = klist[k];
-      acc = warp_chain(coff[code], coff[code + 1], [&](int i, float& v) {
-        const int row = crow[i];
-        if (fold != nullptr && fold[row] == f) return false;
-        v = Ts[static_cast<size_t>(row) * nc + q];
-        return true;
-      }, lane);
-    } else {
-      int pr = it - ncs;
-      while (pr > rr) {
-        pr -= rr + 1;
-        ++rr;
-      }
-      col = pr;
-      acc = warp_chain(0, nt, [&](int i, float& v) {
-        const float* tr = Ts + static_cast<size_t>(tix[i]) * nc;
-        v = __fmul_rn(tr[rr], tr[col]);
-        return true;
-      }, lane);
+  for (int it = warp; it < ncs; it += kEvalWarps) {
+    const int k = it / nc, q = it % nc;
+    const int code = klist[k];
+    const float acc = warp_masked_chain<2>(Ts, nc, q, posok, coff[code], coff[code + 1], lane);
+    if (lane == 0) cs[k * nc + q] = acc;
+  }
+  // score cross-products (all training rows in order): one warp per chain
+  for (int it = warp; it < ncp; it += kEvalWarps) {
+    int pr = it, rr = 0;
+    while (pr > rr) {
+      pr -= rr + 1;
+      ++rr;
     }
+    const int col = pr;
+    const float acc = warp_product_chain<4>(Tt, nt, nc, rr, col, lane);
     if (lane == 0) {
-      if (it < ncs) {
-        cs[k * nc + q] = acc;
-      } else {
-        cp[rr * nc + col] = acc;
-        cp[col * nc + rr] = acc;
-      }
+      cp[rr * nc + col] = acc;
+      cp[col * nc + rr] = acc;
     }
   }
   __syncthreads();

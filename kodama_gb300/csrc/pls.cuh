@@ -73,7 +73,10 @@ struct PlsEvalArgs {
   float* s_scr;          // S x p x C0max
   float* W;              // S x p x max_components
   float* V;              // S x p x max_components
-  float* T;              // S x L x requested (training-row scores)
+  float* T;              // S x L x requested (training-row scores, by class-list position)
+  float* Tt;             // S x L x requested (the same scores in training order)
+  uint16_t* pos;         // S x L: position of each row in the slice's class list
+  uint8_t* posok;        // S x L: whether the row at a class-list position trains the slice
   float* sc;             // S x L (scores path of the fit)
 };
 
