@@ -629,7 +629,7 @@ def PLSLDAPredict(train, labels, test, *, max_components=10, fixed_components=0,
     return out
 
 
-def CorePLSLDA(x, labels, *, constrain=None, fixed=None, cycles=100, folds=10, stratified=False,
+def CorePLSLDA(x, labels, *, constrain=None, fixed=None, cycles=100, folds=10, stratified=True,
                max_components=10, fixed_components=0, center=True, scale=True,
                evolutionary_search=False, guarded_diversity=False, many_to_one_absorption=False,
                adaptive_proposal_size=True, auto_class_coarsening=False, seed=1, cv_seed=1,

@@ -589,12 +589,55 @@ PlsSlices pls_slices(const std::vector<std::vector<int>>& folds, int R, int L, b
   return sl;
 }
 
+// One problem's slices padded with absent (empty) slices up to F.
+PlsSlices pad_slices(PlsSlices sl, int F) {
+  for (int f = sl.F; f < F; ++f) {
+    sl.train_off.push_back(sl.train_off.back());
+    sl.val_off.push_back(sl.val_off.back());
+    sl.ntrain.push_back(0);
+    sl.present.push_back(0);
+  }
+  sl.F = std::max(sl.F, F);
+  return sl;
+}
+
 struct PlsBuffers {
   kgb::PlsPrepArgs prep{};
   kgb::PlsEvalArgs ev{};
   int S = 0;
   std::vector<int> ntrain, present;
 };
+
+// Device room for slices that change at every evaluation (stratified folds of
+// the labels being evaluated): one problem of n rows and up to F slices.
+struct PlsSliceRoom {
+  int* train_off = nullptr;
+  int* train_idx = nullptr;
+  int* val_off = nullptr;
+  int* val_idx = nullptr;
+  uint8_t* folds = nullptr;
+  float* logprior = nullptr;
+  int* lp_off = nullptr;
+};
+
+// logf(max(k / nt, FLT_MIN)) for every count k of a class of each slice, one
+// table per distinct training size.
+void pls_logprior_tables(const std::vector<int>& ntrain, std::vector<float>& tables, std::vector<int>& lp_off) {
+  std::map<int, int> table_of;
+  tables.clear();
+  lp_off.assign(ntrain.size(), 0);
+  for (size_t s2 = 0; s2 < ntrain.size(); ++s2) {
+    const int nt = ntrain[s2];
+    auto it = table_of.find(nt);
+    if (it == table_of.end()) {
+      it = table_of.emplace(nt, static_cast<int>(tables.size())).first;
+      const float den = static_cast<float>(std::max(1, nt));
+      for (int k = 0; k <= nt; ++k)
+        tables.push_back(std::log(std::max(static_cast<float>(k) / den, std::numeric_limits<float>::min())));
+    }
+    lp_off[s2] = it->second;
+  }
+}
 
 // Statistics, standardised rows and evaluation scratch of a set of slices.
 // d_X: R x L x p rows; d_Xv: R x NV x p rows to predict (predict mode) or null.
@@ -661,21 +704,9 @@ PlsBuffers pls_buffers(Ctx& ctx, const float* d_X, int R, int L, int p, const Pl
   e.NV = NV;
   const std::vector<float> w0 = pls_start_vector(p);
   e.w0 = ctx.upload(w0.data(), w0.size());
-  // logf(max(k / nt, FLT_MIN)) for every count k of a class of the slice
-  std::map<int, int> table_of;
   std::vector<float> tables;
-  std::vector<int> lp_off(static_cast<size_t>(S));
-  for (int s2 = 0; s2 < S; ++s2) {
-    const int nt = sl.ntrain[s2];
-    auto it = table_of.find(nt);
-    if (it == table_of.end()) {
-      it = table_of.emplace(nt, static_cast<int>(tables.size())).first;
-      const float den = static_cast<float>(std::max(1, nt));
-      for (int k = 0; k <= nt; ++k)
-        tables.push_back(std::log(std::max(static_cast<float>(k) / den, std::numeric_limits<float>::min())));
-    }
-    lp_off[s2] = it->second;
-  }
+  std::vector<int> lp_off;
+  pls_logprior_tables(sl.ntrain, tables, lp_off);
   e.logprior = ctx.upload(tables.data(), tables.size());
   e.lp_off = ctx.upload(lp_off.data(), lp_off.size());
   e.pred = ctx.alloc<uint16_t>(static_cast<size_t>(R) * (e.predict_mode ? NV : L));
@@ -690,6 +721,34 @@ PlsBuffers pls_buffers(Ctx& ctx, const float* d_X, int R, int L, int p, const Pl
   e.posok = ctx.alloc<uint8_t>(static_cast<size_t>(S) * L);
   e.sc = ctx.alloc<float>(static_cast<size_t>(S) * L);
   return b;
+}
+
+// Moves one problem's slice set (pad_slices to the buffers' S) into the
+// room and recomputes the fold statistics and standardised rows.
+void pls_refresh_slices(Ctx& ctx, PlsBuffers& b, const PlsSliceRoom& room, const PlsSlices& sl, int n) {
+  if (sl.F != b.S) fail(KGB_EINTERNAL, "slice count changed");
+  ctx.h2d(room.train_off, sl.train_off.data(), sl.train_off.size());
+  ctx.h2d(room.train_idx, sl.train_idx.data(), sl.train_idx.size());
+  ctx.h2d(room.val_off, sl.val_off.data(), sl.val_off.size());
+  ctx.h2d(room.val_idx, sl.val_idx.data(), sl.val_idx.size());
+  ctx.h2d(room.folds, sl.folds8.data(), static_cast<size_t>(n));
+  std::vector<float> tables;
+  std::vector<int> lp_off;
+  pls_logprior_tables(sl.ntrain, tables, lp_off);
+  ctx.h2d(room.logprior, tables.data(), tables.size());
+  ctx.h2d(room.lp_off, lp_off.data(), lp_off.size());
+  b.ntrain = sl.ntrain;
+  b.present = sl.present;
+  b.prep.train_off = room.train_off;
+  b.prep.train_idx = room.train_idx;
+  b.ev.train_off = room.train_off;
+  b.ev.train_idx = room.train_idx;
+  b.ev.val_off = room.val_off;
+  b.ev.val_idx = room.val_idx;
+  b.ev.folds = room.folds;
+  b.ev.logprior = room.logprior;
+  b.ev.lp_off = room.lp_off;
+  ck_launch(kgb::pls_prepare(b.prep, ctx.stream()), "PLS fold preparation");
 }
 
 // Builds the fold Gram matrices (slices with at least p training rows) and
@@ -749,8 +808,11 @@ void pls_check_status(Ctx& ctx, const PlsBuffers& b, PlsStatusSink* sink = nullp
 // maximize_core with the PLS-LDA predictor for P.problems problems whose
 // slices are in `b`: the cycle loop of alternating evolution steps and CV
 // evaluations.  P carries everything but the outputs and scratch.
+// before_eval (may be empty) runs before every evaluation (the labels to
+// evaluate are in b.ev.labels); with it the fold Gram is never used.
 EvolveBuffers run_pls_evolution(Ctx& ctx, kgb::EvolveParams P, PlsBuffers& b, int C0max, bool coarsening,
-                                const kgb_policy& pol, PlsStatusSink* sink = nullptr) {
+                                const kgb_policy& pol, PlsStatusSink* sink = nullptr,
+                                const std::function<void()>& before_eval = {}) {
   const int problems = P.problems, L = P.L, T = P.T;
   cudaStream_t st = ctx.stream();
   EvolveBuffers eb;
@@ -845,7 +907,11 @@ EvolveBuffers run_pls_evolution(Ctx& ctx, kgb::EvolveParams P, PlsBuffers& b, in
   Q.cycle = 0;
   ck_launch(kgb::evolve_pls_launch(Q, grid, smem, st), "PLS evolution step");
   for (int cycle = 0; cycle <= T; ++cycle) {
-    if (cycle == 1) pls_enable_gram(ctx, b);
+    if (before_eval) {
+      before_eval();
+    } else if (cycle == 1) {
+      pls_enable_gram(ctx, b);
+    }
     ck_launch(kgb::pls_evaluate(b.ev, st), "PLS-LDA evaluation");
     Q.phase = 1;
     Q.cycle = cycle;
@@ -2376,12 +2442,11 @@ int kgb_core_plslda(const float* x, int32_t n, int32_t p, const int32_t* labels,
     if (n > 65535) fail(KGB_EINVAL, "at most 65535 rows are supported");
     if (opt->cycles < 0) fail(KGB_EINVAL, "Core cycles must be non-negative.");
     check_pls_options(pls);
-    if (pls->stratified)
-      fail(KGB_EINVAL, "stratified folds are not supported by the CUDA CorePLSLDA entry point (set stratified = 0)");
+    const bool strat = pls->stratified != 0;
     const kgb_policy pol = policy_is_zero(opt->policy) ? default_policy() : opt->policy;
     const std::vector<int> lab(labels, labels + n);
     const std::vector<int> con = constrain ? std::vector<int>(constrain, constrain + n) : std::vector<int>();
-    const std::vector<int> folds = kgb::make_folds(lab, con, pls->folds, false, pls->cv_seed);
+    const std::vector<int> folds = kgb::make_folds(lab, con, pls->folds, strat, pls->cv_seed);
     const uint64_t bc = kgb::unordered_bucket_count(static_cast<size_t>(n));
     const Coding cd = code_labels(labels, n, bc);
     const int C0 = static_cast<int>(cd.code2label.size());
@@ -2405,9 +2470,36 @@ int kgb_core_plslda(const float* x, int32_t n, int32_t p, const int32_t* labels,
     const int requested = pls->fixed_components > 0 ? pls->fixed_components : pls->max_components;
     Ctx ctx(pls->device);
     const float* d_x = ctx.upload(x, static_cast<size_t>(n) * p);
-    const PlsSlices sl = pls_slices({folds}, 1, n, false);
+    // stratified folds follow the labels under evaluation (core_pls_lda: each
+    // evaluation is a fresh PLSLDACV, core.cpp:1626-1646), so the slices are
+    // rebuilt before every evaluation and no fold Gram is kept
+    const PlsSlices sl = strat ? pad_slices(pls_slices({folds}, 1, n, false), pls->folds)
+                               : pls_slices({folds}, 1, n, false);
     PlsBuffers b = pls_buffers(ctx, d_x, 1, n, p, sl, C0max, pls->max_components, requested, pls->center != 0,
                                pls->scale != 0, nullptr, 0);
+    PlsSliceRoom room;
+    std::function<void()> refresh;
+    if (strat) {
+      const int F = sl.F;
+      room.train_off = ctx.alloc<int>(static_cast<size_t>(F) + 1);
+      room.train_idx = ctx.alloc<int>(static_cast<size_t>(F) * n);
+      room.val_off = ctx.alloc<int>(static_cast<size_t>(F) + 1);
+      room.val_idx = ctx.alloc<int>(static_cast<size_t>(n));
+      room.folds = ctx.alloc<uint8_t>(static_cast<size_t>(n));
+      room.logprior = ctx.alloc<float>(static_cast<size_t>(F) * (n + 1));
+      room.lp_off = ctx.alloc<int>(static_cast<size_t>(F));
+      refresh = [&, F]() {
+        std::vector<uint16_t> codes(static_cast<size_t>(n));
+        ctx.download(codes.data(), b.ev.labels, codes.size());
+        ctx.sync();
+        std::vector<int> cur(static_cast<size_t>(n));
+        for (int i = 0; i < n; ++i) cur[i] = cd.code2label[codes[i]];
+        const std::vector<int> fo = kgb::make_folds(cur, con, pls->folds, true, pls->cv_seed);
+        const PlsSlices s2 = pad_slices(pls_slices({fo}, 1, n, false), F);
+        if (s2.F != F) fail(KGB_EINTERNAL, "more folds than the stratified slice room holds");
+        pls_refresh_slices(ctx, b, room, s2, n);
+      };
+    }
     std::vector<int> c2l(static_cast<size_t>(C0max), 0);
     std::copy(cd.code2label.begin(), cd.code2label.end(), c2l.begin());
     const int nco = C0;
@@ -2440,7 +2532,8 @@ int kgb_core_plslda(const float* x, int32_t n, int32_t p, const int32_t* labels,
     P.goff = ctx.upload(goff.data(), goff.size());
     P.gmem = ctx.upload(gmem.data(), gmem.size());
     P.seeds = ctx.upload(&seed, 1);
-    const EvolveBuffers eb = run_pls_evolution(ctx, P, b, C0max, opt->auto_class_coarsening != 0, pol);
+    const EvolveBuffers eb =
+        run_pls_evolution(ctx, P, b, C0max, opt->auto_class_coarsening != 0, pol, nullptr, refresh);
     const int T = opt->cycles;
     std::vector<uint16_t> cb(static_cast<size_t>(n)), cp(static_cast<size_t>(n));
     std::vector<double> va(static_cast<size_t>(std::max(T, 1))), vs(va.size()), best(2);

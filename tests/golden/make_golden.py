@@ -197,6 +197,9 @@ def main():
     cases.append(core_plslda_case("core_plslda_evolutionary", dict(n=900, d=40, seed=34, random_labels=10),
                                   cycles=20, folds=5, stratified=False, components=5, evolutionary=True,
                                   guarded=True, absorption=True, coarsening=True, seed=13, cv_seed=14))
+    cases.append(core_plslda_case("core_plslda_stratified", dict(n=700, d=30, seed=36, random_labels=6),
+                                  cycles=12, folds=5, stratified=True, components=4, evolutionary=True,
+                                  guarded=True, absorption=True, coarsening=False, seed=15, cv_seed=16))
     cases.append(pls_matrix_case("pls_matrix_N1500_d50_M4_T12", dict(n=1500, d=50, seed=35), 20,
                                  seed=99, runs=4, cycles=12, landmarks=10000, splitting=20,
                                  graph_neighbors=20, folds=5, knn_k=10, components=5))

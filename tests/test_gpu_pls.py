@@ -54,17 +54,19 @@ def test_plsldapredict_matches_oracle(kg, orc, n, nt, d, comp):
     assert np.array_equal(got, want)
 
 
-@pytest.mark.parametrize("coarsening,constrained", [(True, False), (False, False), (True, True)])
-def test_core_plslda_matches_oracle(kg, orc, coarsening, constrained):
+@pytest.mark.parametrize("coarsening,constrained,stratified", [(True, False, False), (False, False, False),
+                                                               (True, True, False), (True, False, True),
+                                                               (False, True, True)])
+def test_core_plslda_matches_oracle(kg, orc, coarsening, constrained, stratified):
     x, _ = datasets.low_rank(n=600, d=30, seed=5)
     rng = np.random.default_rng(6)
     labels = rng.integers(1, 12, 600).astype(np.int32)
     con = np.arange(1, 601, dtype=np.int32) if not constrained else rng.integers(0, 300, 600).astype(np.int32)
     fix = (rng.random(600) < 0.05).astype(np.int32) if constrained else None
-    kw = dict(cycles=15, folds=5, stratified=False, evolutionary=True, guarded=True, absorption=True,
+    kw = dict(cycles=15, folds=5, stratified=stratified, evolutionary=True, guarded=True, absorption=True,
               coarsening=coarsening, seed=11, cv_seed=12)
     a = orc.core_plslda(x, labels, constrain=con, fixed=fix, components=4, **kw)
-    b = kg.CorePLSLDA(x, labels, constrain=con, fixed=fix, cycles=15, folds=5, stratified=False,
+    b = kg.CorePLSLDA(x, labels, constrain=con, fixed=fix, cycles=15, folds=5, stratified=stratified,
                       max_components=4, fixed_components=4, evolutionary_search=True,
                       guarded_diversity=True, many_to_one_absorption=True,
                       auto_class_coarsening=coarsening, seed=11, cv_seed=12)
