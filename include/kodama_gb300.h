@@ -136,6 +136,23 @@ int kgb_kodama_matrix(const float* x, int32_t n, int32_t d, const kgb_matrix_opt
 int kgb_kodama_matrix_resident(const float* x_device, int32_t n, int32_t d, const kgb_matrix_options* opt,
                                kgb_matrix_result* out);
 
+/* Resident graph: KODAMAGraph_CUDA (kodama.hpp:1112-1115,
+ * kodama_matrix.cpp:4057-4216) keeps the data and the exact kNN graph
+ * (neighbors columns, at most n - 1) in device memory behind an opaque
+ * handle, as KODAMAGraphHandle does (kodama.hpp:481-504); every call on a
+ * handle holds its lock.  kgb_graph_materialize copies the graph out
+ * (indices one-based, KODAMAGraphMaterialize); kgb_kodama_matrix_graph is
+ * KODAMAMatrix(x, KODAMAGraphResult) (kodama.hpp:1156-1163): the
+ * graph-input path on the resident data and graph, its first
+ * min(neighbors, graph width) columns. */
+typedef struct kgb_graph_handle kgb_graph_handle;
+int kgb_graph_create(const float* x, int32_t n, int32_t d, int32_t neighbors, int32_t device,
+                     kgb_graph_handle** out);
+int kgb_graph_info(const kgb_graph_handle* graph, int32_t* n, int32_t* d, int32_t* neighbors);
+int kgb_graph_materialize(kgb_graph_handle* graph, int32_t* idx, float* dist);
+int kgb_kodama_matrix_graph(kgb_graph_handle* graph, const kgb_matrix_options* opt, kgb_matrix_result* out);
+void kgb_graph_destroy(kgb_graph_handle* graph);
+
 /* A batch of independent KODAMA.matrix problems (each as kgb_kodama_matrix
  * with raw data; no semi-supervised inputs, learned proposal or snapshots).
  * Not a reference entry point: the reference runs such a batch as separate

@@ -25,7 +25,7 @@ import numpy as np
 
 from . import _native as N
 
-__all__ = ["KODAMA_matrix_batch", "train_proposal", "proposal_gradient", "proposal_predict", "KODAMA_matrix", "CoreKNNGraph", "CoreKNNGraph_batch", "knn_graph",
+__all__ = ["KODAMAGraph", "KODAMA_matrix_batch", "train_proposal", "proposal_gradient", "proposal_predict", "KODAMA_matrix", "CoreKNNGraph", "CoreKNNGraph_batch", "knn_graph",
            "KODAMADissimilarityInPlace", "PLSLDACV", "PLSLDAPredict", "CorePLSLDA", "PLSCVResult", "MatrixResult", "CoreResult", "EvolutionPolicy",
            "library_path", "version", "launch_count"]
 
@@ -116,13 +116,64 @@ def _matrix_options(runs, cycles, landmarks, splitting, graph_neighbors, folds, 
                            policy=pol._c())
 
 
+class KODAMAGraph:
+    """KODAMAGraph with backend="cuda" (kgb_graph_create): the data and its
+    exact kNN graph kept resident on the device; ``matrix`` runs
+    KODAMA.matrix on them without rebuilding the graph (KODAMAMatrix(x,
+    KODAMAGraphResult)).  Use as a context manager or call ``close``."""
+
+    def __init__(self, x, neighbors=100, device=0):
+        xa = np.ascontiguousarray(x, dtype=np.float32)
+        if xa.ndim != 2:
+            raise ValueError("x must be a 2-D matrix")
+        self.n, self.d = xa.shape
+        self.device = device
+        h = ctypes.c_void_p()
+        N.check(N.load().kgb_graph_create(_ptr(xa), self.n, self.d, neighbors, device, ctypes.byref(h)))
+        self._h = h
+        k = ctypes.c_int32()
+        N.check(N.load().kgb_graph_info(self._h, None, None, ctypes.byref(k)))
+        self.neighbors = k.value
+
+    def graph(self):
+        """The resident graph: (indices one-based, distances), n x neighbors."""
+        idx = np.zeros((self.n, self.neighbors), np.int32)
+        dist = np.zeros((self.n, self.neighbors), np.float32)
+        N.check(N.load().kgb_graph_materialize(self._h, _ptr(idx), _ptr(dist)))
+        return idx, dist
+
+    def matrix(self, **kw) -> "MatrixResult":
+        """KODAMA_matrix on the resident data and graph (same keywords as
+        KODAMA_matrix, without the data and graph arguments)."""
+        if self._h is None:
+            raise ValueError("the graph handle is closed")
+        return KODAMA_matrix(None, _handle=self, **kw)
+
+    def close(self):
+        if self._h is not None:
+            N.load().kgb_graph_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitting=0,
                   graph_neighbors=100, folds=5, knn_k=30, seed=1234, materialize_graph=False,
                   apply_dissimilarity=True, index_base=-1, device=0, host_threads=0,
                   policy="full", res_out=None, first_run=1, classifier="knn",
                   components=50, proposal_weights=None, snapshot_cycle=None,
                   proposal_greedy=False, starting_labels=None, constrain=None,
-                  fixed=None) -> MatrixResult:
+                  fixed=None, _handle=None) -> MatrixResult:
     """KODAMA.matrix on the GPU with the kNN (``classifier="knn"``) or PLS-LDA
     (``classifier="pls"``, ``components`` latent components) classifier.
     ``proposal_weights`` (the 4801 parameters of ``train_proposal``) selects
@@ -147,7 +198,9 @@ def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitt
     Defaults are those of KODAMAMatrixOptions (kodama.hpp:535-570).
     """
     x_dev = None
-    if hasattr(x, "is_cuda") and x.is_cuda:
+    if _handle is not None:
+        n, d = _handle.n, _handle.d
+    elif hasattr(x, "is_cuda") and x.is_cuda:
         if graph is not None:
             raise ValueError("device-resident input is supported for raw data only")
         x_dev = x
@@ -220,7 +273,9 @@ def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitt
         out.knn_dist = kdist.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
     out.knn_cap = cap
     lib = N.load()
-    if x_dev is not None:
+    if _handle is not None:
+        rc = lib.kgb_kodama_matrix_graph(_handle._h, ctypes.byref(opt), ctypes.byref(out))
+    elif x_dev is not None:
         rc = lib.kgb_kodama_matrix_resident(ctypes.c_void_p(x_dev.data_ptr()), n, d, ctypes.byref(opt),
                                             ctypes.byref(out))
     elif graph is None:

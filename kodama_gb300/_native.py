@@ -21,6 +21,11 @@ EXPORTED = (
     "kgb_kodama_matrix_from_graph_data",
     "kgb_kodama_matrix_resident",
     "kgb_kodama_matrix_batch",
+    "kgb_graph_create",
+    "kgb_graph_info",
+    "kgb_graph_materialize",
+    "kgb_kodama_matrix_graph",
+    "kgb_graph_destroy",
     "kgb_launch_count",
     "kgb_core_knn_graph",
     "kgb_core_knn_graph_batch",
@@ -154,6 +159,12 @@ def load():
                                                ctypes.POINTER(MatrixResult)]
     lib.kgb_kodama_matrix_batch.argtypes = [ctypes.POINTER(MatrixProblem), i32, ctypes.POINTER(BatchOptions),
                                             ctypes.POINTER(BatchReport)]
+    lib.kgb_graph_create.argtypes = [P, i32, i32, i32, i32, ctypes.POINTER(ctypes.c_void_p)]
+    lib.kgb_graph_info.argtypes = [P, P, P, P]
+    lib.kgb_graph_materialize.argtypes = [P, P, P]
+    lib.kgb_kodama_matrix_graph.argtypes = [P, ctypes.POINTER(MatrixOptions), ctypes.POINTER(MatrixResult)]
+    lib.kgb_graph_destroy.argtypes = [P]
+    lib.kgb_graph_destroy.restype = None
     lib.kgb_launch_count.restype = ctypes.c_int64
     lib.kgb_launch_count.argtypes = []
     lib.kgb_kodama_matrix_from_graph_data.argtypes = [
@@ -178,7 +189,7 @@ def load():
     lib.kgb_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     lib.kgb_version.restype = ctypes.c_char_p
     for name in EXPORTED:
-        if name not in ("kgb_version", "kgb_launch_count"):
+        if name not in ("kgb_version", "kgb_launch_count", "kgb_graph_destroy"):
             getattr(lib, name).restype = ctypes.c_int
     _lib = lib
     return lib

@@ -2222,6 +2222,20 @@ namespace kgb {
 void set_last_error(const char* msg) { g_error = msg; }
 }  // namespace kgb
 
+// Resident data and exact kNN graph of KODAMAGraph (see kgb_graph_create).
+struct kgb_graph_handle {
+  std::mutex mu;
+  int device = 0, n = 0, d = 0, K = 0;
+  float* d_x = nullptr;
+  int* d_idx = nullptr;
+  float* d_dist = nullptr;
+  ~kgb_graph_handle() {
+    if (d_x) cudaFree(d_x);
+    if (d_idx) cudaFree(d_idx);
+    if (d_dist) cudaFree(d_dist);
+  }
+};
+
 extern "C" {
 
 int kgb_last_error(char* buf, size_t len) {
@@ -2256,6 +2270,109 @@ int kgb_kodama_matrix_resident(const float* x_device, int32_t n, int32_t d, cons
 int kgb_kodama_matrix_batch(const kgb_matrix_problem* problems, int32_t count, const kgb_batch_options* options,
                             kgb_batch_report* report) {
   return guarded([&]() { batch_entry(problems, count, options, report); });
+}
+
+int kgb_graph_create(const float* x, int32_t n, int32_t d, int32_t neighbors, int32_t device,
+                     kgb_graph_handle** out) {
+  return guarded([&]() {
+    if (x == nullptr || out == nullptr) fail(KGB_EINVAL, "null pointer");
+    *out = nullptr;
+    if (n < 3) fail(KGB_EINVAL, "KODAMAGraph requires at least 3 rows.");
+    if (d < 1) fail(KGB_EINVAL, "Input matrix must have at least one column.");
+    if (neighbors < 1) fail(KGB_EINVAL, "KODAMAGraphOptions::neighbors must be positive.");
+    auto g = std::make_unique<kgb_graph_handle>();
+    g->device = device;
+    g->n = n;
+    g->d = d;
+    g->K = std::min(neighbors, n - 1);
+    Ctx ctx(device);
+    ck(cudaMalloc(&g->d_x, sizeof(float) * static_cast<size_t>(n) * d), "cudaMalloc");
+    ck(cudaMalloc(&g->d_idx, sizeof(int) * static_cast<size_t>(n) * g->K), "cudaMalloc");
+    ck(cudaMalloc(&g->d_dist, sizeof(float) * static_cast<size_t>(n) * g->K), "cudaMalloc");
+    ctx.h2d(g->d_x, x, static_cast<size_t>(n) * d);
+    exact_graph(ctx, g->d_x, n, d, g->K, KGB_KNN_AUTO, g->d_idx, g->d_dist, nullptr);
+    ctx.sync();
+    *out = g.release();
+  });
+}
+
+int kgb_graph_info(const kgb_graph_handle* g, int32_t* n, int32_t* d, int32_t* neighbors) {
+  return guarded([&]() {
+    if (g == nullptr) fail(KGB_EINVAL, "null handle");
+    if (n) *n = g->n;
+    if (d) *d = g->d;
+    if (neighbors) *neighbors = g->K;
+  });
+}
+
+int kgb_graph_materialize(kgb_graph_handle* g, int32_t* idx, float* dist) {
+  return guarded([&]() {
+    if (g == nullptr || idx == nullptr || dist == nullptr) fail(KGB_EINVAL, "null pointer");
+    std::lock_guard<std::mutex> lock(g->mu);
+    Ctx ctx(g->device);
+    const size_t total = static_cast<size_t>(g->n) * g->K;
+    ctx.download(idx, g->d_idx, total);
+    ctx.download(dist, g->d_dist, total);
+    ctx.sync();
+    for (size_t i = 0; i < total; ++i)
+      if (idx[i] >= 0) idx[i] += 1;  // one-based, as NeighborGraph leaves KODAMAGraph
+  });
+}
+
+int kgb_kodama_matrix_graph(kgb_graph_handle* g, const kgb_matrix_options* opt, kgb_matrix_result* out) {
+  return guarded([&]() {
+    if (g == nullptr || out == nullptr) fail(KGB_EINVAL, "null pointer");
+    validate_matrix_options(opt);
+    if (out->res == nullptr || out->acc == nullptr || out->v == nullptr) fail(KGB_EINVAL, "null result buffer");
+    std::lock_guard<std::mutex> lock(g->mu);
+    Clock total, clk;
+    for (double& t : out->timings) t = 0.0;
+    for (double& t : out->kernel_ms) t = 0.0;
+    const int n = g->n, d = g->d;
+    kgb_matrix_options o = *opt;
+    o.device = g->device;
+    Ctx ctx(g->device);
+    const MatrixSizes sz = matrix_sizes(n, &o);
+    const int K = std::max(1, std::min(g->K, sz.neighbors));
+    const int M = o.runs, F = o.folds, nthreads = host_threads(o.host_threads);
+    const int first_run = o.first_run > 0 ? o.first_run : 1;
+    const uint64_t seed = o.seed;
+    const int landmarks = sz.landmarks;
+    std::future<std::vector<kgb::FoldPlan>> folds_future = std::async(std::launch::async, [=]() {
+      std::vector<kgb::FoldPlan> plans(static_cast<size_t>(M));
+      parallel_for(M, nthreads, [&](int r) { plans[r] = kgb::plan_folds(landmarks, F, seed, first_run + r); });
+      return plans;
+    });
+    const int ev_start = ctx.mark();
+    int* d_gidx = g->d_idx;
+    float* d_gdist = g->d_dist;
+    if (K < g->K) {
+      // the first K columns, as normalize_external_graph trims a wider graph
+      int* d_mm = ctx.alloc<int>(2);
+      ck_launch(kgb::graph_minmax(g->d_idx, static_cast<size_t>(n) * g->K, d_mm, ctx.stream()), "graph min/max");
+      d_gidx = ctx.alloc<int>(static_cast<size_t>(n) * K);
+      d_gdist = ctx.alloc<float>(static_cast<size_t>(n) * K);
+      ck_launch(kgb::normalize_external(g->d_idx, g->d_dist, n, g->K, K, 0, d_mm, d_gidx, d_gdist, ctx.stream()),
+                "graph normalisation");
+    }
+    const int ev_graph = ctx.mark();
+    out->timings[1] = clk.lap();
+    MatrixTail tail;
+    matrix_from_device_graph(ctx, g->d_x, n, d, d_gidx, d_gdist, K, &o, out, clk, ev_start, ev_graph, folds_future,
+                             tail);
+    ctx.sync();
+    matrix_finalize(&ctx, tail, out, clk);
+    out->timings[0] = total.lap();
+  });
+}
+
+void kgb_graph_destroy(kgb_graph_handle* g) {
+  if (g == nullptr) return;
+  {
+    std::lock_guard<std::mutex> lock(g->mu);
+    cudaSetDevice(g->device);
+  }
+  delete g;
 }
 
 int64_t kgb_launch_count(void) { return kgb::g_launches_value(); }
