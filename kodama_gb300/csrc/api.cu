@@ -1079,6 +1079,8 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     ctx.fork_after(ev_atlas);
     ck_launch(kgb::plan_landmarks(pa, ctx.side()), "landmark planning");
     ctx.join();
+    // the serial landmark hashes stay on the side stream, beside the k-means
+    ck_launch(kgb::plan_land_hash(pa, ctx.side()), "landmark hashes");
   }
   out->timings[5] = 0.0;
   std::vector<int> land;  // host copy, semi-supervised inputs only
@@ -1485,7 +1487,7 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   }
   tail.ev_dis = ctx.mark();
   tail.land_hash.assign(static_cast<size_t>(M), 0);
-  ctx.download(tail.land_hash.data(), d_land_hash, tail.land_hash.size());
+  ctx.download_side(tail.land_hash.data(), d_land_hash, tail.land_hash.size());
   ctx.download(&tail.plan_status, d_plan_status, 1);
   tail.fold_hash.resize(static_cast<size_t>(M));
   for (int r = 0; r < M; ++r) tail.fold_hash[r] = fold_plans[r].fold_hash;

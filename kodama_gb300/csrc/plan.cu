@@ -540,6 +540,10 @@ int plan_landmarks(const PlanArgs& a, cudaStream_t st) {
   count_launch();
   plan_runs_kernel<<<a.runs, kPlanThreads, 0, st>>>(a, s);
   count_launch();
+  return static_cast<int>(cudaGetLastError());
+}
+
+int plan_land_hash(const PlanArgs& a, cudaStream_t st) {
   land_hash_kernel<<<(a.runs + 127) / 128, 128, 0, st>>>(a.land, a.runs, a.target, a.land_hash);
   count_launch();
   return static_cast<int>(cudaGetLastError());

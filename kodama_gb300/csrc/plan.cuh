@@ -27,13 +27,17 @@ struct PlanArgs {
   int* land = nullptr;         // runs x target, ascending rows
   int* nonland = nullptr;      // runs x (n - target), ascending rows (may be null)
   int* init_rows = nullptr;    // runs x init_k, indices into the run's landmarks
-  uint64_t* land_hash = nullptr;  // runs (FNV-1a of the landmark rows)
+  uint64_t* land_hash = nullptr;  // runs (FNV-1a of the landmark rows, plan_land_hash)
   int* status = nullptr;       // 0 = ok; set non-zero on an invalid atlas or quota
   // scratch (plan_scratch_bytes)
   void* scratch = nullptr;
 };
 
 size_t plan_scratch_bytes(int n, int strata, int target, int runs);
+// Landmarks and initial centroid rows of every run.
 int plan_landmarks(const PlanArgs& a, cudaStream_t st);
+// FNV-1a of each run's landmark rows (hash_integer_vector); serial per run, so
+// it is queued off the critical path after plan_landmarks.
+int plan_land_hash(const PlanArgs& a, cudaStream_t st);
 
 }  // namespace kgb
