@@ -277,12 +277,15 @@ __device__ __forceinline__ int tc_row_words(int dp) {
   return (half % 16 == 8) ? half : half + 8;
 }
 
-size_t assign_tc_smem(int k, int d, int dp) {
+// cent: the fp32 centroids staged too (else the exact recheck reads them from L2).
+size_t assign_tc_smem(int k, int d, int dp, bool cent) {
   const int kpad = (k + 7) / 8 * 8, d4 = (d + 3) & ~3;
   const int half = dp / 2, rw = (half % 16 == 8) ? half : half + 8;
-  return sizeof(uint32_t) * 2 * kpad * rw + sizeof(float) * (static_cast<size_t>(k) * d4 + kpad + 1) +
+  return sizeof(uint32_t) * 2 * kpad * rw + sizeof(float) * ((cent ? static_cast<size_t>(k) * d4 : 0) + kpad + 1) +
          sizeof(float) * kTcAssignWarps * 16 * (kpad + 1);
 }
+
+constexpr size_t kTcSmemLimit = 227 * 1024;
 
 // KS: k-steps of 16 coordinates held in registers (dp <= 16 KS).
 template <int KS>
@@ -295,8 +298,8 @@ __global__ void __launch_bounds__(32 * kTcAssignWarps) assign_tc_kernel(KMeansBa
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
   uint32_t* sch = reinterpret_cast<uint32_t*>(smraw);  // [kpad][rw]
   uint32_t* scl = sch + kpad * rw;
-  float* scf = reinterpret_cast<float*>(scl + kpad * rw);  // [k][d4]
-  float* scn = scf + static_cast<size_t>(k) * d4;          // [kpad] + max
+  float* scf = reinterpret_cast<float*>(scl + kpad * rw);  // [k][d4] when staged
+  float* scn = scf + (B.tc_cent_smem ? static_cast<size_t>(k) * d4 : 0);  // [kpad] + max
   float* sa = scn + kpad + 1 + warp * 16 * (kpad + 1);     // this warp's [16][kpad + 1]
   const uint16_t* gch = B.ch + static_cast<size_t>(p) * k * dp;
   const uint16_t* gcl = B.cl + static_cast<size_t>(p) * k * dp;
@@ -309,7 +312,7 @@ __global__ void __launch_bounds__(32 * kTcAssignWarps) assign_tc_kernel(KMeansBa
       sch[c * rw + w] = c < k ? h32[w] : 0u;
       scl[c * rw + w] = c < k ? l32[w] : 0u;
     }
-    if (c < k)
+    if (c < k && B.tc_cent_smem)
       for (int j = lane; j < d4; j += 32) scf[c * d4 + j] = j < d ? cent[static_cast<size_t>(c) * d + j] : 0.0f;
   }
   for (int c = threadIdx.x; c < kpad; c += blockDim.x)
@@ -406,7 +409,8 @@ __global__ void __launch_bounds__(32 * kTcAssignWarps) assign_tc_kernel(KMeansBa
         const bool have = cpos < k;
         if (!__any_sync(kFull, have)) break;
         const int c = have ? cpos : 0;
-        const float dt = dot_x86_reg<KS>(xv, scf + static_cast<size_t>(c) * d4, d);
+        const float* cc = B.tc_cent_smem ? scf + static_cast<size_t>(c) * d4 : cent + static_cast<size_t>(c) * d;
+        const float dt = dot_x86_reg<KS>(xv, cc, d);
         if (have) {
           const float dist = __fsub_rn(fadd(pn, scn[c]), fmul(2.0f, dt));
           if (dist < bestd || (dist == bestd && c < best)) {
@@ -693,7 +697,12 @@ __global__ void finalize_kernel(KMeansBatch B) {
 
 }  // namespace
 
-bool kmeans_tc_supported(int d, int k) { return d >= 1 && d <= 128 && k >= 1 && k <= 128; }
+// Above 128 centroids the per-warp distance tiles hold the kernel to one
+// 4-warp CTA per SM and the exact assignment is faster.
+bool kmeans_tc_supported(int d, int k) {
+  if (d < 1 || d > 128 || k < 1 || k > 128) return false;
+  return assign_tc_smem(k, d, (d + 15) / 16 * 16, false) <= kTcSmemLimit;
+}
 
 size_t kmeans_sort_smem(int k) { return sizeof(int) * (33 * static_cast<size_t>(k) + 1); }
 
@@ -712,7 +721,8 @@ int kmeans_run(const KMeansBatch& B, cudaStream_t st) {
   const dim3 ngrid((B.k + 127) / 128, B.problems);
   const size_t sum_bytes = sums_smem(B.d);
   const bool tc = B.xh != nullptr && kmeans_tc_supported(B.d, B.k);
-  const size_t tc_bytes = tc ? assign_tc_smem(B.k, B.d, B.dp) : 0;
+  const bool cent_smem = tc && assign_tc_smem(B.k, B.d, B.dp, true) <= kTcSmemLimit;
+  const size_t tc_bytes = tc ? assign_tc_smem(B.k, B.d, B.dp, cent_smem) : 0;
   const bool tc_wide = B.dp > 64;
   if (tc) {
     cudaFuncSetAttribute(assign_tc_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(tc_bytes));
@@ -721,6 +731,7 @@ int kmeans_run(const KMeansBatch& B, cudaStream_t st) {
   // 64-row blocks per CTA: the centroids are staged once per CTA, but the grid
   // keeps at least two CTAs per SM
   KMeansBatch T = B;
+  T.tc_cent_smem = cent_smem ? 1 : 0;
   {
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);

@@ -37,6 +37,7 @@ struct KMeansBatch {
   uint16_t* cl;
   int tc_blocks;            // set by kmeans_run: 64-row blocks per CTA
   float tc_crel;            // set by kmeans_run: the error bound's factor
+  int tc_cent_smem;         // set by kmeans_run: fp32 centroids staged in shared memory (else read from L2)
 };
 
 // The tensor-core assignment applies (d <= 64, k <= 128).

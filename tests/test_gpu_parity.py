@@ -91,6 +91,17 @@ def test_matrix_raw_high_dim(kg, orc, d):
     _assert_matrix_equal(gpu, ref)
 
 
+@pytest.mark.parametrize("d,splitting", [(50, 300), (100, 200), (20, 320)])
+def test_matrix_raw_many_clusters(kg, orc, d, splitting):
+    # more than 128 centroids: the exact assignment; the atlas and the landmark k-means differ in k
+    x, _ = datasets.gaussian_mixture(n=4000, d=d, clusters=25, mean_scale=3.0, seed=d + splitting)
+    kw = _matrix_kw(runs=3, cycles=6, graph_neighbors=30, knn_k=10, splitting=splitting)
+    gpu = kg.KODAMA_matrix(x, materialize_graph=True, **kw)
+    gi, gd = orc.exact_knn(x, 30, threads=8)
+    ref = _oracle_matrix(orc, x, gi, gd, 0, kw)
+    _assert_matrix_equal(gpu, ref)
+
+
 @pytest.mark.parametrize("mode", [
     dict(evolutionary_search=False, guarded_diversity=False, many_to_one_absorption=False, stratified=True),
     dict(evolutionary_search=True, guarded_diversity=True, many_to_one_absorption=True, stratified=False),
