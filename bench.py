@@ -58,12 +58,30 @@ BATCH_KW = dict(runs=50, cycles=50, knn_k=10, components=5, graph_neighbors=30, 
 EVOLVE_TRAFFIC_BYTES = 457883648
 
 
+CONFIG_DESC = ("KODAMA.matrix kNN N=20000 d=50 (12-cluster Gaussian mixture), M=100 runs, "
+               "Tcycle=100, exact graph K=30, knn.k=30, folds=10, splitting=50, landmarks=10000")
+DATA_DESC = "synthetic gaussian_mixture(seed=2)"
+
+
+def _use_config5():
+    """--workload learned100k: the learned-vs-plain comparison at N=100000,
+    d=50 (PCA-like mixture of 30 clusters, sigma_i = 10 / i along random
+    orthonormal axes, Dirichlet(0.5) sizes, seed 5), K=30, M=100, Tcycle=100,
+    kNN classifier, default splitting (300 above N=40000)."""
+    global METRIC, WORKLOAD, CONFIG_DESC, DATA_DESC
+    METRIC = "KODAMA.matrix wall-s at N=100k,d=50,M=100: learned vs plain GPU at equal CV acc"
+    WORKLOAD = dict(n=100000, d=50, runs=100, cycles=100, graph_neighbors=30, knn_k=30, folds=10,
+                    splitting=0, landmarks=10000, seed=1234)
+    CONFIG_DESC = ("KODAMA.matrix kNN N=100000 d=50 (30-cluster PCA-like mixture), M=100 runs, Tcycle=100, "
+                   "exact graph K=30, knn.k=30, folds=10, default splitting (300), landmarks=10000")
+    DATA_DESC = "synthetic pca_mixture(seed=5)"
+
+
 def _config(extra=None):
-    c = {"workload": "KODAMA.matrix kNN N=20000 d=50 (12-cluster Gaussian mixture), M=100 runs, "
-                     "Tcycle=100, exact graph K=30, knn.k=30, folds=10, splitting=50, landmarks=10000",
+    c = {"workload": CONFIG_DESC,
          "global_batch": WORKLOAD["runs"], "seq_len": WORKLOAD["cycles"],
          "parallelism": "replicas", "l2": "flushed between steps (512 MB write)",
-         "data": "synthetic gaussian_mixture(seed=2)"}
+         "data": DATA_DESC}
     if extra:
         c.update(extra)
     return c
@@ -71,7 +89,10 @@ def _config(extra=None):
 
 def _data():
     from kodama_gb300 import datasets
-    x, _ = datasets.gaussian_mixture(n=WORKLOAD["n"], d=WORKLOAD["d"], seed=2)
+    if WORKLOAD["n"] == 100000:
+        x, _ = datasets.pca_mixture(n=WORKLOAD["n"], d=WORKLOAD["d"], seed=5)
+    else:
+        x, _ = datasets.gaussian_mixture(n=WORKLOAD["n"], d=WORKLOAD["d"], seed=2)
     return np.ascontiguousarray(x, np.float32)
 
 
@@ -159,9 +180,21 @@ def cpu_baseline(x, threads=None):
     if not oracle.available():
         oracle.build()
     threads = threads or os.cpu_count() or 1
-    t0 = time.perf_counter()
-    gi, gd = oracle.exact_knn(x, WORKLOAD["graph_neighbors"], threads=threads)
-    t_graph = time.perf_counter() - t0
+    n = x.shape[0]
+    graph_note = f"exact graph (N={n})"
+    if n > 30000:
+        # the exact graph of a 20000-row sample, scaled by (n / 20000)^2; the
+        # runs take the same exact graph from the device search
+        import kodama_gb300 as kg
+        t0 = time.perf_counter()
+        oracle.exact_knn(np.ascontiguousarray(x[:20000]), WORKLOAD["graph_neighbors"], threads=threads)
+        t_graph = (time.perf_counter() - t0) * (n / 20000.0) ** 2
+        gi, gd = kg.knn_graph(x, WORKLOAD["graph_neighbors"])
+        graph_note = f"exact graph of 20000 rows scaled x{(n / 20000.0) ** 2:g}"
+    else:
+        t0 = time.perf_counter()
+        gi, gd = oracle.exact_knn(x, WORKLOAD["graph_neighbors"], threads=threads)
+        t_graph = time.perf_counter() - t0
     kw = _matrix_kw()
     kw["runs"] = CPU_SAMPLE_RUNS
     t1 = time.perf_counter()
@@ -170,7 +203,7 @@ def cpu_baseline(x, threads=None):
     t_atlas, t_runs = float(r.timings[4]), float(r.timings[2])
     total = t_graph + t_atlas + t_runs * (WORKLOAD["runs"] / CPU_SAMPLE_RUNS) + max(0.0, t_matrix - t_atlas - t_runs)
     return {"value": round(total, 4), "unit": "s", "cores": threads, "kind": "port",
-            "sample": f"exact graph (N=20000) + atlas + {CPU_SAMPLE_RUNS} of 100 runs timed "
+            "sample": f"{graph_note} + atlas + {CPU_SAMPLE_RUNS} of 100 runs timed "
                       f"({t_graph + t_matrix:.2f} s), runs scaled x{WORKLOAD['runs'] / CPU_SAMPLE_RUNS:g}",
             "stages_s": {"graph": round(t_graph, 3), "atlas": round(t_atlas, 3),
                          "runs_sample": round(t_runs, 3)}}
@@ -609,7 +642,7 @@ def run_gpu(args):
                 "kernel": "evolve_kernel (persistent, one CTA per run)",
                 "algorithmic_bytes_per_launch": bytes_launch,
                 "launch_ms": round(evo_s * 1000, 3),
-                "traffic": EVOLVE_TRAFFIC_BYTES}
+                "traffic": EVOLVE_TRAFFIC_BYTES if WORKLOAD["n"] == 20000 else None}
     h2d = x.nbytes
     d2h = runs * n * 4 + runs * 8 + runs * cycles * 8 + runs * 3 * 8 + runs * 8 * 4 + runs * cycles * 5 * 4
     line = {"metric": METRIC, "value": round(value, 5), "unit": "s", "n_gpus": world, "steps": args.steps,
@@ -642,10 +675,12 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-proposal comparison")
-    ap.add_argument("--workload", default="knn", choices=["knn", "pls", "batch"],
+    ap.add_argument("--workload", default="knn", choices=["knn", "pls", "batch", "learned100k"],
                     help="knn: the headline configuration; pls: the PLS-LDA configuration; batch: 256 uneven "
-                         "problems in one captured CUDA graph")
+                         "problems in one captured CUDA graph; learned100k: learned vs plain at N=100000")
     args = ap.parse_args()
+    if args.workload == "learned100k":
+        _use_config5()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "pls":
