@@ -304,6 +304,14 @@ int kgb_plsldacv(const float* x, int32_t n, int32_t p, const int32_t* labels, co
                  const kgb_pls_options* opt, int32_t* predicted, int32_t* fold_assignments,
                  int32_t* selected_components, double* accuracy_by_components);
 
+/* Replaces PLSDACV_CUDA (kodama.hpp:913; CPU semantics of run_plscv_host in
+ * PLSMode::PLS_DA, plscv.cpp:2428-2443): the same folds and SIMPLS fits as
+ * kgb_plsldacv, with the class chosen by the one-hot least-squares
+ * regression on the scores instead of LDA. */
+int kgb_plsdacv(const float* x, int32_t n, int32_t p, const int32_t* labels, const int32_t* constrain,
+                const kgb_pls_options* opt, int32_t* predicted, int32_t* fold_assignments,
+                int32_t* selected_components, double* accuracy_by_components);
+
 /* Replaces PLSLDAPredict_CUDA (kodama.hpp:941; CPU semantics
  * plscv.cpp:2976-3005): fit PLS-LDA on train (n x p, labels) and predict
  * test (nt x p). */

@@ -25,7 +25,7 @@ import numpy as np
 
 from . import _native as N
 
-__all__ = ["KODAMAGraph", "KODAMA_matrix_batch", "train_proposal", "proposal_gradient", "proposal_predict", "KODAMA_matrix", "CoreKNNGraph", "CoreKNNGraph_batch", "knn_graph",
+__all__ = ["PLSDACV", "KODAMAGraph", "KODAMA_matrix_batch", "train_proposal", "proposal_gradient", "proposal_predict", "KODAMA_matrix", "CoreKNNGraph", "CoreKNNGraph_batch", "knn_graph",
            "KODAMADissimilarityInPlace", "PLSLDACV", "PLSLDAPredict", "CorePLSLDA", "PLSCVResult", "MatrixResult", "CoreResult", "EvolutionPolicy",
            "library_path", "version", "launch_count"]
 
@@ -663,6 +663,23 @@ def PLSLDACV(x, labels, *, constrain=None, folds=10, stratified=True, max_compon
     opt = _pls_options(folds, stratified, max_components, fixed_components, center, scale, cv_seed, device)
     N.check(N.load().kgb_plsldacv(_ptr(xa), n, p, _ptr(lab), _ptr(con), ctypes.byref(opt), _ptr(pred),
                                   _ptr(fo), ctypes.byref(sel), _ptr(abc)))
+    return PLSCVResult(pred, fo, int(sel.value), abc, float(np.mean(pred == lab)))
+
+
+def PLSDACV(x, labels, *, constrain=None, folds=10, stratified=True, max_components=10,
+            fixed_components=0, center=True, scale=True, cv_seed=1, device=0) -> PLSCVResult:
+    """PLSDACV: cross-validated PLS-DA predictions (plscv.cpp:2897, PLSMode::PLS_DA)."""
+    xa = np.ascontiguousarray(x, dtype=np.float32)
+    n, p = xa.shape
+    lab = np.ascontiguousarray(labels, dtype=np.int32)
+    con = None if constrain is None else np.ascontiguousarray(constrain, dtype=np.int32)
+    pred = np.zeros(n, np.int32)
+    fo = np.zeros(n, np.int32)
+    sel = ctypes.c_int32(0)
+    abc = np.zeros(max(1, max_components), np.float64)
+    opt = _pls_options(folds, stratified, max_components, fixed_components, center, scale, cv_seed, device)
+    N.check(N.load().kgb_plsdacv(_ptr(xa), n, p, _ptr(lab), _ptr(con), ctypes.byref(opt), _ptr(pred),
+                                 _ptr(fo), ctypes.byref(sel), _ptr(abc)))
     return PLSCVResult(pred, fo, int(sel.value), abc, float(np.mean(pred == lab)))
 
 

@@ -33,6 +33,7 @@ EXPORTED = (
     "kgb_knn_graph_ex",
     "kgb_core_knn",
     "kgb_plsldacv",
+    "kgb_plsdacv",
     "kgb_plslda_predict",
     "kgb_core_plslda",
     "kgb_proposal_train",
@@ -182,6 +183,7 @@ def load():
     lib.kgb_proposal_gradient.argtypes = [P, P, P, i32, i32, P, P]
     lib.kgb_proposal_predict.argtypes = [P, P, i32, i32, P]
     lib.kgb_plsldacv.argtypes = [P, i32, i32, P, P, ctypes.POINTER(PlsOptions), P, P, P, P]
+    lib.kgb_plsdacv.argtypes = [P, i32, i32, P, P, ctypes.POINTER(PlsOptions), P, P, P, P]
     lib.kgb_plslda_predict.argtypes = [P, i32, i32, P, P, i32, ctypes.POINTER(PlsOptions), P]
     lib.kgb_core_plslda.argtypes = [P, i32, i32, P, P, P, ctypes.POINTER(CoreOptions),
                                     ctypes.POINTER(PlsOptions), ctypes.POINTER(CoreResult)]

@@ -2466,14 +2466,36 @@ void check_pls_options(const kgb_pls_options* o) {
   if (o->fixed_components > o->max_components)
     fail(KGB_EINVAL, "PLSOptions::fixed_components cannot exceed max_components.");
 }
+
+int plscv_entry(const float* x, int32_t n, int32_t p, const int32_t* labels, const int32_t* constrain,
+                const kgb_pls_options* opt, int32_t* predicted, int32_t* fold_assignments,
+                int32_t* selected_components, double* accuracy_by_components, bool da);
 }  // namespace
 
 int kgb_plsldacv(const float* x, int32_t n, int32_t p, const int32_t* labels, const int32_t* constrain,
                  const kgb_pls_options* opt, int32_t* predicted, int32_t* fold_assignments,
                  int32_t* selected_components, double* accuracy_by_components) {
+  return plscv_entry(x, n, p, labels, constrain, opt, predicted, fold_assignments, selected_components,
+                     accuracy_by_components, false);
+}
+
+int kgb_plsdacv(const float* x, int32_t n, int32_t p, const int32_t* labels, const int32_t* constrain,
+                const kgb_pls_options* opt, int32_t* predicted, int32_t* fold_assignments,
+                int32_t* selected_components, double* accuracy_by_components) {
+  return plscv_entry(x, n, p, labels, constrain, opt, predicted, fold_assignments, selected_components,
+                     accuracy_by_components, true);
+}
+
+}  // extern "C"
+
+namespace {
+// run_plscv_host (plscv.cpp:2293-2507) for PLSLDACV (da = false) and PLSDACV.
+int plscv_entry(const float* x, int32_t n, int32_t p, const int32_t* labels, const int32_t* constrain,
+                const kgb_pls_options* opt, int32_t* predicted, int32_t* fold_assignments,
+                int32_t* selected_components, double* accuracy_by_components, bool da) {
   return guarded([&]() {
     if (x == nullptr || labels == nullptr || opt == nullptr || predicted == nullptr) fail(KGB_EINVAL, "null pointer");
-    if (n < 1 || p < 1) fail(KGB_EINVAL, "PLSLDACV requires a non-empty matrix.");
+    if (n < 1 || p < 1) fail(KGB_EINVAL, da ? "PLSDACV requires a non-empty matrix." : "PLSLDACV requires a non-empty matrix.");
     if (n > 65535) fail(KGB_EINVAL, "at most 65535 rows are supported");
     check_pls_options(opt);
     const std::vector<int> lab(labels, labels + n);
@@ -2493,7 +2515,8 @@ int kgb_plsldacv(const float* x, int32_t n, int32_t p, const int32_t* labels, co
     b.ev.labels = ctx.upload(cd.codes.data(), cd.codes.size());
     b.ev.class_off = ctx.upload(off.data(), off.size());
     b.ev.class_rows = ctx.upload(rows.data(), rows.size());
-    ck_launch(kgb::pls_evaluate(b.ev, ctx.stream()), "PLS-LDA evaluation");
+    b.ev.da_mode = da ? 1 : 0;
+    ck_launch(kgb::pls_evaluate(b.ev, ctx.stream()), da ? "PLS-DA evaluation" : "PLS-LDA evaluation");
     std::vector<uint16_t> pc(static_cast<size_t>(n));
     std::vector<int> comp(static_cast<size_t>(b.S));
     ctx.download(pc.data(), b.ev.pred, pc.size());
@@ -2516,6 +2539,10 @@ int kgb_plsldacv(const float* x, int32_t n, int32_t p, const int32_t* labels, co
     }
   });
 }
+
+}  // namespace
+
+extern "C" {
 
 int kgb_plslda_predict(const float* train, int32_t n, int32_t p, const int32_t* labels, const float* test,
                        int32_t nt, const kgb_pls_options* opt, int32_t* predicted) {

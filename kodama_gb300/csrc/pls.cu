@@ -296,6 +296,54 @@ __device__ bool warp_exact_dot(int n, Term term, int lane, float& out) {
   return round_check(acc, LSB, A, n, out);
 }
 
+// Sequential double sum of n floats, S_seq (acc = 0.0; acc += double(x_k)
+// in order).  All terms are multiples of 2^emin (the smallest ulp); when the
+// sum of |x| stays below 2^(emin + 53), every partial sum is exact in double,
+// so S_seq is the exact fixed-point sum.  Otherwise lane 0 runs the chain.
+template <class Term>
+__device__ double warp_seq_sum_double(int n, Term term, int lane) {
+  int emin = 1 << 20, emax = -(1 << 20), bad = 0;
+  float A = 0.0f;
+  for (int k = lane; k < n; k += 32) {
+    const float x = term(k);
+    const unsigned ux = __float_as_uint(x);
+    const int be = static_cast<int>((ux >> 23) & 0xffu);
+    bad |= be == 0xff;
+    if ((ux << 1) != 0u) {
+      const int ue = be ? be - 150 : -149;
+      emin = min(emin, ue);
+      emax = max(emax, ue);
+      A = __fadd_ru(A, fabsf(x));
+    }
+  }
+  bad = __reduce_or_sync(kFull, bad);
+  emin = __reduce_min_sync(kFull, emin);
+  emax = __reduce_max_sync(kFull, emax);
+  A = warp_sum_ru(A);
+  bool exact = !bad;
+  if (exact && emin == (1 << 20)) return 0.0;  // every term is zero
+  if (exact) exact = emax - emin + 24 + clog2i(n) <= 62 && A < ldexpf(1.0f, min(emin + 53, 127));
+  if (exact) {
+    long long acc = 0;
+    for (int k = lane; k < n; k += 32) {
+      const float x = term(k);
+      const unsigned ux = __float_as_uint(x);
+      if ((ux << 1) == 0u) continue;
+      const int be = static_cast<int>((ux >> 23) & 0xffu);
+      const long long mant = static_cast<long long>((ux & 0x7fffffu) | (be ? 0x800000u : 0u));
+      const long long v = mant << ((be ? be - 150 : -149) - emin);
+      acc += (ux >> 31) ? -v : v;
+    }
+    acc = warp_sum_i64(acc);
+    // |acc| < 2^53: exact in double; 2^emin is a normal double (emin >= -149)
+    return __dmul_rn(__ll2double_rn(acc), __longlong_as_double(static_cast<long long>(emin + 1023) << 52));
+  }
+  double out = 0.0;
+  if (lane == 0)
+    for (int k = 0; k < n; ++k) out = __dadd_rn(out, static_cast<double>(term(k)));
+  return __shfl_sync(kFull, out, 0);
+}
+
 // dot_float / mat_vec_float / t_mat_vec_float element: float(S_seq).
 template <class Term>
 __device__ float warp_seq_dot(int n, Term term, int lane) {
@@ -462,6 +510,7 @@ __global__ void __launch_bounds__(kEvalThreads, 2) eval_kernel(PlsEvalArgs a) {
   float* sol = reinterpret_cast<float*>(carve(sizeof(float) * NCm * C));
   float* lin = reinterpret_cast<float*>(carve(sizeof(float) * C * NCm));
   float* cst = reinterpret_cast<float*>(carve(sizeof(float) * C));
+  double* ssum = reinterpret_cast<double*>(carve(sizeof(double) * NCm));  // PLS-DA score sums
   // shared region: the cross-product (when it fits) and the score tiles,
   // which overlap it unless a slice of the launch computes scores during the
   // fit (no fold Gram)
@@ -784,6 +833,113 @@ __global__ void __launch_bounds__(kEvalThreads, 2) eval_kernel(PlsEvalArgs a) {
     const float acc = warp_masked_chain<2>(Ts, nc, q, posok, coff[code], coff[code + 1], lane);
     if (lane == 0) cs[k * nc + q] = acc;
   }
+  if (a.da_mode) {
+    // --- PLS-DA (the PLS_DA branch of run_plscv_host, plscv.cpp:2428-2443) ---
+    // class means of the one-hot labels (label_means_float, plscv.cpp:1210)
+    __syncthreads();
+    const float inv_n = nt > 0 ? __fdiv_rn(1.0f, static_cast<float>(nt)) : 0.0f;
+    for (int k = threadIdx.x; k < m; k += kEvalThreads) cst[k] = __fmul_rn(static_cast<float>(cnt[klist[k]]), inv_n);
+    // regression_coefficients_centered_one_hot_float (plscv.cpp:1222-1265):
+    // double score sums and double score cross-products over the training rows
+    for (int q = warp; q < nc; q += kEvalWarps) {
+      const double v = warp_seq_sum_double(nt, [&](int i) { return Tt[static_cast<size_t>(i) * nc + q]; }, lane);
+      if (lane == 0) ssum[q] = v;
+    }
+    for (int it = warp; it < ncp; it += kEvalWarps) {
+      int pr = it, rr = 0;
+      while (pr > rr) {
+        pr -= rr + 1;
+        ++rr;
+      }
+      const int col = pr;
+      const float v = warp_seq_dot(nt, [&](int i, float& x, float& y) {
+        x = Tt[static_cast<size_t>(i) * nc + col];
+        y = Tt[static_cast<size_t>(i) * nc + rr];
+      }, lane);
+      if (lane == 0) {
+        pooled[rr * nc + col] = v;
+        pooled[col * nc + rr] = v;
+      }
+    }
+    __syncthreads();
+    for (int it = threadIdx.x; it < nc * m; it += kEvalThreads) {
+      const int q = it / m, k = it % m;
+      sol[q * m + k] = __fsub_rn(cs[k * nc + q], __double2float_rn(__dmul_rn(ssum[q], static_cast<double>(cst[k]))));
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      // solve_linear_float (plscv.cpp:1346-1377): Gauss-Jordan with partial
+      // pivoting on lhs + 1e-9 I
+      float* A = pooled;
+      for (int i = 0; i < nc; ++i) A[i * nc + i] = __fadd_rn(A[i * nc + i], 1.0e-9f);
+      for (int c = 0; c < nc; ++c) {
+        int piv = c;
+        float best = fabsf(A[c * nc + c]);
+        for (int r2 = c + 1; r2 < nc; ++r2) {
+          const float val = fabsf(A[r2 * nc + c]);
+          if (val > best) {
+            best = val;
+            piv = r2;
+          }
+        }
+        if (best < 1.0e-12f) continue;
+        if (piv != c) {
+          for (int j = 0; j < nc; ++j) {
+            const float t = A[c * nc + j];
+            A[c * nc + j] = A[piv * nc + j];
+            A[piv * nc + j] = t;
+          }
+          for (int j = 0; j < m; ++j) {
+            const float t = sol[c * m + j];
+            sol[c * m + j] = sol[piv * m + j];
+            sol[piv * m + j] = t;
+          }
+        }
+        const float dv = A[c * nc + c];
+        for (int j = c; j < nc; ++j) A[c * nc + j] = __fdiv_rn(A[c * nc + j], dv);
+        for (int j = 0; j < m; ++j) sol[c * m + j] = __fdiv_rn(sol[c * m + j], dv);
+        for (int r2 = 0; r2 < nc; ++r2) {
+          if (r2 == c) continue;
+          const float fct = A[r2 * nc + c];
+          if (fct == 0.0f) continue;
+          for (int j = c; j < nc; ++j) A[r2 * nc + j] = __fsub_rn(A[r2 * nc + j], __fmul_rn(fct, A[c * nc + j]));
+          for (int j = 0; j < m; ++j) sol[r2 * m + j] = __fsub_rn(sol[r2 * m + j], __fmul_rn(fct, sol[c * m + j]));
+        }
+      }
+      a.eval_comp[s] = nc;
+    }
+    __syncthreads();
+    // predict_pls_da_labels_float (plscv.cpp:1267-1292): first maximum of
+    // mean + scores x coefficients
+    float* tile = tiles + warp * kTile;
+    for (int b0 = warp * 32; b0 < nv; b0 += kEvalWarps * 32) {
+      const int v = b0 + lane;
+      const int row = v < nv ? (a.predict_mode ? v : vidx[v]) : -1;
+      float sr[kMaxComp];
+      for (int q0 = 0; q0 < nc; q0 += kMaxNC) {
+        const int nq = min(kMaxNC, nc - q0);
+        float acc[kMaxNC];
+        warp_scores(vbase, p, row, Wsm, ldw, q0, nq, tile, lane, acc);
+#pragma unroll
+        for (int q = 0; q < kMaxNC; ++q)
+          if (q < nq) sr[q0 + q] = acc[q];
+      }
+      if (row >= 0) {
+        int best = 0;
+        float bs = -INFINITY;
+        for (int k = 0; k < m; ++k) {
+          float sc = cst[k];
+          for (int q = 0; q < nc; ++q) sc = __fadd_rn(sc, __fmul_rn(sr[q], sol[q * m + k]));
+          if (sc > bs) {
+            bs = sc;
+            best = k;
+          }
+        }
+        pred[row] = static_cast<uint16_t>(klist[best]);
+      }
+    }
+    return;
+  }
   // score cross-products (all training rows in order): one warp per chain
   for (int it = warp; it < ncp; it += kEvalWarps) {
     int pr = it, rr = 0;
@@ -987,7 +1143,7 @@ size_t pls_eval_smem(int p, int C0max, int requested, int max_components, bool s
   b += 3 * al(sizeof(float) * p) + al(sizeof(float) * C);
   b += 2 * al(sizeof(float) * p * max_components);
   b += al(sizeof(float) * C * N) + 3 * al(sizeof(float) * N * N) + al(sizeof(float) * N * C);
-  b += al(sizeof(float) * C * N) + al(sizeof(float) * C);
+  b += al(sizeof(float) * C * N) + al(sizeof(float) * C) + al(sizeof(double) * N);
   const size_t cross = s_in_smem ? sizeof(float) * static_cast<size_t>(p) * C : 0;
   const size_t tiles = sizeof(float) * static_cast<size_t>(kEvalWarps) * kTile;
   b += tiles_after_s ? cross + tiles : (cross > tiles ? cross : tiles);

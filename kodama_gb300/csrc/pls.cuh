@@ -47,6 +47,7 @@ struct PlsEvalArgs {
   int max_components;    // SIMPLS rank limit
   int requested;         // components evaluated: min(requested, fitted rank)
   int predict_mode;      // 1: rows to predict are Zv rows 0..NV-1
+  int da_mode;           // 1: PLS-DA (one-hot regression on the scores) instead of LDA
   int s_in_smem;         // 1: the label cross-product of a slice lives in shared memory
   int tiles_after_s;     // 1: some slice computes training scores during the fit (no fold Gram)
   const float* Z;        // S x L x p

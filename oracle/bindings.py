@@ -254,14 +254,15 @@ def dissimilarity(L, gidx1: np.ndarray, gdist: np.ndarray, res: np.ndarray, thre
 
 
 def plsldacv(L, x, labels, *, folds=10, stratified=True, max_components=10, fixed_components=0,
-             center=True, scale=True, threads=1, cv_seed=1, constrain=None):
-    """PLSLDACV_CPU: returns (predicted, folds, selected_components, acc_by_comp, seconds)."""
+             center=True, scale=True, threads=1, cv_seed=1, constrain=None, da=False):
+    """PLSLDACV_CPU (PLSDACV_CPU with da=True): returns (predicted, folds,
+    selected_components, acc_by_comp, seconds)."""
     x = np.ascontiguousarray(x, np.float32)
     n, d = x.shape
     lab = np.ascontiguousarray(labels, np.int32)
     con = np.ascontiguousarray(constrain if constrain is not None else np.zeros(n), np.int32)
     popts = np.array([folds, int(stratified), max_components, fixed_components, int(center),
-                      int(scale), threads], np.int32)
+                      int(scale), threads, int(da)], np.int32)
     pred = np.zeros(n, np.int32)
     fo = np.zeros(n, np.int32)
     sel = ctypes.c_int(0)

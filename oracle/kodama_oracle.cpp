@@ -1780,7 +1780,8 @@ int orc_plsldacv(const float* x, int n, int d, const int* labels, const int* con
                  const int* popts, unsigned long long cv_seed, int* predicted, int* folds,
                  int* selected_components, double* accuracy_by_components, double* seconds) {
   try {
-    const orc::PLSOpts o = pls_opts(popts, cv_seed);
+    orc::PLSOpts o = pls_opts(popts, cv_seed);
+    o.da = popts[7] != 0;
     std::vector<int> lab(labels, labels + n);
     std::vector<int> con = has_constrain ? std::vector<int>(constrain, constrain + n) : std::vector<int>();
     const auto t0 = std::chrono::steady_clock::now();

@@ -380,6 +380,102 @@ std::vector<int> encode(const std::vector<int>& y, const std::vector<int>& class
 
 }  // namespace
 
+// solve_linear_float (plscv.cpp:1346-1377): Gauss-Jordan with partial
+// pivoting on a + 1e-9 I (row-major n x n), right-hand sides b (n x m).
+Vec solve_linear(Vec a, int n, Vec b, int m) {
+  for (int i = 0; i < n; ++i) a[static_cast<size_t>(i) * n + i] += 1.0e-9f;
+  for (int col = 0; col < n; ++col) {
+    int pivot = col;
+    float best = std::abs(a[static_cast<size_t>(col) * n + col]);
+    for (int r = col + 1; r < n; ++r) {
+      const float val = std::abs(a[static_cast<size_t>(r) * n + col]);
+      if (val > best) {
+        best = val;
+        pivot = r;
+      }
+    }
+    if (best < 1.0e-12f) continue;
+    if (pivot != col) {
+      for (int j = 0; j < n; ++j) std::swap(a[static_cast<size_t>(col) * n + j], a[static_cast<size_t>(pivot) * n + j]);
+      for (int j = 0; j < m; ++j) std::swap(b[static_cast<size_t>(col) * m + j], b[static_cast<size_t>(pivot) * m + j]);
+    }
+    const float div = a[static_cast<size_t>(col) * n + col];
+    for (int j = col; j < n; ++j) a[static_cast<size_t>(col) * n + j] /= div;
+    for (int j = 0; j < m; ++j) b[static_cast<size_t>(col) * m + j] /= div;
+    for (int r = 0; r < n; ++r) {
+      if (r == col) continue;
+      const float f = a[static_cast<size_t>(r) * n + col];
+      if (f == 0.0f) continue;
+      for (int j = col; j < n; ++j) a[static_cast<size_t>(r) * n + j] -= f * a[static_cast<size_t>(col) * n + j];
+      for (int j = 0; j < m; ++j) b[static_cast<size_t>(r) * m + j] -= f * b[static_cast<size_t>(col) * m + j];
+    }
+  }
+  return b;
+}
+
+// The PLS-DA branch of run_plscv_host (plscv.cpp:2428-2443): scores of the
+// training and validation rows (transform_pls_scores_float :995), class means
+// (label_means_float :1210), one-hot regression coefficients
+// (regression_coefficients_centered_one_hot_float :1222-1265) and the
+// prediction argmax (predict_pls_da_labels_float :1267-1292).
+std::vector<int> da_predict(const Vec& zt, int nt, const std::vector<int>& code, const Vec& zv, int nv, int p,
+                            const Fit& fit, int m, int nc) {
+  auto scores = [&](const Vec& z, int rows) {
+    Vec t(static_cast<size_t>(rows) * nc, 0.0f);
+    for (int i = 0; i < rows; ++i) {
+      float* out = t.data() + static_cast<size_t>(i) * nc;
+      for (int j = 0; j < p; ++j) {
+        const float v = z[static_cast<size_t>(i) * p + j];
+        const float* wr = fit.w.data() + static_cast<size_t>(j) * fit.rank;
+        for (int a = 0; a < nc; ++a) out[a] += v * wr[a];
+      }
+    }
+    return t;
+  };
+  const Vec tt = scores(zt, nt), tv = scores(zv, nv);
+  std::vector<float> ymean(static_cast<size_t>(m), 0.0f);
+  for (int i = 0; i < nt; ++i) ymean[code[i]] += 1.0f;
+  const float inv_n = nt > 0 ? 1.0f / static_cast<float>(nt) : 0.0f;
+  for (float& v : ymean) v *= inv_n;
+  Vec lhs(static_cast<size_t>(nc) * nc), rhs(static_cast<size_t>(nc) * m, 0.0f);
+  std::vector<double> ssum(static_cast<size_t>(nc), 0.0), lacc(static_cast<size_t>(nc) * nc, 0.0);
+  for (int r = 0; r < nt; ++r) {
+    const int c = code[r];
+    const float* tr = tt.data() + static_cast<size_t>(r) * nc;
+    for (int a = 0; a < nc; ++a) {
+      const double value = tr[a];
+      rhs[static_cast<size_t>(a) * m + c] += static_cast<float>(value);
+      ssum[a] += value;
+      for (int b = a; b < nc; ++b) lacc[static_cast<size_t>(a) * nc + b] += value * static_cast<double>(tr[b]);
+    }
+  }
+  for (int a = 0; a < nc; ++a)
+    for (int b = a; b < nc; ++b) {
+      const float v = static_cast<float>(lacc[static_cast<size_t>(a) * nc + b]);
+      lhs[static_cast<size_t>(a) * nc + b] = v;
+      lhs[static_cast<size_t>(b) * nc + a] = v;
+    }
+  for (int a = 0; a < nc; ++a)
+    for (int c = 0; c < m; ++c)
+      rhs[static_cast<size_t>(a) * m + c] -= static_cast<float>(ssum[a] * static_cast<double>(ymean[c]));
+  const Vec coef = solve_linear(lhs, nc, rhs, m);
+  std::vector<int> pred(static_cast<size_t>(nv), 0);
+  for (int i = 0; i < nv; ++i) {
+    int best = 0;
+    float bs = -std::numeric_limits<float>::infinity();
+    for (int c = 0; c < m; ++c) {
+      float sc = ymean[c];
+      for (int a = 0; a < nc; ++a) sc += tv[static_cast<size_t>(i) * nc + a] * coef[static_cast<size_t>(a) * m + c];
+      if (sc > bs) {
+        bs = sc;
+        best = c;
+      }
+    }
+    pred[i] = best;
+  }
+  return pred;
+}
+
 // get_pls_fold_x_cache_float (plscv.cpp:593-667) and the uncached branch of
 // run_plscv_host (:2371-2381) compute the same per-fold data.
 PLSFoldCache pls_fold_cache(const float* x, int n, int p, const std::vector<int>& folds, const PLSOpts& o) {
@@ -448,7 +544,8 @@ PLSCVOut plsldacv_on_cache(const PLSFoldCache& cache, int n, int p, const std::v
     const int a = std::min(requested, fit.rank);
     evaluated = std::min(evaluated, a);
     const std::vector<int> pc =
-        lda_streamed(d.x_train, nt, code, d.x_val, static_cast<int>(d.validation.size()), p, fit, m, a);
+        o.da ? da_predict(d.x_train, nt, code, d.x_val, static_cast<int>(d.validation.size()), p, fit, m, a)
+             : lda_streamed(d.x_train, nt, code, d.x_val, static_cast<int>(d.validation.size()), p, fit, m, a);
     for (size_t i = 0; i < d.validation.size(); ++i) out.predicted[d.validation[i]] = classes[pc[i]];
   }
   const int best = std::min(evaluated, o.max_components);

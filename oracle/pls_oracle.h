@@ -19,6 +19,7 @@ struct PLSOpts {
   int fixed_components = 0;
   bool center = true;
   bool scale = true;
+  bool da = false;  // PLSDACV (PLSMode::PLS_DA): one-hot regression on the scores instead of LDA
 };
 
 struct PLSCVOut {

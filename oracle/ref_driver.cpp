@@ -249,8 +249,9 @@ int ref_dissimilarity(int* gidx, float* gdist, int samples, int gk, const int* r
   }
 }
 
-// PLSLDACV_CPU (kodama.hpp:906).  popts: folds, stratified, max_components,
-// fixed_components, center, scale, threads.
+// PLSLDACV_CPU (kodama.hpp:906), or PLSDACV_CPU (:899) with popts[7] != 0.
+// popts: folds, stratified, max_components, fixed_components, center, scale,
+// threads, da.
 int ref_plsldacv(
   const float* x, int n, int d, const int* labels, const int* constrain, int has_constrain,
   const int* popts, unsigned long long cv_seed, int* predicted, int* folds,
@@ -270,7 +271,7 @@ int ref_plsldacv(
     std::vector<int> lab(labels, labels + n);
     std::vector<int> con = has_constrain ? std::vector<int>(constrain, constrain + n) : std::vector<int>();
     const auto t0 = std::chrono::steady_clock::now();
-    const auto r = kodama::PLSLDACV_CPU(view, lab, con, opt);
+    const auto r = popts[7] != 0 ? kodama::PLSDACV_CPU(view, lab, con, opt) : kodama::PLSLDACV_CPU(view, lab, con, opt);
     *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     std::memcpy(predicted, r.predicted_labels.data(), sizeof(int) * n);
     std::memcpy(folds, r.fold_assignments.data(), sizeof(int) * n);

@@ -192,6 +192,10 @@ def main():
                                folds=10, stratified=True, max_components=6, fixed_components=0, cv_seed=7))
     cases.append(plsldacv_case("plsldacv_fixed5", dict(n=1000, d=80, seed=32, flip=0.4),
                                folds=8, stratified=False, max_components=5, fixed_components=5, cv_seed=9))
+    cases.append(plsldacv_case("plsdacv_stratified", dict(n=1100, d=60, seed=37, flip=0.3),
+                               folds=10, stratified=True, max_components=6, fixed_components=0, cv_seed=8, da=True))
+    cases.append(plsldacv_case("plsdacv_fixed4", dict(n=900, d=30, seed=38, flip=0.4),
+                               folds=8, stratified=False, max_components=4, fixed_components=4, cv_seed=9, da=True))
     cases.append(plsldapredict_case("plsldapredict_c5", dict(n=1500, d=50, seed=33, flip=0.2), 1000,
                                     components=5))
     cases.append(core_plslda_case("core_plslda_evolutionary", dict(n=900, d=40, seed=34, random_labels=10),

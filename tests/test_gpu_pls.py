@@ -46,6 +46,19 @@ def test_plsldacv_degenerate_and_single_class_folds(kg, orc):
     assert np.array_equal(g.predicted_labels, pred) and g.selected_components == sel
 
 
+@pytest.mark.parametrize("n,d,stratified,maxc,fixc", [(300, 20, True, 5, 0), (500, 40, False, 5, 5),
+                                                     (800, 60, True, 8, 3), (400, 10, False, 4, 0),
+                                                     (250, 80, True, 6, 6)])
+def test_plsdacv_matches_oracle(kg, orc, n, d, stratified, maxc, fixc):
+    x, lab = _noisy(n, d, seed=n + d, flip=0.3)
+    kw = dict(folds=10, stratified=stratified, max_components=maxc, fixed_components=fixc, cv_seed=7)
+    pred, folds, sel, abc, _ = orc.plsldacv(x, lab, da=True, **kw)
+    g = kg.PLSDACV(x, lab, **kw)
+    assert np.array_equal(g.fold_assignments, folds)
+    assert np.array_equal(g.predicted_labels, pred) and g.selected_components == sel
+    assert np.array_equal(g.accuracy_by_components[:maxc], abc[:maxc])
+
+
 @pytest.mark.parametrize("n,nt,d,comp", [(400, 300, 30, 5), (150, 500, 200, 4), (1000, 1000, 50, 10)])
 def test_plsldapredict_matches_oracle(kg, orc, n, nt, d, comp):
     x, lab = _noisy(n + nt, d, seed=nt + d, flip=0.2)
@@ -86,8 +99,9 @@ def test_core_plslda_matches_oracle(kg, orc, coarsening, constrained, stratified
 def test_gpu_plsldacv_golden(kg, case):
     x, labels = G.pls_inputs(case["input"])
     o = case["options"]
-    r = kg.PLSLDACV(x, labels, folds=o["folds"], stratified=o["stratified"], max_components=o["max_components"],
-                    fixed_components=o["fixed_components"], cv_seed=o["cv_seed"])
+    fn = kg.PLSDACV if o.get("da") else kg.PLSLDACV
+    r = fn(x, labels, folds=o["folds"], stratified=o["stratified"], max_components=o["max_components"],
+           fixed_components=o["fixed_components"], cv_seed=o["cv_seed"])
     assert r.predicted_labels[:32].tolist() == case["predicted_head"]
     assert G.sha(r.predicted_labels) == case["predicted_sha256"]
     assert G.sha(r.fold_assignments) == case["folds_sha256"]

@@ -112,6 +112,18 @@ def test_pls_matrix_vs_reference(orc):
 
 
 @needs_ref
+@pytest.mark.parametrize("n,d,stratified,maxc,fixc", [(300, 20, True, 5, 0), (500, 40, False, 5, 5),
+                                                     (400, 10, False, 4, 0), (250, 80, True, 6, 6)])
+def test_plsdacv_vs_reference(orc, n, d, stratified, maxc, fixc):
+    x, lab = _low_rank_noisy(n, d, seed=n + d)
+    kw = dict(folds=10, stratified=stratified, max_components=maxc, fixed_components=fixc, cv_seed=7, da=True)
+    a = ref.plsldacv(x, lab, **kw)
+    b = orc.plsldacv(x, lab, **kw)
+    for u, v in zip(a[:4], b[:4]):
+        assert np.array_equal(u, v)
+
+
+@needs_ref
 @pytest.mark.parametrize("classifier", [0, 1])
 @pytest.mark.parametrize("inputs", ["start", "constrain", "fixed", "all"])
 def test_semi_matrix_vs_reference(orc, classifier, inputs):
