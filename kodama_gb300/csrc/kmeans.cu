@@ -108,6 +108,25 @@ __device__ __forceinline__ float dot_x86_reg(const float (&a)[16 * NB], const fl
   return sum;
 }
 
+// The same x86-order dot with the point read from memory (NB*16 >= d).
+template <int NB>
+__device__ __forceinline__ float dot_x86_mem(const float* a, const float* b, int d) {
+  float p[16];
+#pragma unroll
+  for (int l = 0; l < 16; ++l) p[l] = 0.0f;
+  const int nfull = d >> 4;
+  for (int blk = 0; blk < nfull; ++blk) {
+#pragma unroll
+    for (int l = 0; l < 16; ++l) p[l] = fadd(p[l], fmul(a[16 * blk + l], b[16 * blk + l]));
+  }
+  float lane[4];
+#pragma unroll
+  for (int l = 0; l < 4; ++l) lane[l] = fadd(fadd(p[l], p[4 + l]), fadd(p[8 + l], p[12 + l]));
+  float sum = fadd(fadd(fadd(lane[0], lane[1]), lane[2]), lane[3]);
+  for (int i = 16 * nfull; i < d; ++i) sum = fadd(sum, fmul(a[i], b[i]));
+  return sum;
+}
+
 // Two rows per thread; centroids of the problem staged in shared memory with
 // rows padded to a multiple of 4 floats so they are read with 128-bit loads.
 constexpr int kAssignRows = 2;
@@ -394,10 +413,14 @@ __global__ void __launch_bounds__(32 * kTcAssignWarps) assign_tc_kernel(KMeansBa
       for (int c = half; c < k; c += 2) amin = fminf(amin, arow[c]);
       amin = fminf(amin, __shfl_xor_sync(kFull, amin, 16));
       const float thr = amin + 2.0f * fadd(pn, scn[kpad]) * B.tc_crel;
-      float xv[16 * KS];
+      // up to 128 coordinates of the row in registers, wider rows read from L1
+      constexpr int kRegKS = KS <= 8 ? KS : 1;
+      float xv[16 * kRegKS];
       const float* xr = B.x + static_cast<size_t>(grow) * d;
+      if constexpr (KS <= 8) {
 #pragma unroll
-      for (int j = 0; j < 16 * KS; ++j) xv[j] = j < d ? xr[j] : 0.0f;
+        for (int j = 0; j < 16 * KS; ++j) xv[j] = j < d ? xr[j] : 0.0f;
+      }
       int best = k;
       float bestd = INFINITY;
       // each lane walks its own candidates; the lanes compute their dots
@@ -410,7 +433,12 @@ __global__ void __launch_bounds__(32 * kTcAssignWarps) assign_tc_kernel(KMeansBa
         if (!__any_sync(kFull, have)) break;
         const int c = have ? cpos : 0;
         const float* cc = B.tc_cent_smem ? scf + static_cast<size_t>(c) * d4 : cent + static_cast<size_t>(c) * d;
-        const float dt = dot_x86_reg<KS>(xv, cc, d);
+        float dt;
+        if constexpr (KS <= 8) {
+          dt = dot_x86_reg<KS>(xv, cc, d);
+        } else {
+          dt = dot_x86_mem<KS>(xr, cc, d);
+        }
         if (have) {
           const float dist = __fsub_rn(fadd(pn, scn[c]), fmul(2.0f, dt));
           if (dist < bestd || (dist == bestd && c < best)) {
@@ -700,7 +728,7 @@ __global__ void finalize_kernel(KMeansBatch B) {
 // Above 128 centroids the per-warp distance tiles hold the kernel to one
 // 4-warp CTA per SM and the exact assignment is faster.
 bool kmeans_tc_supported(int d, int k) {
-  if (d < 1 || d > 128 || k < 1 || k > 128) return false;
+  if (d < 1 || d > 256 || k < 1 || k > 128) return false;
   return assign_tc_smem(k, d, (d + 15) / 16 * 16, false) <= kTcSmemLimit;
 }
 
@@ -723,10 +751,11 @@ int kmeans_run(const KMeansBatch& B, cudaStream_t st) {
   const bool tc = B.xh != nullptr && kmeans_tc_supported(B.d, B.k);
   const bool cent_smem = tc && assign_tc_smem(B.k, B.d, B.dp, true) <= kTcSmemLimit;
   const size_t tc_bytes = tc ? assign_tc_smem(B.k, B.d, B.dp, cent_smem) : 0;
-  const bool tc_wide = B.dp > 64;
+  const int tc_ks = B.dp <= 64 ? 4 : (B.dp <= 128 ? 8 : 16);
   if (tc) {
     cudaFuncSetAttribute(assign_tc_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(tc_bytes));
     cudaFuncSetAttribute(assign_tc_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(tc_bytes));
+    cudaFuncSetAttribute(assign_tc_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(tc_bytes));
   }
   // 64-row blocks per CTA: the centroids are staged once per CTA, but the grid
   // keeps at least two CTAs per SM
@@ -755,7 +784,8 @@ int kmeans_run(const KMeansBatch& B, cudaStream_t st) {
     if (tc) {
       // the centroids' bf16 split (its own launch is counted there)
       bf16_split_rows(B.cent, B.problems * B.k, B.d, B.dp, B.ch, B.cl, st);
-      if (tc_wide) assign_tc_kernel<8><<<tgrid, 32 * kTcAssignWarps, tc_bytes, st>>>(T, final_pass);
+      if (tc_ks == 16) assign_tc_kernel<16><<<tgrid, 32 * kTcAssignWarps, tc_bytes, st>>>(T, final_pass);
+      else if (tc_ks == 8) assign_tc_kernel<8><<<tgrid, 32 * kTcAssignWarps, tc_bytes, st>>>(T, final_pass);
       else assign_tc_kernel<4><<<tgrid, 32 * kTcAssignWarps, tc_bytes, st>>>(T, final_pass);
       return;
     }

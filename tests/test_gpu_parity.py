@@ -80,9 +80,9 @@ def test_matrix_raw_mixture(kg, orc):
     _assert_matrix_equal(gpu, ref)
 
 
-@pytest.mark.parametrize("d", [72, 100, 128])
+@pytest.mark.parametrize("d", [72, 100, 128, 160, 200])
 def test_matrix_raw_high_dim(kg, orc, d):
-    # tensor-core graph and k-means with 16-coordinate k-steps up to 8
+    # tensor-core graph (d <= 128) and k-means (d <= 256) with 16-coordinate k-steps up to 8 / 16
     x, _ = datasets.gaussian_mixture(n=2500, d=d, clusters=9, mean_scale=3.0, seed=d)
     kw = _matrix_kw(runs=3, cycles=8, graph_neighbors=30, knn_k=10, splitting=100)
     gpu = kg.KODAMA_matrix(x, materialize_graph=True, **kw)
