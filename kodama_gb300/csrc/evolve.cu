@@ -79,7 +79,7 @@ struct Smem {
   int* scratch32;    // per-position counts / bucket offsets
   int* trans;        // class x prediction counts (shared or global)
   unsigned* hist;    // per-warp packed 8-bit vote counters, or nullptr
-  int hist_words;    // words per warp
+  int hist_words;    // words per histogram (two per warp)
   uint64_t* raw;     // engine outputs of one shuffle (global scratch)
   int* cnt;          // per code: count in proposal
   int* firstpos;     // per code: first row
@@ -378,27 +378,37 @@ __device__ __forceinline__ int vote_tiebreak(int code, unsigned tied, const floa
   return bc;
 }
 
-// Fold vote of one row with a per-warp histogram of packed 8-bit counters in
-// shared memory (hist: ceil(C0/4) zeroed words, left zeroed on return).
-__device__ __forceinline__ int vote_row_hist(const uint16_t* lab, uint16_t id, const float* scrow, int w, int lane,
-                                             unsigned* hist) {
-  const int code = id != kNoRow ? static_cast<int>(lab[id]) : -1;
-  if (__ballot_sync(kFull, code >= 0) == 0u) return -1;
-  const int sh = (code & 3) * 8;
-  unsigned old = 0;
-  if (code >= 0) old = atomicAdd(&hist[code >> 2], 1u << sh);
+// Fold votes of two rows with per-row histograms of packed 8-bit counters in
+// shared memory (ceil(C0/4) zeroed words each, left zeroed on return): the
+// two rows' shared-memory round trips overlap.
+__device__ __forceinline__ void vote_rows_hist2(const uint16_t* lab, uint16_t ida, uint16_t idb, const float* sca,
+                                                const float* scb, int w, int lane, unsigned* ha, unsigned* hb,
+                                                int& outa, int& outb) {
+  const int ca = ida != kNoRow ? static_cast<int>(lab[ida]) : -1;
+  const int cb = idb != kNoRow ? static_cast<int>(lab[idb]) : -1;
+  const unsigned va = __ballot_sync(kFull, ca >= 0), vb = __ballot_sync(kFull, cb >= 0);
+  const int sha = (ca & 3) * 8, shb = (cb & 3) * 8;
+  unsigned olda = 0, oldb = 0;
+  if (ca >= 0) olda = atomicAdd(&ha[ca >> 2], 1u << sha);
+  if (cb >= 0) oldb = atomicAdd(&hb[cb >> 2], 1u << shb);
   __syncwarp();
-  const int cnt = code >= 0 ? static_cast<int>((hist[code >> 2] >> sh) & 0xffu) : 0;
-  const bool first = code >= 0 && ((old >> sh) & 0xffu) == 0u;
-  const int maxc = __reduce_max_sync(kFull, cnt);
-  const bool top = code >= 0 && cnt == maxc;
-  const int bestc = static_cast<int>(__reduce_min_sync(kFull, top ? static_cast<unsigned>(code) : 0xffffffffu));
-  const unsigned tied = __ballot_sync(kFull, top && first);
+  const int cnta = ca >= 0 ? static_cast<int>((ha[ca >> 2] >> sha) & 0xffu) : 0;
+  const int cntb = cb >= 0 ? static_cast<int>((hb[cb >> 2] >> shb) & 0xffu) : 0;
+  const bool firsta = ca >= 0 && ((olda >> sha) & 0xffu) == 0u;
+  const bool firstb = cb >= 0 && ((oldb >> shb) & 0xffu) == 0u;
+  const int maxa = __reduce_max_sync(kFull, cnta);
+  const int maxb = __reduce_max_sync(kFull, cntb);
+  const bool topa = ca >= 0 && cnta == maxa, topb = cb >= 0 && cntb == maxb;
+  const int besta = static_cast<int>(__reduce_min_sync(kFull, topa ? static_cast<unsigned>(ca) : 0xffffffffu));
+  const int bestb = static_cast<int>(__reduce_min_sync(kFull, topb ? static_cast<unsigned>(cb) : 0xffffffffu));
+  const unsigned tieda = __ballot_sync(kFull, topa && firsta);
+  const unsigned tiedb = __ballot_sync(kFull, topb && firstb);
   __syncwarp();
-  if (code >= 0) hist[code >> 2] = 0u;
+  if (ca >= 0) ha[ca >> 2] = 0u;
+  if (cb >= 0) hb[cb >> 2] = 0u;
   __syncwarp();
-  if (__popc(tied) == 1) return bestc;
-  return vote_tiebreak(code, tied, scrow, w, lane);
+  outa = va == 0u ? -1 : (__popc(tieda) == 1 ? besta : vote_tiebreak(ca, tieda, sca, w, lane));
+  outb = vb == 0u ? -1 : (__popc(tiedb) == 1 ? bestb : vote_tiebreak(cb, tiedb, scb, w, lane));
 }
 
 // ---------------------------------------------------------------------------
@@ -465,15 +475,34 @@ __device__ void vote_block(const EvolveParams& P, const Smem& s, int prob, const
       const int r = i < count ? (rows ? static_cast<int>(rows[i]) : i) : 0;
       ids[u] = (i < count && lane < w) ? nbp[static_cast<size_t>(r) * w + lane] : kNoRow;
     }
+    if (s.hist) {
+      // two rows per step, each with its own histogram
+      unsigned* ha = s.hist + (2 * warp) * s.hist_words;
+      unsigned* hb = ha + s.hist_words;
 #pragma unroll
-    for (int u = 0; u < kB; ++u) {
-      const int i = i0 + u;
-      if (i >= count) break;
-      const int r = rows ? static_cast<int>(rows[i]) : i;
-      const int best = s.hist ? vote_row_hist(lab, ids[u], scp + static_cast<size_t>(r) * w, w, lane,
-                                              s.hist + warp * s.hist_words)
-                              : vote_row(lab, ids[u], scp + static_cast<size_t>(r) * w, w, lane);
-      if (best >= 0 && lane == 0) out[r] = static_cast<uint16_t>(best);
+      for (int u = 0; u < kB; u += 2) {
+        const int i = i0 + u;
+        if (i >= count) break;
+        const bool two = i + 1 < count;
+        const int ra = rows ? static_cast<int>(rows[i]) : i;
+        const int rb = two ? (rows ? static_cast<int>(rows[i + 1]) : i + 1) : ra;
+        int ba, bb;
+        vote_rows_hist2(lab, ids[u], two ? ids[u + 1] : kNoRow, scp + static_cast<size_t>(ra) * w,
+                        scp + static_cast<size_t>(rb) * w, w, lane, ha, hb, ba, bb);
+        if (lane == 0) {
+          if (ba >= 0) out[ra] = static_cast<uint16_t>(ba);
+          if (two && bb >= 0) out[rb] = static_cast<uint16_t>(bb);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int u = 0; u < kB; ++u) {
+        const int i = i0 + u;
+        if (i >= count) break;
+        const int r = rows ? static_cast<int>(rows[i]) : i;
+        const int best = vote_row(lab, ids[u], scp + static_cast<size_t>(r) * w, w, lane);
+        if (best >= 0 && lane == 0) out[r] = static_cast<uint16_t>(best);
+      }
     }
   }
   if (has_empty) {
@@ -1267,8 +1296,8 @@ __device__ Smem carve_smem(const EvolveParams& P, unsigned char* smem_raw) {
   s.hist_words = (C + 3) / 4;
   if (P.smem_hist) {
     s.hist = reinterpret_cast<unsigned*>(smem_raw + off);
-    off += align_up(sizeof(unsigned) * kWarps * s.hist_words, 16);
-    for (int i = threadIdx.x; i < kWarps * s.hist_words; i += kThreads) s.hist[i] = 0u;
+    off += align_up(sizeof(unsigned) * 2 * kWarps * s.hist_words, 16);
+    for (int i = threadIdx.x; i < 2 * kWarps * s.hist_words; i += kThreads) s.hist[i] = 0u;
   } else {
     s.hist = nullptr;
   }
@@ -1829,7 +1858,7 @@ __global__ void __launch_bounds__(kThreads, 1) evolve_pls_kernel(EvolvePlsParams
 size_t evolve_smem_bytes(int L, int C0max, bool rows_in_smem, bool trans_in_smem, bool hist_in_smem) {
   auto al = [](size_t v) { return (v + 15) / 16 * 16; };
   size_t b = al(sizeof(Fixed));
-  if (hist_in_smem) b += al(sizeof(unsigned) * kWarps * ((C0max + 3) / 4));
+  if (hist_in_smem) b += al(sizeof(unsigned) * 2 * kWarps * ((C0max + 3) / 4));
   b += 6 * al(sizeof(int) * C0max) + al(sizeof(int) * (C0max + 1));
   b += 2 * al(sizeof(double) * C0max) + al(sizeof(double) * 2 * C0max);
   if (trans_in_smem) b += al(sizeof(int) * static_cast<size_t>(C0max) * C0max);
