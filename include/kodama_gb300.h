@@ -377,7 +377,7 @@ int kgb_knn_graph(const float* x, int32_t n, int32_t d, int32_t K, int32_t devic
 #define KGB_KNN_AUTO 0        /* the tensor-core search where it applies, else the brute force */
 #define KGB_KNN_BRUTE_FORCE 1 /* float32 brute force in the canonical order */
 #define KGB_KNN_TENSOR 2      /* bf16 hi+lo tensor-core candidates, canonical re-rank, per-row
-                                 certificate, brute force for uncertified rows; d <= 128, K <= 96 */
+                                 certificate, brute force for uncertified rows; d <= 256, K <= 96 */
 
 /* kgb_knn_graph with an explicit method; fallback_rows (may be NULL) receives
  * how many rows were computed by the brute force. */

@@ -1592,7 +1592,7 @@ void exact_graph(Ctx& ctx, const float* d_x, int n, int d, int K, int method, in
   const int segments = 4;
   const bool tc = method == KGB_KNN_TENSOR || (method == KGB_KNN_AUTO && kgb::knn_tc_supported(n, d, K));
   if (method == KGB_KNN_TENSOR && !kgb::knn_tc_supported(n, d, K))
-    fail(KGB_EINVAL, "the tensor-core kNN search needs d <= 128, K <= 96 and n > 2 * (K + 16) + 64");
+    fail(KGB_EINVAL, "the tensor-core kNN search needs d <= 256, K <= 96 and n > 2 * (K + 16) + 64");
   if (tc) {
     void* scratch = ctx.alloc<unsigned char>(kgb::knn_tc_scratch(n, d, K, segments));
     ck_launch(kgb::knn_tc_graph(d_x, n, d, K, segments, scratch, d_idx, d_dist, ctx.stream()), "kNN graph");

@@ -48,7 +48,9 @@ namespace {
 constexpr int kTcWarps = 4;            // warps per CTA, 16 queries each
 constexpr int kTcQ = 16 * kTcWarps;    // queries per CTA
 constexpr int kTcN = 64;               // candidates per tile
-constexpr int kTcMaxKs = 8;            // k-steps of 16 held in registers (dp <= 128)
+constexpr int kTcRegKs = 8;            // k-steps whose query fragments (hi and lo) sit in registers
+constexpr int kTcMaxKs = 16;           // dp <= 256: above kTcRegKs the lo fragments come from shared memory
+constexpr size_t kTcSmemLimit = 227 * 1024;
 constexpr int kTileStride = kTcN + 8;  // floats per row of a warp's distance tile
 
 __device__ __forceinline__ uint32_t bf16_bits(float v) {
@@ -134,17 +136,24 @@ constexpr int kMaxPer = 8;   // re-rank candidates per lane (segs x 2 x kp <= 25
 
 // Shared memory: 2 x (hi, lo) candidate tiles, 2 x tile norms, per warp a
 // 16 x kTileStride distance tile, 16 x 4 flag masks, 32 thresholds and 32
-// lane-interleaved max-heaps of kp (distance, row) entries.
-size_t tc_smem_bytes(int row_words, int kp) {
+// lane-interleaved max-heaps of kp (distance, row) entries; above kTcRegKs
+// k-steps also the warp's 16 lo query rows (row stride row_words, the
+// candidate tiles' conflict-free stride).
+size_t tc_smem_bytes(int row_words, int kp, int dp) {
+  const size_t lo_rows = dp > 16 * kTcRegKs ? kTcWarps * 16 * static_cast<size_t>(row_words) * 4 : 0;
   return 2 * 2 * static_cast<size_t>(kTcN) * row_words * 4 + 2 * kTcN * 4 +
-         kTcWarps * (16 * kTileStride * 4 + 64 * 4 + 32 * 4 + 32 * static_cast<size_t>(kp) * 8);
+         kTcWarps * (16 * kTileStride * 4 + 64 * 4 + 32 * 4 + 32 * static_cast<size_t>(kp) * 8) + lo_rows;
 }
 
-// KS: k-steps of 16 coordinates in the query fragments (dp <= 16 KS); each
-// thread copies 2 KS 16-byte chunks of a candidate tile (kTcN x dp / 8 / 128).
+// KS: k-steps of 16 coordinates in the query fragments (dp <= 16 KS).  Up to
+// kTcRegKs every thread keeps its 2 KS 16-byte chunks of a candidate tile
+// (kTcN x dp / 8 / 128) in registers; above it the chunks are recomputed per
+// tile and the lo query fragments are read from shared memory per k-step.
 template <int KS>
 __global__ void __launch_bounds__(32 * kTcWarps, 2) tc_candidates_kernel(TcArgs A) {
-  constexpr int kMaxLoads = 2 * KS;
+  constexpr bool kLoShared = KS > kTcRegKs;
+  constexpr int kMaxLoads = kLoShared ? 1 : 2 * KS;
+  constexpr int kRegLo = kLoShared ? 1 : KS;
   extern __shared__ __align__(16) unsigned char smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
   const int n = A.n, dp = A.dp, kp = A.kp, rw = A.row_words, ksn = dp >> 4;
@@ -159,8 +168,20 @@ __global__ void __launch_bounds__(32 * kTcWarps, 2) tc_candidates_kernel(TcArgs 
   htau[lane] = INFINITY;
 
   const int q0 = blockIdx.x * kTcQ + warp * 16;
+  // the warp's 16 lo query rows in shared memory (only above kTcRegKs)
+  uint32_t* qlo = reinterpret_cast<uint32_t*>(cnb + 2 * kTcN + kTcWarps * (16 * kTileStride + 64 + 32 + 32 * kp * 2)) +
+                  warp * 16 * rw;
+  if (kLoShared) {
+    const int hw = dp >> 1;  // 32-bit words per row
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(A.xl);
+    for (int w = lane; w < 16 * hw; w += 32) {
+      const int rr = w / hw, c = w - rr * hw;
+      qlo[rr * rw + c] = src[static_cast<size_t>(min(q0 + rr, n - 1)) * hw + c];
+    }
+    __syncwarp();
+  }
   // query fragments: rows g and g + 8 of the warp's 16 queries
-  uint32_t ah[KS][4], al[KS][4];
+  uint32_t ah[KS][4], al[kRegLo][4];
   {
     const int ra = min(q0 + g, n - 1), rb = min(q0 + g + 8, n - 1);
 #pragma unroll
@@ -169,11 +190,15 @@ __global__ void __launch_bounds__(32 * kTcWarps, 2) tc_candidates_kernel(TcArgs 
       if (ks < ksn) {
         pa = *reinterpret_cast<const uint2*>(A.xh + static_cast<size_t>(ra) * dp + ks * 16 + 4 * tig);
         pb = *reinterpret_cast<const uint2*>(A.xh + static_cast<size_t>(rb) * dp + ks * 16 + 4 * tig);
-        qa = *reinterpret_cast<const uint2*>(A.xl + static_cast<size_t>(ra) * dp + ks * 16 + 4 * tig);
-        qb = *reinterpret_cast<const uint2*>(A.xl + static_cast<size_t>(rb) * dp + ks * 16 + 4 * tig);
+        if (!kLoShared) {
+          qa = *reinterpret_cast<const uint2*>(A.xl + static_cast<size_t>(ra) * dp + ks * 16 + 4 * tig);
+          qb = *reinterpret_cast<const uint2*>(A.xl + static_cast<size_t>(rb) * dp + ks * 16 + 4 * tig);
+        }
       }
       ah[ks][0] = pa.x; ah[ks][2] = pa.y; ah[ks][1] = pb.x; ah[ks][3] = pb.y;
-      al[ks][0] = qa.x; al[ks][2] = qa.y; al[ks][1] = qb.x; al[ks][3] = qb.y;
+      if (!kLoShared) {
+        al[ks][0] = qa.x; al[ks][2] = qa.y; al[ks][1] = qb.x; al[ks][3] = qb.y;
+      }
     }
   }
   const int qa_row = q0 + g, qb_row = q0 + g + 8;
@@ -195,7 +220,7 @@ __global__ void __launch_bounds__(32 * kTcWarps, 2) tc_candidates_kernel(TcArgs 
     ld_row[t] = 0;
     ld_col[t] = 0;
     ld_smem[t] = 0;
-    if (e < kTcN * chunks) {
+    if (!kLoShared && e < kTcN * chunks) {
       const int c = e / chunks, ch = e - c * chunks;
       ld_row[t] = c;
       ld_col[t] = ch * 8;
@@ -219,9 +244,23 @@ __global__ void __launch_bounds__(32 * kTcWarps, 2) tc_candidates_kernel(TcArgs 
     const int base = tile * kTcN;
     uint32_t* dh = cbuf + (buf * 2 + 0) * kTcN * rw;
     uint32_t* dl = cbuf + (buf * 2 + 1) * kTcN * rw;
+    if (kLoShared) {
+      for (int e = threadIdx.x; e < kTcN * chunks; e += 32 * kTcWarps) {
+        const int c = e / chunks, ch = e - c * chunks;
+        const int so = c * rw + ch * 4;
+        if (base + c < n) {
+          const size_t src = static_cast<size_t>(base + c) * dp + ch * 8;
+          cp_async16(dh + so, A.xh + src);
+          cp_async16(dl + so, A.xl + src);
+        } else {
+          *reinterpret_cast<uint4*>(dh + so) = make_uint4(0u, 0u, 0u, 0u);
+          *reinterpret_cast<uint4*>(dl + so) = make_uint4(0u, 0u, 0u, 0u);
+        }
+      }
+    }
 #pragma unroll
     for (int t = 0; t < kMaxLoads; ++t) {
-      if (t < nld) {
+      if (!kLoShared && t < nld) {
         const int row = base + ld_row[t];
         if (row < n) {
           const size_t src = static_cast<size_t>(row) * dp + ld_col[t];
@@ -266,6 +305,15 @@ __global__ void __launch_bounds__(32 * kTcWarps, 2) tc_candidates_kernel(TcArgs 
 #pragma unroll
     for (int ks = 0; ks < KS; ++ks) {
       if (ks < ksn) {
+        uint32_t lo[4];
+        if (kLoShared) {
+          const uint2 la = *reinterpret_cast<const uint2*>(qlo + g * rw + ks * 8 + 2 * tig);
+          const uint2 lb = *reinterpret_cast<const uint2*>(qlo + (g + 8) * rw + ks * 8 + 2 * tig);
+          lo[0] = la.x; lo[2] = la.y; lo[1] = lb.x; lo[3] = lb.y;
+        } else {
+#pragma unroll
+          for (int i = 0; i < 4; ++i) lo[i] = al[kLoShared ? 0 : ks][i];
+        }
 #pragma unroll
         for (int nt = 0; nt < 8; ++nt) {
           const int off = (nt * 8 + g) * rw + ks * 8 + 2 * tig;
@@ -273,7 +321,7 @@ __global__ void __launch_bounds__(32 * kTcWarps, 2) tc_candidates_kernel(TcArgs 
           const uint2 bl = *reinterpret_cast<const uint2*>(tl + off);
           mma16816(accs[nt], ah[ks], bh);
           mma16816(accs[nt], ah[ks], bl);
-          mma16816(accs[nt], al[ks], bh);
+          mma16816(accs[nt], lo, bh);
         }
       }
     }
@@ -508,7 +556,10 @@ int bf16_split_rows(const float* x, int n, int d, int dp, uint16_t* xh, uint16_t
 bool knn_tc_supported(int n, int d, int K) {
   int segs = 0, kp = 0;
   tc_shape(K, &segs, &kp);
-  return d >= 1 && d <= 16 * kTcMaxKs && K >= 1 && K <= 96 && n > 2 * kp + kTcN;
+  if (!(d >= 1 && d <= 16 * kTcMaxKs && K >= 1 && K <= 96 && n > 2 * kp + kTcN)) return false;
+  const int dp = (d + 15) / 16 * 16, half = dp / 2;
+  const int rw = (half % 16 == 8) ? half : half + 8;
+  return tc_smem_bytes(rw, kp, dp) <= kTcSmemLimit;
 }
 
 namespace {
@@ -572,18 +623,23 @@ int knn_tc_graph(const float* x, int n, int d, int K, int segments, void* scratc
   A.cand = cand;
   A.cand_a = cand_a;
   A.bound = bound;
-  const size_t smem = tc_smem_bytes(L.rw, L.kp);
+  const size_t smem = tc_smem_bytes(L.rw, L.kp, L.dp);
   const dim3 grid((n + kTcQ - 1) / kTcQ, L.segs);
   if (L.dp <= 64) {
     e = cudaFuncSetAttribute(tc_candidates_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              static_cast<int>(smem));
     if (e != cudaSuccess) return static_cast<int>(e);
     tc_candidates_kernel<4><<<grid, 32 * kTcWarps, smem, st>>>(A);
-  } else {
+  } else if (L.dp <= 16 * kTcRegKs) {
     e = cudaFuncSetAttribute(tc_candidates_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              static_cast<int>(smem));
     if (e != cudaSuccess) return static_cast<int>(e);
     tc_candidates_kernel<8><<<grid, 32 * kTcWarps, smem, st>>>(A);
+  } else {
+    e = cudaFuncSetAttribute(tc_candidates_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(smem));
+    if (e != cudaSuccess) return static_cast<int>(e);
+    tc_candidates_kernel<16><<<grid, 32 * kTcWarps, smem, st>>>(A);
   }
   const float crel = 1e-4f + 2e-6f * static_cast<float>(L.dp);
   tc_rerank_kernel<<<(n + 3) / 4, 128, 0, st>>>(x, n, d, K, L.segs * 2 * L.kp, L.segs, cand, cand_a, bound, nrm,
