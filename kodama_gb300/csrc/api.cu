@@ -674,6 +674,7 @@ PlsBuffers pls_buffers(Ctx& ctx, const float* d_X, int R, int L, int p, const Pl
   a.sdev = ctx.alloc<float>(static_cast<size_t>(S) * p);
   a.Z = ctx.alloc<float>(static_cast<size_t>(S) * L * p);
   a.xsum = ctx.alloc<float>(static_cast<size_t>(S) * p);
+  a.zexp = ctx.alloc<int>(static_cast<size_t>(S) * p);
   a.Xv = d_Xv;
   a.NV = NV;
   a.Zv = d_Xv != nullptr ? ctx.alloc<float>(static_cast<size_t>(R) * NV * p) : nullptr;
@@ -693,6 +694,7 @@ PlsBuffers pls_buffers(Ctx& ctx, const float* d_X, int R, int L, int p, const Pl
   e.tiles_after_s = 1;  // no fold Gram yet: every slice computes scores in the fit
   e.Z = a.Z;
   e.xsum = a.xsum;
+  e.zexp = a.zexp;
   e.gram = nullptr;
   e.use_gram = ctx.alloc<uint8_t>(S);
   ck(cudaMemsetAsync(const_cast<uint8_t*>(e.use_gram), 0, S, st), "memset");

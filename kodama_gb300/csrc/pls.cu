@@ -110,8 +110,13 @@ __global__ void standardize_kernel(PlsPrepArgs a) {
   }
 }
 
+__device__ __forceinline__ int biased_exp1(float v) {
+  return max(static_cast<int>((__float_as_uint(v) >> 23) & 0xffu), 1);
+}
+
 // Column sums of the standardised training rows in row order (the x_sum of
-// the cross-product, label independent).
+// the cross-product, label independent), and each column's largest biased
+// exponent over those rows (the fixed-point bound of block_loading).
 __global__ void xsum_kernel(PlsPrepArgs a) {
   const int s = blockIdx.x;
   const int j = blockIdx.y * blockDim.x + threadIdx.x;
@@ -119,52 +124,81 @@ __global__ void xsum_kernel(PlsPrepArgs a) {
   const float* Zs = a.Z + static_cast<size_t>(s) * a.L * a.p;
   const int b = a.train_off[s], e = a.train_off[s + 1];
   float acc = 0.0f;
+  int ze = 1;
   for (int t = b; t < e; t += 8) {
     float v[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) v[q] = t + q < e ? Zs[static_cast<size_t>(a.train_idx[t + q]) * a.p + j] : 0.0f;
 #pragma unroll
     for (int q = 0; q < 8; ++q)
-      if (t + q < e) acc = __fadd_rn(acc, v[q]);
+      if (t + q < e) {
+        acc = __fadd_rn(acc, v[q]);
+        ze = max(ze, biased_exp1(v[q]));
+      }
   }
   a.xsum[static_cast<size_t>(s) * a.p + j] = acc;
+  a.zexp[static_cast<size_t>(s) * a.p + j] = ze;
 }
 
 // densef_gram: G(j, k) = sum over training rows (ascending) of z_j * z_k, one
-// 32 x 32 tile of the lower triangle per CTA (blockIdx.y enumerates tiles),
-// written to both triangles.
-__global__ void __launch_bounds__(1024) gram_kernel(PlsPrepArgs a, const uint8_t* want) {
+// kGramT x kGramT tile of the lower triangle per CTA (blockIdx.y enumerates
+// tiles), written to both triangles.  Each thread keeps a 4 x 4 block of
+// entries, every one a float chain over the rows in ascending order; rows are
+// staged kGramR at a time (padding rows and columns are never added).
+constexpr int kGramT = 64;
+constexpr int kGramR = 32;
+__global__ void __launch_bounds__(256) gram_kernel(PlsPrepArgs a, const uint8_t* want) {
   const int s = blockIdx.x;
   if (!want[s]) return;
-  // tile index -> (jb, kb), kb <= jb
   int tile = blockIdx.y, jb = 0;
   while (tile > jb) {
     tile -= jb + 1;
     ++jb;
   }
   const int kb = tile;
-  __shared__ float zj[32][33];
-  __shared__ float zk[32][33];
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const int J = jb * 32 + ty, K = kb * 32 + tx;
+  __shared__ __align__(16) float zj[kGramR][kGramT];
+  __shared__ __align__(16) float zk[kGramR][kGramT];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   const float* Zs = a.Z + static_cast<size_t>(s) * a.L * a.p;
   const int b = a.train_off[s], e = a.train_off[s + 1];
-  float acc = 0.0f;
-  for (int t0 = b; t0 < e; t0 += 32) {
-    const int t = t0 + ty;
-    const int row = t < e ? a.train_idx[t] : -1;
-    const int cj = jb * 32 + tx, ck = kb * 32 + tx;
-    zj[ty][tx] = (row >= 0 && cj < a.p) ? Zs[static_cast<size_t>(row) * a.p + cj] : 0.0f;
-    zk[ty][tx] = (row >= 0 && ck < a.p) ? Zs[static_cast<size_t>(row) * a.p + ck] : 0.0f;
+  float acc[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) acc[u][v] = 0.0f;
+  for (int t0 = b; t0 < e; t0 += kGramR) {
+    for (int i = threadIdx.x; i < kGramR * kGramT; i += 256) {
+      const int q = i / kGramT, c = i - q * kGramT;
+      const int row = t0 + q < e ? a.train_idx[t0 + q] : -1;
+      const int cj = jb * kGramT + c, ck = kb * kGramT + c;
+      zj[q][c] = (row >= 0 && cj < a.p) ? Zs[static_cast<size_t>(row) * a.p + cj] : 0.0f;
+      zk[q][c] = (row >= 0 && ck < a.p) ? Zs[static_cast<size_t>(row) * a.p + ck] : 0.0f;
+    }
     __syncthreads();
-    const int cnt = min(32, e - t0);
-    for (int q = 0; q < cnt; ++q) acc = __fadd_rn(acc, __fmul_rn(zj[q][ty], zk[q][tx]));
+    const int cnt = min(kGramR, e - t0);
+    for (int q = 0; q < cnt; ++q) {
+      const float4 vj = *reinterpret_cast<const float4*>(&zj[q][ty * 4]);
+      const float4 vk = *reinterpret_cast<const float4*>(&zk[q][tx * 4]);
+      const float fj[4] = {vj.x, vj.y, vj.z, vj.w}, fk[4] = {vk.x, vk.y, vk.z, vk.w};
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = __fadd_rn(acc[u][v], __fmul_rn(fj[u], fk[v]));
+    }
     __syncthreads();
   }
-  if (J < a.p && K < a.p && K <= J) {
-    float* G = a.gram + static_cast<size_t>(s) * a.p * a.p;
-    G[static_cast<size_t>(J) * a.p + K] = acc;
-    G[static_cast<size_t>(K) * a.p + J] = acc;
+  float* G = a.gram + static_cast<size_t>(s) * a.p * a.p;
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int J = jb * kGramT + ty * 4 + u;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int K = kb * kGramT + tx * 4 + v;
+      if (J < a.p && K < a.p && K <= J) {
+        G[static_cast<size_t>(J) * a.p + K] = acc[u][v];
+        G[static_cast<size_t>(K) * a.p + J] = acc[u][v];
+      }
+    }
   }
 }
 
@@ -253,6 +287,31 @@ __device__ __forceinline__ bool round_check(long long V, int LSB, float A, int n
   return true;
 }
 
+// First pass of an exact dot, one term: the largest product exponent (top),
+// non-finite operands (bad) and an upward-rounded bound A of sum |x y|.
+__device__ __forceinline__ void exact_scan_term(float x, float y, int& top, int& bad, float& A) {
+  const unsigned ux = __float_as_uint(x), uy = __float_as_uint(y);
+  const int ex = static_cast<int>((ux >> 23) & 0xffu), ey = static_cast<int>((uy >> 23) & 0xffu);
+  bad |= (ex == 0xff) | (ey == 0xff);
+  if ((ux << 1) != 0u && (uy << 1) != 0u) top = max(top, max(ex, 1) + max(ey, 1) - 252);
+  A = __fadd_ru(A, __fmul_ru(fabsf(x), fabsf(y)));
+}
+
+// Second pass, one term: x y as a multiple of 2^LSB (truncated below it).
+__device__ __forceinline__ long long exact_fixed_term(float x, float y, int LSB) {
+  const unsigned ux = __float_as_uint(x), uy = __float_as_uint(y);
+  const unsigned bx = (ux >> 23) & 0xffu, by = (uy >> 23) & 0xffu;
+  const unsigned mx = (ux & 0x7fffffu) | (bx ? 0x800000u : 0u), my = (uy & 0x7fffffu) | (by ? 0x800000u : 0u);
+  const unsigned long long P = static_cast<unsigned long long>(mx) * my;
+  if (P == 0ull) return 0;
+  const int E = (bx ? static_cast<int>(bx) - 150 : -149) + (by ? static_cast<int>(by) - 150 : -149);
+  const int sh = E - LSB;
+  unsigned long long v;
+  if (sh >= 0) v = P << sh;
+  else v = -sh >= 64 ? 0ull : P >> (-sh);
+  return ((ux ^ uy) >> 31) ? -static_cast<long long>(v) : static_cast<long long>(v);
+}
+
 // Exact fixed-point sum over the warp; returns whether `out` is float(S_seq).
 template <class Term>
 __device__ bool warp_exact_dot(int n, Term term, int lane, float& out) {
@@ -261,11 +320,7 @@ __device__ bool warp_exact_dot(int n, Term term, int lane, float& out) {
   for (int k = lane; k < n; k += 32) {
     float x, y;
     term(k, x, y);
-    const unsigned ux = __float_as_uint(x), uy = __float_as_uint(y);
-    const int ex = static_cast<int>((ux >> 23) & 0xffu), ey = static_cast<int>((uy >> 23) & 0xffu);
-    bad |= (ex == 0xff) | (ey == 0xff);
-    if ((ux << 1) != 0u && (uy << 1) != 0u) top = max(top, max(ex, 1) + max(ey, 1) - 252);
-    A = __fadd_ru(A, __fmul_ru(fabsf(x), fabsf(y)));
+    exact_scan_term(x, y, top, bad, A);
   }
   bad = __reduce_or_sync(kFull, bad);
   top = __reduce_max_sync(kFull, top);
@@ -280,17 +335,7 @@ __device__ bool warp_exact_dot(int n, Term term, int lane, float& out) {
   for (int k = lane; k < n; k += 32) {
     float x, y;
     term(k, x, y);
-    const unsigned ux = __float_as_uint(x), uy = __float_as_uint(y);
-    const unsigned bx = (ux >> 23) & 0xffu, by = (uy >> 23) & 0xffu;
-    const unsigned mx = (ux & 0x7fffffu) | (bx ? 0x800000u : 0u), my = (uy & 0x7fffffu) | (by ? 0x800000u : 0u);
-    const unsigned long long P = static_cast<unsigned long long>(mx) * my;
-    if (P == 0ull) continue;
-    const int E = (bx ? static_cast<int>(bx) - 150 : -149) + (by ? static_cast<int>(by) - 150 : -149);
-    const int sh = E - LSB;
-    unsigned long long v;
-    if (sh >= 0) v = P << sh;
-    else v = -sh >= 64 ? 0ull : P >> (-sh);
-    acc += ((ux ^ uy) >> 31) ? -static_cast<long long>(v) : static_cast<long long>(v);
+    acc += exact_fixed_term(x, y, LSB);
   }
   acc = warp_sum_i64(acc);
   return round_check(acc, LSB, A, n, out);
@@ -383,6 +428,108 @@ __device__ float warp_power_norm(const float* v, int n, int lane) {
     out = power_norm2(acc);
   }
   return __shfl_sync(kFull, out, 0);
+}
+
+// loading[j] = float(S_seq) of sum over training rows k (ascending) of
+// double(Z[tix[k]][j]) * double(sc[k]), for every column j: t_mat_vec_float
+// of the scores path (plscv.cpp:884).  A thread per column and row group, so
+// the loads of a row are coalesced, and one pass over the rows: the fixed
+// point of warp_exact_dot is placed from an upper bound of the largest
+// product exponent, zexp[j] (the column's largest exponent, label
+// independent) plus the scores' largest exponent, instead of the exact one
+// (every term still fits: the bound only lowers the magnitudes).  The row
+// indices and scores are staged in shared memory so the loads of Z issue
+// back to back.  Partial sums of row groups combine exactly (integers), the
+// partial bounds of sum |x y| rounding upward; the check and the sequential
+// fallback are those of warp_exact_dot / warp_seq_dot.  `scratch` holds
+// 4 * kEvalThreads + 2 * kLoadChunk words plus 8 bytes of alignment; every
+// thread of the block calls this.
+constexpr int kLoadChunk = 1024;
+__device__ void block_loading(const float* __restrict__ Zs, int p, const int* __restrict__ tix, int nt,
+                              const float* __restrict__ sc, const int* __restrict__ zexp, float* ld, float* scratch,
+                              int lane, int warp) {
+  long long* pacc = reinterpret_cast<long long*>((reinterpret_cast<uintptr_t>(scratch) + 7) & ~uintptr_t(7));
+  float* pA = reinterpret_cast<float*>(pacc + kEvalThreads);
+  int* pflag = reinterpret_cast<int*>(pA + kEvalThreads);  // bit 0: non-finite, bit 1: a nonzero term
+  int* srow = pflag + kEvalThreads;
+  float* ssc = reinterpret_cast<float*>(srow + kLoadChunk);
+  int* flist = reinterpret_cast<int*>(pacc);  // undecided columns (after the partials are read)
+  __shared__ int fcount, smax;
+  const int t = threadIdx.x, lg = clog2i(nt);
+  if (t == 0) smax = 1;
+  __syncthreads();
+  {
+    int m = 1;
+    for (int k = t; k < nt; k += kEvalThreads) m = max(m, biased_exp1(sc[k]));
+    m = __reduce_max_sync(kFull, m);
+    if (lane == 0) atomicMax(&smax, m);
+  }
+  __syncthreads();
+  const int se = smax;
+  for (int j0 = 0; j0 < p; j0 += kEvalThreads) {
+    const int PB = min(p - j0, kEvalThreads), G = kEvalThreads / PB;
+    const int g = t / PB, jj = t - g * PB, j = j0 + jj;
+    const bool on = g < G;
+    const int LSB = (on ? zexp[j] : 1) + se - 252 + lg - 62;
+    long long acc = 0;
+    float A = 0.0f;
+    int bad = 0, nz = 0;
+    for (int k0 = 0; k0 < nt; k0 += kLoadChunk) {
+      const int cn = min(kLoadChunk, nt - k0);
+      for (int i = t; i < cn; i += kEvalThreads) {
+        srow[i] = tix[k0 + i];
+        ssc[i] = sc[k0 + i];
+      }
+      __syncthreads();
+      if (on) {
+#pragma unroll 8
+        for (int i = g; i < cn; i += G) {
+          const float x = Zs[static_cast<size_t>(srow[i]) * p + j], y = ssc[i];
+          const unsigned ux = __float_as_uint(x), uy = __float_as_uint(y);
+          bad |= (((ux >> 23) & 0xffu) == 0xffu) | (((uy >> 23) & 0xffu) == 0xffu);
+          nz |= ((ux << 1) != 0u) & ((uy << 1) != 0u);
+          A = __fadd_ru(A, __fmul_ru(fabsf(x), fabsf(y)));
+          acc += exact_fixed_term(x, y, LSB);
+        }
+      }
+      __syncthreads();
+    }
+    if (on) {
+      pacc[t] = acc;
+      pA[t] = A;
+      pflag[t] = bad | (nz << 1);
+    }
+    __syncthreads();
+    float out = 0.0f;
+    bool ok = false;
+    if (t < PB) {
+      int fl = pflag[t];
+      for (int q = 1; q < G; ++q) {
+        acc += pacc[t + q * PB];
+        A = __fadd_ru(A, pA[t + q * PB]);
+        fl |= pflag[t + q * PB];
+      }
+      if (!(fl & 1)) ok = (fl & 2) ? round_check(acc, LSB, A, nt, out) : (out = 0.0f, true);
+    }
+    if (t == 0) fcount = 0;
+    __syncthreads();
+    if (t < PB) {
+      if (ok) ld[j] = out;
+      else flist[atomicAdd(&fcount, 1)] = j;
+    }
+    __syncthreads();
+    const int nf = fcount;
+    for (int f = warp; f < nf; f += kEvalWarps) {
+      if (lane == 0) {
+        const int jf = flist[f];
+        double s = 0.0;
+        for (int k = 0; k < nt; ++k)
+          s = fma(static_cast<double>(Zs[static_cast<size_t>(tix[k]) * p + jf]), static_cast<double>(sc[k]), s);
+        ld[jf] = __double2float_rn(s);
+      }
+    }
+    __syncthreads();
+  }
 }
 
 // Scores of 32 rows (one per lane; row < 0 = none) for components
@@ -715,14 +862,7 @@ __global__ void __launch_bounds__(kEvalThreads, 2) eval_kernel(PlsEvalArgs a) {
       for (int t = threadIdx.x; t < nt; t += kEvalThreads) scv[t] = __fmul_rn(scv[t], inv);
       for (int j = threadIdx.x; j < p; j += kEvalThreads) w[j] = __fmul_rn(w[j], inv);
       __syncthreads();
-      for (int j = warp; j < p; j += kEvalWarps) {
-        const float v = warp_seq_dot(nt, [&](int k, float& x, float& y) {
-          x = Zs[static_cast<size_t>(tix[k]) * p + j];
-          y = scv[k];
-        }, lane);
-        if (lane == 0) ld[j] = v;
-      }
-      __syncthreads();
+      block_loading(Zs, p, tix, nt, scv, a.zexp + static_cast<size_t>(s) * p, ld, tiles, lane, warp);
     }
     for (int j = threadIdx.x; j < p; j += kEvalThreads) pw[j] = w[j];
     // Gram-Schmidt against the previous loadings
@@ -1128,9 +1268,9 @@ int pls_prepare(const PlsPrepArgs& a, cudaStream_t st) {
 
 int pls_build_gram(const PlsPrepArgs& a, const uint8_t* want, cudaStream_t st) {
   const int S = a.problems * a.F;
-  const int JB = (a.p + 31) / 32;
+  const int JB = (a.p + kGramT - 1) / kGramT;
   dim3 grid(S, JB * (JB + 1) / 2);
-  gram_kernel<<<grid, dim3(32, 32), 0, st>>>(a, want);
+  gram_kernel<<<grid, 256, 0, st>>>(a, want);
   count_launch();
   return static_cast<int>(cudaGetLastError());
 }

@@ -28,6 +28,7 @@ struct PlsPrepArgs {
   float* sdev;           // S x p
   float* Z;              // S x L x p standardised rows (all L rows, with the slice's statistics)
   float* xsum;           // S x p
+  int* zexp;             // S x p: largest biased exponent (at least 1) of each column over the training rows
   float* gram;           // S x p x p (only for build_gram)
   // predict mode: standardise NV extra rows per problem with the slice's statistics
   const float* Xv;       // R x NV x p, or nullptr
@@ -52,6 +53,7 @@ struct PlsEvalArgs {
   int tiles_after_s;     // 1: some slice computes training scores during the fit (no fold Gram)
   const float* Z;        // S x L x p
   const float* xsum;     // S x p
+  const int* zexp;       // S x p (PlsPrepArgs::zexp)
   const float* gram;     // S x p x p, or nullptr
   const uint8_t* use_gram;  // S (with gram != nullptr)
   const uint8_t* folds;  // R x L fold ids (CV), nullptr in predict mode
