@@ -552,41 +552,69 @@ struct PlsSlices {
   std::vector<uint8_t> folds8;
 };
 
+// Slices (r, f) of R problems of L rows: training rows = the rows outside
+// fold f (every row in predict mode), validation rows = fold f, both
+// ascending; fold ids are made dense per problem.  Sized by counting first
+// and filled in parallel over the problems (this runs while the device
+// works, and a serial push_back build of 500 slices took longer than that).
 PlsSlices pls_slices(const std::vector<std::vector<int>>& folds, int R, int L, bool predict) {
   PlsSlices sl;
-  std::vector<std::vector<int>> dense(static_cast<size_t>(R));
+  const int threads = host_threads(0);
+  std::vector<int> dense(predict ? 0 : static_cast<size_t>(R) * L);
   std::vector<int> nf(static_cast<size_t>(R), 1);
   if (!predict) {
-    sl.F = 0;
-    for (int r = 0; r < R; ++r) {
+    parallel_for(R, threads, [&](int r) {
       std::vector<int> ids = folds[r];
       std::sort(ids.begin(), ids.end());
       ids.erase(std::unique(ids.begin(), ids.end()), ids.end());
       nf[r] = static_cast<int>(ids.size());
-      sl.F = std::max(sl.F, nf[r]);
-      dense[r].resize(static_cast<size_t>(L));
+      int* dr = dense.data() + static_cast<size_t>(r) * L;
       for (int i = 0; i < L; ++i)
-        dense[r][i] = static_cast<int>(std::lower_bound(ids.begin(), ids.end(), folds[r][i]) - ids.begin());
-    }
+        dr[i] = static_cast<int>(std::lower_bound(ids.begin(), ids.end(), folds[r][i]) - ids.begin());
+    });
+    sl.F = 0;
+    for (int r = 0; r < R; ++r) sl.F = std::max(sl.F, nf[r]);
     if (sl.F > 255) fail(KGB_EINVAL, "at most 255 folds are supported");
     sl.folds8.resize(static_cast<size_t>(R) * L);
   }
-  sl.train_off.push_back(0);
-  sl.val_off.push_back(0);
-  for (int r = 0; r < R; ++r) {
-    for (int f = 0; f < sl.F; ++f) {
+  const int F = sl.F;
+  // validation counts per slice, then the offsets
+  std::vector<int> nval(static_cast<size_t>(R) * F, 0);
+  if (!predict)
+    parallel_for(R, threads, [&](int r) {
+      const int* dr = dense.data() + static_cast<size_t>(r) * L;
+      int* c = nval.data() + static_cast<size_t>(r) * F;
+      for (int i = 0; i < L; ++i) ++c[dr[i]];
+    });
+  const size_t S = static_cast<size_t>(R) * F;
+  sl.train_off.resize(S + 1);
+  sl.val_off.resize(S + 1);
+  sl.ntrain.resize(S);
+  sl.present.resize(S);
+  sl.train_off[0] = 0;
+  sl.val_off[0] = 0;
+  for (size_t q = 0; q < S; ++q) {
+    sl.ntrain[q] = L - nval[q];
+    sl.train_off[q + 1] = sl.train_off[q] + sl.ntrain[q];
+    sl.val_off[q + 1] = sl.val_off[q] + nval[q];
+    sl.present[q] = static_cast<int>(q % F) < nf[q / F] ? 1 : 0;
+  }
+  sl.train_idx.resize(static_cast<size_t>(sl.train_off[S]));
+  sl.val_idx.resize(static_cast<size_t>(sl.val_off[S]));
+  parallel_for(R, threads, [&](int r) {
+    const int* dr = predict ? nullptr : dense.data() + static_cast<size_t>(r) * L;
+    for (int f = 0; f < F; ++f) {
+      const size_t q = static_cast<size_t>(r) * F + f;
+      int* tr = sl.train_idx.data() + sl.train_off[q];
+      int* va = sl.val_idx.data() + sl.val_off[q];
       for (int i = 0; i < L; ++i) {
-        const bool val = !predict && dense[r][i] == f;
-        (val ? sl.val_idx : sl.train_idx).push_back(i);
+        if (dr != nullptr && dr[i] == f) *va++ = i;
+        else *tr++ = i;
       }
-      sl.train_off.push_back(static_cast<int>(sl.train_idx.size()));
-      sl.val_off.push_back(static_cast<int>(sl.val_idx.size()));
-      sl.ntrain.push_back(sl.train_off.back() - sl.train_off[sl.train_off.size() - 2]);
-      sl.present.push_back(f < nf[r] ? 1 : 0);
     }
     if (!predict)
-      for (int i = 0; i < L; ++i) sl.folds8[static_cast<size_t>(r) * L + i] = static_cast<uint8_t>(dense[r][i]);
-  }
+      for (int i = 0; i < L; ++i) sl.folds8[static_cast<size_t>(r) * L + i] = static_cast<uint8_t>(dr[i]);
+  });
   return sl;
 }
 
@@ -600,6 +628,29 @@ PlsSlices pad_slices(PlsSlices sl, int F) {
   }
   sl.F = std::max(sl.F, F);
   return sl;
+}
+
+// Host preparation that depends only on (seed, run, L): the fold plans and,
+// for the PLS classifier, the cross-validation slices over them.  Started on
+// host threads at the beginning of a call, so it overlaps the graph and the
+// k-means on the device.
+struct FoldWork {
+  std::vector<kgb::FoldPlan> plans;
+  PlsSlices slices;
+  bool has_slices = false;
+};
+
+FoldWork plan_fold_work(int M, int L, int F, uint64_t seed, int first_run, int nthreads, bool pls) {
+  FoldWork w;
+  w.plans.resize(static_cast<size_t>(M));
+  parallel_for(M, nthreads, [&](int r) { w.plans[r] = kgb::plan_folds(L, F, seed, first_run + r); });
+  if (pls) {
+    std::vector<std::vector<int>> fl(static_cast<size_t>(M));
+    for (int r = 0; r < M; ++r) fl[r].assign(w.plans[r].folds.begin(), w.plans[r].folds.end());
+    w.slices = pls_slices(fl, M, L, false);
+    w.has_slices = true;
+  }
+  return w;
 }
 
 struct PlsBuffers {
@@ -987,7 +1038,7 @@ struct MatrixTail {
 // work is done (no host wait on the plain path, so a batch can capture it).
 void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_gidx, float* d_gdist, int K,
                               const kgb_matrix_options* o, kgb_matrix_result* out, Clock& clk, int ev_start,
-                              int ev_graph, std::future<std::vector<kgb::FoldPlan>>& folds_future,
+                              int ev_graph, std::future<FoldWork>& folds_future,
                               MatrixTail& tail, const std::function<void()>& build_graph = {}) {
   const kgb_policy pol = policy_is_zero(o->policy) ? default_policy() : o->policy;
   int landmarks = o->landmarks > 0 ? o->landmarks : 10000;
@@ -1142,8 +1193,9 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     tc_kmeans_inputs(ctx, B, d_x, n, d, tc_split);
     ck_launch(kgb::kmeans_run(B, st), "landmark k-means");
   }
-  // folds were planned on the host while the device worked
-  std::vector<kgb::FoldPlan> fold_plans = folds_future.get();
+  // folds (and the PLS slices) were planned on the host while the device worked
+  FoldWork fold_work = folds_future.get();
+  std::vector<kgb::FoldPlan>& fold_plans = fold_work.plans;
   // label coding and the initial-label hashes on the device; with
   // semi-supervised inputs the start labels are built and coded on the host
   const uint64_t bc = kgb::unordered_bucket_count(static_cast<size_t>(L));
@@ -1172,6 +1224,7 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
       }
       semi_codes[r] = code_labels(lr, L, bc);
     });
+    if (!identity_groups) fold_work.has_slices = false;  // the folds follow the start labels
     for (const auto& c : semi_codes) C0max = std::max<int>(C0max, static_cast<int>(c.code2label.size()));
     ck(cudaMemcpyAsync(d_init_labels, init_host.data(), sizeof(int) * init_host.size(), cudaMemcpyHostToDevice, st),
        "H2D");
@@ -1303,9 +1356,15 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     const int p = d;
     float* d_xl = ctx.alloc<float>(static_cast<size_t>(M) * L * p);
     ck_launch(kgb::pls_gather_rows(d_x, p, d_land, static_cast<size_t>(M) * L, d_xl, st), "landmark rows");
-    std::vector<std::vector<int>> fl(static_cast<size_t>(M));
-    for (int r = 0; r < M; ++r) fl[r].assign(fold_plans[r].folds.begin(), fold_plans[r].folds.end());
-    const PlsSlices sl = pls_slices(fl, M, L, false);
+    const bool planned = fold_work.has_slices && fold_work.slices.folds8.size() == static_cast<size_t>(M) * L;
+    PlsSlices sl;
+    if (planned) {
+      sl = std::move(fold_work.slices);
+    } else {
+      std::vector<std::vector<int>> fl(static_cast<size_t>(M));
+      for (int r = 0; r < M; ++r) fl[r].assign(fold_plans[r].folds.begin(), fold_plans[r].folds.end());
+      sl = pls_slices(fl, M, L, false);
+    }
     const int comps = o->components;
     PlsBuffers b = pls_buffers(ctx, d_xl, M, L, p, sl, C0max, comps, comps, true, true, nullptr, 0);
     ev_tables = ctx.mark();
@@ -1796,10 +1855,9 @@ std::unique_ptr<BatchGraph> build_batch(const kgb_matrix_problem* probs, int cou
         const int M = q.options.runs, F = q.options.folds;
         const int first_run = q.options.first_run > 0 ? q.options.first_run : 1;
         const uint64_t seed = q.options.seed;
-        std::future<std::vector<kgb::FoldPlan>> folds = std::async(std::launch::deferred, [=]() {
-          std::vector<kgb::FoldPlan> plans(static_cast<size_t>(M));
-          for (int r = 0; r < M; ++r) plans[r] = kgb::plan_folds(landmarks, F, seed, first_run + r);
-          return plans;
+        const bool pls_classifier = q.options.classifier == 1;
+        std::future<FoldWork> folds = std::async(std::launch::deferred, [=]() {
+          return plan_fold_work(M, landmarks, F, seed, first_run, 1, pls_classifier);
         });
         const float* d_x = g->d_x + bp.x_off;
         const int ev_start = ctx.mark();
@@ -1977,10 +2035,9 @@ void matrix_entry(const float* x, bool x_on_device, int n, int d, const int32_t*
   const int M = opt->runs, F = opt->folds, nthreads = host_threads(opt->host_threads);
   const int first_run = opt->first_run > 0 ? opt->first_run : 1;
   const uint64_t seed = opt->seed;
-  std::future<std::vector<kgb::FoldPlan>> folds_future = std::async(std::launch::async, [=]() {
-    std::vector<kgb::FoldPlan> plans(static_cast<size_t>(M));
-    parallel_for(M, nthreads, [&](int r) { plans[r] = kgb::plan_folds(landmarks, F, seed, first_run + r); });
-    return plans;
+  const bool pls_classifier = opt->classifier == 1;
+  std::future<FoldWork> folds_future = std::async(std::launch::async, [=]() {
+    return plan_fold_work(M, landmarks, F, seed, first_run, nthreads, pls_classifier);
   });
   const int ev_start = ctx.mark();
   const float* d_x = x_on_device ? x : ctx.upload(x, static_cast<size_t>(n) * d);
@@ -2371,10 +2428,9 @@ int kgb_kodama_matrix_graph(kgb_graph_handle* g, const kgb_matrix_options* opt, 
     const int first_run = o.first_run > 0 ? o.first_run : 1;
     const uint64_t seed = o.seed;
     const int landmarks = sz.landmarks;
-    std::future<std::vector<kgb::FoldPlan>> folds_future = std::async(std::launch::async, [=]() {
-      std::vector<kgb::FoldPlan> plans(static_cast<size_t>(M));
-      parallel_for(M, nthreads, [&](int r) { plans[r] = kgb::plan_folds(landmarks, F, seed, first_run + r); });
-      return plans;
+    const bool pls_classifier = o.classifier == 1;
+    std::future<FoldWork> folds_future = std::async(std::launch::async, [=]() {
+      return plan_fold_work(M, landmarks, F, seed, first_run, nthreads, pls_classifier);
     });
     const int ev_start = ctx.mark();
     int* d_gidx = g->d_idx;
