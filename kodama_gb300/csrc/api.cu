@@ -693,6 +693,13 @@ void pls_logprior_tables(const std::vector<int>& ntrain, std::vector<float>& tab
 
 // Statistics, standardised rows and evaluation scratch of a set of slices.
 // d_X: R x L x p rows; d_Xv: R x NV x p rows to predict (predict mode) or null.
+// Whether the label cross-product of an evaluation lives in shared memory.
+bool pls_s_in_smem(int p, int C0max, int requested, int max_components, bool tiles_after_s, bool few_slices) {
+  const size_t two_ctas = 110 * 1024;
+  const size_t bytes = kgb::pls_eval_smem(p, C0max, requested, max_components, true, tiles_after_s);
+  return bytes <= two_ctas || (few_slices && bytes <= 200 * 1024);
+}
+
 PlsBuffers pls_buffers(Ctx& ctx, const float* d_X, int R, int L, int p, const PlsSlices& sl, int C0max,
                        int max_components, int requested, bool center, bool scale, const float* d_Xv, int NV) {
   PlsBuffers b;
@@ -702,10 +709,10 @@ PlsBuffers pls_buffers(Ctx& ctx, const float* d_X, int R, int L, int p, const Pl
   b.present = sl.present;
   if (requested > kgb::kPlsMaxComponents || max_components > kgb::kPlsMaxComponents)
     fail(KGB_EINVAL, "at most 64 PLS components are supported by the CUDA PLS-LDA kernel");
-  // the cross-product in shared memory when two CTAs still fit on an SM for
-  // the Gram evaluations and one CTA for those that compute scores in the fit
-  const bool s_in_smem = kgb::pls_eval_smem(p, C0max, requested, max_components, true, false) <= 110 * 1024 &&
-                         kgb::pls_eval_smem(p, C0max, requested, max_components, true, true) <= 200 * 1024;
+  // the cross-product in shared memory when two CTAs still fit on an SM
+  // (evaluations that compute scores in the fit hold the score tiles beside
+  // it); with no more slices than SMs one CTA per SM costs nothing
+  const bool s_in_smem = pls_s_in_smem(p, C0max, requested, max_components, true, S <= ctx.sms());
   if (kgb::pls_eval_smem(p, C0max, requested, max_components, s_in_smem, true) > 200 * 1024)
     fail(KGB_EINVAL, "too many features, classes or components for the PLS-LDA kernel");
   cudaStream_t st = ctx.stream();
@@ -818,6 +825,10 @@ void pls_enable_gram(Ctx& ctx, PlsBuffers& b) {
   ck_launch(kgb::pls_build_gram(b.prep, d_want, ctx.stream()), "fold Gram");
   b.ev.gram = b.prep.gram;
   b.ev.tiles_after_s = std::all_of(want.begin(), want.end(), [](uint8_t v) { return v != 0; }) ? 0 : 1;
+  b.ev.s_in_smem = pls_s_in_smem(p, b.ev.C0max, b.ev.requested, b.ev.max_components, b.ev.tiles_after_s != 0,
+                                 S <= ctx.sms())
+                       ? 1
+                       : 0;
 }
 
 // Host class lists of coded labels: rows grouped by code, ascending within.

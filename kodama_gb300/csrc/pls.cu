@@ -341,6 +341,42 @@ __device__ bool warp_exact_dot(int n, Term term, int lane, float& out) {
   return round_check(acc, LSB, A, n, out);
 }
 
+// The reference's sequential double chains, acc = fma(x_k, y_k, acc) for k
+// ascending, by a whole warp.  A product of two floats is exact in double,
+// so fma(x, y, acc) is acc + x*y rounded once: the lanes form 32 products at a
+// time, every lane adds them in order (the same chain in every lane) and the
+// next 32 terms load meanwhile.  n can be a column over the training rows,
+// where one lane's loop would wait on every load.
+template <class Term>
+__device__ double warp_fma_chain(int n, Term term, int lane) {
+  double s = 0.0;
+  float x = 0.0f, y = 0.0f;
+  if (lane < n) term(lane, x, y);
+  for (int k0 = 0; k0 < n; k0 += 32) {
+    const double prod = __dmul_rn(static_cast<double>(x), static_cast<double>(y));
+    x = 0.0f;
+    y = 0.0f;
+    if (k0 + 32 + lane < n) term(k0 + 32 + lane, x, y);
+    const int cnt = min(32, n - k0);
+    for (int q = 0; q < cnt; ++q) s = __dadd_rn(s, __shfl_sync(kFull, prod, q));
+  }
+  return s;
+}
+
+// acc = 0.0; acc += double(x_k) for k ascending, the same way.
+template <class Term>
+__device__ double warp_add_chain(int n, Term term, int lane) {
+  double s = 0.0;
+  float x = lane < n ? term(lane) : 0.0f;
+  for (int k0 = 0; k0 < n; k0 += 32) {
+    const double v = static_cast<double>(x);
+    x = k0 + 32 + lane < n ? term(k0 + 32 + lane) : 0.0f;
+    const int cnt = min(32, n - k0);
+    for (int q = 0; q < cnt; ++q) s = __dadd_rn(s, __shfl_sync(kFull, v, q));
+  }
+  return s;
+}
+
 // Sequential double sum of n floats, S_seq (acc = 0.0; acc += double(x_k)
 // in order).  All terms are multiples of 2^emin (the smallest ulp); when the
 // sum of |x| stays below 2^(emin + 53), every partial sum is exact in double,
@@ -383,28 +419,14 @@ __device__ double warp_seq_sum_double(int n, Term term, int lane) {
     // |acc| < 2^53: exact in double; 2^emin is a normal double (emin >= -149)
     return __dmul_rn(__ll2double_rn(acc), __longlong_as_double(static_cast<long long>(emin + 1023) << 52));
   }
-  double out = 0.0;
-  if (lane == 0)
-    for (int k = 0; k < n; ++k) out = __dadd_rn(out, static_cast<double>(term(k)));
-  return __shfl_sync(kFull, out, 0);
+  return warp_add_chain(n, term, lane);
 }
 
 // dot_float / mat_vec_float / t_mat_vec_float element: float(S_seq).
 template <class Term>
 __device__ float warp_seq_dot(int n, Term term, int lane) {
   float out = 0.0f;
-  if (!warp_exact_dot(n, term, lane, out)) {
-    if (lane == 0) {
-      double acc = 0.0;
-      for (int k = 0; k < n; ++k) {
-        float x, y;
-        term(k, x, y);
-        acc = fma(static_cast<double>(x), static_cast<double>(y), acc);
-      }
-      out = __double2float_rn(acc);
-    }
-    out = __shfl_sync(kFull, out, 0);
-  }
+  if (!warp_exact_dot(n, term, lane, out)) out = __double2float_rn(warp_fma_chain(n, term, lane));
   return out;
 }
 
@@ -422,12 +444,7 @@ __device__ float warp_power_norm(const float* v, int n, int lane) {
     y = v[k];
   };
   if (warp_exact_dot(n, t, lane, out)) return __fsqrt_rn(out);
-  if (lane == 0) {
-    double acc = 0.0;
-    for (int k = 0; k < n; ++k) acc = fma(static_cast<double>(v[k]), static_cast<double>(v[k]), acc);
-    out = power_norm2(acc);
-  }
-  return __shfl_sync(kFull, out, 0);
+  return power_norm2(warp_fma_chain(n, t, lane));
 }
 
 // loading[j] = float(S_seq) of sum over training rows k (ascending) of
@@ -520,13 +537,12 @@ __device__ void block_loading(const float* __restrict__ Zs, int p, const int* __
     __syncthreads();
     const int nf = fcount;
     for (int f = warp; f < nf; f += kEvalWarps) {
-      if (lane == 0) {
-        const int jf = flist[f];
-        double s = 0.0;
-        for (int k = 0; k < nt; ++k)
-          s = fma(static_cast<double>(Zs[static_cast<size_t>(tix[k]) * p + jf]), static_cast<double>(sc[k]), s);
-        ld[jf] = __double2float_rn(s);
-      }
+      const int jf = flist[f];
+      const double s = warp_fma_chain(nt, [&](int k, float& x, float& y) {
+        x = Zs[static_cast<size_t>(tix[k]) * p + jf];
+        y = sc[k];
+      }, lane);
+      if (lane == 0) ld[jf] = __double2float_rn(s);
     }
     __syncthreads();
   }
