@@ -23,7 +23,8 @@ def _noisy(n, d, seed, flip=0.3):
 
 @pytest.mark.parametrize("n,d,stratified,maxc,fixc", [(300, 20, True, 5, 0), (500, 40, False, 5, 5),
                                                        (200, 300, False, 4, 4), (120, 10, True, 12, 0),
-                                                       (2000, 60, False, 8, 0)])
+                                                       (2000, 60, False, 8, 0), (300, 600, False, 4, 0),
+                                                       (240, 1100, True, 3, 0)])
 def test_plsldacv_matches_oracle(kg, orc, n, d, stratified, maxc, fixc):
     x, lab = _noisy(n, d, seed=n + d)
     kw = dict(folds=10, stratified=stratified, max_components=maxc, fixed_components=fixc, cv_seed=7)
@@ -59,7 +60,8 @@ def test_plsdacv_matches_oracle(kg, orc, n, d, stratified, maxc, fixc):
     assert np.array_equal(g.accuracy_by_components[:maxc], abc[:maxc])
 
 
-@pytest.mark.parametrize("n,nt,d,comp", [(400, 300, 30, 5), (150, 500, 200, 4), (1000, 1000, 50, 10)])
+@pytest.mark.parametrize("n,nt,d,comp", [(400, 300, 30, 5), (150, 500, 200, 4), (1000, 1000, 50, 10),
+                                         (200, 150, 700, 3)])
 def test_plsldapredict_matches_oracle(kg, orc, n, nt, d, comp):
     x, lab = _noisy(n + nt, d, seed=nt + d, flip=0.2)
     want = orc.plsldapredict(x[:n], lab[:n], x[n:], components=comp)
