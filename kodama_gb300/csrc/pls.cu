@@ -88,25 +88,27 @@ __global__ void stats_kernel(PlsPrepArgs a) {
 // subset_scale_float for every row of every slice (and, in predict mode, for
 // the rows to predict).
 __global__ void standardize_kernel(PlsPrepArgs a) {
-  const size_t per = static_cast<size_t>(a.L) * a.p;
-  const size_t total = static_cast<size_t>(a.problems) * a.F * per;
-  for (size_t e = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; e < total;
-       e += static_cast<size_t>(gridDim.x) * blockDim.x) {
-    const size_t s = e / per, rem = e - s * per;
-    const int j = static_cast<int>(rem % a.p);
-    const size_t r = s / a.F;
-    const float x = a.X[r * per + rem];
-    a.Z[e] = __fdiv_rn(__fsub_rn(x, a.mean[s * a.p + j]), a.sdev[s * a.p + j]);
+  // blockIdx.y strides over slices (problems in predict mode), blockIdx.x over
+  // rows, threads over columns: no index division per element
+  const int S = a.problems * a.F, p = a.p;
+  for (int s = blockIdx.y; s < S; s += gridDim.y) {
+    const float* X = a.X + static_cast<size_t>(s / a.F) * a.L * p;
+    float* Z = a.Z + static_cast<size_t>(s) * a.L * p;
+    const float* mu = a.mean + static_cast<size_t>(s) * p;
+    const float* sd = a.sdev + static_cast<size_t>(s) * p;
+    for (int i = blockIdx.x; i < a.L; i += gridDim.x)
+      for (int j = threadIdx.x; j < p; j += blockDim.x)
+        Z[static_cast<size_t>(i) * p + j] = __fdiv_rn(__fsub_rn(X[static_cast<size_t>(i) * p + j], mu[j]), sd[j]);
   }
   if (a.Xv == nullptr) return;
-  const size_t pv = static_cast<size_t>(a.NV) * a.p;
-  const size_t tv = static_cast<size_t>(a.problems) * pv;
-  for (size_t e = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; e < tv;
-       e += static_cast<size_t>(gridDim.x) * blockDim.x) {
-    const size_t r = e / pv;
-    const int j = static_cast<int>((e - r * pv) % a.p);
-    const size_t s = r * a.F;
-    a.Zv[e] = __fdiv_rn(__fsub_rn(a.Xv[e], a.mean[s * a.p + j]), a.sdev[s * a.p + j]);
+  for (int r = blockIdx.y; r < a.problems; r += gridDim.y) {
+    const size_t s = static_cast<size_t>(r) * a.F;
+    const float* Xv = a.Xv + static_cast<size_t>(r) * a.NV * p;
+    float* Zv = a.Zv + static_cast<size_t>(r) * a.NV * p;
+    for (int i = blockIdx.x; i < a.NV; i += gridDim.x)
+      for (int j = threadIdx.x; j < p; j += blockDim.x)
+        Zv[static_cast<size_t>(i) * p + j] =
+            __fdiv_rn(__fsub_rn(Xv[static_cast<size_t>(i) * p + j], a.mean[s * p + j]), a.sdev[s * p + j]);
   }
 }
 
@@ -1273,7 +1275,11 @@ int pls_prepare(const PlsPrepArgs& a, cudaStream_t st) {
   count_launch();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return static_cast<int>(e);
-  standardize_kernel<<<4 * 152, 256, 0, st>>>(a);
+  {
+    const int ys = std::max(1, std::min(S, 65535));
+    const int xs = std::max(1, std::min(std::max(a.L, a.NV), std::max(1, 4096 / ys)));
+    standardize_kernel<<<dim3(xs, ys), a.p <= 128 ? 128 : 256, 0, st>>>(a);
+  }
   count_launch();
   e = cudaGetLastError();
   if (e != cudaSuccess) return static_cast<int>(e);
