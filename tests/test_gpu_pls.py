@@ -145,6 +145,22 @@ def test_pls_matrix_matches_oracle(kg, orc):
     assert np.array_equal(a.hashes, b.run_hashes)
 
 
+def test_pls_matrix_many_slices_matches_oracle(kg, orc):
+    # 16 runs x 10 folds = 160 slices (more than the SMs) and 150 initial
+    # clusters: the Gram-less first evaluation keeps the label cross-product
+    # in global memory, the Gram evaluations in shared memory
+    x, _ = datasets.low_rank(n=800, d=100, seed=5)
+    gi, gd = orc.exact_knn(x, 20, threads=8)
+    kw = dict(runs=16, cycles=4, landmarks=600, splitting=150, graph_neighbors=20, folds=10, knn_k=10,
+              components=4)
+    a = orc.kodama_matrix_graph_data(x, gi, gd, 0, seed=91, threads=8, materialize=1, classifier=1, **kw)
+    b = kg.KODAMA_matrix(x, graph=(gi, gd), index_base=0, seed=91, materialize_graph=True,
+                         classifier="pls", **kw)
+    for f in ("res", "acc", "v", "run_counters", "cycle_diag", "pls_counters"):
+        assert np.array_equal(getattr(a, f), getattr(b, f)), f
+    assert np.array_equal(a.hashes, b.run_hashes)
+
+
 @pytest.mark.parametrize("case", [c for c in G.cases() if c["kind"] == "kodama_matrix" and "input" in c],
                          ids=lambda c: c["name"])
 def test_gpu_pls_matrix_golden(kg, case):
