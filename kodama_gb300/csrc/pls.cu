@@ -177,7 +177,9 @@ __global__ void __launch_bounds__(256) gram_kernel(PlsPrepArgs a, const uint8_t*
       zk[q][c] = (row >= 0 && ck < a.p) ? Zs[static_cast<size_t>(row) * a.p + ck] : 0.0f;
     }
     __syncthreads();
-    const int cnt = min(kGramR, e - t0);
+    // rows of the tile past the last column hold no entry (warp-uniform: a
+    // warp is two values of ty)
+    const int cnt = jb * kGramT + ty * 4 < a.p ? min(kGramR, e - t0) : 0;
     for (int q = 0; q < cnt; ++q) {
       const float4 vj = *reinterpret_cast<const float4*>(&zj[q][ty * 4]);
       const float4 vk = *reinterpret_cast<const float4*>(&zk[q][tx * 4]);
