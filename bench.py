@@ -16,8 +16,10 @@ learned: the learned relabelling proposal (shipped weights) at the smallest
          cycle count reaching the plain run's mean final CV accuracy, timed
          the same way, with the Spearman correlation of its dissimilarities;
 cpu_baseline / --impl reference: the CPU restatement of the reference
-         algorithm (oracle/, all host threads) on a bounded sample of the same
-         workload, extrapolated to M=100 runs.
+         algorithm (oracle/, all host threads) on the whole workload, exact
+         graph and all M=100 runs, nothing extrapolated; its result is also
+         compared field by field with the timed GPU result
+         (parity_vs_oracle), outside the timed region.
 
 Launch: python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 (N>1 under torchrun: every rank runs its own replica; weak scaling).
@@ -41,12 +43,10 @@ sys.path.insert(0, HERE)
 METRIC = "KODAMA.matrix wall-s at N=20k,d=50,M=100: learned vs plain GPU at equal CV acc"
 WORKLOAD = dict(n=20000, d=50, runs=100, cycles=100, graph_neighbors=30, knn_k=30, folds=10,
                 splitting=50, landmarks=10000, seed=1234)
-CPU_SAMPLE_RUNS = 16
 # --workload pls: the PLS-LDA configuration (CorePLSLDA inside KODAMA.matrix)
 PLS_METRIC = "KODAMA.matrix PLS-LDA wall-s at N=10k,d=200,ncomp=5,F=10,M=50,Tcycle=50"
 PLS_WORKLOAD = dict(n=10000, d=200, runs=50, cycles=50, graph_neighbors=30, knn_k=30, folds=10,
                     splitting=0, landmarks=10000, seed=1234, components=5)
-PLS_CPU_SAMPLE_RUNS = 16
 # --workload batch: 256 independent KODAMA.matrix problems of uneven size
 # (datasets.uneven_batch: N log-uniform in [500, 20000], d in {10, 50, 100},
 # Gaussian mixtures of 3-20 clusters, half kNN k=10, half PLS-LDA ncomp=5),
@@ -174,39 +174,36 @@ class ClockSampler:
 
 
 def cpu_baseline(x, threads=None):
-    """The CPU restatement on a bounded sample: exact graph + atlas + 16 runs,
-    extrapolated to M=100 runs (runs are independent)."""
+    """The CPU restatement of the whole workload on all host threads: the
+    exact graph, then the full KODAMA.matrix call (all M runs), timed with
+    nothing extrapolated.  Returns (baseline dict, the restatement's result),
+    the result serving as the parity check of the GPU run."""
     from oracle import oracle
     if not oracle.available():
         oracle.build()
     threads = threads or os.cpu_count() or 1
-    n = x.shape[0]
-    graph_note = f"exact graph (N={n})"
-    if n > 30000:
-        # the exact graph of a 20000-row sample, scaled by (n / 20000)^2; the
-        # runs take the same exact graph from the device search
-        import kodama_gb300 as kg
-        t0 = time.perf_counter()
-        oracle.exact_knn(np.ascontiguousarray(x[:20000]), WORKLOAD["graph_neighbors"], threads=threads)
-        t_graph = (time.perf_counter() - t0) * (n / 20000.0) ** 2
-        gi, gd = kg.knn_graph(x, WORKLOAD["graph_neighbors"])
-        graph_note = f"exact graph of 20000 rows scaled x{(n / 20000.0) ** 2:g}"
-    else:
-        t0 = time.perf_counter()
-        gi, gd = oracle.exact_knn(x, WORKLOAD["graph_neighbors"], threads=threads)
-        t_graph = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    gi, gd = oracle.exact_knn(x, WORKLOAD["graph_neighbors"], threads=threads)
+    t_graph = time.perf_counter() - t0
     kw = _matrix_kw()
-    kw["runs"] = CPU_SAMPLE_RUNS
     t1 = time.perf_counter()
     r = oracle.kodama_matrix_graph_data(x, gi, gd, 0, seed=kw.pop("seed"), threads=threads, materialize=0, **kw)
     t_matrix = time.perf_counter() - t1
-    t_atlas, t_runs = float(r.timings[4]), float(r.timings[2])
-    total = t_graph + t_atlas + t_runs * (WORKLOAD["runs"] / CPU_SAMPLE_RUNS) + max(0.0, t_matrix - t_atlas - t_runs)
-    return {"value": round(total, 4), "unit": "s", "cores": threads, "kind": "port",
-            "sample": f"{graph_note} + atlas + {CPU_SAMPLE_RUNS} of 100 runs timed "
-                      f"({t_graph + t_matrix:.2f} s), runs scaled x{WORKLOAD['runs'] / CPU_SAMPLE_RUNS:g}",
-            "stages_s": {"graph": round(t_graph, 3), "atlas": round(t_atlas, 3),
-                         "runs_sample": round(t_runs, 3)}}
+    total = t_graph + t_matrix
+    return ({"value": round(total, 4), "unit": "s", "cores": threads, "kind": "port",
+             "sample": f"the whole workload: exact graph (N={x.shape[0]}) + KODAMA.matrix with all "
+                       f"{WORKLOAD['runs']} runs, nothing extrapolated",
+             "stages_s": {"graph": round(t_graph, 3), "atlas": round(float(r.timings[4]), 3),
+                          "runs": round(float(r.timings[2]), 3)}}, r)
+
+
+def _parity(gpu_res, gpu_acc, gpu_v, gpu_hashes, gpu_counters, ref):
+    """Field-by-field bit equality of a GPU KODAMA.matrix result with the CPU
+    restatement's on the same workload."""
+    checks = {"res": np.array_equal(gpu_res, ref.res), "acc": np.array_equal(gpu_acc, ref.acc),
+              "v": np.array_equal(gpu_v, ref.v), "run_hashes": np.array_equal(gpu_hashes, ref.hashes),
+              "run_counters": np.array_equal(gpu_counters, ref.run_counters)}
+    return {"bit_exact": all(checks.values()), "fields": checks}
 
 
 def _pls_data():
@@ -234,8 +231,9 @@ def _pls_config(extra=None):
 
 
 def pls_cpu_baseline(x, threads=None):
-    """The CPU restatement of the PLS-LDA path on a bounded sample: exact graph,
-    atlas and PLS_CPU_SAMPLE_RUNS runs (one per thread), scaled to M=50."""
+    """The CPU restatement of the whole PLS-LDA workload on all host threads:
+    exact graph plus the full KODAMA.matrix call (all M runs), nothing
+    extrapolated.  Returns (baseline dict, the restatement's result)."""
     from oracle import oracle
     if not oracle.available():
         oracle.build()
@@ -245,23 +243,17 @@ def pls_cpu_baseline(x, threads=None):
     gi, gd = oracle.exact_knn(x, w["graph_neighbors"], threads=threads)
     t_graph = time.perf_counter() - t0
     kw = _pls_kw()
-    kw["runs"] = PLS_CPU_SAMPLE_RUNS
     seed = kw.pop("seed")
     t1 = time.perf_counter()
     r = oracle.kodama_matrix_graph_data(x, gi, gd, 0, seed=seed, threads=threads, materialize=0,
                                         classifier=1, **kw)
     t_matrix = time.perf_counter() - t1
-    t_atlas, t_runs = float(r.timings[4]), float(r.timings[2])
-    # runs are independent; with `threads` workers the sample wall time covers
-    # ceil(sample / threads) waves of runs
-    waves_sample = -(-PLS_CPU_SAMPLE_RUNS // threads)
-    waves_full = -(-w["runs"] // threads)
-    total = t_graph + t_atlas + t_runs * (waves_full / waves_sample) + max(0.0, t_matrix - t_atlas - t_runs)
-    return {"value": round(total, 4), "unit": "s", "cores": threads, "kind": "port",
-            "sample": f"exact graph + atlas + {PLS_CPU_SAMPLE_RUNS} of {w['runs']} runs timed "
-                      f"({t_graph + t_matrix:.2f} s), run waves scaled x{waves_full / waves_sample:g}",
-            "stages_s": {"graph": round(t_graph, 3), "atlas": round(t_atlas, 3), "runs_sample": round(t_runs, 3)},
-            "mean_final_cv_acc_sample": round(float(np.mean(r.acc)), 6)}
+    return ({"value": round(t_graph + t_matrix, 4), "unit": "s", "cores": threads, "kind": "port",
+             "sample": f"the whole workload: exact graph + KODAMA.matrix PLS-LDA with all {w['runs']} runs, "
+                       "nothing extrapolated",
+             "stages_s": {"graph": round(t_graph, 3), "atlas": round(float(r.timings[4]), 3),
+                          "runs": round(float(r.timings[2]), 3)},
+             "mean_final_cv_acc": round(float(np.mean(r.acc)), 6)}, r)
 
 
 def run_gpu_pls(args):
@@ -327,8 +319,11 @@ def run_gpu_pls(args):
             "stage_ms": {k: round(v, 3) for k, v in r.kernel_ms.items()},
             "mean_final_cv_acc": round(float(np.mean(accs)), 6)}
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = pls_cpu_baseline(x)
+        line["cpu_baseline"], ref = pls_cpu_baseline(x)
+        line["parity_vs_oracle"] = _parity(res_dev.cpu().numpy(), r.acc, r.v, r.run_hashes, r.run_counters, ref)
     print(json.dumps(line))
+    if "parity_vs_oracle" in line and not line["parity_vs_oracle"]["bit_exact"]:
+        sys.exit("GPU result differs from the CPU restatement on the timed workload")
 
 
 def _batch_config(extra=None):
@@ -486,19 +481,22 @@ def run_reference(args):
                           "e2e": {"value": round(v, 3), "unit": "s", "h2d_bytes_per_step": 0,
                                   "d2h_bytes_per_step": 0}}))
         return
-    x = _data()
+    pls = args.workload == "pls"
+    x = _pls_data() if pls else _data()
+    base = pls_cpu_baseline if pls else cpu_baseline
     for _ in range(args.warmup):
-        cpu_baseline(x)
+        base(x)
     vals = []
     last = None
     for _ in range(args.steps):
-        last = cpu_baseline(x)
+        last, _ = base(x)
         vals.append(last["value"])
     v = float(np.mean(vals))
-    line = {"metric": METRIC, "value": round(v, 4), "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(v * 1000, 2), "higher_is_better": False,
-            "scaling": "weak", "vs_baseline": None, "dtype": "int32/f64", "data": "synthetic",
-            "config": _config(), "impl": "reference",
+    line = {"metric": PLS_METRIC if pls else METRIC, "value": round(v, 4), "unit": "s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(v * 1000, 2),
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32/f64" if pls else "int32/f64", "data": "synthetic",
+            "config": _pls_config() if pls else _config(), "impl": "reference",
             "cpu_baseline": dict(last, value=round(v, 4)),
             "e2e": {"value": round(v, 4), "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -610,6 +608,7 @@ def run_gpu(args):
     launches = (kg.launch_count() - launches0) // max(1, args.steps)
     value = float(np.mean(spans))
     stage_ms = {k: round(v, 3) for k, v in r.kernel_ms.items()}
+    timed_res = res_dev.cpu().numpy()   # the timed call's label matrix, for the parity check
 
     # end-to-end through the host-buffer C-ABI call
     e2e = []
@@ -661,8 +660,11 @@ def run_gpu(args):
         line["learned"] = learned_comparison(kg, x, x_dev, res_dev, local, kw, flush, float(np.mean(accs)), value,
                                              evo_s * 1000.0, args.steps)
     if world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(x)
+        line["cpu_baseline"], ref = cpu_baseline(x)
+        line["parity_vs_oracle"] = _parity(timed_res, r.acc, r.v, r.run_hashes, r.run_counters, ref)
     print(json.dumps(line))
+    if "parity_vs_oracle" in line and not line["parity_vs_oracle"]["bit_exact"]:
+        sys.exit("GPU result differs from the CPU restatement on the timed workload")
     if dist is not None:
         dist.destroy_process_group()
 

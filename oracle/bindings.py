@@ -400,6 +400,21 @@ def exact_knn(L, x, K, threads=1):
     return idx, dist
 
 
+def exact_knn_rows(L, x, K, rows, threads=1):
+    """exact_knn for the listed query rows only: (len(rows), K) results."""
+    x = np.ascontiguousarray(x, np.float32)
+    n, d = x.shape
+    rows = np.ascontiguousarray(rows, np.int32)
+    idx = np.zeros((len(rows), K), np.int32)
+    dist = np.zeros((len(rows), K), np.float32)
+    rc = L.exact_knn_rows(x.ctypes.data_as(ctypes.c_void_p), n, d, K, rows.ctypes.data_as(ctypes.c_void_p),
+                          len(rows), idx.ctypes.data_as(ctypes.c_void_p), dist.ctypes.data_as(ctypes.c_void_p),
+                          threads)
+    if rc != 0:
+        raise RuntimeError(_err(L))
+    return idx, dist
+
+
 def kmeans(L, x, k, rng_seed, discard=0, max_iter=10):
     x = np.ascontiguousarray(x, np.float32)
     n, p = x.shape

@@ -54,16 +54,30 @@ thread_local std::string g_error;
 // lane0+lane1+lane2+lane3, then the tail added sequentially.
 // ---------------------------------------------------------------------------
 float dot_x86_order(const float* a, const float* b, int n) {
-  float p[16] = {0};
+  // Four 4-lane accumulators (GCC generic vectors: SSE on x86-64, NEON on
+  // aarch64, no intrinsics); lane l of accumulator j holds p[4j + l].  With
+  // -ffp-contract=off the multiply and the add stay separately rounded.
+  typedef float v4f __attribute__((vector_size(16)));
+  v4f s0 = {0, 0, 0, 0}, s1 = s0, s2 = s0, s3 = s0;
   int i = 0;
   for (; i + 15 < n; i += 16) {
-    for (int l = 0; l < 16; ++l) {
-      const float prod = a[i + l] * b[i + l];
-      p[l] = p[l] + prod;
-    }
+    v4f a0, a1, a2, a3, b0, b1, b2, b3;
+    std::memcpy(&a0, a + i, 16);
+    std::memcpy(&a1, a + i + 4, 16);
+    std::memcpy(&a2, a + i + 8, 16);
+    std::memcpy(&a3, a + i + 12, 16);
+    std::memcpy(&b0, b + i, 16);
+    std::memcpy(&b1, b + i + 4, 16);
+    std::memcpy(&b2, b + i + 8, 16);
+    std::memcpy(&b3, b + i + 12, 16);
+    const v4f m0 = a0 * b0, m1 = a1 * b1, m2 = a2 * b2, m3 = a3 * b3;
+    s0 = s0 + m0;
+    s1 = s1 + m1;
+    s2 = s2 + m2;
+    s3 = s3 + m3;
   }
-  float lane[4];
-  for (int l = 0; l < 4; ++l) lane[l] = (p[l] + p[4 + l]) + (p[8 + l] + p[12 + l]);
+  const v4f l01 = s0 + s1, l23 = s2 + s3;
+  const v4f lane = l01 + l23;
   float sum = lane[0] + lane[1];
   sum = sum + lane[2];
   sum = sum + lane[3];
@@ -91,10 +105,15 @@ inline float sqdist_canonical(const float* a, const float* b, int d) {
   return acc;
 }
 
-void exact_knn(const float* x, int n, int d, int K, int* idx, float* dist, int threads) {
+// rows == nullptr: every row i writes output row i; else the nrows listed
+// query rows write output rows 0..nrows-1.
+void exact_knn(const float* x, int n, int d, int K, int* idx, float* dist, int threads,
+               const int* rows = nullptr, int nrows = 0) {
+  const int nq = rows ? nrows : n;
   auto work = [&](int t) {
     std::vector<std::pair<float, int>> row(static_cast<size_t>(n));
-    for (int i = t; i < n; i += threads) {
+    for (int q = t; q < nq; q += threads) {
+      const int i = rows ? rows[q] : q;
       int m = 0;
       for (int j = 0; j < n; ++j) {
         if (j == i) continue;
@@ -104,11 +123,11 @@ void exact_knn(const float* x, int n, int d, int K, int* idx, float* dist, int t
       std::partial_sort(row.begin(), row.begin() + take, row.begin() + m);
       for (int c = 0; c < K; ++c) {
         if (c < take) {
-          idx[static_cast<size_t>(i) * K + c] = row[c].second;
-          dist[static_cast<size_t>(i) * K + c] = std::sqrt(row[c].first);
+          idx[static_cast<size_t>(q) * K + c] = row[c].second;
+          dist[static_cast<size_t>(q) * K + c] = std::sqrt(row[c].first);
         } else {
-          idx[static_cast<size_t>(i) * K + c] = -1;
-          dist[static_cast<size_t>(i) * K + c] = std::numeric_limits<float>::infinity();
+          idx[static_cast<size_t>(q) * K + c] = -1;
+          dist[static_cast<size_t>(q) * K + c] = std::numeric_limits<float>::infinity();
         }
       }
     }
@@ -210,7 +229,8 @@ void split_empty_clusters(int rows, int dims, int k, std::vector<float>& sizes, 
 }
 
 // Returns labels 1..k for the n rows of x (row-major n x p).
-std::vector<int> kmeans_labels(const float* x, int n, int p, int k, std::mt19937_64& rng, int max_iter = 10) {
+std::vector<int> kmeans_labels(const float* x, int n, int p, int k, std::mt19937_64& rng, int max_iter = 10,
+                              int threads = 1) {
   k = std::max(1, std::min(k, n));
   const uint64_t kseed = rng() & 0x7fffffffULL;
   const std::vector<int> order = permutation_head(n, kseed + 1u, k);
@@ -219,10 +239,11 @@ std::vector<int> kmeans_labels(const float* x, int n, int p, int k, std::mt19937
   std::vector<int> assign(static_cast<size_t>(n), -1);
   std::vector<float> pnorm(static_cast<size_t>(n)), cnorm(static_cast<size_t>(k)), sizes(static_cast<size_t>(k));
   for (int r = 0; r < n; ++r) pnorm[r] = dot_x86_order(x + static_cast<size_t>(r) * p, x + static_cast<size_t>(r) * p, p);
-  auto assign_step = [&]() {
-    for (int c = 0; c < k; ++c) cnorm[c] = dot_x86_order(cent.data() + static_cast<size_t>(c) * p, cent.data() + static_cast<size_t>(c) * p, p);
+  // Rows are independent: with threads > 1 they are split into contiguous
+  // blocks, as the reference's OpenMP static schedule does (:735-758).
+  auto assign_rows = [&](int r0, int r1) {
     int changed = 0;
-    for (int r = 0; r < n; ++r) {
+    for (int r = r0; r < r1; ++r) {
       int best = 0;
       float bestd = std::numeric_limits<float>::infinity();
       const float* pt = x + static_cast<size_t>(r) * p;
@@ -241,6 +262,20 @@ std::vector<int> kmeans_labels(const float* x, int n, int p, int k, std::mt19937
       }
     }
     return changed;
+  };
+  auto assign_step = [&]() {
+    for (int c = 0; c < k; ++c) cnorm[c] = dot_x86_order(cent.data() + static_cast<size_t>(c) * p, cent.data() + static_cast<size_t>(c) * p, p);
+    const int nt = std::max(1, std::min(threads, n / 256));
+    if (nt == 1) return assign_rows(0, n);
+    std::atomic<int> changed{0};
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nt; ++t) {
+      const int r0 = static_cast<int>(static_cast<long long>(n) * t / nt);
+      const int r1 = static_cast<int>(static_cast<long long>(n) * (t + 1) / nt);
+      pool.emplace_back([&, r0, r1]() { changed.fetch_add(assign_rows(r0, r1)); });
+    }
+    for (auto& th : pool) th.join();
+    return changed.load();
   };
   for (int it = 0; it < std::max(1, max_iter); ++it) {
     const int changed = assign_step();
@@ -479,36 +514,78 @@ VoteTable build_vote_table(const int* gidx, const float* gdist, int samples, int
 // `uniq` is the label universe (sorted): the initial labels' distinct values,
 // rebuilt from the current labels only if one of them is unseen
 // (core.cpp:392-420 initialize_knn_label_map, :795-808).
-std::vector<int> vote_predict(const VoteTable& t, const std::vector<int>& labels, std::vector<int>& uniq, int folds_n) {
+// Buffers reused across the evaluations of one run (the reference keeps the
+// same kind of scratch, KNNPredictionScratch).  `lut` maps a label value v in
+// [lut_lo, lut_lo + lut.size()) to its code in `uniq` (-1: not in `uniq`).
+struct VoteScratch {
+  std::vector<int> lut, code, cnt, touched, all, fold_counts, fallback;
+  std::vector<double> ssum;
+  std::vector<char> empty, fold_present;
+  int lut_lo = 0;
+  bool lut_ok = false;
+};
+
+void vote_lookup(VoteScratch& s, const std::vector<int>& uniq) {
+  s.lut_ok = false;
+  if (uniq.empty()) return;
+  const long long span = static_cast<long long>(uniq.back()) - uniq.front() + 1;
+  if (span > (1LL << 22)) return;  // sparse label values: binary search instead
+  s.lut_lo = uniq.front();
+  s.lut.assign(static_cast<size_t>(span), -1);
+  for (size_t c = 0; c < uniq.size(); ++c) s.lut[static_cast<size_t>(uniq[c] - s.lut_lo)] = static_cast<int>(c);
+  s.lut_ok = true;
+}
+
+inline int vote_code(const VoteScratch& s, const std::vector<int>& uniq, int v) {
+  if (s.lut_ok) {
+    const long long o = static_cast<long long>(v) - s.lut_lo;
+    return o < 0 || o >= static_cast<long long>(s.lut.size()) ? -1 : s.lut[static_cast<size_t>(o)];
+  }
+  const auto it = std::lower_bound(uniq.begin(), uniq.end(), v);
+  return it == uniq.end() || *it != v ? -1 : static_cast<int>(it - uniq.begin());
+}
+
+std::vector<int> vote_predict(const VoteTable& t, const std::vector<int>& labels, std::vector<int>& uniq, int folds_n,
+                              VoteScratch& s) {
   const int n = t.samples;
   std::vector<int> pred(static_cast<size_t>(n), 0);
-  for (int l : labels) {
-    if (!std::binary_search(uniq.begin(), uniq.end(), l)) {
+  if (!s.lut_ok && s.lut.empty()) vote_lookup(s, uniq);
+  s.code.resize(static_cast<size_t>(n));
+  for (int i = 0; i < n; ++i) {
+    const int c = vote_code(s, uniq, labels[i]);
+    if (c < 0) {
+      // an unseen label: the universe is rebuilt from the current labels
       uniq = labels;
       std::sort(uniq.begin(), uniq.end());
       uniq.erase(std::unique(uniq.begin(), uniq.end()), uniq.end());
+      vote_lookup(s, uniq);
+      for (int j = 0; j < n; ++j) s.code[j] = vote_code(s, uniq, labels[j]);
       break;
     }
+    s.code[i] = c;
   }
-  std::vector<int> code(static_cast<size_t>(n));
-  for (int i = 0; i < n; ++i) code[i] = static_cast<int>(std::lower_bound(uniq.begin(), uniq.end(), labels[i]) - uniq.begin());
   const int C = static_cast<int>(uniq.size());
-  std::vector<int> cnt(static_cast<size_t>(C), 0);
-  std::vector<double> ssum(static_cast<size_t>(C), 0.0);
-  std::vector<int> touched;
-  std::vector<char> empty(static_cast<size_t>(n), 0);
+  s.cnt.assign(static_cast<size_t>(C), 0);
+  s.ssum.assign(static_cast<size_t>(C), 0.0);
+  s.empty.assign(static_cast<size_t>(n), 0);
+  const int* code = s.code.data();
+  int* cnt = s.cnt.data();
+  double* ssum = s.ssum.data();
+  std::vector<int>& touched = s.touched;
   for (int r = 0; r < n; ++r) {
     touched.clear();
+    const int* nbr = t.nb.data() + static_cast<size_t>(r) * t.width;
+    const float* sc = t.score.data() + static_cast<size_t>(r) * t.width;
     for (int j = 0; j < t.width; ++j) {
-      const int nb = t.nb[static_cast<size_t>(r) * t.width + j];
+      const int nb = nbr[j];
       if (nb < 0) continue;
       const int c = code[nb];
       if (cnt[c] == 0) touched.push_back(c);
       cnt[c]++;
-      ssum[c] += static_cast<double>(t.score[static_cast<size_t>(r) * t.width + j]);
+      ssum[c] += static_cast<double>(sc[j]);
     }
     if (touched.empty()) {
-      empty[r] = 1;
+      s.empty[r] = 1;
       continue;
     }
     int bl = 0, bc = -1;
@@ -526,26 +603,28 @@ std::vector<int> vote_predict(const VoteTable& t, const std::vector<int>& labels
     pred[r] = bl;
   }
   // training-fold majority for rows without any out-of-fold neighbour
-  std::vector<int> all(static_cast<size_t>(C), 0);
-  for (int i = 0; i < n; ++i) all[code[i]]++;
-  std::vector<std::vector<int>> fold_counts(static_cast<size_t>(folds_n), std::vector<int>(static_cast<size_t>(C), 0));
-  for (int i = 0; i < n; ++i) fold_counts[t.folds[i]][code[i]]++;
-  std::vector<int> fallback(static_cast<size_t>(folds_n), 0);
-  std::vector<char> fold_present(static_cast<size_t>(folds_n), 0);
-  for (int i = 0; i < n; ++i) fold_present[t.folds[i]] = 1;
+  s.all.assign(static_cast<size_t>(C), 0);
+  s.fold_counts.assign(static_cast<size_t>(folds_n) * C, 0);
+  s.fold_present.assign(static_cast<size_t>(folds_n), 0);
+  s.fallback.assign(static_cast<size_t>(folds_n), 0);
+  for (int i = 0; i < n; ++i) {
+    s.all[code[i]]++;
+    s.fold_counts[static_cast<size_t>(t.folds[i]) * C + code[i]]++;
+    s.fold_present[t.folds[i]] = 1;
+  }
   for (int f = 0; f < folds_n; ++f) {
-    if (!fold_present[f]) continue;
+    if (!s.fold_present[f]) continue;
     int bl = C ? uniq[0] : 0, bc = -1;
     for (int c = 0; c < C; ++c) {
-      const int count = all[c] - fold_counts[f][c];
+      const int count = s.all[c] - s.fold_counts[static_cast<size_t>(f) * C + c];
       if (count > bc || (count == bc && uniq[c] < bl)) {
         bl = uniq[c];
         bc = count;
       }
     }
-    fallback[f] = bl;
+    s.fallback[f] = bl;
   }
-  for (int r = 0; r < n; ++r) if (empty[r]) pred[r] = fallback[t.folds[r]];
+  for (int r = 0; r < n; ++r) if (s.empty[r]) pred[r] = s.fallback[t.folds[r]];
   return pred;
 }
 
@@ -685,8 +764,8 @@ bool coarsening(std::vector<int>& labels, const std::vector<int>& prev, const st
 
 // Many-to-one absorption (core.cpp:980-993 build_class_transition_stats,
 // :1110-1226 propose_many_to_one_absorption).
-bool absorption(std::vector<int>& labels, const std::vector<int>& prev, const std::vector<int>& fixed,
-                std::mt19937_64& rng) {
+bool absorption_map(std::vector<int>& labels, const std::vector<int>& prev, const std::vector<int>& fixed,
+                    std::mt19937_64& rng) {
   std::map<int, int> sizes, movable;
   std::map<int, std::map<int, int>> trans;
   for (size_t i = 0; i < labels.size(); ++i) {
@@ -765,6 +844,145 @@ bool absorption(std::vector<int>& labels, const std::vector<int>& prev, const st
   return true;
 }
 
+// The same proposal over dense codes: label and prediction values are ranked
+// in ascending order, which is the order the std::map statistics iterate in,
+// so every comparison, every sum and the one discrete draw are the map form's.
+// Falls back to absorption_map for sparse values or many classes.
+bool absorption(std::vector<int>& labels, const std::vector<int>& prev, const std::vector<int>& fixed,
+                std::mt19937_64& rng) {
+  const size_t n_rows = labels.size();
+  if (n_rows == 0) return false;
+  int lo = labels[0], hi = labels[0];
+  for (size_t i = 0; i < n_rows; ++i) {
+    lo = std::min(lo, std::min(labels[i], prev[i]));
+    hi = std::max(hi, std::max(labels[i], prev[i]));
+  }
+  const long long span = static_cast<long long>(hi) - lo + 1;
+  if (span > (1LL << 20)) return absorption_map(labels, prev, fixed, rng);
+  thread_local std::vector<int> lut, vals, sizes, movable, trans, remap;
+  thread_local std::vector<char> seen;
+  lut.assign(static_cast<size_t>(span), -1);
+  for (size_t i = 0; i < n_rows; ++i) {
+    lut[static_cast<size_t>(labels[i] - lo)] = 0;
+    lut[static_cast<size_t>(prev[i] - lo)] = 0;
+  }
+  vals.clear();
+  for (long long v = 0; v < span; ++v)
+    if (lut[static_cast<size_t>(v)] == 0) {
+      lut[static_cast<size_t>(v)] = static_cast<int>(vals.size());
+      vals.push_back(static_cast<int>(v + lo));
+    }
+  const int C = static_cast<int>(vals.size());
+  if (C > 2048) return absorption_map(labels, prev, fixed, rng);
+  sizes.assign(static_cast<size_t>(C), 0);
+  movable.assign(static_cast<size_t>(C), 0);
+  trans.assign(static_cast<size_t>(C) * C, 0);
+  for (size_t i = 0; i < n_rows; ++i) {
+    const int a = lut[static_cast<size_t>(labels[i] - lo)];
+    const int b = lut[static_cast<size_t>(prev[i] - lo)];
+    ++sizes[a];
+    ++trans[static_cast<size_t>(a) * C + b];
+    if (fixed[i] != 1) ++movable[a];
+  }
+  int nc = 0;
+  for (int a = 0; a < C; ++a) nc += sizes[a] > 0;
+  if (nc <= 2) return false;
+  const double n = static_cast<double>(n_rows);
+  struct Src { int source; double surplus; };
+  struct Tgt { int target = 0; double weight = 0.0; std::vector<Src> sources; };
+  std::map<int, Tgt> by_target;
+  for (int a = 0; a < C; ++a) {
+    if (sizes[a] == 0 || movable[a] <= 0) continue;
+    const int src = vals[a], ssize = sizes[a];
+    const int* row = trans.data() + static_cast<size_t>(a) * C;
+    const int stay = row[a];
+    int bt = src, bcount = 0, bsize = ssize;
+    double bsur = 0.0;
+    for (int b = 0; b < C; ++b) {
+      if (row[b] == 0 || b == a || sizes[b] == 0) continue;
+      const double expected = static_cast<double>(ssize) * static_cast<double>(sizes[b]) / std::max(1.0, n);
+      const double sur = static_cast<double>(row[b]) - expected;
+      const int dv = vals[b];
+      if (sur > bsur || (sur == bsur && row[b] > bcount) ||
+          (sur == bsur && row[b] == bcount && sizes[b] > bsize) ||
+          (sur == bsur && row[b] == bcount && sizes[b] == bsize && dv < bt)) {
+        bt = dv;
+        bsize = sizes[b];
+        bcount = row[b];
+        bsur = sur;
+      }
+    }
+    if (bt == src || bsur <= 0.0 || bcount <= stay) continue;
+    Tgt& t = by_target[bt];
+    t.target = bt;
+    t.weight += bsur;
+    t.sources.push_back(Src{src, bsur});
+  }
+  if (by_target.empty()) return false;
+  std::vector<Tgt> multi, single;
+  for (auto& kv : by_target) {
+    std::sort(kv.second.sources.begin(), kv.second.sources.end(), [](const Src& x, const Src& y) {
+      if (x.surplus != y.surplus) return x.surplus > y.surplus;
+      return x.source < y.source;
+    });
+    (kv.second.sources.size() > 1 ? multi : single).push_back(std::move(kv.second));
+  }
+  std::vector<Tgt>& moves = multi.empty() ? single : multi;
+  if (moves.empty()) return false;
+  std::vector<double> w;
+  for (const Tgt& t : moves) w.push_back(std::max(t.weight, std::numeric_limits<double>::min()));
+  std::discrete_distribution<int> pick(w.begin(), w.end());
+  const Tgt& sel = moves[static_cast<size_t>(pick(rng))];
+  remap.assign(static_cast<size_t>(C), -1);
+  bool any = false;
+  for (const Src& x : sel.sources)
+    if (x.source != sel.target) {
+      remap[static_cast<size_t>(lut[static_cast<size_t>(x.source - lo)])] = lut[static_cast<size_t>(sel.target - lo)];
+      any = true;
+    }
+  if (!any) return false;
+  bool changed = false;
+  seen.assign(static_cast<size_t>(C), 0);
+  thread_local std::vector<int> prop;
+  prop.resize(n_rows);
+  for (size_t i = 0; i < n_rows; ++i) {
+    int a = lut[static_cast<size_t>(labels[i] - lo)];
+    if (fixed[i] != 1 && remap[static_cast<size_t>(a)] >= 0) {
+      a = remap[static_cast<size_t>(a)];
+      changed = true;
+    }
+    prop[i] = a;
+    seen[static_cast<size_t>(a)] = 1;
+  }
+  if (!changed) return false;
+  int after = 0;
+  for (int a = 0; a < C; ++a) after += seen[a];
+  if (after <= 1 || after >= nc) return false;
+  for (size_t i = 0; i < n_rows; ++i) labels[i] = vals[static_cast<size_t>(prop[i])];
+  return true;
+}
+
+// Number of distinct values (a value-range bitmap; a sort for sparse values).
+int count_distinct(const std::vector<int>& v) {
+  if (v.empty()) return 0;
+  const auto mm = std::minmax_element(v.begin(), v.end());
+  const long long span = static_cast<long long>(*mm.second) - *mm.first + 1;
+  if (span > (1LL << 22)) {
+    std::vector<int> u = v;
+    std::sort(u.begin(), u.end());
+    return static_cast<int>(std::unique(u.begin(), u.end()) - u.begin());
+  }
+  thread_local std::vector<char> bits;
+  bits.assign(static_cast<size_t>(span), 0);
+  int d = 0;
+  for (int x : v) {
+    char& b = bits[static_cast<size_t>(x - *mm.first)];
+    d += b == 0;
+    b = 1;
+  }
+  return d;
+}
+
 int proposal_count(int G, int cycle, int cycles, bool adaptive, std::mt19937_64& rng) {
   if (G <= 1) return std::max(0, G);
   if (!adaptive || cycles <= 1) {
@@ -828,11 +1046,7 @@ CoreOut core_run(int samples, const std::vector<int>& init, const std::vector<in
     for (size_t i = 0; i < a.size(); ++i) ok += a[i] == b[i];
     return static_cast<double>(ok) / static_cast<double>(a.size());
   };
-  auto distinct = [](const std::vector<int>& v) {
-    std::vector<int> u = v;
-    std::sort(u.begin(), u.end());
-    return static_cast<int>(std::unique(u.begin(), u.end()) - u.begin());
-  };
+  auto distinct = [](const std::vector<int>& v) { return count_distinct(v); };
   std::mt19937_64 rng(o.seed);
   r.clbest = init;
   r.cvpredbest = predict(r.clbest);
@@ -980,8 +1194,9 @@ CoreOut core_knn_graph(const int* gidx, const float* gdist, int samples, int gk,
   std::vector<int> universe = init;
   std::sort(universe.begin(), universe.end());
   universe.erase(std::unique(universe.begin(), universe.end()), universe.end());
+  VoteScratch scratch;
   CoreOut r = core_run(samples, init, constrain, fixed_in, o, [&](const std::vector<int>& labels) {
-    return vote_predict(table, labels, universe, nfold);
+    return vote_predict(table, labels, universe, nfold, scratch);
   });
   r.folds = folds;
   return r;
@@ -1138,8 +1353,9 @@ CoreOut core_knn(const float* x, int n, int d, const std::vector<int>& init, con
   std::vector<int> universe = init;
   std::sort(universe.begin(), universe.end());
   universe.erase(std::unique(universe.begin(), universe.end()), universe.end());
+  VoteScratch scratch;
   CoreOut r = core_run(n, init, constrain, fixed_in, o, [&](const std::vector<int>& labels) {
-    return vote_predict(table, labels, universe, nfold);
+    return vote_predict(table, labels, universe, nfold, scratch);
   });
   r.folds = folds;
   return r;
@@ -1361,7 +1577,7 @@ void kodama_matrix(const float* x, int n, int d, const int* gidx_in, const float
   // shared landmark atlas (kodama_matrix.cpp:3662-3734)
   const int coarse_k = std::max(2, std::min(splitting, n));
   std::mt19937_64 shared_rng(seed + 1u);
-  const std::vector<int> shared = kmeans_labels(x, n, d, coarse_k, shared_rng, 10);
+  const std::vector<int> shared = kmeans_labels(x, n, d, coarse_k, shared_rng, 10, o.threads);
   const Strata strata = index_strata(shared, coarse_k);
   const double t_atlas = since(t0);
   const auto t1 = std::chrono::steady_clock::now();
@@ -1537,6 +1753,17 @@ int orc_last_error(char* buf, int len) {
 int orc_exact_knn(const float* x, int n, int d, int K, int* idx, float* dist, int threads) {
   try {
     orc::exact_knn(x, n, d, K, idx, dist, std::max(1, threads));
+    return 0;
+  } catch (const std::exception& e) {
+    orc::g_error = e.what();
+    return 1;
+  }
+}
+
+int orc_exact_knn_rows(const float* x, int n, int d, int K, const int* rows, int nrows, int* idx, float* dist,
+                       int threads) {
+  try {
+    orc::exact_knn(x, n, d, K, idx, dist, std::max(1, threads), rows, nrows);
     return 0;
   } catch (const std::exception& e) {
     orc::g_error = e.what();

@@ -62,15 +62,52 @@ Vec standardize(const float* x, int p, const std::vector<int>& rows, const Vec& 
 
 // densef_gram (plscv.cpp:436-447): lower triangle, float sums over samples.
 Vec gram_of(const Vec& z, int n, int p) {
+  // Each entry is its own float chain over the samples in order, as in
+  // densef_gram.  The samples are walked in chunks that stay in cache, and
+  // within a chunk blocks of 4 x 8 entries advance side by side; an entry's
+  // partial sum is carried from chunk to chunk, so its order is unchanged.
   Vec g(static_cast<size_t>(p) * p, 0.0f);
-  for (int row = 0; row < p; ++row) {
-    for (int col = 0; col <= row; ++col) {
-      float v = 0.0f;
-      for (int s = 0; s < n; ++s) v += z[static_cast<size_t>(s) * p + row] * z[static_cast<size_t>(s) * p + col];
-      g[static_cast<size_t>(row) * p + col] = v;
-      g[static_cast<size_t>(col) * p + row] = v;
+  constexpr int BR = 4, BC = 8, CHUNK = 256;
+  for (int s0 = 0; s0 < n; s0 += CHUNK) {
+    const int s1 = std::min(n, s0 + CHUNK);
+    for (int r0 = 0; r0 < p; r0 += BR) {
+      for (int c0 = 0; c0 < r0 + BR && c0 < p; c0 += BC) {
+        float acc[BR][BC];
+        for (int i = 0; i < BR; ++i)
+          for (int j = 0; j < BC; ++j) {
+            const int row = std::min(r0 + i, p - 1), col = std::min(c0 + j, p - 1);
+            acc[i][j] = g[static_cast<size_t>(row) * p + col];
+          }
+        if (r0 + BR <= p && c0 + BC <= p) {
+          for (int s = s0; s < s1; ++s) {
+            const float* zr = z.data() + static_cast<size_t>(s) * p;
+            for (int i = 0; i < BR; ++i) {
+              const float a = zr[r0 + i];
+              for (int j = 0; j < BC; ++j) {
+                const float prod = a * zr[c0 + j];
+                acc[i][j] = acc[i][j] + prod;
+              }
+            }
+          }
+        } else {
+          for (int s = s0; s < s1; ++s) {
+            const float* zr = z.data() + static_cast<size_t>(s) * p;
+            for (int i = 0; i < BR && r0 + i < p; ++i)
+              for (int j = 0; j < BC && c0 + j < p; ++j) {
+                const float prod = zr[r0 + i] * zr[c0 + j];
+                acc[i][j] = acc[i][j] + prod;
+              }
+          }
+        }
+        for (int i = 0; i < BR && r0 + i < p; ++i)
+          for (int j = 0; j < BC && c0 + j < p; ++j)
+            g[static_cast<size_t>(r0 + i) * p + c0 + j] = acc[i][j];
+      }
     }
   }
+  // mirror the lower triangle (row >= col), as densef_gram stores both halves
+  for (int row = 0; row < p; ++row)
+    for (int col = 0; col < row; ++col) g[static_cast<size_t>(col) * p + row] = g[static_cast<size_t>(row) * p + col];
   return g;
 }
 
@@ -283,12 +320,25 @@ std::vector<int> lda_streamed(const Vec& zt, int nt, const std::vector<int>& cod
   Vec cs(static_cast<size_t>(m) * nc, 0.0f), cp(static_cast<size_t>(nc) * nc, 0.0f), sr(static_cast<size_t>(nc));
   std::vector<int> counts(static_cast<size_t>(m), 0);
   for (int i = 0; i < nt; ++i) counts[code[i]]++;
+  // the weights padded to 8 lanes per feature (zeros past nc), so that the
+  // nc float chains of a score row run as unconditional vector lanes
+  const int nb = (nc + 7) / 8;
+  Vec wp(static_cast<size_t>(p) * nb * 8, 0.0f);
+  for (int j = 0; j < p; ++j)
+    for (int a = 0; a < nc; ++a) wp[(static_cast<size_t>(j) * nb + a / 8) * 8 + a % 8] = fit.w[static_cast<size_t>(j) * fit.rank + a];
   auto score_row = [&](const Vec& z, int i) {
-    std::fill(sr.begin(), sr.end(), 0.0f);
-    for (int j = 0; j < p; ++j) {
-      const float v = z[static_cast<size_t>(i) * p + j];
-      const float* wr = fit.w.data() + static_cast<size_t>(j) * fit.rank;
-      for (int a = 0; a < nc; ++a) sr[a] += v * wr[a];
+    const float* zr = z.data() + static_cast<size_t>(i) * p;
+    for (int b = 0; b < nb; ++b) {
+      float acc[8] = {};
+      for (int j = 0; j < p; ++j) {
+        const float v = zr[j];
+        const float* wr = wp.data() + (static_cast<size_t>(j) * nb + b) * 8;
+        for (int a = 0; a < 8; ++a) {
+          const float prod = v * wr[a];
+          acc[a] = acc[a] + prod;
+        }
+      }
+      for (int a = 0; a < 8 && b * 8 + a < nc; ++a) sr[b * 8 + a] = acc[a];
     }
   };
   for (int i = 0; i < nt; ++i) {
