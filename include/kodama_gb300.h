@@ -7,7 +7,7 @@
  * inst/include/kodama/kodama.hpp whose CUDA variants are only declared in the
  * reference tree (the kernels live outside it).  Each entry point below
  * replaces one of those declarations; a C++ `*_CUDA` definition marshals its
- * std::vector arguments into these plain pointers (see INTEGRATION.md).
+ * std::vector arguments into these plain pointers.
  *
  * Conventions
  *   - All pointers are HOST pointers; arrays are row-major, C-contiguous.
@@ -393,16 +393,18 @@ int kgb_dissimilarity_inplace(int32_t* gidx, float* gdist, int32_t samples, int3
 /* The same co-label proximity as kgb_dissimilarity_inplace, on DEVICE
  * pointers (gidx, gdist: samples x gk one-based graph, rewritten in place;
  * res: runs x samples labels) and on the caller's `stream` (a cudaStream_t;
- * NULL = the legacy default stream) of `device`; it returns after that work
- * has finished.  It allocates no device memory: for callers that cannot call
+ * NULL = the legacy default stream) of `device`.  Before it returns, the call
+ * synchronises that stream to read back its index-check flag, so the
+ * results are complete when it returns.  It allocates no device memory: for callers that cannot call
  * cudaMalloc/cudaFree, such as a process whose caching allocator already
  * holds the GPU, or a serving loop where cudaFree would stall the device.
  * Its scratch is a fixed 16 MiB array inside the library, so
  * samples * runs <= 4194240 and gk <= 2048; larger inputs return KGB_EINVAL
- * (use kgb_dissimilarity_inplace).  The first call on each device resolves
- * that array's address and may load the module; make it before any stream
- * capture.  Calls that overlap on one device share the scratch and race:
- * serialise them.  No counterpart in the reference. */
+ * (use kgb_dissimilarity_inplace).  Every call looks up that array's
+ * address on the device; the first call on a device may load the module
+ * there, so make it before any stream capture.  Calls that overlap on one
+ * device share the scratch and race: serialise them.  No counterpart in the
+ * reference. */
 int kgb_dissimilarity_inplace_device(int32_t* gidx, float* gdist, int32_t samples, int32_t gk,
                                      const int32_t* res, int32_t runs, int32_t device, void* stream);
 

@@ -250,17 +250,24 @@ __global__ void fnv_rows_kernel(const int* __restrict__ data, int rows, int n, u
   out[r] = h;
 }
 
+// 32 x 32 tiles; a CTA walks the run tiles blockIdx.y, blockIdx.y + gridDim.y,
+// ... so any number of runs fits the grid's y limit.
 __global__ void transpose_kernel(const int* __restrict__ res, int runs, int n, int* __restrict__ out) {
   __shared__ int tile[32][33];
-  const int r0 = blockIdx.y * 32, s0 = blockIdx.x * 32;
-  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
-    const int r = r0 + k, s = s0 + threadIdx.x;
-    if (r < runs && s < n) tile[k][threadIdx.x] = res[static_cast<size_t>(r) * n + s];
-  }
-  __syncthreads();
-  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
-    const int s = s0 + k, r = r0 + threadIdx.x;
-    if (r < runs && s < n) out[static_cast<size_t>(s) * runs + r] = tile[threadIdx.x][k];
+  const int s0 = blockIdx.x * 32;
+  const int run_tiles = (runs + 31) / 32;
+  for (int rt = blockIdx.y; rt < run_tiles; rt += gridDim.y) {
+    const int r0 = rt * 32;
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+      const int r = r0 + k, s = s0 + threadIdx.x;
+      if (r < runs && s < n) tile[k][threadIdx.x] = res[static_cast<size_t>(r) * n + s];
+    }
+    __syncthreads();
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+      const int s = s0 + k, r = r0 + threadIdx.x;
+      if (r < runs && s < n) out[static_cast<size_t>(s) * runs + r] = tile[threadIdx.x][k];
+    }
+    __syncthreads();
   }
 }
 
@@ -402,10 +409,15 @@ int fnv_rows(const int* data, int rows, int n, uint64_t* out, cudaStream_t st) {
 }
 
 int transpose_runs(const int* res, int runs, int n, int* out, cudaStream_t st) {
-  dim3 grid((n + 31) / 32, (runs + 31) / 32);
-  transpose_kernel<<<grid, dim3(32, 8), 0, st>>>(res, runs, n, out);
+  const int run_tiles = (runs + 31) / 32;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((n + 31) / 32, run_tiles < 65535 ? run_tiles : 65535);
+  cfg.blockDim = dim3(32, 8);
+  cfg.stream = st;
+  // the launch's own status (not an error left over from earlier work)
+  const cudaError_t e = cudaLaunchKernelEx(&cfg, transpose_kernel, res, runs, n, out);
   count_launch();
-  return static_cast<int>(cudaGetLastError());
+  return static_cast<int>(e);
 }
 
 int dissimilarity(const DissimArgs& a, cudaStream_t st) {

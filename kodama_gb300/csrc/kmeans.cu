@@ -13,6 +13,7 @@
 //   empty clusters split from a donor picked by a float Fenwick tree over
 //   max(0, size-1) with mt19937(1234) uniforms (:566-662).
 // Every product and sum uses explicit round-to-nearest intrinsics.
+#include "bf16_split.cuh"
 #include "kmeans.cuh"
 #include "knn.cuh"
 #include "launch_count.cuh"
@@ -289,11 +290,6 @@ __device__ __forceinline__ void mma_bf16_16816(float* c, const uint32_t* a, uint
       "{%0,%1,%2,%3};\n"
       : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b.x), "r"(b.y));
-}
-
-__device__ __forceinline__ int tc_row_words(int dp) {
-  const int half = dp / 2;
-  return (half % 16 == 8) ? half : half + 8;
 }
 
 // cent: the fp32 centroids staged too (else the exact recheck reads them from L2).
@@ -723,6 +719,383 @@ __global__ void finalize_kernel(KMeansBatch B) {
   B.changed[p] = 0;
 }
 
+// ---------------------------------------------------------------------------
+// Persistent batched k-means: one CTA per problem runs every Lloyd iteration
+// and the final assignment with block barriers only, so a batch of M
+// problems is one launch instead of 5 per iteration.  Same arithmetic as the
+// multi-launch path above (tensor-core candidate distances with the exact
+// x86-order recheck, centroid sums in ascending row order, the float Fenwick
+// split of empty clusters), hence the same labels bit for bit.
+//
+// Per iteration, in shared memory: the centroids (fp32 and their bf16 hi/lo
+// split in the mma B layout), their norms, each warp's 16-row distance tile,
+// the problem's assignments, per-warp cluster histograms.  The member lists
+// (rows grouped by cluster, ascending) go to global memory (L2).
+//   assignment: a warp takes 16-row tiles; mma.sync approximations into its
+//     tile; then two rows at a time, one per half-warp: the row's minimum
+//     and threshold, and for each candidate centroid (ascending) the exact
+//     x86-order dot, the 16 partial sums held by the 16 lanes (coalesced row
+//     loads), combined by shuffles in the reference's order;
+//   grouping: per-warp counts over contiguous row ranges, prefix sums, stable
+//     scatter of the row ids into the member lists;
+//   sums: a warp per (cluster, 64-column block), taken from a shared queue;
+//     lane j keeps the float chains of columns j and j + 32 down the member
+//     rows in ascending order, 8 rows' loads in flight;
+//   split: one thread, as finalize_kernel.
+// ---------------------------------------------------------------------------
+constexpr int kPkWarps = 16;
+constexpr int kPkThreads = 32 * kPkWarps;
+
+struct PkLayout {
+  size_t o_ch, o_cl, o_cf, o_cn, o_sa, o_as, o_wh, o_off, o_fs, o_misc, total;
+};
+
+__host__ __device__ inline size_t pk_align(size_t v) { return (v + 15) & ~static_cast<size_t>(15); }
+
+__host__ __device__ inline PkLayout pk_layout(int n, int k, int d, int dp) {
+  const int kpad = (k + 7) / 8 * 8, rw = tc_row_words(dp), d4 = (d + 3) & ~3;
+  PkLayout L{};
+  size_t o = 0;
+  L.o_ch = o; o = pk_align(o + sizeof(uint32_t) * kpad * rw);
+  L.o_cl = o; o = pk_align(o + sizeof(uint32_t) * kpad * rw);
+  L.o_cf = o; o = pk_align(o + sizeof(float) * static_cast<size_t>(k) * d4);
+  L.o_cn = o; o = pk_align(o + sizeof(float) * (kpad + 1));
+  L.o_sa = o; o = pk_align(o + sizeof(float) * kPkWarps * 16 * (kpad + 1));
+  L.o_as = o; o = pk_align(o + sizeof(int) * static_cast<size_t>(n));
+  L.o_wh = o; o = pk_align(o + sizeof(int) * kPkWarps * k);
+  L.o_off = o; o = pk_align(o + sizeof(int) * (k + 1));
+  L.o_fs = o; o = pk_align(o + sizeof(float) * (3 * k + 1));
+  L.o_misc = o; o = pk_align(o + sizeof(int) * 4);
+  L.total = o;
+  return L;
+}
+
+template <int KS>
+__global__ void __launch_bounds__(kPkThreads, 1) kmeans_persistent_kernel(KMeansBatch B) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int p = blockIdx.x;
+  const int k = B.k, d = B.d, dp = B.dp, n = B.n;
+  const int kpad = (k + 7) / 8 * 8, rw = tc_row_words(dp), d4 = (d + 3) & ~3, ksn = dp >> 4;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, tig = lane & 3;
+  const int half = lane >> 4, hl = lane & 15;
+  const PkLayout Ly = pk_layout(n, k, d, dp);
+  uint32_t* sch = reinterpret_cast<uint32_t*>(smraw + Ly.o_ch);
+  uint32_t* scl = reinterpret_cast<uint32_t*>(smraw + Ly.o_cl);
+  float* scf = reinterpret_cast<float*>(smraw + Ly.o_cf);     // [k][d4]
+  float* scn = reinterpret_cast<float*>(smraw + Ly.o_cn);     // [kpad] + max
+  float* sa = reinterpret_cast<float*>(smraw + Ly.o_sa) + warp * 16 * (kpad + 1);
+  int* sas = reinterpret_cast<int*>(smraw + Ly.o_as);         // [n] assignments
+  int* whist = reinterpret_cast<int*>(smraw + Ly.o_wh);       // [warps][k]
+  int* soff = reinterpret_cast<int*>(smraw + Ly.o_off);       // [k + 1]
+  float* fsize = reinterpret_cast<float*>(smraw + Ly.o_fs);   // [k], tree [k + 1], vals [k]
+  int* misc = reinterpret_cast<int*>(smraw + Ly.o_misc);      // changed, sums queue
+  const int* prow = B.rows + static_cast<size_t>(p) * n;
+  int* mem = B.members + static_cast<size_t>(p) * n;
+  const int nfull = d >> 4, tn = d - 16 * nfull;
+
+  // initial centroids: the problem's rows init_rows[0..k)
+  for (int i = tid; i < k * d4; i += kPkThreads) {
+    const int c = i / d4, j = i % d4;
+    const int grow = prow[B.init_rows[static_cast<size_t>(p) * k + c]];
+    scf[i] = j < d ? B.x[static_cast<size_t>(grow) * d + j] : 0.0f;
+  }
+  for (int i = tid; i < n; i += kPkThreads) sas[i] = -1;
+  const int iters = B.max_iter > 1 ? B.max_iter : 1;
+  for (int it = 0; it <= iters; ++it) {
+    const bool final_pass = it == iters;
+    if (tid == 0) misc[0] = 0;
+    __syncthreads();
+    // centroid norms and the bf16 split of the centroids
+    for (int c = tid; c < kpad; c += kPkThreads)
+      scn[c] = c < k ? dot_x86([&](int j) { return scf[c * d4 + j]; }, [&](int j) { return scf[c * d4 + j]; }, d)
+                     : 0.0f;
+    {
+      uint16_t* h16 = reinterpret_cast<uint16_t*>(sch);
+      uint16_t* l16 = reinterpret_cast<uint16_t*>(scl);
+      for (int e = tid; e < kpad * dp; e += kPkThreads) {
+        const int c = e / dp, j = e % dp;
+        const float v = (c < k && j < d) ? scf[c * d4 + j] : 0.0f;
+        const uint32_t hb = bf16_bits(v);
+        const uint32_t lb = bf16_bits(__fsub_rn(v, __uint_as_float(hb << 16)));
+        h16[c * 2 * rw + perm16(j)] = static_cast<uint16_t>(hb);
+        l16[c * 2 * rw + perm16(j)] = static_cast<uint16_t>(lb);
+      }
+    }
+    __syncthreads();
+    if (warp == 0) {
+      float mx = 0.0f;
+      for (int c = lane; c < k; c += 32) mx = fmaxf(mx, scn[c]);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(kFull, mx, o));
+      if (lane == 0) scn[kpad] = mx;
+    }
+    __syncthreads();
+
+    // ---- assignment ----
+    const int ntiles = (n + 15) / 16;
+    for (int tile = warp; tile < ntiles; tile += kPkWarps) {
+      const int r0 = tile * 16;
+      const int ga = prow[min(r0 + g, n - 1)], gb = prow[min(r0 + g + 8, n - 1)];
+      uint32_t ah[KS][4], al[KS][4];
+#pragma unroll
+      for (int ks = 0; ks < KS; ++ks) {
+        uint2 pa = make_uint2(0u, 0u), pb = pa, qa = pa, qb = pa;
+        if (ks < ksn) {
+          pa = *reinterpret_cast<const uint2*>(B.xh + static_cast<size_t>(ga) * dp + ks * 16 + 4 * tig);
+          pb = *reinterpret_cast<const uint2*>(B.xh + static_cast<size_t>(gb) * dp + ks * 16 + 4 * tig);
+          qa = *reinterpret_cast<const uint2*>(B.xl + static_cast<size_t>(ga) * dp + ks * 16 + 4 * tig);
+          qb = *reinterpret_cast<const uint2*>(B.xl + static_cast<size_t>(gb) * dp + ks * 16 + 4 * tig);
+        }
+        ah[ks][0] = pa.x; ah[ks][2] = pa.y; ah[ks][1] = pb.x; ah[ks][3] = pb.y;
+        al[ks][0] = qa.x; al[ks][2] = qa.y; al[ks][1] = qb.x; al[ks][3] = qb.y;
+      }
+      const float pna = B.pnorm[ga], pnb = B.pnorm[gb];
+      for (int nt0 = 0; nt0 < kpad / 8; nt0 += 8) {
+        float acc[8][4];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.0f;
+#pragma unroll
+        for (int ks = 0; ks < KS; ++ks) {
+          if (ks < ksn) {
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+              if (nt0 + t < kpad / 8) {
+                const int off = ((nt0 + t) * 8 + g) * rw + ks * 8 + 2 * tig;
+                const uint2 bh = *reinterpret_cast<const uint2*>(sch + off);
+                const uint2 bl = *reinterpret_cast<const uint2*>(scl + off);
+                mma_bf16_16816(acc[t], ah[ks], bh);
+                mma_bf16_16816(acc[t], ah[ks], bl);
+                mma_bf16_16816(acc[t], al[ks], bh);
+              }
+            }
+          }
+        }
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+          if (nt0 + t < kpad / 8) {
+            const int c = (nt0 + t) * 8 + 2 * tig;
+            sa[g * (kpad + 1) + c] = __fsub_rn(fadd(pna, scn[c]), fmul(2.0f, acc[t][0]));
+            sa[g * (kpad + 1) + c + 1] = __fsub_rn(fadd(pna, scn[c + 1]), fmul(2.0f, acc[t][1]));
+            sa[(g + 8) * (kpad + 1) + c] = __fsub_rn(fadd(pnb, scn[c]), fmul(2.0f, acc[t][2]));
+            sa[(g + 8) * (kpad + 1) + c + 1] = __fsub_rn(fadd(pnb, scn[c + 1]), fmul(2.0f, acc[t][3]));
+          }
+        }
+      }
+      __syncwarp();
+      // exact recheck, one row per half-warp
+      for (int rr = 0; rr < 8; ++rr) {
+        const int r = half * 8 + rr;
+        const int i = r0 + r;
+        const bool valid = i < n;
+        const int grow = prow[valid ? i : n - 1];
+        const float pn = B.pnorm[grow];
+        const float* arow = sa + r * (kpad + 1);
+        float amin = INFINITY;
+        for (int c = hl; c < k; c += 16) amin = fminf(amin, arow[c]);
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1) amin = fminf(amin, __shfl_xor_sync(kFull, amin, o));
+        const float thr = amin + 2.0f * fadd(pn, scn[kpad]) * B.tc_crel;
+        // the row: lane hl holds coordinates hl + 16 b (b < nfull) and the
+        // tail coordinate 16 nfull + hl
+        const float* xr = B.x + static_cast<size_t>(grow) * d;
+        float xv[KS];
+#pragma unroll
+        for (int b = 0; b < KS; ++b) xv[b] = b < nfull ? xr[hl + 16 * b] : 0.0f;
+        const float xt = hl < tn ? xr[16 * nfull + hl] : 0.0f;
+        int best = k;
+        float bestd = INFINITY;
+        // candidates in ascending cluster order: a half scans 16-cluster
+        // groups until it has candidates; the halves keep their own group
+        // positions but execute every ballot and shuffle together
+        const int groups = (k + 15) / 16;
+        int m = 0, mcur = 0;
+        unsigned bits = 0u;
+        for (;;) {
+          for (;;) {
+            const bool need = bits == 0u && m < groups;
+            if (!__any_sync(kFull, need)) break;
+            const int cq = hl + 16 * m;
+            const bool cand = need && cq < k && !(arow[cq] > thr);
+            const unsigned bal = __ballot_sync(kFull, cand);
+            if (need) {
+              bits = (bal >> (16 * half)) & 0xffffu;
+              mcur = m;
+              ++m;
+            }
+          }
+          const bool have = bits != 0u;
+          if (!__any_sync(kFull, have)) break;
+          const int c = have ? (__ffs(bits) - 1) + 16 * mcur : 0;
+          const float* cc = scf + c * d4;
+          float pp = 0.0f;
+#pragma unroll
+          for (int b = 0; b < KS; ++b)
+            if (b < nfull) pp = fadd(pp, fmul(xv[b], cc[hl + 16 * b]));
+          const int hb = half * 16;
+          const float q4 = __shfl_sync(kFull, pp, hb + ((hl + 4) & 15));
+          const float q8 = __shfl_sync(kFull, pp, hb + ((hl + 8) & 15));
+          const float q12 = __shfl_sync(kFull, pp, hb + ((hl + 12) & 15));
+          const float lv = fadd(fadd(pp, q4), fadd(q8, q12));
+          float sum = fadd(fadd(fadd(__shfl_sync(kFull, lv, hb), __shfl_sync(kFull, lv, hb + 1)),
+                                __shfl_sync(kFull, lv, hb + 2)),
+                           __shfl_sync(kFull, lv, hb + 3));
+          for (int t = 0; t < tn; ++t) sum = fadd(sum, fmul(__shfl_sync(kFull, xt, hb + t), cc[16 * nfull + t]));
+          if (have) {
+            const float dist = __fsub_rn(fadd(pn, scn[c]), fmul(2.0f, sum));
+            if (dist < bestd || (dist == bestd && c < best)) {
+              bestd = dist;
+              best = c;
+            }
+            bits &= bits - 1u;
+          }
+        }
+        if (best >= k) best = 0;
+        if (valid && hl == 0) {
+          if (final_pass) {
+            B.labels[static_cast<size_t>(p) * n + i] = best + 1;
+          } else if (sas[i] != best) {
+            sas[i] = best;
+            misc[0] = 1;
+          }
+        }
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+    if (final_pass) break;
+
+    // ---- grouping: member lists in ascending row order per cluster ----
+    for (int i = tid; i < kPkWarps * k; i += kPkThreads) whist[i] = 0;
+    __syncthreads();
+    const int per = (n + kPkWarps - 1) / kPkWarps;
+    const int beg = warp * per, end = min(n, beg + per);
+    for (int base = beg; base < end; base += 32) {
+      const int r = base + lane;
+      const int c = r < end ? sas[r] : -1;
+      const unsigned mm = __match_any_sync(kFull, c);
+      if (c >= 0 && (__ffs(mm) - 1) == lane) whist[warp * k + c] += __popc(mm);
+    }
+    __syncthreads();
+    for (int c = tid; c < k; c += kPkThreads) {
+      int run = 0;
+      for (int w = 0; w < kPkWarps; ++w) {
+        const int v = whist[w * k + c];
+        whist[w * k + c] = run;
+        run += v;
+      }
+      soff[c] = run;  // size for now
+    }
+    __syncthreads();
+    if (tid == 0) {
+      int run = 0;
+      for (int c = 0; c < k; ++c) {
+        const int sz = soff[c];
+        soff[c] = run;
+        run += sz;
+      }
+      soff[k] = run;
+      misc[1] = 0;
+    }
+    __syncthreads();
+    for (int i = tid; i < kPkWarps * k; i += kPkThreads) whist[i] += soff[i % k];
+    __syncthreads();
+    for (int base = beg; base < end; base += 32) {
+      const int r = base + lane;
+      const int c = r < end ? sas[r] : -1;
+      const unsigned mm = __match_any_sync(kFull, c);
+      if (c >= 0) mem[whist[warp * k + c] + __popc(mm & ((1u << lane) - 1u))] = prow[r];
+      __syncwarp();
+      if (c >= 0 && (__ffs(mm) - 1) == lane) whist[warp * k + c] += __popc(mm);
+      __syncwarp();
+    }
+    __syncthreads();
+
+    // ---- centroid sums in ascending row order ----
+    const int nblk = (d + 63) / 64;
+    for (;;) {
+      int item = 0;
+      if (lane == 0) item = atomicAdd(&misc[1], 1);
+      item = __shfl_sync(kFull, item, 0);
+      if (item >= k * nblk) break;
+      const int c = item / nblk, j0 = (item % nblk) * 64 + lane, j1 = j0 + 32;
+      const int b0 = soff[c], b1 = soff[c + 1];
+      const int cnt = b1 - b0;
+      float s0 = 0.0f, s1 = 0.0f;
+      for (int mb = b0; mb < b1; mb += 8) {
+        float v0[8], v1[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int id = mb + u < b1 ? mem[mb + u] : -1;
+          const float* xr = B.x + static_cast<size_t>(id < 0 ? 0 : id) * d;
+          v0[u] = (id >= 0 && j0 < d) ? xr[j0] : 0.0f;
+          v1[u] = (id >= 0 && j1 < d) ? xr[j1] : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          if (mb + u < b1) {
+            s0 = fadd(s0, v0[u]);
+            s1 = fadd(s1, v1[u]);
+          }
+        }
+      }
+      const float inv = cnt != 0 ? __fdiv_rn(1.0f, static_cast<float>(cnt)) : 0.0f;
+      if (j0 < d) scf[c * d4 + j0] = cnt != 0 ? fmul(s0, inv) : s0;
+      if (j1 < d) scf[c * d4 + j1] = cnt != 0 ? fmul(s1, inv) : s1;
+    }
+    __syncthreads();
+
+    // ---- empty-cluster split (finalize_kernel) ----
+    if (tid == 0) {
+      float* ftree = fsize + k;
+      float* fvals = ftree + k + 1;
+      bool any_empty = false;
+      for (int c = 0; c < k; ++c) {
+        fsize[c] = static_cast<float>(soff[c + 1] - soff[c]);
+        any_empty |= soff[c + 1] == soff[c];
+      }
+      if (any_empty && n > k) {
+        const float eps = 1.0f / 1024.0f;
+        Fenwick fw{ftree, fvals, k};
+        for (int i = 0; i <= k; ++i) ftree[i] = 0.0f;
+        for (int i = 0; i < k; ++i) fvals[i] = 0.0f;
+        for (int c = 0; c < k; ++c) fw.set(c, pos_part(__fsub_rn(fsize[c], 1.0f)));
+        int u = 0;  // the uniforms restart with every split, as in finalize_kernel
+        for (int e = 0; e < k; ++e) {
+          if (fsize[e] != 0.0f) continue;
+          const float total = fw.total();
+          int donor = -1;
+          if (total > 0.0f) donor = fw.select(fmul(B.split_uniform[u++], total));
+          if (donor < 0) {
+            donor = 0;
+            for (int c = 1; c < k; ++c) if (fsize[c] > fsize[donor]) donor = c;
+          }
+          float* ec = scf + e * d4;
+          float* dc = scf + donor * d4;
+          for (int j = 0; j < d; ++j) ec[j] = dc[j];
+          for (int j = 0; j < d; ++j) {
+            if ((j & 1) == 0) {
+              ec[j] = fmul(ec[j], fadd(1.0f, eps));
+              dc[j] = fmul(dc[j], __fsub_rn(1.0f, eps));
+            } else {
+              ec[j] = fmul(ec[j], __fsub_rn(1.0f, eps));
+              dc[j] = fmul(dc[j], fadd(1.0f, eps));
+            }
+          }
+          fsize[e] = __fdiv_rn(fsize[donor], 2.0f);
+          fsize[donor] = __fsub_rn(fsize[donor], fsize[e]);
+          fw.set(e, pos_part(__fsub_rn(fsize[e], 1.0f)));
+          fw.set(donor, pos_part(__fsub_rn(fsize[donor], 1.0f)));
+        }
+      }
+    }
+    __syncthreads();
+    // early exit: no assignment changed in this iteration (checked after the
+    // update, as the reference does); go to the final assignment
+    if (misc[0] == 0) it = iters - 1;
+    __syncthreads();
+  }
+}
+
 }  // namespace
 
 // Above 128 centroids the per-warp distance tiles hold the kernel to one
@@ -740,8 +1113,50 @@ int kmeans_row_norms(const float* x, int n, int d, float* out, cudaStream_t st) 
   return static_cast<int>(cudaGetLastError());
 }
 
+namespace {
+
+// |a - dist| <= (|x|^2 + max |c|^2) * crel: both share RN(|x|^2 + |c|^2);
+// 2 |dot_tc - dot_x86| <= 2 (3.1 * 2^-16 [the hi + lo split] +
+// 3 dp * 2^-22 [f32 accumulation of 3 dp products, two ulps per add] +
+// (d / 16 + 5) 2^-24 [the x86-order dot]) sum|x_i c_i|, with
+// sum|x_i c_i| <= 0.51 (|x|^2 + |c|^2); the two final subtractions round
+// values of at most 2.03 (|x|^2 + |c|^2) each
+float tc_error_factor(int d, int dp) {
+  const double tc = 3.1 * std::ldexp(1.0, -16) + 3.0 * dp * std::ldexp(1.0, -22) + (d / 16 + 5) * std::ldexp(1.0, -24);
+  return static_cast<float>(1.05 * (1.02 * tc + 4.1 * std::ldexp(1.0, -24)) + 1e-7);
+}
+
+// The persistent kernel applies: a batch of several problems given by row
+// lists, the tensor-core assignment with d <= 64, and its shared memory fits.
+bool persistent_supported(const KMeansBatch& B) {
+  if (B.problems < 2 || B.rows == nullptr || B.xh == nullptr || B.members == nullptr) return false;
+  if (!kmeans_tc_supported(B.d, B.k) || B.dp > 64 || B.n < 1) return false;
+  return pk_layout(B.n, B.k, B.d, B.dp).total <= kTcSmemLimit;
+}
+
+}  // namespace
+
 int kmeans_run(const KMeansBatch& B, cudaStream_t st) {
   if (B.problems <= 0) return 0;
+  if (persistent_supported(B)) {
+    KMeansBatch P = B;
+    P.tc_crel = tc_error_factor(B.d, B.dp);
+    const size_t bytes = pk_layout(B.n, B.k, B.d, B.dp).total;
+    cudaError_t e;
+    if (B.dp <= 16) {
+      e = cudaFuncSetAttribute(kmeans_persistent_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+      if (e == cudaSuccess) kmeans_persistent_kernel<1><<<B.problems, kPkThreads, bytes, st>>>(P);
+    } else if (B.dp <= 32) {
+      e = cudaFuncSetAttribute(kmeans_persistent_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+      if (e == cudaSuccess) kmeans_persistent_kernel<2><<<B.problems, kPkThreads, bytes, st>>>(P);
+    } else {
+      e = cudaFuncSetAttribute(kmeans_persistent_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+      if (e == cudaSuccess) kmeans_persistent_kernel<4><<<B.problems, kPkThreads, bytes, st>>>(P);
+    }
+    if (e != cudaSuccess) return static_cast<int>(e);
+    count_launch();
+    return static_cast<int>(cudaGetLastError());
+  }
   init_centroids_kernel<<<dim3(B.k, B.problems), 64, 0, st>>>(B);
   const size_t cs_bytes = sizeof(float) * (static_cast<size_t>(B.k) * ((B.d + 3) & ~3) + B.k);
   const size_t sort_bytes = kmeans_sort_smem(B.k);
@@ -768,15 +1183,7 @@ int kmeans_run(const KMeansBatch& B, cudaStream_t st) {
     const long long blocks = static_cast<long long>((B.n + 16 * kTcAssignWarps - 1) / (16 * kTcAssignWarps)) * B.problems;
     long long per = blocks / (2LL * sms);
     T.tc_blocks = static_cast<int>(per < 1 ? 1 : (per > 8 ? 8 : per));
-    // |a - dist| <= (|x|^2 + max |c|^2) * tc_crel: both share RN(|x|^2 + |c|^2);
-    // 2 |dot_tc - dot_x86| <= 2 (3.1 * 2^-16 [the hi + lo split] +
-    // 3 dp * 2^-22 [f32 accumulation of 3 dp products, two ulps per add] +
-    // (d / 16 + 5) 2^-24 [the x86-order dot]) sum|x_i c_i|, with
-    // sum|x_i c_i| <= 0.51 (|x|^2 + |c|^2); the two final subtractions round
-    // values of at most 2.03 (|x|^2 + |c|^2) each
-    const double tc = 3.1 * std::ldexp(1.0, -16) + 3.0 * B.dp * std::ldexp(1.0, -22) +
-                      (B.d / 16 + 5) * std::ldexp(1.0, -24);
-    T.tc_crel = static_cast<float>(1.05 * (1.02 * tc + 4.1 * std::ldexp(1.0, -24)) + 1e-7);
+    T.tc_crel = tc_error_factor(B.d, B.dp);
   }
   const int rows_per_cta = 16 * kTcAssignWarps * T.tc_blocks;
   const dim3 tgrid((B.n + rows_per_cta - 1) / rows_per_cta, B.problems);

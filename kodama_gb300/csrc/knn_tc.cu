@@ -37,6 +37,8 @@
 #include "knn.cuh"
 #include "launch_count.cuh"
 
+#include "bf16_split.cuh"
+
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -52,20 +54,6 @@ constexpr int kTcRegKs = 8;            // k-steps whose query fragments (hi and 
 constexpr int kTcMaxKs = 16;           // dp <= 256: above kTcRegKs the lo fragments come from shared memory
 constexpr size_t kTcSmemLimit = 227 * 1024;
 constexpr int kTileStride = kTcN + 8;  // floats per row of a warp's distance tile
-
-__device__ __forceinline__ uint32_t bf16_bits(float v) {
-  // round to the nearest bfloat16 (ties to even); inf / nan kept
-  const uint32_t u = __float_as_uint(v);
-  if ((u & 0x7f800000u) == 0x7f800000u) return u >> 16;
-  return (u + 0x7fffu + ((u >> 16) & 1u)) >> 16;
-}
-
-// Position of coordinate k inside its 16-block: the four values a lane feeds
-// to one m16n8k16 fragment (k = 2t, 2t+1, 2t+8, 2t+9) are contiguous at 4t.
-__device__ __forceinline__ int perm16(int k) {
-  const int kk = k & 15;
-  return (k & ~15) | (4 * ((kk & 7) >> 1) + ((kk & 1) | ((kk >> 3) << 1)));
-}
 
 __global__ void tc_prep_kernel(const float* __restrict__ x, int n, int d, int dp, uint16_t* __restrict__ xh,
                                uint16_t* __restrict__ xl, float* __restrict__ nrm, unsigned* __restrict__ nrm_max,

@@ -25,7 +25,6 @@
 
 #include <cmath>
 #include <cstdint>
-#include <mutex>
 #include <string>
 
 #include "graph_ops.cuh"
@@ -42,13 +41,10 @@ constexpr size_t kScratchBytes = size_t(16) << 20;
 constexpr size_t kHeaderBytes = 256;
 constexpr size_t kMaxLabelCells = (kScratchBytes - kHeaderBytes) / sizeof(int);
 constexpr int kMaxNeighbors = 2048;  // 8 warps x K x 8 bytes of shared memory <= 128 KB
-constexpr int kMaxDevices = 64;
 constexpr unsigned kFullMask = 0xffffffffu;
 
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
-std::mutex g_setup_mu;
-unsigned char* g_scratch_addr[kMaxDevices] = {};
 
 // Flags any stored index outside {negative (missing)} U [1, n].
 __global__ void check_one_based_kernel(const int* __restrict__ idx, size_t total, int n, int* bad) {
@@ -138,22 +134,16 @@ void ck(cudaError_t e, const char* what) {
   if (e != cudaSuccess) throw Fail{KGB_ECUDA, std::string(what) + ": " + cudaGetErrorString(e)};
 }
 
-// Device address of g_scratch on `device`, resolved on the first call for
-// that device with the device current.  Resolving may load the module onto
-// the device, which is why the first call per device must not happen while
-// a stream is being captured.
-unsigned char* scratch_on(int device) {
-  std::lock_guard<std::mutex> lock(g_setup_mu);
-  if (g_scratch_addr[device] != nullptr) return g_scratch_addr[device];
-  int prev = 0;
-  ck(cudaGetDevice(&prev), "cudaGetDevice");
-  ck(cudaSetDevice(device), "cudaSetDevice");
+// Device address of g_scratch on the current device.  It is looked up on
+// every call (cheap once the module is loaded), so a call after a
+// cudaDeviceReset, which reloads the module and may move the array, uses
+// the array's new address.  The first lookup on a device may load the
+// module onto it, which is why the first call per device must not happen
+// while a stream is being captured.
+unsigned char* scratch_here() {
   void* p = nullptr;
-  const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
-  cudaSetDevice(prev);
-  ck(e, "cudaGetSymbolAddress(scratch)");
-  g_scratch_addr[device] = static_cast<unsigned char*>(p);
-  return g_scratch_addr[device];
+  ck(cudaGetSymbolAddress(&p, g_scratch), "cudaGetSymbolAddress(scratch)");
+  return static_cast<unsigned char*>(p);
 }
 
 // Restores the caller's current device when the call ends.
@@ -185,11 +175,11 @@ void run(int32_t* gidx, float* gdist, int32_t samples, int32_t gk, const int32_t
   }
   int ndev = 0;
   ck(cudaGetDeviceCount(&ndev), "cudaGetDeviceCount");
-  if (device < 0 || device >= ndev || device >= kMaxDevices) {
+  if (device < 0 || device >= ndev) {
     throw Fail{KGB_EINVAL, "kgb_dissimilarity_inplace_device: no CUDA device " + std::to_string(device)};
   }
-  unsigned char* scratch = scratch_on(device);
   DeviceGuard guard(device);
+  unsigned char* scratch = scratch_here();
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   int* bad = reinterpret_cast<int*>(scratch);
   int* lbs = reinterpret_cast<int*>(scratch + kHeaderBytes);
@@ -197,10 +187,16 @@ void run(int32_t* gidx, float* gdist, int32_t samples, int32_t gk, const int32_t
 
   ck(cudaMemsetAsync(scratch, 0, kHeaderBytes, st), "clear scratch header");
   const size_t want = (total + 255) / 256;
-  const int blocks = static_cast<int>(want < 1024 ? want : 1024);
-  check_one_based_kernel<<<blocks, 256, 0, st>>>(gidx, total, samples, bad);
+  // each launch through cudaLaunchKernelEx, so its own status is checked and
+  // an error left on the thread by earlier, unrelated work is left alone
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(static_cast<unsigned>(want < 1024 ? want : 1024));
+  cfg.blockDim = dim3(256);
+  cfg.stream = st;
+  ck(cudaLaunchKernelEx(&cfg, check_one_based_kernel, static_cast<const int*>(gidx), total, static_cast<int>(samples),
+                        bad),
+     "check indices");
   kgb::count_launch();
-  ck(cudaGetLastError(), "check indices");
   ck(static_cast<cudaError_t>(kgb::transpose_runs(res, runs, samples, lbs, st)), "transpose");
   const int wpb = 8;
   const size_t smem = static_cast<size_t>(wpb) * gk * (sizeof(float) + sizeof(int));
@@ -209,10 +205,14 @@ void run(int32_t* gidx, float* gdist, int32_t samples, int32_t gk, const int32_t
                             static_cast<int>(smem)),
        "shared memory size");
   }
-  dissimilarity_inplace_kernel<<<(samples + wpb - 1) / wpb, wpb * 32, smem, st>>>(gidx, gdist, samples, gk, runs, lbs,
-                                                                                 bad);
+  cfg.gridDim = dim3(static_cast<unsigned>((samples + wpb - 1) / wpb));
+  cfg.blockDim = dim3(wpb * 32);
+  cfg.dynamicSmemBytes = smem;
+  ck(cudaLaunchKernelEx(&cfg, dissimilarity_inplace_kernel, static_cast<int*>(gidx), static_cast<float*>(gdist),
+                        static_cast<int>(samples), static_cast<int>(gk), static_cast<int>(runs),
+                        static_cast<const int*>(lbs), static_cast<const int*>(bad)),
+     "dissimilarity");
   kgb::count_launch();
-  ck(cudaGetLastError(), "dissimilarity");
   int h_bad = 0;
   ck(cudaMemcpyAsync(&h_bad, bad, sizeof(int), cudaMemcpyDeviceToHost, st), "read index check");
   ck(cudaStreamSynchronize(st), "synchronize");

@@ -1,7 +1,8 @@
-"""World-size-2 gloo test of the run sharding used for more than one GPU:
-the two ranks compute disjoint blocks of runs with the CPU restatement, the
-blocks are gathered and the proximity is applied to the full label matrix;
-the result must equal one process computing every run."""
+"""gloo tests of the run sharding used for more than one GPU: the ranks
+compute disjoint blocks of runs with the CPU restatement, the blocks are
+gathered (tensor all_gather) and the proximity is applied to the full label
+matrix; the result must equal one process computing every run.  World size 2
+with 6 runs, and world size 3 with 2 runs (one rank's block is empty)."""
 
 import os
 import socket
@@ -41,7 +42,7 @@ def _oracle_matrix(orc):
     return fn
 
 
-def _worker(rank, world, port, out_path):
+def _worker(rank, world, port, out_path, runs):
     sys.path.insert(0, ROOT)
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
     dist.init_process_group("gloo", rank=rank, world_size=world)
@@ -50,7 +51,7 @@ def _worker(rank, world, port, out_path):
     from oracle import oracle as orc
     x = datasets.spirals()[0].astype(np.float32)
     graph = orc.exact_knn(x, 50, threads=2)
-    r = kodama_matrix_sharded(x, runs=RUNS, graph=graph, matrix_fn=_oracle_matrix(orc),
+    r = kodama_matrix_sharded(x, runs=runs, graph=graph, matrix_fn=_oracle_matrix(orc),
                               dissimilarity_fn=lambda i, d, res: orc.dissimilarity(i, d, res), dist=dist, **KW)
     if rank == 0:
         np.savez(out_path, res=r.res, acc=r.acc, v=r.v, hashes=r.run_hashes, counters=r.run_counters,
@@ -59,14 +60,16 @@ def _worker(rank, world, port, out_path):
     dist.destroy_process_group()
 
 
-def test_sharded_runs_equal_single_process(orc, tmp_path):
+@pytest.mark.parametrize("world,runs", [(2, RUNS), (3, 2)])
+def test_sharded_runs_equal_single_process(orc, tmp_path, world, runs):
     out = str(tmp_path / "sharded.npz")
-    mp.start_processes(_worker, args=(2, _free_port(), out), nprocs=2, join=True, start_method="spawn")
+    mp.start_processes(_worker, args=(world, _free_port(), out, runs), nprocs=world, join=True,
+                       start_method="spawn")
     got = np.load(out)
     from kodama_gb300 import datasets
     x = datasets.spirals()[0].astype(np.float32)
     gi, gd = orc.exact_knn(x, 50, threads=2)
-    ref = orc.kodama_matrix_graph_data(x, gi, gd, 0, seed=SEED, runs=RUNS, threads=2, materialize=1, **KW)
+    ref = orc.kodama_matrix_graph_data(x, gi, gd, 0, seed=SEED, runs=runs, threads=2, materialize=1, **KW)
     assert np.array_equal(got["res"], ref.res)
     assert np.array_equal(got["acc"], ref.acc)
     assert np.array_equal(got["v"], ref.v)
