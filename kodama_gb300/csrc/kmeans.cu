@@ -728,14 +728,17 @@ __global__ void finalize_kernel(KMeansBatch B) {
 // split of empty clusters), hence the same labels bit for bit.
 //
 // Per iteration, in shared memory: the centroids (fp32 and their bf16 hi/lo
-// split in the mma B layout), their norms, each warp's 16-row distance tile,
-// the problem's assignments, per-warp cluster histograms.  The member lists
-// (rows grouped by cluster, ascending) go to global memory (L2).
-//   assignment: a warp takes 16-row tiles; mma.sync approximations into its
-//     tile; then two rows at a time, one per half-warp: the row's minimum
-//     and threshold, and for each candidate centroid (ascending) the exact
-//     x86-order dot, the 16 partial sums held by the 16 lanes (coalesced row
-//     loads), combined by shuffles in the reference's order;
+// split in the mma B layout), their norms, the problem's assignments,
+// per-warp cluster histograms.  The member lists (rows grouped by cluster,
+// ascending) go to global memory (L2).
+//   assignment: a warp takes 16-row tiles; the mma.sync approximations stay
+//     in the accumulator registers, where each quad of lanes finds its two
+//     rows' minima, thresholds and candidate masks (shuffles).  A row with
+//     finite approximations and a single candidate takes it; the other rows
+//     get, for each candidate centroid (ascending), the exact x86-order dot,
+//     its 16 partial sums held by 16 lanes (coalesced row loads) and combined
+//     by shuffles in the reference's order.  Up to 64 centroids one pass;
+//     up to 128 the approximations are computed twice (minima, then masks);
 //   grouping: per-warp counts over contiguous row ranges, prefix sums, stable
 //     scatter of the row ids into the member lists;
 //   sums: a warp per (cluster, 64-column block), taken from a shared queue;
@@ -747,7 +750,7 @@ constexpr int kPkWarps = 16;
 constexpr int kPkThreads = 32 * kPkWarps;
 
 struct PkLayout {
-  size_t o_ch, o_cl, o_cf, o_cn, o_sa, o_as, o_wh, o_off, o_fs, o_misc, total;
+  size_t o_ch, o_cl, o_cf, o_cn, o_as, o_wh, o_off, o_fs, o_misc, total;
 };
 
 __host__ __device__ inline size_t pk_align(size_t v) { return (v + 15) & ~static_cast<size_t>(15); }
@@ -760,7 +763,6 @@ __host__ __device__ inline PkLayout pk_layout(int n, int k, int d, int dp) {
   L.o_cl = o; o = pk_align(o + sizeof(uint32_t) * kpad * rw);
   L.o_cf = o; o = pk_align(o + sizeof(float) * static_cast<size_t>(k) * d4);
   L.o_cn = o; o = pk_align(o + sizeof(float) * (kpad + 1));
-  L.o_sa = o; o = pk_align(o + sizeof(float) * kPkWarps * 16 * (kpad + 1));
   L.o_as = o; o = pk_align(o + sizeof(int) * static_cast<size_t>(n));
   L.o_wh = o; o = pk_align(o + sizeof(int) * kPkWarps * k);
   L.o_off = o; o = pk_align(o + sizeof(int) * (k + 1));
@@ -770,7 +772,7 @@ __host__ __device__ inline PkLayout pk_layout(int n, int k, int d, int dp) {
   return L;
 }
 
-template <int KS>
+template <int KS, int NC>
 __global__ void __launch_bounds__(kPkThreads, 1) kmeans_persistent_kernel(KMeansBatch B) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int p = blockIdx.x;
@@ -783,7 +785,6 @@ __global__ void __launch_bounds__(kPkThreads, 1) kmeans_persistent_kernel(KMeans
   uint32_t* scl = reinterpret_cast<uint32_t*>(smraw + Ly.o_cl);
   float* scf = reinterpret_cast<float*>(smraw + Ly.o_cf);     // [k][d4]
   float* scn = reinterpret_cast<float*>(smraw + Ly.o_cn);     // [kpad] + max
-  float* sa = reinterpret_cast<float*>(smraw + Ly.o_sa) + warp * 16 * (kpad + 1);
   int* sas = reinterpret_cast<int*>(smraw + Ly.o_as);         // [n] assignments
   int* whist = reinterpret_cast<int*>(smraw + Ly.o_wh);       // [warps][k]
   int* soff = reinterpret_cast<int*>(smraw + Ly.o_off);       // [k + 1]
@@ -832,6 +833,7 @@ __global__ void __launch_bounds__(kPkThreads, 1) kmeans_persistent_kernel(KMeans
     __syncthreads();
 
     // ---- assignment ----
+    const float crel = B.tc_crel, cmax = scn[kpad];
     const int ntiles = (n + 15) / 16;
     for (int tile = warp; tile < ntiles; tile += kPkWarps) {
       const int r0 = tile * 16;
@@ -850,8 +852,10 @@ __global__ void __launch_bounds__(kPkThreads, 1) kmeans_persistent_kernel(KMeans
         al[ks][0] = qa.x; al[ks][2] = qa.y; al[ks][1] = qb.x; al[ks][3] = qb.y;
       }
       const float pna = B.pnorm[ga], pnb = B.pnorm[gb];
-      for (int nt0 = 0; nt0 < kpad / 8; nt0 += 8) {
-        float acc[8][4];
+      // approximate distances of rows g (acc[t][0..1]) and g + 8 (acc[t][2..3])
+      // to the centroids of n-tile ch * 8 + t, columns 2 tig and 2 tig + 1
+      float acc[8][4];
+      auto approx = [&](int ch) {
 #pragma unroll
         for (int t = 0; t < 8; ++t) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.0f;
 #pragma unroll
@@ -859,8 +863,8 @@ __global__ void __launch_bounds__(kPkThreads, 1) kmeans_persistent_kernel(KMeans
           if (ks < ksn) {
 #pragma unroll
             for (int t = 0; t < 8; ++t) {
-              if (nt0 + t < kpad / 8) {
-                const int off = ((nt0 + t) * 8 + g) * rw + ks * 8 + 2 * tig;
+              if (ch * 8 + t < kpad / 8) {
+                const int off = ((ch * 8 + t) * 8 + g) * rw + ks * 8 + 2 * tig;
                 const uint2 bh = *reinterpret_cast<const uint2*>(sch + off);
                 const uint2 bl = *reinterpret_cast<const uint2*>(scl + off);
                 mma_bf16_16816(acc[t], ah[ks], bh);
@@ -872,94 +876,160 @@ __global__ void __launch_bounds__(kPkThreads, 1) kmeans_persistent_kernel(KMeans
         }
 #pragma unroll
         for (int t = 0; t < 8; ++t) {
-          if (nt0 + t < kpad / 8) {
-            const int c = (nt0 + t) * 8 + 2 * tig;
-            sa[g * (kpad + 1) + c] = __fsub_rn(fadd(pna, scn[c]), fmul(2.0f, acc[t][0]));
-            sa[g * (kpad + 1) + c + 1] = __fsub_rn(fadd(pna, scn[c + 1]), fmul(2.0f, acc[t][1]));
-            sa[(g + 8) * (kpad + 1) + c] = __fsub_rn(fadd(pnb, scn[c]), fmul(2.0f, acc[t][2]));
-            sa[(g + 8) * (kpad + 1) + c + 1] = __fsub_rn(fadd(pnb, scn[c + 1]), fmul(2.0f, acc[t][3]));
+          const int c = (ch * 8 + t) * 8 + 2 * tig;
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const int cc = c + (e & 1);
+            const float pn = e < 2 ? pna : pnb;
+            acc[t][e] = cc < k ? __fsub_rn(fadd(pn, scn[cc]), fmul(2.0f, acc[t][e])) : INFINITY;
+          }
+        }
+      };
+      // pass 1: row minima (with the values of a single chunk kept for pass 2)
+      float ming = INFINITY, ming8 = INFINITY;
+      bool fin_g = true, fin_g8 = true;
+#pragma unroll
+      for (int ch = 0; ch < NC; ++ch) {
+        approx(ch);
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+          const int c = (ch * 8 + t) * 8 + 2 * tig;
+#pragma unroll
+          for (int e = 0; e < 2; ++e) {
+            if (c + e < k) {
+              ming = fminf(ming, acc[t][e]);
+              ming8 = fminf(ming8, acc[t][2 + e]);
+              fin_g = fin_g && isfinite(acc[t][e]);
+              fin_g8 = fin_g8 && isfinite(acc[t][2 + e]);
+            }
           }
         }
       }
-      __syncwarp();
-      // exact recheck, one row per half-warp
-      for (int rr = 0; rr < 8; ++rr) {
-        const int r = half * 8 + rr;
-        const int i = r0 + r;
-        const bool valid = i < n;
-        const int grow = prow[valid ? i : n - 1];
-        const float pn = B.pnorm[grow];
-        const float* arow = sa + r * (kpad + 1);
-        float amin = INFINITY;
-        for (int c = hl; c < k; c += 16) amin = fminf(amin, arow[c]);
 #pragma unroll
-        for (int o = 8; o > 0; o >>= 1) amin = fminf(amin, __shfl_xor_sync(kFull, amin, o));
-        const float thr = amin + 2.0f * fadd(pn, scn[kpad]) * B.tc_crel;
-        // the row: lane hl holds coordinates hl + 16 b (b < nfull) and the
-        // tail coordinate 16 nfull + hl
-        const float* xr = B.x + static_cast<size_t>(grow) * d;
-        float xv[KS];
+      for (int o = 1; o <= 2; o <<= 1) {
+        ming = fminf(ming, __shfl_xor_sync(kFull, ming, o));
+        ming8 = fminf(ming8, __shfl_xor_sync(kFull, ming8, o));
+      }
+      const float thr_g = ming + 2.0f * fadd(pna, cmax) * crel;
+      const float thr_g8 = ming8 + 2.0f * fadd(pnb, cmax) * crel;
+      // pass 2: candidate masks (bit c of word c / 32) of both rows
+      uint32_t mg[4] = {0u, 0u, 0u, 0u}, mg8[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
-        for (int b = 0; b < KS; ++b) xv[b] = b < nfull ? xr[hl + 16 * b] : 0.0f;
-        const float xt = hl < tn ? xr[16 * nfull + hl] : 0.0f;
-        int best = k;
-        float bestd = INFINITY;
-        // candidates in ascending cluster order: a half scans 16-cluster
-        // groups until it has candidates; the halves keep their own group
-        // positions but execute every ballot and shuffle together
-        const int groups = (k + 15) / 16;
-        int m = 0, mcur = 0;
-        unsigned bits = 0u;
-        for (;;) {
-          for (;;) {
-            const bool need = bits == 0u && m < groups;
-            if (!__any_sync(kFull, need)) break;
-            const int cq = hl + 16 * m;
-            const bool cand = need && cq < k && !(arow[cq] > thr);
-            const unsigned bal = __ballot_sync(kFull, cand);
-            if (need) {
-              bits = (bal >> (16 * half)) & 0xffffu;
-              mcur = m;
-              ++m;
+      for (int ch = 0; ch < NC; ++ch) {
+        if (NC > 1) approx(ch);
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+          const int c = (ch * 8 + t) * 8 + 2 * tig;
+#pragma unroll
+          for (int e = 0; e < 2; ++e) {
+            if (c + e < k) {
+              // column c + e sits in word (ch * 8 + t) / 4 at bit c + e mod 32
+              const uint32_t bit = 1u << ((((ch * 8 + t) & 3) << 3) + 2 * tig + e);
+              if (!(acc[t][e] > thr_g)) mg[(ch * 8 + t) >> 2] |= bit;
+              if (!(acc[t][2 + e] > thr_g8)) mg8[(ch * 8 + t) >> 2] |= bit;
             }
-          }
-          const bool have = bits != 0u;
-          if (!__any_sync(kFull, have)) break;
-          const int c = have ? (__ffs(bits) - 1) + 16 * mcur : 0;
-          const float* cc = scf + c * d4;
-          float pp = 0.0f;
-#pragma unroll
-          for (int b = 0; b < KS; ++b)
-            if (b < nfull) pp = fadd(pp, fmul(xv[b], cc[hl + 16 * b]));
-          const int hb = half * 16;
-          const float q4 = __shfl_sync(kFull, pp, hb + ((hl + 4) & 15));
-          const float q8 = __shfl_sync(kFull, pp, hb + ((hl + 8) & 15));
-          const float q12 = __shfl_sync(kFull, pp, hb + ((hl + 12) & 15));
-          const float lv = fadd(fadd(pp, q4), fadd(q8, q12));
-          float sum = fadd(fadd(fadd(__shfl_sync(kFull, lv, hb), __shfl_sync(kFull, lv, hb + 1)),
-                                __shfl_sync(kFull, lv, hb + 2)),
-                           __shfl_sync(kFull, lv, hb + 3));
-          for (int t = 0; t < tn; ++t) sum = fadd(sum, fmul(__shfl_sync(kFull, xt, hb + t), cc[16 * nfull + t]));
-          if (have) {
-            const float dist = __fsub_rn(fadd(pn, scn[c]), fmul(2.0f, sum));
-            if (dist < bestd || (dist == bestd && c < best)) {
-              bestd = dist;
-              best = c;
-            }
-            bits &= bits - 1u;
           }
         }
-        if (best >= k) best = 0;
-        if (valid && hl == 0) {
+      }
+#pragma unroll
+      for (int w = 0; w < 4; ++w) {
+#pragma unroll
+        for (int o = 1; o <= 2; o <<= 1) {
+          mg[w] |= __shfl_xor_sync(kFull, mg[w], o);
+          mg8[w] |= __shfl_xor_sync(kFull, mg8[w], o);
+        }
+      }
+      {
+        // a row whose approximations and norm are all finite and that has a
+        // single candidate: that candidate is the exact nearest centroid
+        // (the nearest is always a candidate, and an exact tie would make
+        // both tied centroids candidates); other rows take the exact recheck
+        bool fg = fin_g && isfinite(pna), fg8 = fin_g8 && isfinite(pnb);
+#pragma unroll
+        for (int o = 1; o <= 2; o <<= 1) {
+          fg = __shfl_xor_sync(kFull, static_cast<int>(fg), o) != 0 && fg;
+          fg8 = __shfl_xor_sync(kFull, static_cast<int>(fg8), o) != 0 && fg8;
+        }
+        const int pop_g = __popc(mg[0]) + __popc(mg[1]) + __popc(mg[2]) + __popc(mg[3]);
+        const int pop_g8 = __popc(mg8[0]) + __popc(mg8[1]) + __popc(mg8[2]) + __popc(mg8[3]);
+        const bool single_g = fg && pop_g == 1, single_g8 = fg8 && pop_g8 == 1;
+        auto first_bit = [](const uint32_t (&m)[4]) {
+          return m[0] ? __ffs(m[0]) - 1 : m[1] ? 31 + __ffs(m[1]) : m[2] ? 63 + __ffs(m[2]) : 95 + __ffs(m[3]);
+        };
+        auto put = [&](int i, int best) {
+          if (i >= n) return;
           if (final_pass) {
             B.labels[static_cast<size_t>(p) * n + i] = best + 1;
           } else if (sas[i] != best) {
             sas[i] = best;
             misc[0] = 1;
           }
+        };
+        if (tig == 0) {
+          if (single_g) put(r0 + g, first_bit(mg));
+          if (single_g8) put(r0 + g + 8, first_bit(mg8));
+        }
+        // rows left for the exact recheck: bit r of `multi`
+        const unsigned bal_g = __ballot_sync(kFull, tig == 0 && !single_g);
+        const unsigned bal_g8 = __ballot_sync(kFull, tig == 0 && !single_g8);
+        unsigned multi = 0u;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          multi |= ((bal_g >> (4 * q)) & 1u) << q;
+          multi |= ((bal_g8 >> (4 * q)) & 1u) << (q + 8);
+        }
+        while (multi != 0u) {
+          const int r = __ffs(multi) - 1;
+          multi &= multi - 1u;
+          const int i = r0 + r;
+          if (i >= n) continue;
+          const int src = 4 * (r & 7);
+          uint32_t m[4];
+#pragma unroll
+          for (int w = 0; w < 4; ++w) m[w] = __shfl_sync(kFull, r < 8 ? mg[w] : mg8[w], src);
+          const int grow = prow[i];
+          const float pn = B.pnorm[grow];
+          // the row: lane hl holds coordinates hl + 16 b (b < nfull) and the
+          // tail coordinate 16 nfull + hl; both halves compute the same dots
+          const float* xr = B.x + static_cast<size_t>(grow) * d;
+          float xv[KS];
+#pragma unroll
+          for (int bb = 0; bb < KS; ++bb) xv[bb] = bb < nfull ? xr[hl + 16 * bb] : 0.0f;
+          const float xt = hl < tn ? xr[16 * nfull + hl] : 0.0f;
+          int best = k;
+          float bestd = INFINITY;
+#pragma unroll
+          for (int w = 0; w < 4; ++w) {
+            uint32_t bits = m[w];
+            while (bits != 0u) {
+              const int c = 32 * w + __ffs(bits) - 1;
+              bits &= bits - 1u;
+              const float* cc = scf + c * d4;
+              float pp = 0.0f;
+#pragma unroll
+              for (int bb = 0; bb < KS; ++bb)
+                if (bb < nfull) pp = fadd(pp, fmul(xv[bb], cc[hl + 16 * bb]));
+              const int hb = half * 16;
+              const float q4 = __shfl_sync(kFull, pp, hb + ((hl + 4) & 15));
+              const float q8 = __shfl_sync(kFull, pp, hb + ((hl + 8) & 15));
+              const float q12 = __shfl_sync(kFull, pp, hb + ((hl + 12) & 15));
+              const float lv = fadd(fadd(pp, q4), fadd(q8, q12));
+              float sum = fadd(fadd(fadd(__shfl_sync(kFull, lv, hb), __shfl_sync(kFull, lv, hb + 1)),
+                                    __shfl_sync(kFull, lv, hb + 2)),
+                               __shfl_sync(kFull, lv, hb + 3));
+              for (int t = 0; t < tn; ++t)
+                sum = fadd(sum, fmul(__shfl_sync(kFull, xt, hb + t), cc[16 * nfull + t]));
+              const float dist = __fsub_rn(fadd(pn, scn[c]), fmul(2.0f, sum));
+              if (dist < bestd || (dist == bestd && c < best)) {
+                bestd = dist;
+                best = c;
+              }
+            }
+          }
+          if (best >= k) best = 0;
+          if (lane == 0) put(i, best);
         }
       }
-      __syncwarp();
     }
     __syncthreads();
     if (final_pass) break;
@@ -1143,16 +1213,17 @@ int kmeans_run(const KMeansBatch& B, cudaStream_t st) {
     P.tc_crel = tc_error_factor(B.d, B.dp);
     const size_t bytes = pk_layout(B.n, B.k, B.d, B.dp).total;
     cudaError_t e;
-    if (B.dp <= 16) {
-      e = cudaFuncSetAttribute(kmeans_persistent_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
-      if (e == cudaSuccess) kmeans_persistent_kernel<1><<<B.problems, kPkThreads, bytes, st>>>(P);
-    } else if (B.dp <= 32) {
-      e = cudaFuncSetAttribute(kmeans_persistent_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
-      if (e == cudaSuccess) kmeans_persistent_kernel<2><<<B.problems, kPkThreads, bytes, st>>>(P);
-    } else {
-      e = cudaFuncSetAttribute(kmeans_persistent_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
-      if (e == cudaSuccess) kmeans_persistent_kernel<4><<<B.problems, kPkThreads, bytes, st>>>(P);
-    }
+    const int nc = ((B.k + 7) / 8 + 7) / 8;  // 8-n-tile chunks: 1 (k <= 64) or 2 (k <= 128)
+    auto go = [&](auto kern) {
+      const cudaError_t err =
+          cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+      if (err != cudaSuccess) return err;
+      kern<<<B.problems, kPkThreads, bytes, st>>>(P);
+      return cudaSuccess;
+    };
+    if (B.dp <= 16) e = nc == 1 ? go(kmeans_persistent_kernel<1, 1>) : go(kmeans_persistent_kernel<1, 2>);
+    else if (B.dp <= 32) e = nc == 1 ? go(kmeans_persistent_kernel<2, 1>) : go(kmeans_persistent_kernel<2, 2>);
+    else e = nc == 1 ? go(kmeans_persistent_kernel<4, 1>) : go(kmeans_persistent_kernel<4, 2>);
     if (e != cudaSuccess) return static_cast<int>(e);
     count_launch();
     return static_cast<int>(cudaGetLastError());
