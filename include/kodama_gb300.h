@@ -67,7 +67,8 @@ typedef struct kgb_matrix_options {
   int32_t components;        /* PLS components, default 50 */
   int32_t materialize_graph; /* return the (corrected) graph */
   int32_t apply_dissimilarity;
-  int32_t metric;            /* 2 = Euclidean (the only metric of the path) */
+  int32_t metric;            /* KGB_METRIC_* (KODAMAMatrixOptions::metric, default Euclidean):
+                                the exact graph's metric and the vote score rule */
   int32_t device;            /* CUDA device ordinal */
   int32_t host_threads;      /* host worker threads for per-run set-up, 0 = auto */
   int32_t first_run;         /* id of the first run (default 1): runs first_run .. first_run+runs-1
@@ -161,7 +162,11 @@ int kgb_kodama_matrix_from_graph(const int32_t* gidx, const float* gdist, int32_
  * graph-input path on the resident data and graph, its first
  * min(neighbors, graph width) columns. */
 typedef struct kgb_graph_handle kgb_graph_handle;
-int kgb_graph_create(const float* x, int32_t n, int32_t d, int32_t neighbors, int32_t device,
+/* metric: KODAMAGraphOptions::metric (KGB_METRIC_*; the graph as
+ * kgb_knn_graph_metric builds it).  The matrix on a handle scores neighbours
+ * by its own kgb_matrix_options::metric and, like the reference's
+ * graph-input path, first clamps the graph's distances at zero. */
+int kgb_graph_create(const float* x, int32_t n, int32_t d, int32_t neighbors, int32_t metric, int32_t device,
                      kgb_graph_handle** out);
 int kgb_graph_info(const kgb_graph_handle* graph, int32_t* n, int32_t* d, int32_t* neighbors);
 int kgb_graph_materialize(kgb_graph_handle* graph, int32_t* idx, float* dist);
@@ -221,6 +226,10 @@ typedef struct kgb_core_options {
   int32_t adaptive_proposal_size;
   int32_t device;
   int32_t auto_class_coarsening; /* CoreOptions::auto_class_coarsening (PLS-LDA classifier only) */
+  int32_t metric;            /* knn.metric, KGB_METRIC_* (0 = cosine, the KNNOptions default):
+                                the graph vote scores -(d*d) for Euclidean, 1 - d otherwise
+                                (core.cpp:672-677); the raw-data search metric of kgb_core_knn is
+                                its own argument */
   uint64_t seed;
   uint64_t cv_seed;
   kgb_policy policy;
@@ -383,6 +392,16 @@ int kgb_knn_graph(const float* x, int32_t n, int32_t d, int32_t K, int32_t devic
  * how many rows were computed by the brute force. */
 int kgb_knn_graph_ex(const float* x, int32_t n, int32_t d, int32_t K, int32_t device, int32_t method,
                      int32_t* idx, float* dist, int32_t* fallback_rows);
+
+/* The exact graph under a metric (KGB_METRIC_*), as self_knn_graph
+ * (kodama_matrix.cpp:391-533) asks native_cuda_exact_knn_search for it: K
+ * neighbours, self excluded, ties by index.  Euclidean: kgb_knn_graph.
+ * Inner product: internal distance minus the inner product (float32,
+ * coordinate order, no FMA), reported 1 + internal; cosine: the same on rows
+ * scaled as normalize_rows_for_cosine (kodama_matrix.cpp:155-167), reported
+ * max(0, 1 + internal) (native_knn.cpp:1157-1164). */
+int kgb_knn_graph_metric(const float* x, int32_t n, int32_t d, int32_t K, int32_t metric, int32_t device,
+                         int32_t* idx, float* dist);
 
 /* Replaces the Backend::CUDA branch of KODAMADissimilarityInPlace
  * (kodama.hpp:1181-1189, kodama_matrix.cpp:4383-4463): co-label proximity on a

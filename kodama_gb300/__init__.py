@@ -105,13 +105,13 @@ _KERNEL_NAMES = ("knn_graph", "atlas_kmeans", "landmark_kmeans", "vote_tables", 
 
 def _matrix_options(runs, cycles, landmarks, splitting, graph_neighbors, folds, knn_k, seed,
                     materialize_graph, apply_dissimilarity, device, host_threads, policy, first_run=1,
-                    classifier=0, components=50):
+                    classifier=0, components=50, metric=2):
     pol = policy if isinstance(policy, EvolutionPolicy) else EvolutionPolicy.from_name(policy or "full")
     return N.MatrixOptions(runs=runs, cycles=cycles, landmarks=landmarks, splitting=splitting,
                            graph_neighbors=graph_neighbors, folds=folds, knn_k=knn_k,
                            classifier=classifier, components=components,
                            materialize_graph=int(materialize_graph),
-                           apply_dissimilarity=int(apply_dissimilarity), metric=2, device=device,
+                           apply_dissimilarity=int(apply_dissimilarity), metric=metric, device=device,
                            host_threads=host_threads, first_run=first_run, reserved=0, seed=seed,
                            policy=pol._c())
 
@@ -136,14 +136,15 @@ class KODAMAGraph:
     KODAMA.matrix on them without rebuilding the graph (KODAMAMatrix(x,
     KODAMAGraphResult)).  Use as a context manager or call ``close``."""
 
-    def __init__(self, x, neighbors=100, device=0):
+    def __init__(self, x, neighbors=100, device=0, metric="euclidean"):
         xa = np.ascontiguousarray(x, dtype=np.float32)
         if xa.ndim != 2:
             raise ValueError("x must be a 2-D matrix")
         self.n, self.d = xa.shape
         self.device = device
         h = ctypes.c_void_p()
-        N.check(N.load().kgb_graph_create(_ptr(xa), self.n, self.d, neighbors, device, ctypes.byref(h)))
+        N.check(N.load().kgb_graph_create(_ptr(xa), self.n, self.d, neighbors, _metric(metric), device,
+                                          ctypes.byref(h)))
         self._h = h
         k = ctypes.c_int32()
         N.check(N.load().kgb_graph_info(self._h, None, None, ctypes.byref(k)))
@@ -188,7 +189,7 @@ def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitt
                   components=50, proposal_weights=None, snapshot_cycle=None,
                   proposal_greedy=False, starting_labels=None, constrain=None,
                   fixed=None, _handle=None, graph_only=False, feature_components=0,
-                  feature_steps=3) -> MatrixResult:
+                  feature_steps=3, metric="euclidean") -> MatrixResult:
     """KODAMA.matrix on the GPU with the kNN (``classifier="knn"``) or PLS-LDA
     (``classifier="pls"``, ``components`` latent components) classifier.
     ``proposal_weights`` (the 4801 parameters of ``train_proposal``) selects
@@ -210,6 +211,9 @@ def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitt
     then read in place from HBM (kgb_kodama_matrix_resident); pass
     ``res_out`` (a CUDA int32 tensor of shape (runs, n)) to keep the label
     matrix on the device too.
+    ``metric`` ("euclidean", "cosine", "inner_product") is
+    KODAMAMatrixOptions::metric: the metric of the exact graph built from raw
+    data and the vote score rule (-(d*d) for Euclidean, 1 - d otherwise).
     Defaults are those of KODAMAMatrixOptions (kodama.hpp:535-570).
     """
     x_dev = None
@@ -234,7 +238,7 @@ def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitt
         raise ValueError("Unsupported KODAMA.matrix classifier.")
     opt = _matrix_options(runs, cycles, landmarks, splitting, graph_neighbors, folds, knn_k, seed,
                           materialize_graph, apply_dissimilarity, device, host_threads, policy, first_run,
-                          cls, components)
+                          cls, components, _metric(metric))
     res = np.zeros((runs, n), np.int32)
     acc = np.zeros(runs, np.float64)
     v = np.zeros((runs, max(cycles, 0)), np.float64)
@@ -368,7 +372,7 @@ def KODAMA_matrix_batch(problems, *, runs=100, cycles=20, landmarks=10000, split
             raise ValueError("Unsupported KODAMA.matrix classifier.")
         opt = _matrix_options(kw["runs"], kw["cycles"], kw["landmarks"], kw["splitting"], kw["graph_neighbors"],
                               kw["folds"], kw["knn_k"], kw["seed"], materialize_graph, apply_dissimilarity,
-                              device, 0, policy, 1, cls, kw["components"])
+                              device, 0, policy, 1, cls, kw["components"], _metric(pr.get("metric", "euclidean")))
         M, T = kw["runs"], kw["cycles"]
         b = dict(x=x, res=np.zeros((M, n), np.int32), acc=np.zeros(M, np.float64),
                  v=np.zeros((M, max(T, 0)), np.float64), hashes=np.zeros((M, 3), np.uint64),
@@ -439,14 +443,16 @@ class CoreResult:
 
 
 def _core_options(cycles, k, folds, stratified, evolutionary_search, guarded_diversity,
-                  many_to_one_absorption, adaptive_proposal_size, seed, cv_seed, device, policy):
+                  many_to_one_absorption, adaptive_proposal_size, seed, cv_seed, device, policy,
+                  metric="cosine"):
     pol = policy if isinstance(policy, EvolutionPolicy) else EvolutionPolicy.from_name(policy or "full")
     return N.CoreOptions(cycles=cycles, k=k, folds=folds, stratified=int(stratified),
                          evolutionary_search=int(evolutionary_search),
                          guarded_diversity=int(guarded_diversity),
                          many_to_one_absorption=int(many_to_one_absorption),
                          adaptive_proposal_size=int(adaptive_proposal_size), device=device,
-                         auto_class_coarsening=0, seed=seed, cv_seed=cv_seed, policy=pol._c())
+                         auto_class_coarsening=0, metric=_metric(metric), seed=seed, cv_seed=cv_seed,
+                         policy=pol._c())
 
 
 def _alloc_core(samples, cycles):
@@ -477,8 +483,10 @@ def CoreKNNGraph_batch(graph_idx, graph_dist, labels, seeds, cv_seeds, *, cycles
                        folds=10, stratified=True, evolutionary_search=False,
                        guarded_diversity=False, many_to_one_absorption=False,
                        adaptive_proposal_size=True, index_base=-1, device=0,
-                       policy="full") -> list[CoreResult]:
-    """`len(seeds)` independent CoreKNNGraph evolutions over one graph in one launch."""
+                       policy="full", metric="cosine") -> list[CoreResult]:
+    """`len(seeds)` independent CoreKNNGraph evolutions over one graph in one launch.
+    ``metric`` is KNNOptions::metric (default cosine, as in the reference):
+    the vote scores -(d*d) for "euclidean", 1 - d otherwise."""
     gi = np.ascontiguousarray(graph_idx, dtype=np.int32)
     gd = np.ascontiguousarray(graph_dist, dtype=np.float32)
     samples, gk = gi.shape
@@ -489,7 +497,7 @@ def CoreKNNGraph_batch(graph_idx, graph_dist, labels, seeds, cv_seeds, *, cycles
     if s.shape[0] != problems or cs.shape[0] != problems:
         raise ValueError("one seed and one cv seed per problem")
     opt = _core_options(cycles, k, folds, stratified, evolutionary_search, guarded_diversity,
-                        many_to_one_absorption, adaptive_proposal_size, 0, 0, device, policy)
+                        many_to_one_absorption, adaptive_proposal_size, 0, 0, device, policy, metric)
     arr = (N.CoreResult * problems)()
     keep = []
     for p in range(problems):
@@ -505,8 +513,10 @@ def CoreKNNGraph_batch(graph_idx, graph_dist, labels, seeds, cv_seeds, *, cycles
 def CoreKNNGraph(graph_idx, graph_dist, labels, *, constrain=None, fixed=None, cycles=100, k=30,
                  folds=10, stratified=True, evolutionary_search=False, guarded_diversity=False,
                  many_to_one_absorption=False, adaptive_proposal_size=True, seed=1, cv_seed=1,
-                 index_base=-1, device=0, policy="full") -> CoreResult:
-    """CoreKNNGraph_CUDA (kodama.hpp:1043): label evolution over a neighbour graph."""
+                 index_base=-1, device=0, policy="full", metric="cosine") -> CoreResult:
+    """CoreKNNGraph_CUDA (kodama.hpp:1043): label evolution over a neighbour graph.
+    ``metric`` is KNNOptions::metric (default cosine, as in the reference):
+    the vote scores -(d*d) for "euclidean", 1 - d otherwise (core.cpp:672-677)."""
     gi = np.ascontiguousarray(graph_idx, dtype=np.int32)
     gd = np.ascontiguousarray(graph_dist, dtype=np.float32)
     samples, gk = gi.shape
@@ -516,7 +526,7 @@ def CoreKNNGraph(graph_idx, graph_dist, labels, *, constrain=None, fixed=None, c
     con = None if constrain is None else np.ascontiguousarray(constrain, dtype=np.int32)
     fix = None if fixed is None else np.ascontiguousarray(fixed, dtype=np.int32)
     opt = _core_options(cycles, k, folds, stratified, evolutionary_search, guarded_diversity,
-                        many_to_one_absorption, adaptive_proposal_size, seed, cv_seed, device, policy)
+                        many_to_one_absorption, adaptive_proposal_size, seed, cv_seed, device, policy, metric)
     r, bufs = _alloc_core(samples, cycles)
     rc = N.load().kgb_core_knn_graph(_ptr(gi), _ptr(gd), samples, gk, index_base, _ptr(lab),
                                      _ptr(con), _ptr(fix), ctypes.byref(opt), ctypes.byref(r))
@@ -632,14 +642,20 @@ def CoreKNN(x, labels, *, constrain=None, fixed=None, cycles=100, folds=10, stra
 KNN_METHODS = {"auto": 0, "brute_force": 1, "tensor": 2}
 
 
-def knn_graph(x, K: int, *, device: int = 0, method: str = "auto", return_fallback: bool = False):
-    """Exact kNN graph: zero-based (n, K) indices and sqrt distances.
-    ``method``: "auto", "brute_force" or "tensor" (same result);
-    ``return_fallback`` adds the number of rows the brute force computed."""
+def knn_graph(x, K: int, *, device: int = 0, method: str = "auto", return_fallback: bool = False,
+              metric: str = "euclidean"):
+    """Exact kNN graph: zero-based (n, K) indices and the reference's reported
+    distances (sqrt for "euclidean"; 1 - <x,y> for "inner_product";
+    max(0, 1 - cos) for "cosine").  ``method`` ("auto", "brute_force" or
+    "tensor", same result) and ``return_fallback`` (rows computed by the
+    brute force) apply to the Euclidean search."""
     x = np.ascontiguousarray(x, dtype=np.float32)
     n, d = x.shape
     idx = np.zeros((n, K), np.int32)
     dist = np.zeros((n, K), np.float32)
+    if _metric(metric) != N.METRICS["euclidean"]:
+        N.check(N.load().kgb_knn_graph_metric(_ptr(x), n, d, K, _metric(metric), device, _ptr(idx), _ptr(dist)))
+        return (idx, dist, n) if return_fallback else (idx, dist)
     fb = ctypes.c_int32(0)
     N.check(N.load().kgb_knn_graph_ex(_ptr(x), n, d, K, device, KNN_METHODS[method], _ptr(idx), _ptr(dist),
                                       ctypes.byref(fb)))

@@ -33,6 +33,7 @@ EXPORTED = (
     "kgb_core_knn_graph_batch",
     "kgb_knncv",
     "kgb_knn_graph_ex",
+    "kgb_knn_graph_metric",
     "kgb_core_knn",
     "kgb_plsldacv",
     "kgb_plsdacv",
@@ -108,7 +109,7 @@ class BatchReport(ctypes.Structure):
 class CoreOptions(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int32) for n in (
         "cycles", "k", "folds", "stratified", "evolutionary_search", "guarded_diversity",
-        "many_to_one_absorption", "adaptive_proposal_size", "device", "auto_class_coarsening")] + [
+        "many_to_one_absorption", "adaptive_proposal_size", "device", "auto_class_coarsening", "metric")] + [
         ("seed", ctypes.c_uint64), ("cv_seed", ctypes.c_uint64), ("policy", Policy)]
 
 
@@ -165,7 +166,7 @@ def load():
     lib.kgb_graph_features.argtypes = [P, P, i32, i32, i32, i32, i32, ctypes.c_uint64, P]
     lib.kgb_kodama_matrix_from_graph.argtypes = [P, P, i32, i32, i32, i32, i32, ctypes.POINTER(MatrixOptions),
                                                  ctypes.POINTER(MatrixResult)]
-    lib.kgb_graph_create.argtypes = [P, i32, i32, i32, i32, ctypes.POINTER(ctypes.c_void_p)]
+    lib.kgb_graph_create.argtypes = [P, i32, i32, i32, i32, i32, ctypes.POINTER(ctypes.c_void_p)]
     lib.kgb_graph_info.argtypes = [P, P, P, P]
     lib.kgb_graph_materialize.argtypes = [P, P, P]
     lib.kgb_kodama_matrix_graph.argtypes = [P, ctypes.POINTER(MatrixOptions), ctypes.POINTER(MatrixResult)]
@@ -181,6 +182,7 @@ def load():
                                              ctypes.POINTER(CoreResult)]
     lib.kgb_knn_graph.argtypes = [P, i32, i32, i32, i32, P, P]
     lib.kgb_knn_graph_ex.argtypes = [P, i32, i32, i32, i32, i32, P, P, P]
+    lib.kgb_knn_graph_metric.argtypes = [P, i32, i32, i32, i32, i32, P, P]
     lib.kgb_knncv.argtypes = [P, i32, i32, P, P, ctypes.POINTER(KnnOptions), P, P]
     lib.kgb_core_knn.argtypes = [P, i32, i32, i32, P, P, P, ctypes.POINTER(CoreOptions), ctypes.POINTER(CoreResult)]
     lib.kgb_dissimilarity_inplace.argtypes = [P, P, i32, i32, P, i32, i32]

@@ -989,13 +989,18 @@ EvolveBuffers run_pls_evolution(Ctx& ctx, kgb::EvolveParams P, PlsBuffers& b, in
 }
 
 
+void check_metric(int metric) {
+  if (metric != KGB_METRIC_COSINE && metric != KGB_METRIC_INNER_PRODUCT && metric != KGB_METRIC_EUCLIDEAN)
+    fail(KGB_EINVAL, "unknown distance metric");
+}
+
 void validate_matrix_options(const kgb_matrix_options* o) {
   if (o == nullptr) fail(KGB_EINVAL, "options pointer is null");
   if (o->runs < 1) fail(KGB_EINVAL, "KODAMAMatrixOptions::runs must be positive.");
   if (o->cycles < 0) fail(KGB_EINVAL, "KODAMAMatrixOptions::cycles must be non-negative.");
   if (o->folds < 2) fail(KGB_EINVAL, "KODAMAMatrixOptions::folds must be at least two.");
   if (o->folds > 255) fail(KGB_EINVAL, "at most 255 folds are supported");
-  if (o->metric != 2 && o->metric != 0) fail(KGB_EINVAL, "only the Euclidean metric is supported");
+  check_metric(o->metric);
 }
 
 // The KODAMA.matrix path after the global graph (n x K zero-based, compacted,
@@ -1425,6 +1430,7 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     a.folds = d_folds;
     a.nb = d_nb;
     a.sc = d_sc;
+    a.score_one_minus = o->metric != KGB_METRIC_EUCLIDEAN;
     ck_launch(kgb::build_vote_tables(a, st), "vote tables");
   }
   ev_tables = ctx.mark();
@@ -1652,16 +1658,31 @@ void matrix_finalize(Ctx* ctx, MatrixTail& t, kgb_matrix_result* out, Clock& clk
   out->effective_landmarks = L;
 }
 
-// Shared body of the KODAMA.matrix entry points: x on the host (copied in) or
-// already on the device; a caller graph (normalised like
-// normalize_external_graph) or the exact graph built on the device.
-// The exact kNN graph of d_x (n x d, device) into d_idx / d_dist (n x K):
-// the tensor-core candidate search with its certificate where it applies
-// (knn_tc.cu), else the brute force.  fallback_rows (host, may be null)
-// receives how many rows the certificate sent to the brute force.
-void exact_graph(Ctx& ctx, const float* d_x, int n, int d, int K, int method, int* d_idx, float* d_dist,
+// The exact kNN graph of d_x (n x d, device) into d_idx / d_dist (n x K),
+// self excluded, reported distances as the reference reports them
+// (native_knn.cpp:1157-1164).  Euclidean: the tensor-core candidate search
+// with its certificate where it applies (knn_tc.cu), else the brute force.
+// Cosine (rows scaled as normalize_rows_for_cosine, kodama_matrix.cpp:155)
+// and inner product: the brute-force search on minus the inner product.
+// fallback_rows (host, may be null) receives how many rows the brute force
+// computed.
+void exact_graph(Ctx& ctx, const float* d_x, int n, int d, int K, int method, int metric, int* d_idx, float* d_dist,
                  int* fallback_rows) {
   const int segments = 4;
+  if (metric != KGB_METRIC_EUCLIDEAN) {
+    if (method == KGB_KNN_TENSOR) fail(KGB_EINVAL, "the tensor-core kNN search is for the Euclidean metric");
+    const float* xs = d_x;
+    if (metric == KGB_METRIC_COSINE) {
+      float* xn = ctx.alloc<float>(static_cast<size_t>(n) * d);
+      ck_launch(kgb::normalize_rows(d_x, n, d, 2, xn, ctx.stream()), "cosine rows");
+      xs = xn;
+    }
+    void* scratch = ctx.alloc<unsigned char>(kgb::knn_bruteforce_scratch(n, K, segments));
+    ck_launch(kgb::knn_bruteforce_inner(xs, n, d, K, metric, segments, scratch, d_idx, d_dist, ctx.stream()),
+              "kNN graph");
+    if (fallback_rows != nullptr) *fallback_rows = n;
+    return;
+  }
   const bool tc = method == KGB_KNN_TENSOR || (method == KGB_KNN_AUTO && kgb::knn_tc_supported(n, d, K));
   if (method == KGB_KNN_TENSOR && !kgb::knn_tc_supported(n, d, K))
     fail(KGB_EINVAL, "the tensor-core kNN search needs d <= 256, K <= 96 and n > 2 * (K + 16) + 64");
@@ -1679,6 +1700,25 @@ void exact_graph(Ctx& ctx, const float* d_x, int n, int d, int K, int method, in
     ck_launch(kgb::knn_bruteforce(d_x, n, d, K, segments, scratch, d_idx, d_dist, ctx.stream()), "kNN graph");
     if (fallback_rows != nullptr) *fallback_rows = n;
   }
+}
+
+// The exact graph a KODAMA.matrix call works on: under the cosine and
+// inner-product metrics it then passes through normalize_external_graph
+// (kodama_matrix.cpp:1292-1330), as the reference's graph-input path does
+// with a caller graph, which clamps the reported distances at zero (1 - <x,y>
+// can be negative).
+void matrix_graph(Ctx& ctx, const float* d_x, int n, int d, int K, int metric, int* d_gidx, float* d_gdist) {
+  if (metric == KGB_METRIC_EUCLIDEAN) {
+    exact_graph(ctx, d_x, n, d, K, KGB_KNN_AUTO, metric, d_gidx, d_gdist, nullptr);
+    return;
+  }
+  int* t_idx = ctx.alloc<int>(static_cast<size_t>(n) * K);
+  float* t_dist = ctx.alloc<float>(static_cast<size_t>(n) * K);
+  exact_graph(ctx, d_x, n, d, K, KGB_KNN_AUTO, metric, t_idx, t_dist, nullptr);
+  int* d_mm = ctx.alloc<int>(2);
+  ck_launch(kgb::graph_minmax(t_idx, static_cast<size_t>(n) * K, d_mm, ctx.stream()), "graph min/max");
+  ck_launch(kgb::normalize_external(t_idx, t_dist, n, K, K, 0, d_mm, d_gidx, d_gdist, ctx.stream()),
+            "graph normalisation");
 }
 
 // Landmarks and graph width of a call (run_kodama_matrix,
@@ -1879,7 +1919,7 @@ std::unique_ptr<BatchGraph> build_batch(const kgb_matrix_problem* probs, int cou
         Clock clk;
         matrix_from_device_graph(ctx, d_x, q.n, q.d, d_gidx, d_gdist, K, &o, &bp.shadow, clk, ev_start, -1, folds,
                                  bp.tail, [&]() {
-                                   exact_graph(ctx, d_x, q.n, q.d, K, KGB_KNN_AUTO, d_gidx, d_gdist, nullptr);
+                                   matrix_graph(ctx, d_x, q.n, q.d, K, o.metric, d_gidx, d_gdist);
                                  });
         ctx.release();
       }
@@ -2074,7 +2114,7 @@ void matrix_entry(const float* x, bool x_on_device, int n, int d, const int32_t*
     out->timings[1] = clk.lap();
     MatrixTail tail;
     matrix_from_device_graph(ctx, d_x, n, d, d_gidx, d_gdist, K, opt, out, clk, ev_start, -1, folds_future, tail,
-                             [&]() { exact_graph(ctx, d_x, n, d, K, KGB_KNN_AUTO, d_gidx, d_gdist, nullptr); });
+                             [&]() { matrix_graph(ctx, d_x, n, d, K, opt->metric, d_gidx, d_gdist); });
     ctx.sync();
     matrix_finalize(&ctx, tail, out, clk);
     out->timings[0] = total.lap();
@@ -2104,6 +2144,7 @@ void core_knn_run(Ctx& ctx, int samples, int problems, const int32_t* labels, co
   if (samples > 65535) fail(KGB_EINVAL, "at most 65535 samples per problem are supported");
   if (problems < 1) fail(KGB_EINVAL, "problems must be positive");
   if (opt->cycles < 0) fail(KGB_EINVAL, "Core cycles must be non-negative.");
+  check_metric(opt->metric);
   if (opt->k < 1) fail(KGB_EINVAL, "KNNOptions::k must be positive.");
   if (opt->folds < 2) fail(KGB_EINVAL, "Number of folds must be at least 2.");
   if (opt->folds > 255) fail(KGB_EINVAL, "at most 255 folds are supported");
@@ -2260,6 +2301,7 @@ void core_graph_problems(const int32_t* gidx, const float* gdist, int samples, i
                  a.folds = d_folds;
                  a.nb = d_nb;
                  a.sc = d_sc;
+                 a.score_one_minus = opt->metric != KGB_METRIC_EUCLIDEAN;
                  ck_launch(kgb::build_vote_tables(a, st), "vote tables");
                });
 }
@@ -2282,10 +2324,6 @@ const float* search_matrix(Ctx& ctx, const float* d_x, int n, int d, int metric,
   return xs;
 }
 
-void check_metric(int metric) {
-  if (metric != KGB_METRIC_COSINE && metric != KGB_METRIC_INNER_PRODUCT && metric != KGB_METRIC_EUCLIDEAN)
-    fail(KGB_EINVAL, "unknown distance metric");
-}
 
 }  // namespace
 
@@ -2298,7 +2336,7 @@ void set_last_error(const char* msg) { g_error = msg; }
 // Resident data and exact kNN graph of KODAMAGraph (see kgb_graph_create).
 struct kgb_graph_handle {
   std::mutex mu;
-  int device = 0, n = 0, d = 0, K = 0;
+  int device = 0, n = 0, d = 0, K = 0, metric = KGB_METRIC_EUCLIDEAN;
   float* d_x = nullptr;
   int* d_idx = nullptr;
   float* d_dist = nullptr;
@@ -2373,11 +2411,12 @@ int kgb_kodama_matrix_from_graph(const int32_t* gidx, const float* gdist, int32_
   });
 }
 
-int kgb_graph_create(const float* x, int32_t n, int32_t d, int32_t neighbors, int32_t device,
+int kgb_graph_create(const float* x, int32_t n, int32_t d, int32_t neighbors, int32_t metric, int32_t device,
                      kgb_graph_handle** out) {
   return guarded([&]() {
     if (x == nullptr || out == nullptr) fail(KGB_EINVAL, "null pointer");
     *out = nullptr;
+    check_metric(metric);
     if (n < 3) fail(KGB_EINVAL, "KODAMAGraph requires at least 3 rows.");
     if (d < 1) fail(KGB_EINVAL, "Input matrix must have at least one column.");
     if (neighbors < 1) fail(KGB_EINVAL, "KODAMAGraphOptions::neighbors must be positive.");
@@ -2386,12 +2425,13 @@ int kgb_graph_create(const float* x, int32_t n, int32_t d, int32_t neighbors, in
     g->n = n;
     g->d = d;
     g->K = std::min(neighbors, n - 1);
+    g->metric = metric;
     Ctx ctx(device);
     ck(cudaMalloc(&g->d_x, sizeof(float) * static_cast<size_t>(n) * d), "cudaMalloc");
     ck(cudaMalloc(&g->d_idx, sizeof(int) * static_cast<size_t>(n) * g->K), "cudaMalloc");
     ck(cudaMalloc(&g->d_dist, sizeof(float) * static_cast<size_t>(n) * g->K), "cudaMalloc");
     ctx.h2d(g->d_x, x, static_cast<size_t>(n) * d);
-    exact_graph(ctx, g->d_x, n, d, g->K, KGB_KNN_AUTO, g->d_idx, g->d_dist, nullptr);
+    exact_graph(ctx, g->d_x, n, d, g->K, KGB_KNN_AUTO, metric, g->d_idx, g->d_dist, nullptr);
     ctx.sync();
     *out = g.release();
   });
@@ -2446,8 +2486,9 @@ int kgb_kodama_matrix_graph(kgb_graph_handle* g, const kgb_matrix_options* opt, 
     const int ev_start = ctx.mark();
     int* d_gidx = g->d_idx;
     float* d_gdist = g->d_dist;
-    if (K < g->K) {
+    if (K < g->K || g->metric != KGB_METRIC_EUCLIDEAN) {
       // the first K columns, as normalize_external_graph trims a wider graph
+      // (and clamps at zero the distances 1 - <x,y> of a non-Euclidean graph)
       int* d_mm = ctx.alloc<int>(2);
       ck_launch(kgb::graph_minmax(g->d_idx, static_cast<size_t>(n) * g->K, d_mm, ctx.stream()), "graph min/max");
       d_gidx = ctx.alloc<int>(static_cast<size_t>(n) * K);
@@ -2509,11 +2550,28 @@ int kgb_knn_graph_ex(const float* x, int32_t n, int32_t d, int32_t K, int32_t de
     int* d_idx = ctx.alloc<int>(static_cast<size_t>(n) * K);
     float* d_dist = ctx.alloc<float>(static_cast<size_t>(n) * K);
     int fb = 0;
-    exact_graph(ctx, d_x, n, d, K, method, d_idx, d_dist, &fb);
+    exact_graph(ctx, d_x, n, d, K, method, KGB_METRIC_EUCLIDEAN, d_idx, d_dist, &fb);
     ctx.download(idx, d_idx, static_cast<size_t>(n) * K);
     ctx.download(dist, d_dist, static_cast<size_t>(n) * K);
     ctx.sync();
     if (fallback_rows != nullptr) *fallback_rows = fb;
+  });
+}
+
+int kgb_knn_graph_metric(const float* x, int32_t n, int32_t d, int32_t K, int32_t metric, int32_t device,
+                         int32_t* idx, float* dist) {
+  return guarded([&]() {
+    if (x == nullptr || idx == nullptr || dist == nullptr) fail(KGB_EINVAL, "null pointer");
+    if (n < 1 || d < 1 || K < 1) fail(KGB_EINVAL, "invalid kNN graph dimensions");
+    check_metric(metric);
+    Ctx ctx(device);
+    const float* d_x = ctx.upload(x, static_cast<size_t>(n) * d);
+    int* d_idx = ctx.alloc<int>(static_cast<size_t>(n) * K);
+    float* d_dist = ctx.alloc<float>(static_cast<size_t>(n) * K);
+    exact_graph(ctx, d_x, n, d, K, KGB_KNN_AUTO, metric, d_idx, d_dist, nullptr);
+    ctx.download(idx, d_idx, static_cast<size_t>(n) * K);
+    ctx.download(dist, d_dist, static_cast<size_t>(n) * K);
+    ctx.sync();
   });
 }
 

@@ -7,7 +7,8 @@
 //   normalize_indices: normalize_graph_indices (core.cpp:586-622): positions
 //     kept, invalid ids -> -1, non-finite or negative distances -> +inf.
 //   build_vote_tables: per problem and landmark row, the first k' valid,
-//     non-self, out-of-fold neighbours among landmark rows with score -(d*d):
+//     non-self, out-of-fold neighbours among landmark rows with score -(d*d)
+//     (Euclidean metric) or 1 - d (cosine, inner product; core.cpp:672-677):
 //     subset_graph_to_rows (kodama_matrix.cpp:1332-1365) followed by
 //     precompute_knn_cv_graph (core.cpp:624-692).
 //   project_labels: non-landmark label = majority over the first knn.k
@@ -122,7 +123,7 @@ __global__ void vote_table_kernel(VoteTableArgs a) {
     if (!isfinite(dist)) continue;
     const float dc = (0.0f < dist) ? dist : 0.0f;
     nb[col] = static_cast<uint16_t>(loc);
-    sc[col] = -__fmul_rn(dc, dc);
+    sc[col] = a.score_one_minus ? __fsub_rn(1.0f, dc) : -__fmul_rn(dc, dc);
     ++col;
   }
   for (; col < a.w; ++col) {

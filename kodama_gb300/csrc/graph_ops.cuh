@@ -18,6 +18,7 @@ struct VoteTableArgs {
   const uint8_t* folds;   // problems x L
   uint16_t* nb;           // problems x L x w
   float* sc;              // problems x L x w
+  int score_one_minus;    // 0: score -(d*d) (Euclidean), 1: score 1 - d (cosine, inner product)
 };
 
 struct ReverseArgs {

@@ -858,20 +858,29 @@ __global__ void __launch_bounds__(kPkThreads, 1) kmeans_persistent_kernel(KMeans
       auto approx = [&](int ch) {
 #pragma unroll
         for (int t = 0; t < 8; ++t) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.0f;
+        // the three products of a k-step go round the 8 n-tiles in turn, so
+        // consecutive mma.sync never wait on the same accumulator
 #pragma unroll
         for (int ks = 0; ks < KS; ++ks) {
           if (ks < ksn) {
+            uint2 bf[8];
 #pragma unroll
-            for (int t = 0; t < 8; ++t) {
-              if (ch * 8 + t < kpad / 8) {
-                const int off = ((ch * 8 + t) * 8 + g) * rw + ks * 8 + 2 * tig;
-                const uint2 bh = *reinterpret_cast<const uint2*>(sch + off);
-                const uint2 bl = *reinterpret_cast<const uint2*>(scl + off);
-                mma_bf16_16816(acc[t], ah[ks], bh);
-                mma_bf16_16816(acc[t], ah[ks], bl);
-                mma_bf16_16816(acc[t], al[ks], bh);
-              }
-            }
+            for (int t = 0; t < 8; ++t)
+              if (ch * 8 + t < kpad / 8)
+                bf[t] = *reinterpret_cast<const uint2*>(sch + ((ch * 8 + t) * 8 + g) * rw + ks * 8 + 2 * tig);
+#pragma unroll
+            for (int t = 0; t < 8; ++t)
+              if (ch * 8 + t < kpad / 8) mma_bf16_16816(acc[t], ah[ks], bf[t]);
+#pragma unroll
+            for (int t = 0; t < 8; ++t)
+              if (ch * 8 + t < kpad / 8) mma_bf16_16816(acc[t], al[ks], bf[t]);
+#pragma unroll
+            for (int t = 0; t < 8; ++t)
+              if (ch * 8 + t < kpad / 8)
+                bf[t] = *reinterpret_cast<const uint2*>(scl + ((ch * 8 + t) * 8 + g) * rw + ks * 8 + 2 * tig);
+#pragma unroll
+            for (int t = 0; t < 8; ++t)
+              if (ch * 8 + t < kpad / 8) mma_bf16_16816(acc[t], ah[ks], bf[t]);
           }
         }
 #pragma unroll

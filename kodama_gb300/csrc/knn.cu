@@ -197,8 +197,20 @@ __global__ void __launch_bounds__(kQ) knn_segment_generic_kernel(const float* __
   }
 }
 
+// Reported distance of an internal one (native_knn_output_distance,
+// native_knn.cpp:1157-1164): sqrt for Euclidean, max(0, 1 + v) for cosine,
+// 1 + v for inner product; kOutRaw keeps the internal value.
+enum OutMode { kOutSqrt = 0, kOutRaw = 1, kOutCosine = 2, kOutInner = 3 };
+
+__device__ __forceinline__ float output_distance(float v, int mode) {
+  if (mode == kOutSqrt) return __fsqrt_rn(v);
+  if (mode == kOutRaw) return v;
+  const float o = __fadd_rn(1.0f, v);
+  return mode == kOutCosine ? ((0.0f < o) ? o : 0.0f) : o;
+}
+
 __global__ void knn_merge_kernel(int n, int K, int segs, const float* __restrict__ pd, const int* __restrict__ pi,
-                                 const int* __restrict__ qrows, const int* __restrict__ nq, bool raw,
+                                 const int* __restrict__ qrows, const int* __restrict__ nq, int mode,
                                  int* __restrict__ idx, float* __restrict__ dist) {
   const int qi = blockIdx.x * blockDim.x + threadIdx.x;
   const int qrow = query_row(qrows, nq, n, qi);
@@ -229,7 +241,7 @@ __global__ void knn_merge_kernel(int n, int K, int segs, const float* __restrict
     }
     ++head[bs];
     idx[out] = biv;
-    dist[out] = raw ? bdv : __fsqrt_rn(bdv);
+    dist[out] = output_distance(bdv, mode);
   }
 }
 
@@ -237,8 +249,9 @@ __global__ void knn_merge_kernel(int n, int K, int segs, const float* __restrict
 // by 1 / sqrt(sum of squares) when that norm is finite and positive, then
 // rounded to float.  mode 0: the squares summed sequentially in double
 // (knncv.cpp:85-108); mode 1: summed in x86 80-bit extended precision and
-// rounded to double (core.cpp:182-188, ext80.h).  One thread per row, the
-// coordinates in order.
+// rounded to double (core.cpp:182-188, ext80.h); mode 2: the extended sum of
+// mode 1, the row then scaled in float (normalize_rows_for_cosine,
+// kodama_matrix.cpp:155-167).  One thread per row, the coordinates in order.
 __global__ void normalize_rows_kernel(const float* __restrict__ x, int n, int d, int mode, float* __restrict__ out) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n) return;
@@ -257,6 +270,14 @@ __global__ void normalize_rows_kernel(const float* __restrict__ x, int n, int d,
     ss = finite ? ext80_to_double(acc) : INFINITY;
   }
   const double nrm = __dsqrt_rn(ss);
+  if (mode == 2) {
+    // normalize_rows_for_cosine: the row multiplied in float by the float
+    // rounding of 1 / norm; rows with a zero or non-finite norm unchanged
+    const bool ok = nrm > 0.0 && isfinite(nrm);
+    const float fs = ok ? __double2float_rn(__ddiv_rn(1.0, nrm)) : 1.0f;
+    for (int j = 0; j < d; ++j) out[static_cast<size_t>(r) * d + j] = ok ? __fmul_rn(row[j], fs) : row[j];
+    return;
+  }
   const double scale = (nrm > 0.0 && isfinite(nrm)) ? __ddiv_rn(1.0, nrm) : 1.0;
   for (int j = 0; j < d; ++j)
     out[static_cast<size_t>(r) * d + j] = __double2float_rn(__dmul_rn(static_cast<double>(row[j]), scale));
@@ -348,7 +369,7 @@ int knn_bruteforce(const float* x, int n, int d, int K, int segments, void* scra
   int* pi = reinterpret_cast<int*>(pd + static_cast<size_t>(segments) * n * K);
   const int e = launch_segments<false, false>(x, n, d, K, segments, nullptr, nullptr, nullptr, pd, pi, st);
   if (e != 0) return e;
-  knn_merge_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, K, segments, pd, pi, nullptr, nullptr, false, idx, dist);
+  knn_merge_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, K, segments, pd, pi, nullptr, nullptr, kOutSqrt, idx, dist);
   count_launch();
   return static_cast<int>(cudaGetLastError());
 }
@@ -361,7 +382,7 @@ int knn_bruteforce_rows(const float* x, int n, int d, int K, int segments, const
   int* pi = reinterpret_cast<int*>(pd + static_cast<size_t>(segments) * n * K);
   const int e = launch_segments<false, false>(x, n, d, K, segments, nullptr, rows, nrows, pd, pi, st);
   if (e != 0) return e;
-  knn_merge_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, K, segments, pd, pi, rows, nrows, false, idx, dist);
+  knn_merge_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, K, segments, pd, pi, rows, nrows, kOutSqrt, idx, dist);
   count_launch();
   return static_cast<int>(cudaGetLastError());
 }
@@ -375,7 +396,21 @@ int knn_fold_search(const float* x, int n, int d, int K, bool inner, const int* 
   const int e = inner ? launch_segments<true, true>(x, n, d, K, segments, folds, nullptr, nullptr, pd, pi, st)
                       : launch_segments<false, true>(x, n, d, K, segments, folds, nullptr, nullptr, pd, pi, st);
   if (e != 0) return e;
-  knn_merge_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, K, segments, pd, pi, nullptr, nullptr, true, idx, dist);
+  knn_merge_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, K, segments, pd, pi, nullptr, nullptr, kOutRaw, idx, dist);
+  count_launch();
+  return static_cast<int>(cudaGetLastError());
+}
+
+int knn_bruteforce_inner(const float* x, int n, int d, int K, int metric, int segments, void* scratch, int* idx,
+                         float* dist, cudaStream_t st) {
+  if (segments < 1) segments = 1;
+  if (segments > kMaxSegments) segments = kMaxSegments;
+  float* pd = static_cast<float*>(scratch);
+  int* pi = reinterpret_cast<int*>(pd + static_cast<size_t>(segments) * n * K);
+  const int e = launch_segments<true, false>(x, n, d, K, segments, nullptr, nullptr, nullptr, pd, pi, st);
+  if (e != 0) return e;
+  knn_merge_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, K, segments, pd, pi, nullptr, nullptr,
+                                                   metric == 0 ? kOutCosine : kOutInner, idx, dist);
   count_launch();
   return static_cast<int>(cudaGetLastError());
 }

@@ -41,7 +41,16 @@ int bf16_split_rows(const float* x, int n, int d, int dp, uint16_t* xh, uint16_t
 int knn_fold_search(const float* x, int n, int d, int K, bool inner, const int* folds, int segments, void* scratch,
                     int* idx, float* dist, cudaStream_t st);
 
-// Cosine search matrix: mode 0 = knncv.cpp:85-108, mode 1 = core.cpp:166-195.
+// Global exact graph under the inner product (metric 1) or cosine (metric 0,
+// on rows already scaled by normalize_rows mode 2): for each row the K other
+// rows of smallest internal distance, minus the inner product (float chain in
+// coordinate order), ties to the smaller row; reported distance 1 + v
+// (inner product) or max(0, 1 + v) (cosine).  Scratch as knn_bruteforce.
+int knn_bruteforce_inner(const float* x, int n, int d, int K, int metric, int segments, void* scratch, int* idx,
+                         float* dist, cudaStream_t st);
+
+// Cosine search matrix: mode 0 = knncv.cpp:85-108, mode 1 = core.cpp:166-195,
+// mode 2 = kodama_matrix.cpp:155-167.
 int normalize_rows(const float* x, int n, int d, int mode, float* out, cudaStream_t st);
 
 // Majority vote of every row over its K fold-wise neighbours (knncv.cpp:111-131).

@@ -20,7 +20,8 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 
 OPT_FIELDS = ("runs", "cycles", "landmarks", "splitting", "graph_neighbors", "folds",
-              "knn_k", "threads", "materialize", "classifier", "components", "apply_dissim", "first_run")
+              "knn_k", "threads", "materialize", "classifier", "components", "apply_dissim", "first_run",
+              "metric")
 
 _i32p = np.ctypeslib.ndpointer(np.int32, flags="C")
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C")
@@ -71,7 +72,7 @@ class MatrixResult:
 def matrix_options(**kw) -> np.ndarray:
     defaults = dict(runs=100, cycles=20, landmarks=10000, splitting=0, graph_neighbors=100,
                     folds=5, knn_k=30, threads=1, materialize=0, classifier=0, components=50,
-                    apply_dissim=1, first_run=1)
+                    apply_dissim=1, first_run=1, metric=2)
     defaults.update(kw)
     return np.array([defaults[f] for f in OPT_FIELDS], dtype=np.int32)
 
@@ -206,14 +207,15 @@ class CoreResult:
 
 def core_knn_graph(L, gidx, gdist, labels, *, index_base=-1, constrain=None, fixed=None, cycles=20,
                    k=10, folds=10, stratified=True, evolutionary=False, guarded=False,
-                   absorption=False, adaptive=True, seed=1, cv_seed=1) -> CoreResult:
-    """CoreKNNGraph_CPU."""
+                   absorption=False, adaptive=True, seed=1, cv_seed=1, metric=2) -> CoreResult:
+    """CoreKNNGraph_CPU; metric is KNNOptions::metric (0 cosine, 1 inner
+    product, 2 Euclidean): the vote score 1 - d or -(d*d)."""
     samples, gk = gidx.shape
     lab = np.ascontiguousarray(labels, np.int32)
     con = np.ascontiguousarray(constrain if constrain is not None else np.zeros(samples), np.int32)
     fix = np.ascontiguousarray(fixed if fixed is not None else np.zeros(samples), np.int32)
     copts = np.array([cycles, k, folds, int(stratified), int(evolutionary), int(guarded),
-                      int(absorption), int(adaptive)], np.int32)
+                      int(absorption), int(adaptive), metric], np.int32)
     out = dict(clbest=np.zeros(samples, np.int32), cvpredbest=np.zeros(samples, np.int32),
                folds=np.zeros(samples, np.int32), vect_acc=np.zeros(cycles, np.float64),
                vect_score=np.zeros(cycles, np.float64), proposal_size=np.zeros(cycles, np.int32),
@@ -365,7 +367,7 @@ def core_knn(L, x, labels, *, metric=2, constrain=None, fixed=None, cycles=20, k
     con = np.ascontiguousarray(constrain if constrain is not None else np.zeros(samples), np.int32)
     fix = np.ascontiguousarray(fixed if fixed is not None else np.zeros(samples), np.int32)
     copts = np.array([cycles, k, folds, int(stratified), int(evolutionary), int(guarded),
-                      int(absorption), int(adaptive)], np.int32)
+                      int(absorption), int(adaptive), metric], np.int32)
     out = dict(clbest=np.zeros(samples, np.int32), cvpredbest=np.zeros(samples, np.int32),
                folds=np.zeros(samples, np.int32), vect_acc=np.zeros(cycles, np.float64),
                vect_score=np.zeros(cycles, np.float64), proposal_size=np.zeros(cycles, np.int32),
@@ -395,6 +397,20 @@ def exact_knn(L, x, K, threads=1):
     dist = np.zeros((n, K), np.float32)
     rc = L.exact_knn(x.ctypes.data_as(ctypes.c_void_p), n, d, K, idx.ctypes.data_as(ctypes.c_void_p),
                      dist.ctypes.data_as(ctypes.c_void_p), threads)
+    if rc != 0:
+        raise RuntimeError(_err(L))
+    return idx, dist
+
+
+def exact_knn_metric(L, x, K, metric, threads=1):
+    """Exact graph under a metric (0 cosine, 1 inner product, 2 Euclidean):
+    zero-based indices and the reference's reported distances."""
+    x = np.ascontiguousarray(x, np.float32)
+    n, d = x.shape
+    idx = np.zeros((n, K), np.int32)
+    dist = np.zeros((n, K), np.float32)
+    rc = L.exact_knn_metric(x.ctypes.data_as(ctypes.c_void_p), n, d, K, int(metric),
+                            idx.ctypes.data_as(ctypes.c_void_p), dist.ctypes.data_as(ctypes.c_void_p), threads)
     if rc != 0:
         raise RuntimeError(_err(L))
     return idx, dist

@@ -473,7 +473,7 @@ struct VoteTable {
 };
 
 VoteTable build_vote_table(const int* gidx, const float* gdist, int samples, int gk, int index_base,
-                           const std::vector<int>& folds, int k) {
+                           const std::vector<int>& folds, int k, bool euclidean) {
   int mn = std::numeric_limits<int>::max(), mx = std::numeric_limits<int>::min();
   const size_t total = static_cast<size_t>(samples) * gk;
   for (size_t i = 0; i < total; ++i) {
@@ -501,7 +501,8 @@ VoteTable build_vote_table(const int* gidx, const float* gdist, int samples, int
       if (!std::isfinite(dd)) continue;
       const float dc = std::max(0.0f, dd);
       t.nb[static_cast<size_t>(r) * t.width + col] = id;
-      t.score[static_cast<size_t>(r) * t.width + col] = -(dc * dc);
+      // precompute_knn_cv_graph (core.cpp:672-677)
+      t.score[static_cast<size_t>(r) * t.width + col] = euclidean ? -(dc * dc) : 1.0f - dc;
       ++col;
     }
   }
@@ -997,8 +998,12 @@ int proposal_count(int G, int cycle, int cycles, bool adaptive, std::mt19937_64&
   return d(rng);
 }
 
+// DistanceMetric values (kodama.hpp:27-31)
+constexpr int kMetricCosine = 0, kMetricInner = 1, kMetricEuclidean = 2;
+
 struct CoreOpts {
   int cycles = 100, k = 30, folds = 10;
+  int metric = 2;  // knn.metric of the graph vote: 2 Euclidean (score -(d*d)), else 1 - d
   bool stratified = true, evolutionary = false, guarded = false, absorption = false, adaptive = true;
   bool coarsening = false;  // auto_class_coarsening (PLS-LDA classifier)
   uint64_t seed = 1, cv_seed = 1;
@@ -1188,7 +1193,8 @@ CoreOut core_knn_graph(const int* gidx, const float* gdist, int samples, int gk,
                        const std::vector<int>& init, const std::vector<int>& constrain,
                        const std::vector<int>& fixed_in, const CoreOpts& o) {
   const std::vector<int> folds = make_folds(init, constrain, o.folds, o.stratified, o.cv_seed);
-  const VoteTable table = build_vote_table(gidx, gdist, samples, gk, index_base, folds, o.k);
+  const VoteTable table = build_vote_table(gidx, gdist, samples, gk, index_base, folds, o.k,
+                                           o.metric == kMetricEuclidean);
   int nfold = 0;
   for (int f : folds) nfold = std::max(nfold, f + 1);
   std::vector<int> universe = init;
@@ -1211,14 +1217,13 @@ CoreOut core_knn_graph(const int* gidx, const float* gdist, int samples, int gk,
 // neighbours ranked by (distance, row).
 // ---------------------------------------------------------------------------
 
-constexpr int kMetricCosine = 0, kMetricInner = 1, kMetricEuclidean = 2;
-
 // Rows as searched (make_search_matrix): cosine rows multiplied in double by
 // 1 / ||row|| (when finite and positive) and rounded to float; other metrics
 // unchanged.  mode 0 sums the squares sequentially in double
 // (knncv.cpp:85-108); mode 1 is core.cpp:166-195's long double sum in the x86
 // 80-bit format (ext80.h: exact float squares, 64-bit significand sums)
-// rounded to double.
+// rounded to double; mode 2 is that sum with the row scaled in float
+// (kodama_matrix.cpp:155-167, the global graph of KODAMA.matrix).
 std::vector<float> search_matrix(const float* x, int n, int d, int metric, int mode) {
   std::vector<float> out(x, x + static_cast<size_t>(n) * d);
   if (metric != kMetricCosine) return out;
@@ -1238,6 +1243,14 @@ std::vector<float> search_matrix(const float* x, int n, int d, int metric, int m
       ss = finite ? ext80_to_double(acc) : std::numeric_limits<double>::infinity();
     }
     const double nrm = std::sqrt(ss);
+    if (mode == 2) {
+      // normalize_rows_for_cosine (kodama_matrix.cpp:155-167): the float row
+      // times the float rounding of 1 / norm; zero or non-finite norms skip
+      if (!(nrm > 0.0) || !std::isfinite(nrm)) continue;
+      const float scale = static_cast<float>(1.0 / nrm);
+      for (int j = 0; j < d; ++j) out[static_cast<size_t>(r) * d + j] = row[j] * scale;
+      continue;
+    }
     const double scale = nrm > 0.0 && std::isfinite(nrm) ? 1.0 / nrm : 1.0;
     for (int j = 0; j < d; ++j)
       out[static_cast<size_t>(r) * d + j] = static_cast<float>(static_cast<double>(row[j]) * scale);
@@ -1260,6 +1273,46 @@ float canon_distance(const float* a, const float* b, int d, bool inner) {
     acc = acc + diff * diff;
   }
   return acc;
+}
+
+// The exact global graph under a metric (kgb_knn_graph_metric): cosine on the
+// rows of search_matrix mode 2, ranked by (canon_distance, row), self
+// excluded; reported distance native_knn_output_distance
+// (native_knn.cpp:1157-1164): max(0, 1 + v) for cosine, 1 + v for the inner
+// product.  The Euclidean graph is exact_knn.
+void exact_knn_metric(const float* x, int n, int d, int K, int metric, int* idx, float* dist, int threads) {
+  if (metric == kMetricEuclidean) {
+    exact_knn(x, n, d, K, idx, dist, threads);
+    return;
+  }
+  const std::vector<float> xs = search_matrix(x, n, d, metric, 2);
+  auto work = [&](int t) {
+    std::vector<std::pair<float, int>> row(static_cast<size_t>(n));
+    for (int i = t; i < n; i += threads) {
+      int m = 0;
+      for (int j = 0; j < n; ++j) {
+        if (j == i) continue;
+        row[m++] = {canon_distance(xs.data() + static_cast<size_t>(i) * d, xs.data() + static_cast<size_t>(j) * d, d,
+                                   true), j};
+      }
+      const int take = std::min(K, m);
+      std::partial_sort(row.begin(), row.begin() + take, row.begin() + m);
+      for (int c = 0; c < K; ++c) {
+        const size_t o = static_cast<size_t>(i) * K + c;
+        if (c < take) {
+          idx[o] = row[c].second;
+          const float v = 1.0f + row[c].first;
+          dist[o] = metric == kMetricCosine ? std::max(0.0f, v) : v;
+        } else {
+          idx[o] = -1;
+          dist[o] = std::numeric_limits<float>::infinity();
+        }
+      }
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int t = 0; t < threads; ++t) pool.emplace_back(work, t);
+  for (auto& th : pool) th.join();
 }
 
 // Every fold must keep training rows (knncv.cpp:142, core.cpp:705).
@@ -1402,7 +1455,7 @@ uint64_t fnv_hash(const std::vector<int>& v) {
 
 struct MatrixOpts {
   int runs, cycles, landmarks, splitting, graph_neighbors, folds, knn_k, threads, materialize,
-      classifier, components, apply_dissim, first_run;
+      classifier, components, apply_dissim, first_run, metric;
 };
 
 int majority_of(const std::vector<int>& v) {
@@ -1677,6 +1730,7 @@ void kodama_matrix(const float* x, int n, int d, const int* gidx_in, const float
       co.adaptive = true;
       co.seed = seed + static_cast<uint64_t>(run);
       co.cv_seed = seed + static_cast<uint64_t>(run);
+      co.metric = o.metric;
       const CoreOut core = core_knn_graph(lidx.data(), ldist.data(), L, K, -1, init, constrain, xfix, co);
       // projection of non-landmarks (kodama_matrix.cpp:3221-3261, majority_label :169)
       ro.res.assign(static_cast<size_t>(n), 0);
@@ -1753,6 +1807,16 @@ int orc_last_error(char* buf, int len) {
 int orc_exact_knn(const float* x, int n, int d, int K, int* idx, float* dist, int threads) {
   try {
     orc::exact_knn(x, n, d, K, idx, dist, std::max(1, threads));
+    return 0;
+  } catch (const std::exception& e) {
+    orc::g_error = e.what();
+    return 1;
+  }
+}
+
+int orc_exact_knn_metric(const float* x, int n, int d, int K, int metric, int* idx, float* dist, int threads) {
+  try {
+    orc::exact_knn_metric(x, n, d, K, metric, idx, dist, std::max(1, threads));
     return 0;
   } catch (const std::exception& e) {
     orc::g_error = e.what();
@@ -1865,6 +1929,7 @@ int orc_core_knn_graph(
     o.guarded = copts[5] != 0;
     o.absorption = copts[6] != 0;
     o.adaptive = copts[7] != 0;
+    o.metric = copts[8];
     o.seed = seed;
     o.cv_seed = cv_seed;
     std::vector<int> lab(labels, labels + samples);
@@ -1965,7 +2030,7 @@ int orc_kodama_matrix_graph_data_ex(
   const int* starting, const int* constrain, const int* fixed
 ) {
   try {
-    orc::MatrixOpts mo{o[0], o[1], o[2], o[3], o[4], o[5], o[6], o[7], o[8], o[9], o[10], o[11], o[12]};
+    orc::MatrixOpts mo{o[0], o[1], o[2], o[3], o[4], o[5], o[6], o[7], o[8], o[9], o[10], o[11], o[12], o[13]};
     if (timings) for (int i = 0; i < 6; ++i) timings[i] = 0.0;
     orc::kodama_matrix(x, n, d, gidx, gdist, gk, index_base, mo, seed, res, acc, v,
                        reinterpret_cast<uint64_t*>(hashes), run_counters, cycle_diag, out_idx, out_dist, out_k,

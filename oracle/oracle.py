@@ -33,6 +33,7 @@ core_knn_graph = _bind(_b.core_knn_graph)
 dissimilarity = _bind(_b.dissimilarity)
 exact_knn = _bind(_b.exact_knn)
 exact_knn_rows = _bind(_b.exact_knn_rows)
+exact_knn_metric = _bind(_b.exact_knn_metric)
 kmeans = _bind(_b.kmeans)
 dot_x86 = _bind(_b.dot_x86)
 quota_sample = _bind(_b.quota_sample)

@@ -25,8 +25,14 @@ thread_local std::string g_error;
 enum Opt {
   O_RUNS = 0, O_CYCLES, O_LANDMARKS, O_SPLITTING, O_GRAPH_NEIGHBORS, O_FOLDS,
   O_KNN_K, O_THREADS, O_MATERIALIZE, O_CLASSIFIER, O_COMPONENTS, O_APPLY_DISSIM,
+  O_FIRST_RUN, O_METRIC,
   O_COUNT
 };
+
+kodama::DistanceMetric metric_of(int m) {
+  return m == 0 ? kodama::DistanceMetric::Cosine :
+    (m == 1 ? kodama::DistanceMetric::InnerProduct : kodama::DistanceMetric::Euclidean);
+}
 
 kodama::KODAMAMatrixOptions matrix_options(const int* o, unsigned long long seed) {
   kodama::KODAMAMatrixOptions opt;
@@ -43,7 +49,7 @@ kodama::KODAMAMatrixOptions matrix_options(const int* o, unsigned long long seed
   opt.components = o[O_COMPONENTS];
   opt.apply_kodama_dissimilarity = o[O_APPLY_DISSIM] != 0;
   opt.seed = seed;
-  opt.metric = kodama::DistanceMetric::Euclidean;
+  opt.metric = metric_of(o[O_METRIC]);
   opt.backend = kodama::Backend::CPU;
   opt.compute_visual_init = false;
   opt.progress = false;
@@ -246,7 +252,7 @@ int ref_core_knn_graph(
     opt.guarded_diversity = copts[5] != 0;
     opt.many_to_one_absorption = copts[6] != 0;
     opt.adaptive_proposal_size = copts[7] != 0;
-    opt.knn.metric = kodama::DistanceMetric::Euclidean;
+    opt.knn.metric = metric_of(copts[8]);
     opt.seed = seed;
     opt.knn.cv.seed = cv_seed;
     std::vector<int> lab(labels, labels + samples);

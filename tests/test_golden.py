@@ -121,7 +121,7 @@ def test_gpu_core_golden(kg, case):
                                 np.array([o["cv_seed"]], np.uint64), cycles=o["cycles"], k=o["k"],
                                 folds=o["folds"], stratified=o["stratified"],
                                 evolutionary_search=o["evolutionary"], guarded_diversity=o["guarded"],
-                                many_to_one_absorption=o["absorption"], index_base=0)
+                                many_to_one_absorption=o["absorption"], index_base=0, metric="euclidean")
     G.check_core(case, out[0], folds_attr="fold_assignments")
 
 
@@ -156,7 +156,8 @@ def test_gpu_core_graph_input_golden(kg, case):
     x, labels, con, fix = G.knn_inputs(case["input"])
     gi, gd = kg.knn_graph(x, case["K"])
     assert G.sha(gi) + ":" + G.sha(gd) == case["graph_sha256"], "exact graph"
-    r = kg.CoreKNNGraph(gi, gd, labels, index_base=0, constrain=con, fixed=fix, **_gpu_core_kw(case["options"]))
+    r = kg.CoreKNNGraph(gi, gd, labels, index_base=0, constrain=con, fixed=fix, metric="euclidean",
+                        **_gpu_core_kw(case["options"]))
     G.check_core(case, r, folds_attr="fold_assignments")
 
 

@@ -83,7 +83,7 @@ def test_constrained_fixed_core_matches_oracle(kg, orc, graph):
     ev = dict(evolutionary_search=True, guarded_diversity=True, many_to_one_absorption=True)
     if graph:
         gi, gd = kg.knn_graph(x, 25)
-        a = kg.CoreKNNGraph(gi, gd, init, index_base=0, constrain=con, fixed=fix, **kw, **ev)
+        a = kg.CoreKNNGraph(gi, gd, init, index_base=0, constrain=con, fixed=fix, metric="euclidean", **kw, **ev)
         b = orc.core_knn_graph(gi, gd, init, index_base=0, constrain=con, fixed=fix, evolutionary=True,
                                guarded=True, absorption=True, **kw)
     else:

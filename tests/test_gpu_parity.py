@@ -116,7 +116,8 @@ def test_core_knn_graph_batch(kg, orc, mode):
     labels = np.stack([rng.integers(1, 2 + 3 * p, 2000) for p in range(problems)]).astype(np.int32) * 3 - 5
     seeds = np.arange(10, 10 + problems, dtype=np.uint64)
     cv_seeds = np.arange(100, 100 + problems, dtype=np.uint64)
-    out = kg.CoreKNNGraph_batch(gi, gd, labels, seeds, cv_seeds, cycles=25, k=10, folds=7, index_base=0, **mode)
+    out = kg.CoreKNNGraph_batch(gi, gd, labels, seeds, cv_seeds, cycles=25, k=10, folds=7, index_base=0,
+                                metric="euclidean", **mode)
     omode = dict(evolutionary=mode["evolutionary_search"], guarded=mode["guarded_diversity"],
                  absorption=mode["many_to_one_absorption"], stratified=mode["stratified"],
                  adaptive=mode.get("adaptive_proposal_size", True))

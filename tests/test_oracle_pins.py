@@ -24,6 +24,48 @@ def test_matrix_spirals_vs_reference(orc):
 
 
 @needs_ref
+@pytest.mark.parametrize("metric", [0, 1])
+def test_matrix_metric_vs_reference(orc, metric):
+    """KODAMA.matrix under the cosine (0) and inner-product (1) metrics on
+    the exact graph of that metric: the vote scores 1 - d (core.cpp:672-677)
+    and the caller graph's distances (1 - <x,y> can be negative for the
+    inner product) clamped at zero (kodama_matrix.cpp:1292-1330)."""
+    # overlapping clusters and knn.k = 4: count ties are frequent, and the
+    # two score rules order some tied sums differently; scaled by 0.2 the
+    # inner-product graph has both negative (clamped) and positive distances
+    x, _ = datasets.gaussian_mixture(n=1800, d=12, clusters=6, mean_scale=1.0, seed=8)
+    x = (x * 0.2).astype(np.float32)
+    gi, gd = orc.exact_knn_metric(x, 30, metric, threads=8)
+    if metric == 1:
+        assert (gd < 0).any() and (gd > 0).any(), "the inner-product case should exercise clamping"
+    kw = dict(runs=5, cycles=12, landmarks=10000, splitting=20, graph_neighbors=30, folds=10, knn_k=4,
+              threads=4, materialize=1, metric=metric)
+    r = ref.kodama_matrix_graph_data(x, gi, gd, 0, seed=99, **kw)
+    o = orc.kodama_matrix_graph_data(x, gi, gd, 0, seed=99, **kw)
+    for f in ("res", "acc", "v", "hashes", "run_counters", "cycle_diag", "knn_idx", "knn_dist"):
+        assert np.array_equal(getattr(r, f), getattr(o, f)), f
+    e = orc.kodama_matrix_graph_data(x, gi, gd, 0, seed=99, **dict(kw, metric=2))
+    assert not (np.array_equal(e.res, o.res) and np.array_equal(e.cycle_diag, o.cycle_diag)), \
+        "the score rule should change the evolution"
+
+
+@needs_ref
+def test_core_knn_graph_cosine_vs_reference(orc):
+    """CoreKNNGraph with KNNOptions' default cosine metric (score 1 - d)."""
+    x, _ = datasets.gaussian_mixture(n=1200, d=16, seed=6)
+    gi, gd = orc.exact_knn_metric(x, 25, 0, threads=8)
+    labels = np.random.default_rng(3).integers(1, 6, 1200).astype(np.int32)
+    kw = dict(index_base=0, cycles=15, k=10, folds=5, seed=3, cv_seed=4, evolutionary=True, guarded=True,
+              absorption=True, stratified=False, metric=0)
+    a = ref.core_knn_graph(gi, gd, labels, **kw)
+    b = orc.core_knn_graph(gi, gd, labels, **kw)
+    for f in ("clbest", "cvpredbest", "folds", "vect_acc", "vect_score", "proposal_size",
+              "active_classes", "flags", "counters"):
+        assert np.array_equal(getattr(a, f), getattr(b, f)), f
+    assert a.accbest == b.accbest and a.scorebest == b.scorebest
+
+
+@needs_ref
 @pytest.mark.parametrize("constrained", [False, True])
 @pytest.mark.parametrize("evolutionary", [False, True])
 def test_core_knn_graph_vs_reference(orc, constrained, evolutionary):
