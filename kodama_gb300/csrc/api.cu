@@ -155,8 +155,14 @@ class Ctx {
     if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) fail(KGB_ECUDA, "no CUDA device is available");
     if (device < 0 || device >= count) fail(KGB_EINVAL, "CUDA device ordinal out of range");
     ck(cudaSetDevice(device), "cudaSetDevice");
-    ck(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
-    ck(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking), "cudaStreamCreate");
+    // the call's chain of dependent stages runs at the highest priority; bulk
+    // work that overlaps it (the exact graph) at the lowest, so the block
+    // scheduler hands free SMs to the chain first
+    int least = 0, greatest = 0;
+    ck(cudaDeviceGetStreamPriorityRange(&least, &greatest), "stream priorities");
+    ck(cudaStreamCreateWithPriority(&stream_, cudaStreamNonBlocking, greatest), "cudaStreamCreate");
+    ck(cudaStreamCreateWithPriority(&side_, cudaStreamNonBlocking, greatest), "cudaStreamCreate");
+    ck(cudaStreamCreateWithPriority(&bg_, cudaStreamNonBlocking, least), "cudaStreamCreate");
     ck(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, device), "device attribute");
     cudaMemPool_t pool;
     if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
@@ -167,15 +173,43 @@ class Ctx {
   ~Ctx() {
     if (owns_streams_) {
       cudaStreamSynchronize(side_);  // side-stream work reads buffers freed below
+      cudaStreamSynchronize(bg_);
       for (void* p : bufs_) cudaFreeAsync(p, stream_);
       cudaStreamSynchronize(stream_);
     }
     for (int i = 0; i < nev_; ++i) cudaEventDestroy(ev_[i]);
     for (int i = 0; i < njoin_; ++i) cudaEventDestroy(join_[i]);
     if (owns_streams_) {
+      cudaStreamDestroy(bg_);
       cudaStreamDestroy(side_);
       cudaStreamDestroy(stream_);
     }
+  }
+  // Queues f's work on the low-priority background stream, after everything
+  // queued on the main stream so far: while f runs, stream() is that stream
+  // (launches and allocations of f go there).  Returns false, running
+  // nothing, in capture mode, where there is no background stream.  Timing
+  // events a and b (marks on the background stream) bracket f's work.
+  template <class F>
+  bool on_background(F&& f, int* a, int* b) {
+    if (bg_ == nullptr) return false;
+    const int e = mark();
+    ck(cudaStreamWaitEvent(bg_, ev_[e], 0), "cudaStreamWaitEvent");
+    std::swap(stream_, bg_);
+    *a = mark();
+    f();
+    *b = mark();
+    std::swap(stream_, bg_);
+    return true;
+  }
+  // The main stream waits for everything queued on the background stream.
+  void join_background() {
+    if (bg_ == nullptr) return;
+    if (njoin_ >= kMaxEvents) fail(KGB_EINTERNAL, "too many stream joins");
+    ck(cudaEventCreateWithFlags(&join_[njoin_], cudaEventDisableTiming), "cudaEventCreate");
+    ck(cudaEventRecord(join_[njoin_], bg_), "cudaEventRecord");
+    ck(cudaStreamWaitEvent(stream_, join_[njoin_], 0), "cudaStreamWaitEvent");
+    ++njoin_;
   }
   bool capturing() const { return arena_ != nullptr; }
   // Capture mode: joins the side stream and frees every allocation inside the
@@ -262,6 +296,7 @@ class Ctx {
     if (capturing()) fail(KGB_EINTERNAL, "host synchronisation inside a captured batch");
     ck(cudaStreamSynchronize(stream_), "stream synchronize");
     ck(cudaStreamSynchronize(side_), "stream synchronize");
+    if (bg_ != nullptr) ck(cudaStreamSynchronize(bg_), "stream synchronize");
   }
   cudaStream_t stream() const { return stream_; }
   int sms() const { return sms_; }
@@ -276,6 +311,7 @@ class Ctx {
   static constexpr int kMaxEvents = 32;
   cudaStream_t stream_ = nullptr;
   cudaStream_t side_ = nullptr;
+  cudaStream_t bg_ = nullptr;  // low-priority background stream (not in capture mode)
   CaptureArena* arena_ = nullptr;
   bool owns_streams_ = true;
   int sms_ = 1;
@@ -1045,11 +1081,15 @@ struct MatrixTail {
   std::vector<int> gi;
   std::vector<float> gd;
   int ev_start = -1, ev_atlas = -1, ev_graph = -1, ev_init = -1, ev_tables = -1, ev_evo0 = -1, ev_evo1 = -1,
-      ev_proj = -1, ev_dis = -1;
+      ev_proj = -1, ev_dis = -1, ev_bg0 = -1, ev_bg1 = -1;
+  bool graph_bg = false;  // the graph was built on the background stream (ev_bg0 .. ev_bg1)
 };
 
-// build_graph (may be empty): queues the kNN graph into d_gidx / d_gdist; it
-// runs right after the atlas k-means, beside the landmark planning.  Queues
+// build_graph (may be empty): queues the kNN graph into d_gidx / d_gdist.  It
+// needs only x, so outside a captured batch it runs on the low-priority
+// background stream from the start of the call, beside the atlas k-means, the
+// landmark planning and the landmark k-means, and is joined before anything
+// reads the graph; in a captured batch it runs right after the atlas.  Queues
 // the whole call; the results are read by matrix_finalize once the device
 // work is done (no host wait on the plain path, so a batch can capture it).
 void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_gidx, float* d_gdist, int K,
@@ -1073,6 +1113,10 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   if (!pls && knn_k > kgb::kMaxProjectK) fail(KGB_EINVAL, "knn.k too large for the projection kernel");
   if (pls && o->components < 1) fail(KGB_EINVAL, "PLSOptions::max_components must be positive.");
   cudaStream_t st = ctx.stream();
+
+  int ev_bg0 = -1, ev_bg1 = -1;
+  const bool graph_bg =
+      static_cast<bool>(build_graph) && ctx.on_background([&]() { build_graph(); }, &ev_bg0, &ev_bg1);
 
   // shared landmark atlas (kodama_matrix.cpp:3662-3734)
   float* d_pnorm = ctx.alloc<float>(n);
@@ -1110,7 +1154,7 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     ck_launch(kgb::kmeans_run(B, st), "atlas k-means");
   }
   const int ev_atlas = ctx.mark();
-  const bool graph_here = static_cast<bool>(build_graph);
+  const bool graph_here = static_cast<bool>(build_graph) && !graph_bg;
   if (graph_here) {
     build_graph();
     ev_graph = ctx.mark();
@@ -1365,6 +1409,7 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   int* d_res = nullptr;
   int ev_tables = 0, ev_evo0 = 0, ev_evo1 = 0, ev_proj = 0;
   int cstride = 16;
+  if (graph_bg) ctx.join_background();  // everything below may read the graph
   if (pls) {
     // PLS-LDA classifier (run_iteration, kodama_matrix.cpp:3105-3158, 3262-3276):
     // CorePLSLDA on the landmark rows of every run, PLSLDAPredict for the rest
@@ -1571,6 +1616,9 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   tail.fold_hash.resize(static_cast<size_t>(M));
   for (int r = 0; r < M; ++r) tail.fold_hash[r] = fold_plans[r].fold_hash;
   tail.graph_here = graph_here;
+  tail.graph_bg = graph_bg;
+  tail.ev_bg0 = ev_bg0;
+  tail.ev_bg1 = ev_bg1;
   tail.ev_start = ev_start;
   tail.ev_atlas = ev_atlas;
   tail.ev_graph = ev_graph;
@@ -1591,7 +1639,12 @@ void matrix_finalize(Ctx* ctx, MatrixTail& t, kgb_matrix_result* out, Clock& clk
   if (!t.v.empty()) std::memcpy(out->v, t.v.data(), sizeof(double) * t.v.size());
   const double t_dl = clk.lap();
   auto ms = [&](int a, int b) { return ctx == nullptr ? 0.0 : ctx->ms(a, b); };
-  if (t.graph_here) {
+  if (t.graph_bg) {
+    // the graph beside the atlas and the landmark initialisation
+    out->kernel_ms[0] = ms(t.ev_bg0, t.ev_bg1);
+    out->kernel_ms[1] = ms(t.ev_start, t.ev_atlas);
+    out->kernel_ms[2] = ms(t.ev_atlas, t.ev_init);
+  } else if (t.graph_here) {
     // order on the device: atlas, graph, landmark initialisation
     out->kernel_ms[0] = ms(t.ev_atlas, t.ev_graph);
     out->kernel_ms[1] = ms(t.ev_start, t.ev_atlas);
