@@ -137,21 +137,6 @@ int kgb_kodama_matrix(const float* x, int32_t n, int32_t d, const kgb_matrix_opt
 int kgb_kodama_matrix_resident(const float* x_device, int32_t n, int32_t d, const kgb_matrix_options* opt,
                                kgb_matrix_result* out);
 
-/* Replaces KODAMAMatrixFromGraph_CUDA (kodama.hpp:1242-1249,
- * kodama_matrix.cpp:4740-4760): KODAMA.matrix from a neighbour graph alone
- * (n x gk; index_base 0, 1 or -1 = detect).  As in the reference the
- * Laplacian features of the graph (graph_laplacian_operator_features,
- * kodama_matrix.cpp:1575-1603; feature_components <= 0 -> options
- * components, max(8, feature_steps) iterations, opt->seed) are computed on
- * the host and stand in for the data of the graph-input path.
- * kgb_graph_features returns those features alone (n x min(components, n),
- * row-major; host computation, no device needed). */
-int kgb_graph_features(const int32_t* gidx, const float* gdist, int32_t n, int32_t gk, int32_t index_base,
-                       int32_t components, int32_t steps, uint64_t seed, float* out);
-int kgb_kodama_matrix_from_graph(const int32_t* gidx, const float* gdist, int32_t n, int32_t gk,
-                                 int32_t index_base, int32_t feature_components, int32_t feature_steps,
-                                 const kgb_matrix_options* opt, kgb_matrix_result* out);
-
 /* Resident graph: KODAMAGraph_CUDA (kodama.hpp:1112-1115,
  * kodama_matrix.cpp:4057-4216) keeps the data and the exact kNN graph
  * (neighbors columns, at most n - 1) in device memory behind an opaque

@@ -25,7 +25,7 @@ import numpy as np
 
 from . import _native as N
 
-__all__ = ["KODAMA_graph_features", "PLSDACV", "KODAMAGraph", "KODAMA_matrix_batch", "train_proposal", "proposal_gradient", "proposal_predict", "KODAMA_matrix", "CoreKNNGraph", "CoreKNNGraph_batch", "knn_graph",
+__all__ = ["PLSDACV", "KODAMAGraph", "KODAMA_matrix_batch", "train_proposal", "proposal_gradient", "proposal_predict", "KODAMA_matrix", "CoreKNNGraph", "CoreKNNGraph_batch", "knn_graph",
            "KODAMADissimilarityInPlace", "PLSLDACV", "PLSLDAPredict", "CorePLSLDA", "PLSCVResult", "MatrixResult", "CoreResult", "EvolutionPolicy",
            "library_path", "version", "launch_count"]
 
@@ -116,20 +116,6 @@ def _matrix_options(runs, cycles, landmarks, splitting, graph_neighbors, folds, 
                            policy=pol._c())
 
 
-def KODAMA_graph_features(gidx, gdist, *, index_base=-1, components=50, steps=3, seed=1234):
-    """KODAMAGraphFeatures: Laplacian features of a neighbour graph (host
-    computation, as the reference's CUDA graph-only path does)."""
-    gi = np.ascontiguousarray(gidx, dtype=np.int32)
-    gd = np.ascontiguousarray(gdist, dtype=np.float32)
-    if gi.shape != gd.shape or gi.ndim != 2:
-        raise ValueError("NeighborGraph indices/distances size must equal samples * neighbors.")
-    n = gi.shape[0]
-    out = np.zeros((n, max(1, min(components, n))), np.float32)
-    N.check(N.load().kgb_graph_features(_ptr(gi), _ptr(gd), n, gi.shape[1], index_base, components, steps,
-                                        ctypes.c_uint64(seed), _ptr(out)))
-    return out
-
-
 class KODAMAGraph:
     """KODAMAGraph with backend="cuda" (kgb_graph_create): the data and its
     exact kNN graph kept resident on the device; ``matrix`` runs
@@ -188,8 +174,7 @@ def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitt
                   policy="full", res_out=None, first_run=1, classifier="knn",
                   components=50, proposal_weights=None, snapshot_cycle=None,
                   proposal_greedy=False, starting_labels=None, constrain=None,
-                  fixed=None, _handle=None, graph_only=False, feature_components=0,
-                  feature_steps=3, metric="euclidean") -> MatrixResult:
+                  fixed=None, _handle=None, metric="euclidean") -> MatrixResult:
     """KODAMA.matrix on the GPU with the kNN (``classifier="knn"``) or PLS-LDA
     (``classifier="pls"``, ``components`` latent components) classifier.
     ``proposal_weights`` (the 4801 parameters of ``train_proposal``) selects
@@ -217,11 +202,7 @@ def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitt
     Defaults are those of KODAMAMatrixOptions (kodama.hpp:535-570).
     """
     x_dev = None
-    if graph_only:
-        if graph is None:
-            raise ValueError("graph_only needs graph=(indices, distances)")
-        n, d = np.asarray(graph[0]).shape[0], 1
-    elif _handle is not None:
+    if _handle is not None:
         n, d = _handle.n, _handle.d
     elif hasattr(x, "is_cuda") and x.is_cuda:
         if graph is not None:
@@ -296,14 +277,7 @@ def KODAMA_matrix(x, graph=None, *, runs=100, cycles=20, landmarks=10000, splitt
         out.knn_dist = kdist.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
     out.knn_cap = cap
     lib = N.load()
-    if graph_only:
-        gi = np.ascontiguousarray(graph[0], dtype=np.int32)
-        gd = np.ascontiguousarray(graph[1], dtype=np.float32)
-        if gi.shape != gd.shape or gi.shape[0] != n:
-            raise ValueError("NeighborGraph indices/distances size must equal samples * neighbors.")
-        rc = lib.kgb_kodama_matrix_from_graph(_ptr(gi), _ptr(gd), n, gi.shape[1], index_base, feature_components,
-                                              feature_steps, ctypes.byref(opt), ctypes.byref(out))
-    elif _handle is not None:
+    if _handle is not None:
         rc = lib.kgb_kodama_matrix_graph(_handle._h, ctypes.byref(opt), ctypes.byref(out))
     elif x_dev is not None:
         rc = lib.kgb_kodama_matrix_resident(ctypes.c_void_p(x_dev.data_ptr()), n, d, ctypes.byref(opt),

@@ -21,8 +21,6 @@ EXPORTED = (
     "kgb_kodama_matrix_from_graph_data",
     "kgb_kodama_matrix_resident",
     "kgb_kodama_matrix_batch",
-    "kgb_graph_features",
-    "kgb_kodama_matrix_from_graph",
     "kgb_graph_create",
     "kgb_graph_info",
     "kgb_graph_materialize",
@@ -163,9 +161,6 @@ def load():
                                                ctypes.POINTER(MatrixResult)]
     lib.kgb_kodama_matrix_batch.argtypes = [ctypes.POINTER(MatrixProblem), i32, ctypes.POINTER(BatchOptions),
                                             ctypes.POINTER(BatchReport)]
-    lib.kgb_graph_features.argtypes = [P, P, i32, i32, i32, i32, i32, ctypes.c_uint64, P]
-    lib.kgb_kodama_matrix_from_graph.argtypes = [P, P, i32, i32, i32, i32, i32, ctypes.POINTER(MatrixOptions),
-                                                 ctypes.POINTER(MatrixResult)]
     lib.kgb_graph_create.argtypes = [P, i32, i32, i32, i32, i32, ctypes.POINTER(ctypes.c_void_p)]
     lib.kgb_graph_info.argtypes = [P, P, P, P]
     lib.kgb_graph_materialize.argtypes = [P, P, P]

@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libkodama_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["api.cu", "evolve.cu", "kmeans.cu", "graph_ops.cu", "knn.cu", "knn_tc.cu", "noalloc.cu", "pls.cu", "mlp.cu", "plan.cu", "host_plan.cpp", "graph_features.cpp"]
+SOURCES = ["api.cu", "evolve.cu", "kmeans.cu", "graph_ops.cu", "knn.cu", "knn_tc.cu", "noalloc.cu", "pls.cu", "mlp.cu", "plan.cu", "host_plan.cpp"]
 
 
 def _nvcc() -> str:

@@ -14,7 +14,6 @@
 #include "pls.cuh"
 #include "mlp.cuh"
 #include "plan.cuh"
-#include "graph_features.h"
 
 #include <cuda_runtime.h>
 
@@ -2434,34 +2433,6 @@ int kgb_kodama_matrix_resident(const float* x_device, int32_t n, int32_t d, cons
 int kgb_kodama_matrix_batch(const kgb_matrix_problem* problems, int32_t count, const kgb_batch_options* options,
                             kgb_batch_report* report) {
   return guarded([&]() { batch_entry(problems, count, options, report); });
-}
-
-int kgb_graph_features(const int32_t* gidx, const float* gdist, int32_t n, int32_t gk, int32_t index_base,
-                       int32_t components, int32_t steps, uint64_t seed, float* out) {
-  return guarded([&]() {
-    if (gidx == nullptr || gdist == nullptr || out == nullptr) fail(KGB_EINVAL, "null pointer");
-    const std::vector<float> f = kgb::graph_laplacian_features(gidx, gdist, n, gk, index_base, components, steps, seed);
-    std::copy(f.begin(), f.end(), out);
-  });
-}
-
-int kgb_kodama_matrix_from_graph(const int32_t* gidx, const float* gdist, int32_t n, int32_t gk,
-                                 int32_t index_base, int32_t feature_components, int32_t feature_steps,
-                                 const kgb_matrix_options* opt, kgb_matrix_result* out) {
-  return guarded([&]() {
-    if (gidx == nullptr || gdist == nullptr || opt == nullptr || out == nullptr) fail(KGB_EINVAL, "null pointer");
-    validate_matrix_options(opt);
-    // KODAMAGraphFeatures (kodama_matrix.cpp:4621-4638): the feature count is
-    // graph_feature_components, else max(1, components)
-    const int comps = std::max(1, feature_components > 0 ? feature_components : std::max(1, opt->components));
-    Clock clk;
-    const std::vector<float> f =
-        kgb::graph_laplacian_features(gidx, gdist, n, gk, index_base, comps, feature_steps, opt->seed);
-    const double t_features = clk.lap();
-    const int p = static_cast<int>(f.size() / static_cast<size_t>(n));
-    matrix_entry(f.data(), false, n, p, gidx, gdist, gk, index_base, opt, out);
-    out->timings[0] += t_features;
-  });
 }
 
 int kgb_graph_create(const float* x, int32_t n, int32_t d, int32_t neighbors, int32_t metric, int32_t device,

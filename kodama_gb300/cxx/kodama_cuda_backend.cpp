@@ -154,7 +154,6 @@ struct MatrixCall {
   const float* x = nullptr;
   int n = 0, d = 0;
   const NeighborGraph* graph = nullptr;  // caller graph (graph-input path)
-  bool graph_only = false;               // KODAMAMatrixFromGraph: no data
 };
 
 KODAMAMatrixResult run_matrix(const MatrixCall& c, const std::vector<int>& starting, const std::vector<int>& con,
@@ -191,11 +190,7 @@ KODAMAMatrixResult run_matrix(const MatrixCall& c, const std::vector<int>& start
   out.knn_dist = kdist.empty() ? nullptr : kdist.data();
   out.knn_cap = cap;
   out.pls_counters = pls.data();
-  if (c.graph_only) {
-    check(kgb_kodama_matrix_from_graph(c.graph->indices.data(), c.graph->distances.data(), n, c.graph->neighbors,
-                                       base_of(c.graph->index_base), o.graph_feature_components,
-                                       o.graph_feature_steps, &ko, &out));
-  } else if (c.graph != nullptr) {
+  if (c.graph != nullptr) {
     check(kgb_kodama_matrix_from_graph_data(c.x, n, c.d, c.graph->indices.data(), c.graph->distances.data(),
                                             c.graph->neighbors, base_of(c.graph->index_base), &ko, &out));
   } else {
@@ -408,15 +403,25 @@ KODAMAMatrixResult KODAMAMatrixFromGraphData_CUDA(MatrixView x, const NeighborGr
   return run_matrix(c, starting_labels, constrain, fixed, options);
 }
 
+// As the reference's CUDA variant does (kodama_matrix.cpp:4743-4762): the
+// graph's Laplacian features by the reference's own host code
+// (KODAMAGraphFeatures_CPU), then the graph-input path on the device with the
+// features as the data.
 KODAMAMatrixResult KODAMAMatrixFromGraph_CUDA(const NeighborGraph& graph, int samples,
                                               const std::vector<int>& starting_labels,
                                               const std::vector<int>& constrain, const std::vector<int>& fixed,
                                               const KODAMAMatrixOptions& options) {
+  Timer feature_timer;
+  std::vector<float> features = KODAMAGraphFeatures_CPU(graph, samples, options);
+  const double feature_seconds = feature_timer.seconds();
   MatrixCall c;
+  c.x = features.data();
   c.n = samples;
+  c.d = static_cast<int>(features.size() / static_cast<std::size_t>(samples));
   c.graph = &graph;
-  c.graph_only = true;
-  return run_matrix(c, starting_labels, constrain, fixed, options);
+  KODAMAMatrixResult r = run_matrix(c, starting_labels, constrain, fixed, options);
+  r.graph_feature_seconds = feature_seconds;
+  return r;
 }
 
 // The exact graph, materialised on the host (knn, zero-based as

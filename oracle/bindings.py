@@ -136,41 +136,6 @@ def kodama_matrix_graph_data(L, x: np.ndarray, gidx: np.ndarray, gdist: np.ndarr
     return _wrap(n, opts, b)
 
 
-def graph_features(L, gidx: np.ndarray, gdist: np.ndarray, index_base: int, components: int, steps: int = 3,
-                   seed: int = 1234) -> np.ndarray:
-    """KODAMAGraphFeatures_CPU (reference library only)."""
-    n, gk = gidx.shape
-    p = max(1, min(components, n))
-    out = np.zeros((n, p), np.float32)
-    rc = L.graph_features(np.ascontiguousarray(gidx, np.int32).ctypes.data_as(ctypes.c_void_p),
-                          np.ascontiguousarray(gdist, np.float32).ctypes.data_as(ctypes.c_void_p), n, gk,
-                          index_base, components, steps, ctypes.c_ulonglong(seed),
-                          out.ctypes.data_as(ctypes.c_void_p))
-    if rc != 0:
-        raise RuntimeError(_err(L))
-    return out
-
-
-def kodama_matrix_from_graph(L, gidx: np.ndarray, gdist: np.ndarray, index_base: int, feature_components: int = 0,
-                             feature_steps: int = 3, seed: int = 1234, **kw) -> MatrixResult:
-    """KODAMAMatrixFromGraph_CPU (reference library only): a graph without data."""
-    n, gk = gidx.shape
-    opts = matrix_options(**kw)
-    opts[4] = opts[4] if opts[4] > 0 else 100
-    b = _alloc_matrix(n, opts)
-    rc = L.kodama_matrix_from_graph(
-        np.ascontiguousarray(gidx, np.int32).ctypes.data_as(ctypes.c_void_p),
-        np.ascontiguousarray(gdist, np.float32).ctypes.data_as(ctypes.c_void_p), n, gk, index_base,
-        feature_components, feature_steps, opts.ctypes.data_as(ctypes.c_void_p), ctypes.c_ulonglong(seed),
-        *[b[f].ctypes.data_as(ctypes.c_void_p) for f in
-          ("res", "acc", "v", "hashes", "run_counters", "cycle_diag", "out_idx", "out_dist")],
-        ctypes.byref(b["out_k"]), b["timings"].ctypes.data_as(ctypes.c_void_p),
-        b["pls"].ctypes.data_as(ctypes.c_void_p))
-    if rc != 0:
-        raise RuntimeError(_err(L))
-    return _wrap(n, opts, b)
-
-
 def kodama_matrix_raw(L, x: np.ndarray, seed: int = 1234, **kw) -> MatrixResult:
     """KODAMAMatrix_CPU: raw data, the reference's own HNSW graph."""
     x = np.ascontiguousarray(x, np.float32)

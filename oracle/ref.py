@@ -30,5 +30,3 @@ plsldapredict = _bind(_b.plsldapredict)
 knncv = _bind(_b.knncv)
 core_plslda = _bind(_b.core_plslda)
 core_knn = _bind(_b.core_knn)
-graph_features = _bind(_b.graph_features)
-kodama_matrix_from_graph = _bind(_b.kodama_matrix_from_graph)

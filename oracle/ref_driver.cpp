@@ -164,46 +164,6 @@ kodama::NeighborGraph make_graph(const int* gidx, const float* gdist, int n, int
   return g;
 }
 
-// KODAMAGraphFeatures_CPU (kodama.hpp:1191): out has n x min(components, n)
-// floats.
-int ref_graph_features(const int* gidx, const float* gdist, int n, int gk, int index_base, int components,
-                       int steps, unsigned long long seed, float* out) {
-  try {
-    kodama::KODAMAMatrixOptions opt;
-    opt.graph_feature_components = components;
-    opt.graph_feature_steps = steps;
-    opt.seed = seed;
-    opt.n_threads = 1;
-    const std::vector<float> f = kodama::KODAMAGraphFeatures_CPU(make_graph(gidx, gdist, n, gk, index_base), n, opt);
-    std::memcpy(out, f.data(), sizeof(float) * f.size());
-    return 0;
-  } catch (const std::exception& e) {
-    g_error = e.what();
-    return 1;
-  }
-}
-
-// KODAMAMatrixFromGraph_CPU (kodama.hpp:1197): a graph without data.
-int ref_kodama_matrix_from_graph(
-  const int* gidx, const float* gdist, int n, int gk, int index_base, int feature_components, int feature_steps,
-  const int* o, unsigned long long seed,
-  int* res, double* acc, double* v, unsigned long long* hashes, int* run_counters,
-  int* cycle_diag, int* out_idx, float* out_dist, int* out_k, double* timings, int* pls_counters
-) {
-  try {
-    auto opt = matrix_options(o, seed);
-    opt.graph_feature_components = feature_components;
-    opt.graph_feature_steps = feature_steps;
-    const auto r = kodama::KODAMAMatrixFromGraph_CPU(make_graph(gidx, gdist, n, gk, index_base), n, {}, {}, {}, opt);
-    export_matrix_result(r, n, opt.runs, opt.cycles, res, acc, v, hashes, run_counters,
-                         cycle_diag, out_idx, out_dist, out_k, timings, pls_counters);
-    return 0;
-  } catch (const std::exception& e) {
-    g_error = e.what();
-    return 1;
-  }
-}
-
 // KODAMAMatrix_CPU (kodama.hpp:1069): raw data, the reference's own HNSW graph.
 int ref_kodama_matrix_raw(
   const float* x, int n, int d, const int* o, unsigned long long seed,

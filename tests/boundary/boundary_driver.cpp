@@ -72,6 +72,7 @@ int main() {
   KODAMAGraphResult graph = KODAMAGraph(view, gcpu);
   report("KODAMAMatrix(graph)->CoreKNNGraph_CUDA", [&] { (void)KODAMAMatrix(view, graph, {}, {}, {}, cu); });
   report("KODAMAMatrixFromGraphData_CUDA", [&] { (void)KODAMAMatrixFromGraphData(view, graph.knn, {}, {}, {}, cu); });
+  report("KODAMAMatrixFromGraph_CUDA", [&] { (void)KODAMAMatrixFromGraph(graph.knn, n, {}, {}, {}, cu); });
 
   KNNOptions ko;
   ko.backend = Backend::CUDA;

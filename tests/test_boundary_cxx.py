@@ -3,7 +3,8 @@ built against the reference's own kodama.hpp and linked into the reference's
 C++ core in place of its *_CUDA stubs (oracle/build_boundary.sh).
 
 The driver (tests/boundary/boundary_driver.cpp) calls the reference's public
-dispatching functions (KODAMAMatrix, KODAMAGraph, KNNCV, CoreKNN, CorePLSLDA,
+dispatching functions (KODAMAMatrix, KODAMAGraph, KODAMAMatrixFromGraph --
+whose features the reference's own host code computes -- KNNCV, CoreKNN, CorePLSLDA,
 PLSLDACV, PLSDACV, PLSLDAPredict; KODAMAMatrix on a host graph, which calls
 CoreKNNGraph_CUDA per run; the CUDA proximity of KODAMADissimilarityInPlace)
 with Backend::CUDA.  Compiling proves the shim matches the reference's
@@ -24,7 +25,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 DRIVER = os.path.join(ROOT, "oracle", "_ref", "boundary", "boundary_driver")
 
 ENTRY_POINTS = ("KODAMAMatrix_CUDA", "KODAMAGraph_CUDA", "KODAMAMatrix(graph)->CoreKNNGraph_CUDA",
-                "KODAMAMatrixFromGraphData_CUDA", "KNNCV_CUDA", "CoreKNN_CUDA", "CorePLSLDA_CUDA", "PLSLDACV_CUDA",
+                "KODAMAMatrixFromGraphData_CUDA", "KODAMAMatrixFromGraph_CUDA", "KNNCV_CUDA", "CoreKNN_CUDA", "CorePLSLDA_CUDA", "PLSLDACV_CUDA",
                 "PLSDACV_CUDA", "PLSLDAPredict_CUDA", "apply_kodama_dissimilarity_cuda")
 
 

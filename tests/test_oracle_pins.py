@@ -189,40 +189,6 @@ def test_semi_matrix_vs_reference(orc, classifier, inputs):
         assert np.array_equal(getattr(a, f), getattr(b, f)), f
 
 
-def _feature_graph(n=1200, d=12, K=15, seed=61):
-    from oracle import oracle
-    x, _ = datasets.gaussian_mixture(n=n, d=d, clusters=6, mean_scale=3.0, seed=seed)
-    gi, gd = oracle.exact_knn(x, K, threads=8)
-    rng = np.random.default_rng(seed)
-    gi = gi.copy()
-    gi[rng.random(gi.shape) < 0.03] = -1  # a few missing entries
-    return gi, gd
-
-
-@needs_ref
-@pytest.mark.parametrize("base,components,steps", [(0, 8, 3), (1, 5, 10), (-1, 20, 8)])
-def test_graph_features_vs_reference(kg, base, components, steps):
-    # the library's host restatement of graph_laplacian_operator_features
-    gi, gd = _feature_graph()
-    g_in = np.where(gi >= 0, gi + 1, gi) if base == 1 else gi
-    a = ref.graph_features(g_in, gd, base, components, steps, seed=77)
-    b = kg.KODAMA_graph_features(g_in, gd, index_base=base, components=components, steps=steps, seed=77)
-    assert np.array_equal(a, b)
-
-
-@needs_ref
-def test_matrix_from_graph_vs_reference(kg, orc):
-    # KODAMAMatrixFromGraph = the graph-input path on the graph's features
-    gi, gd = _feature_graph()
-    kw = dict(runs=3, cycles=8, landmarks=10000, splitting=20, graph_neighbors=15, folds=5, knn_k=10,
-              threads=4, materialize=1, components=6)
-    a = ref.kodama_matrix_from_graph(gi, gd, 0, feature_components=0, feature_steps=3, seed=5, **kw)
-    f = kg.KODAMA_graph_features(gi, gd, index_base=0, components=6, steps=3, seed=5)
-    b = orc.kodama_matrix_graph_data(f, gi, gd, 0, seed=5, **kw)
-    for fld in ("res", "acc", "v", "hashes", "run_counters", "cycle_diag", "knn_idx", "knn_dist"):
-        assert np.array_equal(getattr(a, fld), getattr(b, fld)), fld
-
-
 def _clustered(n, d, seed):
     rng = np.random.default_rng(seed)
     sizes = [n // 3, n // 3, n - 2 * (n // 3)]
