@@ -164,41 +164,48 @@ __device__ void block_exclusive_scan(int* a, int n, Fixed& f) {
 constexpr int kProducerThreads = 320;
 __device__ __forceinline__ void producer_sync() { asm volatile("bar.sync 1, 320;" ::: "memory"); }
 
-__device__ void mt64_refill_group(Mt64State& g, int t) {
-  uint64_t v = 0;
-  if (t < kMtN - kMtM) v = mt64_mix(g.mt[t], g.mt[t + 1], g.mt[t + kMtM]);
-  producer_sync();
-  if (t < kMtN - kMtM) {
-    g.mt[t] = v;
-    g.out[t] = mt64_temper(v);
-  }
-  producer_sync();
-  if (t >= kMtN - kMtM && t < kMtN) {
-    v = t < kMtN - 1 ? mt64_mix(g.mt[t], g.mt[t + 1], g.mt[t - (kMtN - kMtM)])
-                     : mt64_mix(g.mt[kMtN - 1], g.mt[0], g.mt[kMtM - 1]);
-  }
-  producer_sync();
-  if (t >= kMtN - kMtM && t < kMtN) {
-    g.mt[t] = v;
-    g.out[t] = mt64_temper(v);
-  }
-  if (t == 0) g.pos = 0;
-  producer_sync();
-}
-
 // Copy the next `count` engine outputs into raw[start..] (producer group).
+// The outputs left in g.out are copied first; every whole block of 312 that
+// follows is regenerated with its tempered words written straight into raw
+// (g.out is only refreshed for the last block, whose tail later draws read).
 __device__ void produce_outputs_group(Mt64State& g, uint64_t* raw, int start, int count, int t) {
-  int done = 0;
+  const int pos0 = g.pos;
+  const int lead = min(kMtN - pos0, count);
+  for (int i = t; i < lead; i += kProducerThreads) raw[start + i] = g.out[pos0 + i];
+  int done = lead;
+  int pos = pos0 + lead;
   while (done < count) {
-    if (g.pos >= kMtN) mt64_refill_group(g, t);
-    const int pos = g.pos;
-    const int take = min(kMtN - pos, count - done);
-    for (int i = t; i < take; i += kProducerThreads) raw[start + done + i] = g.out[pos + i];
+    // one regeneration of the 312 state words; word k's output goes to
+    // raw[start + done + k] while done + k < count, else to g.out[k]
+    const int take = min(kMtN, count - done);
+    uint64_t v = 0;
+    if (t < kMtN - kMtM) v = mt64_mix(g.mt[t], g.mt[t + 1], g.mt[t + kMtM]);
     producer_sync();
-    if (t == 0) g.pos = pos + take;
+    if (t < kMtN - kMtM) {
+      g.mt[t] = v;
+      const uint64_t o = mt64_temper(v);
+      if (t < take) raw[start + done + t] = o;
+      if (take < kMtN) g.out[t] = o;
+    }
+    producer_sync();
+    if (t >= kMtN - kMtM && t < kMtN) {
+      v = t < kMtN - 1 ? mt64_mix(g.mt[t], g.mt[t + 1], g.mt[t - (kMtN - kMtM)])
+                       : mt64_mix(g.mt[kMtN - 1], g.mt[0], g.mt[kMtM - 1]);
+    }
+    producer_sync();
+    if (t >= kMtN - kMtM && t < kMtN) {
+      g.mt[t] = v;
+      const uint64_t o = mt64_temper(v);
+      if (t < take) raw[start + done + t] = o;
+      if (take < kMtN) g.out[t] = o;
+    }
+    // the next regeneration reads words this one wrote
     producer_sync();
     done += take;
+    pos = take;
   }
+  if (t == 0) g.pos = pos;
+  producer_sync();
 }
 
 // Swap targets J[i] of every step of the shuffle of G groups.  Warp 0 streams
@@ -578,16 +585,23 @@ __device__ int dirty_rows_block(const EvolveParams& P, const Smem& s, int prob) 
 }
 
 // Count labels of `lab` per code, first positions and distinct count.
-__device__ int label_census(const EvolveParams& P, const Smem& s, const uint16_t* lab, int C0) {
+// have_cnt: s.cnt already holds the counts of `lab` (absorption_block counted
+// the same labels and left them unchanged).  A thread's rows come in
+// increasing order and a first position only decreases, so a row at or past
+// the current first position of its code needs no atomicMin: the plain read
+// filters nearly all of them after the first rows of each code.
+__device__ int label_census(const EvolveParams& P, const Smem& s, const uint16_t* lab, int C0,
+                            bool have_cnt = false) {
   for (int c = threadIdx.x; c < C0; c += kThreads) {
-    s.cnt[c] = 0;
+    if (!have_cnt) s.cnt[c] = 0;
     s.firstpos[c] = 0x7fffffff;
   }
   __syncthreads();
+  volatile int* fp = s.firstpos;
   for (int r = threadIdx.x; r < P.L; r += kThreads) {
     const int code = lab[r];
-    atomicAdd(&s.cnt[code], 1);
-    atomicMin(&s.firstpos[code], r);
+    if (!have_cnt) atomicAdd(&s.cnt[code], 1);
+    if (r < fp[code]) atomicMin(&s.firstpos[code], r);
   }
   __syncthreads();
   int local = 0;
@@ -681,11 +695,20 @@ __device__ int absorption_block(const EvolveParams& P, const Smem& s, int prob, 
     s.bt[c] = -1;
   }
   __syncthreads();
+  // one atomic per row: the class sizes are the rows of the class x
+  // prediction table, and without fixed rows every row is movable
+  const bool any_fixed = s.f->fxd != nullptr;
   for (int r = threadIdx.x; r < P.L; r += kThreads) {
     const int a = s.cl[r];
-    atomicAdd(&s.cnt[a], 1);
     atomicAdd(&tr[a * C + pp[r]], 1);
-    if (s.f->fxd == nullptr || s.f->fxd[r] != 1) atomicAdd(&s.movable[a], 1);
+    if (any_fixed && s.f->fxd[r] != 1) atomicAdd(&s.movable[a], 1);
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < C0; c += kThreads) {
+    int sz = 0;
+    for (int q = 0; q < C0; ++q) sz += tr[c * C + q];
+    s.cnt[c] = sz;
+    if (!any_fixed) s.movable[c] = sz;
   }
   __syncthreads();
   int local = 0;
@@ -1157,10 +1180,12 @@ __device__ void evolve_problem(const EvolveParams& P, const Smem& s, int prob) {
     __syncthreads();
 
     int absorbed = 0;
+    bool cnt_of_cl = false;  // s.cnt holds the counts of s.cl
     if (P.pol_transition && P.absorption) {
       ++tr_att;
       absorbed = absorption_block(P, s, prob, s.curpred, C0);
       absorb_moves += absorbed;
+      cnt_of_cl = absorbed == 0;
     }
 
     {
@@ -1177,7 +1202,7 @@ __device__ void evolve_problem(const EvolveParams& P, const Smem& s, int prob) {
     for (int r = threadIdx.x; r < L; r += kThreads) ok += s.cl[r] == s.pred[r];
     ok = block_sum(ok, f);
     const double acc = __ddiv_rn(static_cast<double>(ok), n);
-    const int nc = label_census(P, s, s.cl, C0);
+    const int nc = label_census(P, s, s.cl, C0, cnt_of_cl);
     const double score = objective(P, s, prob, acc, nc, C0);
     ++proposals;
 
@@ -1382,11 +1407,20 @@ __device__ int transition_stats(const EvolveParams& P, const Smem& s, const uint
     s.movable[c] = 0;
   }
   __syncthreads();
+  // one atomic per row: the class sizes are the rows of the class x
+  // prediction table, and without fixed rows every row is movable
+  const bool any_fixed = s.f->fxd != nullptr;
   for (int r = threadIdx.x; r < P.L; r += kThreads) {
     const int a = s.cl[r];
-    atomicAdd(&s.cnt[a], 1);
     atomicAdd(&tr[a * C + pp[r]], 1);
-    if (s.f->fxd == nullptr || s.f->fxd[r] != 1) atomicAdd(&s.movable[a], 1);
+    if (any_fixed && s.f->fxd[r] != 1) atomicAdd(&s.movable[a], 1);
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < C0; c += kThreads) {
+    int sz = 0;
+    for (int q = 0; q < C0; ++q) sz += tr[c * C + q];
+    s.cnt[c] = sz;
+    if (!any_fixed) s.movable[c] = sz;
   }
   __syncthreads();
   int local = 0;
