@@ -22,7 +22,9 @@ cpu_baseline / --impl reference: the CPU restatement of the reference
          (parity_vs_oracle), outside the timed region.
 
 Launch: python bench.py [--gpus N --steps K --warmup W] [--impl reference]
-(N>1 under torchrun: every rank runs its own replica; weak scaling).
+(N>1 under torchrun: the M=100 runs of the one job are split across the
+ranks, the label blocks all-gathered over NCCL and the proximity applied on
+rank 0; strong scaling.  --sharded runs that path at N=1 too).
 """
 
 from __future__ import annotations
@@ -558,6 +560,123 @@ def learned_comparison(kg, x, x_dev, res_dev, local, kw, flush, plain_acc, plain
             "spearman_plain_other_seed": round(_spearman(plain_g2.knn_dist.ravel(), plain_g.knn_dist.ravel()), 4)}
 
 
+def run_gpu_sharded(args):
+    """The headline job on N GPUs of one node with its M runs split across the
+    ranks (strong scaling: the job is fixed, N grows).  Per step and rank:
+    KODAMA.matrix on its block of runs (first_run, count; the rank builds the
+    exact graph itself, runs draw only from seed + run id), an NCCL all_gather
+    of the label blocks (device tensors padded to the largest block), and on
+    rank 0 the co-label proximity of the graph over all M label rows on the
+    device (kgb_dissimilarity_inplace_device).  Timed between barriers, the
+    maximum over ranks.  With --sharded it also runs at N=1 (one rank), which
+    is how the path is exercised on a single GPU; there the result is
+    compared with the single-call job and the CPU restatement."""
+    import torch
+    import torch.distributed as dist
+
+    import kodama_gb300 as kg
+    from kodama_gb300 import build as kbuild
+    from kodama_gb300.distributed import shard
+
+    kbuild.build()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if not dist.is_initialized():
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        os.environ.setdefault("MASTER_PORT", "29541")
+        dist.init_process_group("nccl", rank=rank, world_size=world)
+    dev = f"cuda:{local}"
+    x = _data()
+    kw = _matrix_kw()
+    n, M, T = WORKLOAD["n"], WORKLOAD["runs"], WORKLOAD["cycles"]
+    counts = [shard(M, world, r)[1] for r in range(world)]
+    first, count = shard(M, world, rank)
+    cap = max(max(counts), 1)
+    block_kw = {k: v for k, v in kw.items() if k != "runs"}
+    x_dev = torch.from_numpy(x).to(dev)
+    x_pin = torch.from_numpy(x).pin_memory()
+    blk = torch.zeros((cap, n), dtype=torch.int32, device=dev)
+    gathered = [torch.empty_like(blk) for _ in range(world)]
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def job(xin):
+        """One job; rank 0 returns (full label matrix, corrected graph) on the device."""
+        r = None
+        if count > 0:
+            r = kg.KODAMA_matrix(xin, res_out=blk[:count], device=local, runs=count, first_run=first,
+                                 apply_dissimilarity=False, materialize_graph=rank == 0, **block_kw)
+        dist.all_gather(gathered, blk)
+        if rank != 0:
+            return None, r
+        full = torch.cat([g[:c] for g, c in zip(gathered, counts)]).contiguous()
+        gi = torch.from_numpy(r.knn_idx).to(dev)
+        gd = torch.from_numpy(r.knn_dist).to(dev)
+        kg.KODAMADissimilarityInPlace_device(gi, gd, full, device=local)
+        return (full, gi, gd), r
+
+    def timed(xfn, steps, d2h):
+        out, times, last = None, [], None
+        for _ in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            dist.barrier()
+            t0 = time.perf_counter()
+            out, last = job(xfn())
+            if rank == 0 and d2h:
+                # end to end: the label matrix and the corrected graph come back to the host
+                for t in out:
+                    t.cpu()
+            torch.cuda.synchronize()
+            dist.barrier()
+            t = torch.tensor([time.perf_counter() - t0], dtype=torch.float64, device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            times.append(float(t))
+        return out, last, float(np.mean(times))
+
+    def dev_input():
+        return x_dev
+
+    def host_input():
+        return x_pin.to(dev, non_blocking=True)
+
+    for _ in range(args.warmup):
+        job(x_dev)
+    launches0 = kg.launch_count()
+    with ClockSampler(local) as clocks:
+        out, last, value = timed(dev_input, args.steps, False)
+    launches = (kg.launch_count() - launches0) // max(1, args.steps)
+    _, _, e2e_v = timed(host_input, args.steps, True)
+    if rank != 0:
+        dist.barrier()
+        dist.destroy_process_group()
+        return
+    full, gi, gd = out
+    res_host = full.cpu().numpy()
+    line = {"metric": METRIC, "value": round(value, 5), "unit": "s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(value * 1000, 3), "higher_is_better": False,
+            "scaling": "strong", "vs_baseline": None, "dtype": "int32/f64", "data": "synthetic",
+            "config": _config({"parallelism": f"the {M} runs split over {world} GPU(s) ({counts} runs), "
+                                              "label blocks all-gathered over NCCL, proximity on rank 0"}),
+            "e2e": {"value": round(e2e_v, 5), "unit": "s", "h2d_bytes_per_step": world * x.nbytes + gi.numel() * 8,
+                    "d2h_bytes_per_step": M * n * 4 + gi.numel() * 8},
+            "gpu_launches": int(launches), "clocks": clocks.summary(),
+            "stage_ms_rank0": {k: round(v, 3) for k, v in last.kernel_ms.items()} if last is not None else None}
+    if world == 1:
+        # the sharded job equals the single-call job, labels and corrected graph
+        ref_call = kg.KODAMA_matrix(x, device=local, materialize_graph=True, **kw)
+        line["matches_single_call"] = bool(np.array_equal(res_host, ref_call.res) and
+                                           np.array_equal(gi.cpu().numpy(), ref_call.knn_idx) and
+                                           np.array_equal(gd.cpu().numpy(), ref_call.knn_dist))
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"], ref = cpu_baseline(x)
+            line["parity_vs_oracle"] = {"bit_exact": bool(np.array_equal(res_host, ref.res))}
+    print(json.dumps(line))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
 def run_gpu(args):
     import torch
 
@@ -677,6 +796,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-proposal comparison")
+    ap.add_argument("--sharded", action="store_true",
+                    help="split the runs across ranks even at N=1 (the N>1 path always does)")
     ap.add_argument("--workload", default="knn", choices=["knn", "pls", "batch", "learned100k"],
                     help="knn: the headline configuration; pls: the PLS-LDA configuration; batch: 256 uneven "
                          "problems in one captured CUDA graph; learned100k: learned vs plain at N=100000")
@@ -689,6 +810,8 @@ def main():
         run_gpu_pls(args)
     elif args.workload == "batch":
         run_gpu_batch(args)
+    elif args.workload == "knn" and (args.sharded or int(os.environ.get("WORLD_SIZE", "1")) > 1):
+        run_gpu_sharded(args)
     else:
         run_gpu(args)
 

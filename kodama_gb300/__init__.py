@@ -25,7 +25,7 @@ import numpy as np
 
 from . import _native as N
 
-__all__ = ["PLSDACV", "KODAMAGraph", "KODAMA_matrix_batch", "train_proposal", "proposal_gradient", "proposal_predict", "KODAMA_matrix", "CoreKNNGraph", "CoreKNNGraph_batch", "knn_graph",
+__all__ = ["KODAMADissimilarityInPlace_device", "PLSDACV", "KODAMAGraph", "KODAMA_matrix_batch", "train_proposal", "proposal_gradient", "proposal_predict", "KODAMA_matrix", "CoreKNNGraph", "CoreKNNGraph_batch", "knn_graph",
            "KODAMADissimilarityInPlace", "PLSLDACV", "PLSLDAPredict", "CorePLSLDA", "PLSCVResult", "MatrixResult", "CoreResult", "EvolutionPolicy",
            "library_path", "version", "launch_count"]
 
@@ -647,6 +647,25 @@ def KODAMADissimilarityInPlace(graph_idx: np.ndarray, graph_dist: np.ndarray, ru
     samples, gk = graph_idx.shape
     N.check(N.load().kgb_dissimilarity_inplace(_ptr(graph_idx), _ptr(graph_dist), samples, gk, _ptr(res),
                                                res.shape[0], device))
+
+
+def KODAMADissimilarityInPlace_device(graph_idx, graph_dist, run_labels, *, device: int = 0) -> None:
+    """KODAMADissimilarityInPlace on CUDA torch tensors (graph_idx int32 and
+    graph_dist float32 of shape (n, K), one-based, rewritten in place;
+    run_labels int32 of shape (runs, n)), on torch's current stream, through
+    kgb_dissimilarity_inplace_device: no device memory is allocated, at most
+    samples * runs = 4,194,240 labels and K = 2048."""
+    import torch
+
+    for t, dt in ((graph_idx, torch.int32), (graph_dist, torch.float32), (run_labels, torch.int32)):
+        if not (t.is_cuda and t.dtype == dt and t.is_contiguous()):
+            raise ValueError("graph_idx / graph_dist / run_labels must be contiguous CUDA int32 / float32 / int32")
+    n, k = int(graph_idx.shape[0]), int(graph_idx.shape[1])
+    stream = torch.cuda.current_stream(device)
+    N.check(N.load().kgb_dissimilarity_inplace_device(
+        ctypes.c_void_p(graph_idx.data_ptr()), ctypes.c_void_p(graph_dist.data_ptr()), n, k,
+        ctypes.c_void_p(run_labels.data_ptr()), int(run_labels.shape[0]), device,
+        ctypes.c_void_p(stream.cuda_stream)))
 
 
 def _pls_options(folds, stratified, max_components, fixed_components, center, scale, cv_seed, device):
