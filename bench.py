@@ -57,7 +57,7 @@ BATCH_METRIC = "256-problem uneven KODAMA.matrix batch wall-s (M=50, Tcycle=50 e
 BATCH_KW = dict(runs=50, cycles=50, knn_k=10, components=5, graph_neighbors=30, folds=10, seed=1234)
 # DRAM bytes (read + write) of one evolution-kernel launch, scaled from the
 # ncu capture summarised in profiles/evolve_kernel_cfg2.md (None until captured).
-EVOLVE_TRAFFIC_BYTES = 503518976
+EVOLVE_TRAFFIC_BYTES = 484564992
 
 
 CONFIG_DESC = ("KODAMA.matrix kNN N=20000 d=50 (12-cluster Gaussian mixture), M=100 runs, "
@@ -258,6 +258,29 @@ def pls_cpu_baseline(x, threads=None):
              "mean_final_cv_acc": round(float(np.mean(r.acc)), 6)}, r)
 
 
+def pls_fp64_check(x):
+    """The float32 PLS-LDA arithmetic (reproduced bit for bit on the GPU)
+    against an FP64 restatement of one 10-fold PLSLDACV on the workload's
+    data (5 components, the 8 classes of the generator, and the same labels
+    with 20% of them redrawn): label disagreements and the float64 relative
+    LDA margin where they occur (oracle/pls_fp64.py)."""
+    from kodama_gb300 import datasets
+    from oracle import oracle, pls_fp64
+    _, y = datasets.low_rank(n=PLS_WORKLOAD["n"], d=PLS_WORKLOAD["d"], seed=3)
+    rng = np.random.default_rng(0)
+    out = {}
+    for name, noise in (("true_classes", 0.0), ("labels_20pct_redrawn", 0.2)):
+        lab = y.copy()
+        flip = rng.random(len(y)) < noise
+        lab[flip] = rng.integers(1, 9, int(flip.sum()))
+        pred, folds, _, _, _ = oracle.plsldacv(x, lab, folds=PLS_WORKLOAD["folds"], stratified=False,
+                                               max_components=PLS_WORKLOAD["components"],
+                                               fixed_components=PLS_WORKLOAD["components"],
+                                               threads=os.cpu_count() or 1, cv_seed=7)
+        out[name] = pls_fp64.compare(oracle._LIB, x, lab, folds, pred, PLS_WORKLOAD["components"])
+    return out
+
+
 def run_gpu_pls(args):
     import torch
 
@@ -323,6 +346,7 @@ def run_gpu_pls(args):
     if not args.no_cpu_baseline:
         line["cpu_baseline"], ref = pls_cpu_baseline(x)
         line["parity_vs_oracle"] = _parity(res_dev.cpu().numpy(), r.acc, r.v, r.run_hashes, r.run_counters, ref)
+        line["fp64_check"] = pls_fp64_check(x)
     print(json.dumps(line))
     if "parity_vs_oracle" in line and not line["parity_vs_oracle"]["bit_exact"]:
         sys.exit("GPU result differs from the CPU restatement on the timed workload")

@@ -330,7 +330,7 @@ __device__ int final_position_of(const Smem& s, int e) {
 // (smaller magnitude first for non-positive scores, larger for non-negative);
 // otherwise the double sums are formed in neighbour order.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ int vote_tiebreak(int code, unsigned tied, const float* scrow, int w, int lane) {
+__device__ __noinline__ int vote_tiebreak(int code, unsigned tied, const float* scrow, int w, int lane) {
   const float my = lane < w ? scrow[lane] : 0.0f;
   const uint32_t bits = __float_as_uint(my);
   const uint32_t ef = (bits >> 23) & 0xffu;
@@ -460,6 +460,44 @@ __device__ __forceinline__ int vote_row(const uint16_t* lab, uint16_t id, const 
   return vote_tiebreak(code, tied, scrow, w, lane);
 }
 
+// Rows with no out-of-fold neighbour take the majority label of their
+// training folds (ties to the smaller code); kept out of line, as it is rare.
+__device__ __noinline__ void vote_empty_rows(const EvolveParams& P, const Smem& s, int prob, const uint16_t* lab,
+                                             uint16_t* out, int C0) {
+  const int L = P.L, w = P.w;
+  const uint16_t* nbp = P.nb + static_cast<size_t>(prob) * L * w;
+  // per-fold training majority (codes in [0, C0))
+  int* fc = P.foldcnt + static_cast<size_t>(prob) * P.F * P.C0max;
+  for (int i = threadIdx.x; i < P.F * P.C0max; i += kThreads) fc[i] = 0;
+  for (int c = threadIdx.x; c < C0; c += kThreads) s.aux[c] = 0;
+  __syncthreads();
+  const uint8_t* fo = P.folds + static_cast<size_t>(prob) * L;
+  for (int r = threadIdx.x; r < L; r += kThreads) {
+    atomicAdd(&fc[fo[r] * P.C0max + lab[r]], 1);
+    atomicAdd(&s.aux[lab[r]], 1);
+  }
+  __syncthreads();
+  for (int fo_i = threadIdx.x; fo_i < P.F; fo_i += kThreads) {
+    int bl = 0, bcount = -1;
+    for (int c = 0; c < C0; ++c) {
+      const int cnt = s.aux[c] - fc[fo_i * P.C0max + c];
+      if (cnt > bcount) {  // ascending codes: ties keep the smaller label
+        bl = c;
+        bcount = cnt;
+      }
+    }
+    s.order[fo_i] = bl;  // order[] is free here; F <= C0max guaranteed by host
+  }
+  __syncthreads();
+  for (int r = threadIdx.x; r < L; r += kThreads) {
+    if (nbp[static_cast<size_t>(r) * w] == kNoRow) out[r] = static_cast<uint16_t>(s.order[fo[r]]);
+  }
+}
+
+// Rows per warp batch of the vote: the batch loop is unrolled, so this also
+// sets how many copies of the paired-vote code the kernel carries.
+constexpr int kVoteBatch = 8;
+
 // Vote rows into `out`: every row (rows == nullptr) or the nrows rows listed
 // in `rows` (the caller has filled the others).  Rows with no out-of-fold
 // neighbour take the majority label of their training folds (ties to the
@@ -473,7 +511,7 @@ __device__ void vote_block(const EvolveParams& P, const Smem& s, int prob, const
   const uint16_t* nbp = P.nb + static_cast<size_t>(prob) * L * w;
   const float* scp = P.sc + static_cast<size_t>(prob) * L * w;
   const int count = rows ? nrows : L;
-  constexpr int kB = 16;
+  constexpr int kB = kVoteBatch;
   for (int i0 = warp * kB; i0 < count; i0 += kWarps * kB) {
     uint16_t ids[kB];
 #pragma unroll
@@ -512,34 +550,7 @@ __device__ void vote_block(const EvolveParams& P, const Smem& s, int prob, const
       }
     }
   }
-  if (has_empty) {
-    // per-fold training majority (codes in [0, C0))
-    int* fc = P.foldcnt + static_cast<size_t>(prob) * P.F * P.C0max;
-    for (int i = threadIdx.x; i < P.F * P.C0max; i += kThreads) fc[i] = 0;
-    for (int c = threadIdx.x; c < C0; c += kThreads) s.aux[c] = 0;
-    __syncthreads();
-    const uint8_t* fo = P.folds + static_cast<size_t>(prob) * L;
-    for (int r = threadIdx.x; r < L; r += kThreads) {
-      atomicAdd(&fc[fo[r] * P.C0max + lab[r]], 1);
-      atomicAdd(&s.aux[lab[r]], 1);
-    }
-    __syncthreads();
-    for (int fo_i = threadIdx.x; fo_i < P.F; fo_i += kThreads) {
-      int bl = 0, bcount = -1;
-      for (int c = 0; c < C0; ++c) {
-        const int cnt = s.aux[c] - fc[fo_i * P.C0max + c];
-        if (cnt > bcount) {  // ascending codes: ties keep the smaller label
-          bl = c;
-          bcount = cnt;
-        }
-      }
-      s.order[fo_i] = bl;  // order[] is free here; F <= C0max guaranteed by host
-    }
-    __syncthreads();
-    for (int r = threadIdx.x; r < L; r += kThreads) {
-      if (nbp[static_cast<size_t>(r) * w] == kNoRow) out[r] = static_cast<uint16_t>(s.order[fo[r]]);
-    }
-  }
+  if (has_empty) vote_empty_rows(P, s, prob, lab, out, C0);
   __syncthreads();
 }
 
@@ -611,7 +622,7 @@ __device__ int label_census(const EvolveParams& P, const Smem& s, const uint16_t
 
 // s.order[0..nc) = the codes of the census in the iteration order of
 // std::unordered_map<int,int> after reserve(L) and insertion in row order.
-__device__ void map_order(const EvolveParams& P, const Smem& s, int prob, int C0) {
+__device__ __noinline__ void map_order(const EvolveParams& P, const Smem& s, int prob, int C0) {
   const bool nocollide = P.nocollide[prob] != 0;
   if (nocollide) {
     // every key has its own bucket: each new key goes to the list front
@@ -824,7 +835,7 @@ __device__ int absorption_block(const EvolveParams& P, const Smem& s, int prob, 
 
 // Relabel of sampled groups when draws are needed (groups of several rows, or
 // no prediction guidance).  Thread 0, in shuffled order.
-__device__ void relabel_serial(const EvolveParams& P, const Smem& s, const uint16_t* pp, int ns, int C0) {
+__device__ __noinline__ void relabel_serial(const EvolveParams& P, const Smem& s, const uint16_t* pp, int ns, int C0) {
   Fixed& f = *s.f;
   int* hist = s.aux;
   for (int c = 0; c < C0; ++c) hist[c] = 0;
@@ -948,7 +959,7 @@ __device__ __forceinline__ float gumbel_noise(uint64_t seed, int cycle, int row)
 // replacement from the network's softmax over the candidates) above the row,
 // so all keys are distinct and ties go to the smaller row.  The take-th
 // largest key is found by a 4-pass radix select with 8-bit digits.
-__device__ void learned_flip(const EvolveParams& P, const Smem& s, int prob, int cycle, int take, int C0) {
+__device__ __noinline__ void learned_flip(const EvolveParams& P, const Smem& s, int prob, int cycle, int take, int C0) {
   Fixed& f = *s.f;
   if (take <= 0) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1047,7 +1058,7 @@ __device__ void learned_flip(const EvolveParams& P, const Smem& s, int prob, int
 
 // Training snapshot of the current state: features of every row and its
 // label / prediction codes.
-__device__ void snapshot_state(const EvolveParams& P, const Smem& s, int prob, int cycle, int C0) {
+__device__ __noinline__ void snapshot_state(const EvolveParams& P, const Smem& s, int prob, int cycle, int C0) {
   census_cur(P, s, C0);
   const float progress = static_cast<float>(cycle) / static_cast<float>(P.T > 0 ? P.T : 1);
   for (int r = threadIdx.x; r < P.L; r += kThreads) {
@@ -1064,7 +1075,7 @@ __device__ void snapshot_state(const EvolveParams& P, const Smem& s, int prob, i
 // Points the CTA at problem prob's groups and fixed flags: shared by all
 // problems, or one block per problem (per_problem_groups: goff stride L + 1,
 // gmem and fixed stride L, group count gcount[prob]).
-__device__ void bind_groups(const EvolveParams& P, const Smem& s, int prob) {
+__device__ __noinline__ void bind_groups(const EvolveParams& P, const Smem& s, int prob) {
   if (threadIdx.x == 0) {
     const bool per = P.per_problem_groups != 0;
     s.f->goff = P.goff + (per ? static_cast<size_t>(prob) * (P.L + 1) : 0);

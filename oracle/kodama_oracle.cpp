@@ -1814,6 +1814,15 @@ int orc_exact_knn(const float* x, int n, int d, int K, int* idx, float* dist, in
   }
 }
 
+// The randomized SIMPLS start vector (plscv.cpp:833-838): p draws of
+// std::normal_distribution<float> on std::mt19937(1).
+int orc_pls_start(int p, float* out) {
+  std::mt19937 gen(1u);
+  std::normal_distribution<float> nd(0.0f, 1.0f);
+  for (int j = 0; j < p; ++j) out[j] = nd(gen);
+  return 0;
+}
+
 int orc_exact_knn_metric(const float* x, int n, int d, int K, int metric, int* idx, float* dist, int threads) {
   try {
     orc::exact_knn_metric(x, n, d, K, metric, idx, dist, std::max(1, threads));
