@@ -185,14 +185,15 @@ class Ctx {
     }
   }
   // Queues f's work on the low-priority background stream, after everything
-  // queued on the main stream so far: while f runs, stream() is that stream
-  // (launches and allocations of f go there).  Returns false, running
-  // nothing, in capture mode, where there is no background stream.  Timing
-  // events a and b (marks on the background stream) bracket f's work.
+  // queued on the main stream so far (or after the main-stream mark `after`):
+  // while f runs, stream() is that stream (launches and allocations of f go
+  // there).  Returns false, running nothing, in capture mode, where there is
+  // no background stream.  Timing events a and b (marks on the background
+  // stream) bracket f's work.
   template <class F>
-  bool on_background(F&& f, int* a, int* b) {
+  bool on_background(F&& f, int* a, int* b, int after = -1) {
     if (bg_ == nullptr) return false;
-    const int e = mark();
+    const int e = after >= 0 ? after : mark();
     ck(cudaStreamWaitEvent(bg_, ev_[e], 0), "cudaStreamWaitEvent");
     std::swap(stream_, bg_);
     *a = mark();
@@ -225,6 +226,7 @@ class Ctx {
   // side stream for work that overlaps the main stream: fork() makes it wait
   // for everything queued on the main stream so far.
   cudaStream_t side() const { return side_; }
+  bool has_background() const { return bg_ != nullptr; }
   void fork() {
     const int e = mark();
     ck(cudaStreamWaitEvent(side_, ev_[e], 0), "cudaStreamWaitEvent");
@@ -1086,9 +1088,10 @@ struct MatrixTail {
 
 // build_graph (may be empty): queues the kNN graph into d_gidx / d_gdist.  It
 // needs only x, so outside a captured batch it runs on the low-priority
-// background stream from the start of the call, beside the atlas k-means, the
-// landmark planning and the landmark k-means, and is joined before anything
-// reads the graph; in a captured batch it runs right after the atlas.  Queues
+// background stream beside the landmark planning and the landmark k-means
+// (from the start of the call, beside the atlas k-means too, when it is the
+// longer branch), and is joined before anything reads the graph; in a
+// captured batch it runs right after the atlas.  Queues
 // the whole call; the results are read by matrix_finalize once the device
 // work is done (no host wait on the plain path, so a batch can capture it).
 void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_gidx, float* d_gdist, int K,
@@ -1113,9 +1116,16 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   if (pls && o->components < 1) fail(KGB_EINVAL, "PLSOptions::max_components must be positive.");
   cudaStream_t st = ctx.stream();
 
-  int ev_bg0 = -1, ev_bg1 = -1;
-  const bool graph_bg =
-      static_cast<bool>(build_graph) && ctx.on_background([&]() { build_graph(); }, &ev_bg0, &ev_bg1);
+  // Where the background graph starts.  Its CTAs, once resident, hold the SMs
+  // that the atlas k-means' many short launches wait for, so it starts after
+  // the atlas -- unless it is the longer branch: the candidate search grows as
+  // n^2 d and the atlas plus the landmark stage about as n, and from about
+  // n = 40000 at d = 64 (N=20000, d=50: graph 2 ms, atlas + landmarks 6.5 ms;
+  // N=100000: 55 ms against 25 ms) the graph starts with the call.
+  const bool graph_first = static_cast<double>(n) * n * d >= 1.0e11;
+  int ev_bg0 = -1, ev_bg1 = -1, ev_planned = -1;
+  bool graph_bg = static_cast<bool>(build_graph) && graph_first &&
+                  ctx.on_background([&]() { build_graph(); }, &ev_bg0, &ev_bg1);
 
   // shared landmark atlas (kodama_matrix.cpp:3662-3734)
   float* d_pnorm = ctx.alloc<float>(n);
@@ -1153,7 +1163,7 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     ck_launch(kgb::kmeans_run(B, st), "atlas k-means");
   }
   const int ev_atlas = ctx.mark();
-  const bool graph_here = static_cast<bool>(build_graph) && !graph_bg;
+  const bool graph_here = static_cast<bool>(build_graph) && !ctx.has_background();
   if (graph_here) {
     build_graph();
     ev_graph = ctx.mark();
@@ -1161,7 +1171,7 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   out->timings[2] = clk.lap();
 
   // per-run landmarks and k-means seeds, drawn on the device from the atlas
-  // (side stream, beside the graph build); quota_sample returns exactly
+  // (side stream); quota_sample returns exactly
   // min(target, n) rows
   const int init_k = std::max(2, std::min(splitting, landmarks));
   const int kk = std::max(1, std::min(init_k, landmarks));
@@ -1172,6 +1182,7 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
   int* d_plan_init = ctx.alloc<int>(static_cast<size_t>(M) * kk);
   uint64_t* d_land_hash = ctx.alloc<uint64_t>(M);
   int* d_plan_status = ctx.alloc<int>(1);
+  int* d_km_assign = nullptr;
   {
     ck(cudaMemsetAsync(d_plan_status, 0, sizeof(int), st), "memset");
     kgb::PlanArgs pa;
@@ -1189,9 +1200,17 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     pa.land_hash = d_land_hash;
     pa.status = d_plan_status;
     pa.scratch = ctx.alloc<char>(kgb::plan_scratch_bytes(n, coarse_k, L, M));
-    ctx.fork_after(ev_atlas);
+    ctx.fork();  // after the atlas and the status reset
     ck_launch(kgb::plan_landmarks(pa, ctx.side()), "landmark planning");
+    // the landmark k-means' assignment scratch is cleared beside the
+    // planning, so that the k-means launch is the first thing the main
+    // stream runs once the planning ends
+    if (o->starting_labels == nullptr) {
+      d_km_assign = ctx.alloc<int>(static_cast<size_t>(M) * L);
+      ck(cudaMemsetAsync(d_km_assign, 0xff, sizeof(int) * static_cast<size_t>(M) * L, st), "memset");
+    }
     ctx.join();
+    ev_planned = ctx.mark();
     // the serial landmark hashes stay on the side stream, beside the k-means
     ck_launch(kgb::plan_land_hash(pa, ctx.side()), "landmark hashes");
   }
@@ -1241,8 +1260,7 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     B.split_uniform = d_split;
     B.cent = ctx.alloc<float>(static_cast<size_t>(M) * kk * d);
     B.cnorm = ctx.alloc<float>(static_cast<size_t>(M) * kk);
-    B.assign = ctx.alloc<int>(static_cast<size_t>(M) * L);
-    ck(cudaMemsetAsync(B.assign, 0xff, sizeof(int) * static_cast<size_t>(M) * L, st), "memset");
+    B.assign = d_km_assign;
     B.active = ctx.alloc<int>(M);
     B.changed = ctx.alloc<int>(M);
     B.labels = d_init_labels;
@@ -1252,6 +1270,11 @@ void matrix_from_device_graph(Ctx& ctx, const float* d_x, int n, int d, int* d_g
     tc_kmeans_inputs(ctx, B, d_x, n, d, tc_split);
     ck_launch(kgb::kmeans_run(B, st), "landmark k-means");
   }
+  // the background graph becomes ready with the landmark k-means and is
+  // queued after it, so the k-means' CTAs (a whole SM each) are placed first
+  // and the graph fills the SMs they leave
+  if (static_cast<bool>(build_graph) && !graph_first && !graph_here)
+    graph_bg = ctx.on_background([&]() { build_graph(); }, &ev_bg0, &ev_bg1, ev_planned);
   // folds (and the PLS slices) were planned on the host while the device worked
   FoldWork fold_work = folds_future.get();
   std::vector<kgb::FoldPlan>& fold_plans = fold_work.plans;

@@ -46,7 +46,6 @@ struct PlanScratch {
   int* quota;     // runs x strata
   uint8_t* flags; // runs x n
   int* perm;      // runs x target
-  uint32_t* bits; // runs x ceil(n/32): selected positions of the strata row list
 };
 
 PlanScratch carve(const PlanArgs& a) {
@@ -69,7 +68,6 @@ PlanScratch carve(const PlanArgs& a) {
   s.quota = reinterpret_cast<int*>(take(sizeof(int) * S * R));
   s.flags = reinterpret_cast<uint8_t*>(take(static_cast<size_t>(a.n) * R));
   s.perm = reinterpret_cast<int*>(take(sizeof(int) * static_cast<size_t>(a.target) * R));
-  s.bits = reinterpret_cast<uint32_t*>(take(sizeof(uint32_t) * static_cast<size_t>((a.n + 31) / 32) * R));
   return s;
 }
 
@@ -217,124 +215,192 @@ __device__ uint64_t draw_below_warp(Mt64State& rng, uint64_t range, int lane) {
   }
 }
 
-// Selected positions of the strata row list, accumulated one 32-bit word at a
-// time (positions only grow within a run).
-struct BitSink {
-  uint32_t* bits;
-  int word = -1;
-  uint32_t acc = 0;
-  __device__ void set(int pos, int lane) {
-    const int w = pos >> 5;
-    if (w != word) {
-      if (word >= 0 && acc != 0 && lane == 0) bits[word] = acc;
-      word = w;
-      acc = 0;
-    }
-    acc |= 1u << (pos & 31);
-  }
-  __device__ void flush(int lane) {
-    if (word >= 0 && acc != 0 && lane == 0) bits[word] = acc;
-    word = -1;
-    acc = 0;
-  }
+// Shared state of one std::sample call run by the whole CTA.
+struct __align__(16) SampleShared {
+  uint32_t p1[kMtN];  // the two acceptance positions of each step of a batch
+  uint32_t p2[kMtN];
+  uint16_t sel[kMtN]; // the walk's decisions: bit 0 the first row of a step, bit 8 the second
+  long long uns, nq;  // rows not yet visited, rows still wanted
+  int i, taken;       // next row of the stratum, rows taken so far
+  int rej;            // first step of the batch whose draw Lemire's method rejects
+  int visited;        // rows the batch's walk visited
+  int redraw;         // the rejected step is next and is drawn one output at a time
 };
 
 // std::sample of q rows out of the size rows starting at position first of
 // the strata row list (forward population): selection sampling, two
-// acceptance positions per draw while two or more rows remain.  One warp in
-// lockstep: the lanes draw up to 32 consecutive steps at once (a step's range
-// depends only on how many rows remain), then the acceptance recursion walks
-// them in order; a draw that Lemire's method would reject (probability about
-// range / 2^64) ends the batch and is redrawn step by step.
-__device__ int sample_warp(int first, int size, int q, BitSink& sink, Mt64State& rng, int lane) {
+// acceptance positions per draw while two or more rows remain.  The whole CTA
+// in batches: a step's range depends only on how many rows remain, so the
+// threads draw the acceptance positions of up to the rest of the engine's
+// output block at once (one output per step); thread 0 then walks the
+// acceptance recursion over them in order -- a compare and a decrement per
+// row, the decisions stored as bytes -- and the CTA flags the taken rows.  A
+// draw that Lemire's method would reject (probability about range / 2^64)
+// ends the batch; warp 0 redraws that step one output at a time, as it does
+// the single draws once fewer than two rows remain.  Called by every thread;
+// the count of rows taken is returned to thread 0.
+__device__ int sample_cta(int first, int size, int q, const int* __restrict__ rows, uint8_t* __restrict__ flags,
+                          Mt64State& rng, SampleShared& ss, int tid) {
   if (size <= 0) return 0;
-  long long uns = size;
-  long long nq = q < uns ? q : uns;
-  int taken = 0, i = 0;
-  while (nq != 0 && uns >= 2) {
-    if (rng.pos >= kMtN) mt64_refill_warp(rng, lane);
-    const int avail = kMtN - rng.pos;
+  const int lane = tid & 31;
+  if (tid == 0) {
+    ss.uns = size;
+    ss.nq = q < size ? q : size;
+    ss.i = 0;
+    ss.taken = 0;
+  }
+  __syncthreads();
+  long long uns = 0, nq = 0;
+  for (;;) {
+    uns = ss.uns;
+    nq = ss.nq;
+    const int pos0 = rng.pos, i0 = ss.i;
+    __syncthreads();  // every thread has read the state before it changes
+    if (nq == 0 || uns < 2) break;
+    if (pos0 >= kMtN) {
+      if (tid < 32) mt64_refill_warp(rng, lane);
+      __syncthreads();
+    }
+    const int pos = pos0 >= kMtN ? 0 : pos0;
     const long long steps_left = uns / 2;
-    const long long cap = avail < 32 ? avail : 32;
-    const int batch = static_cast<int>(cap < steps_left ? cap : steps_left);
-    // lane l evaluates step l of the batch
-    const long long ul = uns - 2LL * lane;
-    uint64_t p1 = 0, p2 = 0;
-    bool rejected = false;
-    if (lane < batch) {
+    const int batch = static_cast<int>(kMtN - pos < steps_left ? kMtN - pos : steps_left);
+    if (tid == 0) ss.rej = batch;
+    __syncthreads();
+    for (int j = tid; j < batch; j += kPlanThreads) {
+      const long long ul = uns - 2LL * j;
       const uint64_t b1 = static_cast<uint64_t>(ul - 1);
       const uint64_t range = static_cast<uint64_t>(ul) * b1;
-      const uint64_t u = rng.out[rng.pos + lane];
+      const uint64_t u = rng.out[pos + j];
       const uint64_t lo = u * range;
-      rejected = lo < range && lo < (0ull - range) % range;
+      if (lo < range && lo < (0ull - range) % range) atomicMin(&ss.rej, j);
+      uint64_t p1, p2;
       divmod_u64(__umul64hi(u, range), b1, p1, p2);
+      ss.p1[j] = static_cast<uint32_t>(p1);
+      ss.p2[j] = static_cast<uint32_t>(p2);
     }
-    const unsigned rej = __ballot_sync(0xffffffffu, rejected);
-    const int usable = rej ? (__ffs(rej) - 1) : batch;
-    int consumed = 0;
-    bool done = false;
-    for (int l = 0; l < usable; ++l) {
-      if (nq == 0) {
-        done = true;
-        break;
+    __syncthreads();
+    if (tid == 0) {
+      // nq <= size < 2^31: 32-bit counters; after a step that ends the sample
+      // (nn == 0) nothing more is taken, and the step's second row counts as
+      // visited only if the first did not end it
+      const int usable = ss.rej;
+      uint32_t nn = static_cast<uint32_t>(nq), n1 = nn;
+      int l = 0;
+      bool done = false;
+      // eight steps per pass without branches: once nn reaches 0 every later
+      // compare fails and nn stays 0, so the pass runs to its end and the
+      // step that ended the sample (and its n1) is picked out afterwards;
+      // p1, p2 and sel start 16-byte aligned
+      for (; l + 8 <= usable; l += 8) {
+        const uint4 P0 = *reinterpret_cast<const uint4*>(ss.p1 + l);
+        const uint4 P1 = *reinterpret_cast<const uint4*>(ss.p1 + l + 4);
+        const uint4 Q0 = *reinterpret_cast<const uint4*>(ss.p2 + l);
+        const uint4 Q1 = *reinterpret_cast<const uint4*>(ss.p2 + l + 4);
+        const uint32_t a1[8] = {P0.x, P0.y, P0.z, P0.w, P1.x, P1.y, P1.z, P1.w};
+        const uint32_t a2[8] = {Q0.x, Q0.y, Q0.z, Q0.w, Q1.x, Q1.y, Q1.z, Q1.w};
+        uint32_t sel[8];
+        int stop = 8;
+        uint32_t stop_n1 = 0;
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+          const uint32_t before = nn;
+          const uint32_t t1 = a1[e] < nn ? 1u : 0u;
+          const uint32_t m1 = nn - t1;
+          const uint32_t t2 = a2[e] < m1 ? 1u : 0u;
+          nn = m1 - t2;
+          sel[e] = t1 | (t2 << 8);
+          const bool hit = before != 0 && nn == 0;
+          stop = hit ? e : stop;
+          stop_n1 = hit ? m1 : stop_n1;
+        }
+        *reinterpret_cast<uint4*>(ss.sel + l) =
+            make_uint4(sel[0] | (sel[1] << 16), sel[2] | (sel[3] << 16), sel[4] | (sel[5] << 16), sel[6] | (sel[7] << 16));
+        if (nn == 0) {
+          l += stop;  // the step that ended the sample
+          n1 = stop_n1;
+          done = true;
+          break;
+        }
       }
-      const long long a1 = static_cast<long long>(__shfl_sync(0xffffffffu, p1, l));
-      const long long a2 = static_cast<long long>(__shfl_sync(0xffffffffu, p2, l));
-      consumed = l + 1;
-      --uns;
-      if (a1 < nq) {
-        sink.set(first + i, lane);
-        --nq;
-        ++taken;
+      for (; l < usable && !done; ++l) {
+        const uint32_t a1 = ss.p1[l], a2 = ss.p2[l];
+        const uint32_t t1 = a1 < nn ? 1u : 0u;
+        n1 = nn - t1;
+        const uint32_t t2 = a2 < n1 ? 1u : 0u;
+        nn = n1 - t2;
+        ss.sel[l] = static_cast<uint16_t>(t1 | (t2 << 8));
+        if (nn == 0) {
+          done = true;
+          break;
+        }
       }
-      ++i;
-      if (nq == 0) {
-        done = true;
-        break;
-      }
-      --uns;
-      if (a2 < nq) {
-        sink.set(first + i, lane);
-        --nq;
-        ++taken;
-      }
-      ++i;
+      const int steps = done ? l + 1 : usable;
+      const int visited = done ? 2 * l + 1 + (n1 != 0 ? 1 : 0) : 2 * usable;
+      rng.pos = pos + steps;
+      ss.uns = uns - visited;
+      ss.nq = nn;
+      ss.i = i0 + visited;
+      ss.taken += static_cast<int>(nq - static_cast<long long>(nn));
+      ss.visited = visited;
+      ss.redraw = !done && usable < batch;
     }
-    __syncwarp();
-    if (lane == 0) rng.pos += consumed;
-    __syncwarp();
-    if (done || nq == 0) break;
-    if (usable < batch) {
-      // the rejected step, drawn one output at a time
-      const uint64_t b1 = static_cast<uint64_t>(uns - 1);
-      uint64_t a1, a2;
-      divmod_u64(draw_below_warp(rng, static_cast<uint64_t>(uns) * b1, lane), b1, a1, a2);
-      --uns;
-      if (static_cast<long long>(a1) < nq) {
-        sink.set(first + i, lane);
-        --nq;
-        ++taken;
+    __syncthreads();
+    for (int k = tid; k < ss.visited; k += kPlanThreads)
+      if ((ss.sel[k >> 1] >> (8 * (k & 1))) & 1u) flags[rows[first + i0 + k]] = 1;
+    if (ss.redraw) {
+      // the rejected step, drawn one output at a time by warp 0
+      if (tid < 32) {
+        long long un = ss.uns, nn = ss.nq;
+        int i = ss.i, taken = ss.taken;
+        const uint64_t b1 = static_cast<uint64_t>(un - 1);
+        uint64_t a1, a2;
+        divmod_u64(draw_below_warp(rng, static_cast<uint64_t>(un) * b1, lane), b1, a1, a2);
+        --un;
+        if (static_cast<long long>(a1) < nn) {
+          if (tid == 0) flags[rows[first + i]] = 1;
+          --nn;
+          ++taken;
+        }
+        ++i;
+        if (nn != 0) {
+          --un;
+          if (static_cast<long long>(a2) < nn) {
+            if (tid == 0) flags[rows[first + i]] = 1;
+            --nn;
+            ++taken;
+          }
+          ++i;
+        }
+        __syncwarp();
+        if (tid == 0) {
+          ss.uns = un;
+          ss.nq = nn;
+          ss.i = i;
+          ss.taken = taken;
+        }
       }
-      ++i;
-      if (nq == 0) break;
-      --uns;
-      if (static_cast<long long>(a2) < nq) {
-        sink.set(first + i, lane);
-        --nq;
-        ++taken;
-      }
-      ++i;
     }
+    __syncthreads();
   }
-  for (; nq != 0; ++i) {
-    --uns;
-    if (static_cast<long long>(draw_below_warp(rng, static_cast<uint64_t>(uns) + 1, lane)) < nq) {
-      sink.set(first + i, lane);
-      --nq;
-      ++taken;
+  if (nq != 0) {
+    // fewer than two rows left: one draw per row (warp 0)
+    if (tid < 32) {
+      long long un = uns, nn = nq;
+      int i = ss.i, taken = ss.taken;
+      for (; nn != 0; ++i) {
+        --un;
+        if (static_cast<long long>(draw_below_warp(rng, static_cast<uint64_t>(un) + 1, lane)) < nn) {
+          if (tid == 0) flags[rows[first + i]] = 1;
+          --nn;
+          ++taken;
+        }
+      }
+      __syncwarp();
+      if (tid == 0) ss.taken = taken;
     }
+    __syncthreads();
   }
-  return taken;
+  return tid == 0 ? ss.taken : 0;
 }
 
 // std::mt19937 (Matsumoto & Nishimura 1998: n=624, m=397), serial.
@@ -368,6 +434,7 @@ __device__ uint32_t mt32_next(Mt32State& s) {
 __global__ void __launch_bounds__(kPlanThreads) plan_runs_kernel(PlanArgs a, PlanScratch s) {
   __shared__ Mt64State rng;
   __shared__ Mt32State rng32;
+  __shared__ SampleShared ss;
   __shared__ int sh_bad, sh_total;
   __shared__ uint32_t sh_kseed;
   __shared__ int sh_warp[kPlanThreads / 32];
@@ -376,13 +443,11 @@ __global__ void __launch_bounds__(kPlanThreads) plan_runs_kernel(PlanArgs a, Pla
   uint8_t* flags = s.flags + static_cast<size_t>(run) * a.n;
   int* quota = s.quota + static_cast<size_t>(run) * a.strata;
   int* order = s.order + static_cast<size_t>(run) * a.strata;
-  uint32_t* bits = s.bits + static_cast<size_t>(run) * ((a.n + 31) / 32);
   for (int r = tid; r < a.n; r += kPlanThreads) flags[r] = 0;
-  for (int w = tid; w < (a.n + 31) / 32; w += kPlanThreads) bits[w] = 0;
   for (int t = tid; t < a.strata; t += kPlanThreads) quota[t] = s.base[t];
   __syncthreads();
-  if (warp == 0) {
-    if (lane == 0) {
+  {
+    if (tid == 0) {
       int bad = 0;
       mt64_seed(rng, a.seed + static_cast<uint64_t>(a.first_run + run));
       (void)mt64_next_serial(rng);
@@ -428,21 +493,18 @@ __global__ void __launch_bounds__(kPlanThreads) plan_runs_kernel(PlanArgs a, Pla
       }
       sh_bad = bad;
     }
-    __syncwarp();
+    __syncthreads();
     if (sh_bad == 0) {
-      BitSink sink;
-      sink.bits = bits;
       int total = 0;
       for (int t = 0; t < a.strata; ++t) {
         const int q = quota[t];
         if (q <= 0) continue;
-        total += sample_warp(s.offsets[t], s.offsets[t + 1] - s.offsets[t], q, sink, rng, lane);
+        total += sample_cta(s.offsets[t], s.offsets[t + 1] - s.offsets[t], q, s.rows, flags, rng, ss, tid);
       }
-      sink.flush(lane);
-      if (lane == 0 && total != a.target) sh_bad = 3;
+      if (tid == 0 && total != a.target) sh_bad = 3;
     }
-    __syncwarp();
-    if (lane == 0) {
+    __syncthreads();
+    if (tid == 0) {
       sh_kseed = static_cast<uint32_t>((mt64_next_serial(rng) & 0x7fffffffull) + 1ull);
       sh_total = 0;
     }
@@ -452,9 +514,6 @@ __global__ void __launch_bounds__(kPlanThreads) plan_runs_kernel(PlanArgs a, Pla
     if (tid == 0) atomicExch(a.status, sh_bad);
     return;
   }
-  for (int p = tid; p < a.n; p += kPlanThreads)
-    if ((bits[p >> 5] >> (p & 31)) & 1u) flags[s.rows[p]] = 1;
-  __syncthreads();
   // ascending compaction of the selected rows (and of the others)
   int* land = a.land + static_cast<size_t>(run) * a.target;
   int* nonland = a.nonland == nullptr ? nullptr : a.nonland + static_cast<size_t>(run) * (a.n - a.target);
@@ -527,8 +586,7 @@ size_t plan_scratch_bytes(int n, int strata, int target, int runs) {
   const size_t S = static_cast<size_t>(strata), R = static_cast<size_t>(runs);
   return align256(sizeof(int) * S) * 3 + align256(sizeof(int) * (S + 1)) + align256(sizeof(int) * n) +
          align256(sizeof(Ext80) * S) + align256(sizeof(int)) + align256(sizeof(int) * S * R) * 2 +
-         align256(static_cast<size_t>(n) * R) + align256(sizeof(int) * static_cast<size_t>(target) * R) +
-         align256(sizeof(uint32_t) * static_cast<size_t>((n + 31) / 32) * R);
+         align256(static_cast<size_t>(n) * R) + align256(sizeof(int) * static_cast<size_t>(target) * R);
 }
 
 int plan_landmarks(const PlanArgs& a, cudaStream_t st) {
