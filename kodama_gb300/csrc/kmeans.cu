@@ -665,9 +665,92 @@ __global__ void __launch_bounds__(kSumThreads) sums_kernel(KMeansBatch B) {
   }
 }
 
+// Update step, sort and sums in one (one CTA per cluster and problem, d up
+// to 4 x kScanThreads): the CTA scans the problem's assignments in chunks of
+// kScanChunk rows -- a ballot per 32 rows, prefix over the warps -- so the
+// cluster's members of a chunk land in shared memory in ascending row order;
+// thread j then adds columns j, j + 256, ... down them, up to 32 rows' loads
+// in flight.  The size goes to offsets[c] (finalize_kernel reads sizes).
+// Without the member lists and the one-CTA sort this replaces sort_kernel and
+// sums_kernel when each problem's assignments are read by its k CTAs anyway.
+constexpr int kScanThreads = 256;
+constexpr int kScanChunk = 4 * kScanThreads;
+constexpr int kScanCols = 4;  // columns per thread
+constexpr int kScanBatch = 16;  // member rows whose loads are issued together
+
+__global__ void __launch_bounds__(kScanThreads) scan_sums_kernel(KMeansBatch B) {
+  __shared__ int mem[kScanChunk];
+  __shared__ int wcount[kScanThreads / 32];
+  const int c = blockIdx.x, p = blockIdx.y;
+  if (!B.active[p]) return;
+  const int n = B.n, d = B.d, tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int* as = B.assign + static_cast<size_t>(p) * n;
+  const int* rows = B.rows != nullptr ? B.rows + static_cast<size_t>(p) * n : nullptr;
+  float s[kScanCols];
+#pragma unroll
+  for (int q = 0; q < kScanCols; ++q) s[q] = 0.0f;
+  int count = 0;
+  for (int base = 0; base < n; base += kScanChunk) {
+    // warp w scans rows base + 128 w .. + 127, 32 at a time
+    unsigned bal[4];
+    int cw = 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int r = base + warp * 128 + i * 32 + lane;
+      bal[i] = __ballot_sync(kFull, r < n && as[r] == c);
+      cw += __popc(bal[i]);
+    }
+    if (lane == 0) wcount[warp] = cw;
+    __syncthreads();
+    int off = 0, total = 0;
+#pragma unroll
+    for (int q = 0; q < kScanThreads / 32; ++q) {
+      const int v = wcount[q];
+      off += q < warp ? v : 0;
+      total += v;
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      if ((bal[i] >> lane) & 1u) {
+        const int r = base + warp * 128 + i * 32 + lane;
+        mem[off + __popc(bal[i] & ((1u << lane) - 1u))] = rows != nullptr ? rows[r] : r;
+      }
+      off += __popc(bal[i]);
+    }
+    __syncthreads();
+    for (int m0 = 0; m0 < total; m0 += kScanBatch) {
+      const int mb = min(kScanBatch, total - m0);
+#pragma unroll
+      for (int q = 0; q < kScanCols; ++q) {
+        const int j = tid + q * kScanThreads;
+        if (q * kScanThreads < d) {
+          float v[kScanBatch];
+#pragma unroll
+          for (int u = 0; u < kScanBatch; ++u)
+            v[u] = (u < mb && j < d) ? B.x[static_cast<size_t>(mem[m0 + u]) * d + j] : 0.0f;
+#pragma unroll
+          for (int u = 0; u < kScanBatch; ++u)
+            if (u < mb) s[q] = fadd(s[q], v[u]);
+        }
+      }
+    }
+    count += total;
+    __syncthreads();  // mem and wcount are rewritten by the next chunk
+  }
+  const float inv = count != 0 ? __fdiv_rn(1.0f, static_cast<float>(count)) : 0.0f;
+  float* cent = B.cent + (static_cast<size_t>(p) * B.k + c) * d;
+#pragma unroll
+  for (int q = 0; q < kScanCols; ++q) {
+    const int j = tid + q * kScanThreads;
+    if (j < d) cent[j] = count != 0 ? fmul(s[q], inv) : s[q];
+  }
+  if (tid == 0) B.offsets[static_cast<size_t>(p) * (B.k + 1) + c] = count;
+}
+
 // Update step, part 3 (one thread per problem): empty-cluster splitting and
-// the early-exit flag.
-__global__ void finalize_kernel(KMeansBatch B) {
+// the early-exit flag.  sizes: offsets[c] holds cluster c's size (after
+// scan_sums_kernel) rather than its start (after sort_kernel).
+__global__ void finalize_kernel(KMeansBatch B, int sizes) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= B.problems || !B.active[p]) return;
   const int k = B.k, d = B.d, n = B.n;
@@ -678,8 +761,9 @@ __global__ void finalize_kernel(KMeansBatch B) {
   float* fvals = ftree + k + 1;
   bool any_empty = false;
   for (int c = 0; c < k; ++c) {
-    fsize[c] = static_cast<float>(off[c + 1] - off[c]);
-    any_empty |= off[c + 1] == off[c];
+    const int size = sizes ? off[c] : off[c + 1] - off[c];
+    fsize[c] = static_cast<float>(size);
+    any_empty |= size == 0;
   }
   if (any_empty && n > k) {
     const float eps = 1.0f / 1024.0f;
@@ -1288,16 +1372,21 @@ int kmeans_run(const KMeansBatch& B, cudaStream_t st) {
   cudaFuncSetAttribute(sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sort_bytes));
   cudaFuncSetAttribute(sums_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sum_bytes));
   const int iters = B.max_iter > 1 ? B.max_iter : 1;
+  const bool scan = B.d <= kScanCols * kScanThreads;
   for (int it = 0; it < iters; ++it) {
     centroid_norms_kernel<<<ngrid, 128, 0, st>>>(B, 0);
     launch_assign(0);
-    sort_kernel<<<B.problems, 1024, sort_bytes, st>>>(B);
-    sums_kernel<<<B.problems * B.k, kSumThreads, sum_bytes, st>>>(B);
-    finalize_kernel<<<(B.problems + 63) / 64, 64, 0, st>>>(B);
+    if (scan) {
+      scan_sums_kernel<<<dim3(B.k, B.problems), kScanThreads, 0, st>>>(B);
+    } else {
+      sort_kernel<<<B.problems, 1024, sort_bytes, st>>>(B);
+      sums_kernel<<<B.problems * B.k, kSumThreads, sum_bytes, st>>>(B);
+    }
+    finalize_kernel<<<(B.problems + 63) / 64, 64, 0, st>>>(B, scan ? 1 : 0);
   }
   centroid_norms_kernel<<<ngrid, 128, 0, st>>>(B, 1);
   launch_assign(1);
-  count_launch(1 + 5 * iters + 2);
+  count_launch(1 + (scan ? 4 : 5) * iters + 2);
   return static_cast<int>(cudaGetLastError());
 }
 
