@@ -517,19 +517,16 @@ EvolveBuffers run_evolution(Ctx& ctx, kgb::EvolveParams P, int C0max) {
   const int grid = std::min(problems, ctx.sms());
   constexpr size_t kSmemBudget = 224 * 1024;
   const size_t Lp = (static_cast<size_t>(L) + 7) / 8 * 8;
-  // prefer (in order): rows, vote histograms, transitions in shared memory
+  // prefer (in order): rows, transitions in shared memory
   bool placed = false;
   size_t smem = 0;
-  const bool hist_ok = C0max <= 1024;
-  for (int option = 0; option < 6 && !placed; ++option) {
-    const bool rows = option < 3;
-    const bool hist = hist_ok && (option % 3) < 2;
-    const bool trans = (option % 3) == 0;
-    smem = kgb::evolve_smem_bytes(L, C0max, rows, trans, hist);
+  for (int option = 0; option < 4 && !placed; ++option) {
+    const bool rows = option < 2;
+    const bool trans = (option % 2) == 0;
+    smem = kgb::evolve_smem_bytes(L, C0max, rows, trans);
     if (smem <= kSmemBudget) {
       placed = true;
       P.smem_rows = rows;
-      P.smem_hist = hist;
       P.smem_trans = trans;
     }
   }
@@ -949,11 +946,10 @@ EvolveBuffers run_pls_evolution(Ctx& ctx, kgb::EvolveParams P, PlsBuffers& b, in
   for (int option = 0; option < 4 && !placed; ++option) {
     const bool rows = option < 2;
     const bool trans = (option % 2) == 0;
-    smem = kgb::evolve_smem_bytes(L, C0max, rows, trans, false);
+    smem = kgb::evolve_smem_bytes(L, C0max, rows, trans);
     if (smem <= kSmemBudget) {
       placed = true;
       P.smem_rows = rows;
-      P.smem_hist = 0;
       P.smem_trans = trans;
     }
   }

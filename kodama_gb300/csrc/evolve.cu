@@ -78,8 +78,6 @@ struct Smem {
   uint16_t* list;    // shuffle steps bucketed by swap target
   int* scratch32;    // per-position counts / bucket offsets
   int* trans;        // class x prediction counts (shared or global)
-  unsigned* hist;    // per-warp packed 8-bit vote counters, or nullptr
-  int hist_words;    // words per histogram (two per warp)
   uint64_t* raw;     // engine outputs of one shuffle (global scratch)
   int* cnt;          // per code: count in proposal
   int* firstpos;     // per code: first row
@@ -385,79 +383,35 @@ __device__ __noinline__ int vote_tiebreak(int code, unsigned tied, const float* 
   return bc;
 }
 
-// Fold votes of two rows with per-row histograms of packed 8-bit counters in
-// shared memory (ceil(C0/4) zeroed words each, left zeroed on return): the
-// two rows' shared-memory round trips overlap.
-__device__ __forceinline__ void vote_rows_hist2(const uint16_t* lab, uint16_t ida, uint16_t idb, const float* sca,
-                                                const float* scb, int w, int lane, unsigned* ha, unsigned* hb,
-                                                int& outa, int& outb) {
-  const int ca = ida != kNoRow ? static_cast<int>(lab[ida]) : -1;
-  const int cb = idb != kNoRow ? static_cast<int>(lab[idb]) : -1;
-  const unsigned va = __ballot_sync(kFull, ca >= 0), vb = __ballot_sync(kFull, cb >= 0);
-  const int sha = (ca & 3) * 8, shb = (cb & 3) * 8;
-  unsigned olda = 0, oldb = 0;
-  if (ca >= 0) olda = atomicAdd(&ha[ca >> 2], 1u << sha);
-  if (cb >= 0) oldb = atomicAdd(&hb[cb >> 2], 1u << shb);
-  __syncwarp();
-  const int cnta = ca >= 0 ? static_cast<int>((ha[ca >> 2] >> sha) & 0xffu) : 0;
-  const int cntb = cb >= 0 ? static_cast<int>((hb[cb >> 2] >> shb) & 0xffu) : 0;
-  const bool firsta = ca >= 0 && ((olda >> sha) & 0xffu) == 0u;
-  const bool firstb = cb >= 0 && ((oldb >> shb) & 0xffu) == 0u;
-  const int maxa = __reduce_max_sync(kFull, cnta);
-  const int maxb = __reduce_max_sync(kFull, cntb);
-  const bool topa = ca >= 0 && cnta == maxa, topb = cb >= 0 && cntb == maxb;
-  const int besta = static_cast<int>(__reduce_min_sync(kFull, topa ? static_cast<unsigned>(ca) : 0xffffffffu));
-  const int bestb = static_cast<int>(__reduce_min_sync(kFull, topb ? static_cast<unsigned>(cb) : 0xffffffffu));
-  const unsigned tieda = __ballot_sync(kFull, topa && firsta);
-  const unsigned tiedb = __ballot_sync(kFull, topb && firstb);
-  __syncwarp();
-  if (ca >= 0) ha[ca >> 2] = 0u;
-  if (cb >= 0) hb[cb >> 2] = 0u;
-  __syncwarp();
-  outa = va == 0u ? -1 : (__popc(tieda) == 1 ? besta : vote_tiebreak(ca, tieda, sca, w, lane));
-  outb = vb == 0u ? -1 : (__popc(tiedb) == 1 ? bestb : vote_tiebreak(cb, tiedb, scb, w, lane));
-}
-
-// ---------------------------------------------------------------------------
-// Fold vote of one row by one warp (lane j holds neighbour slot j).  Winner:
-// largest count, then largest double score sum (neighbour order), then the
-// smallest code.  Returns -1 for a row without valid neighbours.
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ int vote_row(const uint16_t* lab, uint16_t id, const float* scrow, int w, int lane) {
-  const int code = id != kNoRow ? static_cast<int>(lab[id]) : -1;
-  const unsigned valid = __ballot_sync(kFull, code >= 0);
-  if (valid == 0u) return -1;
-  // pass 1: the distinct labels of the row (warp-uniform loop): the largest
-  // count and the smallest code reaching it; note ties
-  int maxc = 0, bestc = 0x7fffffff, nmax = 0;
-  unsigned rem = valid;
-  while (rem) {
-    const int ld = __ffs(rem) - 1;
-    const int v = __shfl_sync(kFull, code, ld);
-    const unsigned msk = __ballot_sync(kFull, code == v);
-    rem &= ~msk;
-    const int c = __popc(msk);
-    if (c > maxc) {
-      maxc = c;
-      bestc = v;
-      nmax = 1;
-    } else if (c == maxc) {
-      ++nmax;
-      if (v < bestc) bestc = v;
-    }
+// Fold votes of R rows by one warp (lane j holds neighbour slot j of every
+// row).  Lanes holding the same label find each other with __match_any_sync,
+// so a label's count is a popcount; winner: largest count, then (tie-break)
+// largest double score sum, then the smallest code.  The R rows' steps are
+// interleaved so their latencies overlap.  out[q] = -1 for a row without
+// valid neighbours.
+template <int R>
+__device__ __forceinline__ void vote_rows_match(const uint16_t* lab, const uint16_t* id, const float* const* sc, int w,
+                                                int lane, int* out) {
+  int c[R], cnt[R], mx[R], best[R];
+  unsigned m[R], tied[R];
+#pragma unroll
+  for (int q = 0; q < R; ++q) c[q] = id[q] != kNoRow ? static_cast<int>(lab[id[q]]) : -1;
+#pragma unroll
+  for (int q = 0; q < R; ++q) m[q] = __match_any_sync(kFull, c[q]);
+#pragma unroll
+  for (int q = 0; q < R; ++q) cnt[q] = c[q] >= 0 ? __popc(m[q]) : 0;
+#pragma unroll
+  for (int q = 0; q < R; ++q) mx[q] = __reduce_max_sync(kFull, cnt[q]);
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    const bool top = c[q] >= 0 && cnt[q] == mx[q];
+    best[q] = static_cast<int>(__reduce_min_sync(kFull, top ? static_cast<unsigned>(c[q]) : 0xffffffffu));
+    // one lane (the lowest) per label reaching the top count
+    tied[q] = __ballot_sync(kFull, top && (__ffs(m[q]) - 1) == lane);
   }
-  if (nmax == 1) return bestc;
-  // one lane per label reaching the top count
-  unsigned tied = 0u;
-  rem = valid;
-  while (rem) {
-    const int ld = __ffs(rem) - 1;
-    const int v = __shfl_sync(kFull, code, ld);
-    const unsigned msk = __ballot_sync(kFull, code == v);
-    rem &= ~msk;
-    if (__popc(msk) == maxc) tied |= 1u << ld;
-  }
-  return vote_tiebreak(code, tied, scrow, w, lane);
+#pragma unroll
+  for (int q = 0; q < R; ++q)
+    out[q] = mx[q] == 0 ? -1 : (__popc(tied[q]) == 1 ? best[q] : vote_tiebreak(c[q], tied[q], sc[q], w, lane));
 }
 
 // Rows with no out-of-fold neighbour take the majority label of their
@@ -494,9 +448,11 @@ __device__ __noinline__ void vote_empty_rows(const EvolveParams& P, const Smem& 
   }
 }
 
-// Rows per warp batch of the vote: the batch loop is unrolled, so this also
-// sets how many copies of the paired-vote code the kernel carries.
+// Rows per warp batch of the vote (a multiple of kVoteRows): the batch loop
+// is unrolled, so this also sets how many copies of the vote code the kernel
+// carries.
 constexpr int kVoteBatch = 8;
+constexpr int kVoteRows = 4;
 
 // Vote rows into `out`: every row (rows == nullptr) or the nrows rows listed
 // in `rows` (the caller has filled the others).  Rows with no out-of-fold
@@ -520,33 +476,25 @@ __device__ void vote_block(const EvolveParams& P, const Smem& s, int prob, const
       const int r = i < count ? (rows ? static_cast<int>(rows[i]) : i) : 0;
       ids[u] = (i < count && lane < w) ? nbp[static_cast<size_t>(r) * w + lane] : kNoRow;
     }
-    if (s.hist) {
-      // two rows per step, each with its own histogram
-      unsigned* ha = s.hist + (2 * warp) * s.hist_words;
-      unsigned* hb = ha + s.hist_words;
 #pragma unroll
-      for (int u = 0; u < kB; u += 2) {
-        const int i = i0 + u;
-        if (i >= count) break;
-        const bool two = i + 1 < count;
-        const int ra = rows ? static_cast<int>(rows[i]) : i;
-        const int rb = two ? (rows ? static_cast<int>(rows[i + 1]) : i + 1) : ra;
-        int ba, bb;
-        vote_rows_hist2(lab, ids[u], two ? ids[u + 1] : kNoRow, scp + static_cast<size_t>(ra) * w,
-                        scp + static_cast<size_t>(rb) * w, w, lane, ha, hb, ba, bb);
-        if (lane == 0) {
-          if (ba >= 0) out[ra] = static_cast<uint16_t>(ba);
-          if (two && bb >= 0) out[rb] = static_cast<uint16_t>(bb);
-        }
+    for (int u = 0; u < kB; u += kVoteRows) {
+      const int i = i0 + u;
+      if (i >= count) break;
+      int rr[kVoteRows], best[kVoteRows];
+      uint16_t id[kVoteRows];
+      const float* sc[kVoteRows];
+#pragma unroll
+      for (int q = 0; q < kVoteRows; ++q) {
+        const bool in = i + q < count;
+        rr[q] = in ? (rows ? static_cast<int>(rows[i + q]) : i + q) : -1;
+        id[q] = in ? ids[u + q] : kNoRow;
+        sc[q] = scp + static_cast<size_t>(in ? rr[q] : 0) * w;
       }
-    } else {
+      vote_rows_match<kVoteRows>(lab, id, sc, w, lane, best);
+      if (lane == 0) {
 #pragma unroll
-      for (int u = 0; u < kB; ++u) {
-        const int i = i0 + u;
-        if (i >= count) break;
-        const int r = rows ? static_cast<int>(rows[i]) : i;
-        const int best = vote_row(lab, ids[u], scp + static_cast<size_t>(r) * w, w, lane);
-        if (best >= 0 && lane == 0) out[r] = static_cast<uint16_t>(best);
+        for (int q = 0; q < kVoteRows; ++q)
+          if (rr[q] >= 0 && best[q] >= 0) out[rr[q]] = static_cast<uint16_t>(best[q]);
       }
     }
   }
@@ -569,9 +517,10 @@ __device__ int dirty_rows_block(const EvolveParams& P, const Smem& s, int prob) 
     changed += s.cl[r] != s.cur[r];
   }
   changed = block_sum(changed, f);
-  // expected dirty rows = changed * mean in-degree; past half of the rows a
-  // full vote is cheaper than gathering the reverse lists
-  if (2ll * changed * roff[L] > static_cast<long long>(L) * L) return -1;
+  // changed * mean in-degree reverse entries mark about L (1 - exp(-e / L))
+  // distinct rows for e entries; the gather costs little next to a vote, so
+  // the full vote is kept for e > 3 L (about 95% of the rows dirty)
+  if (static_cast<long long>(changed) * roff[L] > 3ll * L * L) return -1;
   for (int r = threadIdx.x; r < L; r += kThreads) {
     if (s.cl[r] == s.cur[r]) continue;
     const int b = roff[r], e = roff[r + 1];
@@ -1329,14 +1278,6 @@ __device__ Smem carve_smem(const EvolveParams& P, unsigned char* smem_raw) {
   s.weight = reinterpret_cast<double*>(smem_raw + off); off += align_up(sizeof(double) * C, 16);
   s.cp = reinterpret_cast<double*>(smem_raw + off); off += align_up(sizeof(double) * 2 * C, 16);
   const size_t Lp = align_up(static_cast<size_t>(P.L), 8);
-  s.hist_words = (C + 3) / 4;
-  if (P.smem_hist) {
-    s.hist = reinterpret_cast<unsigned*>(smem_raw + off);
-    off += align_up(sizeof(unsigned) * 2 * kWarps * s.hist_words, 16);
-    for (int i = threadIdx.x; i < 2 * kWarps * s.hist_words; i += kThreads) s.hist[i] = 0u;
-  } else {
-    s.hist = nullptr;
-  }
   s.raw = P.raw_scratch + static_cast<size_t>(blockIdx.x) * (P.L / 2 + 64);
   if (P.smem_trans) {
     s.trans = reinterpret_cast<int*>(smem_raw + off);
@@ -1900,10 +1841,9 @@ __global__ void __launch_bounds__(kThreads, 1) evolve_pls_kernel(EvolvePlsParams
 
 }  // namespace
 
-size_t evolve_smem_bytes(int L, int C0max, bool rows_in_smem, bool trans_in_smem, bool hist_in_smem) {
+size_t evolve_smem_bytes(int L, int C0max, bool rows_in_smem, bool trans_in_smem) {
   auto al = [](size_t v) { return (v + 15) / 16 * 16; };
   size_t b = al(sizeof(Fixed));
-  if (hist_in_smem) b += al(sizeof(unsigned) * 2 * kWarps * ((C0max + 3) / 4));
   b += 6 * al(sizeof(int) * C0max) + al(sizeof(int) * (C0max + 1));
   b += 2 * al(sizeof(double) * C0max) + al(sizeof(double) * 2 * C0max);
   if (trans_in_smem) b += al(sizeof(int) * static_cast<size_t>(C0max) * C0max);

@@ -25,7 +25,6 @@ struct EvolveParams {
   uint64_t bucket_count;   // libstdc++ bucket count after reserve(L)
   int smem_rows;           // 1 = per-row arrays in shared memory
   int smem_trans;          // 1 = class x prediction counts in shared memory
-  int smem_hist;           // 1 = per-warp vote histograms in shared memory
   // inputs
   const uint16_t* nb;      // problems x L x w local neighbour ids (kNoRow = none)
   const float* sc;         // problems x L x w scores -(d*d)
@@ -99,7 +98,7 @@ struct EvolvePlsParams {
 };
 
 constexpr int kEvolveRowArrays = 8;
-size_t evolve_smem_bytes(int L, int C0max, bool rows_in_smem, bool trans_in_smem, bool hist_in_smem);
+size_t evolve_smem_bytes(int L, int C0max, bool rows_in_smem, bool trans_in_smem);
 int evolve_launch(const EvolveParams& p, int grid, size_t smem, void* stream);
 int evolve_pls_launch(const EvolvePlsParams& q, int grid, size_t smem, void* stream);
 
