@@ -41,6 +41,7 @@ constexpr int kRowArrays = 8;  // cl, cur, curpred, pred/perm, J, list, 2 x (32-
 
 struct Fixed {
   Mt64State rng;
+  uint64_t mt_alt[kMtN];  // the engine state's second buffer (produce_outputs_group)
   int first_reject;
   int i0;
   int ns;
@@ -157,57 +158,62 @@ __device__ void block_exclusive_scan(int* a, int n, Fixed& f) {
   __syncthreads();
 }
 
-// Engine producer group: the first 320 threads (warps 0-9) synchronised by
-// named barrier 1, one state word per thread in each regeneration phase.
-constexpr int kProducerThreads = 320;
-__device__ __forceinline__ void producer_sync() { asm volatile("bar.sync 1, 320;" ::: "memory"); }
+// Engine producer group: the first 160 threads (warps 0-4) synchronised by
+// named barrier 1.
+constexpr int kProducerThreads = 160;
+__device__ __forceinline__ void producer_sync() { asm volatile("bar.sync 1, 160;" ::: "memory"); }
 
 // Copy the next `count` engine outputs into raw[start..] (producer group).
 // The outputs left in g.out are copied first; every whole block of 312 that
 // follows is regenerated with its tempered words written straight into raw
 // (g.out is only refreshed for the last block, whose tail later draws read).
-__device__ void produce_outputs_group(Mt64State& g, uint64_t* raw, int start, int count, int t) {
+// A regeneration reads the old state words from one buffer and writes the new
+// ones to the other (g.mt and alt in turn), so one barrier separates
+// regenerations: thread t < 156 forms word t from old words t, t + 1, t + 156
+// and then word t + 156 from old words t + 156, t + 157 and its own new word t
+// (word 311 takes the new word 0, which thread 155 forms again itself).
+__device__ void produce_outputs_group(Mt64State& g, uint64_t* alt, uint64_t* raw, int start, int count, int t) {
   const int pos0 = g.pos;
   const int lead = min(kMtN - pos0, count);
   for (int i = t; i < lead; i += kProducerThreads) raw[start + i] = g.out[pos0 + i];
   int done = lead;
   int pos = pos0 + lead;
+  uint64_t* cur = g.mt;
+  uint64_t* nxt = alt;
   while (done < count) {
-    // one regeneration of the 312 state words; word k's output goes to
-    // raw[start + done + k] while done + k < count, else to g.out[k]
     const int take = min(kMtN, count - done);
-    uint64_t v = 0;
-    if (t < kMtN - kMtM) v = mt64_mix(g.mt[t], g.mt[t + 1], g.mt[t + kMtM]);
-    producer_sync();
     if (t < kMtN - kMtM) {
-      g.mt[t] = v;
-      const uint64_t o = mt64_temper(v);
-      if (t < take) raw[start + done + t] = o;
-      if (take < kMtN) g.out[t] = o;
+      const int h = t + kMtM;
+      const uint64_t lo = mt64_mix(cur[t], cur[t + 1], cur[h]);
+      const uint64_t hi = h < kMtN - 1 ? mt64_mix(cur[h], cur[h + 1], lo)
+                                       : mt64_mix(cur[h], mt64_mix(cur[0], cur[1], cur[kMtM]), lo);
+      nxt[t] = lo;
+      nxt[h] = hi;
+      const uint64_t tl = mt64_temper(lo), th = mt64_temper(hi);
+      if (t < take) raw[start + done + t] = tl;
+      if (h < take) raw[start + done + h] = th;
+      if (take < kMtN) {
+        g.out[t] = tl;
+        g.out[h] = th;
+      }
     }
+    // the next regeneration reads what this one wrote and overwrites what it read
     producer_sync();
-    if (t >= kMtN - kMtM && t < kMtN) {
-      v = t < kMtN - 1 ? mt64_mix(g.mt[t], g.mt[t + 1], g.mt[t - (kMtN - kMtM)])
-                       : mt64_mix(g.mt[kMtN - 1], g.mt[0], g.mt[kMtM - 1]);
-    }
-    producer_sync();
-    if (t >= kMtN - kMtM && t < kMtN) {
-      g.mt[t] = v;
-      const uint64_t o = mt64_temper(v);
-      if (t < take) raw[start + done + t] = o;
-      if (take < kMtN) g.out[t] = o;
-    }
-    // the next regeneration reads words this one wrote
-    producer_sync();
+    uint64_t* const tmp = cur;
+    cur = nxt;
+    nxt = tmp;
     done += take;
     pos = take;
+  }
+  if (cur != g.mt) {
+    for (int k = t; k < kMtN; k += kProducerThreads) g.mt[k] = cur[k];
   }
   if (t == 0) g.pos = pos;
   producer_sync();
 }
 
-// Swap targets J[i] of every step of the shuffle of G groups.  Warp 0 streams
-// the engine outputs the pair draws consume into `raw`; the whole CTA then
+// Swap targets J[i] of every step of the shuffle of G groups.  The producer
+// group streams the engine outputs the pair draws consume into `raw`; the whole CTA then
 // downscales them in parallel.  A rejected draw (Lemire resampling, about one
 // in 2^64/G^2) shifts every later pair by one output: the pairs from the
 // rejection on are redone with the next output appended.
@@ -223,7 +229,7 @@ __device__ void shuffle_targets_block(Fixed& f, uint16_t* J, int G, uint64_t* ra
   const int i0 = f.i0;
   const int npairs = (G - i0) >> 1;
   if (npairs <= 0) return;
-  if (threadIdx.x < kProducerThreads) produce_outputs_group(f.rng, raw, 0, npairs, threadIdx.x);
+  if (threadIdx.x < kProducerThreads) produce_outputs_group(f.rng, f.mt_alt, raw, 0, npairs, threadIdx.x);
   __syncthreads();
   int from = 0, shift = 0;
   for (;;) {
@@ -250,7 +256,7 @@ __device__ void shuffle_targets_block(Fixed& f, uint16_t* J, int G, uint64_t* ra
     const int r = f.first_reject;
     if (r >= npairs) break;
     // the output at r + shift was rejected: pairs r.. use one output later
-    if (threadIdx.x < kProducerThreads) produce_outputs_group(f.rng, raw, npairs + shift, 1, threadIdx.x);
+    if (threadIdx.x < kProducerThreads) produce_outputs_group(f.rng, f.mt_alt, raw, npairs + shift, 1, threadIdx.x);
     ++shift;
     from = r;
     __syncthreads();
@@ -677,35 +683,43 @@ __device__ int absorption_block(const EvolveParams& P, const Smem& s, int prob, 
   if (nc <= 2) return 0;
   const double n = static_cast<double>(P.L);
   const double nmax = (1.0 < n) ? n : 1.0;  // std::max(1.0, n)
-  for (int src = threadIdx.x; src < C0; src += kThreads) {
+  // one warp per source, its lanes over the destinations.  The reference
+  // scans the destinations in ascending order keeping the best by
+  // (surplus, count, destination size, smaller destination), starting from
+  // (0, 0, source size, source): that is the lexicographic maximum of those
+  // keys, found here by a warp reduction.
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int src = warp; src < C0; src += kWarps) {
     const int ssize = s.cnt[src];
     if (ssize == 0 || s.movable[src] <= 0) continue;
     const int* row = tr + src * C;
     const int stay = row[src];
-    int bt = src, bcount = 0, bsize = ssize;
-    double bsur = 0.0;
     // exact surplus x n = cnt*n - ssize*dsize; only the candidates at the
-    // exact maximum can win the double comparison chain below (double
-    // rounding is far below the 1/n spacing of distinct exact surpluses)
+    // exact maximum can win the double comparison chain (double rounding is
+    // far below the 1/n spacing of distinct exact surpluses)
     long long kmax = -0x7fffffffffffffffll;
-    for (int dst = 0; dst < C0; ++dst) {
+    for (int dst = lane; dst < C0; dst += 32) {
       const int cntd = row[dst];
-      if (dst == src || cntd == 0) continue;
       const int dsize = s.cnt[dst];
-      if (dsize == 0) continue;
+      if (dst == src || cntd == 0 || dsize == 0) continue;
       const long long kx = static_cast<long long>(cntd) * P.L - static_cast<long long>(ssize) * dsize;
       if (kx > kmax) kmax = kx;
     }
-    for (int dst = 0; dst < C0; ++dst) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const long long other = __shfl_xor_sync(kFull, kmax, o);
+      if (other > kmax) kmax = other;
+    }
+    int bt = src, bcount = 0, bsize = ssize;
+    double bsur = 0.0;
+    for (int dst = lane; dst < C0; dst += 32) {
       const int cntd = row[dst];
-      if (dst == src || cntd == 0) continue;
       const int dsize = s.cnt[dst];
-      if (dsize == 0) continue;
+      if (dst == src || cntd == 0 || dsize == 0) continue;
       if (static_cast<long long>(cntd) * P.L - static_cast<long long>(ssize) * dsize != kmax) continue;
       const double expected = __ddiv_rn(__dmul_rn(static_cast<double>(ssize), static_cast<double>(dsize)), nmax);
       const double sur = __dsub_rn(static_cast<double>(cntd), expected);
-      if (sur > bsur || (sur == bsur && cntd > bcount) ||
-          (sur == bsur && cntd == bcount && dsize > bsize) ||
+      if (sur > bsur || (sur == bsur && cntd > bcount) || (sur == bsur && cntd == bcount && dsize > bsize) ||
           (sur == bsur && cntd == bcount && dsize == bsize && dst < bt)) {
         bt = dst;
         bsize = dsize;
@@ -713,9 +727,24 @@ __device__ int absorption_block(const EvolveParams& P, const Smem& s, int prob, 
         bsur = sur;
       }
     }
-    if (bt == src || bsur <= 0.0 || bcount <= stay) continue;
-    s.bt[src] = bt;
-    s.bsur[src] = bsur;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double osur = __shfl_xor_sync(kFull, bsur, o);
+      const int ocount = __shfl_xor_sync(kFull, bcount, o);
+      const int osize = __shfl_xor_sync(kFull, bsize, o);
+      const int obt = __shfl_xor_sync(kFull, bt, o);
+      if (osur > bsur || (osur == bsur && ocount > bcount) || (osur == bsur && ocount == bcount && osize > bsize) ||
+          (osur == bsur && ocount == bcount && osize == bsize && obt < bt)) {
+        bt = obt;
+        bsize = osize;
+        bcount = ocount;
+        bsur = osur;
+      }
+    }
+    if (lane == 0 && !(bt == src || bsur <= 0.0 || bcount <= stay)) {
+      s.bt[src] = bt;
+      s.bsur[src] = bsur;
+    }
   }
   __syncthreads();
   if (threadIdx.x == 0) {
