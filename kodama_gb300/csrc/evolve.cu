@@ -52,6 +52,7 @@ struct Fixed {
   int moves_sel;
   int n_empty;
   int selected_target;
+  int rev_total;   // this problem's reverse-neighbour entries (rev_off[L])
   double acc;
   double score;
   int accept;
@@ -511,41 +512,104 @@ __device__ void vote_block(const EvolveParams& P, const Smem& s, int prob, const
 // Rows whose vote may differ from the current state's: reverse neighbours of
 // the rows whose label changed.  Returns the number listed in s.list, or -1
 // when so many rows changed that a full vote is cheaper.
+//   pass 1: each warp takes a contiguous range of rows, clears their flags
+//     and counts the changed rows (ballots); a scan of the warp counts
+//     places each warp's changed rows' reverse-list bounds in s.list (free
+//     until pass 2), so the gather waits on one global load only;
+//   gather: each warp takes four changed rows at a time, its lanes reading
+//     32 reverse entries of each per step (all four rows' loads in flight);
+//   pass 2: the flagged rows, listed in row order in s.list the same way.
 __device__ int dirty_rows_block(const EvolveParams& P, const Smem& s, int prob) {
   Fixed& f = *s.f;
   const int L = P.L;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned below = (1u << lane) - 1u;
   uint8_t* flag = reinterpret_cast<uint8_t*>(s.scratch32);
+  int* bounds = reinterpret_cast<int*>(s.list);  // 2 ints per changed row, room for Lp / 4 rows
   const int* roff = P.rev_off + static_cast<size_t>(prob) * (L + 1);
   const uint16_t* ridx = P.rev_idx + static_cast<size_t>(prob) * L * P.w;
-  int changed = 0;
-  for (int r = threadIdx.x; r < L; r += kThreads) {
-    flag[r] = 0;
-    changed += s.cl[r] != s.cur[r];
+  const int chunk = ((L + kWarps - 1) / kWarps + 31) / 32 * 32;
+  const int beg = min(L, warp * chunk), end = min(L, beg + chunk);
+  int wc = 0;
+  for (int b = beg; b < end; b += 32) {
+    const int r = b + lane;
+    bool ch = false;
+    if (r < end) {
+      flag[r] = 0;
+      ch = s.cl[r] != s.cur[r];
+    }
+    wc += __popc(__ballot_sync(kFull, ch));
   }
-  changed = block_sum(changed, f);
+  if (lane == 0) f.red_i[warp] = wc;
+  __syncthreads();
+  int base = 0, changed = 0;
+#pragma unroll 8
+  for (int q = 0; q < kWarps; ++q) {
+    const int v = f.red_i[q];
+    base += q < warp ? v : 0;
+    changed += v;
+  }
   // changed * mean in-degree reverse entries mark about L (1 - exp(-e / L))
   // distinct rows for e entries; the gather costs little next to a vote, so
-  // the full vote is kept for e > 3 L (about 95% of the rows dirty)
-  if (static_cast<long long>(changed) * roff[L] > 3ll * L * L) return -1;
-  for (int r = threadIdx.x; r < L; r += kThreads) {
-    if (s.cl[r] == s.cur[r]) continue;
-    const int b = roff[r], e = roff[r + 1];
-    for (int k = b; k < e; ++k) flag[ridx[k]] = 1;
+  // the full vote is kept for e > 3 L (about 95% of the rows dirty), and for
+  // more changed rows than the bounds' room (a quarter of the rows)
+  if (static_cast<long long>(changed) * f.rev_total > 3ll * L * L || changed > L / 4) return -1;
+  for (int b = beg; b < end; b += 32) {
+    const int r = b + lane;
+    const bool ch = r < end && s.cl[r] != s.cur[r];
+    const unsigned bm = __ballot_sync(kFull, ch);
+    if (ch) {
+      const int slot = base + __popc(bm & below);
+      bounds[2 * slot] = roff[r];
+      bounds[2 * slot + 1] = roff[r + 1];
+    }
+    base += __popc(bm);
   }
-  if (threadIdx.x == 0) f.flag = 0;
   __syncthreads();
-  const int lane = threadIdx.x & 31;
-  for (int base = threadIdx.x - lane; base < L; base += kThreads) {
-    const int r = base + lane;
-    const bool d = r < L && flag[r];
+  for (int i0 = 4 * warp; i0 < changed; i0 += 4 * kWarps) {
+    int b[4], e[4];
+    int span = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int i = i0 + q;
+      b[q] = i < changed ? bounds[2 * i] : 0;
+      e[q] = i < changed ? bounds[2 * i + 1] : 0;
+      span = max(span, e[q] - b[q]);
+    }
+    for (int k0 = 0; k0 < span; k0 += 32) {
+      uint16_t v[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int k = b[q] + k0 + lane;
+        v[q] = k < e[q] ? ridx[k] : kNoRow;
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (v[q] != kNoRow) flag[v[q]] = 1;
+    }
+  }
+  __syncthreads();
+  int dc = 0;
+  for (int b = beg; b < end; b += 32) {
+    const int r = b + lane;
+    dc += __popc(__ballot_sync(kFull, r < end && flag[r] != 0));
+  }
+  if (lane == 0) f.red_i[warp] = dc;
+  __syncthreads();
+  int dbase = 0, n = 0;
+#pragma unroll 8
+  for (int q = 0; q < kWarps; ++q) {
+    const int v = f.red_i[q];
+    dbase += q < warp ? v : 0;
+    n += v;
+  }
+  for (int b = beg; b < end; b += 32) {
+    const int r = b + lane;
+    const bool d = r < end && flag[r] != 0;
     const unsigned bm = __ballot_sync(kFull, d);
-    int slot0 = 0;
-    if (lane == 0 && bm) slot0 = atomicAdd(&f.flag, __popc(bm));
-    slot0 = __shfl_sync(kFull, slot0, 0);
-    if (d) s.list[slot0 + __popc(bm & ((1u << lane) - 1u))] = static_cast<uint16_t>(r);
+    if (d) s.list[dbase + __popc(bm & below)] = static_cast<uint16_t>(r);
+    dbase += __popc(bm);
   }
-  __syncthreads();
-  const int n = f.flag;
   __syncthreads();
   return n;
 }
@@ -670,16 +734,20 @@ __device__ int absorption_block(const EvolveParams& P, const Smem& s, int prob, 
     if (any_fixed && s.f->fxd[r] != 1) atomicAdd(&s.movable[a], 1);
   }
   __syncthreads();
-  for (int c = threadIdx.x; c < C0; c += kThreads) {
-    int sz = 0;
-    for (int q = 0; q < C0; ++q) sz += tr[c * C + q];
-    s.cnt[c] = sz;
-    if (!any_fixed) s.movable[c] = sz;
-  }
-  __syncthreads();
+  // class sizes: one warp per class, its lanes over the predictions
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int local = 0;
-  for (int c = threadIdx.x; c < C0; c += kThreads) local += s.cnt[c] > 0;
-  const int nc = block_sum(local, f);
+  for (int c = warp; c < C0; c += kWarps) {
+    int sz = 0;
+    for (int q = lane; q < C0; q += 32) sz += tr[c * C + q];
+    sz = __reduce_add_sync(kFull, sz);
+    if (lane == 0) {
+      s.cnt[c] = sz;
+      if (!any_fixed) s.movable[c] = sz;
+      local += sz > 0;
+    }
+  }
+  const int nc = block_sum(local, f);  // its barriers also publish the sizes
   if (nc <= 2) return 0;
   const double n = static_cast<double>(P.L);
   const double nmax = (1.0 < n) ? n : 1.0;  // std::max(1.0, n)
@@ -688,7 +756,6 @@ __device__ int absorption_block(const EvolveParams& P, const Smem& s, int prob, 
   // (surplus, count, destination size, smaller destination), starting from
   // (0, 0, source size, source): that is the lexicographic maximum of those
   // keys, found here by a warp reduction.
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int src = warp; src < C0; src += kWarps) {
     const int ssize = s.cnt[src];
     if (ssize == 0 || s.movable[src] <= 0) continue;
@@ -712,11 +779,13 @@ __device__ int absorption_block(const EvolveParams& P, const Smem& s, int prob, 
     }
     int bt = src, bcount = 0, bsize = ssize;
     double bsur = 0.0;
+    bool cand = false;
     for (int dst = lane; dst < C0; dst += 32) {
       const int cntd = row[dst];
       const int dsize = s.cnt[dst];
       if (dst == src || cntd == 0 || dsize == 0) continue;
       if (static_cast<long long>(cntd) * P.L - static_cast<long long>(ssize) * dsize != kmax) continue;
+      cand = true;
       const double expected = __ddiv_rn(__dmul_rn(static_cast<double>(ssize), static_cast<double>(dsize)), nmax);
       const double sur = __dsub_rn(static_cast<double>(cntd), expected);
       if (sur > bsur || (sur == bsur && cntd > bcount) || (sur == bsur && cntd == bcount && dsize > bsize) ||
@@ -727,6 +796,15 @@ __device__ int absorption_block(const EvolveParams& P, const Smem& s, int prob, 
         bsur = sur;
       }
     }
+    const unsigned cands = __ballot_sync(kFull, cand);
+    if (cands == 0u) continue;
+    if ((cands & (cands - 1u)) == 0u) {
+      // one lane holds every candidate: its best is the warp's
+      const int ld = __ffs(cands) - 1;
+      bt = __shfl_sync(kFull, bt, ld);
+      bcount = __shfl_sync(kFull, bcount, ld);
+      bsur = __shfl_sync(kFull, bsur, ld);
+    } else {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       const double osur = __shfl_xor_sync(kFull, bsur, o);
@@ -740,6 +818,7 @@ __device__ int absorption_block(const EvolveParams& P, const Smem& s, int prob, 
         bcount = ocount;
         bsur = osur;
       }
+    }
     }
     if (lane == 0 && !(bt == src || bsur <= 0.0 || bcount <= stay)) {
       s.bt[src] = bt;
@@ -1080,7 +1159,10 @@ __device__ void evolve_problem(const EvolveParams& P, const Smem& s, int prob) {
   uint8_t* fl = P.flags + static_cast<size_t>(prob) * T * 3;
   const uint16_t* nbp = P.nb + static_cast<size_t>(prob) * L * P.w;
 
-  if (threadIdx.x == 0) mt64_seed(f.rng, P.seeds[prob]);
+  if (threadIdx.x == 0) {
+    mt64_seed(f.rng, P.seeds[prob]);
+    f.rev_total = P.rev_off[static_cast<size_t>(prob) * (L + 1) + L];
+  }
   int local_empty = 0;
   for (int r = threadIdx.x; r < L; r += kThreads) {
     s.cur[r] = init[r];
