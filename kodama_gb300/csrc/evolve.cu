@@ -48,7 +48,8 @@ struct Fixed {
   int red_i[kWarps];
   int flag;
   int nc;          // distinct labels of the proposal
-  int changed_cnt;
+  int changed_cnt;  // dirty_rows_block: rows whose label changed
+  int dirty_cnt;    // dirty_rows_block: rows listed for the vote
   int moves_sel;
   int n_empty;
   int selected_target;
@@ -510,62 +511,64 @@ __device__ void vote_block(const EvolveParams& P, const Smem& s, int prob, const
 }
 
 // Rows whose vote may differ from the current state's: reverse neighbours of
-// the rows whose label changed.  Returns the number listed in s.list, or -1
-// when so many rows changed that a full vote is cheaper.
-//   pass 1: each warp takes a contiguous range of rows, clears their flags
-//     and counts the changed rows (ballots); a scan of the warp counts
-//     places each warp's changed rows' reverse-list bounds in s.list (free
-//     until pass 2), so the gather waits on one global load only;
-//   gather: each warp takes four changed rows at a time, its lanes reading
-//     32 reverse entries of each per step (all four rows' loads in flight);
-//   pass 2: the flagged rows, listed in row order in s.list the same way.
+// the rows whose label changed.  Lists them in s.jarr (free after the
+// relabel) and returns how many, or returns -1 when so many rows changed that
+// a full vote is cheaper; either way s.pred starts as a copy of s.curpred.
+//   pass: each warp takes a contiguous range of rows, copies their
+//     predictions, clears their flags and appends its changed rows'
+//     reverse-list bounds to s.list (one shared-counter atomic per warp step
+//     that has any);
+//   gather: each warp takes four changed rows at a time, its lanes reading 32
+//     reverse entries of each per step (all four rows' loads in flight); the
+//     lane that sets a row's flag first (atomicOr on the flag's word) appends
+//     the row to the list.
+// The list is in no particular order: every listed row is voted on its own.
 __device__ int dirty_rows_block(const EvolveParams& P, const Smem& s, int prob) {
   Fixed& f = *s.f;
   const int L = P.L;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned below = (1u << lane) - 1u;
   uint8_t* flag = reinterpret_cast<uint8_t*>(s.scratch32);
-  int* bounds = reinterpret_cast<int*>(s.list);  // 2 ints per changed row, room for Lp / 4 rows
+  unsigned* flagw = reinterpret_cast<unsigned*>(s.scratch32);
+  int* bounds = reinterpret_cast<int*>(s.list);  // 2 ints per changed row, room for L / 4 rows
+  uint16_t* dirty = s.jarr;
+  const int cap = L / 4;
   const int* roff = P.rev_off + static_cast<size_t>(prob) * (L + 1);
   const uint16_t* ridx = P.rev_idx + static_cast<size_t>(prob) * L * P.w;
+  if (threadIdx.x == 0) {
+    f.changed_cnt = 0;
+    f.dirty_cnt = 0;
+  }
+  __syncthreads();
   const int chunk = ((L + kWarps - 1) / kWarps + 31) / 32 * 32;
   const int beg = min(L, warp * chunk), end = min(L, beg + chunk);
-  int wc = 0;
   for (int b = beg; b < end; b += 32) {
     const int r = b + lane;
     bool ch = false;
     if (r < end) {
+      s.pred[r] = s.curpred[r];
       flag[r] = 0;
       ch = s.cl[r] != s.cur[r];
     }
-    wc += __popc(__ballot_sync(kFull, ch));
+    const unsigned bm = __ballot_sync(kFull, ch);
+    if (bm != 0u) {
+      int slot0 = 0;
+      if (lane == 0) slot0 = atomicAdd(&f.changed_cnt, __popc(bm));
+      slot0 = __shfl_sync(kFull, slot0, 0);
+      const int slot = slot0 + __popc(bm & below);
+      if (ch && slot < cap) {
+        bounds[2 * slot] = roff[r];
+        bounds[2 * slot + 1] = roff[r + 1];
+      }
+    }
   }
-  if (lane == 0) f.red_i[warp] = wc;
   __syncthreads();
-  int base = 0, changed = 0;
-#pragma unroll 8
-  for (int q = 0; q < kWarps; ++q) {
-    const int v = f.red_i[q];
-    base += q < warp ? v : 0;
-    changed += v;
-  }
+  const int changed = f.changed_cnt;
   // changed * mean in-degree reverse entries mark about L (1 - exp(-e / L))
   // distinct rows for e entries; the gather costs little next to a vote, so
   // the full vote is kept for e > 3 L (about 95% of the rows dirty), and for
-  // more changed rows than the bounds' room (a quarter of the rows)
-  if (static_cast<long long>(changed) * f.rev_total > 3ll * L * L || changed > L / 4) return -1;
-  for (int b = beg; b < end; b += 32) {
-    const int r = b + lane;
-    const bool ch = r < end && s.cl[r] != s.cur[r];
-    const unsigned bm = __ballot_sync(kFull, ch);
-    if (ch) {
-      const int slot = base + __popc(bm & below);
-      bounds[2 * slot] = roff[r];
-      bounds[2 * slot + 1] = roff[r + 1];
-    }
-    base += __popc(bm);
-  }
-  __syncthreads();
+  // more changed rows than the bounds' room
+  if (static_cast<long long>(changed) * f.rev_total > 3ll * L * L || changed > cap) return -1;
   for (int i0 = 4 * warp; i0 < changed; i0 += 4 * kWarps) {
     int b[4], e[4];
     int span = 0;
@@ -584,34 +587,24 @@ __device__ int dirty_rows_block(const EvolveParams& P, const Smem& s, int prob) 
         v[q] = k < e[q] ? ridx[k] : kNoRow;
       }
 #pragma unroll
-      for (int q = 0; q < 4; ++q)
-        if (v[q] != kNoRow) flag[v[q]] = 1;
+      for (int q = 0; q < 4; ++q) {
+        bool first = false;
+        if (v[q] != kNoRow) {
+          const unsigned bit = 1u << (8 * (v[q] & 3u));
+          first = (atomicOr(&flagw[v[q] >> 2], bit) & bit) == 0u;
+        }
+        const unsigned fm = __ballot_sync(kFull, first);
+        if (fm != 0u) {
+          int slot0 = 0;
+          if (lane == 0) slot0 = atomicAdd(&f.dirty_cnt, __popc(fm));
+          slot0 = __shfl_sync(kFull, slot0, 0);
+          if (first) dirty[slot0 + __popc(fm & below)] = v[q];
+        }
+      }
     }
   }
   __syncthreads();
-  int dc = 0;
-  for (int b = beg; b < end; b += 32) {
-    const int r = b + lane;
-    dc += __popc(__ballot_sync(kFull, r < end && flag[r] != 0));
-  }
-  if (lane == 0) f.red_i[warp] = dc;
-  __syncthreads();
-  int dbase = 0, n = 0;
-#pragma unroll 8
-  for (int q = 0; q < kWarps; ++q) {
-    const int v = f.red_i[q];
-    dbase += q < warp ? v : 0;
-    n += v;
-  }
-  for (int b = beg; b < end; b += 32) {
-    const int r = b + lane;
-    const bool d = r < end && flag[r] != 0;
-    const unsigned bm = __ballot_sync(kFull, d);
-    if (d) s.list[dbase + __popc(bm & below)] = static_cast<uint16_t>(r);
-    dbase += __popc(bm);
-  }
-  __syncthreads();
-  return n;
+  return f.dirty_cnt;
 }
 
 // Count labels of `lab` per code, first positions and distinct count.
@@ -1260,13 +1253,11 @@ __device__ void evolve_problem(const EvolveParams& P, const Smem& s, int prob) {
     }
 
     {
-      const int nd = dirty_rows_block(P, s, prob);
+      const int nd = dirty_rows_block(P, s, prob);  // s.pred = s.curpred on return
       if (nd < 0) {
         vote_block(P, s, prob, s.cl, s.pred, C0, has_empty);
       } else {
-        for (int r = threadIdx.x; r < L; r += kThreads) s.pred[r] = s.curpred[r];
-        __syncthreads();
-        vote_block(P, s, prob, s.cl, s.pred, C0, has_empty, s.list, nd);
+        vote_block(P, s, prob, s.cl, s.pred, C0, has_empty, s.jarr, nd);
       }
     }
     ok = 0;
