@@ -265,18 +265,23 @@ __device__ void shuffle_targets_block(Fixed& f, uint16_t* J, int G, uint64_t* ra
   }
 }
 
-// Bucket the steps by swap target: afterwards cnt[q] is the end of bucket q
-// in `list` and the start of bucket q+1.
-__device__ void bucket_steps_block(const Smem& s, int G) {
+// Bucket the steps by swap target, for the targets below lim (the used
+// positions [0, ns)): afterwards cnt[q] is the end of bucket q in `list` and
+// the start of bucket q+1.  A group only moves to higher positions (a later
+// step targeting its position p sits at a position above p), so walks that
+// decide membership of [0, lim) never need a bucket at or above lim.
+__device__ void bucket_steps_block(const Smem& s, int G, int lim) {
   const uint16_t* J = s.jarr;
   int* cnt = s.scratch32;
   uint16_t* list = s.list;
-  for (int q = threadIdx.x; q < G; q += kThreads) cnt[q] = 0;
+  for (int q = threadIdx.x; q < lim; q += kThreads) cnt[q] = 0;
   __syncthreads();
-  for (int st = 1 + threadIdx.x; st < G; st += kThreads) atomicAdd(&cnt[J[st]], 1);
+  for (int st = 1 + threadIdx.x; st < G; st += kThreads)
+    if (J[st] < lim) atomicAdd(&cnt[J[st]], 1);
   __syncthreads();
-  block_exclusive_scan(cnt, G, *s.f);
+  block_exclusive_scan(cnt, lim, *s.f);
   for (int st = 1 + threadIdx.x; st < G; st += kThreads) {
+    if (J[st] >= lim) continue;
     const int slot = atomicAdd(&cnt[J[st]], 1);
     list[slot] = static_cast<uint16_t>(st);
   }
@@ -307,12 +312,15 @@ __device__ int occupant_of(const Smem& s, int G, int p) {
 
 // Final position of group e: it lands on J[e] at step e (group 0 starts at
 // 0), then every later step targeting its position moves it to that step's
-// own position.
-__device__ int final_position_of(const Smem& s, int e) {
+// own position.  Positions only grow, so once the position reaches lim (the
+// buckets' limit) the walk stops and returns that position, which is enough
+// for a `< lim` test.
+__device__ int final_position_of(const Smem& s, int e, int lim) {
   const int* cnt = s.scratch32;
   int pos = e == 0 ? 0 : s.jarr[e];
   int time = e;
   for (;;) {
+    if (pos >= lim) return pos;
     const int b = pos > 0 ? cnt[pos - 1] : 0, en = cnt[pos];
     int next = 0x7fffffff;
     for (int k = b; k < en; ++k) {
@@ -1212,7 +1220,7 @@ __device__ void evolve_problem(const EvolveParams& P, const Smem& s, int prob) {
     const int ns = f.ns;
     if (threadIdx.x == 0) psize[cycle] = ns;
     if (ns > 0) {
-      bucket_steps_block(s, G);
+      bucket_steps_block(s, G, ns);
       if (P.singleton && P.pol_guidance && P.mlp != nullptr) {
         // learned proposal: as many relabellings as the plain draw would make,
         // given to the candidates the network scores highest
@@ -1221,7 +1229,7 @@ __device__ void evolve_problem(const EvolveParams& P, const Smem& s, int prob) {
           const int row = s.f->gmem[g];
           if (s.curpred[row] == s.cur[row]) continue;
           if (s.f->fxd != nullptr && s.f->fxd[row] == 1) continue;
-          take += final_position_of(s, g) < ns;
+          take += final_position_of(s, g, ns) < ns;
         }
         take = block_sum(take, f);
         learned_flip(P, s, prob, cycle, take, C0);
@@ -1233,7 +1241,7 @@ __device__ void evolve_problem(const EvolveParams& P, const Smem& s, int prob) {
           const int row = s.f->gmem[g];
           if (s.curpred[row] == s.cur[row]) continue;
           if (s.f->fxd != nullptr && s.f->fxd[row] == 1) continue;
-          if (final_position_of(s, g) < ns) s.cl[row] = s.curpred[row];
+          if (final_position_of(s, g, ns) < ns) s.cl[row] = s.curpred[row];
         }
       } else {
         for (int p = threadIdx.x; p < ns; p += kThreads) s.perm[p] = static_cast<uint16_t>(occupant_of(s, G, p));
@@ -1710,13 +1718,13 @@ __device__ void pls_propose(const EvolvePlsParams& Q, const Smem& s, int prob, i
   shuffle_targets_block(f, s.jarr, G, s.raw);
   const int ns = f.ns;
   if (ns > 0) {
-    bucket_steps_block(s, G);
+    bucket_steps_block(s, G, ns);
     if (P.singleton && P.pol_guidance) {
       for (int g = threadIdx.x; g < G; g += kThreads) {
         const int row = s.f->gmem[g];
         if (s.curpred[row] == s.cur[row]) continue;
         if (s.f->fxd != nullptr && s.f->fxd[row] == 1) continue;
-        if (final_position_of(s, g) < ns) s.cl[row] = s.curpred[row];
+        if (final_position_of(s, g, ns) < ns) s.cl[row] = s.curpred[row];
       }
     } else {
       for (int q = threadIdx.x; q < ns; q += kThreads) s.perm[q] = static_cast<uint16_t>(occupant_of(s, G, q));
