@@ -621,23 +621,30 @@ __device__ int dirty_rows_block(const EvolveParams& P, const Smem& s, int prob) 
 // increasing order and a first position only decreases, so a row at or past
 // the current first position of its code needs no atomicMin: the plain read
 // filters nearly all of them after the first rows of each code.
+// pred != nullptr: *ok also receives the count of rows with lab == pred
+// (both totals from one block reduction: ok + 2^16 nc, L and C0 < 2^15).
 __device__ int label_census(const EvolveParams& P, const Smem& s, const uint16_t* lab, int C0,
-                            bool have_cnt = false) {
+                            bool have_cnt = false, const uint16_t* pred = nullptr, int* ok = nullptr) {
   for (int c = threadIdx.x; c < C0; c += kThreads) {
     if (!have_cnt) s.cnt[c] = 0;
     s.firstpos[c] = 0x7fffffff;
   }
   __syncthreads();
   volatile int* fp = s.firstpos;
+  int hits = 0;
   for (int r = threadIdx.x; r < P.L; r += kThreads) {
     const int code = lab[r];
+    if (pred != nullptr) hits += code == pred[r];
     if (!have_cnt) atomicAdd(&s.cnt[code], 1);
     if (r < fp[code]) atomicMin(&s.firstpos[code], r);
   }
   __syncthreads();
   int local = 0;
   for (int c = threadIdx.x; c < C0; c += kThreads) local += s.cnt[c] > 0;
-  return block_sum(local, *s.f);
+  if (pred == nullptr) return block_sum(local, *s.f);
+  const int packed = block_sum(hits + (local << 16), *s.f);
+  *ok = packed & 0xffff;
+  return packed >> 16;
 }
 
 // s.order[0..nc) = the codes of the census in the iteration order of
@@ -645,13 +652,16 @@ __device__ int label_census(const EvolveParams& P, const Smem& s, const uint16_t
 __device__ __noinline__ void map_order(const EvolveParams& P, const Smem& s, int prob, int C0) {
   const bool nocollide = P.nocollide[prob] != 0;
   if (nocollide) {
-    // every key has its own bucket: each new key goes to the list front
-    for (int c = threadIdx.x; c < C0; c += kThreads) {
+    // every key has its own bucket: each new key goes to the list front, so
+    // a key's rank counts the keys first seen after it (one warp per key)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int c = warp; c < C0; c += kWarps) {
       if (s.cnt[c] == 0) continue;
       int rank = 0;
       const int fp = s.firstpos[c];
-      for (int c2 = 0; c2 < C0; ++c2) rank += (s.cnt[c2] > 0 && s.firstpos[c2] > fp);
-      s.order[rank] = c;
+      for (int c2 = lane; c2 < C0; c2 += 32) rank += (s.cnt[c2] > 0 && s.firstpos[c2] > fp);
+      rank = __reduce_add_sync(kFull, rank);
+      if (lane == 0) s.order[rank] = c;
     }
     __syncthreads();
   } else if (threadIdx.x == 0) {
@@ -699,13 +709,18 @@ __device__ double objective(const EvolveParams& P, const Smem& s, int prob, doub
   if (reject1 && nc == 1) return -INFINITY;
   if (!use_div) return acc;
   map_order(P, s, prob, C0);
-  if (threadIdx.x == 0) {
-    // psq[c] = (c/L)*(c/L) rounded as the reference rounds each step
-    double same = 0.0;
-    for (int q = 0; q < nc; ++q) same = __dadd_rn(same, P.psq[s.cnt[s.order[q]]]);
-    const double diff = __dsub_rn(1.0, same);
-    const double dlp = (0.0 < diff) ? diff : 0.0;
-    s.f->score = __dmul_rn(acc, __dsqrt_rn(dlp));
+  if (threadIdx.x < 32) {
+    // psq[c] = (c/L)*(c/L) rounded as the reference rounds each step; the
+    // warp loads the terms, lane 0 adds them in iteration order
+    for (int q = threadIdx.x; q < nc; q += 32) s.cp[q] = P.psq[s.cnt[s.order[q]]];
+    __syncwarp();
+    if (threadIdx.x == 0) {
+      double same = 0.0;
+      for (int q = 0; q < nc; ++q) same = __dadd_rn(same, s.cp[q]);
+      const double diff = __dsub_rn(1.0, same);
+      const double dlp = (0.0 < diff) ? diff : 0.0;
+      s.f->score = __dmul_rn(acc, __dsqrt_rn(dlp));
+    }
   }
   __syncthreads();
   const double out = s.f->score;
@@ -1192,11 +1207,10 @@ __device__ void evolve_problem(const EvolveParams& P, const Smem& s, int prob) {
 
   for (int cycle = 0; cycle < T; ++cycle) {
     if (P.snap_feat != nullptr && cycle == P.snap_cycle) snapshot_state(P, s, prob, cycle, C0);
-    // proposal = current (evolutionary) or best (greedy) state; s.cur holds it
-    for (int r = threadIdx.x; r < L; r += kThreads) s.cl[r] = s.cur[r];
-    __syncthreads();
-    if (warp == 0) {
-      if (lane == 0) {
+    // proposal = current (evolutionary) or best (greedy) state; s.cur holds
+    // it.  Thread 0 draws the proposal size before its share of the copy.
+    {
+      if (threadIdx.x == 0) {
         int ns;
         if (G <= 1) {
           ns = G > 0 ? G : 0;
@@ -1213,7 +1227,7 @@ __device__ void evolve_problem(const EvolveParams& P, const Smem& s, int prob) {
         }
         f.ns = ns;
       }
-      __syncwarp();
+      for (int r = threadIdx.x; r < L; r += kThreads) s.cl[r] = s.cur[r];
     }
     __syncthreads();
     shuffle_targets_block(f, s.jarr, G, s.raw);
@@ -1268,11 +1282,14 @@ __device__ void evolve_problem(const EvolveParams& P, const Smem& s, int prob) {
         vote_block(P, s, prob, s.cl, s.pred, C0, has_empty, s.jarr, nd);
       }
     }
-    ok = 0;
-    for (int r = threadIdx.x; r < L; r += kThreads) ok += s.cl[r] == s.pred[r];
-    ok = block_sum(ok, f);
+    const int nc = L < 32768 && C0 < 32768 ? label_census(P, s, s.cl, C0, cnt_of_cl, s.pred, &ok)
+                                           : label_census(P, s, s.cl, C0, cnt_of_cl);
+    if (L >= 32768 || C0 >= 32768) {
+      ok = 0;
+      for (int r = threadIdx.x; r < L; r += kThreads) ok += s.cl[r] == s.pred[r];
+      ok = block_sum(ok, f);
+    }
     const double acc = __ddiv_rn(static_cast<double>(ok), n);
-    const int nc = label_census(P, s, s.cl, C0, cnt_of_cl);
     const double score = objective(P, s, prob, acc, nc, C0);
     ++proposals;
 
