@@ -435,28 +435,45 @@ __device__ __forceinline__ void vote_rows_match(const uint16_t* lab, const uint1
 __device__ __noinline__ void vote_empty_rows(const EvolveParams& P, const Smem& s, int prob, const uint16_t* lab,
                                              uint16_t* out, int C0) {
   const int L = P.L, w = P.w;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint16_t* nbp = P.nb + static_cast<size_t>(prob) * L * w;
-  // per-fold training majority (codes in [0, C0))
-  int* fc = P.foldcnt + static_cast<size_t>(prob) * P.F * P.C0max;
-  for (int i = threadIdx.x; i < P.F * P.C0max; i += kThreads) fc[i] = 0;
+  // per-fold training majority (codes in [0, C0)).  The fold x code counts
+  // sit in s.scratch32 (L ints, free during the vote) when they fit, else in
+  // global memory.
+  const int F = P.F;
+  const bool in_smem = static_cast<long long>(F) * C0 <= L;
+  int* fc = in_smem ? s.scratch32 : P.foldcnt + static_cast<size_t>(prob) * F * P.C0max;
+  const int stride = in_smem ? C0 : P.C0max;
+  for (int i = threadIdx.x; i < F * stride; i += kThreads) fc[i] = 0;
   for (int c = threadIdx.x; c < C0; c += kThreads) s.aux[c] = 0;
   __syncthreads();
   const uint8_t* fo = P.folds + static_cast<size_t>(prob) * L;
   for (int r = threadIdx.x; r < L; r += kThreads) {
-    atomicAdd(&fc[fo[r] * P.C0max + lab[r]], 1);
+    atomicAdd(&fc[fo[r] * stride + lab[r]], 1);
     atomicAdd(&s.aux[lab[r]], 1);
   }
   __syncthreads();
-  for (int fo_i = threadIdx.x; fo_i < P.F; fo_i += kThreads) {
-    int bl = 0, bcount = -1;
-    for (int c = 0; c < C0; ++c) {
-      const int cnt = s.aux[c] - fc[fo_i * P.C0max + c];
-      if (cnt > bcount) {  // ascending codes: ties keep the smaller label
+  // one warp per fold, its lanes over the codes: the largest training count,
+  // ties to the smaller code (the reference scans the codes in ascending
+  // order keeping strict improvements)
+  for (int fo_i = warp; fo_i < F; fo_i += kWarps) {
+    int bl = 0x7fffffff, bcount = -1;
+    for (int c = lane; c < C0; c += 32) {
+      const int cnt = s.aux[c] - fc[fo_i * stride + c];
+      if (cnt > bcount) {
         bl = c;
         bcount = cnt;
       }
     }
-    s.order[fo_i] = bl;  // order[] is free here; F <= C0max guaranteed by host
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const int oc = __shfl_xor_sync(kFull, bcount, o), ol = __shfl_xor_sync(kFull, bl, o);
+      if (oc > bcount || (oc == bcount && ol < bl)) {
+        bcount = oc;
+        bl = ol;
+      }
+    }
+    if (lane == 0) s.order[fo_i] = bl;  // order[] is free here; F <= C0max guaranteed by host
   }
   __syncthreads();
   for (int r = threadIdx.x; r < L; r += kThreads) {
