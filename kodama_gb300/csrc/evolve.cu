@@ -758,26 +758,37 @@ __device__ int absorption_block(const EvolveParams& P, const Smem& s, int prob, 
     s.bt[c] = -1;
   }
   __syncthreads();
-  // one atomic per row: the class sizes are the rows of the class x
-  // prediction table, and without fixed rows every row is movable
+  // one atomic per row into the table: with the table in shared memory the
+  // class sizes are its row sums; with it in global memory a second,
+  // shared-memory atomic per row counts them.  Without fixed rows every row
+  // is movable.
   const bool any_fixed = s.f->fxd != nullptr;
+  const bool count_rows = !P.smem_trans;
   for (int r = threadIdx.x; r < P.L; r += kThreads) {
     const int a = s.cl[r];
     atomicAdd(&tr[a * C + pp[r]], 1);
+    if (count_rows) atomicAdd(&s.cnt[a], 1);
     if (any_fixed && s.f->fxd[r] != 1) atomicAdd(&s.movable[a], 1);
   }
   __syncthreads();
-  // class sizes: one warp per class, its lanes over the predictions
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int local = 0;
-  for (int c = warp; c < C0; c += kWarps) {
-    int sz = 0;
-    for (int q = lane; q < C0; q += 32) sz += tr[c * C + q];
-    sz = __reduce_add_sync(kFull, sz);
-    if (lane == 0) {
-      s.cnt[c] = sz;
-      if (!any_fixed) s.movable[c] = sz;
-      local += sz > 0;
+  if (count_rows) {
+    for (int c = threadIdx.x; c < C0; c += kThreads) {
+      if (!any_fixed) s.movable[c] = s.cnt[c];
+      local += s.cnt[c] > 0;
+    }
+  } else {
+    // class sizes: one warp per class, its lanes over the predictions
+    for (int c = warp; c < C0; c += kWarps) {
+      int sz = 0;
+      for (int q = lane; q < C0; q += 32) sz += tr[c * C + q];
+      sz = __reduce_add_sync(kFull, sz);
+      if (lane == 0) {
+        s.cnt[c] = sz;
+        if (!any_fixed) s.movable[c] = sz;
+        local += sz > 0;
+      }
     }
   }
   const int nc = block_sum(local, f);  // its barriers also publish the sizes
@@ -798,6 +809,7 @@ __device__ int absorption_block(const EvolveParams& P, const Smem& s, int prob, 
     // exact maximum can win the double comparison chain (double rounding is
     // far below the 1/n spacing of distinct exact surpluses)
     long long kmax = -0x7fffffffffffffffll;
+#pragma unroll 4
     for (int dst = lane; dst < C0; dst += 32) {
       const int cntd = row[dst];
       const int dsize = s.cnt[dst];
@@ -813,6 +825,7 @@ __device__ int absorption_block(const EvolveParams& P, const Smem& s, int prob, 
     int bt = src, bcount = 0, bsize = ssize;
     double bsur = 0.0;
     bool cand = false;
+#pragma unroll 4
     for (int dst = lane; dst < C0; dst += 32) {
       const int cntd = row[dst];
       const int dsize = s.cnt[dst];
