@@ -57,7 +57,7 @@ BATCH_METRIC = "256-problem uneven KODAMA.matrix batch wall-s (M=50, Tcycle=50 e
 BATCH_KW = dict(runs=50, cycles=50, knn_k=10, components=5, graph_neighbors=30, folds=10, seed=1234)
 # DRAM bytes (read + write) of one evolution-kernel launch, scaled from the
 # ncu capture summarised in profiles/evolve_kernel_cfg2.md (None until captured).
-EVOLVE_TRAFFIC_BYTES = 484564992
+EVOLVE_TRAFFIC_BYTES = 598524416
 
 
 CONFIG_DESC = ("KODAMA.matrix kNN N=20000 d=50 (12-cluster Gaussian mixture), M=100 runs, "
