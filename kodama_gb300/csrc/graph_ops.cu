@@ -112,19 +112,36 @@ __global__ void vote_table_kernel(VoteTableArgs a) {
   uint16_t* nb = a.nb + t * a.w;
   float* sc = a.sc + t * a.w;
   int col = 0;
-  for (int j = 0; j < a.K && col < a.w; ++j) {
-    const size_t src = static_cast<size_t>(grow) * a.K + j;
-    const int gnb = a.gidx[src];
-    if (gnb < 0 || gnb >= a.n) continue;
-    const int loc = g2l ? g2l[gnb] : gnb;
-    if (loc < 0 || loc == i) continue;
-    if (fo[loc] == myfold) continue;
-    const float dist = a.gdist[src];
-    if (!isfinite(dist)) continue;
-    const float dc = (0.0f < dist) ? dist : 0.0f;
-    nb[col] = static_cast<uint16_t>(loc);
-    sc[col] = a.score_one_minus ? __fsub_rn(1.0f, dc) : -__fmul_rn(dc, dc);
-    ++col;
+  // eight neighbours at a time: their ids and distances, then their local
+  // ids, then their folds are each loaded together, so a chunk waits on three
+  // rounds of loads instead of three per neighbour
+  constexpr int kChunk = 8;
+  for (int j0 = 0; j0 < a.K && col < a.w; j0 += kChunk) {
+    int gnb[kChunk], loc[kChunk], lf[kChunk];
+    float dist[kChunk];
+#pragma unroll
+    for (int u = 0; u < kChunk; ++u) {
+      const int j = j0 + u;
+      const size_t src = static_cast<size_t>(grow) * a.K + j;
+      gnb[u] = j < a.K ? a.gidx[src] : -1;
+      dist[u] = j < a.K ? a.gdist[src] : 0.0f;
+    }
+#pragma unroll
+    for (int u = 0; u < kChunk; ++u)
+      loc[u] = (gnb[u] >= 0 && gnb[u] < a.n) ? (g2l ? g2l[gnb[u]] : gnb[u]) : -1;
+#pragma unroll
+    for (int u = 0; u < kChunk; ++u) lf[u] = loc[u] >= 0 ? fo[loc[u]] : -1;
+#pragma unroll
+    for (int u = 0; u < kChunk; ++u) {
+      if (col >= a.w) break;
+      if (loc[u] < 0 || loc[u] == i) continue;
+      if (lf[u] == myfold) continue;
+      if (!isfinite(dist[u])) continue;
+      const float dc = (0.0f < dist[u]) ? dist[u] : 0.0f;
+      nb[col] = static_cast<uint16_t>(loc[u]);
+      sc[col] = a.score_one_minus ? __fsub_rn(1.0f, dc) : -__fmul_rn(dc, dc);
+      ++col;
+    }
   }
   for (; col < a.w; ++col) {
     nb[col] = 0xFFFFu;
