@@ -164,11 +164,19 @@ __global__ void project_kernel(ProjectArgs a) {
   } else {
     int votes[kMaxProjectK];
     int nv = 0;
-    for (int j = 0; j < a.K && nv < a.pk; ++j) {
-      const int gnb = a.gidx[static_cast<size_t>(r) * a.K + j];
-      if (gnb < 0 || gnb >= a.n) continue;
-      const int l = g2l[gnb];
-      if (l >= 0) votes[nv++] = best[l];
+    // eight neighbours at a time, each level of dependent loads issued together
+    constexpr int kChunk = 8;
+    for (int j0 = 0; j0 < a.K && nv < a.pk; j0 += kChunk) {
+      int g[kChunk], l[kChunk], b[kChunk];
+#pragma unroll
+      for (int u = 0; u < kChunk; ++u) g[u] = j0 + u < a.K ? a.gidx[static_cast<size_t>(r) * a.K + j0 + u] : -1;
+#pragma unroll
+      for (int u = 0; u < kChunk; ++u) l[u] = (g[u] >= 0 && g[u] < a.n) ? g2l[g[u]] : -1;
+#pragma unroll
+      for (int u = 0; u < kChunk; ++u) b[u] = l[u] >= 0 ? best[l[u]] : 0;
+#pragma unroll
+      for (int u = 0; u < kChunk; ++u)
+        if (nv < a.pk && l[u] >= 0) votes[nv++] = b[u];
     }
     if (nv == 0) {
       code = best[0];
@@ -193,34 +201,58 @@ __global__ void project_kernel(ProjectArgs a) {
 // rev_off[v+1]) lists the rows r whose table contains v.  One CTA per problem.
 __global__ void reverse_table_kernel(ReverseArgs a) {
   extern __shared__ int deg[];
-  const int p = blockIdx.x;
+  __shared__ int wsum[32];
+  const int p = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nwarps = (blockDim.x + 31) / 32;
   const uint16_t* nb = a.nb + static_cast<size_t>(p) * a.L * a.w;
   int* off = a.rev_off + static_cast<size_t>(p) * (a.L + 1);
   uint16_t* idx = a.rev_idx + static_cast<size_t>(p) * a.L * a.w;
-  for (int v = threadIdx.x; v <= a.L; v += blockDim.x) deg[v] = 0;
+  for (int v = tid; v <= a.L; v += blockDim.x) deg[v] = 0;
   __syncthreads();
-  const size_t total = static_cast<size_t>(a.L) * a.w;
-  for (size_t e = threadIdx.x; e < total; e += blockDim.x) {
+  const int total = a.L * a.w;  // < 2^22: L < 2^16, w <= 32
+  for (int e = tid; e < total; e += blockDim.x) {
     const uint16_t v = nb[e];
     if (v != 0xFFFFu) atomicAdd(&deg[v], 1);
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    int run = 0;
-    for (int v = 0; v < a.L; ++v) {
-      const int c = deg[v];
-      deg[v] = run;
-      off[v] = run;
-      run += c;
+  // exclusive scan of the in-degrees: each thread a contiguous chunk, then
+  // the warps' and the block's prefixes
+  const int chunk = (a.L + blockDim.x - 1) / blockDim.x;
+  const int b = min(a.L, tid * chunk), e = min(a.L, b + chunk);
+  int local = 0;
+  for (int v = b; v < e; ++v) local += deg[v];
+  int incl = local;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) wsum[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    int w = lane < nwarps ? wsum[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
     }
-    off[a.L] = run;
+    if (lane < nwarps) wsum[lane] = w;  // inclusive warp totals
   }
   __syncthreads();
-  for (size_t e = threadIdx.x; e < total; e += blockDim.x) {
-    const uint16_t v = nb[e];
+  int run = (warp > 0 ? wsum[warp - 1] : 0) + incl - local;
+  for (int v = b; v < e; ++v) {
+    const int c = deg[v];
+    deg[v] = run;
+    off[v] = run;
+    run += c;
+  }
+  if (tid == blockDim.x - 1) off[a.L] = wsum[nwarps - 1];
+  __syncthreads();
+  for (int e2 = tid; e2 < total; e2 += blockDim.x) {
+    const uint16_t v = nb[e2];
     if (v == 0xFFFFu) continue;
     const int slot = atomicAdd(&deg[v], 1);
-    idx[slot] = static_cast<uint16_t>(e / a.w);
+    idx[slot] = static_cast<uint16_t>(static_cast<unsigned>(e2) / static_cast<unsigned>(a.w));
   }
 }
 
