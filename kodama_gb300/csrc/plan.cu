@@ -117,26 +117,36 @@ __global__ void __launch_bounds__(1024) strata_kernel(PlanArgs a, PlanScratch s)
   __syncthreads();
   for (int t = tid; t < a.strata; t += blockDim.x) count[t] = s.offsets[t];  // count becomes the cursor
   __syncthreads();
-  // stable scatter: rows of one stratum keep ascending order
+  // stable scatter: rows of one stratum keep ascending order (one warp; the
+  // labels of eight 32-row steps are loaded ahead of their step)
   if (tid < 32) {
-    for (int b = 0; b < a.n; b += 32) {
-      const int r = b + tid;
-      const bool valid = r < a.n;
-      const unsigned act = __ballot_sync(0xffffffffu, valid);
-      if (valid) {
-        const int l = a.atlas[r] - 1;
-        const unsigned m = __match_any_sync(act, l);
-        const int leader = __ffs(m) - 1;
-        const int rank = __popc(m & ((1u << tid) - 1u));
-        int pos = 0;
-        if (tid == leader) {
-          pos = count[l];
-          count[l] = pos + __popc(m);
-        }
-        pos = __shfl_sync(act, pos, leader);
-        s.rows[pos + rank] = r;
+    for (int b0 = 0; b0 < a.n; b0 += 8 * 32) {
+      int lv[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int r = b0 + 32 * u + tid;
+        lv[u] = r < a.n ? a.atlas[r] - 1 : -1;
       }
-      __syncwarp();
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int r = b0 + 32 * u + tid;
+        const bool valid = r < a.n;
+        const unsigned act = __ballot_sync(0xffffffffu, valid);
+        if (valid) {
+          const int l = lv[u];
+          const unsigned m = __match_any_sync(act, l);
+          const int leader = __ffs(m) - 1;
+          const int rank = __popc(m & ((1u << tid) - 1u));
+          int pos = 0;
+          if (tid == leader) {
+            pos = count[l];
+            count[l] = pos + __popc(m);
+          }
+          pos = __shfl_sync(act, pos, leader);
+          s.rows[pos + rank] = r;
+        }
+        __syncwarp();
+      }
     }
   }
   // quota parts (run-independent)
