@@ -56,7 +56,8 @@ PLS_WORKLOAD = dict(n=10000, d=200, runs=50, cycles=50, graph_neighbors=30, knn_
 BATCH_METRIC = "256-problem uneven KODAMA.matrix batch wall-s (M=50, Tcycle=50 each, one captured CUDA graph)"
 BATCH_KW = dict(runs=50, cycles=50, knn_k=10, components=5, graph_neighbors=30, folds=10, seed=1234)
 # DRAM bytes (read + write) of one evolution-kernel launch, scaled from the
-# ncu capture summarised in profiles/evolve_kernel_cfg2.md (None until captured).
+# ncu capture of the full bench-size launch (dram__bytes_read.sum +
+# dram__bytes_write.sum; None until captured).
 EVOLVE_TRAFFIC_BYTES = 598524416
 
 
